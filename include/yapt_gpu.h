@@ -1,0 +1,249 @@
+/*
+ * yapt_gpu.h -- C ABI of the GB300 spectral path-tracing integrators.
+ *
+ * This is the drop-in boundary that replaces YAPT's integrator plug-in
+ * (PathIntegratorSubStage, Source/Renderer/inc/Renderer/Shared/RenderPipeline/
+ * PathTracer/PathIntegratorSubStage.h:20-72) and the scene ingest it is fed
+ * through (Renderer::createMesh/createMaterial/createRenderObject,
+ * Source/Renderer/inc/Renderer/Renderer.h:52-63). Everything is plain C: opaque
+ * handles, pointers and sizes; no C++ or framework types cross it.
+ *
+ * Conventions
+ *  - Every function returns YG_OK (0) or a negative YG_ERR_* code and never aborts
+ *    the process. yg_last_error() returns a message for the calling thread.
+ *  - Host pointers are read during the call only (the library copies them).
+ *  - Matrices are row-major float[12] (3x4: rotation/scale columns 0..2,
+ *    translation column 3) or float[16] (4x4).
+ *  - One context owns its device memory and one CUDA stream on one GPU.
+ */
+#ifndef YAPT_GPU_H
+#define YAPT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define YG_API __attribute__((visibility("default")))
+
+enum
+{
+    YG_OK = 0,
+    YG_ERR_INVALID_ARGUMENT = -1,
+    YG_ERR_CUDA = -2,
+    YG_ERR_OUT_OF_MEMORY = -3,
+    YG_ERR_NOT_READY = -4, /* e.g. render before yg_build_scene */
+    YG_ERR_IO = -5,
+    YG_ERR_DEVICE_TIMEOUT = -6, /* a bounded device-side wait ran out */
+    YG_ERR_ADMISSION = -7       /* serving: request does not fit the memory budget */
+};
+
+/* Integrators: YAPT's RenderPipeline options BPT / BPT_WITH_NEE / BDPT
+ * (Source/Renderer/inc/Renderer/Shared/RendererVarsList.h:24). */
+enum
+{
+    YG_INTEGRATOR_UNI = 0,
+    YG_INTEGRATOR_NEE = 1,
+    YG_INTEGRATOR_BDPT = 2
+};
+
+/* Material mask bits (materialsCommon.hlsl:7-9) */
+#define YG_MATERIAL_TWO_SIDED (1u << 0)
+#define YG_MATERIAL_DISPERSION (1u << 1)
+#define YG_MATERIAL_ALPHA_BLEND (1u << 2)
+
+/* Principled material: the field set of YAPT's MaterialParameters
+ * (Source/Renderer/inc/Renderer/Shared/MaterialInternal.h:39-115), plus the
+ * spectral extension: *_spectrum >= 0 selects a tabulated curve uploaded with
+ * yg_upload_spectra() instead of the RGB -> spectrum conversion. */
+typedef struct yg_material
+{
+    float albedo[3];
+    float transparency;
+    float specular[3];
+    float metalness;
+    float absorption[3];
+    float dielectric_ior;
+    float emissive[3];
+    float roughness;
+    float anisotropy;
+    float anisotropy_rotation;
+    uint32_t material_mask;
+    float thin_film_thickness_nm;
+    float cauchy[2]; /* A, B [um^2] */
+    float sheen_amount;
+    float emission_focus;
+    float sheen_tint[3];
+    float sheen_roughness;
+    float specular_amount;
+    float clear_coat_amount;
+    float clear_coat_ior;
+    float clear_coat_roughness;
+    float subsurface_radius[3];
+    float subsurface_amount;
+    float subsurface_radius_scale;
+    float alpha_cutoff;
+    int32_t albedo_spectrum;   /* -1: RGB albedo */
+    int32_t specular_spectrum; /* -1: RGB specular */
+    int32_t emission_spectrum; /* -1: RGB emission (times D65, as in the reference) */
+    int32_t reserved;
+} yg_material;
+
+/* Mesh upload (BindlessMeshManager + Mesh.setVertexBuffer/setIndexBuffer/setSubmesh). */
+typedef struct yg_mesh_desc
+{
+    const float* positions; /* vertex_count x 3 */
+    const float* normals;   /* vertex_count x 3, required */
+    const float* tangents;  /* vertex_count x 4 (xyz * w), or NULL */
+    const float* uvs;       /* vertex_count x 2, or NULL */
+    uint32_t vertex_count;
+    const void* indices;
+    uint32_t index_count;
+    uint32_t index_bits;            /* 16 or 32 */
+    const uint32_t* submesh_ranges; /* submesh_count x (first index, index count) */
+    uint32_t submesh_count;
+} yg_mesh_desc;
+
+/* One (render object, submesh) instance, as in YAPT's TLAS instance list
+ * (RaytraceCommonResources.cpp:216-279). world_to_obj must be the inverse of
+ * obj_to_world; both are given so that every consumer uses the same floats. */
+typedef struct yg_instance
+{
+    float obj_to_world[12];
+    float world_to_obj[12];
+    uint32_t mesh;
+    uint32_t submesh;
+    uint32_t material;
+    uint32_t reserved;
+} yg_instance;
+
+/* Camera constants (RaytraceConstantData, raytraceCommonResources.hlsl:8-31). */
+typedef struct yg_camera
+{
+    float uv_to_view[16];
+    float view_to_uv[16];
+    float world_to_view[16];
+    float view_to_world[16];
+    float aperture_radius;
+    float focus_distance;
+    float view_forward_z_sign;
+    float reserved;
+} yg_camera;
+
+#define YG_FLAG_DISABLE_TEXEL_JITTER (1u << 1)
+#define YG_FLAG_NO_FILM (1u << 8)      /* skip film accumulation (sample dump only) */
+#define YG_FLAG_FEATURES (1u << 9)     /* accumulate first-hit albedo/normal/depth */
+#define YG_FLAG_COUNT_TRAVERSAL (1u << 10) /* count BVH nodes visited / triangles tested (slower) */
+
+typedef struct yg_render_params
+{
+    uint32_t integrator; /* YG_INTEGRATOR_* */
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp_start; /* Sobol sample index of the first sample */
+    uint32_t spp_count;
+    uint32_t max_depth;                /* maxRayDepth (reference: 32) */
+    uint32_t regularize_after_vertices; /* Regularize.AfterVertices (reference default 8) */
+    uint32_t regularize_enable;         /* 1: reference behaviour; 0: no roughness widening */
+    float env_intensity_scale;          /* Env.IntensityScale (reference default 1) */
+    uint32_t seed;                      /* 0: reference scramble seeds */
+    uint32_t flags;
+    uint32_t crop_x, crop_y, crop_w, crop_h; /* render only this pixel rectangle (w=h=0: all) */
+    float lambda_min, lambda_max;            /* spectral range; reference: 380..700 nm */
+    uint32_t bdpt_light_paths;               /* BDPT: light subpaths per frame (0: ceil(W/8)*ceil(H/8)) */
+    uint32_t reserved[3];
+} yg_render_params;
+
+/* Per-sample record written by yg_render when sample_dump != NULL:
+ * hero wavelength, radiance at the 4 hero wavelengths, XYZ. */
+typedef struct yg_sample_record
+{
+    float lambda_hero;
+    float radiance[4];
+    float xyz[3];
+} yg_sample_record;
+
+typedef struct yg_context yg_context;
+
+/* Tables produced by the library that any reproducing host code must share. */
+enum
+{
+    YG_TABLE_SOBOL_MATRICES = 0,     /* uint32[256 x 32] */
+    YG_TABLE_LUT_SS_NOFRESNEL = 1,   /* 32 x 32          (MultipleScatterLUT.cpp:76-136) */
+    YG_TABLE_LUT_SS_AVG_NOFRESNEL = 2, /* 32 */
+    YG_TABLE_LUT_SSMS = 3,           /* 16 x 16 x 16 */
+    YG_TABLE_LUT_SSMS_AVG = 4,       /* 16 x 16 */
+    YG_TABLE_LUT_TRANSLUCENT_DENSER = 5,  /* 16^3 */
+    YG_TABLE_LUT_TRANSLUCENT_LIGHTER = 6, /* 16^3 */
+    YG_TABLE_LUT_TRANSLUCENT_AVG_DENSER = 7,  /* 16^2 */
+    YG_TABLE_LUT_TRANSLUCENT_AVG_LIGHTER = 8, /* 16^2 */
+    YG_TABLE_LUT_SHEEN = 9,          /* 16 x 16 */
+    YG_TABLE_CIE_1NM = 10,           /* 471 x 4: xbar ybar zbar d65, 360..830 nm */
+    YG_TABLE_RGB_TO_SPD = 11,        /* 64^3 x 3 sigmoid-polynomial coefficients (sRGB) */
+    YG_TABLE_COUNT = 12
+};
+
+/* -- lifetime -------------------------------------------------------------- */
+YG_API const char* yg_last_error(void);
+YG_API int yg_version(void);
+/* data_dir: folder holding the shipped data tables (CIE, Joe-Kuo). device: CUDA ordinal. */
+YG_API int yg_create(const char* data_dir, int device, yg_context** out);
+YG_API int yg_destroy(yg_context* ctx);
+YG_API int yg_synchronize(yg_context* ctx);
+
+/* -- tables ----------------------------------------------------------------- */
+/* Copies table `which` (YG_TABLE_*) into out (float or uint32 elements). *count
+ * receives the element count; call with out == NULL to query it. */
+YG_API int yg_get_table(yg_context* ctx, int which, void* out, size_t capacity, size_t* count);
+
+/* Same tables generated on the host alone (no CUDA device or context needed):
+ * YG_TABLE_SOBOL_MATRICES, YG_TABLE_LUT_*, YG_TABLE_CIE_1NM, and YG_TABLE_RGB_TO_SPD
+ * for the spectral range lambda_min..lambda_max (whole nm). */
+YG_API int yg_host_table(const char* data_dir, int which, int lambda_min, int lambda_max, void* out, size_t capacity,
+                         size_t* count);
+
+/* -- scene ingest ----------------------------------------------------------- */
+YG_API int yg_upload_mesh(yg_context* ctx, const yg_mesh_desc* desc, uint32_t* mesh_id);
+YG_API int yg_upload_materials(yg_context* ctx, const yg_material* materials, uint32_t count);
+/* n_curves curves of n_points values on a uniform grid lambda_min..lambda_max. */
+YG_API int yg_upload_spectra(yg_context* ctx, const float* values, uint32_t n_curves, uint32_t n_points,
+                             float lambda_min, float lambda_max);
+YG_API int yg_set_instances(yg_context* ctx, const yg_instance* instances, uint32_t count);
+YG_API int yg_set_camera(yg_context* ctx, const yg_camera* camera);
+/* Builds the acceleration structure and the light tables (alias tables over mesh
+ * lights, RaytraceCommonResources.cpp:325-547) for the current meshes/instances/materials. */
+YG_API int yg_build_scene(yg_context* ctx);
+/* Scene statistics: triangles, BVH nodes, lights, device bytes. */
+YG_API int yg_scene_info(yg_context* ctx, uint64_t* n_triangles, uint64_t* n_nodes, uint64_t* n_lights,
+                         uint64_t* device_bytes);
+
+/* -- rendering -------------------------------------------------------------- */
+/* Clears the film to width x height (Kahan FP32 XYZ sums + sample counts). */
+YG_API int yg_film_clear(yg_context* ctx, uint32_t width, uint32_t height);
+/* Renders params->spp_count samples per pixel starting at Sobol index spp_start and
+ * accumulates them into the film in sample order. If sample_dump is non-NULL it
+ * receives crop_w*crop_h*spp_count yg_sample_record (host memory), ordered
+ * [spp][row][column] of the crop. Asynchronous unless sample_dump is given. */
+YG_API int yg_render(yg_context* ctx, const yg_render_params* params, yg_sample_record* sample_dump);
+/* Film readback: mean XYZ per pixel (width*height*3) and per-pixel sample counts
+ * (width*height, may be NULL). Synchronises the context stream. */
+YG_API int yg_film_read(yg_context* ctx, float* xyz_mean, float* counts);
+/* First-hit feature means (YG_FLAG_FEATURES): albedo RGB, normal xyz, depth per pixel. */
+YG_API int yg_features_read(yg_context* ctx, float* albedo, float* normal, float* depth);
+/* relMSE of the film mean against a reference image (host, width*height*3 floats),
+ * reduced in FP64 on the device: mean over pixels and channels of
+ * (x - r)^2 / (r^2 + eps). */
+YG_API int yg_film_relmse(yg_context* ctx, const float* reference_xyz, double eps, double* relmse);
+
+/* Device timing of the most recent yg_render: kernel milliseconds, rays traced. */
+YG_API int yg_last_render_stats(yg_context* ctx, float* kernel_ms, uint64_t* rays, uint32_t* launches);
+/* Traversal work of the most recent render made with YG_FLAG_COUNT_TRAVERSAL. */
+YG_API int yg_last_traversal_counts(yg_context* ctx, uint64_t* nodes_visited, uint64_t* triangles_tested);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YAPT_GPU_H */

@@ -1,0 +1,80 @@
+/*
+ * oracle.h -- CPU oracle for the spectral path-tracing integrators.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is a plain scalar C++ restatement of YAPT's
+ * integrator shaders (uni / NEE), written from the HLSL sources and templated on
+ * the scalar type: float (per-sample parity with the GPU) and double (the
+ * reference images that relMSE is judged against). It is used by tests/, by
+ * smoke() and by bench.py's CPU baseline, never by the product path.
+ *
+ * Parity status: the reference's hot path is HLSL for DX12/Vulkan ray tracing
+ * and cannot be built or run here; its tests hold no golden vectors for this path
+ * (only the Sobol generator matrices of SobolMatrices.h, which pin the sampler).
+ * Integrator parity is therefore "unpinned" beyond the sampler table.
+ */
+#ifndef YAPT_ORACLE_H
+#define YAPT_ORACLE_H
+
+#include <stdint.h>
+#include "../include/yapt_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_instance
+{
+    float o2w[12];
+    float w2o[12];
+    uint32_t first_index; /* into indices */
+    uint32_t prim_count;
+    uint32_t vertex_base;
+    uint32_t material;
+    uint32_t has_tangents;
+    uint32_t reserved[3];
+} oracle_instance;
+
+typedef struct oracle_scene
+{
+    const float* positions; /* 3 per vertex, object space */
+    const float* normals;
+    const float* tangents; /* 4 per vertex (may be NULL when no instance uses tangents) */
+    const uint32_t* indices;
+    const oracle_instance* instances;
+    uint32_t n_instances;
+    const yg_material* materials;
+    uint32_t n_materials;
+    const float* spectra; /* n_curves x spec_points */
+    uint32_t spec_points;
+    float spec_lmin, spec_lmax;
+    const yg_camera* camera;
+    /* tables shared with the GPU path (yg_get_table) */
+    const float* luts[9];     /* YG_TABLE_LUT_* in order */
+    const float* rgb_to_spd;  /* 64^3 x 3 or NULL */
+    const char* data_dir;     /* CIE + Joe-Kuo data files */
+} oracle_scene;
+
+typedef struct oracle_stats
+{
+    uint64_t rays;
+    double seconds;
+} oracle_stats;
+
+/* Renders the crop/spp range of params with `threads` threads. precision: 32 or 64.
+ * records (optional): crop_w*crop_h*spp_count x 8 floats [spp][row][col]: hero lambda,
+ * L[4], XYZ. film_xyz (optional): crop_w*crop_h*3 doubles, mean XYZ over the samples. */
+int oracle_render(const oracle_scene* scene, const yg_render_params* params, int precision, int threads,
+                  float* records, double* film_xyz, oracle_stats* stats);
+
+/* Sobol generator matrices derived here from the Joe-Kuo file (256 x 32 uint32). */
+int oracle_sobol_matrices(const char* data_dir, uint32_t* out);
+
+/* Per-function checks (BSDF known-answer tests): evaluate a material at (wo, wi) for
+ * the given hero wavelength; returns weight[4] and pdf. Object space, normal (0,1,0). */
+int oracle_eval_bsdf(const oracle_scene* scene, uint32_t material, float hero, const float* wo, const float* wi,
+                     int precision, double* weight4, double* pdf);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

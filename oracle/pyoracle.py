@@ -1,0 +1,140 @@
+"""ctypes bridge to the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU baseline, never by the product path.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+import sys  # noqa: E402
+
+sys.path.insert(0, ROOT)
+from yapt_gb300 import _native as N  # noqa: E402  (struct layouts of include/yapt_gpu.h)
+
+
+class OracleInstance(C.Structure):
+    _fields_ = [("o2w", C.c_float * 12), ("w2o", C.c_float * 12), ("first_index", C.c_uint32),
+                ("prim_count", C.c_uint32), ("vertex_base", C.c_uint32), ("material", C.c_uint32),
+                ("has_tangents", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+class OracleScene(C.Structure):
+    _fields_ = [("positions", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+                ("tangents", C.POINTER(C.c_float)), ("indices", C.POINTER(C.c_uint32)),
+                ("instances", C.POINTER(OracleInstance)), ("n_instances", C.c_uint32),
+                ("materials", C.POINTER(N.Material)), ("n_materials", C.c_uint32),
+                ("spectra", C.POINTER(C.c_float)), ("spec_points", C.c_uint32), ("spec_lmin", C.c_float),
+                ("spec_lmax", C.c_float), ("camera", C.POINTER(N.Camera)), ("luts", C.POINTER(C.c_float) * 9),
+                ("rgb_to_spd", C.POINTER(C.c_float)), ("data_dir", C.c_char_p)]
+
+
+class OracleStats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("seconds", C.c_double)]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = C.CDLL(LIB)
+        lib.oracle_render.restype = C.c_int
+        lib.oracle_render.argtypes = [C.POINTER(OracleScene), C.POINTER(N.RenderParams), C.c_int, C.c_int, C.c_void_p,
+                                      C.c_void_p, C.POINTER(OracleStats)]
+        lib.oracle_sobol_matrices.restype = C.c_int
+        lib.oracle_sobol_matrices.argtypes = [C.c_char_p, C.c_void_p]
+        _lib = lib
+    return _lib
+
+
+def sobol_matrices():
+    out = np.zeros(256 * 32, np.uint32)
+    rc = load().oracle_sobol_matrices(N.DATA_DIR.encode(), out.ctypes.data_as(C.c_void_p))
+    assert rc == 0
+    return out
+
+
+class OracleSceneHandle:
+    """Keeps the numpy buffers alive while the oracle reads them."""
+
+    def __init__(self, scene, luts, rgb_to_spd=None):
+        pool = scene.pooled()
+        self.keep = []
+
+        def fp(a, dt=np.float32):
+            a = np.ascontiguousarray(np.asarray(a, dtype=dt))
+            self.keep.append(a)
+            return a
+
+        pos, nrm, tan = fp(pool["positions"]), fp(pool["normals"]), fp(pool["tangents"])
+        idx = fp(pool["indices"], np.uint32)
+        ninst = len(pool["instances"])
+        inst = (OracleInstance * max(1, ninst))()
+        for i, d in enumerate(pool["instances"]):
+            a = np.asarray(d["o2w"][:3, :], np.float32).reshape(-1)
+            b = np.asarray(np.linalg.inv(d["o2w"])[:3, :], np.float32).reshape(-1)
+            for k in range(12):
+                inst[i].o2w[k] = float(a[k])
+                inst[i].w2o[k] = float(b[k])
+            inst[i].first_index = d["first_index"]
+            inst[i].prim_count = d["prim_count"]
+            inst[i].vertex_base = d["vertex_base"]
+            inst[i].material = d["material"]
+            inst[i].has_tangents = 1 if d["has_tangents"] else 0
+        mats = scene.material_structs()
+        spec = fp(scene.spectra_array() if len(scene.spectra) else np.zeros((1, 81), np.float32))
+        cam = scene.camera.struct()
+        s = OracleScene()
+        s.positions = pos.ctypes.data_as(C.POINTER(C.c_float))
+        s.normals = nrm.ctypes.data_as(C.POINTER(C.c_float))
+        s.tangents = tan.ctypes.data_as(C.POINTER(C.c_float))
+        s.indices = idx.ctypes.data_as(C.POINTER(C.c_uint32))
+        s.instances = inst
+        s.n_instances = ninst
+        s.materials = mats
+        s.n_materials = len(scene.materials)
+        s.spectra = spec.ctypes.data_as(C.POINTER(C.c_float))
+        s.spec_points = 81
+        s.spec_lmin, s.spec_lmax = 380.0, 780.0
+        s.camera = C.pointer(cam)
+        for i, name in enumerate(["ss", "ss_avg", "ssms", "ssms_avg", "trans_denser", "trans_lighter",
+                                  "trans_avg_denser", "trans_avg_lighter", "sheen"]):
+            s.luts[i] = fp(luts[name]).ctypes.data_as(C.POINTER(C.c_float))
+        s.rgb_to_spd = fp(rgb_to_spd).ctypes.data_as(C.POINTER(C.c_float)) if rgb_to_spd is not None else None
+        s.data_dir = N.DATA_DIR.encode()
+        self.keep += [inst, mats, cam]
+        self.s = s
+
+    def render(self, params, precision=32, threads=None, records=True, film=False):
+        threads = threads or os.cpu_count() or 1
+        cw = params.crop_w or params.width
+        ch = params.crop_h or params.height
+        rec = np.zeros((params.spp_count, ch, cw, 8), np.float32) if records else None
+        fil = np.zeros((ch, cw, 3), np.float64) if film else None
+        st = OracleStats()
+        rc = load().oracle_render(C.byref(self.s), C.byref(params), precision, threads,
+                                  rec.ctypes.data_as(C.c_void_p) if rec is not None else None,
+                                  fil.ctypes.data_as(C.c_void_p) if fil is not None else None, C.byref(st))
+        if rc != 0:
+            raise RuntimeError("oracle_render failed: %d" % rc)
+        return dict(records=rec, film=fil, rays=st.rays, seconds=st.seconds)
+
+
+def luts_from_context(ctx):
+    names = ["ss", "ss_avg", "ssms", "ssms_avg", "trans_denser", "trans_lighter", "trans_avg_denser",
+             "trans_avg_lighter", "sheen"]
+    return {n: ctx.table(n) for n in names}

@@ -1,0 +1,157 @@
+"""ctypes view of the C ABI in include/yapt_gpu.h (libyaptgpu.so).
+
+This is the thin binding the Python API and the tests use to call the library;
+struct layouts mirror the header field by field.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DATA_DIR = os.path.join(HERE, "data")
+LIB_PATH = os.path.join(HERE, "libyaptgpu.so")
+
+YG_OK = 0
+INTEGRATORS = {"uni": 0, "BPT": 0, "nee": 1, "BPT_WITH_NEE": 1, "bdpt": 2, "BDPT": 2}
+
+YG_MATERIAL_TWO_SIDED = 1
+YG_MATERIAL_DISPERSION = 2
+YG_MATERIAL_ALPHA_BLEND = 4
+YG_FLAG_DISABLE_TEXEL_JITTER = 1 << 1
+YG_FLAG_NO_FILM = 1 << 8
+YG_FLAG_FEATURES = 1 << 9
+YG_FLAG_COUNT_TRAVERSAL = 1 << 10
+
+TABLES = {
+    "sobol": 0, "ss": 1, "ss_avg": 2, "ssms": 3, "ssms_avg": 4, "trans_denser": 5, "trans_lighter": 6,
+    "trans_avg_denser": 7, "trans_avg_lighter": 8, "sheen": 9, "cie": 10, "rgb_to_spd": 11,
+}
+
+
+class Material(C.Structure):
+    _fields_ = [
+        ("albedo", C.c_float * 3), ("transparency", C.c_float),
+        ("specular", C.c_float * 3), ("metalness", C.c_float),
+        ("absorption", C.c_float * 3), ("dielectric_ior", C.c_float),
+        ("emissive", C.c_float * 3), ("roughness", C.c_float),
+        ("anisotropy", C.c_float), ("anisotropy_rotation", C.c_float),
+        ("material_mask", C.c_uint32), ("thin_film_thickness_nm", C.c_float),
+        ("cauchy", C.c_float * 2), ("sheen_amount", C.c_float), ("emission_focus", C.c_float),
+        ("sheen_tint", C.c_float * 3), ("sheen_roughness", C.c_float),
+        ("specular_amount", C.c_float), ("clear_coat_amount", C.c_float),
+        ("clear_coat_ior", C.c_float), ("clear_coat_roughness", C.c_float),
+        ("subsurface_radius", C.c_float * 3), ("subsurface_amount", C.c_float),
+        ("subsurface_radius_scale", C.c_float), ("alpha_cutoff", C.c_float),
+        ("albedo_spectrum", C.c_int32), ("specular_spectrum", C.c_int32),
+        ("emission_spectrum", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("positions", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+        ("tangents", C.POINTER(C.c_float)), ("uvs", C.POINTER(C.c_float)),
+        ("vertex_count", C.c_uint32), ("indices", C.c_void_p), ("index_count", C.c_uint32),
+        ("index_bits", C.c_uint32), ("submesh_ranges", C.POINTER(C.c_uint32)), ("submesh_count", C.c_uint32),
+    ]
+
+
+class Instance(C.Structure):
+    _fields_ = [
+        ("obj_to_world", C.c_float * 12), ("world_to_obj", C.c_float * 12),
+        ("mesh", C.c_uint32), ("submesh", C.c_uint32), ("material", C.c_uint32), ("reserved", C.c_uint32),
+    ]
+
+
+class Camera(C.Structure):
+    _fields_ = [
+        ("uv_to_view", C.c_float * 16), ("view_to_uv", C.c_float * 16),
+        ("world_to_view", C.c_float * 16), ("view_to_world", C.c_float * 16),
+        ("aperture_radius", C.c_float), ("focus_distance", C.c_float),
+        ("view_forward_z_sign", C.c_float), ("reserved", C.c_float),
+    ]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [
+        ("integrator", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+        ("spp_start", C.c_uint32), ("spp_count", C.c_uint32), ("max_depth", C.c_uint32),
+        ("regularize_after_vertices", C.c_uint32), ("regularize_enable", C.c_uint32),
+        ("env_intensity_scale", C.c_float), ("seed", C.c_uint32), ("flags", C.c_uint32),
+        ("crop_x", C.c_uint32), ("crop_y", C.c_uint32), ("crop_w", C.c_uint32), ("crop_h", C.c_uint32),
+        ("lambda_min", C.c_float), ("lambda_max", C.c_float), ("bdpt_light_paths", C.c_uint32),
+        ("reserved", C.c_uint32 * 3),
+    ]
+
+
+class SampleRecord(C.Structure):
+    _fields_ = [("lambda_hero", C.c_float), ("radiance", C.c_float * 4), ("xyz", C.c_float * 3)]
+
+
+_lib = None
+
+# (name, restype, argtypes) for every function include/yapt_gpu.h declares
+SIGNATURES = [
+    ("yg_last_error", C.c_char_p, []),
+    ("yg_version", C.c_int, []),
+    ("yg_create", C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
+    ("yg_destroy", C.c_int, [C.c_void_p]),
+    ("yg_synchronize", C.c_int, [C.c_void_p]),
+    ("yg_get_table", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    ("yg_host_table", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    ("yg_upload_mesh", C.c_int, [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(C.c_uint32)]),
+    ("yg_upload_materials", C.c_int, [C.c_void_p, C.POINTER(Material), C.c_uint32]),
+    ("yg_upload_spectra", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_float, C.c_float]),
+    ("yg_set_instances", C.c_int, [C.c_void_p, C.POINTER(Instance), C.c_uint32]),
+    ("yg_set_camera", C.c_int, [C.c_void_p, C.POINTER(Camera)]),
+    ("yg_build_scene", C.c_int, [C.c_void_p]),
+    ("yg_scene_info", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                C.POINTER(C.c_uint64)]),
+    ("yg_film_clear", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
+    ("yg_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p]),
+    ("yg_film_read", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    ("yg_features_read", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    ("yg_film_relmse", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_double, C.POINTER(C.c_double)]),
+    ("yg_last_render_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint64),
+                                       C.POINTER(C.c_uint32)]),
+    ("yg_last_traversal_counts", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+]
+
+
+class YaptError(RuntimeError):
+    pass
+
+
+def load():
+    """Loads libyaptgpu.so; fails loudly when the native library is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise YaptError("libyaptgpu.so is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(LIB_PATH)
+    for name, res, args in SIGNATURES:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != YG_OK:
+        msg = load().yg_last_error().decode(errors="replace")
+        raise YaptError("yapt_gpu error %d: %s" % (rc, msg))
+    return rc
+
+
+def host_table(name, lambda_range=(380, 700)):
+    """Host-generated table (no GPU needed): same values a context uploads."""
+    import numpy as np
+    lib = load()
+    which = TABLES[name]
+    n = C.c_size_t()
+    check(lib.yg_host_table(DATA_DIR.encode(), which, int(lambda_range[0]), int(lambda_range[1]), None, 0, C.byref(n)))
+    out = np.zeros(n.value, dtype=np.uint32 if name == "sobol" else np.float32)
+    check(lib.yg_host_table(DATA_DIR.encode(), which, int(lambda_range[0]), int(lambda_range[1]),
+                            out.ctypes.data_as(C.c_void_p), out.size, C.byref(n)))
+    return out

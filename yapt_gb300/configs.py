@@ -1,0 +1,201 @@
+"""Seeded synthetic scenes for the benchmark configurations.
+
+There is no public dataset for this path; the scenes are generated from one
+numpy PCG64 generator per configuration, with the shapes, sizes and value
+distributions of the benchmark definitions:
+
+* ``box_scene``      closed-on-5-sides unit box (10 triangles), two rotated inner boxes
+                     (12 triangles each), a 0.25 x 0.25 ceiling quad light with a
+                     D65-shaped spectrum, diffuse principled materials with 8-point
+                     reflectance spectra U(0.05, 0.85) over 380..780 nm. The front (z = 1)
+                     is open; the camera looks in from outside. Env.IntensityScale = 0.
+* ``random_shapes_scene``  N icospheres (subdivision 2, 320 triangles) with centres
+                     U([-10,10] x [0,4] x [-10,10]) (y up), radii U(0.2, 1.0), on a
+                     40 x 40 ground quad, lit by 3 quad lights with blackbody spectra,
+                     T ~ U(2700 K, 6500 K); roughness U(0.05, 1), metallic ~ Bernoulli(0.3),
+                     20% dispersive dielectrics (Cauchy A = 1.5, B = 0.0042 um^2).
+"""
+import numpy as np
+
+from .scene import (SPECTRUM_LMAX, SPECTRUM_LMIN, SPECTRUM_POINTS, CameraDesc, Scene, affine, rotation_y)
+
+GRID = np.linspace(SPECTRUM_LMIN, SPECTRUM_LMAX, SPECTRUM_POINTS)
+
+
+def control_point_spectrum(rng, n=8, lo=0.05, hi=0.85):
+    """Piecewise-linear reflectance through n seeded control points over 380..780 nm."""
+    lam = np.linspace(SPECTRUM_LMIN, SPECTRUM_LMAX, n)
+    vals = rng.uniform(lo, hi, size=n)
+    return np.interp(GRID, lam, vals).astype(np.float32)
+
+
+def blackbody_spectrum(T):
+    """Planck's law sampled on the spectral grid, normalised to a peak of 1 in 380..780 nm."""
+    h, c, k = 6.62607015e-34, 2.99792458e8, 1.380649e-23
+    lam = GRID * 1e-9
+    b = (2 * h * c * c) / (lam ** 5) / np.expm1(h * c / (lam * k * T))
+    return (b / b.max()).astype(np.float32)
+
+
+def quad(w, h):
+    """Unit quad in the xz plane facing -y (a ceiling light), centred at the origin."""
+    p = np.array([[-w / 2, 0, -h / 2], [w / 2, 0, -h / 2], [w / 2, 0, h / 2], [-w / 2, 0, h / 2]], np.float32)
+    n = np.tile(np.float32([0, -1, 0]), (4, 1))
+    # winding so that cross(p1 - p0, p2 - p0) points along -y
+    idx = np.array([0, 1, 2, 0, 2, 3], np.uint32)
+    e = np.cross(p[1] - p[0], p[2] - p[0])
+    if e[1] > 0:
+        idx = np.array([0, 2, 1, 0, 3, 2], np.uint32)
+    return p, n, idx
+
+
+def cuboid():
+    """Axis-aligned unit cube centred at the origin, 12 triangles, outward flat normals."""
+    faces = []
+    for axis in range(3):
+        for sgn in (-1.0, 1.0):
+            n = np.zeros(3)
+            n[axis] = sgn
+            u = np.zeros(3)
+            u[(axis + 1) % 3] = 1.0
+            v = np.cross(n, u)
+            c = n * 0.5
+            corners = [c - u * 0.5 - v * 0.5, c + u * 0.5 - v * 0.5, c + u * 0.5 + v * 0.5, c - u * 0.5 + v * 0.5]
+            faces.append((np.array(corners), n))
+    pos, nrm, idx = [], [], []
+    for (cs, n) in faces:
+        b = len(pos)
+        pos.extend(cs)
+        nrm.extend([n] * 4)
+        tri = [b, b + 1, b + 2, b, b + 2, b + 3]
+        if np.dot(np.cross(cs[1] - cs[0], cs[2] - cs[0]), n) < 0:
+            tri = [b, b + 2, b + 1, b, b + 3, b + 2]
+        idx.extend(tri)
+    return np.array(pos, np.float32), np.array(nrm, np.float32), np.array(idx, np.uint32)
+
+
+def icosphere(subdiv=2):
+    """Unit icosphere: 20 * 4^subdiv triangles, outward winding, smooth normals."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(v, float) / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+             (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+             (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for (a, b, c) in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    pos = np.array(verts, np.float32)
+    idx = []
+    for (a, b, c) in faces:
+        n = np.cross(pos[b] - pos[a], pos[c] - pos[a])
+        if np.dot(n, pos[a] + pos[b] + pos[c]) < 0:
+            b, c = c, b
+        idx += [a, b, c]
+    return pos, pos.copy(), np.array(idx, np.uint32)
+
+
+def diffuse(spectrum_id):
+    # diffuse principled layer set as in the reference's test scenes
+    # (Tests/IntegratorCompare/focused_emission_scene.py:52-56): no metal, no specular, rough
+    return dict(albedo=(0.5, 0.5, 0.5), albedo_spectrum=spectrum_id, metalness=0.0, transparency=0.0,
+                specular_amount=0.0, roughness=1.0)
+
+
+def box_scene(seed=0, light_intensity=12.0, aspect=1.0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene()
+    sc.name = "box(seed=%d)" % seed
+    # the five walls: floor, ceiling, back, left, right; normals point into the box
+    wall_defs = [((0.5, 0.0, 0.5), (0, 1, 0)), ((0.5, 1.0, 0.5), (0, -1, 0)), ((0.5, 0.5, 0.0), (0, 0, 1)),
+                 ((0.0, 0.5, 0.5), (1, 0, 0)), ((1.0, 0.5, 0.5), (-1, 0, 0))]
+    pos, nrm, idx = [], [], []
+    for (c, n) in wall_defs:
+        c, n = np.array(c, float), np.array(n, float)
+        u = np.array([1.0, 0, 0]) if abs(n[0]) < 0.5 else np.array([0, 0, 1.0])
+        v = np.cross(n, u)
+        cs = [c - 0.5 * u - 0.5 * v, c + 0.5 * u - 0.5 * v, c + 0.5 * u + 0.5 * v, c - 0.5 * u + 0.5 * v]
+        b = len(pos)
+        pos.extend(cs)
+        nrm.extend([n] * 4)
+        tri = [b, b + 1, b + 2, b, b + 2, b + 3]
+        if np.dot(np.cross(cs[1] - cs[0], cs[2] - cs[0]), n) < 0:
+            tri = [b, b + 2, b + 1, b, b + 3, b + 2]
+        idx.extend(tri)
+    walls = sc.add_mesh(np.array(pos), np.array(nrm), np.array(idx), submeshes=[(6 * i, 6) for i in range(5)])
+    for i in range(5):
+        sid = sc.add_spectrum(control_point_spectrum(rng))
+        mat = sc.add_material(**diffuse(sid))
+        sc.add_instance(walls, mat, submesh=i)
+    cube = sc.add_mesh(*cuboid())
+    for k in range(2):
+        sid = sc.add_spectrum(control_point_spectrum(rng))
+        mat = sc.add_material(**diffuse(sid))
+        h = rng.uniform(0.25, 0.6)
+        w = rng.uniform(0.18, 0.3)
+        x = 0.3 if k == 0 else 0.7
+        z = rng.uniform(0.3, 0.6)
+        o2w = affine(translation=(x, h / 2, z), rotation=rotation_y(rng.uniform(0, np.pi)), scale=(w, h, w))
+        sc.add_instance(cube, mat, o2w)
+    qp, qn, qi = quad(0.25, 0.25)
+    light = sc.add_mesh(qp, qn, qi)
+    lmat = sc.add_material(albedo=(0.0, 0.0, 0.0), emissive=(light_intensity,) * 3, metalness=0.0, specular_amount=0.0,
+                           roughness=1.0)
+    sc.add_instance(light, lmat, affine(translation=(0.5, 0.999, 0.5)))
+    sc.camera = CameraDesc(eye=(0.5, 0.5, 2.1), target=(0.5, 0.5, 0.0), fovy=np.pi * 0.22, aspect=aspect)
+    return sc
+
+
+def random_shapes_scene(seed=0, n_spheres=500, light_intensity=25.0, aspect=1.0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene()
+    sc.name = "random_shapes(seed=%d, n=%d)" % (seed, n_spheres)
+    ico = sc.add_mesh(*icosphere(2))
+    for _ in range(n_spheres):
+        c = (rng.uniform(-10, 10), rng.uniform(0, 4), rng.uniform(-10, 10))
+        r = rng.uniform(0.2, 1.0)
+        rough = rng.uniform(0.05, 1.0)
+        metallic = rng.uniform() < 0.3
+        dielectric = (not metallic) and rng.uniform() < (0.2 / 0.7)
+        sid = sc.add_spectrum(control_point_spectrum(rng))
+        if metallic:
+            mat = sc.add_material(albedo=(0.8, 0.8, 0.8), albedo_spectrum=sid, specular=(1.0, 1.0, 1.0), metalness=1.0,
+                                  roughness=rough)
+        elif dielectric:
+            mat = sc.add_material(albedo=(1.0, 1.0, 1.0), transparency=1.0, metalness=0.0, specular_amount=1.0,
+                                  roughness=rough, material_mask=2, cauchy=(1.5, 0.0042), dielectric_ior=1.5)
+        else:
+            mat = sc.add_material(albedo=(0.5, 0.5, 0.5), albedo_spectrum=sid, metalness=0.0, specular_amount=1.0,
+                                  roughness=rough)
+        sc.add_instance(ico, mat, affine(translation=c, scale=(r, r, r)))
+    gp, gn, gi = quad(40.0, 40.0)
+    gn = -gn
+    gi = gi[[0, 2, 1, 3, 5, 4]]
+    ground = sc.add_mesh(gp, gn, gi)
+    gsid = sc.add_spectrum(control_point_spectrum(rng))
+    sc.add_instance(ground, sc.add_material(**diffuse(gsid)))
+    lp, ln, li = quad(3.0, 3.0)
+    light = sc.add_mesh(lp, ln, li)
+    for k in range(3):
+        T = rng.uniform(2700.0, 6500.0)
+        sid = sc.add_spectrum(blackbody_spectrum(T))
+        lmat = sc.add_material(albedo=(0.0, 0.0, 0.0), emissive=(light_intensity,) * 3, emission_spectrum=sid,
+                               metalness=0.0, specular_amount=0.0, roughness=1.0)
+        pos = (rng.uniform(-8, 8), rng.uniform(7, 9), rng.uniform(-8, 8))
+        sc.add_instance(light, lmat, affine(translation=pos))
+    sc.camera = CameraDesc(eye=(0.0, 7.0, 19.0), target=(0.0, 1.0, 0.0), fovy=np.pi * 0.3, aspect=aspect)
+    return sc

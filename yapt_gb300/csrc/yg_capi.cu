@@ -1,0 +1,926 @@
+// C-ABI runtime: context, scene ingest, acceleration structure, light tables, render
+// submission and film readback. Mirrors the host side of YAPT's path tracer
+// (RaytraceCommonResources.cpp, BindlessMaterialManager.cpp, LightManager.cpp,
+// PathTraceStage.cpp) on one CUDA stream.
+#include "../../include/yapt_gpu.h"
+#include "yg_bvh.h"
+#include "yg_kernels.h"
+#include "yg_tables.h"
+#include "yg_vec.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace
+{
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string& msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+#define YG_CUDA(call)                                                                                              \
+    do                                                                                                             \
+    {                                                                                                              \
+        cudaError_t e_ = (call);                                                                                   \
+        if (e_ != cudaSuccess)                                                                                     \
+            return fail(e_ == cudaErrorMemoryAllocation ? YG_ERR_OUT_OF_MEMORY : YG_ERR_CUDA,                      \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                                       \
+    } while (0)
+
+struct DevBuf
+{
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n)
+    {
+        if (n <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+struct Mesh
+{
+    uint32_t vertexBase, vertexCount, indexBase, indexCount;
+    bool tangents, uvs;
+    std::vector<std::pair<uint32_t, uint32_t>> submeshes;
+};
+} // namespace
+
+struct yg_context
+{
+    std::mutex lock;
+    int device = 0;
+    int smCount = 152;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t evStart = nullptr, evStop = nullptr;
+    std::string dataDir;
+    // tables
+    std::vector<uint32_t> sobolMatrices;
+    std::vector<double> cie471;
+    yg::MsLuts luts;
+    std::vector<float> rgbToSpd;
+    int rgbLmin = 0, rgbLmax = 0;
+    // scene (host)
+    std::vector<float> positions, normals, uvs;
+    std::vector<float4> tangents;
+    std::vector<uint32_t> indices;
+    std::vector<Mesh> meshes;
+    std::vector<yg_material> materials;
+    std::vector<yg::GpuMaterial> gpuMaterials;
+    std::vector<float> spectra;
+    uint32_t specPoints = 0;
+    float specLmin = 380.f, specLmax = 780.f;
+    std::vector<yg_instance> instances;
+    yg::GpuCamera camera{};
+    bool cameraSet = false;
+    bool sceneBuilt = false;
+    uint64_t nTris = 0, nNodes = 0;
+    // device
+    DevBuf dTris, dNodes, dInst, dMat, dLights, dPos, dNrm, dTan, dUV, dIdx, dSpec;
+    DevBuf dLut[9];
+    DevBuf dCie, dRgb, dSobol, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
+    DevBuf dFilmSum, dFilmComp, dAccA, dAccN;
+    uint32_t nLights = 0;
+    int cieLmin = -1, cieLmax = -1;
+    uint32_t cieN = 0;
+    float cieYSumInv = 0, d65SumInv = 0;
+    uint32_t filmW = 0, filmH = 0;
+    bool featuresOn = false;
+    // stats
+    float lastMs = 0;
+    uint64_t lastRays = 0;
+    uint32_t lastLaunches = 0;
+
+    ~yg_context()
+    {
+        DevBuf* all[] = {&dTris, &dNodes, &dInst, &dMat, &dLights, &dPos, &dNrm, &dTan, &dUV, &dIdx, &dSpec, &dCie, &dRgb,
+                         &dSobol, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
+                         &dFilmComp, &dAccA, &dAccN};
+        for (DevBuf* b : all) b->release();
+        for (auto& b : dLut) b.release();
+        if (evStart) cudaEventDestroy(evStart);
+        if (evStop) cudaEventDestroy(evStop);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace
+{
+template <typename T>
+int upload(yg_context* c, DevBuf& b, const T* src, size_t count)
+{
+    size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
+    YG_CUDA(b.ensure(bytes));
+    if (count) YG_CUDA(cudaMemcpyAsync(b.p, src, sizeof(T) * count, cudaMemcpyHostToDevice, c->stream));
+    return YG_OK;
+}
+
+float saturatef(float x) { return std::min(std::max(x, 0.0f), 1.0f); }
+
+// BindlessMaterialManager.cpp:73-98
+yg::GpuMaterial packMaterial(const yg_material& m)
+{
+    yg::GpuMaterial g{};
+    g.specAmount_ccAmount_ccIOR_ccRough = make_float4(saturatef(m.specular_amount), saturatef(m.clear_coat_amount),
+                                                      m.clear_coat_ior, saturatef(m.clear_coat_roughness));
+    g.albedo_transparency = make_float4(m.albedo[0], m.albedo[1], m.albedo[2], m.transparency);
+    g.specular_metalness = make_float4(m.specular[0], m.specular[1], m.specular[2], m.metalness);
+    g.absorption_ior = make_float4(m.absorption[0], m.absorption[1], m.absorption[2],
+                                   std::min(std::max(m.dielectric_ior, 0.3f), 3.0f));
+    g.emissive_roughness = make_float4(m.emissive[0], m.emissive[1], m.emissive[2], saturatef(m.roughness));
+    g.anisotropy = saturatef(m.anisotropy);
+    g.anisotropyRotation = m.anisotropy_rotation;
+    g.mask = m.material_mask;
+    g.thinFilmNM = m.thin_film_thickness_nm;
+    g.cauchyA = m.cauchy[0];
+    g.cauchyB = m.cauchy[1];
+    g.sheenAmount = m.sheen_amount;
+    g.emissionFocus = m.emission_focus;
+    g.sheenColor_roughness = make_float4(m.sheen_tint[0], m.sheen_tint[1], m.sheen_tint[2], m.sheen_roughness);
+    g.subsurfaceRadius_amount =
+        make_float4(m.subsurface_radius[0] * m.subsurface_radius_scale, m.subsurface_radius[1] * m.subsurface_radius_scale,
+                    m.subsurface_radius[2] * m.subsurface_radius_scale, saturatef(m.subsurface_amount));
+    g.albedoSpectrum = m.albedo_spectrum;
+    g.specularSpectrum = m.specular_spectrum;
+    g.emissionSpectrum = m.emission_spectrum;
+    return g;
+}
+
+bool isGreyOrZero(const float* c) { return c[0] == c[1] && c[0] == c[2]; }
+
+// Vose alias table (RaytraceCommonResources.cpp:325-383)
+void selectionPdfs(std::vector<float>& w)
+{
+    const float kUniform = 0.1f;
+    size_t count = w.size();
+    double total = 0;
+    for (float x : w) total += x;
+    float share = total > 0 ? kUniform : 1.f;
+    for (float& x : w)
+    {
+        float ps = total > 0 ? float(x / total) : 0.f;
+        x = (1.f - share) * ps + share / count;
+    }
+}
+void aliasTable(const std::vector<float>& pdfs, std::vector<float>& thr, std::vector<uint32_t>& alias)
+{
+    size_t count = pdfs.size();
+    thr.assign(count, 0.f);
+    alias.assign(count, 0);
+    std::vector<float> scaled(count);
+    std::vector<uint32_t> small, large;
+    for (size_t i = 0; i < count; ++i)
+    {
+        scaled[i] = pdfs[i] * count;
+        (scaled[i] < 1.f ? small : large).push_back(uint32_t(i));
+    }
+    while (!small.empty() && !large.empty())
+    {
+        uint32_t s = small.back();
+        small.pop_back();
+        uint32_t l = large.back();
+        large.pop_back();
+        thr[s] = scaled[s];
+        alias[s] = l;
+        scaled[l] = (scaled[l] + scaled[s]) - 1.f;
+        (scaled[l] < 1.f ? small : large).push_back(l);
+    }
+    for (uint32_t i : large)
+    {
+        thr[i] = 1.f;
+        alias[i] = i;
+    }
+    for (uint32_t i : small)
+    {
+        thr[i] = 1.f;
+        alias[i] = i;
+    }
+}
+
+int ensureCie(yg_context* c, int lmin, int lmax)
+{
+    if (c->cieLmin == lmin && c->cieLmax == lmax) return YG_OK;
+    std::vector<float> t;
+    float yInv, dInv;
+    if (!yg::cieForRange(c->cie471, lmin, lmax, t, yInv, dInv))
+        return fail(YG_ERR_INVALID_ARGUMENT, "spectral range must be integer nm within [360, 830]");
+    int r = upload(c, c->dCie, t.data(), t.size());
+    if (r) return r;
+    c->cieLmin = lmin;
+    c->cieLmax = lmax;
+    c->cieN = (uint32_t)(lmax - lmin + 1);
+    c->cieYSumInv = yInv;
+    c->d65SumInv = dInv;
+    return YG_OK;
+}
+
+bool sceneNeedsRgbLut(const yg_context* c, float envScale)
+{
+    if (envScale > 0.0f) return true;
+    for (const yg_material& m : c->materials)
+    {
+        if (m.albedo_spectrum < 0 && !isGreyOrZero(m.albedo)) return true;
+        if (m.specular_spectrum < 0 && !isGreyOrZero(m.specular)) return true;
+        if (m.emission_spectrum < 0 && !isGreyOrZero(m.emissive)) return true;
+        if (!isGreyOrZero(m.absorption)) return true;
+        if (m.sheen_amount > 0.0f && !isGreyOrZero(m.sheen_tint)) return true;
+    }
+    return false;
+}
+
+int ensureRgbLut(yg_context* c, int lmin, int lmax)
+{
+    if (!c->rgbToSpd.empty() && c->rgbLmin == lmin && c->rgbLmax == lmax) return YG_OK;
+    yg::buildRgbToSpd(c->cie471, lmin, lmax, c->rgbToSpd);
+    c->rgbLmin = lmin;
+    c->rgbLmax = lmax;
+    return upload(c, c->dRgb, c->rgbToSpd.data(), c->rgbToSpd.size());
+}
+} // namespace
+
+extern "C" {
+
+YG_API const char* yg_last_error(void) { return g_lastError.c_str(); }
+YG_API int yg_version(void) { return 1; }
+
+YG_API int yg_create(const char* data_dir, int device, yg_context** out)
+{
+    if (!out || !data_dir) return fail(YG_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    int n = 0;
+    YG_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(YG_ERR_INVALID_ARGUMENT, "no such CUDA device");
+    YG_CUDA(cudaSetDevice(device));
+    yg_context* c = new yg_context();
+    c->device = device;
+    c->dataDir = data_dir;
+    cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device);
+    std::string err;
+    if (!yg::buildSobolMatrices(c->dataDir + "/joe_kuo_6_21201_first256.txt", c->sobolMatrices, err) ||
+        !yg::loadCie(c->dataDir + "/cie1931_2deg_d65_1nm.txt", c->cie471, err))
+    {
+        delete c;
+        return fail(YG_ERR_IO, err);
+    }
+    yg::buildMsLuts(c->luts);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->evStart);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->evStop);
+    if (e != cudaSuccess)
+    {
+        delete c;
+        return fail(YG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const std::vector<float>* L[9] = {&c->luts.ss, &c->luts.ssAvg, &c->luts.ssms, &c->luts.ssmsAvg, &c->luts.transDenser,
+                                      &c->luts.transLighter, &c->luts.transAvgDenser, &c->luts.transAvgLighter,
+                                      &c->luts.sheen};
+    for (int i = 0; i < 9; ++i)
+    {
+        int r = upload(c, c->dLut[i], L[i]->data(), L[i]->size());
+        if (r)
+        {
+            delete c;
+            return r;
+        }
+    }
+    int r = ensureCie(c, 380, 700);
+    if (r)
+    {
+        delete c;
+        return r;
+    }
+    YG_CUDA(cudaStreamSynchronize(c->stream));
+    *out = c;
+    return YG_OK;
+}
+
+YG_API int yg_destroy(yg_context* ctx)
+{
+    if (!ctx) return YG_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete ctx;
+    return YG_OK;
+}
+
+YG_API int yg_synchronize(yg_context* ctx)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return YG_OK;
+}
+
+YG_API int yg_get_table(yg_context* ctx, int which, void* out, size_t capacity, size_t* count)
+{
+    if (!ctx || !count) return fail(YG_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const void* src = nullptr;
+    size_t n = 0, elem = 4;
+    std::vector<float> tmp;
+    const std::vector<float>* L[9] = {&ctx->luts.ss, &ctx->luts.ssAvg, &ctx->luts.ssms, &ctx->luts.ssmsAvg,
+                                      &ctx->luts.transDenser, &ctx->luts.transLighter, &ctx->luts.transAvgDenser,
+                                      &ctx->luts.transAvgLighter, &ctx->luts.sheen};
+    if (which == YG_TABLE_SOBOL_MATRICES)
+    {
+        src = ctx->sobolMatrices.data();
+        n = ctx->sobolMatrices.size();
+    }
+    else if (which >= YG_TABLE_LUT_SS_NOFRESNEL && which <= YG_TABLE_LUT_SHEEN)
+    {
+        src = L[which - 1]->data();
+        n = L[which - 1]->size();
+    }
+    else if (which == YG_TABLE_CIE_1NM)
+    {
+        tmp.assign(ctx->cie471.begin(), ctx->cie471.end());
+        src = tmp.data();
+        n = tmp.size();
+    }
+    else if (which == YG_TABLE_RGB_TO_SPD)
+    {
+        int lmin = ctx->cieLmin, lmax = ctx->cieLmax;
+        if (ctx->rgbToSpd.empty() || ctx->rgbLmin != lmin || ctx->rgbLmax != lmax)
+        {
+            int r = ensureRgbLut(ctx, lmin, lmax);
+            if (r) return r;
+        }
+        src = ctx->rgbToSpd.data();
+        n = ctx->rgbToSpd.size();
+    }
+    else
+    {
+        return fail(YG_ERR_INVALID_ARGUMENT, "unknown table");
+    }
+    *count = n;
+    if (out)
+    {
+        if (capacity < n) return fail(YG_ERR_INVALID_ARGUMENT, "table buffer too small");
+        std::memcpy(out, src, n * elem);
+    }
+    return YG_OK;
+}
+
+YG_API int yg_host_table(const char* data_dir, int which, int lmin, int lmax, void* out, size_t capacity, size_t* count)
+{
+    if (!data_dir || !count) return fail(YG_ERR_INVALID_ARGUMENT, "null argument");
+    std::string dir(data_dir), err;
+    std::vector<uint32_t> u;
+    std::vector<float> f;
+    std::vector<double> cie;
+    if (which == YG_TABLE_SOBOL_MATRICES)
+    {
+        if (!yg::buildSobolMatrices(dir + "/joe_kuo_6_21201_first256.txt", u, err)) return fail(YG_ERR_IO, err);
+    }
+    else if (which >= YG_TABLE_LUT_SS_NOFRESNEL && which <= YG_TABLE_LUT_SHEEN)
+    {
+        static std::mutex m;
+        static yg::MsLuts cache;
+        static bool built = false;
+        std::lock_guard<std::mutex> g(m);
+        if (!built)
+        {
+            yg::buildMsLuts(cache);
+            built = true;
+        }
+        const std::vector<float>* L[9] = {&cache.ss, &cache.ssAvg, &cache.ssms, &cache.ssmsAvg, &cache.transDenser,
+                                          &cache.transLighter, &cache.transAvgDenser, &cache.transAvgLighter, &cache.sheen};
+        f = *L[which - 1];
+    }
+    else if (which == YG_TABLE_CIE_1NM || which == YG_TABLE_RGB_TO_SPD)
+    {
+        if (!yg::loadCie(dir + "/cie1931_2deg_d65_1nm.txt", cie, err)) return fail(YG_ERR_IO, err);
+        if (which == YG_TABLE_CIE_1NM) f.assign(cie.begin(), cie.end());
+        else
+        {
+            if (lmin < 360 || lmax > 830 || lmax <= lmin) return fail(YG_ERR_INVALID_ARGUMENT, "bad spectral range");
+            yg::buildRgbToSpd(cie, lmin, lmax, f);
+        }
+    }
+    else
+    {
+        return fail(YG_ERR_INVALID_ARGUMENT, "unknown table");
+    }
+    size_t n = u.empty() ? f.size() : u.size();
+    *count = n;
+    if (out)
+    {
+        if (capacity < n) return fail(YG_ERR_INVALID_ARGUMENT, "table buffer too small");
+        std::memcpy(out, u.empty() ? (const void*)f.data() : (const void*)u.data(), n * 4);
+    }
+    return YG_OK;
+}
+
+YG_API int yg_upload_mesh(yg_context* ctx, const yg_mesh_desc* d, uint32_t* mesh_id)
+{
+    if (!ctx || !d || !mesh_id || !d->positions || !d->normals || !d->indices)
+        return fail(YG_ERR_INVALID_ARGUMENT, "mesh: null argument");
+    if (d->index_bits != 16 && d->index_bits != 32) return fail(YG_ERR_INVALID_ARGUMENT, "mesh: index_bits must be 16 or 32");
+    if (d->index_count % 3 != 0) return fail(YG_ERR_INVALID_ARGUMENT, "mesh: index_count must be a multiple of 3");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    Mesh m;
+    m.vertexBase = (uint32_t)(ctx->positions.size() / 3);
+    m.vertexCount = d->vertex_count;
+    m.indexBase = (uint32_t)ctx->indices.size();
+    m.indexCount = d->index_count;
+    m.tangents = d->tangents != nullptr;
+    m.uvs = d->uvs != nullptr;
+    for (uint32_t i = 0; i < d->index_count; ++i)
+    {
+        uint32_t v = d->index_bits == 16 ? ((const uint16_t*)d->indices)[i] : ((const uint32_t*)d->indices)[i];
+        if (v >= d->vertex_count) return fail(YG_ERR_INVALID_ARGUMENT, "mesh: index out of range");
+    }
+    if (d->submesh_count == 0 || !d->submesh_ranges)
+    {
+        m.submeshes.push_back({0u, d->index_count});
+    }
+    else
+    {
+        for (uint32_t s = 0; s < d->submesh_count; ++s)
+        {
+            uint32_t first = d->submesh_ranges[2 * s], cnt = d->submesh_ranges[2 * s + 1];
+            if (first % 3 || cnt % 3 || (uint64_t)first + cnt > d->index_count)
+                return fail(YG_ERR_INVALID_ARGUMENT, "mesh: invalid submesh range");
+            m.submeshes.push_back({first, cnt});
+        }
+    }
+    ctx->positions.insert(ctx->positions.end(), d->positions, d->positions + 3 * (size_t)d->vertex_count);
+    ctx->normals.insert(ctx->normals.end(), d->normals, d->normals + 3 * (size_t)d->vertex_count);
+    for (uint32_t i = 0; i < d->vertex_count; ++i)
+    {
+        ctx->tangents.push_back(d->tangents ? make_float4(d->tangents[4 * i], d->tangents[4 * i + 1], d->tangents[4 * i + 2],
+                                                          d->tangents[4 * i + 3])
+                                            : make_float4(1.f, 0.f, 0.f, 1.f));
+        ctx->uvs.push_back(d->uvs ? d->uvs[2 * i] : 0.5f);
+        ctx->uvs.push_back(d->uvs ? d->uvs[2 * i + 1] : 0.5f);
+    }
+    for (uint32_t i = 0; i < d->index_count; ++i)
+        ctx->indices.push_back(d->index_bits == 16 ? ((const uint16_t*)d->indices)[i] : ((const uint32_t*)d->indices)[i]);
+    *mesh_id = (uint32_t)ctx->meshes.size();
+    ctx->meshes.push_back(m);
+    ctx->sceneBuilt = false;
+    return YG_OK;
+}
+
+YG_API int yg_upload_materials(yg_context* ctx, const yg_material* mats, uint32_t count)
+{
+    if (!ctx || (!mats && count)) return fail(YG_ERR_INVALID_ARGUMENT, "materials: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    for (uint32_t i = 0; i < count; ++i)
+    {
+        if (mats[i].subsurface_amount > 0.0f)
+            return fail(YG_ERR_INVALID_ARGUMENT, "materials: subsurface scattering is not supported by this build");
+    }
+    ctx->materials.assign(mats, mats + count);
+    ctx->gpuMaterials.resize(count);
+    for (uint32_t i = 0; i < count; ++i) ctx->gpuMaterials[i] = packMaterial(mats[i]);
+    ctx->sceneBuilt = false;
+    return upload(ctx, ctx->dMat, ctx->gpuMaterials.data(), ctx->gpuMaterials.size());
+}
+
+YG_API int yg_upload_spectra(yg_context* ctx, const float* values, uint32_t n_curves, uint32_t n_points, float lmin,
+                             float lmax)
+{
+    if (!ctx || (!values && n_curves)) return fail(YG_ERR_INVALID_ARGUMENT, "spectra: null argument");
+    if (n_curves && (n_points < 2 || !(lmax > lmin))) return fail(YG_ERR_INVALID_ARGUMENT, "spectra: need >= 2 points and lmax > lmin");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    ctx->spectra.assign(values, values + (size_t)n_curves * n_points);
+    ctx->specPoints = n_points;
+    ctx->specLmin = lmin;
+    ctx->specLmax = lmax;
+    return upload(ctx, ctx->dSpec, ctx->spectra.data(), ctx->spectra.size());
+}
+
+YG_API int yg_set_instances(yg_context* ctx, const yg_instance* inst, uint32_t count)
+{
+    if (!ctx || (!inst && count)) return fail(YG_ERR_INVALID_ARGUMENT, "instances: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    ctx->instances.assign(inst, inst + count);
+    ctx->sceneBuilt = false;
+    return YG_OK;
+}
+
+YG_API int yg_set_camera(yg_context* ctx, const yg_camera* cam)
+{
+    if (!ctx || !cam) return fail(YG_ERR_INVALID_ARGUMENT, "camera: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    std::memcpy(ctx->camera.uvToView, cam->uv_to_view, 64);
+    std::memcpy(ctx->camera.viewToUV, cam->view_to_uv, 64);
+    std::memcpy(ctx->camera.worldToView, cam->world_to_view, 64);
+    std::memcpy(ctx->camera.viewToWorld, cam->view_to_world, 64);
+    ctx->camera.apertureRadius = std::max(0.0f, cam->aperture_radius);
+    ctx->camera.focusDistance = std::max(1e-4f, cam->focus_distance);
+    ctx->camera.forwardZSign = cam->view_forward_z_sign;
+    ctx->cameraSet = true;
+    return YG_OK;
+}
+
+YG_API int yg_build_scene(yg_context* ctx)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    cudaSetDevice(ctx->device);
+    const uint32_t nCurves = ctx->specPoints ? (uint32_t)(ctx->spectra.size() / ctx->specPoints) : 0u;
+    for (const yg_material& m : ctx->materials)
+    {
+        const int32_t ids[3] = {m.albedo_spectrum, m.specular_spectrum, m.emission_spectrum};
+        for (int32_t id : ids)
+            if (id >= 0 && (uint32_t)id >= nCurves)
+                return fail(YG_ERR_INVALID_ARGUMENT, "material references a spectrum that was not uploaded");
+    }
+    const size_t nInst = ctx->instances.size();
+    std::vector<yg::GpuInstance> gi(nInst);
+    std::vector<float3> v0, v1, v2;
+    std::vector<uint32_t> ki, kp;
+    std::vector<float> power;
+    std::vector<uint32_t> lightInst;
+    for (size_t i = 0; i < nInst; ++i)
+    {
+        const yg_instance& I = ctx->instances[i];
+        if (I.mesh >= ctx->meshes.size()) return fail(YG_ERR_INVALID_ARGUMENT, "instance: bad mesh id");
+        const Mesh& m = ctx->meshes[I.mesh];
+        if (I.submesh >= m.submeshes.size()) return fail(YG_ERR_INVALID_ARGUMENT, "instance: bad submesh");
+        if (I.material >= ctx->materials.size()) return fail(YG_ERR_INVALID_ARGUMENT, "instance: bad material id");
+        yg::GpuInstance& G = gi[i];
+        for (int r = 0; r < 3; ++r)
+        {
+            G.o2w[r] = make_float4(I.obj_to_world[4 * r], I.obj_to_world[4 * r + 1], I.obj_to_world[4 * r + 2], I.obj_to_world[4 * r + 3]);
+            G.w2o[r] = make_float4(I.world_to_obj[4 * r], I.world_to_obj[4 * r + 1], I.world_to_obj[4 * r + 2], I.world_to_obj[4 * r + 3]);
+        }
+        G.firstIndex = m.indexBase + m.submeshes[I.submesh].first;
+        G.primCount = m.submeshes[I.submesh].second / 3;
+        G.vertexBase = m.vertexBase;
+        G.material = I.material;
+        G.lightPdf = 0.0f;
+        G.hasTangents = m.tangents ? 1u : 0u;
+        G.hasUVs = m.uvs ? 1u : 0u;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t p = 0; p < G.primCount; ++p)
+        {
+            float3 w[3];
+            for (int k = 0; k < 3; ++k)
+            {
+                uint32_t vi = ctx->indices[G.firstIndex + 3 * p + k] + G.vertexBase;
+                float3 ob = yg::mk3(ctx->positions[3 * vi], ctx->positions[3 * vi + 1], ctx->positions[3 * vi + 2]);
+                w[k] = yg::xformPoint(G.o2w, ob);
+                lo[0] = std::min(lo[0], w[k].x); lo[1] = std::min(lo[1], w[k].y); lo[2] = std::min(lo[2], w[k].z);
+                hi[0] = std::max(hi[0], w[k].x); hi[1] = std::max(hi[1], w[k].y); hi[2] = std::max(hi[2], w[k].z);
+            }
+            v0.push_back(w[0]);
+            v1.push_back(w[1]);
+            v2.push_back(w[2]);
+            ki.push_back((uint32_t)i);
+            kp.push_back(p);
+        }
+        // mesh lights: emissive materials (LightManager.cpp:145), power estimate of
+        // estimateMeshLightPower (RaytraceCommonResources.cpp:385-404) over the instance bounds
+        const yg_material& M = ctx->materials[I.material];
+        if (M.emissive[0] + M.emissive[1] + M.emissive[2] > 0.0f && G.primCount > 0)
+        {
+            float ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+            float area = ex * ey + ey * ez + ez * ex;
+            float e = 0.2126f * M.emissive[0] + 0.7152f * M.emissive[1] + 0.0722f * M.emissive[2];
+            if (e <= 0.f) e = 1.f;
+            float sides = (M.material_mask & YG_MATERIAL_TWO_SIDED) ? 2.f : 1.f;
+            power.push_back(3.14159274f * e * area * sides);
+            lightInst.push_back((uint32_t)i);
+        }
+    }
+    std::vector<yg::GpuLight> lights(lightInst.size());
+    if (!lightInst.empty())
+    {
+        std::vector<float> thr;
+        std::vector<uint32_t> alias;
+        selectionPdfs(power);
+        aliasTable(power, thr, alias);
+        for (size_t l = 0; l < lightInst.size(); ++l)
+        {
+            lights[l].instance = lightInst[l];
+            lights[l].selectionPdf = power[l];
+            lights[l].aliasThreshold = thr[l];
+            lights[l].aliasIndex = alias[l];
+            gi[lightInst[l]].lightPdf = power[l];
+        }
+    }
+    std::vector<float4> tris, nodes;
+    yg::buildBvh(v0, v1, v2, ki, kp, tris, nodes);
+    ctx->nTris = v0.size();
+    ctx->nNodes = nodes.size() / 4;
+    ctx->nLights = (uint32_t)lights.size();
+    int r;
+    if ((r = upload(ctx, ctx->dTris, tris.data(), tris.size()))) return r;
+    if ((r = upload(ctx, ctx->dNodes, nodes.data(), nodes.size()))) return r;
+    if ((r = upload(ctx, ctx->dInst, gi.data(), gi.size()))) return r;
+    if ((r = upload(ctx, ctx->dLights, lights.data(), lights.size()))) return r;
+    if ((r = upload(ctx, ctx->dPos, ctx->positions.data(), ctx->positions.size()))) return r;
+    if ((r = upload(ctx, ctx->dNrm, ctx->normals.data(), ctx->normals.size()))) return r;
+    if ((r = upload(ctx, ctx->dTan, ctx->tangents.data(), ctx->tangents.size()))) return r;
+    if ((r = upload(ctx, ctx->dUV, ctx->uvs.data(), ctx->uvs.size()))) return r;
+    if ((r = upload(ctx, ctx->dIdx, ctx->indices.data(), ctx->indices.size()))) return r;
+    if (ctx->dSpec.p == nullptr)
+    {
+        float z[4] = {0, 0, 0, 0};
+        if ((r = upload(ctx, ctx->dSpec, z, 4))) return r;
+    }
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->sceneBuilt = true;
+    return YG_OK;
+}
+
+YG_API int yg_scene_info(yg_context* ctx, uint64_t* nt, uint64_t* nn, uint64_t* nl, uint64_t* bytes)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
+    if (nt) *nt = ctx->nTris;
+    if (nn) *nn = ctx->nNodes;
+    if (nl) *nl = ctx->nLights;
+    if (bytes)
+    {
+        const DevBuf* all[] = {&ctx->dTris, &ctx->dNodes, &ctx->dInst, &ctx->dMat, &ctx->dLights, &ctx->dPos, &ctx->dNrm,
+                               &ctx->dTan, &ctx->dUV, &ctx->dIdx, &ctx->dSpec};
+        uint64_t s = 0;
+        for (const DevBuf* b : all) s += b->bytes;
+        *bytes = s;
+    }
+    return YG_OK;
+}
+
+YG_API int yg_film_clear(yg_context* ctx, uint32_t w, uint32_t h)
+{
+    if (!ctx || w == 0 || h == 0) return fail(YG_ERR_INVALID_ARGUMENT, "film: bad size");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    cudaSetDevice(ctx->device);
+    size_t bytes = (size_t)w * h * sizeof(float4);
+    YG_CUDA(ctx->dFilmSum.ensure(bytes));
+    YG_CUDA(ctx->dFilmComp.ensure(bytes));
+    YG_CUDA(ctx->dAccA.ensure(bytes));
+    YG_CUDA(ctx->dAccN.ensure(bytes));
+    YG_CUDA(cudaMemsetAsync(ctx->dFilmSum.p, 0, bytes, ctx->stream));
+    YG_CUDA(cudaMemsetAsync(ctx->dFilmComp.p, 0, bytes, ctx->stream));
+    YG_CUDA(cudaMemsetAsync(ctx->dAccA.p, 0, bytes, ctx->stream));
+    YG_CUDA(cudaMemsetAsync(ctx->dAccN.p, 0, bytes, ctx->stream));
+    ctx->filmW = w;
+    ctx->filmH = h;
+    return YG_OK;
+}
+
+YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_record* dump)
+{
+    if (!ctx || !p) return fail(YG_ERR_INVALID_ARGUMENT, "render: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    if (!ctx->sceneBuilt) return fail(YG_ERR_NOT_READY, "render: call yg_build_scene first");
+    if (!ctx->cameraSet) return fail(YG_ERR_NOT_READY, "render: camera not set");
+    if (p->integrator > YG_INTEGRATOR_NEE)
+        return fail(YG_ERR_INVALID_ARGUMENT, "render: integrator not available in this build");
+    if (p->width == 0 || p->height == 0 || p->spp_count == 0) return fail(YG_ERR_INVALID_ARGUMENT, "render: empty request");
+    uint32_t cx = p->crop_x, cy = p->crop_y, cw = p->crop_w, ch = p->crop_h;
+    if (cw == 0 || ch == 0)
+    {
+        cx = cy = 0;
+        cw = p->width;
+        ch = p->height;
+    }
+    if ((uint64_t)cx + cw > p->width || (uint64_t)cy + ch > p->height) return fail(YG_ERR_INVALID_ARGUMENT, "render: crop outside image");
+    bool film = (p->flags & YG_FLAG_NO_FILM) == 0;
+    if (film && (ctx->filmW != p->width || ctx->filmH != p->height))
+        return fail(YG_ERR_NOT_READY, "render: film size differs, call yg_film_clear");
+    float lminf = p->lambda_min, lmaxf = p->lambda_max;
+    if (lminf == 0.0f && lmaxf == 0.0f)
+    {
+        lminf = 380.f;
+        lmaxf = 700.f;
+    }
+    int lmin = (int)lminf, lmax = (int)lmaxf;
+    if ((float)lmin != lminf || (float)lmax != lmaxf) return fail(YG_ERR_INVALID_ARGUMENT, "render: spectral range must be whole nm");
+    cudaSetDevice(ctx->device);
+    int r = ensureCie(ctx, lmin, lmax);
+    if (r) return r;
+    bool needRgb = sceneNeedsRgbLut(ctx, p->env_intensity_scale);
+    if (needRgb && (r = ensureRgbLut(ctx, lmin, lmax))) return r;
+
+    const uint64_t npix = (uint64_t)cw * ch;
+    const uint64_t maxSamplesPerChunk = 1ull << 26;
+    uint32_t chunkSpp = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->spp_count, maxSamplesPerChunk / npix));
+    bool feats = (p->flags & YG_FLAG_FEATURES) != 0;
+    YG_CUDA(ctx->dSamples.ensure(npix * chunkSpp * sizeof(float4)));
+    if (feats)
+    {
+        YG_CUDA(ctx->dFeatA.ensure(npix * chunkSpp * sizeof(float4)));
+        YG_CUDA(ctx->dFeatN.ensure(npix * chunkSpp * sizeof(float4)));
+    }
+    if (dump) YG_CUDA(ctx->dDump.ensure(npix * chunkSpp * 8 * sizeof(float)));
+    YG_CUDA(ctx->dRayCount.ensure(24));
+    YG_CUDA(cudaMemsetAsync(ctx->dRayCount.p, 0, 24, ctx->stream));
+    // Sobol points of every sample index of the request (RaytraceCommonResources.cpp:623-627)
+    std::vector<uint32_t> pts((size_t)p->spp_count * yg::kSobolDims);
+    for (uint32_t s = 0; s < p->spp_count; ++s)
+        for (uint32_t d = 0; d < (uint32_t)yg::kSobolDims; ++d)
+            pts[(size_t)s * yg::kSobolDims + d] = yg::sobolUint(ctx->sobolMatrices.data(), p->spp_start + s, d);
+    if ((r = upload(ctx, ctx->dSobol, pts.data(), pts.size()))) return r;
+
+    yg::SceneView S{};
+    S.tris = ctx->dTris.as<float4>();
+    S.nodes = ctx->dNodes.as<float4>();
+    S.instances = ctx->dInst.as<yg::GpuInstance>();
+    S.materials = ctx->dMat.as<yg::GpuMaterial>();
+    S.lights = ctx->dLights.as<yg::GpuLight>();
+    S.positions = ctx->dPos.as<float>();
+    S.normals = ctx->dNrm.as<float>();
+    S.tangents = ctx->dTan.as<float4>();
+    S.uvs = ctx->dUV.as<float2>();
+    S.indices = ctx->dIdx.as<uint32_t>();
+    S.spectra = ctx->dSpec.as<float>();
+    S.lutSS = ctx->dLut[0].as<float>();
+    S.lutSSAvg = ctx->dLut[1].as<float>();
+    S.lutSSMS = ctx->dLut[2].as<float>();
+    S.lutSSMSAvg = ctx->dLut[3].as<float>();
+    S.lutTransDenser = ctx->dLut[4].as<float>();
+    S.lutTransLighter = ctx->dLut[5].as<float>();
+    S.lutTransAvgDenser = ctx->dLut[6].as<float>();
+    S.lutTransAvgLighter = ctx->dLut[7].as<float>();
+    S.lutSheen = ctx->dLut[8].as<float>();
+    S.cie = ctx->dCie.as<float4>();
+    S.rgbToSpd = needRgb ? ctx->dRgb.as<float>() : nullptr;
+    S.cam = ctx->camera;
+    S.nLights = ctx->nLights;
+    S.nInstances = (uint32_t)ctx->instances.size();
+    S.specPoints = ctx->specPoints;
+    S.specLmin = ctx->specLmin;
+    S.specLmax = ctx->specLmax;
+    S.cieN = ctx->cieN;
+    S.lambdaMin = lminf;
+    S.lambdaMax = lmaxf;
+    S.cieYSumInv = ctx->cieYSumInv;
+    S.d65SumInv = ctx->d65SumInv;
+
+    yg::LaunchParams L{};
+    L.integrator = p->integrator;
+    L.width = p->width;
+    L.height = p->height;
+    L.cropX = cx;
+    L.cropY = cy;
+    L.cropW = cw;
+    L.cropH = ch;
+    L.maxDepth = p->max_depth;
+    L.regularizeAfter = p->regularize_after_vertices;
+    L.regularizeEnable = p->regularize_enable;
+    L.envScale = p->env_intensity_scale;
+    L.seed = p->seed;
+    L.flags = p->flags;
+    L.rayCounter = ctx->dRayCount.as<unsigned long long>();
+    L.traversalCounter = (p->flags & YG_FLAG_COUNT_TRAVERSAL) ? ctx->dRayCount.as<unsigned long long>() + 1 : nullptr;
+
+    uint32_t launches = 0;
+    YG_CUDA(cudaEventRecord(ctx->evStart, ctx->stream));
+    for (uint32_t s0 = 0; s0 < p->spp_count; s0 += chunkSpp)
+    {
+        uint32_t ns = std::min(chunkSpp, p->spp_count - s0);
+        S.sobol = ctx->dSobol.as<uint32_t>() + (size_t)s0 * yg::kSobolDims;
+        L.sppStart = p->spp_start + s0;
+        L.sppCount = ns;
+        L.nSamples = npix * ns;
+        L.sampleXYZ = ctx->dSamples.as<float4>();
+        L.dump = dump ? ctx->dDump.as<float>() : nullptr;
+        L.featAlbedo = feats ? ctx->dFeatA.as<float4>() : nullptr;
+        L.featNormalDepth = feats ? ctx->dFeatN.as<float4>() : nullptr;
+        launches += yg::launchPathKernel(S, L, ctx->smCount, ctx->stream);
+        if (film)
+            launches += yg::launchFilm(ctx->dFilmSum.as<float4>(), ctx->dFilmComp.as<float4>(), L.sampleXYZ, p->width, cx,
+                                       cy, cw, ch, ns, ctx->smCount, ctx->stream);
+        if (film && feats)
+            launches += yg::launchFeatures(ctx->dAccA.as<float4>(), ctx->dAccN.as<float4>(), L.featAlbedo, L.featNormalDepth,
+                                           p->width, cx, cy, cw, ch, ns, ctx->smCount, ctx->stream);
+        if (dump)
+        {
+            YG_CUDA(cudaMemcpyAsync(dump + (size_t)s0 * npix, ctx->dDump.p, npix * ns * 8 * sizeof(float),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+        }
+    }
+    YG_CUDA(cudaGetLastError());
+    YG_CUDA(cudaEventRecord(ctx->evStop, ctx->stream));
+    ctx->lastLaunches = launches;
+    if (dump)
+    {
+        YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return YG_OK;
+}
+
+YG_API int yg_last_render_stats(yg_context* ctx, float* ms, uint64_t* rays, uint32_t* launches)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
+    YG_CUDA(cudaEventSynchronize(ctx->evStop));
+    float t = 0;
+    YG_CUDA(cudaEventElapsedTime(&t, ctx->evStart, ctx->evStop));
+    unsigned long long rc = 0;
+    if (ctx->dRayCount.p) YG_CUDA(cudaMemcpy(&rc, ctx->dRayCount.p, 8, cudaMemcpyDeviceToHost));
+    if (ms) *ms = t;
+    if (rays) *rays = rc;
+    if (launches) *launches = ctx->lastLaunches;
+    return YG_OK;
+}
+
+YG_API int yg_last_traversal_counts(yg_context* ctx, uint64_t* nodes, uint64_t* tris)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
+    unsigned long long c[3] = {0, 0, 0};
+    if (ctx->dRayCount.p)
+    {
+        YG_CUDA(cudaStreamSynchronize(ctx->stream));
+        YG_CUDA(cudaMemcpy(c, ctx->dRayCount.p, 24, cudaMemcpyDeviceToHost));
+    }
+    if (nodes) *nodes = c[1];
+    if (tris) *tris = c[2];
+    return YG_OK;
+}
+
+YG_API int yg_film_read(yg_context* ctx, float* xyz, float* counts)
+{
+    if (!ctx || !xyz) return fail(YG_ERR_INVALID_ARGUMENT, "film: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    size_t n = (size_t)ctx->filmW * ctx->filmH;
+    if (n == 0) return fail(YG_ERR_NOT_READY, "film: not allocated");
+    std::vector<float4> s(n);
+    YG_CUDA(cudaMemcpyAsync(s.data(), ctx->dFilmSum.p, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < n; ++i)
+    {
+        float c = s[i].w;
+        float inv = c > 0.0f ? 1.0f / c : 0.0f;
+        xyz[3 * i] = s[i].x * inv;
+        xyz[3 * i + 1] = s[i].y * inv;
+        xyz[3 * i + 2] = s[i].z * inv;
+        if (counts) counts[i] = c;
+    }
+    return YG_OK;
+}
+
+YG_API int yg_features_read(yg_context* ctx, float* albedo, float* normal, float* depth)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "features: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    size_t n = (size_t)ctx->filmW * ctx->filmH;
+    if (n == 0) return fail(YG_ERR_NOT_READY, "film: not allocated");
+    std::vector<float4> a(n), nd(n), s(n);
+    YG_CUDA(cudaMemcpyAsync(a.data(), ctx->dAccA.p, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaMemcpyAsync(nd.data(), ctx->dAccN.p, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaMemcpyAsync(s.data(), ctx->dFilmSum.p, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < n; ++i)
+    {
+        float c = s[i].w > 0.f ? 1.0f / s[i].w : 0.f;
+        if (albedo)
+        {
+            albedo[3 * i] = a[i].x * c;
+            albedo[3 * i + 1] = a[i].y * c;
+            albedo[3 * i + 2] = a[i].z * c;
+        }
+        if (normal)
+        {
+            normal[3 * i] = nd[i].x * c;
+            normal[3 * i + 1] = nd[i].y * c;
+            normal[3 * i + 2] = nd[i].z * c;
+        }
+        if (depth) depth[i] = nd[i].w * c;
+    }
+    return YG_OK;
+}
+
+YG_API int yg_film_relmse(yg_context* ctx, const float* ref, double eps, double* out)
+{
+    if (!ctx || !ref || !out) return fail(YG_ERR_INVALID_ARGUMENT, "relmse: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    size_t n = (size_t)ctx->filmW * ctx->filmH;
+    if (n == 0) return fail(YG_ERR_NOT_READY, "film: not allocated");
+    YG_CUDA(ctx->dRef.ensure(n * 3 * sizeof(float)));
+    YG_CUDA(ctx->dRelmse.ensure(sizeof(double)));
+    YG_CUDA(cudaMemcpyAsync(ctx->dRef.p, ref, n * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    YG_CUDA(cudaMemsetAsync(ctx->dRelmse.p, 0, sizeof(double), ctx->stream));
+    yg::launchRelmse(ctx->dFilmSum.as<float4>(), ctx->dRef.as<float>(), (uint32_t)n, eps, ctx->dRelmse.as<double>(),
+                     ctx->smCount, ctx->stream);
+    double s = 0;
+    YG_CUDA(cudaMemcpyAsync(&s, ctx->dRelmse.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = s / (3.0 * (double)n);
+    return YG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,14 @@
+// Kernel launchers shared between the CUDA translation units and the C-ABI runtime.
+#pragma once
+#include "yg_types.h"
+
+namespace yg
+{
+int launchPathKernel(const SceneView& S, const LaunchParams& P, int smCount, cudaStream_t stream);
+int launchFilm(float4* sum, float4* comp, const float4* samples, uint32_t width, uint32_t cx, uint32_t cy, uint32_t cw,
+               uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
+int launchFeatures(float4* accA, float4* accN, const float4* fa, const float4* fn, uint32_t width, uint32_t cx, uint32_t cy,
+                   uint32_t cw, uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
+int launchRelmse(const float4* sum, const float* ref, uint32_t npix, double eps, double* out, int smCount,
+                 cudaStream_t stream);
+} // namespace yg

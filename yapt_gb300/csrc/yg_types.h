@@ -1,0 +1,132 @@
+// Device-resident scene layout shared by the host runtime and the CUDA kernels.
+//
+// HBM layout (one context, all arrays 16-byte aligned, read-only during a render):
+//   tris      float4[3 * T]  world-space triangles in BVH leaf order:
+//                            (v0.xyz, instance) (e1.xyz, primitive) (e2.xyz, 0)
+//   nodes     float4[4 * N]  binary BVH, two child boxes per node (64 B)
+//   instances GpuInstance[I] per (render object, submesh): transforms, mesh refs
+//   materials GpuMaterial[M] principled parameters after the reference's clamps
+//   vertex pools (object space): positions/normals float[3V], tangents float4[V],
+//   uvs float2[V], indices uint32 (local to the mesh, offset by vertex_base)
+//   LUTs / CIE / Sobol tables (a few hundred KB, L2 resident)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace yg
+{
+
+constexpr int kSobolDims = 256;       // NUMBER_OF_RANDOM_SAMPLE_DIMENSIONS (raytraceCommon.hlsl:12)
+constexpr int kMaxVolumes = 4;        // RAY_MAX_VOLUMES_ENTERED (raytraceCommon.hlsl:19)
+constexpr float kRayMinT = 5e-4f;     // DEFAULT_RAY_MIN_T (raytraceCommon.hlsl:24)
+constexpr int kLutSS = 32;            // SS_ALBEDO_LUT_DIM
+constexpr int kLutSSMS = 16;          // SSMS_ALBEDO_LUT_DIM
+constexpr int kLutTrans = 16;         // SS_ALBEDO_TRANSLUCENT_LUT_DIM
+constexpr int kLutSheen = 16;         // SS_ALBEDO_SHEEN_LUT_DIM
+constexpr int kRgbLutRes = 64;        // SRGB_TO_SPD_RES (spectralConstants.h:27)
+
+// MaterialEntryGPU (materialsCommonResources.hlsl:10-38) after the clamps of
+// BindlessMaterialManager.cpp:73-98, plus spectral curve references.
+struct alignas(16) GpuMaterial
+{
+    float4 specAmount_ccAmount_ccIOR_ccRough;
+    float4 albedo_transparency;
+    float4 specular_metalness;
+    float4 absorption_ior;
+    float4 emissive_roughness;
+    float anisotropy, anisotropyRotation;
+    uint32_t mask;
+    float thinFilmNM;
+    float cauchyA, cauchyB, sheenAmount, emissionFocus;
+    float4 sheenColor_roughness;
+    float4 subsurfaceRadius_amount;
+    int albedoSpectrum, specularSpectrum, emissionSpectrum, pad;
+};
+
+// Per (render object, submesh) instance: RenderObjectTransformDataGPU + MeshEntryGPU refs.
+struct alignas(16) GpuInstance
+{
+    float4 o2w[3];
+    float4 w2o[3];
+    uint32_t firstIndex;  // into the index pool
+    uint32_t primCount;   // triangles of the submesh
+    uint32_t vertexBase;  // added to the mesh-local indices
+    uint32_t material;
+    float lightPdf;       // g_instanceLightSelectionPDFs entry (0: not a light)
+    uint32_t hasTangents;
+    uint32_t hasUVs;
+    uint32_t pad;
+};
+
+// LightEntryGPU (materialsCommonResources.hlsl:51-71), mesh lights only.
+struct alignas(16) GpuLight
+{
+    uint32_t instance;
+    float selectionPdf;
+    float aliasThreshold;
+    uint32_t aliasIndex;
+};
+
+struct alignas(16) GpuCamera
+{
+    float uvToView[16];
+    float viewToUV[16];
+    float worldToView[16];
+    float viewToWorld[16];
+    float apertureRadius, focusDistance, forwardZSign, pad;
+};
+
+// All read-only tables and scene arrays a render kernel needs.
+struct SceneView
+{
+    const float4* tris;
+    const float4* nodes;
+    const GpuInstance* instances;
+    const GpuMaterial* materials;
+    const GpuLight* lights;
+    const float* positions;
+    const float* normals;
+    const float4* tangents;
+    const float2* uvs;
+    const uint32_t* indices;
+    const float* spectra;  // n_curves x specPoints
+    const float* lutSS, *lutSSAvg, *lutSSMS, *lutSSMSAvg;
+    const float* lutTransDenser, *lutTransLighter, *lutTransAvgDenser, *lutTransAvgLighter;
+    const float* lutSheen;
+    const float4* cie;     // (xbar, ybar, zbar, d65) per 1 nm over [lambdaMin, lambdaMax]
+    const float* rgbToSpd; // 64^3 x 3, may be null
+    const uint32_t* sobol; // [spp_count][kSobolDims] points of this launch
+    GpuCamera cam;
+    uint32_t nLights;
+    uint32_t nInstances;
+    uint32_t specPoints;
+    float specLmin, specLmax;
+    uint32_t cieN;
+    float lambdaMin, lambdaMax;
+    float cieYSumInv;      // CIE_Y_SUM_INV for the range
+    float d65SumInv;       // CIE_D65_SUM_INV for the range
+    uint32_t rootIsLeaf;
+};
+
+struct LaunchParams
+{
+    uint32_t integrator;
+    uint32_t width, height;
+    uint32_t cropX, cropY, cropW, cropH;
+    uint32_t sppStart, sppCount;
+    uint32_t maxDepth;
+    uint32_t regularizeAfter;
+    uint32_t regularizeEnable;
+    float envScale;
+    uint32_t seed;
+    uint32_t flags;
+    uint64_t nSamples;      // cropW * cropH * sppCount
+    float4* sampleXYZ;      // [sppCount][cropH*cropW] (xyz, 1) per sample
+    float* dump;            // optional per-sample records (8 floats) or null
+    float4* featAlbedo;     // optional per-sample first-hit features or null
+    float4* featNormalDepth;
+    unsigned long long* rayCounter; // optional
+    unsigned long long* traversalCounter; // optional [nodes, triangles]; selects the counting kernel
+};
+
+} // namespace yg

@@ -1,0 +1,129 @@
+"""Python handle on a native render context (C ABI of include/yapt_gpu.h)."""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+class Context:
+    """Owns one yg_context: device memory, one CUDA stream, the uploaded scene and film."""
+
+    def __init__(self, device=0):
+        self.lib = N.load()
+        h = C.c_void_p()
+        N.check(self.lib.yg_create(N.DATA_DIR.encode(), int(device), C.byref(h)))
+        self.h = h
+        self.width = self.height = 0
+
+    def close(self):
+        if self.h:
+            self.lib.yg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- scene -------------------------------------------------------------
+    def upload_scene(self, scene):
+        scene.upload(self.lib, self.h)
+
+    def scene_info(self):
+        v = [C.c_uint64() for _ in range(4)]
+        N.check(self.lib.yg_scene_info(self.h, *[C.byref(x) for x in v]))
+        return dict(triangles=v[0].value, nodes=v[1].value, lights=v[2].value, device_bytes=v[3].value)
+
+    def table(self, name):
+        which = N.TABLES[name]
+        n = C.c_size_t()
+        N.check(self.lib.yg_get_table(self.h, which, None, 0, C.byref(n)))
+        dt = np.uint32 if name == "sobol" else np.float32
+        out = np.zeros(n.value, dtype=dt)
+        if name == "cie":
+            out = np.zeros(n.value, dtype=np.float32)
+        N.check(self.lib.yg_get_table(self.h, which, out.ctypes.data_as(C.c_void_p), out.size, C.byref(n)))
+        return out
+
+    # -- rendering ---------------------------------------------------------
+    def film_clear(self, width, height):
+        N.check(self.lib.yg_film_clear(self.h, int(width), int(height)))
+        self.width, self.height = int(width), int(height)
+
+    @staticmethod
+    def params(integrator="nee", width=64, height=64, spp_start=0, spp=1, max_depth=8, regularize_after=8,
+               regularize=True, env_scale=0.0, seed=0, flags=0, crop=None, lambda_range=(380.0, 700.0)):
+        p = N.RenderParams()
+        p.integrator = N.INTEGRATORS[integrator] if isinstance(integrator, str) else int(integrator)
+        p.width, p.height = int(width), int(height)
+        p.spp_start, p.spp_count = int(spp_start), int(spp)
+        p.max_depth = int(max_depth)
+        p.regularize_after_vertices = int(regularize_after)
+        p.regularize_enable = 1 if regularize else 0
+        p.env_intensity_scale = float(env_scale)
+        p.seed = int(seed)
+        p.flags = int(flags)
+        if crop is not None:
+            p.crop_x, p.crop_y, p.crop_w, p.crop_h = [int(v) for v in crop]
+        p.lambda_min, p.lambda_max = float(lambda_range[0]), float(lambda_range[1])
+        return p
+
+    def render(self, params, dump=False):
+        """Runs one render request; with dump=True returns the per-sample records
+        (spp, crop_h, crop_w, 8): hero lambda, L[4], XYZ."""
+        if dump:
+            cw = params.crop_w or params.width
+            ch = params.crop_h or params.height
+            rec = np.zeros((params.spp_count, ch, cw, 8), np.float32)
+            N.check(self.lib.yg_render(self.h, C.byref(params), rec.ctypes.data_as(C.c_void_p)))
+            return rec
+        N.check(self.lib.yg_render(self.h, C.byref(params), None))
+        return None
+
+    def synchronize(self):
+        N.check(self.lib.yg_synchronize(self.h))
+
+    def film(self):
+        xyz = np.zeros((self.height, self.width, 3), np.float32)
+        cnt = np.zeros((self.height, self.width), np.float32)
+        N.check(self.lib.yg_film_read(self.h, xyz.ctypes.data_as(C.POINTER(C.c_float)),
+                                      cnt.ctypes.data_as(C.POINTER(C.c_float))))
+        return xyz, cnt
+
+    def features(self):
+        a = np.zeros((self.height, self.width, 3), np.float32)
+        n = np.zeros((self.height, self.width, 3), np.float32)
+        d = np.zeros((self.height, self.width), np.float32)
+        N.check(self.lib.yg_features_read(self.h, a.ctypes.data_as(C.POINTER(C.c_float)),
+                                          n.ctypes.data_as(C.POINTER(C.c_float)), d.ctypes.data_as(C.POINTER(C.c_float))))
+        return a, n, d
+
+    def relmse(self, reference_xyz, eps=1e-2):
+        ref = np.ascontiguousarray(np.asarray(reference_xyz, np.float32))
+        out = C.c_double()
+        N.check(self.lib.yg_film_relmse(self.h, ref.ctypes.data_as(C.POINTER(C.c_float)), float(eps), C.byref(out)))
+        return out.value
+
+    def last_stats(self):
+        ms, rays, launches = C.c_float(), C.c_uint64(), C.c_uint32()
+        N.check(self.lib.yg_last_render_stats(self.h, C.byref(ms), C.byref(rays), C.byref(launches)))
+        return dict(ms=ms.value, rays=rays.value, launches=launches.value)
+
+    def traversal_counts(self):
+        n, t = C.c_uint64(), C.c_uint64()
+        N.check(self.lib.yg_last_traversal_counts(self.h, C.byref(n), C.byref(t)))
+        return dict(nodes=n.value, triangles=t.value)
+
+
+def xyz_to_srgb_linear(xyz):
+    """c_srgbXYZToRGB (colorSpaces.hlsl:18-23)."""
+    M = np.array([[3.2406, -1.5372, -0.4986], [-0.9689, 1.8758, 0.0415], [0.0557, -0.2040, 1.0570]], np.float32)
+    return xyz @ M.T
