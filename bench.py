@@ -26,8 +26,8 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(workload="nee_random_shapes_500_icospheres", width=1024, height=1024, spp=64, max_depth=12,
                 integrator="nee", lambda_nm=[380, 780], scene_seed=0)
 METRIC = "Msamples/s (NEE, random-shapes scene, 1024x1024, 64 spp, depth 12, equal relMSE)"
-CPU_CROP = (384, 384, 256, 256)  # bounded CPU sample: 256x256 centre crop
-CPU_SPP = 8
+CPU_CROP = (256, 256, 512, 512)  # bounded CPU sample: 512x512 centre crop
+CPU_SPP = 32
 
 
 def read_peaks():
@@ -142,6 +142,8 @@ def cpu_port_rate(scene, seconds_hint=None, threads=None, spp=CPU_SPP, crop=CPU_
     luts = {n: N.host_table(n) for n in names}
     h = pyoracle.OracleSceneHandle(scene, luts)
     threads = threads or os.cpu_count() or 1
+    side = min(crop[2], WORKLOAD["width"], WORKLOAD["height"])
+    crop = ((WORKLOAD["width"] - side) // 2, (WORKLOAD["height"] - side) // 2, side, side)
     p = Context.params(WORKLOAD["integrator"], WORKLOAD["width"], WORKLOAD["height"], spp=spp,
                        max_depth=WORKLOAD["max_depth"], lambda_range=WORKLOAD["lambda_nm"], crop=crop)
     r = h.render(p, precision=32, threads=threads, records=False, film=False)
@@ -280,7 +282,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--size", type=int, default=0, help="image side for a smaller profiling case")
+    ap.add_argument("--spp", type=int, default=0, help="samples per pixel for a smaller profiling case")
     args = ap.parse_args()
+    if args.size:
+        WORKLOAD["width"] = WORKLOAD["height"] = args.size
+    if args.spp:
+        WORKLOAD["spp"] = args.spp
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
