@@ -136,6 +136,7 @@ typedef struct yg_camera
 #define YG_FLAG_NO_FILM (1u << 8)      /* skip film accumulation (sample dump only) */
 #define YG_FLAG_FEATURES (1u << 9)     /* accumulate first-hit albedo/normal/depth */
 #define YG_FLAG_COUNT_TRAVERSAL (1u << 10) /* count BVH nodes visited / triangles tested (slower) */
+#define YG_FLAG_MEGAKERNEL (1u << 11)      /* one-thread-per-path kernel instead of the wavefront */
 
 typedef struct yg_render_params
 {

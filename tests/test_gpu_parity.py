@@ -127,3 +127,15 @@ def test_invalid_requests_fail_with_codes(built):
             c.render(c.params("nee", 8, 8, spp=1, crop=(4, 4, 8, 8), flags=256))  # crop outside the image
         with pytest.raises(YaptError):
             c.render(c.params("nee", 8, 8, spp=1))  # film not sized
+
+
+def test_wavefront_and_megakernel_give_identical_samples(built):
+    from yapt_gb300._native import YG_FLAG_MEGAKERNEL
+    sc = configs.random_shapes_scene(2, n_spheres=80)
+    with Context(0) as c:
+        c.upload_scene(sc)
+        p = c.params("nee", 96, 64, spp=3, max_depth=12, lambda_range=(380, 780), flags=256)
+        wave = c.render(p, dump=True)
+        p.flags = 256 | YG_FLAG_MEGAKERNEL
+        mega = c.render(p, dump=True)
+    assert np.array_equal(wave, mega)

@@ -20,6 +20,7 @@ YG_FLAG_DISABLE_TEXEL_JITTER = 1 << 1
 YG_FLAG_NO_FILM = 1 << 8
 YG_FLAG_FEATURES = 1 << 9
 YG_FLAG_COUNT_TRAVERSAL = 1 << 10
+YG_FLAG_MEGAKERNEL = 1 << 11
 
 TABLES = {
     "sobol": 0, "ss": 1, "ss_avg": 2, "ssms": 3, "ssms_avg": 4, "trans_denser": 5, "trans_lighter": 6,

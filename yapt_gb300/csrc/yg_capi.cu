@@ -99,7 +99,7 @@ struct yg_context
     DevBuf dTris, dNodes, dInst, dMat, dLights, dPos, dNrm, dTan, dUV, dIdx, dSpec;
     DevBuf dLut[9];
     DevBuf dCie, dRgb, dSobol, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
-    DevBuf dFilmSum, dFilmComp, dAccA, dAccN;
+    DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena;
     uint32_t nLights = 0;
     int cieLmin = -1, cieLmax = -1;
     uint32_t cieN = 0;
@@ -115,7 +115,7 @@ struct yg_context
     {
         DevBuf* all[] = {&dTris, &dNodes, &dInst, &dMat, &dLights, &dPos, &dNrm, &dTan, &dUV, &dIdx, &dSpec, &dCie, &dRgb,
                          &dSobol, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
-                         &dFilmComp, &dAccA, &dAccN};
+                         &dFilmComp, &dAccA, &dAccN, &dArena};
         for (DevBuf* b : all) b->release();
         for (auto& b : dLut) b.release();
         if (evStart) cudaEventDestroy(evStart);
@@ -727,6 +727,9 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         YG_CUDA(ctx->dFeatN.ensure(npix * chunkSpp * sizeof(float4)));
     }
     if (dump) YG_CUDA(ctx->dDump.ensure(npix * chunkSpp * 8 * sizeof(float)));
+    const bool mega = (p->flags & YG_FLAG_MEGAKERNEL) != 0;
+    uint32_t waveCap = (uint32_t)std::min<uint64_t>(npix * chunkSpp, 1ull << 22);
+    if (!mega) YG_CUDA(ctx->dArena.ensure(waveCap * yg::wavefrontBytesPerSlot() + (64u << 10)));
     YG_CUDA(ctx->dRayCount.ensure(24));
     YG_CUDA(cudaMemsetAsync(ctx->dRayCount.p, 0, 24, ctx->stream));
     // Sobol points of every sample index of the request (RaytraceCommonResources.cpp:623-627)
@@ -801,7 +804,8 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         L.dump = dump ? ctx->dDump.as<float>() : nullptr;
         L.featAlbedo = feats ? ctx->dFeatA.as<float4>() : nullptr;
         L.featNormalDepth = feats ? ctx->dFeatN.as<float4>() : nullptr;
-        launches += yg::launchPathKernel(S, L, ctx->smCount, ctx->stream);
+        if (mega) launches += yg::launchPathKernel(S, L, ctx->smCount, ctx->stream);
+        else launches += yg::launchWavefront(S, L, ctx->dArena.p, waveCap, ctx->smCount, ctx->stream);
         if (film)
             launches += yg::launchFilm(ctx->dFilmSum.as<float4>(), ctx->dFilmComp.as<float4>(), L.sampleXYZ, p->width, cx,
                                        cy, cw, ch, ns, ctx->smCount, ctx->stream);

@@ -1,568 +1,359 @@
-// Unidirectional and NEE spectral path integrators (megakernel form) and the
-// compensated FP32 film. Restates, for CUDA, YAPT's DXR ray generation / closest-hit /
-// miss shaders:
-//   rayGenPrimaryRays.hlsl:10-145   (camera ray, bounce loop, Russian roulette, ToXYZ)
-//   rayHitDefault.hlsl:36-585       (surface setup, emitter MIS, NEE, BSDF sampling)
-//   rayMissEnvironment.hlsl:13-31   (environment)
-//   lightSampling.hlsl:31-188, 360-370 (alias light pick, area light sampling)
-//   hitShadersCommon.hlsl:138-222   (absorption, spawn offset, medium start)
-// One thread traces one (pixel, sample index) path. Samples of a launch are written
-// to a [sample][pixel] buffer and folded into the film in sample order, so the film
-// is independent of thread scheduling.
-#include "yg_shading.cuh"
-#include "yg_trace.cuh"
+// Unidirectional and NEE spectral path integrators on the GPU, in two forms that
+// produce bit-identical samples:
+//  * wavefront (default): generate -> closest-hit traversal -> shade (emitter MIS,
+//    NEE request, BSDF sample, Russian roulette) -> shadow traversal -> next bounce,
+//    with path state in HBM (SoA) and ray queues compacted by warp-aggregated appends.
+//    The traversal kernels carry no shading state, so they run at high occupancy.
+//  * megakernel: one thread traces one path to the end (kept as a cross-check).
+// Samples of a launch are written to a [sample][pixel] buffer and folded into the
+// film in sample order, so the film does not depend on thread scheduling.
+#include "yg_path.cuh"
 #include "yg_kernels.h"
 
 namespace yg
 {
 
-constexpr uint32_t kFlagSecondaryTerminated = 1u << 0; // RAYSTATE_FLAGS_* (RayState.hlsl:4-6)
-constexpr uint32_t kFlagRegularize = 1u << 1;
-constexpr uint32_t kFlagDelta = 1u << 2;
-
-struct PathState
+__device__ __forceinline__ uint32_t warpAppend(uint32_t* counter, bool pred)
 {
-    float4 throughput;
-    float4 total;
-    float3 origin;
-    float3 dir;
-    float pdfThisRay;
-    uint32_t flags;
-    uint32_t pathLength;
-    uint32_t nVol;
-    float volIOR[kMaxVolumes];
-    float4 volAbs[kMaxVolumes];
-    uint32_t volMat[kMaxVolumes];
-};
-
-// Payload volume stack (payload.hlsl:15-103)
-YG_DEV float currentIOR(const PathState& p) { return p.nVol != 0 ? p.volIOR[p.nVol - 1] : 1.0f; }
-YG_DEV float previousIOR(const PathState& p) { return p.nVol > 1 ? p.volIOR[p.nVol - 2] : 1.0f; }
-YG_DEV void enteredVolume(PathState& p, float ior, float4 absorption, uint32_t mat)
-{
-    p.nVol = min(p.nVol + 1, (uint32_t)kMaxVolumes);
-    p.volIOR[p.nVol - 1] = ior;
-    p.volAbs[p.nVol - 1] = absorption;
-    p.volMat[p.nVol - 1] = mat;
+    // one atomic per warp; returns this lane's slot (valid only where pred)
+    // called by all 32 lanes of a warp (the callers iterate a warp-uniform trip count)
+    uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t leader = mask ? (uint32_t)(__ffs(mask) - 1) : 0u;
+    uint32_t base = 0;
+    if (mask && lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
 }
-YG_DEV void exitedVolume(PathState& p, uint32_t mat)
+
+__device__ __forceinline__ void countRays(unsigned long long* ctr, uint32_t n)
 {
-    if (p.nVol == 0) return;
-    int index = -1;
-    for (int i = (int)p.nVol - 1; i >= 0; --i)
+    if (!ctr) return;
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+    if ((threadIdx.x & 31) == 0 && n) atomicAdd(ctr, (unsigned long long)n);
+}
+
+__device__ __forceinline__ void countTraversal(unsigned long long* ctr, const TraversalCount& tc)
+{
+    if (!ctr) return;
+    unsigned long long n = tc.nodes, t = tc.tris;
+    for (int o = 16; o > 0; o >>= 1)
     {
-        if (p.volMat[i] == mat) { index = i; break; }
+        n += __shfl_down_sync(0xffffffffu, n, o);
+        t += __shfl_down_sync(0xffffffffu, t, o);
     }
-    if (index < 0) index = (int)p.nVol - 1;
-    for (uint32_t i = (uint32_t)index; i + 1 < p.nVol; ++i)
+    if ((threadIdx.x & 31) == 0)
     {
-        p.volIOR[i] = p.volIOR[i + 1];
-        p.volAbs[i] = p.volAbs[i + 1];
-        p.volMat[i] = p.volMat[i + 1];
-    }
-    --p.nVol;
-}
-
-// spawnRayOrigin, Ray Tracing Gems ch. 6 (hitShadersCommon.hlsl:147-160)
-YG_DEV float spawnComp(float p, float n, int oi)
-{
-    int so = p < 0.0f ? -oi : oi;
-    float off = __int_as_float(__float_as_int(p) + so);
-    return fabsf(p) < (1.0f / 32.0f) ? p + (1.0f / 65536.0f) * n : off;
-}
-YG_DEV float3 spawnRayOrigin(float3 p, float3 gn, float3 dir)
-{
-    float3 n = dot(dir, gn) < 0.0f ? -gn : gn;
-    int ox = (int)(256.0f * n.x), oy = (int)(256.0f * n.y), oz = (int)(256.0f * n.z);
-    return mk3(spawnComp(p.x, n.x, ox), spawnComp(p.y, n.y, oy), spawnComp(p.z, n.z, oz));
-}
-
-YG_DEV float weightMIS(float a, float b)
-{
-    float a2 = a * a, b2 = b * b;
-    return a2 / (a2 + b2);
-}
-YG_DEV float areaToSolidAngle(float3 v, float3 n)
-{
-    float invD2 = 1.0f / dot(v, v);
-    float absDot = fabsf(dot(n, v * sqrtf(invD2)));
-    return 1.0f / (absDot * invD2);
-}
-
-struct TriGeom
-{
-    float3 p1, p2, p3;
-    uint32_t i1, i2, i3;
-};
-YG_DEV TriGeom fetchTri(const SceneView& S, const GpuInstance& I, uint32_t prim)
-{
-    TriGeom g;
-    const uint32_t* ix = S.indices + I.firstIndex + 3u * prim;
-    g.i1 = __ldg(ix) + I.vertexBase;
-    g.i2 = __ldg(ix + 1) + I.vertexBase;
-    g.i3 = __ldg(ix + 2) + I.vertexBase;
-    const float* P = S.positions;
-    g.p1 = mk3(__ldg(P + 3 * g.i1), __ldg(P + 3 * g.i1 + 1), __ldg(P + 3 * g.i1 + 2));
-    g.p2 = mk3(__ldg(P + 3 * g.i2), __ldg(P + 3 * g.i2 + 1), __ldg(P + 3 * g.i2 + 2));
-    g.p3 = mk3(__ldg(P + 3 * g.i3), __ldg(P + 3 * g.i3 + 1), __ldg(P + 3 * g.i3 + 2));
-    return g;
-}
-YG_DEV float3 interp3(const float* A, const TriGeom& g, float b0, float b1, float b2)
-{
-    float3 a = mk3(__ldg(A + 3 * g.i1), __ldg(A + 3 * g.i1 + 1), __ldg(A + 3 * g.i1 + 2));
-    float3 b = mk3(__ldg(A + 3 * g.i2), __ldg(A + 3 * g.i2 + 1), __ldg(A + 3 * g.i2 + 2));
-    float3 c = mk3(__ldg(A + 3 * g.i3), __ldg(A + 3 * g.i3 + 1), __ldg(A + 3 * g.i3 + 2));
-    return a * b0 + b * b1 + c * b2;
-}
-
-// Scalar material parameters before the spectral conversion (SurfaceDefinitionRGB)
-struct SurfaceRGB
-{
-    float3 albedo, specular, absorption, emissive, sheenColor;
-};
-
-YG_DEV float4 rgbOrCurve(const SceneView& S, const Spectral& sp, float3 rgb, int curve)
-{
-    if (curve >= 0) return fromCurve(S, sp, curve);
-    return fromRGB(S, sp, rgb);
-}
-YG_DEV float4 emissionSpectrum(const SceneView& S, const Spectral& sp, float3 rgb, int curve)
-{
-    if (curve >= 0) return fromCurve(S, sp, curve) * fmaxf(fmaxf(rgb.x, rgb.y), rgb.z);
-    if (isZero3(rgb)) return splat4(0.0f);
-    return fromRGBUnbounded(S, sp, rgb);
-}
-
-// regularize (materialsCommon.hlsl:399-418)
-YG_DEV float regularizeR(float lr, bool squared)
-{
-    float r = squared ? lr * lr : lr;
-    if (r < 0.3f)
-    {
-        r = clampf(r * 2.0f, 0.1f, 0.3f);
-        return squared ? sqrtf(r) : r;
-    }
-    return lr;
-}
-
-struct HitSurface
-{
-    Surface s;
-    float3 rayDirOS;
-    uint32_t material;
-    float3 albedoRGB; // first-hit features
-};
-
-// fetch + fetchSurfaceMaterialParameters + two-sided orientation + tangent rotation +
-// regularisation + RGB -> spectral conversion (rayHitDefault.hlsl:470-520)
-YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectral& sp, const Hit& hit, const GpuInstance& I,
-                         float3 rayDirWS, PathState& ps, HitSurface& hs)
-{
-    TriGeom g = fetchTri(S, I, hit.prim);
-    float b0 = 1.0f - hit.b1 - hit.b2;
-    float3 gn = normalize(cross(g.p2 - g.p1, g.p3 - g.p1));
-    float3 nrm = normalize(interp3(S.normals, g, b0, hit.b1, hit.b2));
-    float3 tan = mk3(1.f, 0.f, 0.f);
-    if (I.hasTangents)
-    {
-        float4 t1 = __ldg(S.tangents + g.i1), t2 = __ldg(S.tangents + g.i2), t3 = __ldg(S.tangents + g.i3);
-        float3 a = mk3(t1.x * t1.w, t1.y * t1.w, t1.z * t1.w);
-        float3 b = mk3(t2.x * t2.w, t2.y * t2.w, t2.z * t2.w);
-        float3 c = mk3(t3.x * t3.w, t3.y * t3.w, t3.z * t3.w);
-        tan = normalize(a * b0 + b * hit.b1 + c * hit.b2);
-    }
-    float3 rd = normalize(xformVector(I.w2o, rayDirWS));
-    hs.rayDirOS = rd;
-    hs.material = I.material;
-    const GpuMaterial& M = S.materials[I.material];
-    Surface& s = hs.s;
-    float4 a_t = M.albedo_transparency, s_m = M.specular_metalness, ab_i = M.absorption_ior, e_r = M.emissive_roughness;
-    float4 sc = M.specAmount_ccAmount_ccIOR_ccRough, sh = M.sheenColor_roughness;
-    SurfaceRGB rgb;
-    rgb.albedo = mk3(a_t.x, a_t.y, a_t.z);
-    rgb.specular = mk3(s_m.x, s_m.y, s_m.z);
-    rgb.absorption = mk3(ab_i.x, ab_i.y, ab_i.z);
-    rgb.emissive = mk3(e_r.x, e_r.y, e_r.z);
-    rgb.sheenColor = mk3(sh.x, sh.y, sh.z);
-    s.transparency = a_t.w;
-    s.metalness = s_m.w;
-    s.dielectricIOR = ab_i.w;
-    s.roughness = e_r.w;
-    s.emissionFocus = M.emissionFocus;
-    s.specularAmount = sc.x;
-    s.clearCoatAmount = sc.y;
-    s.clearCoatIOR = sc.z;
-    s.clearCoatRoughness = sc.w;
-    s.cauchyA = M.cauchyA;
-    s.cauchyB = M.cauchyB;
-    s.anisotropy = M.anisotropy;
-    s.anisotropyRotation = M.anisotropyRotation;
-    s.thinFilmNM = M.thinFilmNM;
-    s.flags = M.mask;
-    s.sheenRoughness = fmaxf(sh.w, 0.07f);
-    s.sheenAmount = M.sheenAmount;
-    s.subsurfaceAmount = M.subsurfaceRadius_amount.w;
-    s.coatingLayerNormal = nrm;
-    s.baseLayerNormal = nrm;
-    s.geometryNormal = gn;
-    s.tangent = tan;
-    // handleTwoSidedMaterialOrientation (materialsCommon.hlsl:440-448), wo = -rayDir
-    if (s.transparency == 0.0f && isTwoSided(s.flags))
-    {
-        float3 wo = -rd;
-        if (dot(wo, s.baseLayerNormal) < 0.0f) s.baseLayerNormal = -s.baseLayerNormal;
-        if (dot(wo, s.coatingLayerNormal) < 0.0f) s.coatingLayerNormal = -s.coatingLayerNormal;
-        if (dot(wo, s.geometryNormal) < 0.0f) s.geometryNormal = -s.geometryNormal;
-    }
-    // setupSurfaceOrientation (materialsCommon.hlsl:487-501)
-    if (s.anisotropyRotation > 0.0f)
-    {
-        float ang = s.anisotropyRotation * 2.0f * kPI;
-        float sa, ca;
-        ygm_sincosf(ang, &sa, &ca);
-        float3 t = s.tangent;
-        s.tangent = mk3(ca * t.x + 0.0f * t.y + sa * t.z, 0.0f * t.x + 1.0f * t.y + 0.0f * t.z, -sa * t.x + 0.0f * t.y + ca * t.z);
-    }
-    // regularisation (rayHitDefault.hlsl:494-502)
-    if (P.regularizeEnable)
-    {
-        if (ps.pathLength >= P.regularizeAfter) ps.flags |= kFlagRegularize;
-        if (ps.flags & kFlagRegularize)
-        {
-            s.roughness = regularizeR(s.roughness, true);
-            s.sheenRoughness = regularizeR(s.sheenRoughness, false);
-            s.clearCoatRoughness = regularizeR(s.clearCoatRoughness, true);
-        }
-    }
-    hs.albedoRGB = rgb.albedo;
-    // convertSurfaceDefinitionFromRGB (hitShadersCommon.hlsl:51-91)
-    s.specular = rgbOrCurve(S, sp, rgb.specular, M.specularSpectrum);
-    s.albedo = rgbOrCurve(S, sp, rgb.albedo, M.albedoSpectrum);
-    s.absorption = isZero3(rgb.absorption) ? splat4(0.0f) : fromRGBUnboundedNoIllum(S, sp, rgb.absorption);
-    s.emissive = emissionSpectrum(S, sp, rgb.emissive, M.emissionSpectrum);
-    s.sheenColor = s.sheenAmount > 0.0f ? fromRGB(S, sp, rgb.sheenColor) : splat4(0.0f);
-}
-
-// sampleLight for mesh lights (lightSampling.hlsl:122-188), position part only
-struct LightPoint
-{
-    float4 radiance;
-    float3 pos, n;
-    float pdfPos, focus;
-    uint32_t instance, prim;
-    bool twoSided;
-};
-YG_DEV void sampleMeshLight(const SceneView& S, const Spectral& sp, uint32_t li, float3 r, LightPoint& out)
-{
-    GpuLight L = S.lights[li];
-    const GpuInstance& I = S.instances[L.instance];
-    uint32_t primCount = I.primCount;
-    uint32_t prim = (uint32_t)fminf((float)primCount * r.z, (float)(primCount - 1u));
-    float bx = r.x, by = r.y;
-    if (bx + by > 1.0f)
-    {
-        bx = 1.0f - bx;
-        by = 1.0f - by;
-    }
-    float b0 = 1.0f - bx - by;
-    TriGeom g = fetchTri(S, I, prim);
-    float3 p1 = xformPoint(I.o2w, g.p1), p2 = xformPoint(I.o2w, g.p2), p3 = xformPoint(I.o2w, g.p3);
-    float3 gn = cross(p2 - p1, p3 - p1);
-    float len = length(gn);
-    gn = gn / len;
-    float area = len * 0.5f;
-    out.pos = p1 * b0 + p2 * bx + p3 * by;
-    out.n = gn;
-    const GpuMaterial& M = S.materials[I.material];
-    float4 e = M.emissive_roughness;
-    out.radiance = emissionSpectrum(S, sp, mk3(e.x, e.y, e.z), M.emissionSpectrum);
-    out.pdfPos = 1.0f / ((float)primCount * area);
-    out.focus = M.emissionFocus;
-    out.instance = L.instance;
-    out.prim = prim;
-    out.twoSided = (M.mask & 1u) != 0;
-}
-
-YG_DEV uint32_t sampleLightIndex(const SceneView& S, float u)
-{
-    float scaled = u * (float)S.nLights;
-    uint32_t index = min((uint32_t)scaled, S.nLights - 1u);
-    GpuLight e = S.lights[index];
-    return (scaled - (float)index) < e.aliasThreshold ? index : e.aliasIndex;
-}
-
-// calculateExplicitLightConnectionPDF (rayHitDefault.hlsl:137-166)
-YG_DEV float explicitLightPdf(const SceneView& S, float3 fromTo, uint32_t inst, uint32_t prim)
-{
-    const GpuInstance& I = S.instances[inst];
-    TriGeom g = fetchTri(S, I, prim);
-    float3 p1 = xformPoint(I.o2w, g.p1), p2 = xformPoint(I.o2w, g.p2), p3 = xformPoint(I.o2w, g.p3);
-    float3 gn = cross(p2 - p1, p3 - p1);
-    float len = length(gn);
-    gn = gn / len;
-    float area = len * 0.5f;
-    float posPdf = 1.0f / ((float)I.primCount * area);
-    return posPdf * I.lightPdf * areaToSolidAngle(fromTo, gn);
-}
-
-struct TraceStats
-{
-    uint32_t rays;
-    TraversalCount tc;
-};
-
-// connectToExplicitLight (rayHitDefault.hlsl:204-257) for a surface vertex
-template <bool COUNT>
-YG_DEV void connectToLight(const SceneView& S, const Luts& Lt, const Spectral& sp, const Surface& s, const SurfaceCtx& c,
-                           float3 woOS, float3 posWS, float3 normalWS, const float4* w2o, PathState& ps, RandomSampler& rs,
-                           TraceStats& st)
-{
-    float4 r = rs.r4();
-    uint32_t li = sampleLightIndex(S, r.w);
-    float pick = S.lights[li].selectionPdf;
-    LightPoint lp;
-    sampleMeshLight(S, sp, li, mk3(r.x, r.y, r.z), lp);
-    float3 toLight = lp.pos - posWS;
-    float len = length(toLight);
-    float cosEmit = -dot(lp.n, toLight / len);
-    float4 emission = lp.radiance * evaluateEmissionProfile(cosEmit, lp.focus);
-    float pdf = pick * lp.pdfPos * areaToSolidAngle(toLight, lp.n);
-    float3 toLightWS = toLight / len;
-    if (!lp.twoSided && dot(toLight, lp.n) >= 0.0f)
-    {
-        emission = splat4(0.0f);
-        pdf = 0.0f;
-    }
-    if (allEqual4(emission, 0.0f) || !(pdf > 0.0f)) return;
-    float3 toLightOS = normalize(xformVector(w2o, toLightWS));
-    Eval ev = evaluateSurface(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
-    float4 w = ev.weight;
-    if ((ev.transmission & kTransDispersed) != 0 && !(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(w);
-    if (allEqual4(w, 0.0f)) return;
-    float3 start = spawnRayOrigin(posWS, normalWS, toLightWS);
-    Hit h;
-    st.rays++;
-    bool any = traceClosest<COUNT>(S, start, toLightWS, kRayMinT, len + kRayMinT, h, &st.tc);
-    bool visible = any && h.instance == lp.instance && h.prim == lp.prim;
-    float wMIS = weightMIS(pdf, ev.pdf);
-    if (visible)
-    {
-        w = (w / pdf) * wMIS;
-        ps.total = ps.total + ps.throughput * w * emission;
+        atomicAdd(ctr, n);
+        atomicAdd(ctr + 1, t);
     }
 }
 
+YG_DEV void pixelOf(const LaunchParams& P, uint64_t idx, uint32_t& sl, uint32_t& cx, uint32_t& cy)
+{
+    const uint64_t npix = (uint64_t)P.cropW * P.cropH;
+    sl = (uint32_t)(idx / npix);
+    uint32_t pl = (uint32_t)(idx - (uint64_t)sl * npix);
+    cx = P.cropX + pl % P.cropW;
+    cy = P.cropY + pl / P.cropW;
+}
+
+YG_DEV Luts lutsOf(const SceneView& S)
+{
+    return Luts{S.lutSS, S.lutSSAvg, S.lutSSMS, S.lutSSMSAvg, S.lutTransDenser, S.lutTransLighter,
+                S.lutTransAvgDenser, S.lutTransAvgLighter, S.lutSheen};
+}
+
+YG_DEV void writeSample(const SceneView& S, const LaunchParams& P, uint64_t idx, const Spectral& sp, float4 total,
+                        const FirstHit& fh)
+{
+    float3 X = toXYZ(S, sp, total);
+    P.sampleXYZ[idx] = mk4(X.x, X.y, X.z, 1.0f);
+    if (P.dump)
+    {
+        float* d = P.dump + idx * 8;
+        d[0] = sp.hero;
+        d[1] = total.x; d[2] = total.y; d[3] = total.z; d[4] = total.w;
+        d[5] = X.x; d[6] = X.y; d[7] = X.z;
+    }
+    if (P.featAlbedo)
+    {
+        P.featAlbedo[idx] = mk4(fh.albedo.x, fh.albedo.y, fh.albedo.z, 0.0f);
+        P.featNormalDepth[idx] = mk4(fh.normal.x, fh.normal.y, fh.normal.z, fh.depth);
+    }
+}
+
+// ------------------------------------------------------------------ megakernel
 template <bool NEE, bool COUNT>
 __global__ void __launch_bounds__(128) pathKernel(const SceneView S, const LaunchParams P)
 {
-    Luts Lt{S.lutSS, S.lutSSAvg, S.lutSSMS, S.lutSSMSAvg, S.lutTransDenser, S.lutTransLighter,
-            S.lutTransAvgDenser, S.lutTransAvgLighter, S.lutSheen};
-    const uint64_t npix = (uint64_t)P.cropW * P.cropH;
-    TraceStats st{0, {0, 0}};
+    Luts Lt = lutsOf(S);
+    TraversalCount tc{0, 0};
+    uint32_t rays = 0;
     for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < P.nSamples;
          idx += (uint64_t)gridDim.x * blockDim.x)
     {
-        uint32_t sl = (uint32_t)(idx / npix);
-        uint32_t pl = (uint32_t)(idx - (uint64_t)sl * npix);
-        uint32_t cx = P.cropX + pl % P.cropW;
-        uint32_t cy = P.cropY + pl / P.cropW;
-        uint32_t rayIndex = cy * P.width + cx;
-        uint32_t seed = rayIndex ^ (P.seed * 0x9E3779B9u);
+        uint32_t sl, cx, cy;
+        pixelOf(P, idx, sl, cx, cy);
+        uint32_t seed = (cy * P.width + cx) ^ (P.seed * 0x9E3779B9u);
         RandomSampler rs{S.sobol + (size_t)sl * kSobolDims, 2u, seed};
         Spectral sp;
-        sp.hero = S.lambdaMin + rs.r1() * (S.lambdaMax - S.lambdaMin);
-        sp.lambdas = getSpectralSampleLambdas(sp.hero, S.lambdaMin, S.lambdaMax);
-
-        // generateCameraRay (raytraceCommonResources.hlsl:113-137)
-        float invW = 1.0f / (float)P.width, invH = 1.0f / (float)P.height;
-        float2 uv = make_float2((float)cx * invW + 0.5f * invW, (float)cy * invH + 0.5f * invH);
-        float2 texel = make_float2(sampleDim(rs.point, 0, seed), sampleDim(rs.point, 1, seed));
-        float2 lensR = rs.r2();
-        float2 to = make_float2(0.f, 0.f);
-        if ((P.flags & 2u) == 0) to = make_float2(texel.x - 0.5f, texel.y - 0.5f);
-        to = make_float2(to.x * invW, to.y * invH);
-        float4 pn = mul44(S.cam.uvToView, mk4(uv.x + to.x, uv.y + to.y, 0.0f, 1.0f));
-        pn = pn / pn.w;
-        float3 pin = mk3(pn.x, pn.y, pn.z);
-        float3 focusP = pin * safeDiv(S.cam.focusDistance, fabsf(pin.z));
-        float2 disk = sampleConcentricDisk(lensR);
-        float3 lensP = mk3(disk.x * S.cam.apertureRadius, disk.y * S.cam.apertureRadius, 0.0f);
-        float4 ow = mul44(S.cam.viewToWorld, mk4(lensP.x, lensP.y, lensP.z, 1.0f));
-        float4 dw = mul44(S.cam.viewToWorld, mk4(focusP.x - lensP.x, focusP.y - lensP.y, focusP.z - lensP.z, 0.0f));
-
         PathState ps;
-        ps.throughput = splat4(1.0f);
-        ps.total = splat4(0.0f);
-        ps.origin = mk3(ow.x, ow.y, ow.z);
-        ps.dir = normalize(mk3(dw.x, dw.y, dw.z));
-        ps.pdfThisRay = 0.0f;
-        ps.flags = 0;
-        ps.pathLength = 0;
-        ps.nVol = 0;
+        beginPath(S, P, cx, cy, rs, sp, ps);
+        FirstHit fh{mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), 0.0f};
         bool alive = true;
-        float3 featAlbedo = mk3(0.f, 0.f, 0.f), featNormal = mk3(0.f, 0.f, 0.f);
-        float featDepth = 0.0f;
-
-        for (uint32_t bounce = 0; bounce < P.maxDepth; ++bounce)
+        for (uint32_t bounce = 0; bounce < P.maxDepth && alive; ++bounce)
         {
-            if (!alive) break;
             Hit hit;
-            st.rays++;
-            bool found = traceClosest<COUNT>(S, ps.origin, ps.dir, kRayMinT, __int_as_float(0x7f800000), hit, &st.tc);
-            if (!found)
+            rays++;
+            bool found = traceClosest<COUNT>(S, ps.origin, ps.dir, kRayMinT, __int_as_float(0x7f800000), hit, &tc);
+            ShadowRequest sr;
+            alive = shadeSegment<NEE>(S, P, Lt, sp, found, hit, ps, rs, sr, P.featAlbedo ? &fh : nullptr);
+            if (sr.valid)
             {
-                // rayMissEnvironment: |dir| * Env.IntensityScale, as an unbounded RGB emitter
-                float3 col = mk3(fabsf(ps.dir.x) * P.envScale, fabsf(ps.dir.y) * P.envScale, fabsf(ps.dir.z) * P.envScale);
-                float4 Le = isZero3(col) ? splat4(0.0f) : fromRGBUnbounded(S, sp, col);
-                ps.total = ps.total + ps.throughput * Le;
-                alive = false;
-            }
-            else
-            {
-                const GpuInstance& I = S.instances[hit.instance];
-                HitSurface hs;
-                setupSurface(S, P, sp, hit, I, ps.dir, ps, hs);
-                Surface& s = hs.s;
-                float3 hitPos = ps.origin + ps.dir * hit.t;
-                if (ps.pathLength == 0 && P.featAlbedo)
-                {
-                    featAlbedo = hs.albedoRGB;
-                    featNormal = normalize(xformVectorT(I.w2o, s.baseLayerNormal));
-                    float4 vp = mul44(S.cam.worldToView, mk4(hitPos.x, hitPos.y, hitPos.z, 1.0f));
-                    featDepth = vp.z * S.cam.forwardZSign;
-                }
-                // handleRayStartInsideMedium (hitShadersCommon.hlsl:212-222)
-                if (dot(hs.rayDirOS, s.geometryNormal) > 0.0f && ps.nVol == 0 && !isTwoSided(s.flags))
-                    enteredVolume(ps, s.dielectricIOR, s.absorption, hs.material);
-                // absorption along the segment
-                float4 ab = ps.nVol != 0 ? ps.volAbs[ps.nVol - 1] : splat4(0.0f);
-                if (!allEqual4(ab, 0.0f))
-                {
-                    float4 tr = mk4(ygm_expf(-ab.x * hit.t), ygm_expf(-ab.y * hit.t), ygm_expf(-ab.z * hit.t), ygm_expf(-ab.w * hit.t));
-                    ps.throughput = ps.throughput * tr;
-                }
-                if (!allEqual4(s.emissive, 0.0f))
-                {
-                    float wMIS = 1.0f;
-                    if (NEE && S.nLights > 0 && ps.pdfThisRay > 0.0f && !(ps.flags & kFlagDelta))
-                    {
-                        float lightPdf = explicitLightPdf(S, hitPos - ps.origin, hit.instance, hit.prim);
-                        wMIS = weightMIS(ps.pdfThisRay, lightPdf);
-                    }
-                    float side = dot(s.geometryNormal, -hs.rayDirOS) < 0.0f ? 0.0f : 1.0f;
-                    float profile = 1.0f;
-                    if (s.emissionFocus > 0.0f)
-                    {
-                        float3 gnWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
-                        profile = evaluateEmissionProfile(dot(gnWS, -normalize(ps.dir)), s.emissionFocus);
-                    }
-                    ps.total = ps.total + ps.throughput * s.emissive * wMIS * side * profile;
-                    alive = false;
-                }
-                else
-                {
-                    // evaluateSurfaceAndGenerateNextSampleDirection (rayHitDefault.hlsl:316-435)
-                    float4 rB = rs.r4();
-                    float3 wo = -hs.rayDirOS;
-                    SurfaceCtx c;
-                    makeSurfaceCtx(s, currentIOR(ps), previousIOR(ps), wo, hit.front, c);
-                    float3 normalWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
-                    if (NEE && S.nLights > 0 && !isDeltaDistribution(c.a2, s))
-                        connectToLight<COUNT>(S, Lt, sp, s, c, wo, hitPos, normalWS, I.w2o, ps, rs, st);
-                    // sampleScatteringEvent (scatteringSample.hlsl:30-65)
-                    int layer = selectMaterialLayer(rB.x, c.probs);
-                    float3 wi = mk3(0.f, 0.f, 0.f);
-                    bool isDiffuse = false, isDelta = false;
-                    if (layer != LAYER_SSS && layer < LAYER_COUNT)
-                        wi = sampleLayerDirection(Lt, s, c, layer, rB.y, make_float2(rB.z, rB.w), sp.hero, isDiffuse, isDelta);
-                    Eval ev;
-                    ev.weight = splat4(0.0f);
-                    ev.pdf = 0.0f;
-                    ev.transmission = 0;
-                    if (!isZero3(wi))
-                    {
-                        ev = evaluateSurface(Lt, s, c, wo, wi, isDelta ? kEvalTreatAsDelta : kEvalNone, sp);
-                        if (isDiffuse) ps.flags |= kFlagRegularize;
-                    }
-                    ps.pdfThisRay = ev.pdf;
-                    if (isDelta) ps.flags |= kFlagDelta;
-                    else ps.flags &= ~kFlagDelta;
-                    if (ev.pdf > 0.0f)
-                    {
-                        if (ev.transmission != 0)
-                        {
-                            if ((ev.transmission & kTransDispersed) != 0)
-                            {
-                                if (!(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(ev.weight);
-                                ps.flags |= kFlagSecondaryTerminated;
-                            }
-                            bool entered = (ev.transmission & kTransEntered) != 0;
-                            bool exited = (ev.transmission & kTransExited) != 0;
-                            if (entered != exited)
-                            {
-                                if (exited) exitedVolume(ps, hs.material);
-                                else enteredVolume(ps, s.dielectricIOR, s.absorption, hs.material);
-                            }
-                        }
-                        ev.weight = ev.weight / ev.pdf;
-                    }
-                    ps.throughput = ps.throughput * ev.weight;
-                    if (isZero3(wi) || ps.pdfThisRay == 0.0f)
-                    {
-                        alive = false;
-                    }
-                    else
-                    {
-                        float3 nW = normalize(xformVector(I.o2w, s.geometryNormal));
-                        float3 dW = normalize(xformVector(I.o2w, wi));
-                        ps.origin = spawnRayOrigin(hitPos, nW, dW);
-                        ps.dir = dW;
-                    }
-                }
-            }
-            ps.pathLength += 1;
-            // Russian roulette after every traced segment (rayGenPrimaryRays.hlsl:91-101)
-            if (russianRoulette(ps.throughput, rs.r1()))
-            {
-                alive = false;
-                break;
+                Hit h;
+                rays++;
+                bool any = traceClosest<COUNT>(S, sr.origin, sr.dir, kRayMinT, sr.tmax, h, &tc);
+                if (shadowVisible(any, h, sr.instance, sr.prim)) ps.total = ps.total + sr.contrib;
             }
         }
-        float3 X = toXYZ(S, sp, ps.total);
-        P.sampleXYZ[idx] = mk4(X.x, X.y, X.z, 1.0f);
-        if (P.dump)
-        {
-            float* d = P.dump + idx * 8;
-            d[0] = sp.hero;
-            d[1] = ps.total.x; d[2] = ps.total.y; d[3] = ps.total.z; d[4] = ps.total.w;
-            d[5] = X.x; d[6] = X.y; d[7] = X.z;
-        }
+        writeSample(S, P, idx, sp, ps.total, fh);
+    }
+    countRays(P.rayCounter, rays);
+    if (COUNT) countTraversal(P.traversalCounter, tc);
+}
+
+// ------------------------------------------------------------------ wavefront
+// Path state of one wave, structure of arrays (index = slot = sample index - wave base).
+struct WaveState
+{
+    float4* thr;      // throughput
+    float4* tot;      // accumulated radiance
+    float4* orgPdf;   // ray origin, pdfThisRay
+    float4* dirHero;  // ray direction, hero wavelength
+    uint4* misc;      // flags | pathLength << 8 | nVol << 16, dimension cursor, scramble seed, Sobol row
+    float4* volIOR;   // volume stack (RAY_MAX_VOLUMES_ENTERED = 4)
+    uint4* volMat;
+    float4* volAbs;   // [4][capacity]
+    float4* fhAlb;    // first-hit features of the wave
+    float4* fhNrm;
+    uint32_t capacity;
+};
+struct RayQueue
+{
+    float4* o; // origin, slot
+    float4* d; // direction
+    uint32_t* count;
+};
+struct HitQueue
+{
+    float4* a;    // t, b1, b2, instance
+    uint32_t* b;  // prim | front << 31, or 0xffffffff for a miss
+};
+struct ShadowQueue
+{
+    float4* o;        // origin, slot
+    float4* d;        // direction, tmax
+    uint2* target;    // light instance, primitive
+    float4* contrib;
+    uint32_t* count;
+};
+
+YG_DEV void loadPath(const WaveState& W, uint32_t s, PathState& ps, RandomSampler& rs, Spectral& sp, const SceneView& S)
+{
+    float4 t = W.thr[s], a = W.tot[s], o = W.orgPdf[s], d = W.dirHero[s];
+    uint4 m = W.misc[s];
+    ps.throughput = t;
+    ps.total = a;
+    ps.origin = mk3(o.x, o.y, o.z);
+    ps.pdfThisRay = o.w;
+    ps.dir = mk3(d.x, d.y, d.z);
+    ps.flags = m.x & 0xffu;
+    ps.pathLength = (m.x >> 8) & 0xffu;
+    ps.nVol = (m.x >> 16) & 0xffu;
+    rs.dim = m.y;
+    rs.seed = m.z;
+    rs.point = S.sobol + (size_t)m.w * kSobolDims;
+    spectralOf(S, d.w, sp);
+    if (ps.nVol)
+    {
+        float4 vi = W.volIOR[s];
+        uint4 vm = W.volMat[s];
+        ps.volIOR[0] = vi.x; ps.volIOR[1] = vi.y; ps.volIOR[2] = vi.z; ps.volIOR[3] = vi.w;
+        ps.volMat[0] = vm.x; ps.volMat[1] = vm.y; ps.volMat[2] = vm.z; ps.volMat[3] = vm.w;
+        for (int k = 0; k < kMaxVolumes; ++k) ps.volAbs[k] = W.volAbs[(size_t)k * W.capacity + s];
+    }
+}
+
+YG_DEV void storePath(const WaveState& W, uint32_t s, const PathState& ps, const RandomSampler& rs, float hero,
+                      uint32_t row, bool volumesTouched)
+{
+    W.thr[s] = ps.throughput;
+    W.tot[s] = ps.total;
+    W.orgPdf[s] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, ps.pdfThisRay);
+    W.dirHero[s] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, hero);
+    W.misc[s] = make_uint4(ps.flags | (ps.pathLength << 8) | (ps.nVol << 16), rs.dim, rs.seed, row);
+    if (volumesTouched)
+    {
+        W.volIOR[s] = mk4(ps.volIOR[0], ps.volIOR[1], ps.volIOR[2], ps.volIOR[3]);
+        W.volMat[s] = make_uint4(ps.volMat[0], ps.volMat[1], ps.volMat[2], ps.volMat[3]);
+        for (int k = 0; k < kMaxVolumes; ++k) W.volAbs[(size_t)k * W.capacity + s] = ps.volAbs[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) wfGenerate(const SceneView S, const LaunchParams P, WaveState W, RayQueue Q,
+                                                  uint64_t base, uint32_t n)
+{
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        uint64_t idx = base + s;
+        uint32_t sl, cx, cy;
+        pixelOf(P, idx, sl, cx, cy);
+        uint32_t seed = (cy * P.width + cx) ^ (P.seed * 0x9E3779B9u);
+        RandomSampler rs{S.sobol + (size_t)sl * kSobolDims, 2u, seed};
+        Spectral sp;
+        PathState ps;
+        beginPath(S, P, cx, cy, rs, sp, ps);
+        storePath(W, s, ps, rs, sp.hero, sl, false);
         if (P.featAlbedo)
         {
-            P.featAlbedo[idx] = mk4(featAlbedo.x, featAlbedo.y, featAlbedo.z, 0.0f);
-            P.featNormalDepth[idx] = mk4(featNormal.x, featNormal.y, featNormal.z, featDepth);
+            W.fhAlb[s] = splat4(0.0f);
+            W.fhNrm[s] = splat4(0.0f);
+        }
+        Q.o[s] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, __uint_as_float(s));
+        Q.d[s] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, 0.0f);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, HitQueue H, unsigned long long* rayCtr,
+                                               unsigned long long* travCtr)
+{
+    const uint32_t n = *Q.count;
+    TraversalCount tc{0, 0};
+    uint32_t rays = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        float4 o = Q.o[i], d = Q.d[i];
+        Hit h;
+        bool found = traceClosest<COUNT>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000),
+                                         h, &tc);
+        rays++;
+        H.a[i] = mk4(h.t, h.b1, h.b2, __uint_as_float(h.instance));
+        H.b[i] = found ? (h.prim | (h.front ? 0x80000000u : 0u)) : 0xffffffffu;
+    }
+    countRays(rayCtr, rays);
+    if (COUNT) countTraversal(travCtr, tc);
+}
+
+template <bool NEE>
+__global__ void __launch_bounds__(128) wfShade(const SceneView S, const LaunchParams P, WaveState W, RayQueue Qin,
+                                               HitQueue H, RayQueue Qout, ShadowQueue SQ)
+{
+    Luts Lt = lutsOf(S);
+    const uint32_t n = *Qin.count;
+    // uniform trip count per warp so that the warp-wide appends see every lane
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        uint32_t i = first + r * stride;
+        bool active = i < n;
+        bool alive = false;
+        ShadowRequest sr;
+        sr.valid = false;
+        uint32_t slot = 0;
+        PathState ps;
+        RandomSampler rs;
+        Spectral sp;
+        if (active)
+        {
+            slot = __float_as_uint(Qin.o[i].w);
+            loadPath(W, slot, ps, rs, sp, S);
+            uint32_t nVol0 = ps.nVol;
+            float4 ha = H.a[i];
+            uint32_t hb = H.b[i];
+            bool found = hb != 0xffffffffu;
+            Hit hit;
+            hit.t = ha.x;
+            hit.b1 = ha.y;
+            hit.b2 = ha.z;
+            hit.instance = __float_as_uint(ha.w);
+            hit.prim = hb & 0x7fffffffu;
+            hit.front = (hb & 0x80000000u) != 0;
+            FirstHit fh{mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), 0.0f};
+            bool first = ps.pathLength == 0;
+            alive = shadeSegment<NEE>(S, P, Lt, sp, found, hit, ps, rs, sr, P.featAlbedo ? &fh : nullptr);
+            if (first && P.featAlbedo)
+            {
+                W.fhAlb[slot] = mk4(fh.albedo.x, fh.albedo.y, fh.albedo.z, 0.0f);
+                W.fhNrm[slot] = mk4(fh.normal.x, fh.normal.y, fh.normal.z, fh.depth);
+            }
+            alive = alive && ps.pathLength < P.maxDepth;
+            storePath(W, slot, ps, rs, sp.hero, (uint32_t)(rs.point - S.sobol) / kSobolDims, ps.nVol != 0 || nVol0 != 0);
+        }
+        uint32_t k = warpAppend(Qout.count, alive);
+        if (alive)
+        {
+            Qout.o[k] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, __uint_as_float(slot));
+            Qout.d[k] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, 0.0f);
+        }
+        if (NEE)
+        {
+            uint32_t j = warpAppend(SQ.count, sr.valid);
+            if (sr.valid)
+            {
+                SQ.o[j] = mk4(sr.origin.x, sr.origin.y, sr.origin.z, __uint_as_float(slot));
+                SQ.d[j] = mk4(sr.dir.x, sr.dir.y, sr.dir.z, sr.tmax);
+                SQ.target[j] = make_uint2(sr.instance, sr.prim);
+                SQ.contrib[j] = sr.contrib;
+            }
         }
     }
-    if (P.rayCounter)
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) wfShadow(const SceneView S, WaveState W, ShadowQueue SQ, unsigned long long* rayCtr,
+                                                unsigned long long* travCtr)
+{
+    const uint32_t n = *SQ.count;
+    TraversalCount tc{0, 0};
+    uint32_t rays = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
-        // one atomic per warp
-        uint32_t r = st.rays;
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(P.rayCounter, (unsigned long long)r);
+        float4 o = SQ.o[i], d = SQ.d[i];
+        uint2 tg = SQ.target[i];
+        Hit h;
+        bool any = traceClosest<COUNT>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, h, &tc);
+        rays++;
+        if (shadowVisible(any, h, tg.x, tg.y))
+        {
+            uint32_t s = __float_as_uint(o.w);
+            W.tot[s] = W.tot[s] + SQ.contrib[i];
+        }
     }
-    if (COUNT && P.traversalCounter)
+    countRays(rayCtr, rays);
+    if (COUNT) countTraversal(travCtr, tc);
+}
+
+__global__ void __launch_bounds__(256) wfFinalize(const SceneView S, const LaunchParams P, WaveState W, uint64_t base,
+                                                  uint32_t n)
+{
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
-        unsigned long long n = st.tc.nodes, t = st.tc.tris;
-        for (int o = 16; o > 0; o >>= 1)
+        Spectral sp;
+        spectralOf(S, W.dirHero[s].w, sp);
+        FirstHit fh{mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), 0.0f};
+        if (P.featAlbedo)
         {
-            n += __shfl_down_sync(0xffffffffu, n, o);
-            t += __shfl_down_sync(0xffffffffu, t, o);
+            float4 a = W.fhAlb[s], nd = W.fhNrm[s];
+            fh.albedo = mk3(a.x, a.y, a.z);
+            fh.normal = mk3(nd.x, nd.y, nd.z);
+            fh.depth = nd.w;
         }
-        if ((threadIdx.x & 31) == 0)
-        {
-            atomicAdd(P.traversalCounter, n);
-            atomicAdd(P.traversalCounter + 1, t);
-        }
+        writeSample(S, P, base + s, sp, W.tot[s], fh);
     }
 }
 
@@ -660,6 +451,77 @@ int launchPathKernel(const SceneView& S, const LaunchParams& P, int smCount, cud
         else pathKernel<false, false><<<blocks, threads, 0, stream>>>(S, P);
     }
     return 1;
+}
+
+size_t wavefrontBytesPerSlot()
+{
+    // state (5 x 16 + 16 + 16 + 64) + features (32) + 2 ray queues (64) + hits (20) + shadow queue (56)
+    return 5 * 16 + 16 + 16 + 64 + 32 + 64 + 20 + 56;
+}
+
+int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint32_t capacity, int smCount,
+                    cudaStream_t stream)
+{
+    char* p = static_cast<char*>(arena);
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    size_t C = capacity;
+    WaveState W;
+    W.capacity = capacity;
+    W.thr = (float4*)take(C * 16);
+    W.tot = (float4*)take(C * 16);
+    W.orgPdf = (float4*)take(C * 16);
+    W.dirHero = (float4*)take(C * 16);
+    W.misc = (uint4*)take(C * 16);
+    W.volIOR = (float4*)take(C * 16);
+    W.volMat = (uint4*)take(C * 16);
+    W.volAbs = (float4*)take(C * 64);
+    W.fhAlb = (float4*)take(C * 16);
+    W.fhNrm = (float4*)take(C * 16);
+    uint32_t* counters = (uint32_t*)take(256);
+    RayQueue QA{(float4*)take(C * 16), (float4*)take(C * 16), counters + 0};
+    RayQueue QB{(float4*)take(C * 16), (float4*)take(C * 16), counters + 1};
+    HitQueue H{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
+    ShadowQueue SQ{(float4*)take(C * 16), (float4*)take(C * 16), (uint2*)take(C * 8), (float4*)take(C * 16),
+                   counters + 2};
+    bool count = P.traversalCounter != nullptr;
+    int launches = 0;
+    const int traceBlocks = smCount * 16, shadeBlocks = smCount * 8;
+    for (uint64_t base = 0; base < P.nSamples; base += C)
+    {
+        uint32_t n = (uint32_t)((P.nSamples - base) < C ? (P.nSamples - base) : C);
+        int gblocks = (int)((n + 255) / 256);
+        if (gblocks > smCount * 8) gblocks = smCount * 8;
+        wfGenerate<<<gblocks, 256, 0, stream>>>(S, P, W, QA, base, n);
+        ++launches;
+        RayQueue* cur = &QA;
+        RayQueue* nxt = &QB;
+        for (uint32_t b = 0; b < P.maxDepth; ++b)
+        {
+            if (count) wfTrace<true><<<traceBlocks, 128, 0, stream>>>(S, *cur, H, P.rayCounter, P.traversalCounter);
+            else wfTrace<false><<<traceBlocks, 128, 0, stream>>>(S, *cur, H, P.rayCounter, nullptr);
+            cudaMemsetAsync(nxt->count, 0, 4, stream);
+            cudaMemsetAsync(SQ.count, 0, 4, stream);
+            if (P.integrator == 1) wfShade<true><<<shadeBlocks, 128, 0, stream>>>(S, P, W, *cur, H, *nxt, SQ);
+            else wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, *cur, H, *nxt, SQ);
+            launches += 2;
+            if (P.integrator == 1)
+            {
+                if (count) wfShadow<true><<<traceBlocks, 128, 0, stream>>>(S, W, SQ, P.rayCounter, P.traversalCounter);
+                else wfShadow<false><<<traceBlocks, 128, 0, stream>>>(S, W, SQ, P.rayCounter, nullptr);
+                ++launches;
+            }
+            RayQueue* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+        wfFinalize<<<gblocks, 256, 0, stream>>>(S, P, W, base, n);
+        ++launches;
+    }
+    return launches;
 }
 
 int launchFilm(float4* sum, float4* comp, const float4* samples, uint32_t width, uint32_t cx, uint32_t cy, uint32_t cw,

@@ -5,6 +5,11 @@
 namespace yg
 {
 int launchPathKernel(const SceneView& S, const LaunchParams& P, int smCount, cudaStream_t stream);
+// Wavefront integrator over P.nSamples samples in waves of `capacity` paths; `arena`
+// holds capacity * wavefrontBytesPerSlot() bytes plus 64 KB. Returns the launch count.
+size_t wavefrontBytesPerSlot();
+int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint32_t capacity, int smCount,
+                    cudaStream_t stream);
 int launchFilm(float4* sum, float4* comp, const float4* samples, uint32_t width, uint32_t cx, uint32_t cy, uint32_t cw,
                uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
 int launchFeatures(float4* accA, float4* accN, const float4* fa, const float4* fn, uint32_t width, uint32_t cx, uint32_t cy,

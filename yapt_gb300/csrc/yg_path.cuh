@@ -1,0 +1,541 @@
+// Per-vertex path logic shared by the megakernel and the wavefront kernels: camera
+// ray generation, surface setup, emitter hits with MIS, NEE light sampling (split
+// into a shadow-ray request and its resolution) and BSDF sampling with Russian
+// roulette. Restates, for CUDA, YAPT's DXR ray generation / closest-hit / miss shaders:
+//   rayGenPrimaryRays.hlsl:10-145   (camera ray, bounce loop, Russian roulette, ToXYZ)
+//   rayHitDefault.hlsl:36-585       (surface setup, emitter MIS, NEE, BSDF sampling)
+//   rayMissEnvironment.hlsl:13-31   (environment)
+//   lightSampling.hlsl:31-188, 360-370 (alias light pick, area light sampling)
+//   hitShadersCommon.hlsl:138-222   (absorption, spawn offset, medium start)
+// Each path's arithmetic is the same sequence whichever kernel runs it, so the
+// wavefront and the megakernel give bit-identical samples.
+#pragma once
+#include "yg_shading.cuh"
+#include "yg_trace.cuh"
+
+namespace yg
+{
+
+constexpr uint32_t kFlagSecondaryTerminated = 1u << 0; // RAYSTATE_FLAGS_* (RayState.hlsl:4-6)
+constexpr uint32_t kFlagRegularize = 1u << 1;
+constexpr uint32_t kFlagDelta = 1u << 2;
+
+struct PathState
+{
+    float4 throughput;
+    float4 total;
+    float3 origin;
+    float3 dir;
+    float pdfThisRay;
+    uint32_t flags;
+    uint32_t pathLength;
+    uint32_t nVol;
+    float volIOR[kMaxVolumes];
+    float4 volAbs[kMaxVolumes];
+    uint32_t volMat[kMaxVolumes];
+};
+
+// Payload volume stack (payload.hlsl:15-103)
+YG_DEV float currentIOR(const PathState& p) { return p.nVol != 0 ? p.volIOR[p.nVol - 1] : 1.0f; }
+YG_DEV float previousIOR(const PathState& p) { return p.nVol > 1 ? p.volIOR[p.nVol - 2] : 1.0f; }
+YG_DEV void enteredVolume(PathState& p, float ior, float4 absorption, uint32_t mat)
+{
+    p.nVol = min(p.nVol + 1, (uint32_t)kMaxVolumes);
+    p.volIOR[p.nVol - 1] = ior;
+    p.volAbs[p.nVol - 1] = absorption;
+    p.volMat[p.nVol - 1] = mat;
+}
+YG_DEV void exitedVolume(PathState& p, uint32_t mat)
+{
+    if (p.nVol == 0) return;
+    int index = -1;
+    for (int i = (int)p.nVol - 1; i >= 0; --i)
+    {
+        if (p.volMat[i] == mat) { index = i; break; }
+    }
+    if (index < 0) index = (int)p.nVol - 1;
+    for (uint32_t i = (uint32_t)index; i + 1 < p.nVol; ++i)
+    {
+        p.volIOR[i] = p.volIOR[i + 1];
+        p.volAbs[i] = p.volAbs[i + 1];
+        p.volMat[i] = p.volMat[i + 1];
+    }
+    --p.nVol;
+}
+
+// spawnRayOrigin, Ray Tracing Gems ch. 6 (hitShadersCommon.hlsl:147-160)
+YG_DEV float spawnComp(float p, float n, int oi)
+{
+    int so = p < 0.0f ? -oi : oi;
+    float off = __int_as_float(__float_as_int(p) + so);
+    return fabsf(p) < (1.0f / 32.0f) ? p + (1.0f / 65536.0f) * n : off;
+}
+YG_DEV float3 spawnRayOrigin(float3 p, float3 gn, float3 dir)
+{
+    float3 n = dot(dir, gn) < 0.0f ? -gn : gn;
+    int ox = (int)(256.0f * n.x), oy = (int)(256.0f * n.y), oz = (int)(256.0f * n.z);
+    return mk3(spawnComp(p.x, n.x, ox), spawnComp(p.y, n.y, oy), spawnComp(p.z, n.z, oz));
+}
+
+YG_DEV float weightMIS(float a, float b)
+{
+    float a2 = a * a, b2 = b * b;
+    return a2 / (a2 + b2);
+}
+YG_DEV float areaToSolidAngle(float3 v, float3 n)
+{
+    float invD2 = 1.0f / dot(v, v);
+    float absDot = fabsf(dot(n, v * sqrtf(invD2)));
+    return 1.0f / (absDot * invD2);
+}
+
+struct TriGeom
+{
+    float3 p1, p2, p3;
+    uint32_t i1, i2, i3;
+};
+YG_DEV TriGeom fetchTri(const SceneView& S, const GpuInstance& I, uint32_t prim)
+{
+    TriGeom g;
+    const uint32_t* ix = S.indices + I.firstIndex + 3u * prim;
+    g.i1 = __ldg(ix) + I.vertexBase;
+    g.i2 = __ldg(ix + 1) + I.vertexBase;
+    g.i3 = __ldg(ix + 2) + I.vertexBase;
+    const float* P = S.positions;
+    g.p1 = mk3(__ldg(P + 3 * g.i1), __ldg(P + 3 * g.i1 + 1), __ldg(P + 3 * g.i1 + 2));
+    g.p2 = mk3(__ldg(P + 3 * g.i2), __ldg(P + 3 * g.i2 + 1), __ldg(P + 3 * g.i2 + 2));
+    g.p3 = mk3(__ldg(P + 3 * g.i3), __ldg(P + 3 * g.i3 + 1), __ldg(P + 3 * g.i3 + 2));
+    return g;
+}
+YG_DEV float3 interp3(const float* A, const TriGeom& g, float b0, float b1, float b2)
+{
+    float3 a = mk3(__ldg(A + 3 * g.i1), __ldg(A + 3 * g.i1 + 1), __ldg(A + 3 * g.i1 + 2));
+    float3 b = mk3(__ldg(A + 3 * g.i2), __ldg(A + 3 * g.i2 + 1), __ldg(A + 3 * g.i2 + 2));
+    float3 c = mk3(__ldg(A + 3 * g.i3), __ldg(A + 3 * g.i3 + 1), __ldg(A + 3 * g.i3 + 2));
+    return a * b0 + b * b1 + c * b2;
+}
+
+// Scalar material parameters before the spectral conversion (SurfaceDefinitionRGB)
+struct SurfaceRGB
+{
+    float3 albedo, specular, absorption, emissive, sheenColor;
+};
+
+YG_DEV float4 rgbOrCurve(const SceneView& S, const Spectral& sp, float3 rgb, int curve)
+{
+    if (curve >= 0) return fromCurve(S, sp, curve);
+    return fromRGB(S, sp, rgb);
+}
+YG_DEV float4 emissionSpectrum(const SceneView& S, const Spectral& sp, float3 rgb, int curve)
+{
+    if (curve >= 0) return fromCurve(S, sp, curve) * fmaxf(fmaxf(rgb.x, rgb.y), rgb.z);
+    if (isZero3(rgb)) return splat4(0.0f);
+    return fromRGBUnbounded(S, sp, rgb);
+}
+
+// regularize (materialsCommon.hlsl:399-418)
+YG_DEV float regularizeR(float lr, bool squared)
+{
+    float r = squared ? lr * lr : lr;
+    if (r < 0.3f)
+    {
+        r = clampf(r * 2.0f, 0.1f, 0.3f);
+        return squared ? sqrtf(r) : r;
+    }
+    return lr;
+}
+
+struct HitSurface
+{
+    Surface s;
+    float3 rayDirOS;
+    uint32_t material;
+    float3 albedoRGB; // first-hit features
+};
+
+// fetch + fetchSurfaceMaterialParameters + two-sided orientation + tangent rotation +
+// regularisation + RGB -> spectral conversion (rayHitDefault.hlsl:470-520)
+YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectral& sp, const Hit& hit, const GpuInstance& I,
+                         float3 rayDirWS, PathState& ps, HitSurface& hs)
+{
+    TriGeom g = fetchTri(S, I, hit.prim);
+    float b0 = 1.0f - hit.b1 - hit.b2;
+    float3 gn = normalize(cross(g.p2 - g.p1, g.p3 - g.p1));
+    float3 nrm = normalize(interp3(S.normals, g, b0, hit.b1, hit.b2));
+    float3 tan = mk3(1.f, 0.f, 0.f);
+    if (I.hasTangents)
+    {
+        float4 t1 = __ldg(S.tangents + g.i1), t2 = __ldg(S.tangents + g.i2), t3 = __ldg(S.tangents + g.i3);
+        float3 a = mk3(t1.x * t1.w, t1.y * t1.w, t1.z * t1.w);
+        float3 b = mk3(t2.x * t2.w, t2.y * t2.w, t2.z * t2.w);
+        float3 c = mk3(t3.x * t3.w, t3.y * t3.w, t3.z * t3.w);
+        tan = normalize(a * b0 + b * hit.b1 + c * hit.b2);
+    }
+    float3 rd = normalize(xformVector(I.w2o, rayDirWS));
+    hs.rayDirOS = rd;
+    hs.material = I.material;
+    const GpuMaterial& M = S.materials[I.material];
+    Surface& s = hs.s;
+    float4 a_t = M.albedo_transparency, s_m = M.specular_metalness, ab_i = M.absorption_ior, e_r = M.emissive_roughness;
+    float4 sc = M.specAmount_ccAmount_ccIOR_ccRough, sh = M.sheenColor_roughness;
+    SurfaceRGB rgb;
+    rgb.albedo = mk3(a_t.x, a_t.y, a_t.z);
+    rgb.specular = mk3(s_m.x, s_m.y, s_m.z);
+    rgb.absorption = mk3(ab_i.x, ab_i.y, ab_i.z);
+    rgb.emissive = mk3(e_r.x, e_r.y, e_r.z);
+    rgb.sheenColor = mk3(sh.x, sh.y, sh.z);
+    s.transparency = a_t.w;
+    s.metalness = s_m.w;
+    s.dielectricIOR = ab_i.w;
+    s.roughness = e_r.w;
+    s.emissionFocus = M.emissionFocus;
+    s.specularAmount = sc.x;
+    s.clearCoatAmount = sc.y;
+    s.clearCoatIOR = sc.z;
+    s.clearCoatRoughness = sc.w;
+    s.cauchyA = M.cauchyA;
+    s.cauchyB = M.cauchyB;
+    s.anisotropy = M.anisotropy;
+    s.anisotropyRotation = M.anisotropyRotation;
+    s.thinFilmNM = M.thinFilmNM;
+    s.flags = M.mask;
+    s.sheenRoughness = fmaxf(sh.w, 0.07f);
+    s.sheenAmount = M.sheenAmount;
+    s.subsurfaceAmount = M.subsurfaceRadius_amount.w;
+    s.coatingLayerNormal = nrm;
+    s.baseLayerNormal = nrm;
+    s.geometryNormal = gn;
+    s.tangent = tan;
+    // handleTwoSidedMaterialOrientation (materialsCommon.hlsl:440-448), wo = -rayDir
+    if (s.transparency == 0.0f && isTwoSided(s.flags))
+    {
+        float3 wo = -rd;
+        if (dot(wo, s.baseLayerNormal) < 0.0f) s.baseLayerNormal = -s.baseLayerNormal;
+        if (dot(wo, s.coatingLayerNormal) < 0.0f) s.coatingLayerNormal = -s.coatingLayerNormal;
+        if (dot(wo, s.geometryNormal) < 0.0f) s.geometryNormal = -s.geometryNormal;
+    }
+    // setupSurfaceOrientation (materialsCommon.hlsl:487-501)
+    if (s.anisotropyRotation > 0.0f)
+    {
+        float ang = s.anisotropyRotation * 2.0f * kPI;
+        float sa, ca;
+        ygm_sincosf(ang, &sa, &ca);
+        float3 t = s.tangent;
+        s.tangent = mk3(ca * t.x + 0.0f * t.y + sa * t.z, 0.0f * t.x + 1.0f * t.y + 0.0f * t.z, -sa * t.x + 0.0f * t.y + ca * t.z);
+    }
+    // regularisation (rayHitDefault.hlsl:494-502)
+    if (P.regularizeEnable)
+    {
+        if (ps.pathLength >= P.regularizeAfter) ps.flags |= kFlagRegularize;
+        if (ps.flags & kFlagRegularize)
+        {
+            s.roughness = regularizeR(s.roughness, true);
+            s.sheenRoughness = regularizeR(s.sheenRoughness, false);
+            s.clearCoatRoughness = regularizeR(s.clearCoatRoughness, true);
+        }
+    }
+    hs.albedoRGB = rgb.albedo;
+    // convertSurfaceDefinitionFromRGB (hitShadersCommon.hlsl:51-91)
+    s.specular = rgbOrCurve(S, sp, rgb.specular, M.specularSpectrum);
+    s.albedo = rgbOrCurve(S, sp, rgb.albedo, M.albedoSpectrum);
+    s.absorption = isZero3(rgb.absorption) ? splat4(0.0f) : fromRGBUnboundedNoIllum(S, sp, rgb.absorption);
+    s.emissive = emissionSpectrum(S, sp, rgb.emissive, M.emissionSpectrum);
+    s.sheenColor = s.sheenAmount > 0.0f ? fromRGB(S, sp, rgb.sheenColor) : splat4(0.0f);
+}
+
+// sampleLight for mesh lights (lightSampling.hlsl:122-188), position part only
+struct LightPoint
+{
+    float4 radiance;
+    float3 pos, n;
+    float pdfPos, focus;
+    uint32_t instance, prim;
+    bool twoSided;
+};
+YG_DEV void sampleMeshLight(const SceneView& S, const Spectral& sp, uint32_t li, float3 r, LightPoint& out)
+{
+    GpuLight L = S.lights[li];
+    const GpuInstance& I = S.instances[L.instance];
+    uint32_t primCount = I.primCount;
+    uint32_t prim = (uint32_t)fminf((float)primCount * r.z, (float)(primCount - 1u));
+    float bx = r.x, by = r.y;
+    if (bx + by > 1.0f)
+    {
+        bx = 1.0f - bx;
+        by = 1.0f - by;
+    }
+    float b0 = 1.0f - bx - by;
+    TriGeom g = fetchTri(S, I, prim);
+    float3 p1 = xformPoint(I.o2w, g.p1), p2 = xformPoint(I.o2w, g.p2), p3 = xformPoint(I.o2w, g.p3);
+    float3 gn = cross(p2 - p1, p3 - p1);
+    float len = length(gn);
+    gn = gn / len;
+    float area = len * 0.5f;
+    out.pos = p1 * b0 + p2 * bx + p3 * by;
+    out.n = gn;
+    const GpuMaterial& M = S.materials[I.material];
+    float4 e = M.emissive_roughness;
+    out.radiance = emissionSpectrum(S, sp, mk3(e.x, e.y, e.z), M.emissionSpectrum);
+    out.pdfPos = 1.0f / ((float)primCount * area);
+    out.focus = M.emissionFocus;
+    out.instance = L.instance;
+    out.prim = prim;
+    out.twoSided = (M.mask & 1u) != 0;
+}
+
+YG_DEV uint32_t sampleLightIndex(const SceneView& S, float u)
+{
+    float scaled = u * (float)S.nLights;
+    uint32_t index = min((uint32_t)scaled, S.nLights - 1u);
+    GpuLight e = S.lights[index];
+    return (scaled - (float)index) < e.aliasThreshold ? index : e.aliasIndex;
+}
+
+// calculateExplicitLightConnectionPDF (rayHitDefault.hlsl:137-166)
+YG_DEV float explicitLightPdf(const SceneView& S, float3 fromTo, uint32_t inst, uint32_t prim)
+{
+    const GpuInstance& I = S.instances[inst];
+    TriGeom g = fetchTri(S, I, prim);
+    float3 p1 = xformPoint(I.o2w, g.p1), p2 = xformPoint(I.o2w, g.p2), p3 = xformPoint(I.o2w, g.p3);
+    float3 gn = cross(p2 - p1, p3 - p1);
+    float len = length(gn);
+    gn = gn / len;
+    float area = len * 0.5f;
+    float posPdf = 1.0f / ((float)I.primCount * area);
+    return posPdf * I.lightPdf * areaToSolidAngle(fromTo, gn);
+}
+
+struct TraceStats
+{
+    uint32_t rays;
+    TraversalCount tc;
+};
+
+
+// NEE connection prepared at a vertex: the shadow ray and the contribution it adds
+// to the path total when the sampled light point is visible (connectToExplicitLight,
+// rayHitDefault.hlsl:204-257, with the visibility test deferred).
+struct ShadowRequest
+{
+    float3 origin, dir;
+    float tmax;
+    uint32_t instance, prim;
+    float4 contrib;
+    bool valid;
+};
+
+YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, const Surface& s, const SurfaceCtx& c,
+                       float3 woOS, float3 posWS, float3 normalWS, const float4* w2o, const PathState& ps,
+                       RandomSampler& rs, ShadowRequest& sr)
+{
+    float4 r = rs.r4();
+    uint32_t li = sampleLightIndex(S, r.w);
+    float pick = S.lights[li].selectionPdf;
+    LightPoint lp;
+    sampleMeshLight(S, sp, li, mk3(r.x, r.y, r.z), lp);
+    float3 toLight = lp.pos - posWS;
+    float len = length(toLight);
+    float cosEmit = -dot(lp.n, toLight / len);
+    float4 emission = lp.radiance * evaluateEmissionProfile(cosEmit, lp.focus);
+    float pdf = pick * lp.pdfPos * areaToSolidAngle(toLight, lp.n);
+    float3 toLightWS = toLight / len;
+    if (!lp.twoSided && dot(toLight, lp.n) >= 0.0f)
+    {
+        emission = splat4(0.0f);
+        pdf = 0.0f;
+    }
+    if (allEqual4(emission, 0.0f) || !(pdf > 0.0f)) return;
+    float3 toLightOS = normalize(xformVector(w2o, toLightWS));
+    Eval ev = evaluateSurface(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
+    float4 w = ev.weight;
+    if ((ev.transmission & kTransDispersed) != 0 && !(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(w);
+    if (allEqual4(w, 0.0f)) return;
+    float wMIS = weightMIS(pdf, ev.pdf);
+    w = (w / pdf) * wMIS;
+    sr.origin = spawnRayOrigin(posWS, normalWS, toLightWS);
+    sr.dir = toLightWS;
+    sr.tmax = len + kRayMinT;
+    sr.instance = lp.instance;
+    sr.prim = lp.prim;
+    sr.contrib = ps.throughput * w * emission;
+    sr.valid = true;
+}
+
+// checkLightVisibility (rayHitDefault.hlsl:83-112): the closest hit must be the sampled light triangle
+YG_DEV bool shadowVisible(bool any, const Hit& h, uint32_t inst, uint32_t prim)
+{
+    return any && h.instance == inst && h.prim == prim;
+}
+
+// generateCameraRay (raytraceCommonResources.hlsl:113-137) and the sample set-up of
+// rayGenPrimaryRays.hlsl:13-37
+YG_DEV void beginPath(const SceneView& S, const LaunchParams& P, uint32_t cx, uint32_t cy, RandomSampler& rs, Spectral& sp,
+                      PathState& ps)
+{
+    sp.hero = S.lambdaMin + rs.r1() * (S.lambdaMax - S.lambdaMin);
+    sp.lambdas = getSpectralSampleLambdas(sp.hero, S.lambdaMin, S.lambdaMax);
+    float invW = 1.0f / (float)P.width, invH = 1.0f / (float)P.height;
+    float2 uv = make_float2((float)cx * invW + 0.5f * invW, (float)cy * invH + 0.5f * invH);
+    float2 texel = make_float2(sampleDim(rs.point, 0, rs.seed), sampleDim(rs.point, 1, rs.seed));
+    float2 lensR = rs.r2();
+    float2 to = make_float2(0.f, 0.f);
+    if ((P.flags & 2u) == 0) to = make_float2(texel.x - 0.5f, texel.y - 0.5f);
+    to = make_float2(to.x * invW, to.y * invH);
+    float4 pn = mul44(S.cam.uvToView, mk4(uv.x + to.x, uv.y + to.y, 0.0f, 1.0f));
+    pn = pn / pn.w;
+    float3 pin = mk3(pn.x, pn.y, pn.z);
+    float3 focusP = pin * safeDiv(S.cam.focusDistance, fabsf(pin.z));
+    float2 disk = sampleConcentricDisk(lensR);
+    float3 lensP = mk3(disk.x * S.cam.apertureRadius, disk.y * S.cam.apertureRadius, 0.0f);
+    float4 ow = mul44(S.cam.viewToWorld, mk4(lensP.x, lensP.y, lensP.z, 1.0f));
+    float4 dw = mul44(S.cam.viewToWorld, mk4(focusP.x - lensP.x, focusP.y - lensP.y, focusP.z - lensP.z, 0.0f));
+    ps.throughput = splat4(1.0f);
+    ps.total = splat4(0.0f);
+    ps.origin = mk3(ow.x, ow.y, ow.z);
+    ps.dir = normalize(mk3(dw.x, dw.y, dw.z));
+    ps.pdfThisRay = 0.0f;
+    ps.flags = 0;
+    ps.pathLength = 0;
+    ps.nVol = 0;
+}
+
+YG_DEV void spectralOf(const SceneView& S, float hero, Spectral& sp)
+{
+    sp.hero = hero;
+    sp.lambdas = getSpectralSampleLambdas(hero, S.lambdaMin, S.lambdaMax);
+}
+
+struct FirstHit
+{
+    float3 albedo, normal;
+    float depth;
+};
+
+// One traced segment: the miss shader, or the closest-hit shader at the vertex, then
+// Russian roulette. Returns whether the path continues; the NEE shadow request (if
+// any) must be resolved before the next segment is shaded.
+template <bool NEE>
+YG_DEV bool shadeSegment(const SceneView& S, const LaunchParams& P, const Luts& Lt, const Spectral& sp, bool found,
+                         const Hit& hit, PathState& ps, RandomSampler& rs, ShadowRequest& sr, FirstHit* fh)
+{
+    sr.valid = false;
+    bool alive = true;
+    if (!found)
+    {
+        // rayMissEnvironment: |dir| * Env.IntensityScale, as an unbounded RGB emitter
+        float3 col = mk3(fabsf(ps.dir.x) * P.envScale, fabsf(ps.dir.y) * P.envScale, fabsf(ps.dir.z) * P.envScale);
+        float4 Le = isZero3(col) ? splat4(0.0f) : fromRGBUnbounded(S, sp, col);
+        ps.total = ps.total + ps.throughput * Le;
+        alive = false;
+    }
+    else
+    {
+        const GpuInstance& I = S.instances[hit.instance];
+        HitSurface hs;
+        setupSurface(S, P, sp, hit, I, ps.dir, ps, hs);
+        Surface& s = hs.s;
+        float3 hitPos = ps.origin + ps.dir * hit.t;
+        if (ps.pathLength == 0 && fh)
+        {
+            fh->albedo = hs.albedoRGB;
+            fh->normal = normalize(xformVectorT(I.w2o, s.baseLayerNormal));
+            float4 vp = mul44(S.cam.worldToView, mk4(hitPos.x, hitPos.y, hitPos.z, 1.0f));
+            fh->depth = vp.z * S.cam.forwardZSign;
+        }
+        // handleRayStartInsideMedium (hitShadersCommon.hlsl:212-222)
+        if (dot(hs.rayDirOS, s.geometryNormal) > 0.0f && ps.nVol == 0 && !isTwoSided(s.flags))
+            enteredVolume(ps, s.dielectricIOR, s.absorption, hs.material);
+        // absorption along the segment
+        float4 ab = ps.nVol != 0 ? ps.volAbs[ps.nVol - 1] : splat4(0.0f);
+        if (!allEqual4(ab, 0.0f))
+        {
+            float4 tr = mk4(ygm_expf(-ab.x * hit.t), ygm_expf(-ab.y * hit.t), ygm_expf(-ab.z * hit.t), ygm_expf(-ab.w * hit.t));
+            ps.throughput = ps.throughput * tr;
+        }
+        if (!allEqual4(s.emissive, 0.0f))
+        {
+            float wMIS = 1.0f;
+            if (NEE && S.nLights > 0 && ps.pdfThisRay > 0.0f && !(ps.flags & kFlagDelta))
+            {
+                float lightPdf = explicitLightPdf(S, hitPos - ps.origin, hit.instance, hit.prim);
+                wMIS = weightMIS(ps.pdfThisRay, lightPdf);
+            }
+            float side = dot(s.geometryNormal, -hs.rayDirOS) < 0.0f ? 0.0f : 1.0f;
+            float profile = 1.0f;
+            if (s.emissionFocus > 0.0f)
+            {
+                float3 gnWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
+                profile = evaluateEmissionProfile(dot(gnWS, -normalize(ps.dir)), s.emissionFocus);
+            }
+            ps.total = ps.total + ps.throughput * s.emissive * wMIS * side * profile;
+            alive = false;
+        }
+        else
+        {
+            // evaluateSurfaceAndGenerateNextSampleDirection (rayHitDefault.hlsl:316-435)
+            float4 rB = rs.r4();
+            float3 wo = -hs.rayDirOS;
+            SurfaceCtx c;
+            makeSurfaceCtx(s, currentIOR(ps), previousIOR(ps), wo, hit.front, c);
+            float3 normalWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
+            if (NEE && S.nLights > 0 && !isDeltaDistribution(c.a2, s))
+                prepareNee(S, Lt, sp, s, c, wo, hitPos, normalWS, I.w2o, ps, rs, sr);
+            // sampleScatteringEvent (scatteringSample.hlsl:30-65)
+            int layer = selectMaterialLayer(rB.x, c.probs);
+            float3 wi = mk3(0.f, 0.f, 0.f);
+            bool isDiffuse = false, isDelta = false;
+            if (layer != LAYER_SSS && layer < LAYER_COUNT)
+                wi = sampleLayerDirection(Lt, s, c, layer, rB.y, make_float2(rB.z, rB.w), sp.hero, isDiffuse, isDelta);
+            Eval ev;
+            ev.weight = splat4(0.0f);
+            ev.pdf = 0.0f;
+            ev.transmission = 0;
+            if (!isZero3(wi))
+            {
+                ev = evaluateSurface(Lt, s, c, wo, wi, isDelta ? kEvalTreatAsDelta : kEvalNone, sp);
+                if (isDiffuse) ps.flags |= kFlagRegularize;
+            }
+            ps.pdfThisRay = ev.pdf;
+            if (isDelta) ps.flags |= kFlagDelta;
+            else ps.flags &= ~kFlagDelta;
+            if (ev.pdf > 0.0f)
+            {
+                if (ev.transmission != 0)
+                {
+                    if ((ev.transmission & kTransDispersed) != 0)
+                    {
+                        if (!(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(ev.weight);
+                        ps.flags |= kFlagSecondaryTerminated;
+                    }
+                    bool entered = (ev.transmission & kTransEntered) != 0;
+                    bool exited = (ev.transmission & kTransExited) != 0;
+                    if (entered != exited)
+                    {
+                        if (exited) exitedVolume(ps, hs.material);
+                        else enteredVolume(ps, s.dielectricIOR, s.absorption, hs.material);
+                    }
+                }
+                ev.weight = ev.weight / ev.pdf;
+            }
+            ps.throughput = ps.throughput * ev.weight;
+            if (isZero3(wi) || ps.pdfThisRay == 0.0f)
+            {
+                alive = false;
+            }
+            else
+            {
+                float3 nW = normalize(xformVector(I.o2w, s.geometryNormal));
+                float3 dW = normalize(xformVector(I.o2w, wi));
+                ps.origin = spawnRayOrigin(hitPos, nW, dW);
+                ps.dir = dW;
+            }
+        }
+    }
+    ps.pathLength += 1;
+    // Russian roulette after every traced segment (rayGenPrimaryRays.hlsl:91-101); a path
+    // that already ended gains nothing from it, so it is skipped there
+    if (alive && russianRoulette(ps.throughput, rs.r1())) alive = false;
+    return alive;
+}
+
+} // namespace yg
