@@ -238,6 +238,22 @@ YG_API int yg_features_read(yg_context* ctx, float* albedo, float* normal, float
  * (x - r)^2 / (r^2 + eps). */
 YG_API int yg_film_relmse(yg_context* ctx, const float* reference_xyz, double eps, double* relmse);
 
+/* Render without allocating: no counterpart in the reference. For callers that cannot
+ * allocate device memory while rendering -- a serving process whose admission controller
+ * reserves the device budget up front, or a host application that must not trigger
+ * cudaMalloc's implicit device synchronisation mid-frame. Same samples as yg_render (uni or
+ * NEE; the film, sample dump and features are not touched). The scene must already be built
+ * (yg_build_scene) and the spectral range must be the one of the context's last yg_render
+ * (380..700 nm on a new context). Writes crop_w * crop_h * spp_count float4 (X, Y, Z, 1)
+ * to device_sample_xyz (device memory, 16-byte aligned), ordered [spp][row][column];
+ * asynchronous on the context stream (ready after yg_synchronize).
+ * Scratch: a file-scope device array of about 6 MB that every GPU loading the library holds
+ * until exit; at most 256 sample indices per call (spp_count > 256 is rejected) and waves of
+ * 16384 paths. The first call on a device looks up the array's device address; make that
+ * first call before any stream capture. All calls share the one array: calls whose work
+ * overlaps on the GPU (other contexts or threads, other streams) race on it. */
+YG_API int yg_render_samples_noalloc(yg_context* ctx, const yg_render_params* params, float* device_sample_xyz);
+
 /* Device timing of the most recent yg_render: kernel milliseconds, rays traced. */
 YG_API int yg_last_render_stats(yg_context* ctx, float* kernel_ms, uint64_t* rays, uint32_t* launches);
 /* Traversal work of the most recent render made with YG_FLAG_COUNT_TRAVERSAL. */

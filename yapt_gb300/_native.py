@@ -115,6 +115,7 @@ SIGNATURES = [
     ("yg_last_render_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint64),
                                        C.POINTER(C.c_uint32)]),
     ("yg_last_traversal_counts", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("yg_render_samples_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p]),
 ]
 
 

@@ -928,3 +928,176 @@ YG_API int yg_film_relmse(yg_context* ctx, const float* ref, double eps, double*
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// Render entry point that allocates nothing.
+//
+// Some callers cannot allocate device memory while rendering: a serving process whose
+// admission controller reserves the device budget up front, or a host application that
+// must not hit cudaMalloc's implicit device synchronisation in the middle of a frame.
+// yg_render_samples_noalloc renders with the wavefront kernels like yg_render, but its
+// scratch (path-state arena, Sobol points, generator matrices) is the file-scope device
+// array below, a fixed 6 MB that every GPU loading this library holds until exit. The
+// caller passes the scene (already built in the context) and the output buffer.
+namespace
+{
+constexpr uint32_t kNoAllocWaveCapacity = 16384; // paths in flight per wave
+constexpr uint32_t kNoAllocMaxSpp = 256;         // sample indices per call
+constexpr size_t kNoAllocBytesPerSlot = 352;     // >= wavefrontBytesPerSlot(), checked at set-up
+constexpr size_t kNoAllocSobolBytes = (size_t)kNoAllocMaxSpp * yg::kSobolDims * sizeof(uint32_t);
+constexpr size_t kNoAllocMatrixBytes = (size_t)yg::kSobolDims * 32 * sizeof(uint32_t);
+constexpr size_t kNoAllocArenaBytes = (size_t)kNoAllocWaveCapacity * kNoAllocBytesPerSlot + (64u << 10);
+constexpr size_t kNoAllocScratchBytes = kNoAllocSobolBytes + kNoAllocMatrixBytes + kNoAllocArenaBytes;
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+std::mutex g_noallocMutex;
+void* g_noallocDevicePtr[256] = {};
+
+// Device address of the scratch array on `device` (which must be current). The host
+// symbol is only a stand-in, so the address is looked up once per device and cached.
+int noallocScratchAddress(int device, void** out)
+{
+    if (device < 0 || device >= 256) return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: device ordinal out of range");
+    if (yg::wavefrontBytesPerSlot() > kNoAllocBytesPerSlot)
+        return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: scratch layout is smaller than the wavefront state");
+    std::lock_guard<std::mutex> g(g_noallocMutex);
+    if (!g_noallocDevicePtr[device])
+    {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess || !p)
+            return fail(YG_ERR_CUDA, std::string("no-alloc render: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noallocDevicePtr[device] = p;
+    }
+    *out = g_noallocDevicePtr[device];
+    return YG_OK;
+}
+
+// Sobol points for sample indices [start, start + count), all 256 dimensions
+__global__ void noallocSobolPoints(const uint32_t* __restrict__ matrices, uint32_t start, uint32_t count,
+                                   uint32_t* __restrict__ out)
+{
+    const uint32_t n = count * (uint32_t)yg::kSobolDims;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        uint32_t s = i / yg::kSobolDims, d = i % yg::kSobolDims;
+        uint32_t index = start + s, v = 0;
+        for (uint32_t k = d * 32; index != 0; index >>= 1, ++k)
+            if (index & 1u) v ^= matrices[k];
+        out[i] = v;
+    }
+}
+} // namespace
+
+extern "C" {
+
+YG_API int yg_render_samples_noalloc(yg_context* ctx, const yg_render_params* p, float* device_sample_xyz)
+{
+    if (!ctx || !p || !device_sample_xyz) return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: null argument");
+    if (((uintptr_t)device_sample_xyz & 15u) != 0)
+        return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: output must be 16-byte aligned device memory");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    if (!ctx->sceneBuilt) return fail(YG_ERR_NOT_READY, "no-alloc render: call yg_build_scene first");
+    if (!ctx->cameraSet) return fail(YG_ERR_NOT_READY, "no-alloc render: camera not set");
+    if (p->integrator > YG_INTEGRATOR_NEE)
+        return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: only the uni and NEE integrators are available");
+    if (p->width == 0 || p->height == 0 || p->spp_count == 0)
+        return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: empty request");
+    if (p->spp_count > kNoAllocMaxSpp)
+        return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: spp_count " + std::to_string(p->spp_count) +
+                                                 " exceeds the maximum of " + std::to_string(kNoAllocMaxSpp) +
+                                                 " sample indices per call");
+    uint32_t cx = p->crop_x, cy = p->crop_y, cw = p->crop_w, ch = p->crop_h;
+    if (cw == 0 || ch == 0)
+    {
+        cx = cy = 0;
+        cw = p->width;
+        ch = p->height;
+    }
+    if ((uint64_t)cx + cw > p->width || (uint64_t)cy + ch > p->height)
+        return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: crop outside image");
+    float lminf = p->lambda_min, lmaxf = p->lambda_max;
+    if (lminf == 0.0f && lmaxf == 0.0f)
+    {
+        lminf = 380.f;
+        lmaxf = 700.f;
+    }
+    if ((float)ctx->cieLmin != lminf || (float)ctx->cieLmax != lmaxf)
+        return fail(YG_ERR_NOT_READY, "no-alloc render: spectral range differs from the context's current range "
+                                      "(render once with yg_render at this range first)");
+    bool needRgb = sceneNeedsRgbLut(ctx, p->env_intensity_scale);
+    if (needRgb && (ctx->rgbToSpd.empty() || ctx->rgbLmin != ctx->cieLmin || ctx->rgbLmax != ctx->cieLmax || !ctx->dRgb.p))
+        return fail(YG_ERR_NOT_READY, "no-alloc render: the RGB spectral fit is not resident "
+                                      "(render once with yg_render at this range first)");
+    YG_CUDA(cudaSetDevice(ctx->device));
+    void* scratch = nullptr;
+    int r = noallocScratchAddress(ctx->device, &scratch);
+    if (r) return r;
+    char* base = static_cast<char*>(scratch);
+    uint32_t* sobolPts = reinterpret_cast<uint32_t*>(base);
+    uint32_t* matrices = reinterpret_cast<uint32_t*>(base + kNoAllocSobolBytes);
+    void* arena = base + kNoAllocSobolBytes + kNoAllocMatrixBytes;
+    YG_CUDA(cudaMemcpyAsync(matrices, ctx->sobolMatrices.data(), kNoAllocMatrixBytes, cudaMemcpyHostToDevice, ctx->stream));
+    noallocSobolPoints<<<ctx->smCount, 256, 0, ctx->stream>>>(matrices, p->spp_start, p->spp_count, sobolPts);
+
+    yg::SceneView S{};
+    S.tris = ctx->dTris.as<float4>();
+    S.nodes = ctx->dNodes.as<float4>();
+    S.instances = ctx->dInst.as<yg::GpuInstance>();
+    S.materials = ctx->dMat.as<yg::GpuMaterial>();
+    S.lights = ctx->dLights.as<yg::GpuLight>();
+    S.positions = ctx->dPos.as<float>();
+    S.normals = ctx->dNrm.as<float>();
+    S.tangents = ctx->dTan.as<float4>();
+    S.uvs = ctx->dUV.as<float2>();
+    S.indices = ctx->dIdx.as<uint32_t>();
+    S.spectra = ctx->dSpec.as<float>();
+    S.lutSS = ctx->dLut[0].as<float>();
+    S.lutSSAvg = ctx->dLut[1].as<float>();
+    S.lutSSMS = ctx->dLut[2].as<float>();
+    S.lutSSMSAvg = ctx->dLut[3].as<float>();
+    S.lutTransDenser = ctx->dLut[4].as<float>();
+    S.lutTransLighter = ctx->dLut[5].as<float>();
+    S.lutTransAvgDenser = ctx->dLut[6].as<float>();
+    S.lutTransAvgLighter = ctx->dLut[7].as<float>();
+    S.lutSheen = ctx->dLut[8].as<float>();
+    S.cie = ctx->dCie.as<float4>();
+    S.rgbToSpd = needRgb ? ctx->dRgb.as<float>() : nullptr;
+    S.sobol = sobolPts;
+    S.cam = ctx->camera;
+    S.nLights = ctx->nLights;
+    S.nInstances = (uint32_t)ctx->instances.size();
+    S.specPoints = ctx->specPoints;
+    S.specLmin = ctx->specLmin;
+    S.specLmax = ctx->specLmax;
+    S.cieN = ctx->cieN;
+    S.lambdaMin = lminf;
+    S.lambdaMax = lmaxf;
+    S.cieYSumInv = ctx->cieYSumInv;
+    S.d65SumInv = ctx->d65SumInv;
+
+    yg::LaunchParams L{};
+    L.integrator = p->integrator;
+    L.width = p->width;
+    L.height = p->height;
+    L.cropX = cx;
+    L.cropY = cy;
+    L.cropW = cw;
+    L.cropH = ch;
+    L.sppStart = p->spp_start;
+    L.sppCount = p->spp_count;
+    L.maxDepth = p->max_depth;
+    L.regularizeAfter = p->regularize_after_vertices;
+    L.regularizeEnable = p->regularize_enable;
+    L.envScale = p->env_intensity_scale;
+    L.seed = p->seed;
+    L.flags = p->flags;
+    L.nSamples = (uint64_t)cw * ch * p->spp_count;
+    L.sampleXYZ = reinterpret_cast<float4*>(device_sample_xyz);
+    yg::launchWavefront(S, L, arena, kNoAllocWaveCapacity, ctx->smCount, ctx->stream);
+    YG_CUDA(cudaGetLastError());
+    return YG_OK;
+}
+
+} // extern "C"
