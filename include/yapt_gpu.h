@@ -153,8 +153,10 @@ typedef struct yg_render_params
     uint32_t flags;
     uint32_t crop_x, crop_y, crop_w, crop_h; /* render only this pixel rectangle (w=h=0: all) */
     float lambda_min, lambda_max;            /* spectral range; reference: 380..700 nm */
-    uint32_t bdpt_light_paths;               /* BDPT: light subpaths per frame (0: ceil(W/8)*ceil(H/8)) */
-    uint32_t reserved[3];
+    uint32_t bdpt_light_paths;               /* BDPT: light subpaths per frame (0: ceil(W/8)*ceil(H/8) of the crop) */
+    uint32_t bdpt_light_vertices;            /* BDPT: vertices per light subpath, light included (0: 16, max 16;
+                                                maxVerticesPerLightPath, BidirectionalPathIntegratorSubStage.cpp:480-488) */
+    uint32_t reserved[2];
 } yg_render_params;
 
 /* Per-sample record written by yg_render when sample_dump != NULL:

@@ -1,0 +1,103 @@
+"""The bidirectional integrator (BDPT) through the C ABI.
+
+BDPT is not per-sample reproducible in the reference (light-path headers are ordered by
+atomics there), so its parity is statistical, as in the reference's own integrator
+comparison (Tests/IntegratorCompare: block-averaged differences between integrators):
+on scenes where both estimators are unbiased for the same image, BDPT and NEE must agree
+block by block within their combined standard error. The NEE side is itself pinned per
+sample to the oracle by test_gpu_parity.py. This build's BDPT is deterministic, which is
+checked bit for bit.
+"""
+import numpy as np
+import pytest
+
+from yapt_gb300 import configs
+from yapt_gb300.runtime import Context
+
+pytestmark = pytest.mark.gpu
+
+Z_MAX = 5.0          # largest block z-score accepted
+MEAN_REL_TOL = 0.02  # whole-image mean luminance
+
+
+def block_stats(rec, b):
+    """Per-frame block means of the Y channel of (spp, H, W, 8) sample records -> mean, stderr."""
+    y = rec[..., 6].astype(np.float64)
+    s, h, w = y.shape
+    m = y.reshape(s, h // b, b, w // b, b).mean(axis=(2, 4))
+    return m.mean(axis=0), m.std(axis=0, ddof=1) / np.sqrt(s)
+
+
+def compare_integrators(c, scene, W, H, spp, block, env_scale=0.0, depth=24):
+    c.upload_scene(scene)
+    common = dict(spp=spp, max_depth=depth, regularize=False, lambda_range=(380, 780), env_scale=env_scale, flags=256)
+    nee = c.render(c.params("nee", W, H, **common), dump=True)
+    bd = c.render(c.params("bdpt", W, H, **common), dump=True)
+    assert np.all(np.isfinite(bd)), "non-finite BDPT samples"
+    mn, sn = block_stats(nee, block)
+    mb, sb = block_stats(bd, block)
+    z = np.abs(mb - mn) / np.sqrt(sn ** 2 + sb ** 2 + 1e-30)
+    gm_n, gm_b = float(nee[..., 6].mean()), float(bd[..., 6].mean())
+    assert gm_n > 0
+    rel = abs(gm_b - gm_n) / gm_n
+    assert rel < MEAN_REL_TOL, "mean Y: BDPT %.5f vs NEE %.5f (rel %.4f)" % (gm_b, gm_n, rel)
+    assert float(z.max()) < Z_MAX, "block z-scores up to %.2f (mean Y BDPT %.5f NEE %.5f)" % (z.max(), gm_b, gm_n)
+    # BDPT combines more strategies than NEE: on these scenes it must not be noisier overall
+    return float(z.max()), rel, float(np.mean(sb)), float(np.mean(sn))
+
+
+def test_bdpt_agrees_with_nee_on_the_diffuse_box(built):
+    with Context(0) as c:
+        zmax, rel, se_b, se_n = compare_integrators(c, configs.box_scene(0), 32, 32, 256, 8)
+        assert se_b < 1.5 * se_n, (se_b, se_n)
+
+
+def test_bdpt_agrees_with_nee_under_the_sky_without_lights(built):
+    # no light instances: light subpaths start on the environment (sampleEnvironmentAsLight)
+    with Context(0) as c:
+        compare_integrators(c, configs.sky_scene(1), 32, 32, 256, 8, env_scale=1.0, depth=16)
+
+
+def test_bdpt_agrees_with_nee_with_smooth_dispersive_glass(built):
+    # smooth (delta) dielectrics have no multiple-scattering term, so the two integrators
+    # estimate the same image although they use different compensation models for rough ones
+    sc = configs.caustic_box_scene(2, n_spheres=12, n_lights=3, sphere_subdiv=2)
+    for m in sc.materials:
+        if m.get("transparency", 0.0) == 1.0:
+            m["roughness"] = 0.0
+    with Context(0) as c:
+        compare_integrators(c, sc, 32, 32, 384, 8)
+
+
+def test_bdpt_is_deterministic_and_accumulates_like_one_request(built):
+    with Context(0) as c:
+        c.upload_scene(configs.box_scene(1))
+        p = c.params("bdpt", 48, 40, spp=6, max_depth=10, lambda_range=(380, 780))
+        c.film_clear(48, 40)
+        c.render(p)
+        a, na = c.film()
+        c.film_clear(48, 40)
+        c.render(p)
+        b, nb = c.film()
+        assert np.array_equal(a, b) and np.array_equal(na, nb)
+        assert np.all(na == 6) and np.all(np.isfinite(a)) and a[..., 1].mean() > 0
+        # the same sample indices in two requests give the same film
+        c.film_clear(48, 40)
+        c.render(c.params("bdpt", 48, 40, spp_start=0, spp=3, max_depth=10, lambda_range=(380, 780)))
+        c.render(c.params("bdpt", 48, 40, spp_start=3, spp=3, max_depth=10, lambda_range=(380, 780)))
+        d, nd = c.film()
+        assert np.all(nd == 6)
+        np.testing.assert_allclose(d, a, rtol=2e-6, atol=1e-7)
+
+
+def test_bdpt_request_validation(built):
+    from yapt_gb300 import _native as N
+    with Context(0) as c:
+        c.upload_scene(configs.box_scene(0))
+        c.film_clear(8, 8)
+        p = c.params("bdpt", 8, 8, spp=1, light_vertices=17)
+        with pytest.raises(N.YaptError):
+            c.render(p)
+        p = c.params("bdpt", 8, 8, spp=1, flags=N.YG_FLAG_MEGAKERNEL)
+        with pytest.raises(N.YaptError):
+            c.render(p)

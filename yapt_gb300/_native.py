@@ -80,7 +80,7 @@ class RenderParams(C.Structure):
         ("env_intensity_scale", C.c_float), ("seed", C.c_uint32), ("flags", C.c_uint32),
         ("crop_x", C.c_uint32), ("crop_y", C.c_uint32), ("crop_w", C.c_uint32), ("crop_h", C.c_uint32),
         ("lambda_min", C.c_float), ("lambda_max", C.c_float), ("bdpt_light_paths", C.c_uint32),
-        ("reserved", C.c_uint32 * 3),
+        ("bdpt_light_vertices", C.c_uint32), ("reserved", C.c_uint32 * 2),
     ]
 
 

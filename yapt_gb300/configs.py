@@ -199,3 +199,55 @@ def random_shapes_scene(seed=0, n_spheres=500, light_intensity=25.0, aspect=1.0)
         sc.add_instance(light, lmat, affine(translation=pos))
     sc.camera = CameraDesc(eye=(0.0, 7.0, 19.0), target=(0.0, 1.0, 0.0), fovy=np.pi * 0.3, aspect=aspect)
     return sc
+
+
+def caustic_box_scene(seed=0, n_spheres=150, n_lights=10, sphere_subdiv=3, light_intensity=12.0,
+                      sphere_light_intensity=3.0, aspect=1.0):
+    """The box layout of ``box_scene`` (same seed, same walls, blocks and ceiling light) filled
+    with ``n_spheres`` small icospheres, 60% of them dispersive dielectrics (Cauchy A = 1.5,
+    B = 0.0042 um^2; half of those smooth, half with roughness U(0.05, 0.3)) and 40% diffuse,
+    plus ``n_lights`` emissive spheres of radius 0.05 with a D65-shaped spectrum. With the
+    defaults the scene holds about 196k triangles."""
+    sc = box_scene(seed, light_intensity=light_intensity, aspect=aspect)
+    sc.name = "caustic_box(seed=%d, n=%d)" % (seed, n_spheres)
+    rng = np.random.Generator(np.random.PCG64(seed + 7919))
+    ball = sc.add_mesh(*icosphere(sphere_subdiv))
+    for _ in range(n_spheres):
+        r = rng.uniform(0.03, 0.08)
+        c = (rng.uniform(0.05 + r, 0.95 - r), rng.uniform(r, 0.85), rng.uniform(0.05 + r, 0.95 - r))
+        if rng.uniform() < 0.6:
+            rough = 0.0 if rng.uniform() < 0.5 else rng.uniform(0.05, 0.3)
+            mat = sc.add_material(albedo=(1.0, 1.0, 1.0), transparency=1.0, metalness=0.0, specular_amount=1.0,
+                                  roughness=rough, material_mask=2, cauchy=(1.5, 0.0042), dielectric_ior=1.5)
+        else:
+            mat = sc.add_material(**diffuse(sc.add_spectrum(control_point_spectrum(rng))))
+        sc.add_instance(ball, mat, affine(translation=c, scale=(r, r, r)))
+    bulb = sc.add_mesh(*icosphere(2))
+    lmat = sc.add_material(albedo=(0.0, 0.0, 0.0), emissive=(sphere_light_intensity,) * 3, metalness=0.0,
+                           specular_amount=0.0, roughness=1.0)
+    for _ in range(n_lights):
+        c = (rng.uniform(0.1, 0.9), rng.uniform(0.6, 0.9), rng.uniform(0.1, 0.9))
+        sc.add_instance(bulb, lmat, affine(translation=c, scale=(0.05, 0.05, 0.05)))
+    return sc
+
+
+def sky_scene(seed=0, aspect=1.0):
+    """No lights: a diffuse ground quad and three diffuse blocks under the analytic sky of the
+    reference's miss shader (|dir| x Env.IntensityScale), for the environment light paths."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sc = Scene()
+    sc.name = "sky(seed=%d)" % seed
+    gp, gn, gi = quad(6.0, 6.0)
+    gn = -gn
+    gi = gi[[0, 2, 1, 3, 5, 4]]
+    ground = sc.add_mesh(gp, gn, gi)
+    sc.add_instance(ground, sc.add_material(**diffuse(sc.add_spectrum(control_point_spectrum(rng)))))
+    cube = sc.add_mesh(*cuboid())
+    for k in range(3):
+        mat = sc.add_material(**diffuse(sc.add_spectrum(control_point_spectrum(rng))))
+        h = rng.uniform(0.5, 1.5)
+        o2w = affine(translation=(-1.2 + 1.2 * k, h / 2, rng.uniform(-0.5, 0.5)),
+                     rotation=rotation_y(rng.uniform(0, np.pi)), scale=(0.6, h, 0.6))
+        sc.add_instance(cube, mat, o2w)
+    sc.camera = CameraDesc(eye=(0.0, 2.5, 5.0), target=(0.0, 0.5, 0.0), fovy=np.pi * 0.3, aspect=aspect)
+    return sc

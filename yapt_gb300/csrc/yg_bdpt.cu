@@ -1,0 +1,1095 @@
+// Bidirectional path tracing with MIS (the BDPT render pipeline), restated for CUDA from
+// YAPT's compute shaders:
+//   BDPTCommon.hlsl:26-1223           node format, MIS ratio sums, connections
+//   BDPTTraceLightPath.comp:6-362     light subpaths
+//   BDPTTraceCameraPath.comp:40-432   camera subpaths + connections to every light vertex
+//   BDPTCalculatePureLightPaths.comp:107-206, BDPTAccumulatePureLightPaths.comp:7-31
+//                                     light tracing to the lens (t = 1)
+// The BSDF runs with the Kulla-Conty multiple-scattering model (RECIPROCAL_MULTISCATTER,
+// BDPTCommon.hlsl:6), as in the reference.
+//
+// Layout on the device: light vertices are stored by (sample index, light path, vertex),
+// so the reference's header/vertex counters, linked lists and sort pass are not needed.
+// The light paths that produced vertices are compacted in index order, which makes the
+// random light-path pick of a camera group deterministic (the reference orders them by
+// atomic arrival). A camera group is one CUDA block of 64 threads over 64 pixels of a fixed
+// pixel permutation, and stages its light path in shared memory once, with every light
+// vertex's spectral surface and forward shading frame already set up: the group shares the
+// hero wavelength of its light path, so those do not depend on the pixel. Light-tracing
+// splats are summed in 64-bit fixed point, so the film does not depend on atomic order.
+#include <algorithm>
+
+#include "yg_path.cuh"
+#include "yg_kernels.h"
+
+namespace yg
+{
+
+constexpr uint32_t NF_TERMINATED = 1u << 0; // LIGHT_PATH_NODE_FLAG_* (BDPTCommon.hlsl:13-24)
+constexpr uint32_t NF_FRONT = 1u << 1;
+constexpr uint32_t NF_ENV = 1u << 2;
+constexpr uint32_t NF_DELTA = 1u << 3;
+constexpr uint32_t NF_REGULARIZED = 1u << 4;
+constexpr float kMaxPdfRatioSum = 1e16f;    // MAX_PDF_RATIO_SUM
+constexpr float kVisibilityEps = 0.001f;    // VISIBILITY_RAY_EPSILON
+constexpr double kSplatScale = 16777216.0;  // fixed-point units per XYZ unit (2^24)
+constexpr int kGroupSize = 64;              // THREAD_GROUP_DIM_SIZE_CAM_RAY^2
+
+// LightPathNode (BDPTCommon.hlsl:52-67): 80 bytes, the normal kept in FP32 (the reference
+// packs it to FP16 and spends the 4 bytes on a linked-list index instead).
+struct alignas(16) LightNode
+{
+    float4 radiance;
+    float3 normal;
+    uint32_t flags;
+    float3 pos;
+    uint32_t instance;
+    float2 bary;
+    uint32_t prim;
+    float pdfFwd;
+    float pdfBwd, iorPrev, iorCur, pad;
+};
+
+struct BdptParams
+{
+    uint32_t frames;        // sample indices in this launch
+    uint32_t lightPaths;    // light subpaths per sample index
+    uint32_t maxLightVerts; // g_maxVerticesPerLightPath
+    uint32_t groups;        // camera groups per sample index
+    uint32_t camDimOffset;  // g_cameraPathRandomDimensionOffset
+    uint32_t lensDimOffset; // g_pureLightPathLensRandomDimensionOffset
+    LightNode* nodes;       // [frame][path][vertex]
+    uint32_t* counts;       // [frame][path] stored vertices (0: no header)
+    float* heroes;          // [frame][path]
+    uint32_t* valid;        // [frame][header] path index of each header, ascending
+    uint32_t* validCount;   // [frame] header count
+    const uint32_t* perm;   // [cropW*cropH] pixel permutation (crop-relative indices)
+    unsigned long long* splat; // [frame][crop pixel][3] fixed-point XYZ
+    float3 worldCenter;
+    float worldRadiusSqr;
+};
+
+YG_DEV Luts bdptLuts(const SceneView& S)
+{
+    return Luts{S.lutSS, S.lutSSAvg, S.lutSSMS, S.lutSSMSAvg, S.lutTransDenser, S.lutTransLighter,
+                S.lutTransAvgDenser, S.lutTransAvgLighter, S.lutSheen};
+}
+
+// ------------------------------------------------------------------ densities and ratios
+// solidAngleToAreaDensityMultiplier (commonMath.hlsl)
+YG_DEV float solidAngleToArea(float3 v, float3 n)
+{
+    float invD2 = 1.0f / dot(v, v);
+    return fabsf(dot(n, v * sqrtf(invD2))) * invD2;
+}
+// calculatePDFRatio / accumulateRISum (BDPTCommon.hlsl:555-577)
+YG_DEV float pdfRatio(float nom, float denom)
+{
+    nom = nom < 0.0f ? 1.0f : nom;
+    denom = denom < 0.0f ? 1.0f : denom;
+    return fminf(safeDiv(nom, denom), kMaxPdfRatioSum);
+}
+YG_DEV float accumulateRISum(float riSum, float nom, float denom, bool connectable = true)
+{
+    float ri = pdfRatio(nom, denom);
+    bool acc = connectable && nom > 0.0f && denom > 0.0f;
+    riSum = ri * riSum;
+    if (acc) riSum += ri;
+    return fminf(riSum, kMaxPdfRatioSum);
+}
+// miscBrdf.hlsl:43-67, 108-118
+YG_DEV float3 sampleCosPowHemi(float2 r, float e)
+{
+    float y = ygm_powf(1.0f - r.x, 1.0f / (e + 2.0f));
+    float rr = sqrtf(fmaxf(0.0f, 1.0f - sqr(y)));
+    float sn, cs;
+    ygm_sincosf(2.0f * kPI * r.y, &sn, &cs);
+    return mk3(rr * cs, y, rr * sn);
+}
+YG_DEV float3 sampleCosPowSphere(float2 s, float e)
+{
+    bool flip = s.x < 0.5f;
+    s.x = flip ? s.x * 2.0f : (s.x - 0.5f) * 2.0f;
+    float3 d = sampleCosPowHemi(s, e);
+    d.y = flip ? -d.y : d.y;
+    return d;
+}
+YG_DEV float pdfCosPowHemi(float d, float e) { return (e + 2.0f) * kINVPI * 0.5f * ygm_powf(saturate(d), e + 1.0f); }
+YG_DEV float pdfCosPowSphere(float d, float e) { return (e + 2.0f) * kINVPI * 0.25f * ygm_powf(fabsf(d), e + 1.0f); }
+
+// environmentSelectionPDF / pdfEnvironmentDirection / pdfEnvironmentPosition (lightSampling.hlsl:23-76);
+// ENV_LIGHT_SELECTION_PROBABILITY is 0, so the environment starts light paths only without lights
+YG_DEV float envSelectionPdf(const SceneView& S) { return S.nLights == 0 ? 1.0f : 0.0f; }
+YG_DEV float pdfEnvDirection(float3 d)
+{
+    float c = clampf(d.z, -1.0f, 1.0f);
+    float s = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    return safeDiv(1.0f, 2.0f * kPI * kPI * s);
+}
+YG_DEV float pdfEnvPosition(const BdptParams& B) { return safeDiv(1.0f, kPI * B.worldRadiusSqr); }
+// getSkyBoxColor without an environment map (|dir|) as an unbounded RGB emitter
+YG_DEV float4 skyRadiance(const SceneView& S, const LaunchParams& P, const Spectral& sp, float3 d)
+{
+    float3 col = mk3(fabsf(d.x) * P.envScale, fabsf(d.y) * P.envScale, fabsf(d.z) * P.envScale);
+    return isZero3(col) ? splat4(0.0f) : fromRGBUnbounded(S, sp, col);
+}
+// constructVectorBase (commonMath.hlsl:87-93)
+YG_DEV void vectorBase(float3 v, float3& a, float3& b)
+{
+    if (fabsf(v.x) > fabsf(v.y)) a = mk3(-v.z, 0.0f, v.x) / sqrtf(v.x * v.x + v.z * v.z);
+    else a = mk3(0.0f, v.z, -v.y) / sqrtf(v.y * v.y + v.z * v.z);
+    b = cross(v, a);
+}
+
+// calculateCameraDirectionalPDF (BDPTCommon.hlsl:536-550)
+YG_DEV float cameraDirectionalPdf(const SceneView& S, const LaunchParams& P, float3 v)
+{
+    float4 mn = mul44(S.cam.uvToView, mk4(0.f, 0.f, 0.f, 1.f));
+    float4 mx = mul44(S.cam.uvToView, mk4(1.f, 1.f, 0.f, 1.f));
+    mn = mn / mn.w;
+    mx = mx / mx.w;
+    float ex = fabsf(mx.x - mn.x), ey = fabsf(mx.y - mn.y);
+    float area = safeDiv(ex * ey, mn.z * mn.z);
+    float4 vs = mul44(S.cam.worldToView, mk4(v.x, v.y, v.z, 0.0f));
+    float3 vv = mk3(vs.x, vs.y, vs.z);
+    float c = fabsf(vv.z) * (1.0f / sqrtf(fmaxf(0.0001f, dot(vv, vv))));
+    return safeDiv((float)P.width * (float)P.height, area * c * c * c);
+}
+
+// pdfForSamplingLight (lightSampling.hlsl:191-230) for a point on a mesh light
+YG_DEV void pdfForSamplingLight(const SceneView& S, uint32_t inst, uint32_t prim, float3 n, float3 towards, float& pick,
+                                float& posPdf, float& dirPdf)
+{
+    const GpuInstance& I = S.instances[inst];
+    pick = (1.0f - envSelectionPdf(S)) * I.lightPdf;
+    const GpuMaterial& M = S.materials[I.material];
+    TriGeom g = fetchTri(S, I, prim);
+    float3 p1 = xformPoint(I.o2w, g.p1), p2 = xformPoint(I.o2w, g.p2), p3 = xformPoint(I.o2w, g.p3);
+    float area = length(cross(p2 - p1, p3 - p1)) * 0.5f;
+    posPdf = 1.0f / ((float)I.primCount * area);
+    float c = dot(n, towards);
+    if (M.mask & 1u) dirPdf = pdfCosPowSphere(c, M.emissionFocus);
+    else dirPdf = c >= 0.0f ? pdfCosPowHemi(c, M.emissionFocus) : 0.0f;
+}
+
+// ------------------------------------------------------------------ scattering with both densities
+struct ScatterEval
+{
+    float4 weight;
+    float pdfFwd, pdfBwd;
+    uint32_t transmission;
+};
+
+// evaluateSurfaceAndPDFs (BDPTCommon.hlsl:377-443) without the ray-state update: the forward
+// evaluation, and the density of sampling wo from wi with the frame rebuilt for wi
+YG_DEV ScatterEval evaluateBoth(const Luts& L, const Spectral& sp, const Surface& s, const SurfaceCtx& c, float curIOR,
+                                float prevIOR, float3 wo, float3 wi, bool front, bool fromLight, bool treatAsDelta)
+{
+    ScatterEval r;
+    uint32_t flags = kEvalNone | (fromLight ? kEvalLightPath : 0u) | (treatAsDelta ? kEvalTreatAsDelta : 0u);
+    Eval fwd = evaluateSurface<true>(L, s, c, wo, wi, flags, sp);
+    r.weight = fwd.weight;
+    r.pdfFwd = fwd.pdf;
+    r.transmission = fwd.transmission;
+    bool transmitted = dot(wo, s.geometryNormal) * dot(wi, s.geometryNormal) < 0.0f;
+    SurfaceCtx rc;
+    makeSurfaceCtx(s, curIOR, prevIOR, wi, transmitted ? !front : front, rc);
+    if (transmitted)
+    {
+        rc.fromIOR = c.toIOR;
+        rc.toIOR = c.fromIOR;
+    }
+    r.pdfBwd = evaluateSurface<true>(L, s, rc, wi, wo, kEvalPdfOnly, sp).pdf;
+    return r;
+}
+
+// the ray-state part of evaluateSurfaceAndPDFs; returns whether this event dispersed first
+YG_DEV bool applyTransmission(PathState& st, uint32_t trans, const Surface& s, uint32_t material)
+{
+    bool dispersed = false;
+    if (trans != 0)
+    {
+        if (trans & kTransDispersed)
+        {
+            dispersed = (st.flags & kFlagSecondaryTerminated) == 0;
+            st.flags |= kFlagSecondaryTerminated;
+        }
+        if (trans & kTransExited) exitedVolume(st, material);
+        else if (trans & kTransEntered) enteredVolume(st, s.dielectricIOR, s.absorption, material);
+    }
+    return dispersed;
+}
+
+// absorption of the medium on the far side of a connection: the state applyTransmission
+// would leave, read without changing the path state
+YG_DEV float4 absorptionAfter(const PathState& st, uint32_t trans, const Surface& s, uint32_t material)
+{
+    if (trans & kTransExited)
+    {
+        if (st.nVol == 0) return splat4(0.0f);
+        int index = -1;
+        for (int i = (int)st.nVol - 1; i >= 0; --i)
+            if (st.volMat[i] == material)
+            {
+                index = i;
+                break;
+            }
+        if (index < 0 || index == (int)st.nVol - 1) return st.nVol > 1 ? st.volAbs[st.nVol - 2] : splat4(0.0f);
+        return st.volAbs[st.nVol - 1];
+    }
+    if (trans & kTransEntered) return s.absorption;
+    return st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
+}
+
+YG_DEV float4 transmittance(float4 ab, float d)
+{
+    return mk4(ygm_expf(-ab.x * d), ygm_expf(-ab.y * d), ygm_expf(-ab.z * d), ygm_expf(-ab.w * d));
+}
+
+// sampleScatteringEvent (scatteringSample.hlsl:30-65) for the local lobes; the subsurface
+// lobe ends the path as it does in the unidirectional integrators of this library
+YG_DEV float3 sampleScatter(const Luts& L, const Spectral& sp, const Surface& s, const SurfaceCtx& c, float4 r,
+                            bool& isDiffuse, bool& isDelta)
+{
+    int layer = selectMaterialLayer(r.x, c.probs);
+    isDiffuse = false;
+    isDelta = false;
+    if (layer == LAYER_SSS || layer >= LAYER_COUNT) return mk3(0.f, 0.f, 0.f);
+    return sampleLayerDirection<true>(L, s, c, layer, r.y, make_float2(r.z, r.w), sp.hero, isDiffuse, isDelta);
+}
+
+// calculateCommonSurfaceParams (BDPTCommon.hlsl:653-684) at a ray hit; the regularisation flag
+// of the path state has been set by the caller
+YG_DEV void vertexSurface(const SceneView& S, const LaunchParams& P, const Spectral& sp, const Hit& hit, const GpuInstance& I,
+                          float3 rayDirWS, PathState& st, HitSurface& hs, SurfaceCtx& c)
+{
+    LaunchParams Pn = P;
+    Pn.regularizeAfter = 0xffffffffu;
+    st.pathLength = 0;
+    setupSurface(S, Pn, sp, hit, I, rayDirWS, st, hs);
+    const Surface& s = hs.s;
+    if (dot(hs.rayDirOS, s.geometryNormal) > 0.0f && st.nVol == 0 && !isTwoSided(s.flags))
+        enteredVolume(st, s.dielectricIOR, s.absorption, hs.material);
+    makeSurfaceCtx(s, currentIOR(st), previousIOR(st), -hs.rayDirOS, hit.front, c);
+}
+
+YG_DEV void initState(PathState& st)
+{
+    st.throughput = splat4(1.0f);
+    st.total = splat4(0.0f);
+    st.pdfThisRay = 0.0f;
+    st.flags = 0;
+    st.pathLength = 0;
+    st.nVol = 0;
+}
+
+// ------------------------------------------------------------------ light subpaths
+// sampleLightOrEnv (BDPTCommon.hlsl:697-721) with sampleLight (lightSampling.hlsl:122-188)
+// or sampleEnvironmentLighting (lightSampling.hlsl:78-118)
+YG_DEV bool startLightPath(const SceneView& S, const LaunchParams& P, const BdptParams& B, const Spectral& sp, float pickR,
+                           float4 r0, float2 r1, LightNode& n0, float4& radiance, float3& origin, float3& dir, float& pdfDir,
+                           float& originPosPdf)
+{
+    const float envPdf = envSelectionPdf(S);
+    float4 Le;
+    float3 pos, n;
+    float pdfPos, sel, profile;
+    if (pickR < envPdf)
+    {
+        float st, ct, sph, cph;
+        ygm_sincosf(r0.x * kPI, &st, &ct);
+        ygm_sincosf(r0.y * 2.0f * kPI, &sph, &cph);
+        dir = mk3(st * cph, st * sph, ct);
+        pdfDir = safeDiv(1.0f, 2.0f * kPI * kPI * st);
+        float3 v1, v2;
+        vectorBase(dir, v1, v2);
+        float2 cd = sampleConcentricDisk(make_float2(r0.z, r0.w));
+        float radius = sqrtf(B.worldRadiusSqr);
+        pos = B.worldCenter - dir * radius + (v1 * cd.x + v2 * cd.y) * radius;
+        pdfPos = pdfEnvPosition(B);
+        Le = skyRadiance(S, P, sp, -dir);
+        n = dir;
+        sel = envPdf;
+        profile = 1.0f;
+        n0.instance = 0xffffffffu;
+        n0.prim = 0xffffffffu;
+        n0.flags = NF_ENV;
+    }
+    else
+    {
+        uint32_t li = sampleLightIndex(S, (pickR - envPdf) / (1.0f - envPdf));
+        sel = (1.0f - envPdf) * S.lights[li].selectionPdf;
+        LightPoint lp;
+        sampleMeshLight(S, sp, li, mk3(r0.x, r0.y, r0.z), lp);
+        const GpuInstance& LI = S.instances[lp.instance];
+        float3 tangent = mk3(1.f, 0.f, 0.f);
+        if (LI.hasTangents)
+        {
+            TriGeom g = fetchTri(S, LI, lp.prim);
+            float bx = r0.x, by = r0.y;
+            if (bx + by > 1.0f)
+            {
+                bx = 1.0f - bx;
+                by = 1.0f - by;
+            }
+            float b0 = 1.0f - bx - by;
+            float4 t1 = __ldg(S.tangents + g.i1), t2 = __ldg(S.tangents + g.i2), t3 = __ldg(S.tangents + g.i3);
+            tangent = normalize(mk3(t1.x * t1.w, t1.y * t1.w, t1.z * t1.w) * b0 + mk3(t2.x * t2.w, t2.y * t2.w, t2.z * t2.w) * bx +
+                                mk3(t3.x * t3.w, t3.y * t3.w, t3.z * t3.w) * by);
+        }
+        tangent = normalize(xformVectorT(LI.w2o, tangent));
+        float3 ld = lp.twoSided ? sampleCosPowSphere(r1, lp.focus) : sampleCosPowHemi(r1, lp.focus);
+        pdfDir = lp.twoSided ? pdfCosPowSphere(ld.y, lp.focus) : pdfCosPowHemi(ld.y, lp.focus);
+        profile = evaluateEmissionProfile(ld.y, lp.focus);
+        dir = fromLocal(constructBasis(lp.n, tangent), ld);
+        pos = lp.pos;
+        n = lp.n;
+        pdfPos = lp.pdfPos;
+        Le = lp.radiance;
+        n0.instance = lp.instance;
+        n0.prim = lp.prim;
+        n0.flags = 0;
+    }
+    if (allEqual4(Le, 0.0f) || pdfPos == 0.0f || pdfDir == 0.0f || sel == 0.0f) return false;
+    n0.bary = make_float2(-1.0f, -1.0f);
+    n0.normal = n;
+    n0.radiance = Le;
+    n0.pos = pos;
+    n0.pdfFwd = (n0.flags & NF_ENV) ? pdfDir * sel : pdfPos * sel;
+    n0.pdfBwd = 0.0f;
+    n0.iorPrev = 1.0f;
+    n0.iorCur = 1.0f;
+    n0.pad = 0.0f;
+    originPosPdf = pdfPos;
+    origin = spawnRayOrigin(pos, n, dir);
+    radiance = Le * profile * fabsf(dot(n, dir)) / (sel * pdfPos * pdfDir);
+    return true;
+}
+
+// traceLightRays (BDPTTraceLightPath.comp:6-362): one thread per (sample index, light path)
+__global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const LaunchParams P, BdptParams B)
+{
+    const Luts Lt = bdptLuts(S);
+    const uint32_t total = B.frames * B.lightPaths;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+    {
+        const uint32_t f = t / B.lightPaths, l = t - f * B.lightPaths;
+        LightNode* out = B.nodes + (size_t)t * B.maxLightVerts;
+        RandomSampler rs{S.sobol + (size_t)f * kSobolDims, 2u, l ^ (P.seed * 0x9E3779B9u)};
+        Spectral sp;
+        spectralOf(S, S.lambdaMin + rs.r1() * (S.lambdaMax - S.lambdaMin), sp);
+        B.heroes[t] = sp.hero;
+        B.counts[t] = 0;
+        float4 r0 = rs.r4(), r1 = rs.r4();
+        LightNode nodes[2];
+        float4 radiance;
+        float3 rayOrigin, rayDir;
+        float pdfForward, originPosPdf;
+        if (!startLightPath(S, P, B, sp, r1.w, r0, make_float2(r1.x, r1.y), nodes[0], radiance, rayOrigin, rayDir, pdfForward,
+                            originPosPdf))
+            continue;
+        const bool originEnv = (nodes[0].flags & NF_ENV) != 0;
+        const float maxRadiance = max4(radiance);
+        uint32_t stored = 0;
+        bool prevDelta = false;
+        PathState st;
+        initState(st);
+        for (uint32_t i = 1; i < B.maxLightVerts; ++i)
+        {
+            float4 rv = rs.r4();
+            Hit hit;
+            if (!traceClosest<false>(S, rayOrigin, rayDir, kRayMinT, __int_as_float(0x7f800000), hit, nullptr)) break;
+            LightNode& cur = nodes[i & 1];
+            LightNode& prev = nodes[(i - 1) & 1];
+            const GpuInstance& I = S.instances[hit.instance];
+            if (P.regularizeEnable && i - 1 >= P.regularizeAfter) st.flags |= kFlagRegularize;
+            uint32_t nflags = hit.front ? NF_FRONT : 0u;
+            nflags |= (st.flags & kFlagSecondaryTerminated) ? NF_TERMINATED : 0u;
+            nflags |= (st.flags & kFlagRegularize) ? NF_REGULARIZED : 0u;
+            HitSurface hs;
+            SurfaceCtx c;
+            vertexSurface(S, P, sp, hit, I, rayDir, st, hs, c);
+            const Surface& s = hs.s;
+            if (isDeltaDistribution(c.a2, s)) nflags |= NF_DELTA;
+            float3 normalWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
+            float3 posWS = rayOrigin + rayDir * hit.t;
+            float pdfFwdMIS;
+            if (i == 1 && originEnv) pdfFwdMIS = originPosPdf * fabsf(dot(rayDir, normalWS));
+            else pdfFwdMIS = prevDelta ? -1.0f : pdfForward * solidAngleToArea(posWS - rayOrigin, normalWS);
+            float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
+            if (!allEqual4(ab, 0.0f)) radiance = radiance * transmittance(ab, hit.t);
+            cur.instance = hit.instance;
+            cur.prim = hit.prim;
+            cur.bary = make_float2(hit.b1, hit.b2);
+            cur.normal = normalWS;
+            cur.radiance = radiance;
+            cur.pos = posWS;
+            cur.pdfFwd = pdfFwdMIS;
+            cur.pdfBwd = 0.0f;
+            cur.iorPrev = previousIOR(st);
+            cur.iorCur = currentIOR(st);
+            cur.flags = nflags;
+            cur.pad = 0.0f;
+            bool isDiffuse, sDelta;
+            float3 wo = -hs.rayDirOS;
+            float3 wi = sampleScatter(Lt, sp, s, c, rv, isDiffuse, sDelta);
+            if (isZero3(wi)) break;
+            if (isDiffuse) st.flags |= kFlagRegularize;
+            ScatterEval ev = evaluateBoth(Lt, sp, s, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, true, sDelta);
+            bool dispersed = applyTransmission(st, ev.transmission, s, hs.material);
+            pdfForward = ev.pdfFwd;
+            float4 w = ev.weight * safeDiv(1.0f, pdfForward);
+            prev.pdfBwd = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - posWS, prev.normal);
+            if (i == 1 && originEnv && !sDelta) prev.pdfBwd = ev.pdfBwd;
+            out[stored++] = prev;
+            radiance = radiance * w;
+            if (dispersed) terminateSecondary(radiance);
+            // applyRussianRoulette normalised by the emitted radiance
+            float p = clampf(max4(radiance) / maxRadiance, 0.05f, 1.0f);
+            if (rs.r1() > p) break;
+            radiance = radiance * (1.0f / p);
+            if (allEqual4(radiance, 0.0f)) break;
+            rayDir = normalize(xformVectorT(I.w2o, wi));
+            rayOrigin = spawnRayOrigin(posWS, normalWS, rayDir);
+            prevDelta = sDelta;
+        }
+        // the last vertex reached (BDPTTraceLightPath.comp:335-352)
+        out[stored] = nodes[stored & 1];
+        B.counts[t] = stored + 1;
+    }
+}
+
+// per sample index, the light paths that stored vertices in ascending index order (the headers)
+__global__ void __launch_bounds__(1024) bdptHeaders(BdptParams B)
+{
+    const uint32_t f = blockIdx.x;
+    const uint32_t* cnt = B.counts + (size_t)f * B.lightPaths;
+    uint32_t* out = B.valid + (size_t)f * B.lightPaths;
+    __shared__ uint32_t warpSums[32];
+    __shared__ uint32_t base;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t c0 = 0; c0 < B.lightPaths; c0 += blockDim.x)
+    {
+        uint32_t i = c0 + threadIdx.x;
+        uint32_t v = (i < B.lightPaths && cnt[i] > 0) ? 1u : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) warpSums[w] = x;
+        __syncthreads();
+        if (w == 0)
+        {
+            uint32_t s = lane < nw ? warpSums[lane] : 0u;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= (uint32_t)o) s += y;
+            }
+            warpSums[lane] = s;
+        }
+        __syncthreads();
+        uint32_t excl = base + (w ? warpSums[w - 1] : 0u) + x - v;
+        if (v) out[excl] = i;
+        uint32_t blockTotal = warpSums[nw - 1];
+        __syncthreads();
+        if (threadIdx.x == 0) base += blockTotal;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) B.validCount[f] = base;
+}
+
+// ------------------------------------------------------------------ camera subpaths + connections
+// ExtractedLightPathNodeData (BDPTCommon.hlsl:69-74) with the spectral surface and the forward
+// shading frame of the vertex, which depend only on the light path
+struct SharedNode
+{
+    LightNode n;
+    Surface s;
+    SurfaceCtx c;
+    float4 w2o[3];
+    float3 woOS;
+    uint32_t material;
+    float emissionFocus;
+    uint32_t twoSided;
+};
+
+YG_DEV void prepareSharedNode(const SceneView& S, const LaunchParams& P, const Spectral& sp, const LightNode& src,
+                              float3 prevPos, uint32_t index, SharedNode& d)
+{
+    d.n = src;
+    if (src.flags & NF_ENV) return;
+    const GpuInstance& I = S.instances[src.instance];
+    d.w2o[0] = I.w2o[0];
+    d.w2o[1] = I.w2o[1];
+    d.w2o[2] = I.w2o[2];
+    d.material = I.material;
+    const GpuMaterial& M = S.materials[I.material];
+    d.emissionFocus = M.emissionFocus;
+    d.twoSided = M.mask & 1u;
+    if (index == 0) return;
+    // fillSurfaceDefRGB + regularizeMaterial + convertSurfaceDefinitionFromRGB, no two-sided
+    // orientation (BDPTCommon.hlsl:845-869)
+    Hit h;
+    h.instance = src.instance;
+    h.prim = src.prim;
+    h.b1 = src.bary.x;
+    h.b2 = src.bary.y;
+    h.front = (src.flags & NF_FRONT) != 0;
+    h.t = 0.0f;
+    PathState st;
+    initState(st);
+    if (src.flags & NF_REGULARIZED) st.flags |= kFlagRegularize;
+    LaunchParams Pn = P;
+    Pn.regularizeAfter = 0xffffffffu;
+    HitSurface hs;
+    setupSurface(S, Pn, sp, h, I, src.normal, st, hs, false);
+    d.s = hs.s;
+    float3 lpos = xformPoint(I.w2o, src.pos);
+    float3 ppos = xformPoint(I.w2o, prevPos);
+    d.woOS = normalize(ppos - lpos);
+    makeSurfaceCtx(d.s, src.iorCur, src.iorPrev, d.woOS, h.front, d.c);
+}
+
+// calculateConnectingLightNodeWeightsAndPDFs (BDPTCommon.hlsl:725-876) for the light end of a
+// connection to nextPos; returns false when the connection carries nothing
+YG_DEV bool lightEndOfConnection(const SceneView& S, const BdptParams& B, const Luts& Lt, const Spectral& sp,
+                                 const SharedNode& sn, uint32_t index, float3 nextPos, bool alreadyTerminated,
+                                 ScatterEval& ev, float& pdfFwdMIS)
+{
+    const LightNode& n = sn.n;
+    ev.weight = splat4(0.0f);
+    ev.pdfFwd = 0.0f;
+    ev.pdfBwd = 0.0f;
+    ev.transmission = 0;
+    if (index == 0 && (n.flags & NF_ENV))
+    {
+        float pdfDir = envSelectionPdf(S) * pdfEnvDirection(n.normal);
+        if (pdfDir <= 0.0f)
+        {
+            pdfFwdMIS = 0.0f;
+            return false;
+        }
+        ev.pdfFwd = pdfDir;
+        ev.weight = splat4(1.0f / pdfDir);
+        pdfFwdMIS = pdfEnvPosition(B);
+        return true;
+    }
+    if (index == 0)
+    {
+        float3 fromLight = nextPos - n.pos;
+        if (dot(fromLight, n.normal) <= 0.0f && !sn.twoSided)
+        {
+            pdfFwdMIS = 0.0f;
+            return false;
+        }
+        ev.pdfFwd = n.pdfFwd * (1.0f / solidAngleToArea(-fromLight, n.normal));
+        float cosE = dot(n.normal, normalize(fromLight));
+        ev.weight = splat4(safeDiv(evaluateEmissionProfile(cosE, sn.emissionFocus), ev.pdfFwd));
+        pdfFwdMIS = sn.twoSided ? pdfCosPowSphere(cosE, sn.emissionFocus)
+                                : (cosE >= 0.0f ? pdfCosPowHemi(cosE, sn.emissionFocus) : 0.0f);
+        return true;
+    }
+    float3 lpos = xformPoint(sn.w2o, n.pos);
+    float3 cpos = xformPoint(sn.w2o, nextPos);
+    float3 wi = normalize(cpos - lpos);
+    bool front = (n.flags & NF_FRONT) != 0;
+    ev = evaluateBoth(Lt, sp, sn.s, sn.c, n.iorCur, n.iorPrev, sn.woOS, wi, front, true, false);
+    bool terminated = alreadyTerminated || (n.flags & NF_TERMINATED);
+    if ((ev.transmission & kTransDispersed) && !terminated) terminateSecondary(ev.weight);
+    pdfFwdMIS = ev.pdfFwd;
+    return !(ev.pdfBwd == 0.0f || allEqual4(ev.weight, 0.0f));
+}
+
+struct CamVertex
+{
+    float3 pos, normal, prevPos, prevNormal;
+    float pdfRatioSum, prevPdfFwd, curPdfFwd;
+};
+struct LightVertexCtx
+{
+    float3 prevPos, prevNormal;
+    float prevPdfFwd, riSum;
+    uint32_t originFlags;
+};
+
+// calculateMISWeight (BDPTCommon.hlsl:918-1006)
+YG_DEV float misWeight(const SceneView& S, uint32_t camIndex, const CamVertex& cv, uint32_t lightIndex,
+                       const LightVertexCtx& lv, const LightNode& ln, float fwdCam, float bwdCam, float fwdLight, float bwdLight)
+{
+    float riCam = cv.pdfRatioSum;
+    if (camIndex > 0)
+        riCam = accumulateRISum(riCam, bwdCam * solidAngleToArea(cv.prevPos - cv.pos, cv.prevNormal), cv.prevPdfFwd);
+    const bool env0 = lightIndex == 0 && (ln.flags & NF_ENV);
+    float toCamArea = env0 ? fwdLight * fabsf(dot(cv.normal, ln.normal)) : fwdLight * solidAngleToArea(cv.pos - ln.pos, cv.normal);
+    riCam = accumulateRISum(riCam, toCamArea, cv.curPdfFwd);
+    float riLight = lv.riSum;
+    if (lightIndex == 0)
+    {
+        float pick, posPdf, dirPdf, toLight;
+        if (env0)
+        {
+            pick = envSelectionPdf(S);
+            posPdf = pdfEnvDirection(ln.normal);
+            toLight = fwdCam;
+        }
+        else
+        {
+            float3 camToLight = ln.pos - cv.pos;
+            float len = length(camToLight);
+            pdfForSamplingLight(S, ln.instance, ln.prim, ln.normal, -camToLight / len, pick, posPdf, dirPdf);
+            toLight = fwdCam * solidAngleToArea(camToLight, ln.normal);
+        }
+        riLight = pdfRatio(toLight, pick * posPdf);
+    }
+    else
+    {
+        float bwdPrev = bwdLight;
+        bool prevEnv = lightIndex == 1 && (lv.originFlags & NF_ENV);
+        if (!prevEnv) bwdPrev *= solidAngleToArea(lv.prevPos - ln.pos, lv.prevNormal);
+        riLight = accumulateRISum(riLight, bwdPrev, lv.prevPdfFwd);
+        riLight = accumulateRISum(riLight, fwdCam * solidAngleToArea(ln.pos - cv.pos, ln.normal), ln.pdfFwd);
+    }
+    return 1.0f / (1.0f + riCam + riLight);
+}
+
+// traceCameraRays (BDPTTraceCameraPath.comp:40-432): one block per camera group of 64
+// permuted pixels sharing one light subpath
+__global__ void __launch_bounds__(kGroupSize) bdptCamera(const SceneView S, const LaunchParams P, BdptParams B)
+{
+    __shared__ SharedNode nodes[kBdptMaxLightVertices];
+    __shared__ uint32_t sCount, sPath;
+    __shared__ float sHero;
+    const Luts Lt = bdptLuts(S);
+    const uint32_t f = blockIdx.y, g = blockIdx.x;
+    const uint64_t cropPix = (uint64_t)P.cropW * P.cropH;
+    const uint64_t slot = (uint64_t)g * kGroupSize + threadIdx.x;
+    const bool active = slot < cropPix;
+    const uint32_t pix = active ? B.perm[slot] : 0u;
+    const uint32_t px = P.cropX + pix % P.cropW, py = P.cropY + pix / P.cropW;
+    const uint32_t* point = S.sobol + (size_t)f * kSobolDims;
+    const uint32_t seed = (py * P.width + px) ^ (P.seed * 0x9E3779B9u);
+    RandomSampler rs{point, B.camDimOffset + 2u, seed};
+    float2 lensR = rs.r2();
+    if (threadIdx.x == 0)
+    {
+        uint32_t hc = B.validCount[f];
+        if (hc == 0)
+        {
+            sCount = 0;
+            sPath = 0;
+            sHero = S.lambdaMin + rs.r1() * (S.lambdaMax - S.lambdaMin);
+        }
+        else
+        {
+            RandomSampler rt{point, 2u, g ^ (P.seed * 0x9E3779B9u)};
+            uint32_t h = (uint32_t)fminf(floorf(rt.r1() * (float)hc), (float)(hc - 1u));
+            uint32_t l = B.valid[(size_t)f * B.lightPaths + h];
+            sPath = l;
+            sCount = B.counts[(size_t)f * B.lightPaths + l];
+            sHero = B.heroes[(size_t)f * B.lightPaths + l];
+        }
+    }
+    __syncthreads();
+    const uint32_t count = sCount;
+    Spectral sp;
+    spectralOf(S, sHero, sp);
+    if (threadIdx.x < count)
+    {
+        const LightNode* src = B.nodes + ((size_t)f * B.lightPaths + sPath) * B.maxLightVerts;
+        uint32_t k = threadIdx.x;
+        prepareSharedNode(S, P, sp, src[k], k ? src[k - 1].pos : src[0].pos, k, nodes[k]);
+    }
+    __syncthreads();
+    if (!active) return;
+
+    // generateCameraRay (raytraceCommonResources.hlsl:113-137) with the group's wavelength
+    float invW = 1.0f / (float)P.width, invH = 1.0f / (float)P.height;
+    float2 uv = make_float2((float)px * invW + 0.5f * invW, (float)py * invH + 0.5f * invH);
+    float2 texel = make_float2(sampleDim(point, 0, seed), sampleDim(point, 1, seed));
+    float2 to = make_float2(0.f, 0.f);
+    if ((P.flags & 2u) == 0) to = make_float2(texel.x - 0.5f, texel.y - 0.5f);
+    to = make_float2(to.x * invW, to.y * invH);
+    float4 pn = mul44(S.cam.uvToView, mk4(uv.x + to.x, uv.y + to.y, 0.0f, 1.0f));
+    pn = pn / pn.w;
+    float3 pin = mk3(pn.x, pn.y, pn.z);
+    float3 focusP = pin * safeDiv(S.cam.focusDistance, fabsf(pin.z));
+    float2 disk = sampleConcentricDisk(lensR);
+    float3 lensP = mk3(disk.x * S.cam.apertureRadius, disk.y * S.cam.apertureRadius, 0.0f);
+    float4 ow = mul44(S.cam.viewToWorld, mk4(lensP.x, lensP.y, lensP.z, 1.0f));
+    float4 dw = mul44(S.cam.viewToWorld, mk4(focusP.x - lensP.x, focusP.y - lensP.y, focusP.z - lensP.z, 0.0f));
+    float3 rayOrigin = mk3(ow.x, ow.y, ow.z);
+    float3 rayDir = normalize(mk3(dw.x, dw.y, dw.z));
+
+    float4 total = splat4(0.0f);
+    FirstHit fh;
+    fh.albedo = mk3(0.f, 0.f, 0.f);
+    fh.normal = mk3(0.f, 0.f, 0.f);
+    fh.depth = 0.0f;
+    PathState st;
+    initState(st);
+    CamVertex cv;
+    cv.pdfRatioSum = 0.0f;
+    cv.prevPdfFwd = 0.0f;
+    cv.prevPos = mk3(0.f, 0.f, 0.f);
+    cv.prevNormal = mk3(0.f, 0.f, 0.f);
+    float pdfFwdCam = cameraDirectionalPdf(S, P, rayDir);
+    float deferredRI = 0.0f;
+    for (uint32_t ci = 0; ci < P.maxDepth; ++ci)
+    {
+        Hit hit;
+        bool found = traceClosest<false>(S, rayOrigin, rayDir, kRayMinT, __int_as_float(0x7f800000), hit, nullptr);
+        float4 rv = rs.r4();
+        if (!found)
+        {
+            // calculateMISWeightOnCameraPathMissing (BDPTCommon.hlsl:1039-1059)
+            cv.curPdfFwd = pdfFwdCam;
+            float mis = 1.0f;
+            if (ci > 0)
+            {
+                float ri = accumulateRISum(cv.pdfRatioSum, pdfEnvPosition(B) * fabsf(dot(cv.prevNormal, rayDir)), cv.prevPdfFwd);
+                ri = accumulateRISum(ri, envSelectionPdf(S) * pdfEnvDirection(-rayDir), cv.curPdfFwd);
+                mis = 1.0f / (1.0f + ri);
+            }
+            total = total + st.throughput * skyRadiance(S, P, sp, rayDir) * mis;
+            break;
+        }
+        const GpuInstance& I = S.instances[hit.instance];
+        if (P.regularizeEnable && ci >= P.regularizeAfter) st.flags |= kFlagRegularize;
+        HitSurface hs;
+        SurfaceCtx c;
+        vertexSurface(S, P, sp, hit, I, rayDir, st, hs, c);
+        const Surface& s = hs.s;
+        cv.pos = rayOrigin + rayDir * hit.t;
+        cv.normal = normalize(xformVectorT(I.w2o, s.geometryNormal));
+        const float3 wo = -hs.rayDirOS;
+        if (ci == 0)
+        {
+            fh.albedo = hs.albedoRGB;
+            fh.normal = normalize(xformVectorT(I.w2o, s.baseLayerNormal));
+            float4 vp = mul44(S.cam.worldToView, mk4(cv.pos.x, cv.pos.y, cv.pos.z, 1.0f));
+            fh.depth = vp.z * S.cam.forwardZSign;
+        }
+        const bool delta = isDeltaDistribution(c.a2, s);
+        cv.curPdfFwd = pdfFwdCam < 0.0f ? -1.0f : pdfFwdCam * solidAngleToArea(cv.pos - rayOrigin, cv.normal);
+        float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
+        if (!allEqual4(ab, 0.0f)) st.throughput = st.throughput * transmittance(ab, hit.t);
+        if (!allEqual4(s.emissive, 0.0f))
+        {
+            // calculateMISWeightOnCameraPathHittingLight (BDPTCommon.hlsl:1008-1035)
+            float mis = 1.0f;
+            if (ci > 0)
+            {
+                float3 towards = cv.prevPos - cv.pos;
+                float pick, posPdf, dirPdf;
+                pdfForSamplingLight(S, hit.instance, hit.prim, cv.normal, normalize(towards), pick, posPdf, dirPdf);
+                float ri = accumulateRISum(cv.pdfRatioSum, dirPdf * solidAngleToArea(towards, cv.prevNormal), cv.prevPdfFwd);
+                ri = accumulateRISum(ri, pick * posPdf, cv.curPdfFwd);
+                mis = 1.0f / (1.0f + ri);
+            }
+            if (isTwoSided(s.flags) || dot(s.geometryNormal, wo) > 0.0f)
+            {
+                float profile = evaluateEmissionProfile(dot(cv.normal, -rayDir), s.emissionFocus);
+                total = total + st.throughput * s.emissive * mis * profile;
+            }
+            break;
+        }
+        if (!delta && !allEqual4(st.throughput, 0.0f))
+        {
+            // connect to every vertex of the group's light path (BDPTTraceCameraPath.comp:240-282)
+            LightVertexCtx lv;
+            lv.riSum = 0.0f;
+            lv.originFlags = 0;
+            lv.prevPos = mk3(0.f, 0.f, 0.f);
+            lv.prevNormal = mk3(0.f, 0.f, 0.f);
+            lv.prevPdfFwd = 0.0f;
+            float deferredLight = 0.0f;
+            const bool camTerminated = (st.flags & kFlagSecondaryTerminated) != 0;
+            for (uint32_t li = 0; li < count; ++li)
+            {
+                const SharedNode& sn = nodes[li];
+                const LightNode& ln = sn.n;
+                if (!(ln.flags & NF_DELTA))
+                {
+                    // getLightNodeConnection + calculateLightPathRadiance (BDPTCommon.hlsl:622-635, 1062-1215)
+                    const bool atInfinity = li == 0 && (ln.flags & NF_ENV);
+                    float3 toLightDir;
+                    float dist;
+                    if (atInfinity)
+                    {
+                        toLightDir = -ln.normal;
+                        dist = __int_as_float(0x7f800000);
+                    }
+                    else
+                    {
+                        float3 toLight = ln.pos - cv.pos;
+                        dist = length(toLight);
+                        toLightDir = toLight / dist;
+                    }
+                    const float3 wi = normalize(xformVector(I.w2o, toLightDir));
+                    const bool lightTerminated = (ln.flags & NF_TERMINATED) != 0;
+                    const bool terminatedBefore = camTerminated || lightTerminated;
+                    ScatterEval ce = evaluateBoth(Lt, sp, s, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, false, false);
+                    if ((ce.transmission & kTransDispersed) && !terminatedBefore) terminateSecondary(ce.weight);
+                    if (ce.pdfFwd != 0.0f && !allEqual4(ce.weight, 0.0f))
+                    {
+                        const bool terminatedNow = terminatedBefore || (ce.transmission & kTransDispersed);
+                        ScatterEval le;
+                        float fwdLight;
+                        if (lightEndOfConnection(S, B, Lt, sp, sn, li, cv.pos, terminatedNow, le, fwdLight))
+                        {
+                            float3 start = spawnRayOrigin(cv.pos, cv.normal, toLightDir);
+                            Hit vh;
+                            float tmax = atInfinity ? __int_as_float(0x7f800000) : kRayMinT + dist + kVisibilityEps;
+                            bool any = traceClosest<false>(S, start, toLightDir, kRayMinT, tmax, vh, nullptr);
+                            bool visible = atInfinity ? !any : (any && vh.instance == ln.instance && vh.prim == ln.prim);
+                            if (visible)
+                            {
+                                float mis = misWeight(S, ci, cv, li, lv, ln, ce.pdfFwd, ce.pdfBwd, fwdLight, le.pdfBwd);
+                                float G = li > 0 ? 1.0f / (dist * dist) : 1.0f;
+                                float4 wc = ce.weight;
+                                if (!atInfinity)
+                                {
+                                    float4 cab = absorptionAfter(st, ce.transmission, s, hs.material);
+                                    if (!allEqual4(cab, 0.0f)) wc = wc * transmittance(cab, dist);
+                                }
+                                float4 r = le.weight * wc * st.throughput * ln.radiance * G * mis;
+                                if (camTerminated && lightTerminated) r.x *= 0.25f; // undoSecondaryWavelengthRescale
+                                total = total + r;
+                            }
+                        }
+                    }
+                }
+                lv.riSum = deferredLight;
+                deferredLight = accumulateRISum(deferredLight, ln.pdfBwd, ln.pdfFwd);
+                lv.prevNormal = ln.normal;
+                lv.prevPos = ln.pos;
+                lv.prevPdfFwd = ln.pdfFwd;
+                if (li == 0) lv.originFlags = ln.flags;
+            }
+        }
+        bool isDiffuse, sDelta;
+        float3 wiS = sampleScatter(Lt, sp, s, c, rv, isDiffuse, sDelta);
+        if (isZero3(wiS)) break;
+        if (isDiffuse) st.flags |= kFlagRegularize;
+        ScatterEval ev = evaluateBoth(Lt, sp, s, c, currentIOR(st), previousIOR(st), wo, wiS, hit.front, false, sDelta);
+        bool dispersed = applyTransmission(st, ev.transmission, s, hs.material);
+        float4 w = ev.weight * safeDiv(1.0f, ev.pdfFwd);
+        if (dispersed) terminateSecondary(st.throughput);
+        if (russianRoulette(st.throughput, rs.r1())) break;
+        if (ci > 0)
+        {
+            float bwdPrev = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - cv.pos, cv.prevNormal);
+            deferredRI = accumulateRISum(deferredRI, bwdPrev, cv.prevPdfFwd);
+            cv.pdfRatioSum = deferredRI;
+        }
+        cv.prevNormal = cv.normal;
+        cv.prevPos = cv.pos;
+        cv.prevPdfFwd = cv.curPdfFwd;
+        pdfFwdCam = sDelta ? -1.0f : ev.pdfFwd;
+        st.throughput = st.throughput * w;
+        rayDir = normalize(xformVectorT(I.w2o, wiS));
+        rayOrigin = spawnRayOrigin(cv.pos, cv.normal, rayDir);
+    }
+    const uint64_t idx = (uint64_t)f * cropPix + pix;
+    float3 X = toXYZ(S, sp, total);
+    P.sampleXYZ[idx] = mk4(X.x, X.y, X.z, 1.0f);
+    if (P.dump)
+    {
+        float* d = P.dump + idx * 8;
+        d[0] = sp.hero;
+        d[1] = total.x;
+        d[2] = total.y;
+        d[3] = total.z;
+        d[4] = total.w;
+        d[5] = X.x;
+        d[6] = X.y;
+        d[7] = X.z;
+    }
+    if (P.featAlbedo)
+    {
+        P.featAlbedo[idx] = mk4(fh.albedo.x, fh.albedo.y, fh.albedo.z, 0.0f);
+        P.featNormalDepth[idx] = mk4(fh.normal.x, fh.normal.y, fh.normal.z, fh.depth);
+    }
+}
+
+// ------------------------------------------------------------------ light tracing to the lens (t = 1)
+// calculatePureLightPaths (BDPTCalculatePureLightPaths.comp:107-206): one thread per header
+__global__ void __launch_bounds__(128) bdptLightTrace(const SceneView S, const LaunchParams P, BdptParams B)
+{
+    const Luts Lt = bdptLuts(S);
+    const uint32_t total = B.frames * B.lightPaths;
+    const uint64_t cropPix = (uint64_t)P.cropW * P.cropH;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+    {
+        const uint32_t f = t / B.lightPaths, h = t - f * B.lightPaths;
+        const uint32_t hc = B.validCount[f];
+        if (h >= hc) continue;
+        const uint32_t l = B.valid[(size_t)f * B.lightPaths + h];
+        const uint32_t vCount = B.counts[(size_t)f * B.lightPaths + l];
+        if (vCount <= 1) continue;
+        Spectral sp;
+        spectralOf(S, B.heroes[(size_t)f * B.lightPaths + l], sp);
+        const LightNode* nodes = B.nodes + ((size_t)f * B.lightPaths + l) * B.maxLightVerts;
+        RandomSampler lr{S.sobol + (size_t)f * kSobolDims, B.lensDimOffset + 2u, h ^ (P.seed * 0x9E3779B9u)};
+        float2 disk = sampleConcentricDisk(lr.r2());
+        float3 lensVS = mk3(disk.x * S.cam.apertureRadius, disk.y * S.cam.apertureRadius, 0.0f);
+        float4 lw = mul44(S.cam.viewToWorld, mk4(lensVS.x, lensVS.y, lensVS.z, 1.0f));
+        float3 lensWS = mk3(lw.x, lw.y, lw.z);
+        LightNode n0 = nodes[0];
+        float3 prevPos = n0.pos, prevNormal = n0.normal;
+        float prevPdfFwd = n0.pdfFwd;
+        const uint32_t originFlags = n0.flags;
+        float riSum = 0.0f;
+        float deferred = accumulateRISum(0.0f, n0.pdfBwd, n0.pdfFwd);
+        for (uint32_t i = 1; i < vCount; ++i)
+        {
+            LightNode n = nodes[i];
+            // projectThroughLensToUV (raytraceCommonResources.hlsl:140-160)
+            float4 pv = mul44(S.cam.worldToView, mk4(n.pos.x, n.pos.y, n.pos.z, 1.0f));
+            float3 lensToPos = mk3(pv.x, pv.y, pv.z) - lensVS;
+            float fwd = lensToPos.z * S.cam.forwardZSign;
+            bool onScreen = false;
+            uint32_t tx = 0, ty = 0;
+            if (fwd > 0.0f)
+            {
+                float3 fp = lensVS + lensToPos * (S.cam.focusDistance / fwd);
+                float4 us = mul44(S.cam.viewToUV, mk4(fp.x, fp.y, fp.z, 1.0f));
+                float u = us.x / us.w, v = us.y / us.w;
+                onScreen = u >= 0.0f && v >= 0.0f && u <= 1.0f && v <= 1.0f;
+                tx = (uint32_t)floorf(fminf(saturate(u) * (float)P.width, (float)P.width - 1.0f));
+                ty = (uint32_t)floorf(fminf(saturate(v) * (float)P.height, (float)P.height - 1.0f));
+            }
+            bool inCrop = tx >= P.cropX && tx < P.cropX + P.cropW && ty >= P.cropY && ty < P.cropY + P.cropH;
+            if (onScreen && inCrop && !(n.flags & NF_DELTA))
+            {
+                SharedNode sn;
+                prepareSharedNode(S, P, sp, n, prevPos, i, sn);
+                ScatterEval ev;
+                float unused;
+                if (lightEndOfConnection(S, B, Lt, sp, sn, i, lensWS, false, ev, unused) && !isZero4(ev.weight))
+                {
+                    float3 toLens = lensWS - n.pos;
+                    float len = length(toLens);
+                    bool visible = true;
+                    if (len >= 0.0001f)
+                    {
+                        Hit vh;
+                        visible = !traceClosest<false>(S, n.pos, toLens / len, 0.01f, len, vh, nullptr);
+                    }
+                    if (visible)
+                    {
+                        bool prevEnv = i == 1 && (originFlags & NF_ENV);
+                        float bwdPrev = ev.pdfBwd * (prevEnv ? 1.0f : solidAngleToArea(prevPos - n.pos, prevNormal));
+                        float3 camToNode = n.pos - lensWS;
+                        float pdfCam = cameraDirectionalPdf(S, P, camToNode);
+                        float ri = accumulateRISum(riSum, bwdPrev, prevPdfFwd);
+                        ri = accumulateRISum(ri, pdfCam * solidAngleToArea(camToNode, n.normal), n.pdfFwd);
+                        float mis = 1.0f / (1.0f + ri);
+                        float G = 1.0f / fmaxf(0.0001f, dot(camToNode, camToNode));
+                        float importance = safeDiv(pdfCam, (float)hc);
+                        float4 contrib = n.radiance * ev.weight * mis * G * importance;
+                        float3 X = toXYZ(S, sp, contrib);
+                        unsigned long long* dst =
+                            B.splat + 3 * ((uint64_t)f * cropPix + (uint64_t)(ty - P.cropY) * P.cropW + (tx - P.cropX));
+                        const float xs[3] = {X.x, X.y, X.z};
+                        for (int k = 0; k < 3; ++k)
+                        {
+                            // splat XYZ is non-negative; the fixed-point sum holds 2^39 per pixel
+                            double q = (double)xs[k] * kSplatScale;
+                            if (q > 0.0 && q < 9.0e18) atomicAdd(dst + k, (unsigned long long)llrint(q));
+                        }
+                    }
+                }
+            }
+            riSum = deferred;
+            deferred = accumulateRISum(deferred, n.pdfBwd, n.pdfFwd);
+            prevPos = n.pos;
+            prevNormal = n.normal;
+            prevPdfFwd = n.pdfFwd;
+        }
+    }
+}
+
+// accumulatePureLightPaths (BDPTAccumulatePureLightPaths.comp:7-31): adds the splats of each
+// sample index to its sample image
+__global__ void bdptResolveSplats(const LaunchParams P, BdptParams B)
+{
+    const uint64_t n = (uint64_t)B.frames * P.cropW * P.cropH;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const unsigned long long* s = B.splat + 3 * i;
+        unsigned long long a = s[0], b = s[1], c = s[2];
+        if ((a | b | c) == 0ull) continue;
+        float4 v = P.sampleXYZ[i];
+        v.x += (float)((double)a / kSplatScale);
+        v.y += (float)((double)b / kSplatScale);
+        v.z += (float)((double)c / kSplatScale);
+        P.sampleXYZ[i] = v;
+        if (P.dump)
+        {
+            P.dump[i * 8 + 5] = v.x;
+            P.dump[i * 8 + 6] = v.y;
+            P.dump[i * 8 + 7] = v.z;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host side
+namespace
+{
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+} // namespace
+
+size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVerts, uint64_t cropPixels)
+{
+    size_t b = align256((size_t)frames * lightPaths * maxLightVerts * sizeof(LightNode));
+    b += 3 * align256((size_t)frames * lightPaths * 4);
+    b += align256((size_t)frames * 4);
+    b += align256((size_t)frames * cropPixels * 24);
+    return b;
+}
+
+int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uint32_t* perm, uint32_t lightPaths,
+               uint32_t maxLightVerts, float3 worldCenter, float worldRadiusSqr, int smCount, cudaStream_t stream)
+{
+    BdptParams B;
+    const uint64_t cropPix = (uint64_t)P.cropW * P.cropH;
+    B.frames = P.sppCount;
+    B.lightPaths = lightPaths;
+    B.maxLightVerts = maxLightVerts;
+    B.groups = (uint32_t)((cropPix + kGroupSize - 1) / kGroupSize);
+    B.camDimOffset = maxLightVerts * 5 + 12;
+    B.lensDimOffset = maxLightVerts * 5 + 9;
+    B.perm = perm;
+    B.worldCenter = worldCenter;
+    B.worldRadiusSqr = worldRadiusSqr;
+    char* p = static_cast<char*>(arena);
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += align256(bytes);
+        return r;
+    };
+    B.nodes = reinterpret_cast<LightNode*>(take((size_t)B.frames * lightPaths * maxLightVerts * sizeof(LightNode)));
+    B.counts = reinterpret_cast<uint32_t*>(take((size_t)B.frames * lightPaths * 4));
+    B.heroes = reinterpret_cast<float*>(take((size_t)B.frames * lightPaths * 4));
+    B.valid = reinterpret_cast<uint32_t*>(take((size_t)B.frames * lightPaths * 4));
+    B.validCount = reinterpret_cast<uint32_t*>(take((size_t)B.frames * 4));
+    B.splat = reinterpret_cast<unsigned long long*>(take((size_t)B.frames * cropPix * 24));
+    cudaMemsetAsync(B.splat, 0, (size_t)B.frames * cropPix * 24, stream);
+    const uint32_t lp = B.frames * lightPaths;
+    int lb = (int)std::min<uint64_t>((lp + 127) / 128, (uint64_t)smCount * 16);
+    bdptLightPaths<<<lb, 128, 0, stream>>>(S, P, B);
+    bdptHeaders<<<B.frames, 1024, 0, stream>>>(B);
+    bdptCamera<<<dim3(B.groups, B.frames), kGroupSize, 0, stream>>>(S, P, B);
+    bdptLightTrace<<<lb, 128, 0, stream>>>(S, P, B);
+    int rb = (int)std::min<uint64_t>((B.frames * cropPix + 255) / 256, (uint64_t)smCount * 8);
+    bdptResolveSplats<<<rb, 256, 0, stream>>>(P, B);
+    return 5;
+}
+
+} // namespace yg

@@ -99,8 +99,11 @@ struct yg_context
     DevBuf dTris, dNodes, dInst, dMat, dLights, dPos, dNrm, dTan, dUV, dIdx, dSpec;
     DevBuf dLut[9];
     DevBuf dCie, dRgb, dSobol, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
-    DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena;
+    DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena, dPerm;
     uint32_t nLights = 0;
+    float worldCenter[3] = {0, 0, 0}; // getWorldCenterAndRadiusSqr (raytraceCommonResources.hlsl:99-104)
+    float worldRadiusSqr = 0;
+    uint32_t permW = 0, permH = 0;    // size of the BDPT pixel permutation in dPerm
     int cieLmin = -1, cieLmax = -1;
     uint32_t cieN = 0;
     float cieYSumInv = 0, d65SumInv = 0;
@@ -115,7 +118,7 @@ struct yg_context
     {
         DevBuf* all[] = {&dTris, &dNodes, &dInst, &dMat, &dLights, &dPos, &dNrm, &dTan, &dUV, &dIdx, &dSpec, &dCie, &dRgb,
                          &dSobol, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
-                         &dFilmComp, &dAccA, &dAccN, &dArena};
+                         &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm};
         for (DevBuf* b : all) b->release();
         for (auto& b : dLut) b.release();
         if (evStart) cudaEventDestroy(evStart);
@@ -621,6 +624,26 @@ YG_API int yg_build_scene(yg_context* ctx)
             gi[lightInst[l]].lightPdf = power[l];
         }
     }
+    // world bounds of all triangles (RaytraceCommonResources.cpp:560-600 unions the object bounds)
+    float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t t = 0; t < v0.size(); ++t)
+    {
+        const float3 vs[3] = {v0[t], v1[t], v2[t]};
+        for (const float3& v : vs)
+        {
+            wlo[0] = std::min(wlo[0], v.x); wlo[1] = std::min(wlo[1], v.y); wlo[2] = std::min(wlo[2], v.z);
+            whi[0] = std::max(whi[0], v.x); whi[1] = std::max(whi[1], v.y); whi[2] = std::max(whi[2], v.z);
+        }
+    }
+    if (v0.empty()) wlo[0] = wlo[1] = wlo[2] = whi[0] = whi[1] = whi[2] = 0.0f;
+    float ext2 = 0.0f;
+    for (int k = 0; k < 3; ++k)
+    {
+        ctx->worldCenter[k] = (whi[k] + wlo[k]) * 0.5f;
+        float e = whi[k] - ctx->worldCenter[k];
+        ext2 += e * e;
+    }
+    ctx->worldRadiusSqr = ext2;
     std::vector<float4> tris, nodes;
     yg::buildBvh(v0, v1, v2, ki, kp, tris, nodes);
     ctx->nTris = v0.size();
@@ -688,8 +711,7 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     std::lock_guard<std::mutex> g(ctx->lock);
     if (!ctx->sceneBuilt) return fail(YG_ERR_NOT_READY, "render: call yg_build_scene first");
     if (!ctx->cameraSet) return fail(YG_ERR_NOT_READY, "render: camera not set");
-    if (p->integrator > YG_INTEGRATOR_NEE)
-        return fail(YG_ERR_INVALID_ARGUMENT, "render: integrator not available in this build");
+    if (p->integrator > YG_INTEGRATOR_BDPT) return fail(YG_ERR_INVALID_ARGUMENT, "render: unknown integrator");
     if (p->width == 0 || p->height == 0 || p->spp_count == 0) return fail(YG_ERR_INVALID_ARGUMENT, "render: empty request");
     uint32_t cx = p->crop_x, cy = p->crop_y, cw = p->crop_w, ch = p->crop_h;
     if (cw == 0 || ch == 0)
@@ -717,8 +739,38 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     if (needRgb && (r = ensureRgbLut(ctx, lmin, lmax))) return r;
 
     const uint64_t npix = (uint64_t)cw * ch;
-    const uint64_t maxSamplesPerChunk = 1ull << 26;
+    const bool bdpt = p->integrator == YG_INTEGRATOR_BDPT;
+    const uint64_t maxSamplesPerChunk = bdpt ? (1ull << 24) : (1ull << 26);
     uint32_t chunkSpp = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->spp_count, maxSamplesPerChunk / npix));
+    if (bdpt && (p->flags & YG_FLAG_MEGAKERNEL)) return fail(YG_ERR_INVALID_ARGUMENT, "render: BDPT has no megakernel variant");
+    const uint32_t lightVerts = p->bdpt_light_vertices ? p->bdpt_light_vertices : yg::kBdptMaxLightVertices;
+    if (bdpt && (lightVerts < 2 || lightVerts > yg::kBdptMaxLightVertices))
+        return fail(YG_ERR_INVALID_ARGUMENT, "render: bdpt_light_vertices must be 2..16");
+    const uint32_t lightPaths = p->bdpt_light_paths ? p->bdpt_light_paths : ((cw + 7) / 8) * ((ch + 7) / 8);
+    if (bdpt)
+    {
+        YG_CUDA(ctx->dArena.ensure(yg::bdptArenaBytes(chunkSpp, lightPaths, lightVerts, npix)));
+        if (ctx->permW != cw || ctx->permH != ch)
+        {
+            // fixed pseudo-random permutation of the crop's pixels (the texel remap of
+            // BidirectionalPathIntegratorSubStage.cpp:549-591, from a seeded generator)
+            std::vector<uint32_t> perm(npix);
+            for (uint64_t i = 0; i < npix; ++i) perm[i] = (uint32_t)i;
+            uint64_t state = 0x9E3779B97F4A7C15ull ^ ((uint64_t)cw << 32 | ch);
+            for (uint64_t i = npix - 1; i > 0; --i)
+            {
+                state += 0x9E3779B97F4A7C15ull;
+                uint64_t z = state;
+                z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+                z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+                z ^= z >> 31;
+                std::swap(perm[i], perm[z % (i + 1)]);
+            }
+            if ((r = upload(ctx, ctx->dPerm, perm.data(), perm.size()))) return r;
+            ctx->permW = cw;
+            ctx->permH = ch;
+        }
+    }
     bool feats = (p->flags & YG_FLAG_FEATURES) != 0;
     YG_CUDA(ctx->dSamples.ensure(npix * chunkSpp * sizeof(float4)));
     if (feats)
@@ -729,7 +781,7 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     if (dump) YG_CUDA(ctx->dDump.ensure(npix * chunkSpp * 8 * sizeof(float)));
     const bool mega = (p->flags & YG_FLAG_MEGAKERNEL) != 0;
     uint32_t waveCap = (uint32_t)std::min<uint64_t>(npix * chunkSpp, 1ull << 22);
-    if (!mega) YG_CUDA(ctx->dArena.ensure(waveCap * yg::wavefrontBytesPerSlot() + (64u << 10)));
+    if (!mega && !bdpt) YG_CUDA(ctx->dArena.ensure(waveCap * yg::wavefrontBytesPerSlot() + (64u << 10)));
     YG_CUDA(ctx->dRayCount.ensure(24));
     YG_CUDA(cudaMemsetAsync(ctx->dRayCount.p, 0, 24, ctx->stream));
     // Sobol points of every sample index of the request (RaytraceCommonResources.cpp:623-627)
@@ -804,7 +856,11 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         L.dump = dump ? ctx->dDump.as<float>() : nullptr;
         L.featAlbedo = feats ? ctx->dFeatA.as<float4>() : nullptr;
         L.featNormalDepth = feats ? ctx->dFeatN.as<float4>() : nullptr;
-        if (mega) launches += yg::launchPathKernel(S, L, ctx->smCount, ctx->stream);
+        if (bdpt)
+            launches += yg::launchBdpt(S, L, ctx->dArena.p, ctx->dPerm.as<uint32_t>(), lightPaths, lightVerts,
+                                       yg::mk3(ctx->worldCenter[0], ctx->worldCenter[1], ctx->worldCenter[2]),
+                                       ctx->worldRadiusSqr, ctx->smCount, ctx->stream);
+        else if (mega) launches += yg::launchPathKernel(S, L, ctx->smCount, ctx->stream);
         else launches += yg::launchWavefront(S, L, ctx->dArena.p, waveCap, ctx->smCount, ctx->stream);
         if (film)
             launches += yg::launchFilm(ctx->dFilmSum.as<float4>(), ctx->dFilmComp.as<float4>(), L.sampleXYZ, p->width, cx,

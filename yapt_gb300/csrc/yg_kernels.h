@@ -16,4 +16,11 @@ int launchFeatures(float4* accA, float4* accN, const float4* fa, const float4* f
                    uint32_t cw, uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
 int launchRelmse(const float4* sum, const float* ref, uint32_t npix, double eps, double* out, int smCount,
                  cudaStream_t stream);
+// Bidirectional integrator over P.sppCount sample indices. `arena` holds
+// bdptArenaBytes(P.sppCount, lightPaths, maxLightVerts, cropW*cropH) bytes; `perm` is a
+// permutation of the crop's pixel indices (camera groups take 64 consecutive entries).
+constexpr uint32_t kBdptMaxLightVertices = 16; // MAX_LIGHT_PATH_VERTICES_HARD_LIMIT
+size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVerts, uint64_t cropPixels);
+int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uint32_t* perm, uint32_t lightPaths,
+               uint32_t maxLightVerts, float3 worldCenter, float worldRadiusSqr, int smCount, cudaStream_t stream);
 } // namespace yg

@@ -156,7 +156,7 @@ struct HitSurface
 // fetch + fetchSurfaceMaterialParameters + two-sided orientation + tangent rotation +
 // regularisation + RGB -> spectral conversion (rayHitDefault.hlsl:470-520)
 YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectral& sp, const Hit& hit, const GpuInstance& I,
-                         float3 rayDirWS, PathState& ps, HitSurface& hs)
+                         float3 rayDirWS, PathState& ps, HitSurface& hs, bool orient = true)
 {
     TriGeom g = fetchTri(S, I, hit.prim);
     float b0 = 1.0f - hit.b1 - hit.b2;
@@ -206,8 +206,9 @@ YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectr
     s.baseLayerNormal = nrm;
     s.geometryNormal = gn;
     s.tangent = tan;
-    // handleTwoSidedMaterialOrientation (materialsCommon.hlsl:440-448), wo = -rayDir
-    if (s.transparency == 0.0f && isTwoSided(s.flags))
+    // handleTwoSidedMaterialOrientation (materialsCommon.hlsl:440-448), wo = -rayDir; light
+    // subpath vertices evaluated for a connection keep their normals (BDPTCommon.hlsl:845-852)
+    if (orient && s.transparency == 0.0f && isTwoSided(s.flags))
     {
         float3 wo = -rd;
         if (dot(wo, s.baseLayerNormal) < 0.0f) s.baseLayerNormal = -s.baseLayerNormal;

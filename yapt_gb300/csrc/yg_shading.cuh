@@ -504,6 +504,85 @@ YG_DEV float getEnergyCompensationTranslucent(const Luts& L, float etaR, float d
     return (ss / dirWo) - ss;
 }
 
+// Kulla-Conty compensation and the reciprocal multiple-scattering terms
+// (RECIPROCAL_MULTISCATTER, which BDPTCommon.hlsl:6 switches on for the bidirectional integrator)
+YG_DEV float getAvgFresnel(float etaR)
+{
+    if (etaR < 1.0f) return 0.997118f + 0.1014f * etaR - 0.965241f * etaR * etaR - 0.130607f * etaR * etaR * etaR;
+    return (etaR - 1.0f) / (4.08567f + 1.00071f * etaR);
+}
+YG_DEV float getAverageAlbedoTranslucent(const Luts& L, float etaR, float lr)
+{
+    if (etaR < 1.0f) return lut2(L.trAvgL, kLutTrans, kLutTrans, lr, saturate((etaR - 0.3f) * (1.0f / 0.69f)));
+    return lut2(L.trAvgD, kLutTrans, kLutTrans, lr, saturate((etaR - 1.0f) * 0.333333f));
+}
+YG_DEV float getMsTransmissionRatio(const Luts& L, float etaR, float lr)
+{
+    float etaOut = fmaxf(etaR, 1.0f / etaR);
+    float tOut = 1.0f - getAvgFresnel(etaOut);
+    if (etaR >= 1.0f) return tOut;
+    float eAvgOut = getAverageAlbedoTranslucent(L, etaOut, lr);
+    float eAvgIn = getAverageAlbedoTranslucent(L, etaR, lr);
+    return saturate(safeDiv(tOut * (1.0f - eAvgOut), etaOut * etaOut * (1.0f - eAvgIn)));
+}
+YG_DEV float getEnergyCompensationKulla(const Luts& L, float fms, float dotWo, float dotWi, float lr)
+{
+    float dWo = getSSDirectionalAlbedoNoFresnel(L, fabsf(dotWo), lr);
+    float dWi = getSSDirectionalAlbedoNoFresnel(L, fabsf(dotWi), lr);
+    float eAvg = getAverageSSDirectionalAlbedoNoFresnel(L, lr);
+    float ems = safeDiv((1.0f - dWo) * (1.0f - dWi), (1.0f - eAvg) * kPI);
+    return fms * ems;
+}
+YG_DEV float getEnergyCompensationTranslucentKulla(const Luts& L, float etaR, float dotWo, float dotWi, float lr)
+{
+    bool transmission = dotWo * dotWi < 0.0f;
+    float ratioT = getMsTransmissionRatio(L, etaR, lr);
+    float dWo, dWi, eAvg, ratio;
+    if (transmission)
+    {
+        float etaInv = 1.0f / etaR;
+        dWo = getDirectionalAlbedoTranslucent(L, etaR, dotWo, lr);
+        dWi = getDirectionalAlbedoTranslucent(L, etaInv, dotWi, lr);
+        eAvg = getAverageAlbedoTranslucent(L, etaInv, lr);
+        ratio = ratioT;
+    }
+    else
+    {
+        dWo = getDirectionalAlbedoTranslucent(L, etaR, dotWo, lr);
+        dWi = getDirectionalAlbedoTranslucent(L, etaR, dotWi, lr);
+        eAvg = getAverageAlbedoTranslucent(L, etaR, lr);
+        ratio = 1.0f - ratioT;
+    }
+    return ratio * safeDiv((1.0f - dWo) * (1.0f - dWi), (1.0f - eAvg) * kPI);
+}
+// getEnergyCompensation / getFmsDielectric / getEnergyCompensationTranslucent for either model
+template <bool RECIP>
+YG_DEV float energyComp(const Luts& L, float fms, float dotWo, float dotWi, float lr, float ss)
+{
+    if constexpr (RECIP) return getEnergyCompensationKulla(L, fms, fabsf(dotWo), fabsf(dotWi), lr);
+    else return getEnergyCompensation(L, fms, fabsf(dotWo), fabsf(dotWi), lr, ss);
+}
+template <bool RECIP>
+YG_DEV float fmsDielectric(const Luts& L, float etaR, float lr, float cosTheta)
+{
+    if constexpr (RECIP)
+    {
+        float fAvg = getAvgFresnel(etaR);
+        float eAvg = getAverageSSDirectionalAlbedoNoFresnel(L, lr);
+        return fAvg * eAvg / (1.0f - fAvg * (1.0f - eAvg));
+    }
+    else
+    {
+        return fresnelDielectricDielectric2(etaR, cosTheta);
+    }
+}
+template <bool RECIP>
+YG_DEV float energyCompTrans(const Luts& L, float etaR, float dotWo, float dotWi, float lr, float ss)
+{
+    if constexpr (RECIP) return getEnergyCompensationTranslucentKulla(L, etaR, dotWo, dotWi, lr);
+    else return getEnergyCompensationTranslucent(L, etaR, dotWo, lr, ss);
+}
+
 // ------------------------------------------------------------------ lobes (bsdfSample.hlsl)
 YG_DEV float3 sampleGGXReflectionConductor(float ax, float ay, float3 wo, float2 s)
 {
@@ -662,12 +741,38 @@ struct SpecularLayer
     float etaR;
     bool allowRefl, allowRefr;
 };
-YG_DEV float3 specSampleWi(const SpecularLayer& l, float3 wo, float2 rnd, float sel)
+// sampling probability of the cosine lobe that carries the Kulla-Conty multiple scattering
+// (getMsSamplingProbability, materialLayers.hlsl:310-320); zero in the Turquin configuration
+template <bool RECIP>
+YG_DEV float specMsProbability(const Luts& L, const SpecularLayer& l, float3 wo)
 {
-    // msProb == 0: sel stays (sel - 0) / (1 - 0)
-    float fsel = (sel - 0.0f) / (1.0f - 0.0f);
+    if constexpr (RECIP)
+    {
+        if (!l.allowRefr || isDeltaGGX(l.a2)) return 0.0f;
+        return saturate(1.0f - getDirectionalAlbedoTranslucent(L, l.etaR, wo.y, l.lr));
+    }
+    else
+    {
+        return 0.0f;
+    }
+}
+template <bool RECIP = false>
+YG_DEV float3 specSampleWi(const Luts& L, const SpecularLayer& l, float3 wo, float2 rnd, float sel)
+{
+    float msProb = specMsProbability<RECIP>(L, l, wo);
+    if (sel < msProb)
+    {
+        float sc = sel / msProb;
+        float3 wi = sampleCosineWeightedHemisphere(rnd);
+        float refrSel = l.allowRefl ? getMsTransmissionRatio(L, l.etaR, l.lr) : 1.0f;
+        bool msRefract = sc < refrSel;
+        wi.y = ((wo.y < 0.0f) != msRefract) ? -wi.y : wi.y;
+        return wi;
+    }
+    float fsel = (sel - msProb) / (1.0f - msProb);
     return sampleDielectric(l.etaR, l.a2.x, l.a2.y, wo, rnd, fsel, l.allowRefl, l.allowRefr);
 }
+template <bool RECIP = false>
 YG_DEV float specEvaluate(const Luts& L, const SpecularLayer& l, float3 wo, float3 wi)
 {
     if (onSameHemisphere(wo, wi))
@@ -676,27 +781,33 @@ YG_DEV float specEvaluate(const Luts& L, const SpecularLayer& l, float3 wo, floa
         float ms;
         if (l.allowRefl && l.allowRefr)
         {
-            ms = getEnergyCompensationTranslucent(L, l.etaR, wo.y, l.lr, w);
+            ms = energyCompTrans<RECIP>(L, l.etaR, wo.y, wi.y, l.lr, w);
         }
         else
         {
             float3 wm = normalize(wo + wi);
-            float fms = fresnelDielectricDielectric2(l.etaR, fabsf(dot(wo, wm)));
-            ms = getEnergyCompensation(L, fms, fabsf(wo.y), fabsf(wi.y), l.lr, w);
+            float fms = fmsDielectric<RECIP>(L, l.etaR, l.lr, fabsf(dot(wo, wm)));
+            ms = energyComp<RECIP>(L, fms, fabsf(wo.y), fabsf(wi.y), l.lr, w);
         }
         w += ms;
         w *= fabsf(wi.y);
         return w;
     }
     float w = evaluateGGXTransmitted(l.etaR, l.a2.x, l.a2.y, wo, wi);
-    float ms = getEnergyCompensationTranslucent(L, l.etaR, wo.y, l.lr, w);
+    float ms = energyCompTrans<RECIP>(L, l.etaR, wo.y, wi.y, l.lr, w);
     w += ms;
     w *= fabsf(wi.y);
     return w;
 }
-YG_DEV float specPdf(const SpecularLayer& l, float3 wo, float3 wi)
+template <bool RECIP = false>
+YG_DEV float specPdf(const Luts& L, const SpecularLayer& l, float3 wo, float3 wi)
 {
-    return pdfDielectric(l.etaR, wo, wi, l.a2.x, l.a2.y, l.allowRefl, l.allowRefr);
+    float pdfSS = pdfDielectric(l.etaR, wo, wi, l.a2.x, l.a2.y, l.allowRefl, l.allowRefr);
+    float msProb = specMsProbability<RECIP>(L, l, wo);
+    if (msProb == 0.0f) return pdfSS;
+    float refrSel = l.allowRefl ? getMsTransmissionRatio(L, l.etaR, l.lr) : 1.0f;
+    float pdfMS = pdfCosineWeightedHemisphere(fabsf(wi.y)) * (onSameHemisphere(wo, wi) ? 1.0f - refrSel : refrSel);
+    return lerpf(pdfSS, pdfMS, msProb);
 }
 YG_DEV float specEnergyLeft(const Luts& L, const SpecularLayer& l, float3 wo, float3 wi, float weight)
 {
@@ -792,6 +903,7 @@ YG_DEV int selectMaterialLayer(float rnd, const float* probs)
 }
 
 // getSampleDirectionOSForLayer (materialSample.hlsl:147-257)
+template <bool RECIP = false>
 YG_DEV float3 sampleLayerDirection(const Luts& L, const Surface& s, const SurfaceCtx& c, int layer, float selRnd, float2 rnd,
                                    float hero, bool& isDiffuse, bool& isDelta)
 {
@@ -841,7 +953,7 @@ YG_DEV float3 sampleLayerDirection(const Luts& L, const Surface& s, const Surfac
         SpecularLayer sl;
         sl.a2 = c.a2; sl.lr = s.roughness; sl.etaR = toIOR / fromIOR;
         sl.allowRefl = s.specularAmount > 0.0f; sl.allowRefr = s.transparency > 0.0f;
-        wi = specSampleWi(sl, c.woBase, rnd, selRnd);
+        wi = specSampleWi<RECIP>(L, sl, c.woBase, rnd, selRnd);
         wi = fromLocal(c.baseB, wi);
         isDiffuse = fminf(c.a2.x, c.a2.y) > 0.05f;
         isDelta = isDeltaGGX(c.a2);
@@ -908,7 +1020,10 @@ struct Eval
 constexpr uint32_t kTransEntered = 1, kTransExited = 2, kTransDispersed = 4;
 constexpr uint32_t kEvalNone = 1, kEvalPdfOnly = 2, kEvalLightPath = 4, kEvalTreatAsDelta = 8;
 
-// evaluateSurface (materialSample.hlsl:264-562), camera-path flags only
+// evaluateSurface (materialSample.hlsl:264-562). RECIP selects the multiple-scattering model
+// of the bidirectional integrator; kEvalLightPath adds the shading-normal compensation of light
+// subpaths and drops the camera-side solid-angle compression of refraction.
+template <bool RECIP = false>
 YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c, float3 woOS, float3 wiOS, uint32_t flags,
                             const Spectral& sp)
 {
@@ -930,7 +1045,10 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
     bool baseRefl = dWoG * dWiG > 0.0f;
     bool baseRefr = dWoG * dWiG < 0.0f;
     float energyLeft = 1.0f, energyLayer = 1.0f;
-    const float compC = 1.0f, compB = 1.0f; // shading-normal compensation is for light paths only
+    const bool lightPath = (flags & kEvalLightPath) != 0;
+    // compensateForShadingNormal (materialSample.hlsl:259-262), light paths only
+    const float compC = lightPath ? (fabsf(woC.y) * fabsf(dWiG)) / (fabsf(dWoG) * fabsf(wiC.y)) : 1.0f;
+    const float compB = lightPath ? (fabsf(woB.y) * fabsf(dWiG)) / (fabsf(dWoG) * fabsf(wiB.y)) : 1.0f;
     float diel = 1.0f - s.metalness;
     float specAmount = diel * s.specularAmount;
     bool applyInference = s.thinFilmNM > 0.0f && s.clearCoatAmount > 0.0f && (s.metalness > 0.0f || specAmount > 0.0f);
@@ -954,8 +1072,8 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
                         w = evaluateGGXReflectionDielectric(etaR, a2cc.x, a2cc.y, woC, wiC);
                         w *= fabsf(wiC.y);
                         float3 wm = normalize(woC + wiC);
-                        float fms = fresnelDielectricDielectric2(etaR, fabsf(dot(woC, wm)));
-                        w += getEnergyCompensation(L, fms, fabsf(woC.y), fabsf(wiC.y), s.clearCoatRoughness, w);
+                        float fms = fmsDielectric<RECIP>(L, etaR, s.clearCoatRoughness, fabsf(dot(woC, wm)));
+                        w += energyComp<RECIP>(L, fms, fabsf(woC.y), fabsf(wiC.y), s.clearCoatRoughness, w);
                     }
                     float4 weight = splat4(w) * (s.clearCoatAmount * energyLeft) * compC;
                     if (applyInference) coatAmp = weight;
@@ -1018,7 +1136,9 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
                             float ss = delta ? F / fabsf(wiB.y) : F * G2 * D / denom;
                             // multiscatter: getFmsConductor = Fresnel, Turquin compensation
                             float fms = fresnelDielectricConductor(er, ek, dOM);
-                            float ms = ss * (fms * (1.0f - dirWo) / dirWo);
+                            float ms;
+                            if constexpr (RECIP) ms = getEnergyCompensationKulla(L, fms, fabsf(woB.y), fabsf(wiB.y), s.roughness);
+                            else ms = ss * (fms * (1.0f - dirWo) / dirWo);
                             setLane(w, i, (ss + ms) * fabsf(wiB.y));
                         }
                     }
@@ -1050,12 +1170,12 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
         sl.allowRefl = s.specularAmount > 0.0f; sl.allowRefr = s.transparency > 0.0f;
         if (isDeltaGGX(a2) == treatAsDelta)
         {
-            float pdf = specPdf(sl, woB, wiB);
+            float pdf = specPdf<RECIP>(L, sl, woB, wiB);
             if (pdf > 0.0f)
             {
                 if (!onlyPDF)
                 {
-                    float4 weight = splat4(specEvaluate(L, sl, woB, wiB)) * (specAmount * energyLeft) * compB;
+                    float4 weight = splat4(specEvaluate<RECIP>(L, sl, woB, wiB)) * (specAmount * energyLeft) * compB;
                     if (applyInference)
                     {
                         float etaRC = s.clearCoatIOR / fromIOR;
@@ -1100,7 +1220,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
         SpecularLayer sl;
         sl.a2 = a2; sl.lr = s.roughness; sl.etaR = toIOR / fromIOR;
         sl.allowRefl = s.specularAmount > 0.0f; sl.allowRefr = s.transparency > 0.0f;
-        float pdf = specPdf(sl, woB, wiB);
+        float pdf = specPdf<RECIP>(L, sl, woB, wiB);
         if (pdf > 0.0f)
         {
             pdfSum += c.probs[LAYER_DIEL] * pdf;
@@ -1108,7 +1228,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
             float compression = 1.0f;
             if (!twoSided)
             {
-                compression *= sqr(1.0f / sl.etaR);
+                if (!lightPath) compression *= sqr(1.0f / sl.etaR);
                 res.transmission |= exiting ? kTransExited : kTransEntered;
             }
             else
@@ -1117,7 +1237,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
             }
             if (!onlyPDF)
             {
-                wsum = wsum + splat4(specEvaluate(L, sl, woB, wiB)) * (transAmount * energyLeft) * compression * compB;
+                wsum = wsum + splat4(specEvaluate<RECIP>(L, sl, woB, wiB)) * (transAmount * energyLeft) * compression * compB;
             }
         }
     }

@@ -60,7 +60,8 @@ class Context:
 
     @staticmethod
     def params(integrator="nee", width=64, height=64, spp_start=0, spp=1, max_depth=8, regularize_after=8,
-               regularize=True, env_scale=0.0, seed=0, flags=0, crop=None, lambda_range=(380.0, 700.0)):
+               regularize=True, env_scale=0.0, seed=0, flags=0, crop=None, lambda_range=(380.0, 700.0),
+               light_paths=0, light_vertices=0):
         p = N.RenderParams()
         p.integrator = N.INTEGRATORS[integrator] if isinstance(integrator, str) else int(integrator)
         p.width, p.height = int(width), int(height)
@@ -74,6 +75,8 @@ class Context:
         if crop is not None:
             p.crop_x, p.crop_y, p.crop_w, p.crop_h = [int(v) for v in crop]
         p.lambda_min, p.lambda_max = float(lambda_range[0]), float(lambda_range[1])
+        p.bdpt_light_paths = int(light_paths)
+        p.bdpt_light_vertices = int(light_vertices)
         return p
 
     def render(self, params, dump=False):
