@@ -26,6 +26,12 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(workload="nee_random_shapes_500_icospheres", width=1024, height=1024, spp=64, max_depth=12,
                 integrator="nee", lambda_nm=[380, 780], scene_seed=0)
 METRIC = "Msamples/s (NEE, random-shapes scene, 1024x1024, 64 spp, depth 12, equal relMSE)"
+# --workload bdpt: the bidirectional integrator on the caustic box (box layout, 150 icospheres of
+# which 60% dispersive dielectrics, 10 sphere lights; ~196k triangles), 512 x 512, 32 spp,
+# camera and light subpath depth 10. The CPU oracle has no BDPT, so that line has no CPU baseline.
+BDPT_WORKLOAD = dict(workload="bdpt_caustic_box_150_spheres_10_sphere_lights", width=512, height=512, spp=32,
+                     max_depth=10, light_vertices=10, integrator="bdpt", lambda_nm=[380, 780], scene_seed=0)
+BDPT_METRIC = "Msamples/s (BDPT with MIS, caustic box scene, 512x512, 32 spp, depth 10)"
 CPU_CROP = (256, 256, 512, 512)  # bounded CPU sample: 512x512 centre crop
 CPU_SPP = 32
 
@@ -181,7 +187,8 @@ def run_ours(args, world, rank, local):
     import torch
 
     torch.cuda.set_device(local)
-    scene = configs.random_shapes_scene(WORKLOAD["scene_seed"])
+    bdpt = WORKLOAD["integrator"] == "bdpt"
+    scene = configs.caustic_box_scene(WORKLOAD["scene_seed"]) if bdpt else configs.random_shapes_scene(WORKLOAD["scene_seed"])
     ctx = Context(local)
     ctx.upload_scene(scene)
     info = ctx.scene_info()
@@ -192,7 +199,8 @@ def run_ours(args, world, rank, local):
 
     def params(step, flags=0):
         return ctx.params(WORKLOAD["integrator"], W, H, spp_start=base + step * spp, spp=spp,
-                          max_depth=WORKLOAD["max_depth"], lambda_range=WORKLOAD["lambda_nm"], flags=flags)
+                          max_depth=WORKLOAD["max_depth"], lambda_range=WORKLOAD["lambda_nm"], flags=flags,
+                          light_vertices=WORKLOAD.get("light_vertices", 0))
 
     flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
     for w in range(args.warmup):
@@ -238,25 +246,30 @@ def run_ours(args, world, rank, local):
 
     # algorithmic bytes of the dominant kernel: BVH nodes (64 B) + triangles (48 B) visited,
     # measured once by the counting variant of the same kernel on one step
-    ctx.render(params(0, flags=1 << 10 | 1 << 8))
-    tc = ctx.traversal_counts()
+    if bdpt:
+        tc = {"nodes": 0, "triangles": 0}  # the bidirectional kernels have no counting variant
+    else:
+        ctx.render(params(0, flags=1 << 10 | 1 << 8))
+        tc = ctx.traversal_counts()
     per_launch_bytes = tc["nodes"] * 64 + tc["triangles"] * 48 + W * H * spp * 16
     avg_ms = sum(kernel_ms) / len(kernel_ms)
     achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
     peak, peak_kind = read_peaks()
     traffic = None
     try:
+        if bdpt:
+            raise KeyError("no traffic summary for the bidirectional kernels")
         with open(os.path.join(ROOT, "profiles", "path_kernel_traffic.json")) as f:
             tj = json.load(f)
         traffic = tj["dram_bytes_per_sample"] * W * H * spp
     except Exception:
         pass
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and not bdpt:
         r, threads, sample = cpu_port_rate(scene)
         cpu = {"value": r, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample}
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+        line = {"metric": BDPT_METRIC if bdpt else METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": sum(kernel_ms) / len(kernel_ms), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": dict(WORKLOAD, triangles=info["triangles"], bvh_nodes=info["nodes"], lights=info["lights"],
@@ -284,7 +297,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", type=int, default=0, help="image side for a smaller profiling case")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel for a smaller profiling case")
+    ap.add_argument("--workload", default="nee", choices=["nee", "bdpt"])
     args = ap.parse_args()
+    if args.workload == "bdpt":
+        WORKLOAD.clear()
+        WORKLOAD.update(BDPT_WORKLOAD)
     if args.size:
         WORKLOAD["width"] = WORKLOAD["height"] = args.size
     if args.spp:

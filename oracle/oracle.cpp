@@ -314,6 +314,7 @@ struct Ctx
     };
     std::vector<Node> nodes;
     std::vector<uint32_t> triIdx;
+    float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY}; // world bounds
 };
 
 // LUT read with the texel-centre remap of sampleLUT (materialsCommonResources.hlsl:132-169):
@@ -633,6 +634,9 @@ struct LutSet
     T trL(T eta, T c, T r) const { return lut3(L[5], 16, c, r, saturate((eta - T(0.3f)) * (T(1) / T(0.69f)))); }
     T trD(T eta, T c, T r) const { return lut3(L[4], 16, c, r, saturate((eta - T(1)) * T(0.333333f))); }
     T sheen(T c, T r) const { return lut2(L[8], 16, c, saturate(r - T(0.07f))); }
+    T ssAvg(T r) const { return lut1(L[1], 32, r); }
+    T trAvgL(T eta, T r) const { return lut2(L[7], 16, r, saturate((eta - T(0.3f)) * (T(1) / T(0.69f)))); }
+    T trAvgD(T eta, T r) const { return lut2(L[6], 16, r, saturate((eta - T(1)) * T(0.333333f))); }
 };
 // multiScatter.hlsl (Turquin variant: RECIPROCAL_MULTISCATTER is off for uni/NEE)
 template <typename T> T dirAlbedoTrans(const LutSet<T>& L, T eta, T d, T lr)
@@ -653,6 +657,75 @@ template <typename T> T energyCompTrans(const LutSet<T>& L, T eta, T dWo, T lr, 
 {
     T d = tmax(dirAlbedoTrans(L, eta, std::fabs(dWo), lr), T(0.1f));
     return (ss / d) - ss;
+}
+// Kulla-Conty variant (RECIPROCAL_MULTISCATTER, which BDPTCommon.hlsl:6 switches on):
+// getAvgFresnel, getAverageAlbedoTranslucent, getMsTransmissionRatio,
+// getEnergyCompensationKulla, getEnergyCompensationTranslucentKulla (multiScatter.hlsl:93-213)
+template <typename T> T avgFresnel(T eta)
+{
+    if (eta < T(1)) return T(0.997118f) + T(0.1014f) * eta - T(0.965241f) * eta * eta - T(0.130607f) * eta * eta * eta;
+    return (eta - T(1)) / (T(4.08567f) + T(1.00071f) * eta);
+}
+template <typename T> T avgAlbedoTrans(const LutSet<T>& L, T eta, T lr) { return eta < T(1) ? L.trAvgL(eta, lr) : L.trAvgD(eta, lr); }
+template <typename T> T msTransRatio(const LutSet<T>& L, T eta, T lr)
+{
+    T etaOut = tmax(eta, T(1) / eta);
+    T tOut = T(1) - avgFresnel(etaOut);
+    if (eta >= T(1)) return tOut;
+    T eOut = avgAlbedoTrans(L, etaOut, lr);
+    T eIn = avgAlbedoTrans(L, eta, lr);
+    return saturate(safeDiv(tOut * (T(1) - eOut), etaOut * etaOut * (T(1) - eIn)));
+}
+template <typename T> T energyCompKulla(const LutSet<T>& L, T fms, T dWo, T dWi, T lr)
+{
+    T aWo = L.ssNoF(std::fabs(dWo), lr);
+    T aWi = L.ssNoF(std::fabs(dWi), lr);
+    T eAvg = L.ssAvg(lr);
+    T ems = safeDiv((T(1) - aWo) * (T(1) - aWi), (T(1) - eAvg) * C<T>::PI);
+    return fms * ems;
+}
+template <typename T> T energyCompTransKulla(const LutSet<T>& L, T eta, T dWo, T dWi, T lr)
+{
+    bool transmission = dWo * dWi < T(0);
+    T ratioT = msTransRatio(L, eta, lr);
+    T aWo, aWi, eAvg, ratio;
+    if (transmission)
+    {
+        T inv = T(1) / eta;
+        aWo = dirAlbedoTrans(L, eta, dWo, lr);
+        aWi = dirAlbedoTrans(L, inv, dWi, lr);
+        eAvg = avgAlbedoTrans(L, inv, lr);
+        ratio = ratioT;
+    }
+    else
+    {
+        aWo = dirAlbedoTrans(L, eta, dWo, lr);
+        aWi = dirAlbedoTrans(L, eta, dWi, lr);
+        eAvg = avgAlbedoTrans(L, eta, lr);
+        ratio = T(1) - ratioT;
+    }
+    return ratio * safeDiv((T(1) - aWo) * (T(1) - aWi), (T(1) - eAvg) * C<T>::PI);
+}
+// getEnergyCompensation / getFmsDielectric / getEnergyCompensationTranslucent of either model
+template <typename T, bool R> T energyCompM(const LutSet<T>& L, T fms, T dWo, T dWi, T lr, T ss)
+{
+    if (R) return energyCompKulla(L, fms, std::fabs(dWo), std::fabs(dWi), lr);
+    return energyComp(L, fms, dWo, dWi, lr, ss);
+}
+template <typename T, bool R> T fmsDielM(const LutSet<T>& L, T eta, T lr, T cosT)
+{
+    if (R)
+    {
+        T fAvg = avgFresnel(eta);
+        T eAvg = L.ssAvg(lr);
+        return fAvg * eAvg / (T(1) - fAvg * (T(1) - eAvg));
+    }
+    return fresnelDD(eta, cosT);
+}
+template <typename T, bool R> T energyCompTransM(const LutSet<T>& L, T eta, T dWo, T dWi, T lr, T ss)
+{
+    if (R) return energyCompTransKulla(L, eta, dWo, dWi, lr);
+    return energyCompTrans(L, eta, dWo, lr, ss);
 }
 
 // bsdfSample.hlsl lobes
@@ -787,27 +860,42 @@ struct SpecLayer
     T ax, ay, lr, eta;
     bool aR, aT;
 };
-template <typename T> T specEval(const LutSet<T>& L, const SpecLayer<T>& l, V3<T> wo, V3<T> wi)
+template <typename T, bool R = false> T specEval(const LutSet<T>& L, const SpecLayer<T>& l, V3<T> wo, V3<T> wi)
 {
     if (sameHemi(wo, wi))
     {
         T w = evalDielRefl(l.eta, l.ax, l.ay, wo, wi);
         T ms;
-        if (l.aR && l.aT) ms = energyCompTrans(L, l.eta, wo.y, l.lr, w);
+        if (l.aR && l.aT) ms = energyCompTransM<T, R>(L, l.eta, wo.y, wi.y, l.lr, w);
         else
         {
             V3<T> wm = normalize(wo + wi);
-            T fms = fresnelDD(l.eta, std::fabs(dot(wo, wm)));
-            ms = energyComp(L, fms, std::fabs(wo.y), std::fabs(wi.y), l.lr, w);
+            T fms = fmsDielM<T, R>(L, l.eta, l.lr, std::fabs(dot(wo, wm)));
+            ms = energyCompM<T, R>(L, fms, std::fabs(wo.y), std::fabs(wi.y), l.lr, w);
         }
         w += ms;
         w *= std::fabs(wi.y);
         return w;
     }
     T w = evalTrans(l.eta, l.ax, l.ay, wo, wi);
-    w += energyCompTrans(L, l.eta, wo.y, l.lr, w);
+    w += energyCompTransM<T, R>(L, l.eta, wo.y, wi.y, l.lr, w);
     w *= std::fabs(wi.y);
     return w;
+}
+// getMsSamplingProbability / getMsRefractionSelectionProbability (materialLayers.hlsl:327-344)
+template <typename T, bool R> T specMsProb(const LutSet<T>& L, const SpecLayer<T>& l, V3<T> wo)
+{
+    if (!R || !l.aT || deltaGGX(l.ax, l.ay)) return T(0);
+    return saturate(T(1) - dirAlbedoTrans(L, l.eta, wo.y, l.lr));
+}
+template <typename T, bool R> T specPdf(const LutSet<T>& L, const SpecLayer<T>& l, V3<T> wo, V3<T> wi)
+{
+    T pdfSS = pdfDiel(l.eta, wo, wi, l.ax, l.ay, l.aR, l.aT);
+    T msProb = specMsProb<T, R>(L, l, wo);
+    if (msProb == T(0)) return pdfSS;
+    T refrSel = l.aR ? msTransRatio(L, l.eta, l.lr) : T(1);
+    T pdfMS = pdfCosHemi(std::fabs(wi.y)) * (sameHemi(wo, wi) ? T(1) - refrSel : refrSel);
+    return lerpT(pdfSS, pdfMS, msProb);
 }
 
 // surface (SurfaceDefinition, hitShadersCommon.hlsl:13-47)
@@ -904,12 +992,18 @@ template <typename T> void thinFilm(const T lam[4], const S4<T>& A1, S4<T>& A2, 
         A2[i] = tmax(T(0), A1[i] + A2[i] + T(2) * Mth<T>::sqrt(tmax(T(0), A1[i] * A2[i])) * m[i]);
 }
 
-// evaluateSurface (materialSample.hlsl:264-562), camera path
-template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s, const SCtx<T>& c, V3<T> wo, V3<T> wi,
-                                           bool treatAsDelta, const Spec<T>& sp4)
+// evaluateSurface (materialSample.hlsl:264-562). R selects the Kulla-Conty multiple-scattering
+// model of the bidirectional integrator. Flags as EVALUATE_FLAGS_* (materialSample.hlsl:57-61):
+// EV_LIGHT_PATH adds the shading-normal compensation of light subpaths (compensateForShadingNormal,
+// :259-262) and drops the camera-side 1/eta^2 solid-angle compression of refraction.
+constexpr uint32_t EV_NONE = 1, EV_PDF_ONLY = 2, EV_LIGHT_PATH = 4, EV_TREAT_AS_DELTA = 8;
+template <typename T, bool R> EvalR<T> evalSurfaceF(const LutSet<T>& L, const Surf<T>& s, const SCtx<T>& c, V3<T> wo,
+                                                    V3<T> wi, uint32_t flags, const Spec<T>& sp4)
 {
     EvalR<T> r;
     r.trans = 0;
+    const bool treatAsDelta = (flags & EV_TREAT_AS_DELTA) != 0;
+    const bool lightPath = (flags & EV_LIGHT_PATH) != 0;
     T ccx, ccy;
     roughParams(s.ccRough, T(0), ccx, ccy);
     T fromIOR = c.fromIOR, toIOR = c.toIOR;
@@ -919,6 +1013,8 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
     V3<T> woC = c.woC, woB = c.woB;
     T dWoG = dot(wo, s.geoN), dWiG = dot(wi, s.geoN);
     bool bRefl = dWoG * dWiG > T(0), bRefr = dWoG * dWiG < T(0);
+    const T compC = lightPath ? (std::fabs(woC.y) * std::fabs(dWiG)) / (std::fabs(dWoG) * std::fabs(wiC.y)) : T(1);
+    const T compB = lightPath ? (std::fabs(woB.y) * std::fabs(dWiG)) / (std::fabs(dWoG) * std::fabs(wiB.y)) : T(1);
     T eLeft = 1, eLayer = 1;
     T diel = T(1) - s.metalness, specAmount = diel * s.specAmount;
     bool infer = s.thinFilm > 0 && s.ccAmount > 0 && (s.metalness > 0 || specAmount > 0);
@@ -939,10 +1035,10 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
                     w = evalDielRefl(eta, ccx, ccy, woC, wiC);
                     w *= std::fabs(wiC.y);
                     V3<T> wm = normalize(woC + wiC);
-                    T fms = fresnelDD(eta, std::fabs(dot(woC, wm)));
-                    w += energyComp(L, fms, std::fabs(woC.y), std::fabs(wiC.y), s.ccRough, w);
+                    T fms = fmsDielM<T, R>(L, eta, s.ccRough, std::fabs(dot(woC, wm)));
+                    w += energyCompM<T, R>(L, fms, std::fabs(woC.y), std::fabs(wiC.y), s.ccRough, w);
                 }
-                S4<T> weight = sp(w) * (s.ccAmount * eLeft) * T(1);
+                S4<T> weight = sp(w) * (s.ccAmount * eLeft) * compC;
                 if (infer) coatAmp = weight;
                 else ws = ws + weight;
                 pdfSum += c.probs[0] * pdf;
@@ -959,7 +1055,7 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
             if (pdf > 0 && bRefl)
             {
                 S4<T> w = sameHemi(woB, wiB) ? evalSheen(s.sheenColor, s.sheenRough, woB, wiB) * std::fabs(wiB.y) : sp(T(0));
-                ws = ws + w * (s.sheenAmount * eLeft) * T(1);
+                ws = ws + w * (s.sheenAmount * eLeft) * compB;
                 pdfSum += c.probs[1] * pdf;
             }
         }
@@ -996,11 +1092,12 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
                         T F = fresnelDC(er, ek, dOM);
                         T ss = delta ? F / std::fabs(wiB.y) : F * g2 * D / den;
                         T fms = fresnelDC(er, ek, dOM);
-                        T ms = ss * (fms * (T(1) - dw) / dw);
+                        T ms = R ? energyCompKulla(L, fms, std::fabs(woB.y), std::fabs(wiB.y), s.roughness)
+                                 : ss * (fms * (T(1) - dw) / dw);
                         w[i] = (ss + ms) * std::fabs(wiB.y);
                     }
                 }
-                S4<T> weight = w * (s.metalness * eLeft) * T(1);
+                S4<T> weight = w * (s.metalness * eLeft) * compB;
                 if (infer)
                 {
                     T etaC = s.ccIOR / fromIOR;
@@ -1024,10 +1121,10 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
         SpecLayer<T> sl{c.ax, c.ay, s.roughness, toIOR / fromIOR, s.specAmount > 0, s.transparency > 0};
         if (deltaGGX(c.ax, c.ay) == treatAsDelta)
         {
-            T pdf = pdfDiel(sl.eta, woB, wiB, sl.ax, sl.ay, sl.aR, sl.aT);
+            T pdf = specPdf<T, R>(L, sl, woB, wiB);
             if (pdf > 0)
             {
-                S4<T> weight = sp(specEval(L, sl, woB, wiB)) * (specAmount * eLeft) * T(1);
+                S4<T> weight = sp(specEval<T, R>(L, sl, woB, wiB)) * (specAmount * eLeft) * compB;
                 if (infer)
                 {
                     T etaC = s.ccIOR / fromIOR;
@@ -1050,7 +1147,7 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
         {
             S4<T> alb = s.albedo / C<T>::PI;
             S4<T> w = sameHemi(woB, wiB) ? alb * std::fabs(wiB.y) : sp(T(0));
-            ws = ws + w * (diffAmount * eLeft) * T(1);
+            ws = ws + w * (diffAmount * eLeft) * compB;
             pdfSum += c.probs[4] * pdf;
         }
     }
@@ -1064,7 +1161,7 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
             r.trans |= 4;
         }
         SpecLayer<T> sl{c.ax, c.ay, s.roughness, toIOR / fromIOR, s.specAmount > 0, s.transparency > 0};
-        T pdf = pdfDiel(sl.eta, woB, wiB, sl.ax, sl.ay, sl.aR, sl.aT);
+        T pdf = specPdf<T, R>(L, sl, woB, wiB);
         if (pdf > 0)
         {
             pdfSum += c.probs[3] * pdf;
@@ -1072,20 +1169,29 @@ template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s,
             T comp = 1;
             if (!two)
             {
-                comp *= sqr(T(1) / sl.eta);
+                if (!lightPath) comp *= sqr(T(1) / sl.eta);
                 r.trans |= c.exiting ? 2u : 1u;
             }
             else r.trans |= 3u;
-            ws = ws + sp(specEval(L, sl, woB, wiB)) * (transAmount * eLeft) * comp * T(1);
+            ws = ws + sp(specEval<T, R>(L, sl, woB, wiB)) * (transAmount * eLeft) * comp * compB;
         }
     }
     r.pdf = pdfSum;
     r.w = ws;
     return r;
 }
+// the unidirectional integrators' evaluation (Turquin model, camera path)
+template <typename T> EvalR<T> evalSurface(const LutSet<T>& L, const Surf<T>& s, const SCtx<T>& c, V3<T> wo, V3<T> wi,
+                                           bool treatAsDelta, const Spec<T>& sp4)
+{
+    return evalSurfaceF<T, false>(L, s, c, wo, wi, treatAsDelta ? EV_TREAT_AS_DELTA : EV_NONE, sp4);
+}
 
-// getSampleDirectionOSForLayer (materialSample.hlsl:147-257)
-template <typename T> V3<T> sampleLayer(const Surf<T>& s, const SCtx<T>& c, int layer, T sel, T r0, T r1, T hero, bool& diffuse, bool& delta)
+// getSampleDirectionOSForLayer (materialSample.hlsl:147-257); with R the dielectric layer also
+// samples the multiple-scattering cosine lobe (SpecularLayer::sampleWi, materialLayers.hlsl:346-360)
+template <typename T, bool R = false>
+V3<T> sampleLayer(const LutSet<T>* L, const Surf<T>& s, const SCtx<T>& c, int layer, T sel, T r0, T r1, T hero, bool& diffuse,
+                  bool& delta)
 {
     V3<T> wi = v3(T(0), T(0), T(0));
     bool allowT = s.transparency > 0;
@@ -1130,8 +1236,22 @@ template <typename T> V3<T> sampleLayer(const Surf<T>& s, const SCtx<T>& c, int 
             else toIOR = cauchy(s, hero);
         }
         T eta = toIOR / fromIOR;
-        T fsel = (sel - T(0)) / (T(1) - T(0)); // no multiple-scattering lobe (RECIPROCAL_MULTISCATTER off)
-        wi = mulvM(sampleDiel(eta, c.ax, c.ay, c.woB, r0, r1, fsel, s.specAmount > 0, s.transparency > 0), c.baseB);
+        SpecLayer<T> sl{c.ax, c.ay, s.roughness, eta, s.specAmount > 0, s.transparency > 0};
+        T msProb = R ? specMsProb<T, R>(*L, sl, c.woB) : T(0);
+        if (sel < msProb)
+        {
+            T sc = sel / msProb;
+            V3<T> w = cosHemi(r0, r1);
+            T refrSel = sl.aR ? msTransRatio(*L, sl.eta, sl.lr) : T(1);
+            bool msRefract = sc < refrSel;
+            w.y = ((c.woB.y < T(0)) != msRefract) ? -w.y : w.y;
+            wi = mulvM(w, c.baseB);
+        }
+        else
+        {
+            T fsel = (sel - msProb) / (T(1) - msProb);
+            wi = mulvM(sampleDiel(eta, c.ax, c.ay, c.woB, r0, r1, fsel, s.specAmount > 0, s.transparency > 0), c.baseB);
+        }
         diffuse = tmin(c.ax, c.ay) > T(0.05f);
         delta = deltaGGX(c.ax, c.ay);
     }
@@ -1348,6 +1468,8 @@ template <typename T> bool setup(Ctx<T>& c, const oracle_scene* sc, const Tables
                 w[k] = xPoint<float>(I.o2w, ob);
                 lo[0] = std::min(lo[0], w[k].x); lo[1] = std::min(lo[1], w[k].y); lo[2] = std::min(lo[2], w[k].z);
                 hi[0] = std::max(hi[0], w[k].x); hi[1] = std::max(hi[1], w[k].y); hi[2] = std::max(hi[2], w[k].z);
+                c.wlo[0] = std::min(c.wlo[0], w[k].x); c.wlo[1] = std::min(c.wlo[1], w[k].y); c.wlo[2] = std::min(c.wlo[2], w[k].z);
+                c.whi[0] = std::max(c.whi[0], w[k].x); c.whi[1] = std::max(c.whi[1], w[k].y); c.whi[2] = std::max(c.whi[2], w[k].z);
             }
             typename Ctx<T>::Tri t;
             t.v0 = w[0];
@@ -1404,6 +1526,8 @@ template <typename T> bool setup(Ctx<T>& c, const oracle_scene* sc, const Tables
             c.instLightPdf[lightInst[l]] = power[l];
         }
     }
+    if (c.tris.empty())
+        for (int k = 0; k < 3; ++k) c.wlo[k] = c.whi[k] = 0.0f;
     buildBvh(c);
     return true;
 }
@@ -1497,6 +1621,84 @@ template <typename T> T regularizeR(T lr, bool sq)
     return lr;
 }
 
+// fetch + fetchSurfaceMaterialParameters (with the BindlessMaterialManager clamps) +
+// handleTwoSidedMaterialOrientation (when orient) + setupSurfaceOrientation + regularisation (when
+// regularize) + convertSurfaceDefinitionFromRGB (rayHitDefault.hlsl:470-520, hitShadersCommon.hlsl:51-91)
+template <typename T> void fillSurf(const Ctx<T>& c, const Spec<T>& s4, uint32_t inst, uint32_t prim, T b1, T b2, V3<T> rd,
+                                    bool orient, bool regularize, Surf<T>& s)
+{
+    const oracle_scene* sc = c.sc;
+    const oracle_instance& I = sc->instances[inst];
+    const yg_material& M = sc->materials[I.material];
+    V3<T> p[3];
+    uint32_t id[3];
+    triPositions(c, I, prim, p, id);
+    T b0 = T(1) - b1 - b2;
+
+    V3<T> gn = normalize(cross(p[1] - p[0], p[2] - p[0]));
+    auto nv = [&](uint32_t k) { return v3(T(sc->normals[3 * k]), T(sc->normals[3 * k + 1]), T(sc->normals[3 * k + 2])); };
+    V3<T> nrm = normalize(nv(id[0]) * b0 + nv(id[1]) * b1 + nv(id[2]) * b2);
+    V3<T> tan = v3(T(1), T(0), T(0));
+    if (I.has_tangents)
+    {
+        auto tv = [&](uint32_t k) {
+            const float* t = sc->tangents + 4 * k;
+            return v3(T(t[0] * t[3]), T(t[1] * t[3]), T(t[2] * t[3]));
+        };
+        tan = normalize(tv(id[0]) * b0 + tv(id[1]) * b1 + tv(id[2]) * b2);
+    }
+    // fetchSurfaceMaterialParameters with BindlessMaterialManager clamps
+    auto sat = [](float x) { return std::min(std::max(x, 0.0f), 1.0f); };
+    s.transparency = T(M.transparency);
+    s.metalness = T(M.metalness);
+    s.ior = T(std::min(std::max(M.dielectric_ior, 0.3f), 3.0f));
+    s.roughness = T(sat(M.roughness));
+    s.focus = T(M.emission_focus);
+    s.specAmount = T(sat(M.specular_amount));
+    s.ccAmount = T(sat(M.clear_coat_amount));
+    s.ccIOR = T(M.clear_coat_ior);
+    s.ccRough = T(sat(M.clear_coat_roughness));
+    s.cauchyA = T(M.cauchy[0]);
+    s.cauchyB = T(M.cauchy[1]);
+    s.aniso = T(sat(M.anisotropy));
+    s.anisoRot = T(M.anisotropy_rotation);
+    s.thinFilm = T(M.thin_film_thickness_nm);
+    s.flags = M.material_mask;
+    s.sheenRough = T(std::fmax(M.sheen_roughness, 0.07f));
+    s.sheenAmount = T(M.sheen_amount);
+    s.sssAmount = T(sat(M.subsurface_amount));
+    s.coatN = nrm;
+    s.baseN = nrm;
+    s.geoN = gn;
+    s.tangent = tan;
+    if (orient && s.transparency == T(0) && (s.flags & YG_MATERIAL_TWO_SIDED))
+    {
+        V3<T> wo = -rd;
+        if (dot(wo, s.baseN) < T(0)) s.baseN = -s.baseN;
+        if (dot(wo, s.coatN) < T(0)) s.coatN = -s.coatN;
+        if (dot(wo, s.geoN) < T(0)) s.geoN = -s.geoN;
+    }
+    if (s.anisoRot > T(0))
+    {
+        T ang = s.anisoRot * T(2) * C<T>::PI, sa, ca;
+        Mth<T>::sincos(ang, sa, ca);
+        V3<T> t = s.tangent;
+        s.tangent = v3(ca * t.x + T(0) * t.y + sa * t.z, T(0) * t.x + T(1) * t.y + T(0) * t.z, -sa * t.x + T(0) * t.y + ca * t.z);
+    }
+    if (regularize)
+    {
+        s.roughness = regularizeR(s.roughness, true);
+        s.sheenRough = regularizeR(s.sheenRough, false);
+        s.ccRough = regularizeR(s.ccRough, true);
+    }
+    s.specular = reflectance(c, s4, M.specular, M.specular_spectrum);
+    s.albedo = reflectance(c, s4, M.albedo, M.albedo_spectrum);
+    bool absZero = M.absorption[0] == 0 && M.absorption[1] == 0 && M.absorption[2] == 0;
+    s.absorption = absZero ? sp(T(0)) : setFromRGBUnboundedNoIllum(c, s4, v3(T(M.absorption[0]), T(M.absorption[1]), T(M.absorption[2])));
+    s.emissive = emission(c, s4, M.emissive, M.emission_spectrum);
+    s.sheenColor = s.sheenAmount > T(0) ? setFromRGB(c, s4, v3(T(M.sheen_tint[0]), T(M.sheen_tint[1]), T(M.sheen_tint[2]))) : sp(T(0));
+}
+
 template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P, const uint32_t* point, uint32_t px, uint32_t py,
                                      float* rec, V3<T>& xyzOut, uint64_t& rays)
 {
@@ -1576,79 +1778,10 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
         else
         {
             const oracle_instance& I = sc->instances[h.inst];
-            const yg_material& M = sc->materials[I.material];
-            V3<T> p[3];
-            uint32_t id[3];
-            triPositions(c, I, h.prim, p, id);
-            T b1 = T(h.b1), b2 = T(h.b2), b0 = T(1) - b1 - b2;
-            V3<T> gn = normalize(cross(p[1] - p[0], p[2] - p[0]));
-            auto nv = [&](uint32_t k) { return v3(T(sc->normals[3 * k]), T(sc->normals[3 * k + 1]), T(sc->normals[3 * k + 2])); };
-            V3<T> nrm = normalize(nv(id[0]) * b0 + nv(id[1]) * b1 + nv(id[2]) * b2);
-            V3<T> tan = v3(T(1), T(0), T(0));
-            if (I.has_tangents)
-            {
-                auto tv = [&](uint32_t k) {
-                    const float* t = sc->tangents + 4 * k;
-                    return v3(T(t[0] * t[3]), T(t[1] * t[3]), T(t[2] * t[3]));
-                };
-                tan = normalize(tv(id[0]) * b0 + tv(id[1]) * b1 + tv(id[2]) * b2);
-            }
             V3<T> rd = normalize(xVec<T>(I.w2o, ps.d));
-            // fetchSurfaceMaterialParameters with BindlessMaterialManager clamps
+            if (P.regularize_enable && ps.len >= P.regularize_after_vertices) ps.flags |= F_REG;
             Surf<T> s;
-            auto sat = [](float x) { return std::min(std::max(x, 0.0f), 1.0f); };
-            s.transparency = T(M.transparency);
-            s.metalness = T(M.metalness);
-            s.ior = T(std::min(std::max(M.dielectric_ior, 0.3f), 3.0f));
-            s.roughness = T(sat(M.roughness));
-            s.focus = T(M.emission_focus);
-            s.specAmount = T(sat(M.specular_amount));
-            s.ccAmount = T(sat(M.clear_coat_amount));
-            s.ccIOR = T(M.clear_coat_ior);
-            s.ccRough = T(sat(M.clear_coat_roughness));
-            s.cauchyA = T(M.cauchy[0]);
-            s.cauchyB = T(M.cauchy[1]);
-            s.aniso = T(sat(M.anisotropy));
-            s.anisoRot = T(M.anisotropy_rotation);
-            s.thinFilm = T(M.thin_film_thickness_nm);
-            s.flags = M.material_mask;
-            s.sheenRough = T(std::fmax(M.sheen_roughness, 0.07f));
-            s.sheenAmount = T(M.sheen_amount);
-            s.sssAmount = T(sat(M.subsurface_amount));
-            s.coatN = nrm;
-            s.baseN = nrm;
-            s.geoN = gn;
-            s.tangent = tan;
-            if (s.transparency == T(0) && (s.flags & YG_MATERIAL_TWO_SIDED))
-            {
-                V3<T> wo = -rd;
-                if (dot(wo, s.baseN) < T(0)) s.baseN = -s.baseN;
-                if (dot(wo, s.coatN) < T(0)) s.coatN = -s.coatN;
-                if (dot(wo, s.geoN) < T(0)) s.geoN = -s.geoN;
-            }
-            if (s.anisoRot > T(0))
-            {
-                T ang = s.anisoRot * T(2) * C<T>::PI, sa, ca;
-                Mth<T>::sincos(ang, sa, ca);
-                V3<T> t = s.tangent;
-                s.tangent = v3(ca * t.x + T(0) * t.y + sa * t.z, T(0) * t.x + T(1) * t.y + T(0) * t.z, -sa * t.x + T(0) * t.y + ca * t.z);
-            }
-            if (P.regularize_enable)
-            {
-                if (ps.len >= P.regularize_after_vertices) ps.flags |= F_REG;
-                if (ps.flags & F_REG)
-                {
-                    s.roughness = regularizeR(s.roughness, true);
-                    s.sheenRough = regularizeR(s.sheenRough, false);
-                    s.ccRough = regularizeR(s.ccRough, true);
-                }
-            }
-            s.specular = reflectance(c, s4, M.specular, M.specular_spectrum);
-            s.albedo = reflectance(c, s4, M.albedo, M.albedo_spectrum);
-            bool absZero = M.absorption[0] == 0 && M.absorption[1] == 0 && M.absorption[2] == 0;
-            s.absorption = absZero ? sp(T(0)) : setFromRGBUnboundedNoIllum(c, s4, v3(T(M.absorption[0]), T(M.absorption[1]), T(M.absorption[2])));
-            s.emissive = emission(c, s4, M.emissive, M.emission_spectrum);
-            s.sheenColor = s.sheenAmount > T(0) ? setFromRGB(c, s4, v3(T(M.sheen_tint[0]), T(M.sheen_tint[1]), T(M.sheen_tint[2]))) : sp(T(0));
+            fillSurf(c, s4, h.inst, h.prim, T(h.b1), T(h.b2), rd, true, P.regularize_enable && (ps.flags & F_REG), s);
             V3<T> hitPos = ps.o + ps.d * T(h.t);
             if (dot(rd, s.geoN) > T(0) && ps.nVol == 0 && !(s.flags & YG_MATERIAL_TWO_SIDED)) enterVol(ps, s.ior, s.absorption, I.material);
             S4<T> ab = ps.nVol ? ps.volAbs[ps.nVol - 1] : sp(T(0));
@@ -1773,7 +1906,7 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                 }
                 V3<T> wi = v3(T(0), T(0), T(0));
                 bool diff = false, delta = false;
-                if (layer < 5) wi = sampleLayer(s, sctx, layer, rB[1], rB[2], rB[3], s4.hero, diff, delta);
+                if (layer < 5) wi = sampleLayer<T, false>(&L, s, sctx, layer, rB[1], rB[2], rB[3], s4.hero, diff, delta);
                 EvalR<T> ev;
                 ev.w = sp(T(0));
                 ev.pdf = 0;
@@ -1843,6 +1976,23 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
     }
 }
 
+// whether a render converts RGB colours to spectra, and so needs the scene's rgb_to_spd table
+inline bool needsRgbTable(const oracle_scene* sc, const yg_render_params* P)
+{
+    auto nonGrey = [](const float* v) { return !(v[0] == v[1] && v[1] == v[2]); };
+    auto nonZero = [](const float* v) { return v[0] != 0.0f || v[1] != 0.0f || v[2] != 0.0f; };
+    if (P->env_intensity_scale > 0.0f) return true;
+    for (uint32_t i = 0; i < sc->n_materials; ++i)
+    {
+        const yg_material& m = sc->materials[i];
+        if ((m.albedo_spectrum < 0 && nonGrey(m.albedo)) || (m.specular_spectrum < 0 && nonGrey(m.specular)) ||
+            (m.emission_spectrum < 0 && nonGrey(m.emissive)) || (nonZero(m.absorption) && nonGrey(m.absorption)) ||
+            (m.sheen_amount > 0.0f && nonGrey(m.sheen_tint)))
+            return true;
+    }
+    return false;
+}
+
 template <typename T> int run(const oracle_scene* sc, const yg_render_params* P, int threads, float* records, double* film,
                               oracle_stats* stats)
 {
@@ -1908,6 +2058,8 @@ template <typename T> int run(const oracle_scene* sc, const yg_render_params* P,
     return 0;
 }
 
+#include "oracle_bdpt.inc"
+
 } // namespace orc
 
 extern "C" {
@@ -1916,7 +2068,13 @@ int oracle_render(const oracle_scene* sc, const yg_render_params* P, int precisi
                   oracle_stats* stats)
 {
     if (!sc || !P) return -1;
-    if (P->integrator > YG_INTEGRATOR_NEE) return -1;
+    if (P->integrator > YG_INTEGRATOR_BDPT) return -1;
+    if (!sc->rgb_to_spd && orc::needsRgbTable(sc, P)) return -6; // the RGB -> spectrum table was not given
+    if (P->integrator == YG_INTEGRATOR_BDPT)
+    {
+        if (precision == 64) return orc::runBdpt<double>(sc, P, threads, records, film, stats);
+        return orc::runBdpt<float>(sc, P, threads, records, film, stats);
+    }
     if (precision == 64) return orc::run<double>(sc, P, threads, records, film, stats);
     return orc::run<float>(sc, P, threads, records, film, stats);
 }

@@ -48,3 +48,30 @@ def test_empty_scene_and_black_env_give_zero(host_luts):
     h = pyoracle.OracleSceneHandle(sc, host_luts)
     p = Context.params("uni", 8, 8, spp=1, max_depth=4)
     assert np.all(h.render(p)["records"][..., 1:] == 0)
+
+
+def test_oracle_bdpt_is_deterministic_and_thread_independent(box):
+    _, h = box
+    p = Context.params("bdpt", 24, 24, spp=2, max_depth=8, lambda_range=(380, 780), light_vertices=8)
+    a = h.render(p, precision=32, threads=1)["records"]
+    b = h.render(p, precision=32, threads=5)["records"]
+    assert np.array_equal(a, b)
+    assert np.all(np.isfinite(a)) and a[..., 6].mean() > 0
+
+
+def test_oracle_bdpt_and_nee_estimate_the_same_image_in_fp64(box):
+    # diffuse box, regularisation off, depth large enough that truncation is negligible:
+    # the bidirectional and the NEE estimators converge to the same image
+    _, h = box
+    kw = dict(max_depth=24, regularize=False, lambda_range=(380, 780))
+    W = H = 16
+    spp = 192
+    nee = h.render(Context.params("nee", W, H, spp=spp, **kw), precision=64)["records"][..., 6].astype(np.float64)
+    bd = h.render(Context.params("bdpt", W, H, spp=spp, **kw), precision=64)["records"][..., 6].astype(np.float64)
+    for b in (8,):
+        mn = nee.reshape(spp, H // b, b, W // b, b).mean(axis=(2, 4))
+        mb = bd.reshape(spp, H // b, b, W // b, b).mean(axis=(2, 4))
+        se = np.sqrt(mn.var(axis=0, ddof=1) / spp + mb.var(axis=0, ddof=1) / spp)
+        z = np.abs(mn.mean(axis=0) - mb.mean(axis=0)) / se
+        assert z.max() < 5.0, (z.max(), mn.mean(), mb.mean())
+    assert abs(bd.mean() - nee.mean()) / nee.mean() < 0.03
