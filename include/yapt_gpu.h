@@ -261,6 +261,98 @@ YG_API int yg_last_render_stats(yg_context* ctx, float* kernel_ms, uint64_t* ray
 /* Traversal work of the most recent render made with YG_FLAG_COUNT_TRAVERSAL. */
 YG_API int yg_last_traversal_counts(yg_context* ctx, uint64_t* nodes_visited, uint64_t* triangles_tested);
 
+/* -- serving loop ----------------------------------------------------------------
+ * No counterpart in the reference, which renders one interactive view at a time through
+ * PathTraceStage::update (PathTraceStage.cpp:90-140); this is the request loop of the
+ * serving configuration. A server keeps the scenes of several contexts resident on their
+ * device and renders many requests at once: requests wait in arrival order until their
+ * film fits the memory budget and a slot is free, then every round merges the paths of
+ * all admitted uni/NEE requests (any scene, size, spp, depth) into one wavefront, replayed
+ * as a captured CUDA graph, while BDPT requests advance on a second stream. A request's
+ * result is the same film as yg_render of the same parameters on its context. While a
+ * server exists its contexts must not be rendered with directly. */
+typedef struct yg_server yg_server;
+
+typedef struct yg_server_options
+{
+    uint64_t memory_budget_bytes; /* device bytes for request films and BDPT state (0: 8 GiB) */
+    uint32_t max_active;          /* requests rendered concurrently (0: 64, at most 256) */
+    uint32_t wave_capacity;       /* paths per merged round (0: 2^21; at least one plane of the largest image) */
+    uint32_t round_samples;       /* samples planned per round when several requests share it (0: 2^19) */
+    uint32_t max_depth;           /* largest uni/NEE max_depth accepted (0: 16) */
+    float lambda_min, lambda_max; /* spectral range of every request (0, 0: 380..700) */
+    uint32_t use_graphs;          /* 1: replay the merged round as a captured CUDA graph; 0: plain launches */
+    uint32_t reserved[5];
+} yg_server_options;
+
+typedef struct yg_request
+{
+    uint32_t scene;          /* index into the contexts given to yg_server_create */
+    uint32_t reserved;
+    yg_render_params params; /* flags may hold YG_FLAG_DISABLE_TEXEL_JITTER only */
+} yg_request;
+
+enum
+{
+    YG_REQ_QUEUED = 0,
+    YG_REQ_ACTIVE = 1,
+    YG_REQ_DONE = 2,
+    YG_REQ_FAILED = 3,
+    YG_REQ_CANCELLED = 4
+};
+
+typedef struct yg_request_info
+{
+    int32_t state;  /* YG_REQ_* */
+    int32_t error;  /* YG_ERR_* of a failed request */
+    double t_submit, t_admit, t_done; /* seconds since yg_server_create (-1: not yet) */
+    uint64_t footprint_bytes;
+    uint64_t samples;
+} yg_request_info;
+
+typedef struct yg_server_stats
+{
+    uint64_t submitted, completed, failed, cancelled;
+    uint64_t rounds, graph_replays, bdpt_slices, samples;
+    uint64_t bytes_in_use, peak_bytes_in_use;
+    uint32_t active, queued;
+    double seconds;
+} yg_server_stats;
+
+YG_API int yg_server_create(yg_context* const* scenes, uint32_t n_scenes, const yg_server_options* options,
+                            yg_server** out);
+/* Validates and queues a request (YG_ERR_ADMISSION if it could never fit the budget). */
+YG_API int yg_server_submit(yg_server* server, const yg_request* request, uint64_t* id);
+/* Waits until the request is done, failed or cancelled (YG_ERR_NOT_READY after timeout_s). */
+YG_API int yg_server_wait(yg_server* server, uint64_t id, double timeout_s, yg_request_info* info);
+YG_API int yg_server_info(yg_server* server, uint64_t id, yg_request_info* info);
+/* Mean XYZ per pixel (width x height x 3, zero outside the crop) of a finished request. */
+YG_API int yg_server_result(yg_server* server, uint64_t id, float* xyz_mean, float* counts);
+YG_API int yg_server_cancel(yg_server* server, uint64_t id);
+/* Forgets a finished, failed or cancelled request and its result. */
+YG_API int yg_server_release(yg_server* server, uint64_t id);
+YG_API int yg_server_stats_get(yg_server* server, yg_server_stats* stats);
+/* Cancels what is queued, finishes nothing further, waits for the device and frees it all. */
+YG_API int yg_server_destroy(yg_server* server);
+
+/* One scheduling decision of the serving loop on host data only (no device work), so the
+ * policy can be checked without a GPU. items[i]: pixels, planes still to render, film
+ * footprint, whether admitted already, integrator. Admits queued items in order while the
+ * budget and slots allow (out admit[i] = 1), then plans one merged round for the admitted
+ * uni/NEE items, fewest remaining samples first (out planes[i]). Returns the planned samples. */
+typedef struct yg_sched_item
+{
+    uint64_t pixels;
+    uint32_t planes_left;
+    uint32_t admitted;
+    uint64_t footprint_bytes;
+    uint32_t integrator;
+    uint32_t rounds_waited; /* rounds passed over; from 8 on an item is planned first */
+} yg_sched_item;
+YG_API int64_t yg_server_plan(const yg_sched_item* items, uint32_t n, uint64_t budget_bytes, uint64_t bytes_in_use,
+                              uint32_t max_active, uint32_t wave_capacity, uint32_t round_samples, uint32_t* admit,
+                              uint32_t* planes);
+
 #ifdef __cplusplus
 }
 #endif

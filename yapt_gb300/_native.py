@@ -88,6 +88,44 @@ class SampleRecord(C.Structure):
     _fields_ = [("lambda_hero", C.c_float), ("radiance", C.c_float * 4), ("xyz", C.c_float * 3)]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [
+        ("memory_budget_bytes", C.c_uint64), ("max_active", C.c_uint32), ("wave_capacity", C.c_uint32),
+        ("round_samples", C.c_uint32), ("max_depth", C.c_uint32), ("lambda_min", C.c_float),
+        ("lambda_max", C.c_float), ("use_graphs", C.c_uint32), ("reserved", C.c_uint32 * 5),
+    ]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("reserved", C.c_uint32), ("params", RenderParams)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [
+        ("state", C.c_int32), ("error", C.c_int32), ("t_submit", C.c_double), ("t_admit", C.c_double),
+        ("t_done", C.c_double), ("footprint_bytes", C.c_uint64), ("samples", C.c_uint64),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64), ("cancelled", C.c_uint64),
+        ("rounds", C.c_uint64), ("graph_replays", C.c_uint64), ("bdpt_slices", C.c_uint64), ("samples", C.c_uint64),
+        ("bytes_in_use", C.c_uint64), ("peak_bytes_in_use", C.c_uint64), ("active", C.c_uint32),
+        ("queued", C.c_uint32), ("seconds", C.c_double),
+    ]
+
+
+class SchedItem(C.Structure):
+    _fields_ = [
+        ("pixels", C.c_uint64), ("planes_left", C.c_uint32), ("admitted", C.c_uint32),
+        ("footprint_bytes", C.c_uint64), ("integrator", C.c_uint32), ("rounds_waited", C.c_uint32),
+    ]
+
+
+REQ_STATES = {0: "queued", 1: "active", 2: "done", 3: "failed", 4: "cancelled"}
+
+
 _lib = None
 
 # (name, restype, argtypes) for every function include/yapt_gpu.h declares
@@ -116,6 +154,17 @@ SIGNATURES = [
                                        C.POINTER(C.c_uint32)]),
     ("yg_last_traversal_counts", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("yg_render_samples_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p]),
+    ("yg_server_create", C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
+    ("yg_server_submit", C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    ("yg_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]),
+    ("yg_server_info", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(RequestInfo)]),
+    ("yg_server_result", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    ("yg_server_cancel", C.c_int, [C.c_void_p, C.c_uint64]),
+    ("yg_server_release", C.c_int, [C.c_void_p, C.c_uint64]),
+    ("yg_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("yg_server_destroy", C.c_int, [C.c_void_p]),
+    ("yg_server_plan", C.c_int64, [C.POINTER(SchedItem), C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
+                                   C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
 ]
 
 

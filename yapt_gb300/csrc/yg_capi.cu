@@ -2,10 +2,8 @@
 // submission and film readback. Mirrors the host side of YAPT's path tracer
 // (RaytraceCommonResources.cpp, BindlessMaterialManager.cpp, LightManager.cpp,
 // PathTraceStage.cpp) on one CUDA stream.
-#include "../../include/yapt_gpu.h"
+#include "yg_internal.h"
 #include "yg_bvh.h"
-#include "yg_kernels.h"
-#include "yg_tables.h"
 #include "yg_vec.cuh"
 
 #include <algorithm>
@@ -15,7 +13,7 @@
 #include <string>
 #include <vector>
 
-namespace
+namespace ygi
 {
 thread_local std::string g_lastError;
 
@@ -23,119 +21,6 @@ int fail(int code, const std::string& msg)
 {
     g_lastError = msg;
     return code;
-}
-
-#define YG_CUDA(call)                                                                                              \
-    do                                                                                                             \
-    {                                                                                                              \
-        cudaError_t e_ = (call);                                                                                   \
-        if (e_ != cudaSuccess)                                                                                     \
-            return fail(e_ == cudaErrorMemoryAllocation ? YG_ERR_OUT_OF_MEMORY : YG_ERR_CUDA,                      \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));                                       \
-    } while (0)
-
-struct DevBuf
-{
-    void* p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t n)
-    {
-        if (n <= bytes) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e == cudaSuccess) bytes = n;
-        return e;
-    }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
-struct Mesh
-{
-    uint32_t vertexBase, vertexCount, indexBase, indexCount;
-    bool tangents, uvs;
-    std::vector<std::pair<uint32_t, uint32_t>> submeshes;
-};
-} // namespace
-
-struct yg_context
-{
-    std::mutex lock;
-    int device = 0;
-    int smCount = 152;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t evStart = nullptr, evStop = nullptr;
-    std::string dataDir;
-    // tables
-    std::vector<uint32_t> sobolMatrices;
-    std::vector<double> cie471;
-    yg::MsLuts luts;
-    std::vector<float> rgbToSpd;
-    int rgbLmin = 0, rgbLmax = 0;
-    // scene (host)
-    std::vector<float> positions, normals, uvs;
-    std::vector<float4> tangents;
-    std::vector<uint32_t> indices;
-    std::vector<Mesh> meshes;
-    std::vector<yg_material> materials;
-    std::vector<yg::GpuMaterial> gpuMaterials;
-    std::vector<float> spectra;
-    uint32_t specPoints = 0;
-    float specLmin = 380.f, specLmax = 780.f;
-    std::vector<yg_instance> instances;
-    yg::GpuCamera camera{};
-    bool cameraSet = false;
-    bool sceneBuilt = false;
-    uint64_t nTris = 0, nNodes = 0;
-    // device
-    DevBuf dTris, dNodes, dInst, dMat, dLights, dPos, dNrm, dTan, dUV, dIdx, dSpec;
-    DevBuf dLut[9];
-    DevBuf dCie, dRgb, dSobol, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
-    DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena, dPerm;
-    uint32_t nLights = 0;
-    float worldCenter[3] = {0, 0, 0}; // getWorldCenterAndRadiusSqr (raytraceCommonResources.hlsl:99-104)
-    float worldRadiusSqr = 0;
-    uint32_t permW = 0, permH = 0;    // size of the BDPT pixel permutation in dPerm
-    int cieLmin = -1, cieLmax = -1;
-    uint32_t cieN = 0;
-    float cieYSumInv = 0, d65SumInv = 0;
-    uint32_t filmW = 0, filmH = 0;
-    bool featuresOn = false;
-    // stats
-    float lastMs = 0;
-    uint64_t lastRays = 0;
-    uint32_t lastLaunches = 0;
-
-    ~yg_context()
-    {
-        DevBuf* all[] = {&dTris, &dNodes, &dInst, &dMat, &dLights, &dPos, &dNrm, &dTan, &dUV, &dIdx, &dSpec, &dCie, &dRgb,
-                         &dSobol, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
-                         &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm};
-        for (DevBuf* b : all) b->release();
-        for (auto& b : dLut) b.release();
-        if (evStart) cudaEventDestroy(evStart);
-        if (evStop) cudaEventDestroy(evStop);
-        if (stream) cudaStreamDestroy(stream);
-    }
-};
-
-namespace
-{
-template <typename T>
-int upload(yg_context* c, DevBuf& b, const T* src, size_t count)
-{
-    size_t bytes = std::max<size_t>(sizeof(T) * count, 16);
-    YG_CUDA(b.ensure(bytes));
-    if (count) YG_CUDA(cudaMemcpyAsync(b.p, src, sizeof(T) * count, cudaMemcpyHostToDevice, c->stream));
-    return YG_OK;
 }
 
 float saturatef(float x) { return std::min(std::max(x, 0.0f), 1.0f); }
@@ -259,7 +144,66 @@ int ensureRgbLut(yg_context* c, int lmin, int lmax)
     c->rgbLmax = lmax;
     return upload(c, c->dRgb, c->rgbToSpd.data(), c->rgbToSpd.size());
 }
-} // namespace
+
+// fixed pseudo-random permutation of a crop's pixels for the BDPT camera groups (the texel
+// remap of BidirectionalPathIntegratorSubStage.cpp:549-591, from a seeded splitmix64 generator)
+void pixelPermutation(uint32_t cw, uint32_t ch, std::vector<uint32_t>& perm)
+{
+    const uint64_t npix = (uint64_t)cw * ch;
+    perm.resize(npix);
+    for (uint64_t i = 0; i < npix; ++i) perm[i] = (uint32_t)i;
+    uint64_t state = 0x9E3779B97F4A7C15ull ^ ((uint64_t)cw << 32 | ch);
+    for (uint64_t i = npix - 1; i > 0; --i)
+    {
+        state += 0x9E3779B97F4A7C15ull;
+        uint64_t z = state;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        std::swap(perm[i], perm[z % (i + 1)]);
+    }
+}
+
+void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb, yg::SceneView& S)
+{
+    S = yg::SceneView{};
+    S.tris = ctx->dTris.as<float4>();
+    S.nodes = ctx->dNodes.as<float4>();
+    S.instances = ctx->dInst.as<yg::GpuInstance>();
+    S.materials = ctx->dMat.as<yg::GpuMaterial>();
+    S.lights = ctx->dLights.as<yg::GpuLight>();
+    S.positions = ctx->dPos.as<float>();
+    S.normals = ctx->dNrm.as<float>();
+    S.tangents = ctx->dTan.as<float4>();
+    S.uvs = ctx->dUV.as<float2>();
+    S.indices = ctx->dIdx.as<uint32_t>();
+    S.spectra = ctx->dSpec.as<float>();
+    S.lutSS = ctx->dLut[0].as<float>();
+    S.lutSSAvg = ctx->dLut[1].as<float>();
+    S.lutSSMS = ctx->dLut[2].as<float>();
+    S.lutSSMSAvg = ctx->dLut[3].as<float>();
+    S.lutTransDenser = ctx->dLut[4].as<float>();
+    S.lutTransLighter = ctx->dLut[5].as<float>();
+    S.lutTransAvgDenser = ctx->dLut[6].as<float>();
+    S.lutTransAvgLighter = ctx->dLut[7].as<float>();
+    S.lutSheen = ctx->dLut[8].as<float>();
+    S.cie = ctx->dCie.as<float4>();
+    S.rgbToSpd = needRgb ? ctx->dRgb.as<float>() : nullptr;
+    S.cam = ctx->camera;
+    S.nLights = ctx->nLights;
+    S.nInstances = (uint32_t)ctx->instances.size();
+    S.specPoints = ctx->specPoints;
+    S.specLmin = ctx->specLmin;
+    S.specLmax = ctx->specLmax;
+    S.cieN = ctx->cieN;
+    S.lambdaMin = lminf;
+    S.lambdaMax = lmaxf;
+    S.cieYSumInv = ctx->cieYSumInv;
+    S.d65SumInv = ctx->d65SumInv;
+}
+} // namespace ygi
+
+using namespace ygi;
 
 extern "C" {
 
@@ -752,20 +696,8 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         YG_CUDA(ctx->dArena.ensure(yg::bdptArenaBytes(chunkSpp, lightPaths, lightVerts, npix)));
         if (ctx->permW != cw || ctx->permH != ch)
         {
-            // fixed pseudo-random permutation of the crop's pixels (the texel remap of
-            // BidirectionalPathIntegratorSubStage.cpp:549-591, from a seeded generator)
-            std::vector<uint32_t> perm(npix);
-            for (uint64_t i = 0; i < npix; ++i) perm[i] = (uint32_t)i;
-            uint64_t state = 0x9E3779B97F4A7C15ull ^ ((uint64_t)cw << 32 | ch);
-            for (uint64_t i = npix - 1; i > 0; --i)
-            {
-                state += 0x9E3779B97F4A7C15ull;
-                uint64_t z = state;
-                z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-                z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-                z ^= z >> 31;
-                std::swap(perm[i], perm[z % (i + 1)]);
-            }
+            std::vector<uint32_t> perm;
+            pixelPermutation(cw, ch, perm);
             if ((r = upload(ctx, ctx->dPerm, perm.data(), perm.size()))) return r;
             ctx->permW = cw;
             ctx->permH = ch;
@@ -791,40 +723,8 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
             pts[(size_t)s * yg::kSobolDims + d] = yg::sobolUint(ctx->sobolMatrices.data(), p->spp_start + s, d);
     if ((r = upload(ctx, ctx->dSobol, pts.data(), pts.size()))) return r;
 
-    yg::SceneView S{};
-    S.tris = ctx->dTris.as<float4>();
-    S.nodes = ctx->dNodes.as<float4>();
-    S.instances = ctx->dInst.as<yg::GpuInstance>();
-    S.materials = ctx->dMat.as<yg::GpuMaterial>();
-    S.lights = ctx->dLights.as<yg::GpuLight>();
-    S.positions = ctx->dPos.as<float>();
-    S.normals = ctx->dNrm.as<float>();
-    S.tangents = ctx->dTan.as<float4>();
-    S.uvs = ctx->dUV.as<float2>();
-    S.indices = ctx->dIdx.as<uint32_t>();
-    S.spectra = ctx->dSpec.as<float>();
-    S.lutSS = ctx->dLut[0].as<float>();
-    S.lutSSAvg = ctx->dLut[1].as<float>();
-    S.lutSSMS = ctx->dLut[2].as<float>();
-    S.lutSSMSAvg = ctx->dLut[3].as<float>();
-    S.lutTransDenser = ctx->dLut[4].as<float>();
-    S.lutTransLighter = ctx->dLut[5].as<float>();
-    S.lutTransAvgDenser = ctx->dLut[6].as<float>();
-    S.lutTransAvgLighter = ctx->dLut[7].as<float>();
-    S.lutSheen = ctx->dLut[8].as<float>();
-    S.cie = ctx->dCie.as<float4>();
-    S.rgbToSpd = needRgb ? ctx->dRgb.as<float>() : nullptr;
-    S.cam = ctx->camera;
-    S.nLights = ctx->nLights;
-    S.nInstances = (uint32_t)ctx->instances.size();
-    S.specPoints = ctx->specPoints;
-    S.specLmin = ctx->specLmin;
-    S.specLmax = ctx->specLmax;
-    S.cieN = ctx->cieN;
-    S.lambdaMin = lminf;
-    S.lambdaMax = lmaxf;
-    S.cieYSumInv = ctx->cieYSumInv;
-    S.d65SumInv = ctx->d65SumInv;
+    yg::SceneView S;
+    fillSceneView(ctx, lminf, lmaxf, needRgb, S);
 
     yg::LaunchParams L{};
     L.integrator = p->integrator;
@@ -1097,41 +997,9 @@ YG_API int yg_render_samples_noalloc(yg_context* ctx, const yg_render_params* p,
     YG_CUDA(cudaMemcpyAsync(matrices, ctx->sobolMatrices.data(), kNoAllocMatrixBytes, cudaMemcpyHostToDevice, ctx->stream));
     noallocSobolPoints<<<ctx->smCount, 256, 0, ctx->stream>>>(matrices, p->spp_start, p->spp_count, sobolPts);
 
-    yg::SceneView S{};
-    S.tris = ctx->dTris.as<float4>();
-    S.nodes = ctx->dNodes.as<float4>();
-    S.instances = ctx->dInst.as<yg::GpuInstance>();
-    S.materials = ctx->dMat.as<yg::GpuMaterial>();
-    S.lights = ctx->dLights.as<yg::GpuLight>();
-    S.positions = ctx->dPos.as<float>();
-    S.normals = ctx->dNrm.as<float>();
-    S.tangents = ctx->dTan.as<float4>();
-    S.uvs = ctx->dUV.as<float2>();
-    S.indices = ctx->dIdx.as<uint32_t>();
-    S.spectra = ctx->dSpec.as<float>();
-    S.lutSS = ctx->dLut[0].as<float>();
-    S.lutSSAvg = ctx->dLut[1].as<float>();
-    S.lutSSMS = ctx->dLut[2].as<float>();
-    S.lutSSMSAvg = ctx->dLut[3].as<float>();
-    S.lutTransDenser = ctx->dLut[4].as<float>();
-    S.lutTransLighter = ctx->dLut[5].as<float>();
-    S.lutTransAvgDenser = ctx->dLut[6].as<float>();
-    S.lutTransAvgLighter = ctx->dLut[7].as<float>();
-    S.lutSheen = ctx->dLut[8].as<float>();
-    S.cie = ctx->dCie.as<float4>();
-    S.rgbToSpd = needRgb ? ctx->dRgb.as<float>() : nullptr;
+    yg::SceneView S;
+    fillSceneView(ctx, lminf, lmaxf, needRgb, S);
     S.sobol = sobolPts;
-    S.cam = ctx->camera;
-    S.nLights = ctx->nLights;
-    S.nInstances = (uint32_t)ctx->instances.size();
-    S.specPoints = ctx->specPoints;
-    S.specLmin = ctx->specLmin;
-    S.specLmax = ctx->specLmax;
-    S.cieN = ctx->cieN;
-    S.lambdaMin = lminf;
-    S.lambdaMax = lmaxf;
-    S.cieYSumInv = ctx->cieYSumInv;
-    S.d65SumInv = ctx->d65SumInv;
 
     yg::LaunchParams L{};
     L.integrator = p->integrator;

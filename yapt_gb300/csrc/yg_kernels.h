@@ -16,6 +16,24 @@ int launchFeatures(float4* accA, float4* accN, const float4* fa, const float4* f
                    uint32_t cw, uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
 int launchRelmse(const float4* sum, const float* ref, uint32_t npix, double eps, double* out, int smCount,
                  cudaStream_t stream);
+// Merged wavefront of several requests (serving). All tables live in device memory and are
+// read by the kernels, so a captured launch sequence can be replayed round after round.
+struct MultiTables
+{
+    const SceneView* views;      // [request slot] scene arrays, Sobol points of the round
+    const LaunchParams* params;  // [request slot] image, depth, integrator, sample buffer of the round
+    const uint32_t* segReq;      // [segment] request slot
+    const uint32_t* segStart;    // [segment + 1] first wave slot (prefix sums of plane counts x pixels)
+    const uint32_t* segPixStart; // [segment + 1] first pixel of the film pass (prefix sums of pixels)
+    const uint32_t* nSeg;        // segments in this round
+    float4* const* filmSum;      // [request slot] Kahan film sums and compensations
+    float4* const* filmComp;
+    uint32_t* req;               // [wave slot] request slot (set by the launcher)
+    uint32_t* local;             // [wave slot] sample index within the request's round
+};
+size_t multiWaveBytes(uint32_t capacity);
+int launchWavefrontMulti(const MultiTables& M, void* arena, uint32_t capacity, uint32_t maxDepth,
+                         unsigned long long* rayCounter, int smCount, cudaStream_t stream);
 // Bidirectional integrator over P.sppCount sample indices. `arena` holds
 // bdptArenaBytes(P.sppCount, lightPaths, maxLightVerts, cropW*cropH) bytes; `perm` is a
 // permutation of the crop's pixel indices (camera groups take 64 consecutive entries).

@@ -1,0 +1,265 @@
+// Serving-loop kernels: the merged wavefront that carries the paths of several render
+// requests (different scenes, image sizes, sample counts, depths; uni and NEE) in one set of
+// queues, with a per-segment Kahan film pass.
+#include <algorithm>
+
+#include "yg_wave.cuh"
+
+namespace yg
+{
+
+// ---------------------------------------------------------------- merged wavefront (serving)
+// One wave holds the paths of several requests (each a segment of consecutive wave slots:
+// whole sample planes of one request), possibly of different scenes, sizes, depths and of
+// both unidirectional integrators. Every per-round quantity is read from device tables, so
+// one captured launch sequence serves every round. A path computes exactly what it computes
+// in a request of its own.
+
+YG_DEV uint32_t segmentOf(const MultiTables& M, uint32_t nSeg, uint32_t s)
+{
+    uint32_t lo = 0, hi = nSeg; // segStart[lo] <= s < segStart[hi]
+    while (hi - lo > 1)
+    {
+        uint32_t mid = (lo + hi) >> 1;
+        if (M.segStart[mid] <= s) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) wfmGenerate(MultiTables M, WaveState W, RayQueue Q)
+{
+    const uint32_t nSeg = *M.nSeg;
+    const uint32_t total = M.segStart[nSeg];
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < total; s += gridDim.x * blockDim.x)
+    {
+        uint32_t k = segmentOf(M, nSeg, s);
+        uint32_t req = M.segReq[k];
+        uint32_t local = s - M.segStart[k];
+        const SceneView& S = M.views[req];
+        const LaunchParams& P = M.params[req];
+        uint32_t sl, cx, cy;
+        pixelOf(P, local, sl, cx, cy);
+        uint32_t seed = (cy * P.width + cx) ^ (P.seed * 0x9E3779B9u);
+        RandomSampler rs{S.sobol + (size_t)sl * kSobolDims, 2u, seed};
+        Spectral sp;
+        PathState ps;
+        beginPath(S, P, cx, cy, rs, sp, ps);
+        storePath(W, s, ps, rs, sp.hero, sl, false);
+        M.req[s] = req;
+        M.local[s] = local;
+        Q.o[s] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, __uint_as_float(s));
+        Q.d[s] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, 0.0f);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = total;
+}
+
+__global__ void __launch_bounds__(128) wfmTrace(MultiTables M, RayQueue Q, HitQueue H, unsigned long long* rayCtr)
+{
+    const uint32_t n = *Q.count;
+    uint32_t rays = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        float4 o = Q.o[i], d = Q.d[i];
+        const SceneView& S = M.views[M.req[__float_as_uint(o.w)]];
+        Hit h;
+        bool found = traceClosest<false>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000),
+                                         h, nullptr);
+        rays++;
+        H.a[i] = mk4(h.t, h.b1, h.b2, __uint_as_float(h.instance));
+        H.b[i] = found ? (h.prim | (h.front ? 0x80000000u : 0u)) : 0xffffffffu;
+    }
+    countRays(rayCtr, rays);
+}
+
+__global__ void __launch_bounds__(128) wfmShade(MultiTables M, WaveState W, RayQueue Qin, HitQueue H, RayQueue Qout,
+                                                ShadowQueue SQ)
+{
+    const uint32_t n = *Qin.count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        uint32_t i = first + r * stride;
+        bool active = i < n;
+        bool alive = false;
+        ShadowRequest sr;
+        sr.valid = false;
+        uint32_t slot = 0;
+        PathState ps;
+        if (active)
+        {
+            slot = __float_as_uint(Qin.o[i].w);
+            const uint32_t req = M.req[slot];
+            const SceneView& S = M.views[req];
+            const LaunchParams& P = M.params[req];
+            const Luts Lt = lutsOf(S);
+            RandomSampler rs;
+            Spectral sp;
+            loadPath(W, slot, ps, rs, sp, S);
+            uint32_t nVol0 = ps.nVol;
+            float4 ha = H.a[i];
+            uint32_t hb = H.b[i];
+            bool found = hb != 0xffffffffu;
+            Hit hit;
+            hit.t = ha.x;
+            hit.b1 = ha.y;
+            hit.b2 = ha.z;
+            hit.instance = __float_as_uint(ha.w);
+            hit.prim = hb & 0x7fffffffu;
+            hit.front = (hb & 0x80000000u) != 0;
+            if (P.integrator == 1) alive = shadeSegment<true>(S, P, Lt, sp, found, hit, ps, rs, sr, nullptr);
+            else alive = shadeSegment<false>(S, P, Lt, sp, found, hit, ps, rs, sr, nullptr);
+            alive = alive && ps.pathLength < P.maxDepth;
+            storePath(W, slot, ps, rs, sp.hero, (uint32_t)(rs.point - S.sobol) / kSobolDims, ps.nVol != 0 || nVol0 != 0);
+        }
+        uint32_t k = warpAppend(Qout.count, alive);
+        if (alive)
+        {
+            Qout.o[k] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, __uint_as_float(slot));
+            Qout.d[k] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, 0.0f);
+        }
+        uint32_t j = warpAppend(SQ.count, sr.valid);
+        if (sr.valid)
+        {
+            SQ.o[j] = mk4(sr.origin.x, sr.origin.y, sr.origin.z, __uint_as_float(slot));
+            SQ.d[j] = mk4(sr.dir.x, sr.dir.y, sr.dir.z, sr.tmax);
+            SQ.target[j] = make_uint2(sr.instance, sr.prim);
+            SQ.contrib[j] = sr.contrib;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) wfmShadow(MultiTables M, WaveState W, ShadowQueue SQ, unsigned long long* rayCtr)
+{
+    const uint32_t n = *SQ.count;
+    uint32_t rays = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        float4 o = SQ.o[i], d = SQ.d[i];
+        uint2 tg = SQ.target[i];
+        uint32_t s = __float_as_uint(o.w);
+        const SceneView& S = M.views[M.req[s]];
+        Hit h;
+        bool any = traceClosest<false>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, h, nullptr);
+        rays++;
+        if (shadowVisible(any, h, tg.x, tg.y)) W.tot[s] = W.tot[s] + SQ.contrib[i];
+    }
+    countRays(rayCtr, rays);
+}
+
+__global__ void __launch_bounds__(256) wfmFinalize(MultiTables M, WaveState W)
+{
+    const uint32_t total = M.segStart[*M.nSeg];
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < total; s += gridDim.x * blockDim.x)
+    {
+        const uint32_t req = M.req[s];
+        const SceneView& S = M.views[req];
+        const LaunchParams& P = M.params[req];
+        Spectral sp;
+        spectralOf(S, W.dirHero[s].w, sp);
+        FirstHit fh{mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), 0.0f};
+        writeSample(S, P, M.local[s], sp, W.tot[s], fh);
+    }
+}
+
+// Kahan film of every segment: the request's pixels, its planes of this round in order
+__global__ void __launch_bounds__(256) wfmFilm(MultiTables M)
+{
+    const uint32_t nSeg = *M.nSeg;
+    const uint32_t totalPix = M.segPixStart[nSeg];
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < totalPix; q += gridDim.x * blockDim.x)
+    {
+        uint32_t lo = 0, hi = nSeg;
+        while (hi - lo > 1)
+        {
+            uint32_t mid = (lo + hi) >> 1;
+            if (M.segPixStart[mid] <= q) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t req = M.segReq[lo];
+        const LaunchParams& P = M.params[req];
+        const uint32_t npix = P.cropW * P.cropH;
+        const uint32_t p = q - M.segPixStart[lo];
+        const uint32_t nspp = (M.segStart[lo + 1] - M.segStart[lo]) / npix;
+        const uint32_t x = P.cropX + p % P.cropW, y = P.cropY + p / P.cropW;
+        const size_t fi = (size_t)y * P.width + x;
+        float4* sum = M.filmSum[req];
+        float4* comp = M.filmComp[req];
+        float4 sacc = sum[fi], c = comp[fi];
+        for (uint32_t k = 0; k < nspp; ++k)
+        {
+            float4 v = P.sampleXYZ[(size_t)k * npix + p];
+            float4 yv = v - c;
+            float4 t = sacc + yv;
+            c = (t - sacc) - yv;
+            sacc = t;
+        }
+        sum[fi] = sacc;
+        comp[fi] = c;
+    }
+}
+
+size_t multiWaveBytes(uint32_t capacity)
+{
+    return (size_t)capacity * (wavefrontBytesPerSlot() + 8) + (64u << 10);
+}
+
+int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, uint32_t maxDepth,
+                         unsigned long long* rayCounter, int smCount, cudaStream_t stream)
+{
+    char* p = static_cast<char*>(arena);
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    const size_t C = capacity;
+    MultiTables M = M0;
+    WaveState W;
+    W.capacity = capacity;
+    W.thr = (float4*)take(C * 16);
+    W.tot = (float4*)take(C * 16);
+    W.orgPdf = (float4*)take(C * 16);
+    W.dirHero = (float4*)take(C * 16);
+    W.misc = (uint4*)take(C * 16);
+    W.volIOR = (float4*)take(C * 16);
+    W.volMat = (uint4*)take(C * 16);
+    W.volAbs = (float4*)take(C * 64);
+    W.fhAlb = (float4*)take(C * 16);
+    W.fhNrm = (float4*)take(C * 16);
+    M.req = (uint32_t*)take(C * 4);
+    M.local = (uint32_t*)take(C * 4);
+    uint32_t* counters = (uint32_t*)take(256);
+    RayQueue QA{(float4*)take(C * 16), (float4*)take(C * 16), counters + 0};
+    RayQueue QB{(float4*)take(C * 16), (float4*)take(C * 16), counters + 1};
+    HitQueue H{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
+    ShadowQueue SQ{(float4*)take(C * 16), (float4*)take(C * 16), (uint2*)take(C * 8), (float4*)take(C * 16),
+                   counters + 2};
+    const int traceBlocks = smCount * 16, shadeBlocks = smCount * 8;
+    int gblocks = (int)std::min<uint64_t>((C + 255) / 256, (uint64_t)smCount * 8);
+    int launches = 0;
+    wfmGenerate<<<gblocks, 256, 0, stream>>>(M, W, QA);
+    ++launches;
+    RayQueue* cur = &QA;
+    RayQueue* nxt = &QB;
+    for (uint32_t b = 0; b < maxDepth; ++b)
+    {
+        wfmTrace<<<traceBlocks, 128, 0, stream>>>(M, *cur, H, rayCounter);
+        cudaMemsetAsync(nxt->count, 0, 4, stream);
+        cudaMemsetAsync(SQ.count, 0, 4, stream);
+        wfmShade<<<shadeBlocks, 128, 0, stream>>>(M, W, *cur, H, *nxt, SQ);
+        wfmShadow<<<traceBlocks, 128, 0, stream>>>(M, W, SQ, rayCounter);
+        launches += 3;
+        RayQueue* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    wfmFinalize<<<gblocks, 256, 0, stream>>>(M, W);
+    wfmFilm<<<gblocks, 256, 0, stream>>>(M);
+    launches += 2;
+    return launches;
+}
+
+} // namespace yg

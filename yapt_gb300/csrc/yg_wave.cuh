@@ -1,0 +1,158 @@
+// Device helpers and the structure-of-arrays path state shared by the wavefront kernels
+// (single request: yg_integrator.cu; merged requests of the serving loop: yg_serve_kernels.cu).
+#pragma once
+#include "yg_path.cuh"
+#include "yg_kernels.h"
+
+namespace yg
+{
+
+__device__ __forceinline__ uint32_t warpAppend(uint32_t* counter, bool pred)
+{
+    // one atomic per warp; returns this lane's slot (valid only where pred)
+    // called by all 32 lanes of a warp (the callers iterate a warp-uniform trip count)
+    uint32_t mask = __ballot_sync(0xffffffffu, pred);
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t leader = mask ? (uint32_t)(__ffs(mask) - 1) : 0u;
+    uint32_t base = 0;
+    if (mask && lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void countRays(unsigned long long* ctr, uint32_t n)
+{
+    if (!ctr) return;
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+    if ((threadIdx.x & 31) == 0 && n) atomicAdd(ctr, (unsigned long long)n);
+}
+
+__device__ __forceinline__ void countTraversal(unsigned long long* ctr, const TraversalCount& tc)
+{
+    if (!ctr) return;
+    unsigned long long n = tc.nodes, t = tc.tris;
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        n += __shfl_down_sync(0xffffffffu, n, o);
+        t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(ctr, n);
+        atomicAdd(ctr + 1, t);
+    }
+}
+
+YG_DEV void pixelOf(const LaunchParams& P, uint64_t idx, uint32_t& sl, uint32_t& cx, uint32_t& cy)
+{
+    const uint64_t npix = (uint64_t)P.cropW * P.cropH;
+    sl = (uint32_t)(idx / npix);
+    uint32_t pl = (uint32_t)(idx - (uint64_t)sl * npix);
+    cx = P.cropX + pl % P.cropW;
+    cy = P.cropY + pl / P.cropW;
+}
+
+YG_DEV Luts lutsOf(const SceneView& S)
+{
+    return Luts{S.lutSS, S.lutSSAvg, S.lutSSMS, S.lutSSMSAvg, S.lutTransDenser, S.lutTransLighter,
+                S.lutTransAvgDenser, S.lutTransAvgLighter, S.lutSheen};
+}
+
+YG_DEV void writeSample(const SceneView& S, const LaunchParams& P, uint64_t idx, const Spectral& sp, float4 total,
+                        const FirstHit& fh)
+{
+    float3 X = toXYZ(S, sp, total);
+    P.sampleXYZ[idx] = mk4(X.x, X.y, X.z, 1.0f);
+    if (P.dump)
+    {
+        float* d = P.dump + idx * 8;
+        d[0] = sp.hero;
+        d[1] = total.x; d[2] = total.y; d[3] = total.z; d[4] = total.w;
+        d[5] = X.x; d[6] = X.y; d[7] = X.z;
+    }
+    if (P.featAlbedo)
+    {
+        P.featAlbedo[idx] = mk4(fh.albedo.x, fh.albedo.y, fh.albedo.z, 0.0f);
+        P.featNormalDepth[idx] = mk4(fh.normal.x, fh.normal.y, fh.normal.z, fh.depth);
+    }
+}
+
+// ------------------------------------------------------------------ wavefront
+// Path state of one wave, structure of arrays (index = slot = sample index - wave base).
+struct WaveState
+{
+    float4* thr;      // throughput
+    float4* tot;      // accumulated radiance
+    float4* orgPdf;   // ray origin, pdfThisRay
+    float4* dirHero;  // ray direction, hero wavelength
+    uint4* misc;      // flags | pathLength << 8 | nVol << 16, dimension cursor, scramble seed, Sobol row
+    float4* volIOR;   // volume stack (RAY_MAX_VOLUMES_ENTERED = 4)
+    uint4* volMat;
+    float4* volAbs;   // [4][capacity]
+    float4* fhAlb;    // first-hit features of the wave
+    float4* fhNrm;
+    uint32_t capacity;
+};
+struct RayQueue
+{
+    float4* o; // origin, slot
+    float4* d; // direction
+    uint32_t* count;
+};
+struct HitQueue
+{
+    float4* a;    // t, b1, b2, instance
+    uint32_t* b;  // prim | front << 31, or 0xffffffff for a miss
+};
+struct ShadowQueue
+{
+    float4* o;        // origin, slot
+    float4* d;        // direction, tmax
+    uint2* target;    // light instance, primitive
+    float4* contrib;
+    uint32_t* count;
+};
+
+YG_DEV void loadPath(const WaveState& W, uint32_t s, PathState& ps, RandomSampler& rs, Spectral& sp, const SceneView& S)
+{
+    float4 t = W.thr[s], a = W.tot[s], o = W.orgPdf[s], d = W.dirHero[s];
+    uint4 m = W.misc[s];
+    ps.throughput = t;
+    ps.total = a;
+    ps.origin = mk3(o.x, o.y, o.z);
+    ps.pdfThisRay = o.w;
+    ps.dir = mk3(d.x, d.y, d.z);
+    ps.flags = m.x & 0xffu;
+    ps.pathLength = (m.x >> 8) & 0xffu;
+    ps.nVol = (m.x >> 16) & 0xffu;
+    rs.dim = m.y;
+    rs.seed = m.z;
+    rs.point = S.sobol + (size_t)m.w * kSobolDims;
+    spectralOf(S, d.w, sp);
+    if (ps.nVol)
+    {
+        float4 vi = W.volIOR[s];
+        uint4 vm = W.volMat[s];
+        ps.volIOR[0] = vi.x; ps.volIOR[1] = vi.y; ps.volIOR[2] = vi.z; ps.volIOR[3] = vi.w;
+        ps.volMat[0] = vm.x; ps.volMat[1] = vm.y; ps.volMat[2] = vm.z; ps.volMat[3] = vm.w;
+        for (int k = 0; k < kMaxVolumes; ++k) ps.volAbs[k] = W.volAbs[(size_t)k * W.capacity + s];
+    }
+}
+
+YG_DEV void storePath(const WaveState& W, uint32_t s, const PathState& ps, const RandomSampler& rs, float hero,
+                      uint32_t row, bool volumesTouched)
+{
+    W.thr[s] = ps.throughput;
+    W.tot[s] = ps.total;
+    W.orgPdf[s] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, ps.pdfThisRay);
+    W.dirHero[s] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, hero);
+    W.misc[s] = make_uint4(ps.flags | (ps.pathLength << 8) | (ps.nVol << 16), rs.dim, rs.seed, row);
+    if (volumesTouched)
+    {
+        W.volIOR[s] = mk4(ps.volIOR[0], ps.volIOR[1], ps.volIOR[2], ps.volIOR[3]);
+        W.volMat[s] = make_uint4(ps.volMat[0], ps.volMat[1], ps.volMat[2], ps.volMat[3]);
+        for (int k = 0; k < kMaxVolumes; ++k) W.volAbs[(size_t)k * W.capacity + s] = ps.volAbs[k];
+    }
+}
+
+} // namespace yg

@@ -130,3 +130,118 @@ def xyz_to_srgb_linear(xyz):
     """c_srgbXYZToRGB (colorSpaces.hlsl:18-23)."""
     M = np.array([[3.2406, -1.5372, -0.4986], [-0.9689, 1.8758, 0.0415], [0.0557, -0.2040, 1.0570]], np.float32)
     return xyz @ M.T
+
+
+class Server:
+    """The serving loop (yg_server_*): requests on resident scenes, continuous batching.
+
+    contexts: Context objects with scenes built (they stay resident; do not render on them
+    directly while the server lives). Options as yg_server_options."""
+
+    def __init__(self, contexts, memory_budget_bytes=0, max_active=0, wave_capacity=0, round_samples=0, max_depth=0,
+                 lambda_range=(380.0, 700.0), use_graphs=True):
+        self.lib = N.load()
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
+        o = N.ServerOptions()
+        o.memory_budget_bytes = int(memory_budget_bytes)
+        o.max_active = int(max_active)
+        o.wave_capacity = int(wave_capacity)
+        o.round_samples = int(round_samples)
+        o.max_depth = int(max_depth)
+        o.lambda_min, o.lambda_max = float(lambda_range[0]), float(lambda_range[1])
+        o.use_graphs = 1 if use_graphs else 0
+        h = C.c_void_p()
+        N.check(self.lib.yg_server_create(arr, len(self.contexts), C.byref(o), C.byref(h)))
+        self.h = h
+        self.sizes = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.yg_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, scene, params):
+        """Queues a request (params from Context.params); returns its id."""
+        q = N.Request()
+        q.scene = int(scene)
+        q.params = params
+        rid = C.c_uint64()
+        N.check(self.lib.yg_server_submit(self.h, C.byref(q), C.byref(rid)))
+        self.sizes[rid.value] = (params.width, params.height)
+        return rid.value
+
+    @staticmethod
+    def _info(i):
+        return dict(state=N.REQ_STATES[i.state], error=i.error, t_submit=i.t_submit, t_admit=i.t_admit, t_done=i.t_done,
+                    footprint_bytes=i.footprint_bytes, samples=i.samples)
+
+    def wait(self, rid, timeout=-1.0):
+        """Blocks until the request finishes (or timeout seconds); returns its info dict."""
+        i = N.RequestInfo()
+        rc = self.lib.yg_server_wait(self.h, int(rid), float(timeout), C.byref(i))
+        if rc == -4:
+            return self._info(i)
+        N.check(rc)
+        return self._info(i)
+
+    def info(self, rid):
+        i = N.RequestInfo()
+        N.check(self.lib.yg_server_info(self.h, int(rid), C.byref(i)))
+        return self._info(i)
+
+    def result(self, rid):
+        w, h = self.sizes[rid]
+        xyz = np.zeros((h, w, 3), np.float32)
+        cnt = np.zeros((h, w), np.float32)
+        N.check(self.lib.yg_server_result(self.h, int(rid), xyz.ctypes.data_as(C.POINTER(C.c_float)),
+                                          cnt.ctypes.data_as(C.POINTER(C.c_float))))
+        return xyz, cnt
+
+    def cancel(self, rid):
+        N.check(self.lib.yg_server_cancel(self.h, int(rid)))
+
+    def release(self, rid):
+        N.check(self.lib.yg_server_release(self.h, int(rid)))
+        self.sizes.pop(rid, None)
+
+    def stats(self):
+        s = N.ServerStats()
+        N.check(self.lib.yg_server_stats_get(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.ServerStats._fields_}
+
+
+def plan_round(items, budget_bytes, bytes_in_use=0, max_active=64, wave_capacity=1 << 21, round_samples=1 << 19):
+    """One admission + planning decision of the serving loop on host data (yg_server_plan).
+    items: dicts with pixels, planes_left, admitted, footprint_bytes, integrator, rounds_waited.
+    Returns (admit flags, planes per item, planned samples)."""
+    lib = N.load()
+    n = len(items)
+    arr = (N.SchedItem * max(n, 1))()
+    for i, it in enumerate(items):
+        arr[i].pixels = int(it["pixels"])
+        arr[i].planes_left = int(it["planes_left"])
+        arr[i].admitted = 1 if it.get("admitted") else 0
+        arr[i].footprint_bytes = int(it.get("footprint_bytes", 0))
+        arr[i].integrator = int(N.INTEGRATORS[it["integrator"]] if isinstance(it.get("integrator", 1), str)
+                                else it.get("integrator", 1))
+        arr[i].rounds_waited = int(it.get("rounds_waited", 0))
+    adm = (C.c_uint32 * max(n, 1))()
+    pl = (C.c_uint32 * max(n, 1))()
+    total = lib.yg_server_plan(arr, n, int(budget_bytes), int(bytes_in_use), int(max_active), int(wave_capacity),
+                               int(round_samples), adm, pl)
+    if total < 0:
+        raise N.YaptError(lib.yg_last_error().decode())
+    return [int(adm[i]) for i in range(n)], [int(pl[i]) for i in range(n)], int(total)
