@@ -32,6 +32,14 @@ METRIC = "Msamples/s (NEE, random-shapes scene, 1024x1024, 64 spp, depth 12, equ
 BDPT_WORKLOAD = dict(workload="bdpt_caustic_box_150_spheres_10_sphere_lights", width=512, height=512, spp=32,
                      max_depth=10, light_vertices=10, integrator="bdpt", lambda_nm=[380, 780], scene_seed=0)
 BDPT_METRIC = "Msamples/s (BDPT with MIS, caustic box scene, 512x512, 32 spp, depth 10)"
+# --workload serve: the serving loop. 8 resident scene variants of the box layout (about 10k to
+# 2M triangles), one trace of requests (resolution from {128,256,512,1024}^2, spp from
+# {1,4,16,64}, integrator from {uni, NEE, BDPT}, scene uniform) replayed with Poisson arrivals at
+# each rate; every request is also run alone to give its isolated latency.
+SERVE_WORKLOAD = dict(workload="serve_poisson_8_box_variants_10k_to_2M_triangles", resolutions=[128, 256, 512, 1024],
+                      spp=[1, 4, 16, 64], integrators=["uni", "nee", "bdpt"], rates_per_s=[50, 100, 200, 400, 800],
+                      requests=24, max_depth=8, light_vertices=8, lambda_nm=[380, 780], seed=0)
+SERVE_METRIC = "serve: Msamples/s at full load with p50/p99 latency (Poisson arrivals, mixed sizes/spp/integrators)"
 CPU_CROP = (256, 256, 512, 512)  # bounded CPU sample: 512x512 centre crop
 CPU_SPP = 32
 
@@ -288,6 +296,90 @@ def run_ours(args, world, rank, local):
     ctx.close()
 
 
+def run_serve(args, world, rank, local):
+    import numpy as np
+    from yapt_gb300 import configs
+    from yapt_gb300.runtime import Context, Server
+    if rank != 0:
+        return
+    W = SERVE_WORKLOAD
+    t0 = time.time()
+    scenes = [configs.serve_scene(v) for v in range(8)]
+    ctxs = []
+    for sc in scenes:
+        c = Context(local)
+        c.upload_scene(sc)
+        ctxs.append(c)
+    setup_s = time.time() - t0
+    rng = np.random.Generator(np.random.PCG64(W["seed"]))
+    trace = []
+    for i in range(W["requests"]):
+        res = int(rng.choice(W["resolutions"]))
+        spp = int(rng.choice(W["spp"]))
+        integ = str(rng.choice(W["integrators"]))
+        scene = int(rng.integers(8))
+        p = Context.params(integ, res, res, spp_start=0, spp=spp, max_depth=W["max_depth"],
+                           lambda_range=W["lambda_nm"], seed=i, light_vertices=W["light_vertices"])
+        trace.append((scene, p, integ, res, spp))
+    total_samples = sum(res * res * spp for (_, _, _, res, spp) in trace)
+    srv = Server(ctxs, lambda_range=W["lambda_nm"], max_depth=W["max_depth"], memory_budget_bytes=64 << 30)
+    # warm-up: compile the merged round's graph and touch every scene
+    for s in range(8):
+        srv.wait(srv.submit(s, Context.params("nee", 64, 64, spp=1, max_depth=W["max_depth"], lambda_range=W["lambda_nm"])))
+    srv.wait(srv.submit(0, Context.params("bdpt", 64, 64, spp=1, max_depth=W["max_depth"], lambda_range=W["lambda_nm"],
+                                          light_vertices=W["light_vertices"])))
+    # isolated latency of every request (alone on the server)
+    iso, iso_res = [], []
+    for (scene, p, _, _, _) in trace:
+        rid = srv.submit(scene, p)
+        info = srv.wait(rid)
+        iso.append(info["t_done"] - info["t_submit"])
+        iso_res.append(srv.result(rid)[0])
+        srv.release(rid)
+    per_rate = []
+    identical = 0
+    compared = 0
+    # the rate at which the trace's offered work equals the GPU's capacity (full load), then the
+    # configuration's rates (all of them beyond capacity for this trace)
+    full_load_rate = len(trace) / float(np.sum(iso))
+    for rate in [full_load_rate] + list(W["rates_per_s"]):
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(trace)))
+        start = time.time()
+        ids = []
+        for k, (scene, p, _, _, _) in enumerate(trace):
+            delay = arrivals[k] - (time.time() - start)
+            if delay > 0:
+                time.sleep(delay)
+            ids.append(srv.submit(scene, p))
+        infos = [srv.wait(r) for r in ids]
+        makespan = max(i["t_done"] for i in infos) - min(i["t_submit"] for i in infos)
+        lat = np.array([i["t_done"] - i["t_submit"] for i in infos])
+        slow = lat / np.array(iso)
+        for k, r in enumerate(ids):
+            compared += 1
+            identical += int(np.array_equal(srv.result(r)[0], iso_res[k]))
+            srv.release(r)
+        per_rate.append({"rate_per_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
+                         "p99_latency_s": float(np.percentile(lat, 99)),
+                         "p50_slowdown": float(np.percentile(slow, 50)), "p99_slowdown": float(np.percentile(slow, 99)),
+                         "makespan_s": makespan, "msamples_per_s": total_samples / makespan / 1e6})
+    st = srv.stats()
+    srv.close()
+    for c in ctxs:
+        c.close()
+    best = per_rate[0]
+    line = {"metric": SERVE_METRIC, "value": best["msamples_per_s"], "unit": "Msamples/s", "n_gpus": 1,
+            "steps": len(per_rate), "warmup": 9, "full_load_rate_per_s": full_load_rate, "ms_per_step": best["makespan_s"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(W, triangles=[s.triangle_count() for s in scenes], scene_setup_s=setup_s,
+                           trace_samples=total_samples),
+            "serve": per_rate, "isolated_latency_s": {"p50": float(np.percentile(iso, 50)), "p99": float(np.percentile(iso, 99)),
+                                                      "sum": float(np.sum(iso))},
+            "results_identical_alone_and_in_mix": "%d/%d" % (identical, compared),
+            "server": {k: st[k] for k in ("rounds", "graph_replays", "bdpt_slices", "peak_bytes_in_use")}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -297,7 +389,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", type=int, default=0, help="image side for a smaller profiling case")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel for a smaller profiling case")
-    ap.add_argument("--workload", default="nee", choices=["nee", "bdpt"])
+    ap.add_argument("--workload", default="nee", choices=["nee", "bdpt", "serve"])
     args = ap.parse_args()
     if args.workload == "bdpt":
         WORKLOAD.clear()
@@ -307,6 +399,13 @@ def main():
     if args.spp:
         WORKLOAD["spp"] = args.spp
     world, rank, local = dist_setup()
+    if args.workload == "serve":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop"}), flush=True)
+            return
+        run_serve(args, world, rank, local)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

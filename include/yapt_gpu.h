@@ -353,6 +353,59 @@ YG_API int64_t yg_server_plan(const yg_sched_item* items, uint32_t n, uint64_t b
                               uint32_t max_active, uint32_t wave_capacity, uint32_t round_samples, uint32_t* admit,
                               uint32_t* planes);
 
+/* -- denoiser network operators ----------------------------------------------------
+ * No counterpart in the reference (its denoiser is the a-trous filter of
+ * postprocess/denoise.comp). Building blocks of the learned U-Net denoiser: BF16 tensor-core
+ * 3x3 convolutions with FP32 accumulation (forward, data gradient through flipped weights,
+ * weight gradient), 2x2 average pooling, 2x upsampling, the 1x1 RGB head with its relMSE
+ * loss, Adam and input packing. All pointers are device memory; `stream` is a cudaStream_t
+ * (NULL: the default stream). Tensors are NHWC BF16 views: element (pixel q, channel c) at
+ * data[q * stride + offset + c]; channels, stride and offset are multiples of 16, 8 and 8.
+ * Convolution weights are BF16 [cout][3][3][cin]; the returned status reports a launch
+ * error only (kernels run asynchronously). */
+typedef struct yg_nn_tensor
+{
+    void* data;
+    uint32_t stride;
+    uint32_t offset;
+    uint32_t channels;
+    uint32_t reserved;
+} yg_nn_tensor;
+
+/* y = relu?(conv3x3(x, w) + bias), times (mask > 0) where mask is given, added to y when
+ * accumulate; y->channels must be a multiple of 32. Zero padding, stride 1. */
+YG_API int yg_nn_conv3x3(const yg_nn_tensor* x, const void* weights, const float* bias, const yg_nn_tensor* y,
+                         const yg_nn_tensor* mask, int relu, int accumulate, int n, int h, int w, void* stream);
+/* out[i] = sum over r of in[r * n + i], rows summed in order (deterministic). */
+YG_API int yg_nn_sum_rows(const float* in, int rows, long n, float* out, void* stream);
+/* wt[ci][8 - tap][co] = w[co][tap][ci]: yg_nn_conv3x3(dy, wt) is then the data gradient. */
+YG_API int yg_nn_flip_weights(const void* w, int cout, int cin, void* wt, void* stream);
+/* FP32 bytes of the split-K workspace yg_nn_conv3x3_wgrad needs. */
+YG_API size_t yg_nn_wgrad_workspace(int cin, int cout, int n, int h, int w);
+/* dw[co][tap][ci] = sum over pixels of dy[q][co] * x[q + tap][ci] (FP32), db[co] = sum dy. */
+YG_API int yg_nn_conv3x3_wgrad(const yg_nn_tensor* x, const yg_nn_tensor* dy, float* dw, float* db, void* workspace,
+                               int n, int h, int w, void* stream);
+YG_API int yg_nn_avgpool(const yg_nn_tensor* in, const yg_nn_tensor* out, int n, int h, int w, void* stream);
+/* din = dout / 4 over each 2x2 window (+ add), times (mask > 0); h, w are the input's size. */
+YG_API int yg_nn_avgpool_bwd(const yg_nn_tensor* dout, const yg_nn_tensor* add, const yg_nn_tensor* mask,
+                             const yg_nn_tensor* din, int n, int h, int w, void* stream);
+/* nearest 2x upsampling of an h x w input. */
+YG_API int yg_nn_upsample(const yg_nn_tensor* in, const yg_nn_tensor* out, int n, int h, int w, void* stream);
+YG_API int yg_nn_upsample_bwd(const yg_nn_tensor* dout, const yg_nn_tensor* mask, const yg_nn_tensor* din, int n, int h,
+                              int w, void* stream);
+/* out = expm1(w x + b) per pixel (w: 3 x 32 FP32); with target: per-block sums of
+ * (out - t)^2 / (t^2 + eps) in loss_partial[blocks]; with din: the loss gradient wrt x (mean
+ * over pixels and channels, through the features' ReLU) and per-block partial gradients of w
+ * and b in gw_partial[blocks][99]. */
+YG_API int yg_nn_head(const yg_nn_tensor* in, const float* w, const float* b, long pixels, float* out, const float* target,
+                      float eps, float* loss_partial, const yg_nn_tensor* din, float* gw_partial, int blocks, void* stream);
+/* One Adam step on FP32 parameters (step counts from 1); writes the BF16 copy when given. */
+YG_API int yg_nn_adam(float* params, const float* grads, float* m, float* v, void* params_bf16, long n, float lr, float beta1,
+                      float beta2, float eps, int step, void* stream);
+/* 16-channel network input: log1p(linear sRGB of the mean XYZ), albedo, normal, depth / depth_scale, zeros. */
+YG_API int yg_nn_pack_input(const float* xyz, const float* albedo, const float* normal, const float* depth, float depth_scale,
+                            long pixels, const yg_nn_tensor* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -126,6 +126,11 @@ class SchedItem(C.Structure):
 REQ_STATES = {0: "queued", 1: "active", 2: "done", 3: "failed", 4: "cancelled"}
 
 
+class NNTensor(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("stride", C.c_uint32), ("offset", C.c_uint32), ("channels", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
 _lib = None
 
 # (name, restype, argtypes) for every function include/yapt_gpu.h declares
@@ -163,6 +168,26 @@ SIGNATURES = [
     ("yg_server_release", C.c_int, [C.c_void_p, C.c_uint64]),
     ("yg_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
     ("yg_server_destroy", C.c_int, [C.c_void_p]),
+    ("yg_nn_conv3x3", C.c_int, [C.POINTER(NNTensor), C.c_void_p, C.POINTER(C.c_float), C.POINTER(NNTensor),
+                                C.POINTER(NNTensor), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("yg_nn_sum_rows", C.c_int, [C.POINTER(C.c_float), C.c_int, C.c_long, C.POINTER(C.c_float), C.c_void_p]),
+    ("yg_nn_flip_weights", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    ("yg_nn_wgrad_workspace", C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("yg_nn_conv3x3_wgrad", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.POINTER(C.c_float),
+                                      C.POINTER(C.c_float), C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("yg_nn_avgpool", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("yg_nn_avgpool_bwd", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.POINTER(NNTensor), C.POINTER(NNTensor),
+                                    C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("yg_nn_upsample", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("yg_nn_upsample_bwd", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.POINTER(NNTensor), C.c_int, C.c_int,
+                                     C.c_int, C.c_void_p]),
+    ("yg_nn_head", C.c_int, [C.POINTER(NNTensor), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_long,
+                             C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_float),
+                             C.POINTER(NNTensor), C.POINTER(C.c_float), C.c_int, C.c_void_p]),
+    ("yg_nn_adam", C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                             C.c_void_p, C.c_long, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]),
+    ("yg_nn_pack_input", C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float), C.c_float, C.c_long, C.POINTER(NNTensor), C.c_void_p]),
     ("yg_server_plan", C.c_int64, [C.POINTER(SchedItem), C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32,
                                    C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
 ]

@@ -251,3 +251,27 @@ def sky_scene(seed=0, aspect=1.0):
         sc.add_instance(cube, mat, o2w)
     sc.camera = CameraDesc(eye=(0.0, 2.5, 5.0), target=(0.0, 0.5, 0.0), fovy=np.pi * 0.3, aspect=aspect)
     return sc
+
+
+SERVE_TRIANGLES = (10_000, 21_000, 45_000, 96_000, 205_000, 437_000, 935_000, 2_000_000)
+
+
+def serve_scene(variant, target_triangles=None):
+    """Serving-configuration scene: the ``box_scene`` layout (seed = variant) filled with diffuse
+    and dielectric icospheres (subdivision 3, 1280 triangles) until it holds about
+    ``target_triangles`` (default SERVE_TRIANGLES[variant]: 10k to 2M over the 8 variants)."""
+    target = SERVE_TRIANGLES[variant] if target_triangles is None else int(target_triangles)
+    sc = box_scene(variant)
+    sc.name = "serve(variant=%d, ~%d triangles)" % (variant, target)
+    rng = np.random.Generator(np.random.PCG64(1000 + variant))
+    base = sc.triangle_count()
+    n = max(0, int(round((target - base) / 1280.0)))
+    ball = sc.add_mesh(*icosphere(3))
+    mats = [sc.add_material(**diffuse(sc.add_spectrum(control_point_spectrum(rng)))) for _ in range(6)]
+    mats.append(sc.add_material(albedo=(1.0, 1.0, 1.0), transparency=1.0, metalness=0.0, specular_amount=1.0,
+                                roughness=0.1, material_mask=2, cauchy=(1.5, 0.0042), dielectric_ior=1.5))
+    r = float(np.clip(0.35 / max(n, 1) ** (1.0 / 3.0), 0.004, 0.06))
+    for _ in range(n):
+        c = (rng.uniform(0.05, 0.95), rng.uniform(0.02, 0.8), rng.uniform(0.05, 0.95))
+        sc.add_instance(ball, mats[int(rng.integers(len(mats)))], affine(translation=c, scale=(r, r, r)))
+    return sc

@@ -1,0 +1,723 @@
+// Denoiser network operators: BF16 tensor-core convolutions with FP32 accumulation for the
+// U-Net's forward and backward passes, and the small operators around them.
+//
+// Tensors are NHWC (channels innermost) in BF16, each addressed with a channel stride and a
+// channel offset so that a U-Net skip concatenation is just two writers into one buffer.
+// Channel counts are multiples of 16.
+//
+// conv3x3: implicit GEMM, M = pixels, N = output channels, K = 9 taps x input channels.
+// A 128 x 64 output tile per 256-thread block; K advances in chunks of KC channels of one tap,
+// staged in shared memory by a 3-stage cp.async pipeline (zero-filled outside the image) and
+// fed to mma.sync m16n8k16 (BF16 in, FP32 accumulate) through ldmatrix. The epilogue adds the
+// bias, applies ReLU or a ReLU-derivative mask, optionally accumulates into the destination,
+// and stores BF16. The data gradient is the same kernel on spatially flipped, transposed
+// weights; the weight gradient is a split-K GEMM over pixels with a deterministic reduction.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "../../include/yapt_gpu.h"
+
+namespace ygnn
+{
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ void cpAsync16(void* smem, const void* gmem, bool valid)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    int n = valid ? 16 : 0; // src-size 0 zero-fills the 16 bytes
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cpAsyncWait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+__device__ __forceinline__ void ldmatrixX4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(s));
+}
+__device__ __forceinline__ void ldmatrixX4T(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3, const void* p)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(s));
+}
+__device__ __forceinline__ void mma16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+struct Act
+{
+    bf16* p;          // element (pixel q, channel c) at p[q * stride + off + c]
+    uint32_t stride;  // channels per pixel in the buffer
+    uint32_t off;     // first channel of this tensor
+    uint32_t ch;      // channels of this tensor
+};
+
+// ------------------------------------------------------------------ 3x3 convolution (forward / data gradient)
+constexpr int CM = 128, CN = 64, CSTAGES = 3;
+
+template <int KC>
+__global__ void __launch_bounds__(256) conv3x3Kernel(Act x, const bf16* __restrict__ w, const float* __restrict__ bias,
+                                                     Act y, Act mask, int relu, int accumulate, int nImg, int H, int W)
+{
+    constexpr int RS = KC + 8; // shared row stride (elements): 16-byte aligned, ldmatrix conflict free
+    __shared__ __align__(16) bf16 sA[CSTAGES][CM * RS];
+    __shared__ __align__(16) bf16 sB[CSTAGES][CN * RS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp & 3, wn = warp >> 2;
+    const long P = (long)nImg * H * W;
+    const long m0 = (long)blockIdx.x * CM;
+    const int n0 = blockIdx.y * CN;
+    const int Cin = (int)x.ch, Cout = (int)y.ch;
+    const int chunks = Cin / KC;
+    const int kTiles = 9 * chunks;
+    constexpr int SEGS = KC / 8; // 16-byte segments per row
+
+    auto loadTile = [&](int kt, int stage) {
+        const int tap = kt / chunks, c0 = (kt % chunks) * KC;
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        for (int i = tid; i < CM * SEGS; i += 256)
+        {
+            int r = i / SEGS, sg = i % SEGS;
+            long q = m0 + r;
+            bool ok = q < P;
+            const bf16* src = x.p;
+            if (ok)
+            {
+                int img = (int)(q / ((long)H * W));
+                int rem = (int)(q - (long)img * H * W);
+                int yy = rem / W + dy, xx = rem % W + dx;
+                ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
+                if (ok) src = x.p + ((long)(img * H + yy) * W + xx) * x.stride + x.off + c0 + sg * 8;
+            }
+            cpAsync16(&sA[stage][r * RS + sg * 8], src, ok);
+        }
+        for (int i = tid; i < CN * SEGS; i += 256)
+        {
+            int r = i / SEGS, sg = i % SEGS;
+            int co = n0 + r;
+            bool ok = co < Cout;
+            const bf16* src = ok ? w + ((long)co * 9 + tap) * Cin + c0 + sg * 8 : w;
+            cpAsync16(&sB[stage][r * RS + sg * 8], src, ok);
+        }
+    };
+
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.0f;
+
+#pragma unroll
+    for (int s = 0; s < CSTAGES - 1; ++s)
+    {
+        if (s < kTiles) loadTile(s, s);
+        cpAsyncCommit();
+    }
+    for (int kt = 0; kt < kTiles; ++kt)
+    {
+        cpAsyncWait<CSTAGES - 2>();
+        __syncthreads();
+        const int nk = kt + CSTAGES - 1;
+        if (nk < kTiles) loadTile(nk, nk % CSTAGES);
+        cpAsyncCommit();
+        const bf16* A = sA[kt % CSTAGES];
+        const bf16* B = sB[kt % CSTAGES];
+#pragma unroll
+        for (int kk = 0; kk < KC; kk += 16)
+        {
+            uint32_t a[2][4], b[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+            {
+                int mi = lane >> 3, r = lane & 7;
+                int row = wm * 32 + i * 16 + r + (mi & 1) * 8;
+                int col = kk + (mi >> 1) * 8;
+                ldmatrixX4(a[i][0], a[i][1], a[i][2], a[i][3], A + row * RS + col);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j += 2)
+            {
+                int mi = lane >> 3, r = lane & 7;
+                int row = wn * 32 + j * 8 + r + (mi >> 1) * 8;
+                int col = kk + (mi & 1) * 8;
+                ldmatrixX4(b[j][0], b[j][1], b[j + 1][0], b[j + 1][1], B + row * RS + col);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma16816(acc[i][j], a[i][0], a[i][1], a[i][2], a[i][3], b[j][0], b[j][1]);
+        }
+    }
+    cpAsyncWait<0>();
+    // epilogue
+    const int g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+            long q = m0 + wm * 32 + i * 16 + g + h * 8;
+            if (q >= P) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+            {
+                int co = n0 + wn * 32 + j * 8 + t4 * 2;
+                if (co >= Cout) continue;
+                float v0 = acc[i][j][h * 2], v1 = acc[i][j][h * 2 + 1];
+                if (bias)
+                {
+                    v0 += bias[co];
+                    v1 += bias[co + 1];
+                }
+                if (relu)
+                {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                }
+                if (mask.p)
+                {
+                    __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask.p + q * mask.stride + mask.off + co);
+                    if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
+                    if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
+                }
+                __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(y.p + q * y.stride + y.off + co);
+                if (accumulate)
+                {
+                    __nv_bfloat162 old = *dst;
+                    v0 += __bfloat162float(old.x);
+                    v1 += __bfloat162float(old.y);
+                }
+                *dst = __floats2bfloat162_rn(v0, v1);
+            }
+        }
+}
+
+// ------------------------------------------------------------------ 3x3 weight gradient
+// dW[co][tap][ci] = sum_q dY[q][co] * X[q shifted by tap][ci]: M = Cout (64 per block),
+// N = Cin (64 per block) for one tap, K = pixels, split over blocks (gridDim.z).
+constexpr int WM = 64, WN = 64, WK = 32;
+
+__global__ void __launch_bounds__(256) conv3x3WgradKernel(Act x, Act dy, float* __restrict__ partial, int nImg, int H,
+                                                          int W, long pixelsPerSplit)
+{
+    constexpr int RS = 64 + 8; // rows are pixels (k), 64 channels each, padded
+    __shared__ __align__(16) bf16 sY[2][WK * RS]; // [k][m]
+    __shared__ __align__(16) bf16 sX[2][WK * RS]; // [k][n]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp & 1, wn = warp >> 1; // 2 x 4 warps: 32 (m) x 16 (n) each
+    const int Cin = (int)x.ch, Cout = (int)dy.ch;
+    const int nBlocksN = (Cin + WN - 1) / WN;
+    const int tap = blockIdx.y / nBlocksN;
+    const int c0 = (blockIdx.y % nBlocksN) * WN;
+    const int o0 = blockIdx.x * WM;
+    const int ddy = tap / 3 - 1, ddx = tap % 3 - 1;
+    const long P = (long)nImg * H * W;
+    const long q0 = (long)blockIdx.z * pixelsPerSplit;
+    const long q1 = min(P, q0 + pixelsPerSplit);
+
+    auto load = [&](long qb, int stage) {
+        // 32 pixels x 64 channels for each operand: 256 segments of 16 bytes each
+        for (int i = tid; i < WK * 8; i += 256)
+        {
+            int r = i >> 3, sg = i & 7;
+            long q = qb + r;
+            bool okq = q < q1;
+            int co = o0 + sg * 8;
+            bool okY = okq && co < Cout;
+            const bf16* srcY = okY ? dy.p + q * dy.stride + dy.off + co : dy.p;
+            cpAsync16(&sY[stage][r * RS + sg * 8], srcY, okY);
+            int ci = c0 + sg * 8;
+            bool okX = okq && ci < Cin;
+            const bf16* srcX = x.p;
+            if (okX)
+            {
+                int img = (int)(q / ((long)H * W));
+                int rem = (int)(q - (long)img * H * W);
+                int yy = rem / W + ddy, xx = rem % W + ddx;
+                okX = yy >= 0 && yy < H && xx >= 0 && xx < W;
+                if (okX) srcX = x.p + ((long)(img * H + yy) * W + xx) * x.stride + x.off + ci;
+            }
+            cpAsync16(&sX[stage][r * RS + sg * 8], srcX, okX);
+        }
+    };
+    float acc[2][2][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.0f;
+    const long nk = (q1 - q0 + WK - 1) / WK;
+    if (nk > 0) load(q0, 0);
+    cpAsyncCommit();
+    for (long kt = 0; kt < nk; ++kt)
+    {
+        if (kt + 1 < nk) load(q0 + (kt + 1) * WK, (kt + 1) & 1);
+        cpAsyncCommit();
+        cpAsyncWait<1>();
+        __syncthreads();
+        const bf16* Ys = sY[kt & 1];
+        const bf16* Xs = sX[kt & 1];
+#pragma unroll
+        for (int kk = 0; kk < WK; kk += 16)
+        {
+            uint32_t a[2][4], b[2][2];
+            // A = dY^T (m = channel, k = pixel) from [k][m] storage: transposed loads
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+            {
+                int mi = lane >> 3, r = lane & 7;
+                // matrices: (m0-7,k0-7) (m8-15,k0-7) (m0-7,k8-15) (m8-15,k8-15)
+                int krow = kk + r + (mi >> 1) * 8;
+                int mcol = wm * 32 + i * 16 + (mi & 1) * 8;
+                ldmatrixX4T(a[i][0], a[i][1], a[i][2], a[i][3], Ys + krow * RS + mcol);
+            }
+            // B = X (k = pixel, n = channel) from [k][n] storage: transposed loads give the col layout
+            {
+                int mi = lane >> 3, r = lane & 7;
+                // matrices: (k0-7,n0-7) (k8-15,n0-7) (k0-7,n8-15) (k8-15,n8-15)
+                int krow = kk + r + (mi & 1) * 8;
+                int ncol = wn * 16 + (mi >> 1) * 8;
+                ldmatrixX4T(b[0][0], b[0][1], b[1][0], b[1][1], Xs + krow * RS + ncol);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) mma16816(acc[i][j], a[i][0], a[i][1], a[i][2], a[i][3], b[j][0], b[j][1]);
+        }
+        __syncthreads();
+    }
+    cpAsyncWait<0>();
+    const int g = lane >> 2, t4 = lane & 3;
+    float* out = partial + (long)blockIdx.z * Cout * 9 * Cin;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+            int co = o0 + wm * 32 + i * 16 + g + h * 8;
+            if (co >= Cout) continue;
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+            {
+                int ci = c0 + wn * 16 + j * 8 + t4 * 2;
+                if (ci >= Cin) continue;
+                float* o = out + ((long)co * 9 + tap) * Cin + ci;
+                o[0] = acc[i][j][h * 2];
+                o[1] = acc[i][j][h * 2 + 1];
+            }
+        }
+}
+
+// sums the split-K partials in split order (deterministic) into dW
+__global__ void reduceSplits(const float* __restrict__ partial, int splits, long n, float* __restrict__ out)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    {
+        float s = 0.0f;
+        for (int k = 0; k < splits; ++k) s += partial[(long)k * n + i];
+        out[i] = s;
+    }
+}
+
+// bias gradient: per channel sum over pixels, one block per channel group, fixed order
+__global__ void biasGrad(Act dy, long P, float* __restrict__ db)
+{
+    const int c = blockIdx.x;
+    float s = 0.0f;
+    for (long q = threadIdx.x; q < P; q += blockDim.x) s += __bfloat162float(dy.p[q * dy.stride + dy.off + c]);
+    __shared__ float red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1)
+    {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[c] = red[0];
+}
+
+// Wt[ci][8 - tap][co] = W[co][tap][ci]: the data gradient as a forward convolution
+__global__ void flipWeights(const bf16* __restrict__ w, int Cout, int Cin, bf16* __restrict__ wt)
+{
+    long n = (long)Cout * 9 * Cin;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    {
+        int ci = (int)(i % Cin);
+        int tap = (int)((i / Cin) % 9);
+        int co = (int)(i / ((long)Cin * 9));
+        wt[((long)ci * 9 + (8 - tap)) * Cout + co] = w[i];
+    }
+}
+
+// ------------------------------------------------------------------ pooling / upsampling
+// 2x2 average pooling: out (H/2 x W/2) from in
+__global__ void avgPool(Act in, Act out, int nImg, int H, int W)
+{
+    const int Ho = H / 2, Wo = W / 2, C = (int)in.ch;
+    long n = (long)nImg * Ho * Wo * C;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    {
+        int c = (int)(i % C);
+        long q = i / C;
+        int xo = (int)(q % Wo), yo = (int)((q / Wo) % Ho), img = (int)(q / ((long)Wo * Ho));
+        float s = 0.0f;
+        for (int k = 0; k < 4; ++k)
+        {
+            long qi = ((long)(img * H + 2 * yo + (k >> 1)) * W + 2 * xo + (k & 1));
+            s += __bfloat162float(in.p[qi * in.stride + in.off + c]);
+        }
+        out.p[q * out.stride + out.off + c] = __float2bfloat16_rn(s * 0.25f);
+    }
+}
+// dIn = dOut/4 spread over the 2x2 window (+ add, when add.p), times the ReLU mask of the pooled tensor
+__global__ void avgPoolBwd(Act dOut, Act add, Act mask, Act dIn, int nImg, int H, int W)
+{
+    const int Wo = W / 2, Ho = H / 2, C = (int)dIn.ch;
+    long n = (long)nImg * H * W * C;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    {
+        int c = (int)(i % C);
+        long q = i / C;
+        int x = (int)(q % W), y = (int)((q / W) % H), img = (int)(q / ((long)W * H));
+        long qo = ((long)(img * Ho + y / 2) * Wo + x / 2);
+        float v = 0.25f * __bfloat162float(dOut.p[qo * dOut.stride + dOut.off + c]);
+        if (add.p) v += __bfloat162float(add.p[q * add.stride + add.off + c]);
+        if (mask.p && !(__bfloat162float(mask.p[q * mask.stride + mask.off + c]) > 0.0f)) v = 0.0f;
+        dIn.p[q * dIn.stride + dIn.off + c] = __float2bfloat16_rn(v);
+    }
+}
+// nearest 2x upsampling: out (2H x 2W) from in (H x W)
+__global__ void upsample(Act in, Act out, int nImg, int H, int W)
+{
+    const int Ho = 2 * H, Wo = 2 * W, C = (int)in.ch;
+    long n = (long)nImg * Ho * Wo * C;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    {
+        int c = (int)(i % C);
+        long q = i / C;
+        int x = (int)(q % Wo), y = (int)((q / Wo) % Ho), img = (int)(q / ((long)Wo * Ho));
+        long qi = ((long)(img * H + y / 2) * W + x / 2);
+        out.p[q * out.stride + out.off + c] = in.p[qi * in.stride + in.off + c];
+    }
+}
+// dIn (H x W) = sum of the 2x2 block of dOut (2H x 2W), times the ReLU mask of the upsampled tensor
+__global__ void upsampleBwd(Act dOut, Act mask, Act dIn, int nImg, int H, int W)
+{
+    const int Wo = 2 * W, C = (int)dIn.ch;
+    long n = (long)nImg * H * W * C;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    {
+        int c = (int)(i % C);
+        long q = i / C;
+        int x = (int)(q % W), y = (int)((q / W) % H), img = (int)(q / ((long)W * H));
+        float s = 0.0f;
+        for (int k = 0; k < 4; ++k)
+        {
+            long qo = ((long)(img * 2 * H + 2 * y + (k >> 1)) * Wo + 2 * x + (k & 1));
+            s += __bfloat162float(dOut.p[qo * dOut.stride + dOut.off + c]);
+        }
+        if (mask.p && !(__bfloat162float(mask.p[q * mask.stride + mask.off + c]) > 0.0f)) s = 0.0f;
+        dIn.p[q * dIn.stride + dIn.off + c] = __float2bfloat16_rn(s);
+    }
+}
+
+// ------------------------------------------------------------------ head, loss and its gradient
+// out = expm1(W x + b) (linear RGB, 1x1 convolution from C features in FP32 arithmetic);
+// loss = mean over pixels and 3 channels of (out - t)^2 / (t^2 + eps). With dIn set, writes
+// the gradient of the loss wrt x (BF16) and per-block partial gradients of W and b.
+constexpr int HEAD_C = 32;
+__global__ void __launch_bounds__(256) headKernel(Act in, const float* __restrict__ w, const float* __restrict__ b, long P,
+                                                  float* __restrict__ out, const float* __restrict__ target, float eps,
+                                                  float* __restrict__ lossPartial, Act dIn, float* __restrict__ gwPartial)
+{
+    __shared__ float sw[3 * HEAD_C + 3];
+    __shared__ float red[256];
+    for (int i = threadIdx.x; i < 3 * HEAD_C + 3; i += blockDim.x) sw[i] = i < 3 * HEAD_C ? w[i] : b[i - 3 * HEAD_C];
+    __syncthreads();
+    float lsum = 0.0f;
+    float gw[3 * HEAD_C + 3];
+    if (dIn.p)
+        for (int i = 0; i < 3 * HEAD_C + 3; ++i) gw[i] = 0.0f;
+    const long per = (P + gridDim.x - 1) / gridDim.x;
+    const long qb = (long)blockIdx.x * per, qe = min(P, qb + per);
+    for (long q = qb + threadIdx.x; q < qe; q += blockDim.x)
+    {
+        float xv[HEAD_C];
+        for (int c = 0; c < HEAD_C; ++c) xv[c] = __bfloat162float(in.p[q * in.stride + in.off + c]);
+        float dz[3];
+        for (int o = 0; o < 3; ++o)
+        {
+            float z = sw[3 * HEAD_C + o];
+            for (int c = 0; c < HEAD_C; ++c) z += sw[o * HEAD_C + c] * xv[c];
+            float e = expf(fminf(z, 20.0f));
+            float y = e - 1.0f;
+            if (out) out[q * 3 + o] = y;
+            dz[o] = 0.0f;
+            if (target)
+            {
+                float t = target[q * 3 + o];
+                float den = t * t + eps;
+                float d = y - t;
+                lsum += d * d / den;
+                dz[o] = (2.0f * d / den) * e * (z < 20.0f ? 1.0f : 0.0f) / (float)(P * 3);
+            }
+        }
+        if (dIn.p)
+        {
+            for (int c = 0; c < HEAD_C; ++c)
+            {
+                float g = dz[0] * sw[c] + dz[1] * sw[HEAD_C + c] + dz[2] * sw[2 * HEAD_C + c];
+                if (!(xv[c] > 0.0f)) g = 0.0f; // ReLU of the features
+                dIn.p[q * dIn.stride + dIn.off + c] = __float2bfloat16_rn(g);
+            }
+            for (int o = 0; o < 3; ++o)
+            {
+                for (int c = 0; c < HEAD_C; ++c) gw[o * HEAD_C + c] += dz[o] * xv[c];
+                gw[3 * HEAD_C + o] += dz[o];
+            }
+        }
+    }
+    red[threadIdx.x] = lsum;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1)
+    {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && lossPartial) lossPartial[blockIdx.x] = red[0];
+    if (dIn.p)
+    {
+        // fixed-order block reduction of the weight gradients
+        for (int i = 0; i < 3 * HEAD_C + 3; ++i)
+        {
+            __syncthreads();
+            red[threadIdx.x] = gw[i];
+            __syncthreads();
+            for (int o = blockDim.x / 2; o > 0; o >>= 1)
+            {
+                if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) gwPartial[(long)blockIdx.x * (3 * HEAD_C + 3) + i] = red[0];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ optimiser and input packing
+// Adam (Kingma and Ba, 2015) on FP32 master weights; writes the BF16 copy the convolutions read
+__global__ void adamKernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                           bf16* __restrict__ pb, long n, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    {
+        float gi = g[i];
+        float mi = b1 * m[i] + (1.0f - b1) * gi;
+        float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        p[i] = pi;
+        if (pb) pb[i] = __float2bfloat16_rn(pi);
+    }
+}
+
+// network input (16 channels, BF16) from the film mean XYZ and the feature means:
+// log1p(linear sRGB radiance) 3, albedo 3, normal 3, depth / depthScale 1, zeros 6
+__global__ void packInput(const float* __restrict__ xyz, const float* __restrict__ albedo, const float* __restrict__ normal,
+                          const float* __restrict__ depth, float depthScale, long P, Act out)
+{
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < P; q += (long)gridDim.x * blockDim.x)
+    {
+        float X = xyz[3 * q], Y = xyz[3 * q + 1], Z = xyz[3 * q + 2];
+        // c_srgbXYZToRGB (colorSpaces.hlsl:18-23)
+        float r = 3.2406f * X - 1.5372f * Y - 0.4986f * Z;
+        float gg = -0.9689f * X + 1.8758f * Y + 0.0415f * Z;
+        float bb = 0.0557f * X - 0.2040f * Y + 1.0570f * Z;
+        float v[16] = {log1pf(fmaxf(r, 0.0f)), log1pf(fmaxf(gg, 0.0f)), log1pf(fmaxf(bb, 0.0f)),
+                       albedo[3 * q], albedo[3 * q + 1], albedo[3 * q + 2],
+                       normal[3 * q], normal[3 * q + 1], normal[3 * q + 2],
+                       depth[q] / depthScale, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int c = 0; c < 16; ++c) out.p[q * out.stride + out.off + c] = __float2bfloat16_rn(v[c]);
+    }
+}
+
+int gridFor(long n, int threads = 256)
+{
+    long b = (n + threads - 1) / threads;
+    return (int)std::max<long>(1, std::min<long>(b, 152L * 16));
+}
+} // namespace ygnn
+
+using namespace ygnn;
+
+namespace
+{
+Act act(const yg_nn_tensor* t)
+{
+    Act a;
+    a.p = t ? reinterpret_cast<bf16*>(t->data) : nullptr;
+    a.stride = t ? t->stride : 0;
+    a.off = t ? t->offset : 0;
+    a.ch = t ? t->channels : 0;
+    return a;
+}
+bool okTensor(const yg_nn_tensor* t)
+{
+    return t && t->data && t->channels % 16 == 0 && t->stride % 8 == 0 && t->offset % 8 == 0 &&
+           t->offset + t->channels <= t->stride && ((uintptr_t)t->data & 15u) == 0;
+}
+int status(cudaStream_t s)
+{
+    (void)s;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? YG_OK : YG_ERR_CUDA;
+}
+} // namespace
+
+extern "C" {
+
+YG_API int yg_nn_conv3x3(const yg_nn_tensor* x, const void* weights, const float* bias, const yg_nn_tensor* y,
+                         const yg_nn_tensor* mask, int relu, int accumulate, int n, int h, int w, void* stream)
+{
+    if (!okTensor(x) || !okTensor(y) || !weights || n <= 0 || h <= 0 || w <= 0) return YG_ERR_INVALID_ARGUMENT;
+    if (mask && mask->data && (mask->channels != y->channels || !okTensor(mask))) return YG_ERR_INVALID_ARGUMENT;
+    if (y->channels % 32 != 0 || ((uintptr_t)weights & 15u)) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    long P = (long)n * h * w;
+    dim3 grid((unsigned)((P + CM - 1) / CM), (unsigned)((y->channels + CN - 1) / CN));
+    Act m = act(mask && mask->data ? mask : nullptr);
+    if (x->channels % 32 == 0)
+        conv3x3Kernel<32><<<grid, 256, 0, st>>>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w);
+    else
+        conv3x3Kernel<16><<<grid, 256, 0, st>>>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w);
+    return status(st);
+}
+
+YG_API size_t yg_nn_wgrad_workspace(int cin, int cout, int n, int h, int w)
+{
+    long P = (long)n * h * w;
+    int splits = (int)std::min<long>(64, std::max<long>(1, P / 4096));
+    return (size_t)splits * cout * 9 * cin * sizeof(float);
+}
+
+YG_API int yg_nn_conv3x3_wgrad(const yg_nn_tensor* x, const yg_nn_tensor* dy, float* dw, float* db, void* workspace,
+                               int n, int h, int w, void* stream)
+{
+    if (!okTensor(x) || !okTensor(dy) || !dw || !workspace || dy->channels % 32 != 0) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    long P = (long)n * h * w;
+    int splits = (int)std::min<long>(64, std::max<long>(1, P / 4096));
+    long per = (P + splits - 1) / splits;
+    per = (per + WK - 1) / WK * WK;
+    splits = (int)((P + per - 1) / per);
+    const int cin = (int)x->channels, cout = (int)dy->channels;
+    dim3 grid((unsigned)((cout + WM - 1) / WM), (unsigned)(9 * ((cin + WN - 1) / WN)), (unsigned)splits);
+    float* part = static_cast<float*>(workspace);
+    conv3x3WgradKernel<<<grid, 256, 0, st>>>(act(x), act(dy), part, n, h, w, per);
+    long nw = (long)cout * 9 * cin;
+    reduceSplits<<<gridFor(nw), 256, 0, st>>>(part, splits, nw, dw);
+    if (db) biasGrad<<<cout, 256, 0, st>>>(act(dy), P, db);
+    return status(st);
+}
+
+YG_API int yg_nn_sum_rows(const float* in, int rows, long n, float* out, void* stream)
+{
+    if (!in || !out || rows <= 0 || n <= 0) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    reduceSplits<<<gridFor(n), 256, 0, st>>>(in, rows, n, out);
+    return status(st);
+}
+
+YG_API int yg_nn_flip_weights(const void* w, int cout, int cin, void* wt, void* stream)
+{
+    if (!w || !wt) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    flipWeights<<<gridFor((long)cout * 9 * cin), 256, 0, st>>>((const bf16*)w, cout, cin, (bf16*)wt);
+    return status(st);
+}
+
+YG_API int yg_nn_avgpool(const yg_nn_tensor* in, const yg_nn_tensor* out, int n, int h, int w, void* stream)
+{
+    if (!okTensor(in) || !okTensor(out) || in->channels != out->channels || (h | w) & 1) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    avgPool<<<gridFor((long)n * (h / 2) * (w / 2) * in->channels), 256, 0, st>>>(act(in), act(out), n, h, w);
+    return status(st);
+}
+
+YG_API int yg_nn_avgpool_bwd(const yg_nn_tensor* dout, const yg_nn_tensor* add, const yg_nn_tensor* mask,
+                             const yg_nn_tensor* din, int n, int h, int w, void* stream)
+{
+    if (!okTensor(dout) || !okTensor(din) || (h | w) & 1) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    avgPoolBwd<<<gridFor((long)n * h * w * din->channels), 256, 0, st>>>(act(dout), act(add && add->data ? add : nullptr),
+                                                                          act(mask && mask->data ? mask : nullptr), act(din),
+                                                                          n, h, w);
+    return status(st);
+}
+
+YG_API int yg_nn_upsample(const yg_nn_tensor* in, const yg_nn_tensor* out, int n, int h, int w, void* stream)
+{
+    if (!okTensor(in) || !okTensor(out) || in->channels != out->channels) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    upsample<<<gridFor((long)n * 4 * h * w * in->channels), 256, 0, st>>>(act(in), act(out), n, h, w);
+    return status(st);
+}
+
+YG_API int yg_nn_upsample_bwd(const yg_nn_tensor* dout, const yg_nn_tensor* mask, const yg_nn_tensor* din, int n, int h,
+                              int w, void* stream)
+{
+    if (!okTensor(dout) || !okTensor(din)) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    upsampleBwd<<<gridFor((long)n * h * w * din->channels), 256, 0, st>>>(act(dout), act(mask && mask->data ? mask : nullptr),
+                                                                         act(din), n, h, w);
+    return status(st);
+}
+
+YG_API int yg_nn_head(const yg_nn_tensor* in, const float* w, const float* b, long pixels, float* out, const float* target,
+                      float eps, float* loss_partial, const yg_nn_tensor* din, float* gw_partial, int blocks, void* stream)
+{
+    if (!okTensor(in) || in->channels != HEAD_C || !w || !b || blocks <= 0) return YG_ERR_INVALID_ARGUMENT;
+    if (din && din->data && (!gw_partial || !target)) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    headKernel<<<blocks, 256, 0, st>>>(act(in), w, b, pixels, out, target, eps, loss_partial,
+                                       act(din && din->data ? din : nullptr), gw_partial);
+    return status(st);
+}
+
+YG_API int yg_nn_adam(float* params, const float* grads, float* m, float* v, void* params_bf16, long n, float lr, float beta1,
+                      float beta2, float eps, int step, void* stream)
+{
+    if (!params || !grads || !m || !v || n <= 0 || step <= 0) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+    adamKernel<<<gridFor(n), 256, 0, st>>>(params, grads, m, v, (bf16*)params_bf16, n, lr, beta1, beta2, eps, c1, c2);
+    return status(st);
+}
+
+YG_API int yg_nn_pack_input(const float* xyz, const float* albedo, const float* normal, const float* depth, float depth_scale,
+                            long pixels, const yg_nn_tensor* out, void* stream)
+{
+    if (!xyz || !albedo || !normal || !depth || !okTensor(out) || out->channels != 16) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    packInput<<<gridFor(pixels), 256, 0, st>>>(xyz, albedo, normal, depth, depth_scale, pixels, act(out));
+    return status(st);
+}
+
+} // extern "C"

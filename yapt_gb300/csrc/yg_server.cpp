@@ -640,8 +640,12 @@ YG_API int yg_server_create(yg_context* const* scenes, uint32_t n, const yg_serv
     }
     YG_CUDA(cudaSetDevice(s->device));
     cudaDeviceGetAttribute(&s->smCount, cudaDevAttrMultiProcessorCount, s->device);
-    YG_CUDA(cudaStreamCreateWithFlags(&s->sA, cudaStreamNonBlocking));
-    YG_CUDA(cudaStreamCreateWithFlags(&s->sB, cudaStreamNonBlocking));
+    // merged rounds are short and carry most requests: their stream gets the higher priority,
+    // so their blocks are scheduled ahead of the long BDPT kernels on the other stream
+    int prLeast = 0, prGreatest = 0;
+    YG_CUDA(cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest));
+    YG_CUDA(cudaStreamCreateWithPriority(&s->sA, cudaStreamNonBlocking, prGreatest));
+    YG_CUDA(cudaStreamCreateWithPriority(&s->sB, cudaStreamNonBlocking, prLeast));
     YG_CUDA(cudaEventCreateWithFlags(&s->evA, cudaEventDisableTiming));
     YG_CUDA(cudaEventCreateWithFlags(&s->evB, cudaEventDisableTiming));
     TableLayout T = tableLayout(o.max_active);
