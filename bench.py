@@ -40,6 +40,19 @@ SERVE_WORKLOAD = dict(workload="serve_poisson_8_box_variants_10k_to_2M_triangles
                       spp=[1, 4, 16, 64], integrators=["uni", "nee", "bdpt"], rates_per_s=[50, 100, 200, 400, 800],
                       requests=24, max_depth=8, light_vertices=8, lambda_nm=[380, 780], seed=0)
 SERVE_METRIC = "serve: Msamples/s at full load with p50/p99 latency (Poisson arrivals, mixed sizes/spp/integrators)"
+# --workload denoise: the learned denoiser. Training pairs are rendered by the tracer from seeded
+# box scenes (256x256, 4 spp + first-hit features -> a high-spp target), the U-Net is trained
+# on the GPU with Adam (lr 1e-3), and a held-out 1920x1080 box scene compares the wall time to
+# reach relMSE 1e-3: plain accumulation vs few-spp renders + the network, with a per-tile
+# fallback to plain accumulation where the two-half error estimate exceeds a threshold.
+DENOISE_WORKLOAD = dict(workload="denoise_unet_box_scenes_1080p", train_scenes=48, train_width=384, train_height=216,
+                        train_input_spp=[4, 16], train_target_spp=2048, train_steps=4000, batch=8, crop=128, lr=1e-3,
+                        eval_width=1920, eval_height=1080, eval_reference_spp=4096, eval_seed=100000, integrator="uni",
+                        max_depth=8, tile=64, target_relmse=1e-3, lambda_nm=[380, 780])
+DENOISE_METRIC = "denoise: wall-time speed-up to relMSE 1e-3 at 1920x1080 (plain accumulation time / denoised time)"
+UNET_FLOP_PER_PIXEL = 2 * 9 * (16 * 32 + 32 * 32 + (32 * 64 + 64 * 64) / 4 + (64 * 128 + 128 * 128) / 16 +
+                               (128 * 256 + 256 * 256) / 64 + (384 * 128 + 128 * 128) / 16 + (192 * 64 + 64 * 64) / 4 +
+                               (96 * 32 + 32 * 32)) + 2 * 3 * 32
 CPU_CROP = (256, 256, 512, 512)  # bounded CPU sample: 512x512 centre crop
 CPU_SPP = 32
 
@@ -380,6 +393,146 @@ def run_serve(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_denoise(args, world, rank, local):
+    import numpy as np
+    import torch
+    from yapt_gb300 import configs
+    from yapt_gb300 import denoise as D
+    from yapt_gb300.runtime import Context
+    if rank != 0:
+        return
+    W = DENOISE_WORKLOAD
+    torch.cuda.set_device(local)
+    lam = tuple(W["lambda_nm"])
+    ctx = Context(local)
+    # -- training data: tracer renders of seeded box scenes
+    t0 = time.time()
+    pairs = []
+    TW, TH = W["train_width"], W["train_height"]
+    for seed in range(W["train_scenes"]):
+        ctx.upload_scene(configs.box_scene(seed, aspect=TW / TH))
+        ref = D.render_reference(ctx, TW, TH, W["train_target_spp"], spp_start=100000, integrator=W["integrator"],
+                                 max_depth=W["max_depth"], lambda_range=lam)
+        for k, spp in enumerate(W["train_input_spp"]):
+            inp = D.render_features(ctx, TW, TH, spp, spp_start=1000 * k, integrator=W["integrator"],
+                                    max_depth=W["max_depth"], lambda_range=lam)
+            pairs.append((inp, ref))
+    data_s = time.time() - t0
+    net = D.UNet(seed=0)
+    dev = [(D.to_device_input(net, *inp, depth_scale=4.0), torch.from_numpy(np.ascontiguousarray(ref, np.float32).reshape(-1)).cuda(),
+            TH, TW) for (inp, ref) in pairs]
+    torch.cuda.synchronize()
+    t1 = time.time()
+    hist = D.train(net, dev, steps=W["train_steps"], batch=W["batch"], crop=W["crop"], lr=W["lr"], seed=1)
+    torch.cuda.synchronize()
+    train_s = time.time() - t1
+    # -- held-out evaluation scene at 1920x1080
+    EW, EH = W["eval_width"], W["eval_height"]
+    ctx.upload_scene(configs.box_scene(W["eval_seed"], aspect=EW / EH))
+    kw = dict(integrator=W["integrator"], max_depth=W["max_depth"], lambda_range=lam)
+    ref = D.render_reference(ctx, EW, EH, W["eval_reference_spp"], spp_start=1 << 20, **kw)
+
+    def plain(spp, start=0):
+        torch.cuda.synchronize()
+        t = time.time()
+        ctx.film_clear(EW, EH)
+        ctx.render(ctx.params(W["integrator"], EW, EH, spp_start=start, spp=spp, max_depth=W["max_depth"], lambda_range=lam))
+        xyz, _ = ctx.film()
+        return xyz @ D.SRGB_FROM_XYZ.T, time.time() - t
+
+    plain_curve = []
+    for spp in (4, 16, 64, 256, 1024):
+        img, dt = plain(spp)
+        plain_curve.append((spp, D.relmse(img, ref), dt))
+    # relMSE of plain accumulation ~ c / spp: fit c on the measured points (reference error included)
+    c_fit = float(np.median([r * s for (s, r, _) in plain_curve]))
+    spp_plain = int(np.ceil(c_fit / W["target_relmse"]))
+    img, t_plain = plain(spp_plain)
+    r_plain = D.relmse(img, ref)
+    tile = W["tile"]
+
+    def denoised(spp):
+        # two independent halves (error estimate) and the whole render, then the per-tile fallback
+        torch.cuda.synchronize()
+        t = time.time()
+        half = max(1, spp // 2)
+        xa = D.render_features(ctx, EW, EH, half, spp_start=0, **kw)
+        xb = D.render_features(ctx, EW, EH, half, spp_start=half, **kw)
+        xyz = (xa[0] + xb[0]) * 0.5
+        alb, nrm, dep = (xa[1] + xb[1]) * 0.5, (xa[2] + xb[2]) * 0.5, (xa[3] + xb[3]) * 0.5
+        tn = time.time()
+        da = D.denoise_image(net, D.to_device_input(net, *xa, depth_scale=4.0), EH, EW)
+        db = D.denoise_image(net, D.to_device_input(net, *xb, depth_scale=4.0), EH, EW)
+        out = D.denoise_image(net, D.to_device_input(net, xyz, alb, nrm, dep, depth_scale=4.0), EH, EW)
+        torch.cuda.synchronize()
+        net_s = time.time() - tn
+        # per-tile error estimate of the whole-render result: (da - db)^2 / 4 relative
+        est = ((da - db) ** 2 / 4.0) / (out * out + D.EPS)
+        ty, tx = (EH + tile - 1) // tile, (EW + tile - 1) // tile
+        bad = []
+        for j in range(ty):
+            for i in range(tx):
+                y0, x0 = j * tile, i * tile
+                if float(est[y0:y0 + tile, x0:x0 + tile].mean()) > W["target_relmse"]:
+                    bad.append((x0, y0, min(tile, EW - x0), min(tile, EH - y0)))
+        if bad:
+            # plain accumulation of the flagged tiles (disjoint crops of one film)
+            ctx.film_clear(EW, EH)
+            for (x0, y0, cw, ch) in bad:
+                ctx.render(ctx.params(W["integrator"], EW, EH, spp_start=1 << 16, spp=spp_plain, crop=(x0, y0, cw, ch),
+                                      max_depth=W["max_depth"], lambda_range=lam))
+            f, _ = ctx.film()
+            f = f @ D.SRGB_FROM_XYZ.T
+            for (x0, y0, cw, ch) in bad:
+                out[y0:y0 + ch, x0:x0 + cw] = f[y0:y0 + ch, x0:x0 + cw]
+        return out, time.time() - t, net_s, len(bad), ty * tx
+
+    den_curve = []
+    best = None
+    for spp in (4, 8, 16, 32, 64, 128):
+        out, dt, net_s, fb, tiles = denoised(spp)
+        r = D.relmse(out, ref)
+        den_curve.append({"spp": spp, "relmse": r, "seconds": dt, "network_seconds": net_s, "fallback_tiles": fb,
+                          "tiles": tiles})
+        if r <= W["target_relmse"] and best is None:
+            best = den_curve[-1]
+    # network throughput at 1080p (3 forward passes measured above; time one more with events)
+    packed = D.to_device_input(net, *D.render_features(ctx, EW, EH, 4, **kw), depth_scale=4.0)
+    for _ in range(3):
+        net.forward(packed, 1, EH, EW)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = 10
+    for _ in range(reps):
+        net.forward(packed, 1, EH, EW)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / reps
+    flops = UNET_FLOP_PER_PIXEL * EW * EH
+    tflops = flops / (fwd_ms / 1e3) / 1e12
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops", 1900.0)
+        peak_kind = "measured"
+    except Exception:
+        peak, peak_kind = 1900.0, "fallback"
+    speedup = (t_plain / best["seconds"]) if best else None
+    line = {"metric": DENOISE_METRIC, "value": speedup, "unit": "x", "n_gpus": 1, "steps": W["train_steps"],
+            "warmup": 3, "ms_per_step": train_s * 1e3 / W["train_steps"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": dict(W, plain_spp_for_target=spp_plain, relmse_constant_c=c_fit),
+            "plain": {"spp": spp_plain, "seconds": t_plain, "relmse": r_plain,
+                      "curve": [{"spp": s_, "relmse": r_, "seconds": d_} for (s_, r_, d_) in plain_curve]},
+            "denoised": {"best": best, "curve": den_curve},
+            "training": {"data_seconds": data_s, "train_seconds": train_s, "first_loss": float(np.mean(hist[:20])),
+                         "last_loss": float(np.mean(hist[-20:]))},
+            "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                         "traffic": None, "peak_source": peak_kind, "kernel": "U-Net forward at 1920x1080 (all layers)",
+                         "flop_per_pixel": UNET_FLOP_PER_PIXEL, "forward_ms": fwd_ms}}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,7 +542,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--size", type=int, default=0, help="image side for a smaller profiling case")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel for a smaller profiling case")
-    ap.add_argument("--workload", default="nee", choices=["nee", "bdpt", "serve"])
+    ap.add_argument("--workload", default="nee", choices=["nee", "bdpt", "serve", "denoise"])
     args = ap.parse_args()
     if args.workload == "bdpt":
         WORKLOAD.clear()
@@ -399,6 +552,13 @@ def main():
     if args.spp:
         WORKLOAD["spp"] = args.spp
     world, rank, local = dist_setup()
+    if args.workload == "denoise":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned denoiser"}), flush=True)
+            return
+        run_denoise(args, world, rank, local)
+        return
     if args.workload == "serve":
         if args.impl == "reference":
             if rank == 0:

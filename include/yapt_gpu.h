@@ -393,12 +393,14 @@ YG_API int yg_nn_avgpool_bwd(const yg_nn_tensor* dout, const yg_nn_tensor* add, 
 YG_API int yg_nn_upsample(const yg_nn_tensor* in, const yg_nn_tensor* out, int n, int h, int w, void* stream);
 YG_API int yg_nn_upsample_bwd(const yg_nn_tensor* dout, const yg_nn_tensor* mask, const yg_nn_tensor* din, int n, int h,
                               int w, void* stream);
-/* out = expm1(w x + b) per pixel (w: 3 x 32 FP32); with target: per-block sums of
+/* out = expm1(w x + b + skip[0..2]) per pixel (w: 3 x 32 FP32; skip, when given: the input's
+ * log1p radiance channels, so the network predicts a log-space correction); with target: per-block sums of
  * (out - t)^2 / (t^2 + eps) in loss_partial[blocks]; with din: the loss gradient wrt x (mean
  * over pixels and channels, through the features' ReLU) and per-block partial gradients of w
  * and b in gw_partial[blocks][99]. */
-YG_API int yg_nn_head(const yg_nn_tensor* in, const float* w, const float* b, long pixels, float* out, const float* target,
-                      float eps, float* loss_partial, const yg_nn_tensor* din, float* gw_partial, int blocks, void* stream);
+YG_API int yg_nn_head(const yg_nn_tensor* in, const yg_nn_tensor* skip, const float* w, const float* b, long pixels, float* out,
+                      const float* target, float eps, float* loss_partial, const yg_nn_tensor* din, float* gw_partial, int blocks,
+                      void* stream);
 /* One Adam step on FP32 parameters (step counts from 1); writes the BF16 copy when given. */
 YG_API int yg_nn_adam(float* params, const float* grads, float* m, float* v, void* params_bf16, long n, float lr, float beta1,
                       float beta2, float eps, int step, void* stream);

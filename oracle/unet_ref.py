@@ -107,7 +107,7 @@ def forward(params, x):
     A["d0a"] = cv("d0a", A["cat0"])
     A["d0b"] = cv("d0b", A["d0a"])
     hw, hb = P["head"]
-    z = np.einsum("nhwc,oc->nhwo", A["d0b"], hw) + hb
+    z = np.einsum("nhwc,oc->nhwo", A["d0b"], hw) + hb + A["x0"][..., :3]
     A["z"] = z
     return np.expm1(np.minimum(z, 20.0)), A
 

@@ -181,7 +181,7 @@ SIGNATURES = [
     ("yg_nn_upsample", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.c_int, C.c_int, C.c_int, C.c_void_p]),
     ("yg_nn_upsample_bwd", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.POINTER(NNTensor), C.c_int, C.c_int,
                                      C.c_int, C.c_void_p]),
-    ("yg_nn_head", C.c_int, [C.POINTER(NNTensor), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_long,
+    ("yg_nn_head", C.c_int, [C.POINTER(NNTensor), C.POINTER(NNTensor), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_long,
                              C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_float),
                              C.POINTER(NNTensor), C.POINTER(C.c_float), C.c_int, C.c_void_p]),
     ("yg_nn_adam", C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),

@@ -439,11 +439,13 @@ __global__ void upsampleBwd(Act dOut, Act mask, Act dIn, int nImg, int H, int W)
 }
 
 // ------------------------------------------------------------------ head, loss and its gradient
-// out = expm1(W x + b) (linear RGB, 1x1 convolution from C features in FP32 arithmetic);
+// out = expm1(W x + b + skip) (linear RGB; 1x1 convolution from C features in FP32 arithmetic,
+// added to the first three channels of `skip`, the log1p radiance of the noisy input, so the
+// network predicts a correction in log space and a clean input passes through);
 // loss = mean over pixels and 3 channels of (out - t)^2 / (t^2 + eps). With dIn set, writes
 // the gradient of the loss wrt x (BF16) and per-block partial gradients of W and b.
 constexpr int HEAD_C = 32;
-__global__ void __launch_bounds__(256) headKernel(Act in, const float* __restrict__ w, const float* __restrict__ b, long P,
+__global__ void __launch_bounds__(256) headKernel(Act in, Act skip, const float* __restrict__ w, const float* __restrict__ b, long P,
                                                   float* __restrict__ out, const float* __restrict__ target, float eps,
                                                   float* __restrict__ lossPartial, Act dIn, float* __restrict__ gwPartial)
 {
@@ -466,6 +468,7 @@ __global__ void __launch_bounds__(256) headKernel(Act in, const float* __restric
         {
             float z = sw[3 * HEAD_C + o];
             for (int c = 0; c < HEAD_C; ++c) z += sw[o * HEAD_C + c] * xv[c];
+            if (skip.p) z += __bfloat162float(skip.p[q * skip.stride + skip.off + o]);
             float e = expf(fminf(z, 20.0f));
             float y = e - 1.0f;
             if (out) out[q * 3 + o] = y;
@@ -690,13 +693,16 @@ YG_API int yg_nn_upsample_bwd(const yg_nn_tensor* dout, const yg_nn_tensor* mask
     return status(st);
 }
 
-YG_API int yg_nn_head(const yg_nn_tensor* in, const float* w, const float* b, long pixels, float* out, const float* target,
-                      float eps, float* loss_partial, const yg_nn_tensor* din, float* gw_partial, int blocks, void* stream)
+YG_API int yg_nn_head(const yg_nn_tensor* in, const yg_nn_tensor* skip, const float* w, const float* b, long pixels, float* out,
+                      const float* target, float eps, float* loss_partial, const yg_nn_tensor* din, float* gw_partial, int blocks,
+                      void* stream)
 {
     if (!okTensor(in) || in->channels != HEAD_C || !w || !b || blocks <= 0) return YG_ERR_INVALID_ARGUMENT;
+    if (skip && skip->data && !okTensor(skip)) return YG_ERR_INVALID_ARGUMENT;
     if (din && din->data && (!gw_partial || !target)) return YG_ERR_INVALID_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
-    headKernel<<<blocks, 256, 0, st>>>(act(in), w, b, pixels, out, target, eps, loss_partial,
+    headKernel<<<blocks, 256, 0, st>>>(act(in), act(skip && skip->data ? skip : nullptr), w, b, pixels, out, target, eps,
+                                       loss_partial,
                                        act(din && din->data ? din : nullptr), gw_partial);
     return status(st);
 }

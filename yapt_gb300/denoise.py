@@ -5,7 +5,8 @@ pooling, nearest upsampling, the 1x1 RGB head with its relMSE loss, and Adam. Py
 allocates the device buffers and provides the stream.
 
 Input (10 channels, padded to 16): log1p of the linear sRGB radiance of a few-spp render,
-albedo, normal, depth. Output: linear sRGB radiance. Loss: relMSE, mean (y - t)^2 / (t^2 + eps).
+albedo, normal, depth. Output: linear sRGB radiance, expm1(input log radiance + the network's
+log-space correction), so a clean input passes through. Loss: relMSE, mean (y - t)^2 / (t^2 + eps).
 
 There is no learned denoiser in the reference (its denoiser is the a-trous filter of
 postprocess/denoise.comp); this module is the learned part of the serving configuration.
@@ -163,7 +164,7 @@ class UNet:
         ho = self.lay["head"]
         hw = C.cast(C.c_void_p(self.p.data_ptr() + 4 * ho[0]), C.POINTER(C.c_float))
         hb = C.cast(C.c_void_p(self.p.data_ptr() + 4 * ho[2]), C.POINTER(C.c_float))
-        _check(lib.yg_nn_head(C.byref(view(B["d0b"], 32, 0, 32)), hw, hb, n * h * w,
+        _check(lib.yg_nn_head(C.byref(view(B["d0b"], 32, 0, 32)), C.byref(view(B["x0"], 16, 0, 16)), hw, hb, n * h * w,
                               C.cast(C.c_void_p(B["out"].data_ptr()), C.POINTER(C.c_float)), None, C.c_float(EPS), None,
                               None, None, self.head_blocks, self.stream()), "head")
         return B["out"]
@@ -212,7 +213,8 @@ class UNet:
         st = self.stream()
         ho = self.lay["head"]
         fp = lambda t, off=0: C.cast(C.c_void_p(t.data_ptr() + 4 * off), C.POINTER(C.c_float))  # noqa: E731
-        _check(lib.yg_nn_head(C.byref(V(B["d0b"], 32, 0, 32)), fp(self.p, ho[0]), fp(self.p, ho[2]), n * h * w, fp(B["out"]),
+        _check(lib.yg_nn_head(C.byref(V(B["d0b"], 32, 0, 32)), C.byref(V(B["x0"], 16, 0, 16)), fp(self.p, ho[0]),
+                              fp(self.p, ho[2]), n * h * w, fp(B["out"]),
                               fp(target), C.c_float(EPS), fp(B["loss_part"]), C.byref(V(B["g_d0b"], 32, 0, 32)),
                               fp(B["gw_part"]), self.head_blocks, st), "head")
         _check(lib.yg_nn_sum_rows(fp(B["gw_part"]), self.head_blocks, HEAD, fp(self.g, ho[0]), st), "head grads")
