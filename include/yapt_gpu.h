@@ -249,7 +249,7 @@ YG_API int yg_film_relmse(yg_context* ctx, const float* reference_xyz, double ep
  * (380..700 nm on a new context). Writes crop_w * crop_h * spp_count float4 (X, Y, Z, 1)
  * to device_sample_xyz (device memory, 16-byte aligned), ordered [spp][row][column];
  * asynchronous on the context stream (ready after yg_synchronize).
- * Scratch: a file-scope device array of about 6 MB that every GPU loading the library holds
+ * Scratch: a file-scope device array of about 7 MB that every GPU loading the library holds
  * until exit; at most 256 sample indices per call (spp_count > 256 is rejected) and waves of
  * 16384 paths. The first call on a device looks up the array's device address; make that
  * first call before any stream capture. All calls share the one array: calls whose work

@@ -899,7 +899,7 @@ namespace
 {
 constexpr uint32_t kNoAllocWaveCapacity = 16384; // paths in flight per wave
 constexpr uint32_t kNoAllocMaxSpp = 256;         // sample indices per call
-constexpr size_t kNoAllocBytesPerSlot = 352;     // >= wavefrontBytesPerSlot(), checked at set-up
+constexpr size_t kNoAllocBytesPerSlot = 416;     // >= wavefrontBytesPerSlot(), checked at set-up
 constexpr size_t kNoAllocSobolBytes = (size_t)kNoAllocMaxSpp * yg::kSobolDims * sizeof(uint32_t);
 constexpr size_t kNoAllocMatrixBytes = (size_t)yg::kSobolDims * 32 * sizeof(uint32_t);
 constexpr size_t kNoAllocArenaBytes = (size_t)kNoAllocWaveCapacity * kNoAllocBytesPerSlot + (64u << 10);

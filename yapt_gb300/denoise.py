@@ -371,3 +371,30 @@ def denoise_image(net, packed, h, w):
     """Runs the network on a whole image (sides multiples of 8); returns host linear sRGB (h, w, 3)."""
     out = net.forward(packed, 1, h, w)
     return out.view(h, w, 3).cpu().numpy()
+
+
+def _profile_forward(width, height, reps):
+    """U-Net forward passes on a synthetic input (for timing and kernel profiles)."""
+    torch = _torch()
+    net = UNet(seed=0)
+    rng = np.random.Generator(np.random.PCG64(0))
+    x = torch.from_numpy(rng.uniform(0, 1, width * height * 16).astype(np.float32)).cuda().to(torch.bfloat16)
+    for _ in range(reps):
+        net.forward(x, 1, height, width)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    net.forward(x, 1, height, width)
+    e1.record()
+    torch.cuda.synchronize()
+    print("forward %dx%d: %.3f ms" % (width, height, e0.elapsed_time(e1)))
+
+
+if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser(description="U-Net forward timing on a synthetic input")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args()
+    _profile_forward(a.width, a.height, a.reps)
