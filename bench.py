@@ -374,6 +374,7 @@ def run_serve(args, world, rank, local):
             srv.release(r)
         per_rate.append({"rate_per_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
                          "p99_latency_s": float(np.percentile(lat, 99)),
+                         "p99_latency_over_isolated_p99": float(np.percentile(lat, 99) / np.percentile(iso, 99)),
                          "p50_slowdown": float(np.percentile(slow, 50)), "p99_slowdown": float(np.percentile(slow, 99)),
                          "makespan_s": makespan, "msamples_per_s": total_samples / makespan / 1e6})
     st = srv.stats()

@@ -98,22 +98,6 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, Hi
     if (COUNT) countTraversal(travCtr, tc);
 }
 
-// Shading coherence: before each shade pass the hit queue is regrouped by the kind of work the
-// hit needs (miss, emitter, opaque dielectric base, conductor, transparent dielectric), so that
-// a warp runs one branch of the layered BSDF instead of all of them. A path's result does not
-// depend on its queue position.
-constexpr int kShadeClasses = 5;
-YG_DEV uint32_t shadeClass(const SceneView& S, float4 ha, uint32_t hb)
-{
-    if (hb == 0xffffffffu) return 0;
-    const GpuMaterial& M = S.materials[S.instances[__float_as_uint(ha.w)].material];
-    float4 e = M.emissive_roughness;
-    if (e.x + e.y + e.z > 0.0f) return 1;
-    if (M.albedo_transparency.w > 0.0f) return 4;
-    if (M.specular_metalness.w > 0.0f) return 3;
-    return 2;
-}
-
 __global__ void __launch_bounds__(256) wfClassify(const SceneView S, RayQueue Q, HitQueue H, uint8_t* keys, uint32_t* counts)
 {
     const uint32_t n = *Q.count;
@@ -132,47 +116,6 @@ __global__ void __launch_bounds__(256) wfClassify(const SceneView S, RayQueue Q,
             if (lane == 0 && m) atomicAdd(&counts[c], (uint32_t)__popc(m));
         }
     }
-}
-
-__global__ void __launch_bounds__(256) wfRegroup(RayQueue Q, HitQueue H, const uint8_t* keys, const uint32_t* counts,
-                                                 uint32_t* cursors, RayQueue Qs, HitQueue Hs)
-{
-    const uint32_t n = *Q.count;
-    uint32_t base[kShadeClasses];
-    uint32_t acc = 0;
-    for (int c = 0; c < kShadeClasses; ++c)
-    {
-        base[c] = acc;
-        acc += counts[c];
-    }
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (n + stride - 1) / stride;
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t r = 0; r < rounds; ++r)
-    {
-        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
-        bool active = i < n;
-        uint32_t key = active ? keys[i] : 0xffu;
-        uint32_t pos = 0;
-        for (uint32_t c = 0; c < (uint32_t)kShadeClasses; ++c)
-        {
-            uint32_t m = __ballot_sync(0xffffffffu, key == c);
-            if (!m) continue;
-            uint32_t leader = (uint32_t)(__ffs(m) - 1);
-            uint32_t b0 = 0;
-            if (lane == leader) b0 = atomicAdd(&cursors[c], (uint32_t)__popc(m));
-            b0 = __shfl_sync(0xffffffffu, b0, leader);
-            if (key == c) pos = base[c] + b0 + __popc(m & ((1u << lane) - 1u));
-        }
-        if (active)
-        {
-            Qs.o[pos] = Q.o[i];
-            Qs.d[pos] = Q.d[i];
-            Hs.a[pos] = H.a[i];
-            Hs.b[pos] = H.b[i];
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *Qs.count = n;
 }
 
 template <bool NEE>
@@ -440,7 +383,7 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
             cudaMemsetAsync(SQ.count, 0, 4, stream);
             cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
             wfClassify<<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
-            wfRegroup<<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
+            wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
             if (P.integrator == 1) wfShade<true><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ);
             else wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ);
             launches += 4;

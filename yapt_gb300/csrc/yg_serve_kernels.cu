@@ -72,7 +72,32 @@ __global__ void __launch_bounds__(128) wfmTrace(MultiTables M, RayQueue Q, HitQu
     countRays(rayCtr, rays);
 }
 
-__global__ void __launch_bounds__(128) wfmShade(MultiTables M, WaveState W, RayQueue Qin, HitQueue H, RayQueue Qout,
+__global__ void __launch_bounds__(256) wfmClassify(MultiTables M, RayQueue Q, HitQueue H, uint8_t* keys, uint32_t* counts)
+{
+    const uint32_t n = *Q.count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
+        bool active = i < n;
+        uint32_t key = 0xffu;
+        if (active)
+        {
+            const SceneView& S = M.views[M.req[__float_as_uint(Q.o[i].w)]];
+            key = shadeClass(S, H.a[i], H.b[i]);
+            keys[i] = (uint8_t)key;
+        }
+        for (uint32_t c = 0; c < (uint32_t)kShadeClasses; ++c)
+        {
+            uint32_t m = __ballot_sync(0xffffffffu, key == c);
+            if (lane == 0 && m) atomicAdd(&counts[c], (uint32_t)__popc(m));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128, 4) wfmShade(MultiTables M, WaveState W, RayQueue Qin, HitQueue H, RayQueue Qout,
                                                 ShadowQueue SQ)
 {
     const uint32_t n = *Qin.count;
@@ -237,6 +262,10 @@ int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, 
     HitQueue H{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
     ShadowQueue SQ{(float4*)take(C * 16), (float4*)take(C * 16), (uint2*)take(C * 8), (float4*)take(C * 16),
                    counters + 2};
+    RayQueue QS{(float4*)take(C * 16), (float4*)take(C * 16), counters + 3};
+    HitQueue HS{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
+    uint8_t* keys = (uint8_t*)take(C);
+    uint32_t* classCounts = counters + 8;
     const int traceBlocks = smCount * 16, shadeBlocks = smCount * 8;
     int gblocks = (int)std::min<uint64_t>((C + 255) / 256, (uint64_t)smCount * 8);
     int launches = 0;
@@ -249,9 +278,12 @@ int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, 
         wfmTrace<<<traceBlocks, 128, 0, stream>>>(M, *cur, H, rayCounter);
         cudaMemsetAsync(nxt->count, 0, 4, stream);
         cudaMemsetAsync(SQ.count, 0, 4, stream);
-        wfmShade<<<shadeBlocks, 128, 0, stream>>>(M, W, *cur, H, *nxt, SQ);
+        cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
+        wfmClassify<<<smCount * 4, 256, 0, stream>>>(M, *cur, H, keys, classCounts);
+        wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
+        wfmShade<<<shadeBlocks, 128, 0, stream>>>(M, W, QS, HS, *nxt, SQ);
         wfmShadow<<<traceBlocks, 128, 0, stream>>>(M, W, SQ, rayCounter);
-        launches += 3;
+        launches += 5;
         RayQueue* t = cur;
         cur = nxt;
         nxt = t;

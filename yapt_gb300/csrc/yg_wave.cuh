@@ -155,4 +155,62 @@ YG_DEV void storePath(const WaveState& W, uint32_t s, const PathState& ps, const
     }
 }
 
+// Shading coherence: before each shade pass the hit queue is regrouped by the kind of work the
+// hit needs (miss, emitter, opaque dielectric base, conductor, transparent dielectric), so that
+// a warp runs one branch of the layered BSDF instead of all of them. A path's result does not
+// depend on its queue position.
+constexpr int kShadeClasses = 5;
+YG_DEV uint32_t shadeClass(const SceneView& S, float4 ha, uint32_t hb)
+{
+    if (hb == 0xffffffffu) return 0;
+    const GpuMaterial& M = S.materials[S.instances[__float_as_uint(ha.w)].material];
+    float4 e = M.emissive_roughness;
+    if (e.x + e.y + e.z > 0.0f) return 1;
+    if (M.albedo_transparency.w > 0.0f) return 4;
+    if (M.specular_metalness.w > 0.0f) return 3;
+    return 2;
+}
+
+template <int CLASSES>
+__global__ void __launch_bounds__(256) wfRegroup(RayQueue Q, HitQueue H, const uint8_t* keys, const uint32_t* counts,
+                                                 uint32_t* cursors, RayQueue Qs, HitQueue Hs)
+{
+    const uint32_t n = *Q.count;
+    uint32_t base[CLASSES];
+    uint32_t acc = 0;
+    for (int c = 0; c < CLASSES; ++c)
+    {
+        base[c] = acc;
+        acc += counts[c];
+    }
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
+        bool active = i < n;
+        uint32_t key = active ? keys[i] : 0xffu;
+        uint32_t pos = 0;
+        for (uint32_t c = 0; c < (uint32_t)CLASSES; ++c)
+        {
+            uint32_t m = __ballot_sync(0xffffffffu, key == c);
+            if (!m) continue;
+            uint32_t leader = (uint32_t)(__ffs(m) - 1);
+            uint32_t b0 = 0;
+            if (lane == leader) b0 = atomicAdd(&cursors[c], (uint32_t)__popc(m));
+            b0 = __shfl_sync(0xffffffffu, b0, leader);
+            if (key == c) pos = base[c] + b0 + __popc(m & ((1u << lane) - 1u));
+        }
+        if (active)
+        {
+            Qs.o[pos] = Q.o[i];
+            Qs.d[pos] = Q.d[i];
+            Hs.a[pos] = H.a[i];
+            Hs.b[pos] = H.b[i];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *Qs.count = n;
+}
+
 } // namespace yg
