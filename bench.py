@@ -204,6 +204,7 @@ def run_reference(args, world, rank):
 def run_ours(args, world, rank, local):
     import numpy as np
     from yapt_gb300 import configs
+    from yapt_gb300 import _native as N
     from yapt_gb300.runtime import Context
     import torch
 
@@ -231,6 +232,8 @@ def run_ours(args, world, rank, local):
     kernel_ms = []
     launches = 0
     rays = 0
+    kinds = {}
+    time_flag = 0 if bdpt else N.YG_FLAG_TIME_KERNELS
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
@@ -238,11 +241,17 @@ def run_ours(args, world, rank, local):
         for s in range(args.steps):
             flush.fill_(float(s))
             torch.cuda.synchronize()
-            ctx.render(params(args.warmup + s))
+            ctx.render(params(args.warmup + s, flags=time_flag))
             st = ctx.last_stats()
             kernel_ms.append(st["ms"])
             launches += st["launches"]
             rays += st["rays"]
+            if time_flag:
+                kp = ctx.kernel_profile()
+                for k in N.KERNEL_KINDS:
+                    acc = kinds.setdefault(k, {"ms": 0.0, "launches": 0})
+                    acc["ms"] += kp[k]["ms"]
+                    acc["launches"] += kp[k]["launches"]
         ctx.synchronize()
         torch.cuda.synchronize()
         wall = time.time() - t0
@@ -265,26 +274,54 @@ def run_ours(args, world, rank, local):
     h2d = 128 + spp * 256 * 4  # request struct + its Sobol points
     d2h = W * H * 16  # film sums
 
-    # algorithmic bytes of the dominant kernel: BVH nodes (64 B) + triangles (48 B) visited,
-    # measured once by the counting variant of the same kernel on one step
-    if bdpt:
-        tc = {"nodes": 0, "triangles": 0}  # the bidirectional kernels have no counting variant
-    else:
-        ctx.render(params(0, flags=1 << 10 | 1 << 8))
-        tc = ctx.traversal_counts()
-    per_launch_bytes = tc["nodes"] * 64 + tc["triangles"] * 48 + W * H * spp * 16
-    avg_ms = sum(kernel_ms) / len(kernel_ms)
-    achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
     peak, peak_kind = read_peaks()
     traffic = None
-    try:
-        if bdpt:
-            raise KeyError("no traffic summary for the bidirectional kernels")
-        with open(os.path.join(ROOT, "profiles", "path_kernel_traffic.json")) as f:
-            tj = json.load(f)
-        traffic = tj["dram_bytes_per_sample"] * W * H * spp
-    except Exception:
-        pass
+    if bdpt:
+        # the bidirectional kernels have no counting variant: whole render, node + film bytes unknown
+        tc = {"nodes": 0, "triangles": 0}
+        per_launch_bytes = W * H * spp * 16
+        avg_ms = sum(kernel_ms) / len(kernel_ms)
+        dominant = {"kernel": "whole render (bidirectional)", "avg_launch_ms": avg_ms}
+    else:
+        # per-kind device time from the timed steps; algorithmic bytes from one counting step
+        # of the same workload (same kernels, traversal counters on):
+        #  wfTrace: rays read (32 B), hits written (20 B), BVH nodes (64 B) and triangles (48 B)
+        #           its rays visit;
+        #  wfShade: per shaded path the regrouped ray and hit (52 B) and the path state (80 B)
+        #           read, the state written (80 B), a continuation ray (32 B) for every path
+        #           that continues and a shadow-queue entry (56 B) per light sample; volume
+        #           stacks are not counted (a lower bound).
+        ctx.render(params(0, flags=N.YG_FLAG_COUNT_TRAVERSAL | N.YG_FLAG_NO_FILM | N.YG_FLAG_TIME_KERNELS))
+        kp = ctx.kernel_profile()
+        tc = {"nodes": kp["closest_nodes"] + kp["shadow_nodes"], "triangles": kp["closest_triangles"] + kp["shadow_triangles"]}
+        samples_step = W * H * spp
+        algo = {
+            "trace": (kp["closest_rays"] * (32 + 20) + kp["closest_nodes"] * 64 + kp["closest_triangles"] * 48),
+            "shade": (kp["closest_rays"] * (52 + 80 + 80) + (kp["closest_rays"] - samples_step) * 32 + kp["shadow_rays"] * 56),
+        }
+        names = {"trace": "wfTrace", "shade": "wfShade"}
+        total_ms = sum(v["ms"] for v in kinds.values())
+        kernels = {}
+        for k in ("trace", "shade"):
+            nl = max(1, kp[k]["launches"])
+            avg = kinds[k]["ms"] / max(1, kinds[k]["launches"])
+            kernels[names[k]] = {"algorithmic_bytes_per_launch": algo[k] / nl, "avg_launch_ms": avg,
+                                 "achieved_gbs": algo[k] / nl / (avg / 1e3) / 1e9,
+                                 "share_of_timed_kernels": kinds[k]["ms"] / total_ms}
+        dom = max(kernels, key=lambda n: kernels[n]["share_of_timed_kernels"])
+        per_launch_bytes = kernels[dom]["algorithmic_bytes_per_launch"]
+        avg_ms = kernels[dom]["avg_launch_ms"]
+        dominant = {"kernel": dom, "rays_per_launch": kp["closest_rays"] / max(1, kp["trace"]["launches"]),
+                    "timed_share_by_kind": {k: v["ms"] / total_ms for k, v in kinds.items()}, "kernels": kernels}
+        try:
+            with open(os.path.join(ROOT, "profiles", "path_kernel_traffic.json")) as f:
+                tj = json.load(f)
+            traffic = tj[dom]["dram_bytes_per_launch"]
+            for n in kernels:
+                kernels[n]["traffic"] = tj[n]["dram_bytes_per_launch"]
+        except (OSError, KeyError, ValueError):
+            pass
+    achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and not bdpt:
         r, threads, sample = cpu_port_rate(scene)
@@ -298,7 +335,7 @@ def run_ours(args, world, rank, local):
                                parallelism="replicas: each GPU renders its own sample indices"),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                             "algorithmic_bytes_per_launch": per_launch_bytes,
+                             "algorithmic_bytes_per_launch": per_launch_bytes, "dominant": dominant,
                              "nodes_per_sample": tc["nodes"] / (W * H * spp),
                              "triangles_per_sample": tc["triangles"] / (W * H * spp)},
                 "cpu_baseline": cpu,

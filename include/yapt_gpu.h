@@ -137,6 +137,7 @@ typedef struct yg_camera
 #define YG_FLAG_FEATURES (1u << 9)     /* accumulate first-hit albedo/normal/depth */
 #define YG_FLAG_COUNT_TRAVERSAL (1u << 10) /* count BVH nodes visited / triangles tested (slower) */
 #define YG_FLAG_MEGAKERNEL (1u << 11)      /* one-thread-per-path kernel instead of the wavefront */
+#define YG_FLAG_TIME_KERNELS (1u << 12)    /* time each wavefront kernel kind with CUDA events */
 
 typedef struct yg_render_params
 {
@@ -260,6 +261,22 @@ YG_API int yg_render_samples_noalloc(yg_context* ctx, const yg_render_params* pa
 YG_API int yg_last_render_stats(yg_context* ctx, float* kernel_ms, uint64_t* rays, uint32_t* launches);
 /* Traversal work of the most recent render made with YG_FLAG_COUNT_TRAVERSAL. */
 YG_API int yg_last_traversal_counts(yg_context* ctx, uint64_t* nodes_visited, uint64_t* triangles_tested);
+
+/* Per-kernel device time of the most recent wavefront render made with YG_FLAG_TIME_KERNELS
+ * (CUDA events on the context stream around every launch of a kind), and with
+ * YG_FLAG_COUNT_TRAVERSAL the traversal work split between closest-hit and shadow rays. */
+#define YG_KERNEL_TRACE 0   /* closest-hit traversal of the path queue */
+#define YG_KERNEL_REGROUP 1 /* shading-class keys and the regrouping scatter */
+#define YG_KERNEL_SHADE 2   /* surface interaction, BSDF sampling, light sampling */
+#define YG_KERNEL_SHADOW 3  /* shadow-ray traversal */
+typedef struct yg_kernel_profile
+{
+    float ms[4];          /* summed device milliseconds per YG_KERNEL_* kind */
+    uint32_t launches[4]; /* timed launches per kind */
+    uint64_t closest_rays, closest_nodes, closest_triangles;
+    uint64_t shadow_rays, shadow_nodes, shadow_triangles;
+} yg_kernel_profile;
+YG_API int yg_last_kernel_profile(yg_context* ctx, yg_kernel_profile* out);
 
 /* -- serving loop ----------------------------------------------------------------
  * No counterpart in the reference, which renders one interactive view at a time through

@@ -21,6 +21,7 @@ YG_FLAG_NO_FILM = 1 << 8
 YG_FLAG_FEATURES = 1 << 9
 YG_FLAG_COUNT_TRAVERSAL = 1 << 10
 YG_FLAG_MEGAKERNEL = 1 << 11
+YG_FLAG_TIME_KERNELS = 1 << 12
 
 TABLES = {
     "sobol": 0, "ss": 1, "ss_avg": 2, "ssms": 3, "ssms_avg": 4, "trans_denser": 5, "trans_lighter": 6,
@@ -86,6 +87,16 @@ class RenderParams(C.Structure):
 
 class SampleRecord(C.Structure):
     _fields_ = [("lambda_hero", C.c_float), ("radiance", C.c_float * 4), ("xyz", C.c_float * 3)]
+
+
+class KernelProfile(C.Structure):
+    """yg_kernel_profile: per-kind device time of the last wavefront render."""
+    _fields_ = [("ms", C.c_float * 4), ("launches", C.c_uint32 * 4),
+                ("closest_rays", C.c_uint64), ("closest_nodes", C.c_uint64), ("closest_triangles", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("shadow_nodes", C.c_uint64), ("shadow_triangles", C.c_uint64)]
+
+
+KERNEL_KINDS = ("trace", "regroup", "shade", "shadow")
 
 
 class ServerOptions(C.Structure):
@@ -158,6 +169,7 @@ SIGNATURES = [
     ("yg_last_render_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint64),
                                        C.POINTER(C.c_uint32)]),
     ("yg_last_traversal_counts", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("yg_last_kernel_profile", C.c_int, [C.c_void_p, C.POINTER(KernelProfile)]),
     ("yg_render_samples_noalloc", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p]),
     ("yg_server_create", C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     ("yg_server_submit", C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_uint64)]),

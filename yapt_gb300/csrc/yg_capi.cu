@@ -714,8 +714,28 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     const bool mega = (p->flags & YG_FLAG_MEGAKERNEL) != 0;
     uint32_t waveCap = (uint32_t)std::min<uint64_t>(npix * chunkSpp, 1ull << 22);
     if (!mega && !bdpt) YG_CUDA(ctx->dArena.ensure(waveCap * yg::wavefrontBytesPerSlot() + (64u << 10)));
-    YG_CUDA(ctx->dRayCount.ensure(24));
-    YG_CUDA(cudaMemsetAsync(ctx->dRayCount.p, 0, 24, ctx->stream));
+    const size_t counterBytes = 8 * (1 + yg::kTraversalCounters);
+    YG_CUDA(ctx->dRayCount.ensure(counterBytes));
+    YG_CUDA(cudaMemsetAsync(ctx->dRayCount.p, 0, counterBytes, ctx->stream));
+    yg::KernelTimer timer{nullptr, nullptr, 0, 0};
+    const bool timeKernels = (p->flags & YG_FLAG_TIME_KERNELS) != 0 && !bdpt && !mega;
+    if (timeKernels)
+    {
+        // events for every timed launch of the render: 4 kinds per bounce, per wave
+        uint64_t waves = (npix * (uint64_t)p->spp_count + waveCap - 1) / waveCap;
+        size_t want = (size_t)std::min<uint64_t>(waves * p->max_depth * 4, 1u << 14);
+        while (ctx->kernelKinds.size() < want)
+        {
+            cudaEvent_t a = nullptr, b = nullptr;
+            YG_CUDA(cudaEventCreate(&a));
+            YG_CUDA(cudaEventCreate(&b));
+            ctx->kernelEvents.push_back(a);
+            ctx->kernelEvents.push_back(b);
+            ctx->kernelKinds.push_back(0);
+        }
+        timer = yg::KernelTimer{ctx->kernelEvents.data(), ctx->kernelKinds.data(), (uint32_t)ctx->kernelKinds.size(), 0};
+    }
+    ctx->kernelTimed = 0;
     // Sobol points of every sample index of the request (RaytraceCommonResources.cpp:623-627)
     std::vector<uint32_t> pts((size_t)p->spp_count * yg::kSobolDims);
     for (uint32_t s = 0; s < p->spp_count; ++s)
@@ -761,7 +781,8 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
                                        yg::mk3(ctx->worldCenter[0], ctx->worldCenter[1], ctx->worldCenter[2]),
                                        ctx->worldRadiusSqr, ctx->smCount, ctx->stream);
         else if (mega) launches += yg::launchPathKernel(S, L, ctx->smCount, ctx->stream);
-        else launches += yg::launchWavefront(S, L, ctx->dArena.p, waveCap, ctx->smCount, ctx->stream);
+        else launches += yg::launchWavefront(S, L, ctx->dArena.p, waveCap, ctx->smCount, ctx->stream,
+                                             timeKernels ? &timer : nullptr);
         if (film)
             launches += yg::launchFilm(ctx->dFilmSum.as<float4>(), ctx->dFilmComp.as<float4>(), L.sampleXYZ, p->width, cx,
                                        cy, cw, ch, ns, ctx->smCount, ctx->stream);
@@ -777,6 +798,7 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     YG_CUDA(cudaGetLastError());
     YG_CUDA(cudaEventRecord(ctx->evStop, ctx->stream));
     ctx->lastLaunches = launches;
+    ctx->kernelTimed = timer.used;
     if (dump)
     {
         YG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -801,14 +823,42 @@ YG_API int yg_last_render_stats(yg_context* ctx, float* ms, uint64_t* rays, uint
 YG_API int yg_last_traversal_counts(yg_context* ctx, uint64_t* nodes, uint64_t* tris)
 {
     if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
-    unsigned long long c[3] = {0, 0, 0};
+    unsigned long long c[1 + yg::kTraversalCounters] = {};
     if (ctx->dRayCount.p)
     {
         YG_CUDA(cudaStreamSynchronize(ctx->stream));
-        YG_CUDA(cudaMemcpy(c, ctx->dRayCount.p, 24, cudaMemcpyDeviceToHost));
+        YG_CUDA(cudaMemcpy(c, ctx->dRayCount.p, sizeof(c), cudaMemcpyDeviceToHost));
     }
-    if (nodes) *nodes = c[1];
-    if (tris) *tris = c[2];
+    if (nodes) *nodes = c[1] + c[3];
+    if (tris) *tris = c[2] + c[4];
+    return YG_OK;
+}
+
+static_assert(YG_KERNEL_TRACE == yg::kKernelTrace && YG_KERNEL_REGROUP == yg::kKernelRegroup &&
+                  YG_KERNEL_SHADE == yg::kKernelShade && YG_KERNEL_SHADOW == yg::kKernelShadow,
+              "kernel kinds");
+
+YG_API int yg_last_kernel_profile(yg_context* ctx, yg_kernel_profile* out)
+{
+    if (!ctx || !out) return fail(YG_ERR_INVALID_ARGUMENT, "kernel profile: null argument");
+    std::memset(out, 0, sizeof(*out));
+    YG_CUDA(cudaEventSynchronize(ctx->evStop));
+    for (uint32_t k = 0; k < ctx->kernelTimed; ++k)
+    {
+        float t = 0;
+        YG_CUDA(cudaEventElapsedTime(&t, ctx->kernelEvents[2 * k], ctx->kernelEvents[2 * k + 1]));
+        uint8_t kind = ctx->kernelKinds[k];
+        out->ms[kind] += t;
+        out->launches[kind] += 1;
+    }
+    unsigned long long c[1 + yg::kTraversalCounters] = {};
+    if (ctx->dRayCount.p) YG_CUDA(cudaMemcpy(c, ctx->dRayCount.p, sizeof(c), cudaMemcpyDeviceToHost));
+    out->closest_nodes = c[1];
+    out->closest_triangles = c[2];
+    out->shadow_nodes = c[3];
+    out->shadow_triangles = c[4];
+    out->closest_rays = c[5];
+    out->shadow_rays = c[6];
     return YG_OK;
 }
 

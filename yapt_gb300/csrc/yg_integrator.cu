@@ -95,7 +95,11 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, Hi
         H.b[i] = found ? (h.prim | (h.front ? 0x80000000u : 0u)) : 0xffffffffu;
     }
     countRays(rayCtr, rays);
-    if (COUNT) countTraversal(travCtr, tc);
+    if (COUNT)
+    {
+        countTraversal(travCtr, tc);
+        countRays(travCtr + 4, rays);
+    }
 }
 
 __global__ void __launch_bounds__(256) wfClassify(const SceneView S, RayQueue Q, HitQueue H, uint8_t* keys, uint32_t* counts)
@@ -206,7 +210,11 @@ __global__ void __launch_bounds__(128) wfShadow(const SceneView S, WaveState W, 
         }
     }
     countRays(rayCtr, rays);
-    if (COUNT) countTraversal(travCtr, tc);
+    if (COUNT)
+    {
+        countTraversal(travCtr + 2, tc);
+        countRays(travCtr + 5, rays);
+    }
 }
 
 __global__ void __launch_bounds__(256) wfFinalize(const SceneView S, const LaunchParams P, WaveState W, uint64_t base,
@@ -332,7 +340,7 @@ size_t wavefrontBytesPerSlot()
 }
 
 int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint32_t capacity, int smCount,
-                    cudaStream_t stream)
+                    cudaStream_t stream, KernelTimer* T)
 {
     char* p = static_cast<char*>(arena);
     auto take = [&](size_t bytes) {
@@ -377,20 +385,28 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
         RayQueue* nxt = &QB;
         for (uint32_t b = 0; b < P.maxDepth; ++b)
         {
+            if (T) T->begin(stream);
             if (count) wfTrace<true><<<traceBlocks, 128, 0, stream>>>(S, *cur, H, P.rayCounter, P.traversalCounter);
             else wfTrace<false><<<traceBlocks, 128, 0, stream>>>(S, *cur, H, P.rayCounter, nullptr);
+            if (T) T->end(kKernelTrace, stream);
             cudaMemsetAsync(nxt->count, 0, 4, stream);
             cudaMemsetAsync(SQ.count, 0, 4, stream);
             cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
+            if (T) T->begin(stream);
             wfClassify<<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
             wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
+            if (T) T->end(kKernelRegroup, stream);
+            if (T) T->begin(stream);
             if (P.integrator == 1) wfShade<true><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ);
             else wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ);
+            if (T) T->end(kKernelShade, stream);
             launches += 4;
             if (P.integrator == 1)
             {
+                if (T) T->begin(stream);
                 if (count) wfShadow<true><<<traceBlocks, 128, 0, stream>>>(S, W, SQ, P.rayCounter, P.traversalCounter);
                 else wfShadow<false><<<traceBlocks, 128, 0, stream>>>(S, W, SQ, P.rayCounter, nullptr);
+                if (T) T->end(kKernelShadow, stream);
                 ++launches;
             }
             RayQueue* t = cur;

@@ -68,6 +68,9 @@ struct yg_context
     int smCount = 152;
     cudaStream_t stream = nullptr;
     cudaEvent_t evStart = nullptr, evStop = nullptr;
+    std::vector<cudaEvent_t> kernelEvents; // YG_FLAG_TIME_KERNELS: pairs around timed launches
+    std::vector<uint8_t> kernelKinds;
+    uint32_t kernelTimed = 0;
     std::string dataDir;
     // tables
     std::vector<uint32_t> sobolMatrices;
@@ -116,6 +119,7 @@ struct yg_context
                          &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm};
         for (DevBuf* b : all) b->release();
         for (auto& b : dLut) b.release();
+        for (cudaEvent_t e : kernelEvents) cudaEventDestroy(e);
         if (evStart) cudaEventDestroy(evStart);
         if (evStop) cudaEventDestroy(evStop);
         if (stream) cudaStreamDestroy(stream);

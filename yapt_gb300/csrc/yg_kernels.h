@@ -8,8 +8,35 @@ int launchPathKernel(const SceneView& S, const LaunchParams& P, int smCount, cud
 // Wavefront integrator over P.nSamples samples in waves of `capacity` paths; `arena`
 // holds capacity * wavefrontBytesPerSlot() bytes plus 64 KB. Returns the launch count.
 size_t wavefrontBytesPerSlot();
+// Kernel kinds of the timer (the C-ABI's YG_KERNEL_* values).
+constexpr uint8_t kKernelTrace = 0, kKernelRegroup = 1, kKernelShade = 2, kKernelShadow = 3;
+// Optional CUDA-event timing of launches by kind: events[2k], events[2k+1] bracket the k-th
+// timed launch, whose kind is kinds[k]. Timing stops when the events run out.
+struct KernelTimer
+{
+    cudaEvent_t* events;
+    uint8_t* kinds;
+    uint32_t capacity; // launches
+    uint32_t used;
+    void begin(cudaStream_t s)
+    {
+        if (used < capacity) cudaEventRecord(events[2 * used], s);
+    }
+    void end(uint8_t kind, cudaStream_t s)
+    {
+        if (used < capacity)
+        {
+            cudaEventRecord(events[2 * used + 1], s);
+            kinds[used++] = kind;
+        }
+    }
+};
+// Traversal counters (LaunchParams::traversalCounter): [0] nodes and [1] triangles of
+// closest-hit rays, [2] nodes and [3] triangles of shadow rays, [4] closest-hit rays,
+// [5] shadow rays (the path kernel counts all rays' work in [0] and [1]).
+constexpr int kTraversalCounters = 6;
 int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint32_t capacity, int smCount,
-                    cudaStream_t stream);
+                    cudaStream_t stream, KernelTimer* timer = nullptr);
 int launchFilm(float4* sum, float4* comp, const float4* samples, uint32_t width, uint32_t cx, uint32_t cy, uint32_t cw,
                uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
 int launchFeatures(float4* accA, float4* accN, const float4* fa, const float4* fn, uint32_t width, uint32_t cx, uint32_t cy,

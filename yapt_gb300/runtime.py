@@ -120,6 +120,16 @@ class Context:
         N.check(self.lib.yg_last_render_stats(self.h, C.byref(ms), C.byref(rays), C.byref(launches)))
         return dict(ms=ms.value, rays=rays.value, launches=launches.value)
 
+    def kernel_profile(self):
+        """Per-kind device time of the last render made with YG_FLAG_TIME_KERNELS, and (with
+        YG_FLAG_COUNT_TRAVERSAL) the traversal work of closest-hit and shadow rays."""
+        kp = N.KernelProfile()
+        N.check(self.lib.yg_last_kernel_profile(self.h, C.byref(kp)))
+        out = {k: {"ms": kp.ms[i], "launches": kp.launches[i]} for i, k in enumerate(N.KERNEL_KINDS)}
+        for f in ("closest_rays", "closest_nodes", "closest_triangles", "shadow_rays", "shadow_nodes", "shadow_triangles"):
+            out[f] = getattr(kp, f)
+        return out
+
     def traversal_counts(self):
         n, t = C.c_uint64(), C.c_uint64()
         N.check(self.lib.yg_last_traversal_counts(self.h, C.byref(n), C.byref(t)))
