@@ -210,6 +210,10 @@ YG_API int yg_host_table(const char* data_dir, int which, int lambda_min, int la
 
 /* -- scene ingest ----------------------------------------------------------- */
 YG_API int yg_upload_mesh(yg_context* ctx, const yg_mesh_desc* desc, uint32_t* mesh_id);
+/* Drops every uploaded mesh (mesh ids restart at 0), as when the last reference to a
+ * Mesh is released (MeshManager, Source/Renderer/src/Shared/MeshManager.cpp). The scene
+ * must be rebuilt (yg_set_instances + yg_build_scene) before the next render. */
+YG_API int yg_clear_meshes(yg_context* ctx);
 YG_API int yg_upload_materials(yg_context* ctx, const yg_material* materials, uint32_t count);
 /* n_curves curves of n_points values on a uniform grid lambda_min..lambda_max. */
 YG_API int yg_upload_spectra(yg_context* ctx, const float* values, uint32_t n_curves, uint32_t n_points,

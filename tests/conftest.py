@@ -23,6 +23,15 @@ def built():
     return True
 
 
+@pytest.fixture(scope="session")
+def py_yapt(built):
+    """The pybind11 module (YAPT's Python surface), built next to the library."""
+    from yapt_gb300 import build as B
+    B.build_pybind()
+    from yapt_gb300 import py_yapt as Y
+    return Y
+
+
 LUT_NAMES = ["ss", "ss_avg", "ssms", "ssms_avg", "trans_denser", "trans_lighter", "trans_avg_denser",
              "trans_avg_lighter", "sheen"]
 

@@ -99,8 +99,10 @@ def build_pybind(verbose=False):
 def build_all(verbose=False):
     lib = build_lib(verbose)
     mods = [lib]
-    if os.path.exists(os.path.join(CSRC, "py_yapt.cpp")):
+    if os.path.exists(os.path.join(sysconfig.get_paths()["include"], "Python.h")):
         mods.append(build_pybind(verbose))
+    else:
+        print("py_yapt not built: no Python development headers (Python.h) on this machine", file=sys.stderr)
     return mods
 
 

@@ -428,6 +428,20 @@ YG_API int yg_upload_mesh(yg_context* ctx, const yg_mesh_desc* d, uint32_t* mesh
     return YG_OK;
 }
 
+YG_API int yg_clear_meshes(yg_context* ctx)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    ctx->positions.clear();
+    ctx->normals.clear();
+    ctx->tangents.clear();
+    ctx->uvs.clear();
+    ctx->indices.clear();
+    ctx->meshes.clear();
+    ctx->sceneBuilt = false;
+    return YG_OK;
+}
+
 YG_API int yg_upload_materials(yg_context* ctx, const yg_material* mats, uint32_t count)
 {
     if (!ctx || (!mats && count)) return fail(YG_ERR_INVALID_ARGUMENT, "materials: null argument");
