@@ -285,7 +285,7 @@ def run_ours(args, world, rank, local):
     else:
         # per-kind device time from the timed steps; algorithmic bytes from one counting step
         # of the same workload (same kernels, traversal counters on):
-        #  wfTrace: rays read (32 B), hits written (20 B), BVH nodes (64 B) and triangles (48 B)
+        #  wfTrace: rays read (32 B), hits written (20 B), wide BVH nodes (80 B) and triangles (48 B)
         #           its rays visit;
         #  wfShade: per shaded path the regrouped ray and hit (52 B) and the path state (80 B)
         #           read, the state written (80 B), a continuation ray (32 B) for every path
@@ -296,7 +296,7 @@ def run_ours(args, world, rank, local):
         tc = {"nodes": kp["closest_nodes"] + kp["shadow_nodes"], "triangles": kp["closest_triangles"] + kp["shadow_triangles"]}
         samples_step = W * H * spp
         algo = {
-            "trace": (kp["closest_rays"] * (32 + 20) + kp["closest_nodes"] * 64 + kp["closest_triangles"] * 48),
+            "trace": (kp["closest_rays"] * (32 + 20) + kp["closest_nodes"] * 80 + kp["closest_triangles"] * 48),
             "shade": (kp["closest_rays"] * (52 + 80 + 80) + (kp["closest_rays"] - samples_step) * 32 + kp["shadow_rays"] * 56),
         }
         names = {"trace": "wfTrace", "shade": "wfShade"}

@@ -223,6 +223,10 @@ YG_API int yg_set_camera(yg_context* ctx, const yg_camera* camera);
 /* Builds the acceleration structure and the light tables (alias tables over mesh
  * lights, RaytraceCommonResources.cpp:325-547) for the current meshes/instances/materials. */
 YG_API int yg_build_scene(yg_context* ctx);
+/* Diagnostic of the device-built wide BVH: walks the tree on the host and counts the child
+ * slots whose dequantised box (evaluated in double) does not contain the triangles under
+ * the slot; *violations must be 0. Also returns the node count and the depth in wide levels. */
+YG_API int yg_bvh_check(yg_context* ctx, uint64_t* n_nodes, uint64_t* depth, uint64_t* violations);
 /* Scene statistics: triangles, BVH nodes, lights, device bytes. */
 YG_API int yg_scene_info(yg_context* ctx, uint64_t* n_triangles, uint64_t* n_nodes, uint64_t* n_lights,
                          uint64_t* device_bytes);

@@ -27,8 +27,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + os.path.join(CUDA_HOME, "include"),
              "-Wall", "-Wno-unused-function"]
 
-CUDA_SOURCES = ["yg_integrator.cu", "yg_bdpt.cu", "yg_serve_kernels.cu", "yg_nn.cu", "yg_capi.cu"]
-CXX_SOURCES = ["yg_tables.cpp", "yg_bvh.cpp", "yg_server.cpp"]
+CUDA_SOURCES = ["yg_integrator.cu", "yg_bdpt.cu", "yg_serve_kernels.cu", "yg_nn.cu", "yg_bvh_build.cu", "yg_capi.cu"]
+CXX_SOURCES = ["yg_tables.cpp", "yg_server.cpp"]
 
 
 def _run(cmd):

@@ -3,10 +3,10 @@
 // (RaytraceCommonResources.cpp, BindlessMaterialManager.cpp, LightManager.cpp,
 // PathTraceStage.cpp) on one CUDA stream.
 #include "yg_internal.h"
-#include "yg_bvh.h"
 #include "yg_vec.cuh"
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -495,6 +495,161 @@ YG_API int yg_set_camera(yg_context* ctx, const yg_camera* cam)
     return YG_OK;
 }
 
+extern "C++"
+{
+namespace
+{
+struct WideNodeHost
+{
+    float p[3];
+    uint32_t e[3], imask, childBase, triBase, meta[8], qlo[3][8], qhi[3][8];
+};
+
+WideNodeHost decodeWide(const float4* n)
+{
+    auto u = [](float f) {
+        uint32_t v;
+        std::memcpy(&v, &f, 4);
+        return v;
+    };
+    WideNodeHost w;
+    w.p[0] = n[0].x, w.p[1] = n[0].y, w.p[2] = n[0].z;
+    uint32_t pk = u(n[0].w);
+    w.e[0] = pk & 0xffu, w.e[1] = (pk >> 8) & 0xffu, w.e[2] = (pk >> 16) & 0xffu, w.imask = pk >> 24;
+    w.childBase = u(n[1].x), w.triBase = u(n[1].y);
+    const uint32_t words[10] = {u(n[1].z), u(n[1].w), u(n[2].x), u(n[2].y), u(n[2].z), u(n[2].w), u(n[3].x), u(n[3].y),
+                                u(n[3].z), u(n[3].w)};
+    const uint32_t words2[4] = {u(n[4].x), u(n[4].y), u(n[4].z), u(n[4].w)};
+    auto byteAt = [](uint32_t a, uint32_t b, int i) { return ((i < 4 ? a : b) >> (8 * (i & 3))) & 0xffu; };
+    for (int i = 0; i < 8; ++i)
+    {
+        w.meta[i] = byteAt(words[0], words[1], i);
+        w.qlo[0][i] = byteAt(words[2], words[3], i);
+        w.qlo[1][i] = byteAt(words[4], words[5], i);
+        w.qlo[2][i] = byteAt(words[6], words[7], i);
+        w.qhi[0][i] = byteAt(words[8], words[9], i);
+        w.qhi[1][i] = byteAt(words2[0], words2[1], i);
+        w.qhi[2][i] = byteAt(words2[2], words2[3], i);
+    }
+    return w;
+}
+} // namespace
+
+// Walks the wide tree from the root: every inner child index in range and reached once,
+// every triangle slot in range and referenced once, depth within the traversal stack.
+int ygi::checkWideBvhStructure(yg_context* ctx)
+{
+    std::vector<float4> nodes((size_t)ctx->nNodes * 5);
+    YG_CUDA(cudaMemcpyAsync(nodes.data(), ctx->dNodes.p, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<uint8_t> seen(ctx->nNodes, 0), triSeen(ctx->nTris, 0);
+    std::vector<std::pair<uint32_t, uint32_t>> todo{{0u, 1u}};
+    seen[0] = 1;
+    uint64_t nodeCount = 0, triCount = 0;
+    while (!todo.empty())
+    {
+        auto [idx, depth] = todo.back();
+        todo.pop_back();
+        ++nodeCount;
+        if (depth > (uint32_t)yg::kWideMaxDepth) return fail(YG_ERR_CUDA, "bvh check: tree too deep");
+        WideNodeHost w = decodeWide(&nodes[5 * (size_t)idx]);
+        uint32_t rank = 0;
+        for (int i = 0; i < 8; ++i)
+        {
+            if (w.imask & (1u << i))
+            {
+                uint64_t c = (uint64_t)w.childBase + rank++;
+                if (c >= ctx->nNodes || seen[c]) return fail(YG_ERR_CUDA, "bvh check: bad inner child reference");
+                seen[c] = 1;
+                todo.push_back({(uint32_t)c, depth + 1});
+            }
+            else if (w.meta[i])
+            {
+                uint32_t cnt = w.meta[i] >> 5, off = w.meta[i] & 31u;
+                if (cnt == 0 || cnt > (uint32_t)yg::kMaxLeafTris || off + cnt > 24)
+                    return fail(YG_ERR_CUDA, "bvh check: bad leaf slot");
+                for (uint32_t k = 0; k < cnt; ++k)
+                {
+                    uint64_t t = (uint64_t)w.triBase + off + k;
+                    if (t >= ctx->nTris || triSeen[t]) return fail(YG_ERR_CUDA, "bvh check: bad triangle reference");
+                    triSeen[t] = 1;
+                    ++triCount;
+                }
+            }
+        }
+    }
+    if (nodeCount != ctx->nNodes || triCount != ctx->nTris)
+        return fail(YG_ERR_CUDA, "bvh check: " + std::to_string(nodeCount) + " nodes / " + std::to_string(triCount) +
+                                     " triangles reachable of " + std::to_string(ctx->nNodes) + " / " +
+                                     std::to_string(ctx->nTris));
+    return YG_OK;
+}
+
+} // extern "C++"
+
+YG_API int yg_bvh_check(yg_context* ctx, uint64_t* n_nodes, uint64_t* depth, uint64_t* violations)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    if (!ctx->sceneBuilt) return fail(YG_ERR_NOT_READY, "bvh check: no scene built");
+    int r;
+    if ((r = checkWideBvhStructure(ctx))) return r;
+    std::vector<float4> nodes((size_t)ctx->nNodes * 5), tris((size_t)ctx->nTris * 3);
+    YG_CUDA(cudaMemcpy(nodes.data(), ctx->dNodes.p, nodes.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    if (!tris.empty()) YG_CUDA(cudaMemcpy(tris.data(), ctx->dTris.p, tris.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    // bounds (double) of the triangles under each slot must lie in the slot's dequantised box
+    uint64_t bad = 0;
+    struct Box
+    {
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        void grow(const Box& b)
+        {
+            for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], b.lo[a]), hi[a] = std::max(hi[a], b.hi[a]);
+        }
+    };
+    auto triBox = [&](uint64_t t) {
+        Box b;
+        const float4 *v = &tris[3 * t], *e1 = v + 1, *e2 = v + 2;
+        const double p0[3] = {v->x, v->y, v->z};
+        const double p1[3] = {p0[0] + e1->x, p0[1] + e1->y, p0[2] + e1->z};
+        const double p2[3] = {p0[0] + e2->x, p0[1] + e2->y, p0[2] + e2->z};
+        for (int a = 0; a < 3; ++a)
+        {
+            b.lo[a] = std::min({p0[a], p1[a], p2[a]});
+            b.hi[a] = std::max({p0[a], p1[a], p2[a]});
+        }
+        return b;
+    };
+    uint64_t maxDepth = 0;
+    std::function<Box(uint32_t, uint64_t)> visit = [&](uint32_t idx, uint64_t d) -> Box {
+        maxDepth = std::max(maxDepth, d);
+        WideNodeHost w = decodeWide(&nodes[5 * (size_t)idx]);
+        Box all;
+        uint32_t rank = 0;
+        for (int i = 0; i < 8; ++i)
+        {
+            Box cb;
+            if (w.imask & (1u << i)) cb = visit(w.childBase + rank++, d + 1);
+            else if (w.meta[i])
+                for (uint32_t k = 0; k < (w.meta[i] >> 5); ++k) cb.grow(triBox((uint64_t)w.triBase + (w.meta[i] & 31u) + k));
+            else continue;
+            for (int a = 0; a < 3; ++a)
+            {
+                double scale = std::ldexp(1.0, (int)w.e[a] - 127);
+                double lo = (double)w.p[a] + scale * w.qlo[a][i], hi = (double)w.p[a] + scale * w.qhi[a][i];
+                if (!(cb.lo[a] >= lo && cb.hi[a] <= hi)) ++bad;
+            }
+            all.grow(cb);
+        }
+        return all;
+    };
+    if (ctx->nTris) visit(0, 1);
+    if (n_nodes) *n_nodes = ctx->nNodes;
+    if (depth) *depth = maxDepth;
+    if (violations) *violations = bad;
+    return YG_OK;
+}
+
 YG_API int yg_build_scene(yg_context* ctx)
 {
     if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
@@ -510,10 +665,9 @@ YG_API int yg_build_scene(yg_context* ctx)
     }
     const size_t nInst = ctx->instances.size();
     std::vector<yg::GpuInstance> gi(nInst);
-    std::vector<float3> v0, v1, v2;
-    std::vector<uint32_t> ki, kp;
     std::vector<float> power;
     std::vector<uint32_t> lightInst;
+    std::vector<uint32_t> primStart(nInst + 1, 0);
     for (size_t i = 0; i < nInst; ++i)
     {
         const yg_instance& I = ctx->instances[i];
@@ -534,29 +688,24 @@ YG_API int yg_build_scene(yg_context* ctx)
         G.lightPdf = 0.0f;
         G.hasTangents = m.tangents ? 1u : 0u;
         G.hasUVs = m.uvs ? 1u : 0u;
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (uint32_t p = 0; p < G.primCount; ++p)
-        {
-            float3 w[3];
-            for (int k = 0; k < 3; ++k)
-            {
-                uint32_t vi = ctx->indices[G.firstIndex + 3 * p + k] + G.vertexBase;
-                float3 ob = yg::mk3(ctx->positions[3 * vi], ctx->positions[3 * vi + 1], ctx->positions[3 * vi + 2]);
-                w[k] = yg::xformPoint(G.o2w, ob);
-                lo[0] = std::min(lo[0], w[k].x); lo[1] = std::min(lo[1], w[k].y); lo[2] = std::min(lo[2], w[k].z);
-                hi[0] = std::max(hi[0], w[k].x); hi[1] = std::max(hi[1], w[k].y); hi[2] = std::max(hi[2], w[k].z);
-            }
-            v0.push_back(w[0]);
-            v1.push_back(w[1]);
-            v2.push_back(w[2]);
-            ki.push_back((uint32_t)i);
-            kp.push_back(p);
-        }
+        if ((uint64_t)primStart[i] + G.primCount > 0xffffffffull) return fail(YG_ERR_INVALID_ARGUMENT, "scene: too many triangles");
+        primStart[i + 1] = primStart[i] + G.primCount;
         // mesh lights: emissive materials (LightManager.cpp:145), power estimate of
-        // estimateMeshLightPower (RaytraceCommonResources.cpp:385-404) over the instance bounds
+        // estimateMeshLightPower (RaytraceCommonResources.cpp:385-404) over the instance's
+        // world-space bounds
         const yg_material& M = ctx->materials[I.material];
         if (M.emissive[0] + M.emissive[1] + M.emissive[2] > 0.0f && G.primCount > 0)
         {
+            float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (uint32_t p = 0; p < G.primCount; ++p)
+                for (int k = 0; k < 3; ++k)
+                {
+                    uint32_t vi = ctx->indices[G.firstIndex + 3 * p + k] + G.vertexBase;
+                    float3 ob = yg::mk3(ctx->positions[3 * vi], ctx->positions[3 * vi + 1], ctx->positions[3 * vi + 2]);
+                    float3 w = yg::xformPoint(G.o2w, ob);
+                    lo[0] = std::min(lo[0], w.x); lo[1] = std::min(lo[1], w.y); lo[2] = std::min(lo[2], w.z);
+                    hi[0] = std::max(hi[0], w.x); hi[1] = std::max(hi[1], w.y); hi[2] = std::max(hi[2], w.z);
+                }
             float ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
             float area = ex * ey + ey * ez + ez * ex;
             float e = 0.2126f * M.emissive[0] + 0.7152f * M.emissive[1] + 0.0722f * M.emissive[2];
@@ -582,34 +731,7 @@ YG_API int yg_build_scene(yg_context* ctx)
             gi[lightInst[l]].lightPdf = power[l];
         }
     }
-    // world bounds of all triangles (RaytraceCommonResources.cpp:560-600 unions the object bounds)
-    float wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (size_t t = 0; t < v0.size(); ++t)
-    {
-        const float3 vs[3] = {v0[t], v1[t], v2[t]};
-        for (const float3& v : vs)
-        {
-            wlo[0] = std::min(wlo[0], v.x); wlo[1] = std::min(wlo[1], v.y); wlo[2] = std::min(wlo[2], v.z);
-            whi[0] = std::max(whi[0], v.x); whi[1] = std::max(whi[1], v.y); whi[2] = std::max(whi[2], v.z);
-        }
-    }
-    if (v0.empty()) wlo[0] = wlo[1] = wlo[2] = whi[0] = whi[1] = whi[2] = 0.0f;
-    float ext2 = 0.0f;
-    for (int k = 0; k < 3; ++k)
-    {
-        ctx->worldCenter[k] = (whi[k] + wlo[k]) * 0.5f;
-        float e = whi[k] - ctx->worldCenter[k];
-        ext2 += e * e;
-    }
-    ctx->worldRadiusSqr = ext2;
-    std::vector<float4> tris, nodes;
-    yg::buildBvh(v0, v1, v2, ki, kp, tris, nodes);
-    ctx->nTris = v0.size();
-    ctx->nNodes = nodes.size() / 4;
-    ctx->nLights = (uint32_t)lights.size();
     int r;
-    if ((r = upload(ctx, ctx->dTris, tris.data(), tris.size()))) return r;
-    if ((r = upload(ctx, ctx->dNodes, nodes.data(), nodes.size()))) return r;
     if ((r = upload(ctx, ctx->dInst, gi.data(), gi.size()))) return r;
     if ((r = upload(ctx, ctx->dLights, lights.data(), lights.size()))) return r;
     if ((r = upload(ctx, ctx->dPos, ctx->positions.data(), ctx->positions.size()))) return r;
@@ -622,6 +744,30 @@ YG_API int yg_build_scene(yg_context* ctx)
         float z[4] = {0, 0, 0, 0};
         if ((r = upload(ctx, ctx->dSpec, z, 4))) return r;
     }
+    // the acceleration structure, built on the device
+    yg::WideBvhInput bin{ctx->dInst.as<yg::GpuInstance>(), (uint32_t)nInst, primStart, ctx->dPos.as<float>(),
+                         ctx->dIdx.as<uint32_t>(), primStart[nInst]};
+    yg::WideBvhOutput bout{};
+    std::string berr;
+    if (yg::buildWideBvh(bin, bout, ctx->stream, berr) != 0) return fail(YG_ERR_CUDA, berr);
+    ctx->dTris.adopt(bout.tris, 3 * sizeof(float4) * std::max<uint32_t>(primStart[nInst], 1));
+    ctx->dNodes.adopt(bout.nodes, 5 * sizeof(float4) * (size_t)bout.nNodes);
+    ctx->nTris = primStart[nInst];
+    ctx->nNodes = bout.nNodes;
+    ctx->bvhDepth = bout.depth;
+    ctx->nLights = (uint32_t)lights.size();
+    // every inner node reachable exactly once and every triangle referenced exactly once,
+    // checked before any ray can traverse the tree
+    if ((r = checkWideBvhStructure(ctx))) return r;
+    // world bounds of all triangles (RaytraceCommonResources.cpp:560-600 unions the object bounds)
+    float ext2 = 0.0f;
+    for (int k = 0; k < 3; ++k)
+    {
+        ctx->worldCenter[k] = (bout.hi[k] + bout.lo[k]) * 0.5f;
+        float e = bout.hi[k] - ctx->worldCenter[k];
+        ext2 += e * e;
+    }
+    ctx->worldRadiusSqr = ext2;
     YG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->sceneBuilt = true;
     return YG_OK;

@@ -84,16 +84,17 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, Hi
     const uint32_t n = *Q.count;
     TraversalCount tc{0, 0};
     uint32_t rays = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    {
-        float4 o = Q.o[i], d = Q.d[i];
-        Hit h;
-        bool found = traceClosest<COUNT>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000),
-                                         h, &tc);
-        rays++;
-        H.a[i] = mk4(h.t, h.b1, h.b2, __uint_as_float(h.instance));
-        H.b[i] = found ? (h.prim | (h.front ? 0x80000000u : 0u)) : 0xffffffffu;
-    }
+    traceGrid<COUNT>(
+        n,
+        [&](TraceState& t, uint32_t i) {
+            const float4 o = Q.o[i], d = Q.d[i];
+            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000));
+        },
+        [&](const TraceState& t, uint32_t i) {
+            H.a[i] = mk4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.instance));
+            H.b[i] = t.found ? (t.h.prim | (t.h.front ? 0x80000000u : 0u)) : 0xffffffffu;
+        },
+        tc, rays);
     countRays(rayCtr, rays);
     if (COUNT)
     {
@@ -196,19 +197,21 @@ __global__ void __launch_bounds__(128) wfShadow(const SceneView S, WaveState W, 
     const uint32_t n = *SQ.count;
     TraversalCount tc{0, 0};
     uint32_t rays = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    {
-        float4 o = SQ.o[i], d = SQ.d[i];
-        uint2 tg = SQ.target[i];
-        Hit h;
-        bool any = traceClosest<COUNT>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, h, &tc);
-        rays++;
-        if (shadowVisible(any, h, tg.x, tg.y))
-        {
-            uint32_t s = __float_as_uint(o.w);
-            W.tot[s] = W.tot[s] + SQ.contrib[i];
-        }
-    }
+    traceGrid<COUNT>(
+        n,
+        [&](TraceState& t, uint32_t i) {
+            const float4 o = SQ.o[i], d = SQ.d[i];
+            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w);
+        },
+        [&](const TraceState& t, uint32_t i) {
+            const uint2 tg = SQ.target[i];
+            if (shadowVisible(t.found, t.h, tg.x, tg.y))
+            {
+                const uint32_t s = __float_as_uint(SQ.o[i].w);
+                W.tot[s] = W.tot[s] + SQ.contrib[i];
+            }
+        },
+        tc, rays);
     countRays(rayCtr, rays);
     if (COUNT)
     {

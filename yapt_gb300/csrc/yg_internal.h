@@ -45,6 +45,13 @@ struct DevBuf
         p = nullptr;
         bytes = 0;
     }
+    // takes ownership of a cudaMalloc'd block
+    void adopt(void* q, size_t n)
+    {
+        release();
+        p = q;
+        bytes = n;
+    }
     template <typename T>
     T* as() const { return static_cast<T*>(p); }
 };
@@ -93,6 +100,7 @@ struct yg_context
     bool cameraSet = false;
     bool sceneBuilt = false;
     uint64_t nTris = 0, nNodes = 0;
+    uint32_t bvhDepth = 0;
     // device
     DevBuf dTris, dNodes, dInst, dMat, dLights, dPos, dNrm, dTan, dUV, dIdx, dSpec;
     DevBuf dLut[9];
@@ -143,6 +151,7 @@ int ensureRgbLut(yg_context* c, int lmin, int lmax);
 // The scene arrays and tables of a context as one SceneView (Sobol points left unset); the
 // CIE table of [lmin, lmax] (and the RGB table when needRgb) must be current.
 void fillSceneView(const yg_context* c, float lmin, float lmax, bool needRgb, yg::SceneView& S);
+int checkWideBvhStructure(yg_context* c);
 // the pixel order of the BDPT camera groups for a cw x ch crop
 void pixelPermutation(uint32_t cw, uint32_t ch, std::vector<uint32_t>& perm);
 } // namespace ygi

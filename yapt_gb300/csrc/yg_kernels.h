@@ -2,12 +2,41 @@
 #pragma once
 #include "yg_types.h"
 
+#include <string>
+#include <vector>
+
 namespace yg
 {
 int launchPathKernel(const SceneView& S, const LaunchParams& P, int smCount, cudaStream_t stream);
 // Wavefront integrator over P.nSamples samples in waves of `capacity` paths; `arena`
 // holds capacity * wavefrontBytesPerSlot() bytes plus 64 KB. Returns the launch count.
 size_t wavefrontBytesPerSlot();
+// Device-built 8-wide BVH (yg_bvh_build.cu). Input: the instances, object-space vertex and
+// index pools already on the device, and the first primitive of every instance (host,
+// nInstances + 1 prefix sums of primCount). Output: leaf-ordered world-space triangles (3
+// float4 each: v0 + instance, e1 + primitive, e2) and 80-byte wide nodes (5 float4, layout
+// in yg_trace.cuh), both allocated with cudaMalloc and owned by the caller.
+constexpr int kMaxLeafTris = 3;   // triangles per wide-node leaf slot
+constexpr int kWideMaxDepth = 30; // wide levels (the traversal stack holds one entry per level)
+struct WideBvhInput
+{
+    const GpuInstance* instances;
+    uint32_t nInstances;
+    std::vector<uint32_t> instPrimStart;
+    const float* positions;
+    const uint32_t* indices;
+    uint32_t nPrims;
+};
+struct WideBvhOutput
+{
+    float4* tris;
+    float4* nodes;
+    uint32_t nNodes;
+    uint32_t depth;
+    float lo[3], hi[3]; // world bounds of all triangles
+};
+int buildWideBvh(const WideBvhInput& in, WideBvhOutput& out, cudaStream_t stream, std::string& error);
+
 // Kernel kinds of the timer (the C-ABI's YG_KERNEL_* values).
 constexpr uint8_t kKernelTrace = 0, kKernelRegroup = 1, kKernelShade = 2, kKernelShadow = 3;
 // Optional CUDA-event timing of launches by kind: events[2k], events[2k+1] bracket the k-th

@@ -58,17 +58,19 @@ __global__ void __launch_bounds__(128) wfmTrace(MultiTables M, RayQueue Q, HitQu
 {
     const uint32_t n = *Q.count;
     uint32_t rays = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    {
-        float4 o = Q.o[i], d = Q.d[i];
-        const SceneView& S = M.views[M.req[__float_as_uint(o.w)]];
-        Hit h;
-        bool found = traceClosest<false>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000),
-                                         h, nullptr);
-        rays++;
-        H.a[i] = mk4(h.t, h.b1, h.b2, __uint_as_float(h.instance));
-        H.b[i] = found ? (h.prim | (h.front ? 0x80000000u : 0u)) : 0xffffffffu;
-    }
+    TraversalCount tc{0, 0};
+    traceGrid<false>(
+        n,
+        [&](TraceState& t, uint32_t i) {
+            const float4 o = Q.o[i], d = Q.d[i];
+            const SceneView& S = M.views[M.req[__float_as_uint(o.w)]];
+            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000));
+        },
+        [&](const TraceState& t, uint32_t i) {
+            H.a[i] = mk4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.instance));
+            H.b[i] = t.found ? (t.h.prim | (t.h.front ? 0x80000000u : 0u)) : 0xffffffffu;
+        },
+        tc, rays);
     countRays(rayCtr, rays);
 }
 
@@ -160,17 +162,23 @@ __global__ void __launch_bounds__(128) wfmShadow(MultiTables M, WaveState W, Sha
 {
     const uint32_t n = *SQ.count;
     uint32_t rays = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    {
-        float4 o = SQ.o[i], d = SQ.d[i];
-        uint2 tg = SQ.target[i];
-        uint32_t s = __float_as_uint(o.w);
-        const SceneView& S = M.views[M.req[s]];
-        Hit h;
-        bool any = traceClosest<false>(S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, h, nullptr);
-        rays++;
-        if (shadowVisible(any, h, tg.x, tg.y)) W.tot[s] = W.tot[s] + SQ.contrib[i];
-    }
+    TraversalCount tc{0, 0};
+    traceGrid<false>(
+        n,
+        [&](TraceState& t, uint32_t i) {
+            const float4 o = SQ.o[i], d = SQ.d[i];
+            const SceneView& S = M.views[M.req[__float_as_uint(o.w)]];
+            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w);
+        },
+        [&](const TraceState& t, uint32_t i) {
+            const uint2 tg = SQ.target[i];
+            if (shadowVisible(t.found, t.h, tg.x, tg.y))
+            {
+                const uint32_t s = __float_as_uint(SQ.o[i].w);
+                W.tot[s] = W.tot[s] + SQ.contrib[i];
+            }
+        },
+        tc, rays);
     countRays(rayCtr, rays);
 }
 

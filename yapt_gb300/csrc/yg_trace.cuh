@@ -1,14 +1,22 @@
 // Closest-hit ray traversal of the device BVH (replaces DXR TraceRay / RayQuery,
 // rayGenPrimaryRays.hlsl:62 and rayHitDefault.hlsl:83-133).
 //
-// Node format (64 B, four float4, loaded with 128-bit read-only loads):
-//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   n3 = (child0, child1, count0, count1) as int: count > 0 -> leaf of `count`
-//        triangles starting at triangle `child`; count == 0 -> inner node `child`;
-//        child < 0 -> empty slot.
+// Wide node (80 B, five float4 read with 128-bit read-only loads; built by yg_bvh_build.cu):
+//   n0 = (p.x, p.y, p.z, e.x | e.y << 8 | e.z << 16 | imask << 24)
+//   n1 = (child base, triangle base, meta[0..3], meta[4..7])        (uint32 / uint8 lanes)
+//   n2 = (qlo.x[0..3], qlo.x[4..7], qlo.y[0..3], qlo.y[4..7])
+//   n3 = (qlo.z[0..3], qlo.z[4..7], qhi.x[0..3], qhi.x[4..7])
+//   n4 = (qhi.y[0..3], qhi.y[4..7], qhi.z[0..3], qhi.z[4..7])
+// Child slot i spans p + 2^(e-127) * [qlo[i], qhi[i]] per axis (conservative: the builder
+// rounds outward and pads one quantum). imask bit i: slot i is an inner node, stored at
+// child base + (inner slots below i). Otherwise meta[i] = count << 5 | offset: a leaf of
+// `count` triangles at triangle base + offset; meta[i] == 0: empty slot.
 // Triangles (48 B): (v0.xyz, instance) (e1.xyz, primitive) (e2.xyz, 0), world space.
+//
+// Traversal keeps one group of unvisited inner children (child base, inner mask, hit mask
+// in near-to-far key order) and a stack of such groups. Children sit in slots by octant, so
+// visiting keys in increasing order, slot = key XOR (ray direction sign bits), goes roughly
+// near to far. The triangles of a node's leaf slots are tested when the node is opened.
 //
 // Intersection is Moller-Trumbore with a fixed operation order; hits count when
 // tmin < t < tmax. Equal-t hits resolve to the smaller (instance, primitive) so
@@ -30,8 +38,6 @@ struct Hit
     uint32_t prim;
     bool front;
 };
-
-constexpr int kTraversalStack = 64;
 
 YG_HD bool keyLess(uint32_t ia, uint32_t pa, uint32_t ib, uint32_t pb)
 {
@@ -77,76 +83,178 @@ struct TraversalCount
     uint32_t nodes, tris;
 };
 
+constexpr int kTraversalStack = 32;    // one group per wide level (the builder caps the depth)
+constexpr uint32_t kMaxNodeVisits = 1u << 20; // a guard only: a valid tree never reaches it
+
+// Byte i of the 8-byte lane pair (lo4, hi4) as the float 2^23 + byte: the byte is placed
+// in the low mantissa bits of 2^23 by one PRMT. The 2^23 bias is folded into the plane
+// offset of the node (see traceStep).
+__device__ __forceinline__ float biasedByte(uint32_t lo4, uint32_t hi4, int i)
+{
+    const uint32_t sel = (uint32_t)(i & 3) | 0x7650u; // byte i, then bytes 1..3 of 0x4B000000
+    return __uint_as_float(__byte_perm(i < 4 ? lo4 : hi4, 0x4B000000u, sel));
+}
+
+// One ray's traversal, advanced one node at a time by traceStep so that a persistent
+// kernel can hand a lane a new ray as soon as its ray is done.
+struct TraceState
+{
+    const float4* nodes;
+    const float4* tris;
+    float3 o, d, inv;
+    float tmin;
+    uint32_t oct;
+    Hit h;
+    bool found;
+    uint32_t gBase, gImask, gHits, visits;
+    int sp;
+};
+// the groups waiting below the current one (kept apart from TraceState so that the state's
+// scalars stay in registers)
+struct TraceStack
+{
+    uint2 e[kTraversalStack];
+};
+
+__device__ __forceinline__ void traceBegin(TraceState& t, const SceneView& S, float3 o, float3 d, float tmin, float tmax)
+{
+    t.nodes = S.nodes;
+    t.tris = S.tris;
+    t.o = o;
+    t.d = d;
+    t.inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    t.tmin = tmin;
+    t.oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+    t.h.t = tmax;
+    t.found = false;
+    // the root as the only inner child of a virtual parent
+    t.gBase = 0;
+    t.gImask = 1u;
+    t.gHits = 1u << t.oct;
+    t.visits = 0;
+    t.sp = 0;
+}
+
+// Opens the next node (testing its eight child boxes and the triangles of the leaf slots
+// that are hit); returns false once nothing is left to visit.
+template <bool COUNT>
+__device__ __forceinline__ bool traceStep(TraceState& t, TraceStack& st, TraversalCount* tc)
+{
+    if (t.gHits == 0)
+    {
+        if (t.sp == 0) return false;
+        const uint2 e = st.e[--t.sp];
+        t.gBase = e.x;
+        t.gHits = e.y & 0xffu;
+        t.gImask = e.y >> 8;
+    }
+    const uint32_t slot = (uint32_t)(__ffs(t.gHits) - 1) ^ t.oct;
+    t.gHits &= t.gHits - 1;
+    const uint32_t idx = t.gBase + __popc(t.gImask & ((1u << slot) - 1u));
+    if (++t.visits > kMaxNodeVisits) return false;
+    const float4* __restrict__ np = t.nodes + 5 * (size_t)idx;
+    const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+    if (COUNT) tc->nodes++;
+    const uint32_t packed = __float_as_uint(n0.w);
+    const uint32_t imask = packed >> 24;
+    const float3 inv = t.inv, o = t.o;
+    // per axis: t(q) = q * (scale / d) + (p - o) / d, evaluated as (2^23 + q) * sx + b' with
+    // b' = (p - o) / d - 2^23 * sx. Rounding b' errs by at most half a quantum (|sx| / 2),
+    // within the quantum of outward padding every child box carries.
+    const float sx = __uint_as_float((packed & 0xffu) << 23) * inv.x;
+    const float sy = __uint_as_float(((packed >> 8) & 0xffu) << 23) * inv.y;
+    const float sz = __uint_as_float(((packed >> 16) & 0xffu) << 23) * inv.z;
+    const float bx = fmaf(-8388608.0f, sx, (n0.x - o.x) * inv.x);
+    const float by = fmaf(-8388608.0f, sy, (n0.y - o.y) * inv.y);
+    const float bz = fmaf(-8388608.0f, sz, (n0.z - o.z) * inv.z);
+    const uint32_t m0 = __float_as_uint(n1.z), m1 = __float_as_uint(n1.w);
+    // near and far planes per axis chosen once by the sign of the direction
+    const uint32_t lx0 = __float_as_uint(n2.x), lx1 = __float_as_uint(n2.y);
+    const uint32_t ly0 = __float_as_uint(n2.z), ly1 = __float_as_uint(n2.w);
+    const uint32_t lz0 = __float_as_uint(n3.x), lz1 = __float_as_uint(n3.y);
+    const uint32_t hx0 = __float_as_uint(n3.z), hx1 = __float_as_uint(n3.w);
+    const uint32_t hy0 = __float_as_uint(n4.x), hy1 = __float_as_uint(n4.y);
+    const uint32_t hz0 = __float_as_uint(n4.z), hz1 = __float_as_uint(n4.w);
+    const uint32_t oct = t.oct;
+    const bool nx = oct & 1u, ny = oct & 2u, nz = oct & 4u;
+    const uint32_t nx0 = nx ? hx0 : lx0, nx1 = nx ? hx1 : lx1, fx0 = nx ? lx0 : hx0, fx1 = nx ? lx1 : hx1;
+    const uint32_t ny0 = ny ? hy0 : ly0, ny1 = ny ? hy1 : ly1, fy0 = ny ? ly0 : hy0, fy1 = ny ? ly1 : hy1;
+    const uint32_t nz0 = nz ? hz0 : lz0, nz1 = nz ? hz1 : lz1, fz0 = nz ? lz0 : hz0, fz1 = nz ? lz1 : hz1;
+    const float tmin = t.tmin, tfar = t.h.t;
+    uint32_t hits = 0, triHits = 0;
+    // all eight slots unrolled (a loop over the occupied slots only, with runtime byte
+    // selects, measured slower)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+    {
+        const uint32_t meta = ((i < 4 ? m0 : m1) >> (8 * (i & 3))) & 0xffu;
+        if (meta == 0) continue;
+        const float tnx = fmaf(biasedByte(nx0, nx1, i), sx, bx), tfx = fmaf(biasedByte(fx0, fx1, i), sx, bx);
+        const float tny = fmaf(biasedByte(ny0, ny1, i), sy, by), tfy = fmaf(biasedByte(fy0, fy1, i), sy, by);
+        const float tnz = fmaf(biasedByte(nz0, nz1, i), sz, bz), tfz = fmaf(biasedByte(fz0, fz1, i), sz, bz);
+        // NaN terms (a zero direction component) drop out of fmaxf/fminf: that axis does not cull
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+        // tfar widened by 4 ulp so grazing hits on box faces are kept
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tfar)) * 1.0000005f;
+        if (!(tn <= tf)) continue;
+        if (imask & (1u << i)) hits |= 1u << i;
+        else triHits |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+    }
+    // slot order -> key order: key = slot XOR oct swaps bits, bit pairs and nibbles
+    if (oct & 1u) hits = ((hits & 0x55u) << 1) | ((hits & 0xAAu) >> 1);
+    if (oct & 2u) hits = ((hits & 0x33u) << 2) | ((hits & 0xCCu) >> 2);
+    if (oct & 4u) hits = ((hits & 0x0Fu) << 4) | ((hits & 0xF0u) >> 4);
+    if (triHits)
+    {
+        const uint32_t triBase = __float_as_uint(n1.y);
+        if (COUNT) tc->tris += __popc(triHits);
+        while (triHits)
+        {
+            const uint32_t j = __ffs(triHits) - 1;
+            triHits &= triHits - 1;
+            intersectTri(t.tris, (int)(triBase + j), t.o, t.d, t.tmin, t.h, t.found);
+        }
+    }
+    if (hits)
+    {
+        // descend; the rest of the current group waits on the stack (one entry per
+        // level, and the builder keeps the tree within kTraversalStack levels)
+        if (t.gHits && t.sp < kTraversalStack) st.e[t.sp++] = make_uint2(t.gBase, t.gHits | (t.gImask << 8));
+        t.gBase = __float_as_uint(n1.x);
+        t.gImask = imask;
+        t.gHits = hits;
+    }
+    return t.gHits != 0 || t.sp != 0;
+}
+
 // Returns true if something was hit in (tmin, tmax); h.t starts at tmax.
 template <bool COUNT>
 __device__ __noinline__ bool traceClosest(const SceneView& S, float3 o, float3 d, float tmin, float tmax, Hit& h,
                                           TraversalCount* tc)
 {
-    h.t = tmax;
-    bool found = false;
-    float3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
-    float3 oi = mk3(o.x * inv.x, o.y * inv.y, o.z * inv.z);
-    int stack[kTraversalStack];
-    int sp = 0;
-    int node = 0;
-    const float4* __restrict__ nodes = S.nodes;
-    const float4* __restrict__ tris = S.tris;
-    while (true)
+    TraceState t;
+    TraceStack st;
+    traceBegin(t, S, o, d, tmin, tmax);
+    while (traceStep<COUNT>(t, st, tc)) {}
+    h = t.h;
+    return t.found;
+}
+
+// Traverses rays 0..n-1 of a queue, one ray per thread to completion (grid-stride). Fetching
+// a new ray whenever a lane finishes (persistent threads with a shared queue cursor)
+// measured slower on this kernel: the per-step bookkeeping costs more than the idle lanes.
+template <bool COUNT, typename Begin, typename End>
+__device__ __forceinline__ void traceGrid(uint32_t n, Begin begin, End end, TraversalCount& tc, uint32_t& rays)
+{
+    TraceState t;
+    TraceStack st;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
-        float4 n0 = __ldg(nodes + 4 * node);
-        float4 n1 = __ldg(nodes + 4 * node + 1);
-        float4 n2 = __ldg(nodes + 4 * node + 2);
-        float4 n3 = __ldg(nodes + 4 * node + 3);
-        if (COUNT) tc->nodes++;
-        // slab tests; tfar widened by 4 ulp so grazing hits on box faces are kept
-        float c0lx = fmaf(n0.x, inv.x, -oi.x), c0hx = fmaf(n0.y, inv.x, -oi.x);
-        float c0ly = fmaf(n0.z, inv.y, -oi.y), c0hy = fmaf(n0.w, inv.y, -oi.y);
-        float c0lz = fmaf(n2.x, inv.z, -oi.z), c0hz = fmaf(n2.y, inv.z, -oi.z);
-        float c1lx = fmaf(n1.x, inv.x, -oi.x), c1hx = fmaf(n1.y, inv.x, -oi.x);
-        float c1ly = fmaf(n1.z, inv.y, -oi.y), c1hy = fmaf(n1.w, inv.y, -oi.y);
-        float c1lz = fmaf(n2.z, inv.z, -oi.z), c1hz = fmaf(n2.w, inv.z, -oi.z);
-        float tn0 = fmaxf(fmaxf(fminf(c0lx, c0hx), fminf(c0ly, c0hy)), fmaxf(fminf(c0lz, c0hz), tmin));
-        float tf0 = fminf(fminf(fmaxf(c0lx, c0hx), fmaxf(c0ly, c0hy)), fminf(fmaxf(c0lz, c0hz), h.t)) * 1.0000005f;
-        float tn1 = fmaxf(fmaxf(fminf(c1lx, c1hx), fminf(c1ly, c1hy)), fmaxf(fminf(c1lz, c1hz), tmin));
-        float tf1 = fminf(fminf(fmaxf(c1lx, c1hx), fmaxf(c1ly, c1hy)), fminf(fmaxf(c1lz, c1hz), h.t)) * 1.0000005f;
-        int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
-        int cnt0 = __float_as_int(n3.z), cnt1 = __float_as_int(n3.w);
-        bool hit0 = ch0 >= 0 && tn0 <= tf0;
-        bool hit1 = ch1 >= 0 && tn1 <= tf1;
-        if (hit0 && cnt0 > 0)
-        {
-            for (int i = 0; i < cnt0; ++i) intersectTri(tris, ch0 + i, o, d, tmin, h, found);
-            if (COUNT) tc->tris += cnt0;
-            hit0 = false;
-        }
-        if (hit1 && cnt1 > 0)
-        {
-            for (int i = 0; i < cnt1; ++i) intersectTri(tris, ch1 + i, o, d, tmin, h, found);
-            if (COUNT) tc->tris += cnt1;
-            hit1 = false;
-        }
-        if (hit0 && hit1)
-        {
-            int nearN = tn0 <= tn1 ? ch0 : ch1;
-            int farN = tn0 <= tn1 ? ch1 : ch0;
-            if (sp < kTraversalStack) stack[sp++] = farN;
-            node = nearN;
-        }
-        else if (hit0)
-        {
-            node = ch0;
-        }
-        else if (hit1)
-        {
-            node = ch1;
-        }
-        else
-        {
-            if (sp == 0) break;
-            node = stack[--sp];
-        }
+        begin(t, i);
+        while (traceStep<COUNT>(t, st, &tc)) {}
+        end(t, i);
+        ++rays;
     }
-    return found;
 }
 
 } // namespace yg
