@@ -12,15 +12,17 @@
 // so the reference's header/vertex counters, linked lists and sort pass are not needed.
 // The light paths that produced vertices are compacted in index order, which makes the
 // random light-path pick of a camera group deterministic (the reference orders them by
-// atomic arrival). A camera group is one CUDA block of 64 threads over 64 pixels of a fixed
-// pixel permutation, and stages its light path in shared memory once, with every light
-// vertex's spectral surface and forward shading frame already set up: the group shares the
-// hero wavelength of its light path, so those do not depend on the pixel. Light-tracing
+// atomic arrival). A camera group is 64 consecutive entries of a fixed pixel permutation and
+// connects to one light path; the camera side runs as a wavefront (trace, shade with one
+// connection record per light vertex, visibility, in-order accumulation), with every light
+// vertex's spectral surface and forward shading frame set up once per wave: the group shares
+// the hero wavelength of its light path, so those do not depend on the pixel. Light-tracing
 // splats are summed in 64-bit fixed point, so the film does not depend on atomic order.
 #include <algorithm>
 
 #include "yg_path.cuh"
 #include "yg_kernels.h"
+#include "yg_wave.cuh"
 
 namespace yg
 {
@@ -657,150 +659,316 @@ YG_DEV float misWeight(const SceneView& S, uint32_t camIndex, const CamVertex& c
     return 1.0f / (1.0f + riCam + riLight);
 }
 
-// traceCameraRays (BDPTTraceCameraPath.comp:40-432): one block per camera group of 64
-// permuted pixels sharing one light subpath
-__global__ void __launch_bounds__(kGroupSize) bdptCamera(const SceneView S, const LaunchParams P, BdptParams B)
+// ------------------------------------------------------------------ camera subpaths as a wavefront
+// traceCameraRays (BDPTTraceCameraPath.comp:40-432) split into stages over a wave of camera
+// paths, one bounce at a time: trace the camera rays; shade each vertex (emitter or
+// environment term, or one connection record per light vertex with its contribution and
+// visibility ray, then the scattered continuation); trace the visibility rays; add each
+// path's visible connections in light-vertex order. The sums are formed in the same order as
+// the one-thread-per-path loop of the reference (vertex by vertex, light vertex by light
+// vertex), so a sample does not depend on the staging.
+//
+// A camera group is 64 consecutive entries of the pixel permutation; its light path is
+// picked per (sample index, group) as in the reference. The light vertices' spectral surfaces
+// and forward frames are prepared once per wave in global memory (they depend only on the
+// light path and its hero wavelength, which the group shares).
+struct BdptWave
 {
-    __shared__ SharedNode nodes[kBdptMaxLightVertices];
-    __shared__ uint32_t sCount, sPath;
-    __shared__ float sHero;
-    const Luts Lt = bdptLuts(S);
-    const uint32_t f = blockIdx.y, g = blockIdx.x;
-    const uint64_t cropPix = (uint64_t)P.cropW * P.cropH;
-    const uint64_t slot = (uint64_t)g * kGroupSize + threadIdx.x;
-    const bool active = slot < cropPix;
-    const uint32_t pix = active ? B.perm[slot] : 0u;
-    const uint32_t px = P.cropX + pix % P.cropW, py = P.cropY + pix / P.cropW;
-    const uint32_t* point = S.sobol + (size_t)f * kSobolDims;
-    const uint32_t seed = (py * P.width + px) ^ (P.seed * 0x9E3779B9u);
-    RandomSampler rs{point, B.camDimOffset + 2u, seed};
-    float2 lensR = rs.r2();
-    if (threadIdx.x == 0)
+    uint64_t c0;         // first camera path (frame * cropPixels + permutation slot) of the wave
+    uint32_t n;          // paths in the wave
+    uint32_t fBase;      // first frame the wave touches (prepared nodes start there)
+    uint32_t capacity;
+    SharedNode* prep;    // [(frame - fBase) * lightPaths + path] * maxLightVerts + vertex
+    float4* thr;         // path throughput
+    float4* tot;         // camera-path radiance so far
+    float4* cv0;         // previous vertex position, pdf ratio sum
+    float4* cv1;         // previous vertex normal, its forward area pdf
+    float4* cv2;         // deferred ratio sum, forward pdf of the current ray, hero wavelength
+    uint4* misc;         // flags | volumes << 16, sampler dimension, sampler seed, frame
+    uint4* misc2;        // permutation slot pixel, light path, light vertex count
+    uint2* conn;         // this bounce's connection records: first, count
+    float4* volIOR;
+    uint4* volMat;
+    float4* volAbs;      // [k * capacity + slot]
+    float4* fhAlb;
+    float4* fhNrm;
+    ShadowQueue C;       // connection records (o.w = path slot, d.w = tmax, < 0: no ray)
+    uint8_t* vis;        // visibility of each record
+    uint32_t* connCount;
+};
+
+constexpr uint32_t kNoLightPath = 0xffffffffu;
+
+__device__ __forceinline__ void wbLoadVolumes(const BdptWave& W, uint32_t s, PathState& st)
+{
+    if (!st.nVol) return;
+    float4 vi = W.volIOR[s];
+    uint4 vm = W.volMat[s];
+    st.volIOR[0] = vi.x, st.volIOR[1] = vi.y, st.volIOR[2] = vi.z, st.volIOR[3] = vi.w;
+    st.volMat[0] = vm.x, st.volMat[1] = vm.y, st.volMat[2] = vm.z, st.volMat[3] = vm.w;
+    for (int k = 0; k < kMaxVolumes; ++k) st.volAbs[k] = W.volAbs[(size_t)k * W.capacity + s];
+}
+__device__ __forceinline__ void wbStoreVolumes(const BdptWave& W, uint32_t s, const PathState& st)
+{
+    W.volIOR[s] = mk4(st.volIOR[0], st.volIOR[1], st.volIOR[2], st.volIOR[3]);
+    W.volMat[s] = make_uint4(st.volMat[0], st.volMat[1], st.volMat[2], st.volMat[3]);
+    for (int k = 0; k < kMaxVolumes; ++k) W.volAbs[(size_t)k * W.capacity + s] = st.volAbs[k];
+}
+
+// consecutive records for every lane of the warp: n per lane, one atomic per warp
+__device__ __forceinline__ uint32_t warpReserve(uint32_t* counter, uint32_t n)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t inc = n;
+    for (int o = 1; o < 32; o <<= 1)
     {
-        uint32_t hc = B.validCount[f];
+        uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += u;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + inc - n;
+}
+
+// the light vertices of every light path the wave's frames can pick
+__global__ void __launch_bounds__(128) wbPrepare(const SceneView S, const LaunchParams P, BdptParams B, BdptWave W,
+                                                uint32_t frames)
+{
+    const uint64_t total = (uint64_t)frames * B.lightPaths * B.maxLightVerts;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t k = (uint32_t)(i % B.maxLightVerts);
+        const uint64_t fl = i / B.maxLightVerts;
+        const uint32_t l = (uint32_t)(fl % B.lightPaths), fi = (uint32_t)(fl / B.lightPaths);
+        const uint32_t f = W.fBase + fi;
+        const size_t pl = (size_t)f * B.lightPaths + l;
+        if (k >= B.counts[pl]) continue;
+        Spectral sp;
+        spectralOf(S, B.heroes[pl], sp);
+        const LightNode* src = B.nodes + pl * B.maxLightVerts;
+        prepareSharedNode(S, P, sp, src[k], k ? src[k - 1].pos : src[0].pos, k, W.prep[i]);
+    }
+}
+
+__global__ void __launch_bounds__(128) wbGenerate(const SceneView S, const LaunchParams P, BdptParams B, BdptWave W, RayQueue Q)
+{
+    const uint64_t cropPix = (uint64_t)P.cropW * P.cropH;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < W.n; s += gridDim.x * blockDim.x)
+    {
+        const uint64_t c = W.c0 + s;
+        const uint32_t f = (uint32_t)(c / cropPix);
+        const uint32_t slotInFrame = (uint32_t)(c % cropPix);
+        const uint32_t pix = B.perm[slotInFrame];
+        const uint32_t px = P.cropX + pix % P.cropW, py = P.cropY + pix / P.cropW;
+        const uint32_t* point = S.sobol + (size_t)f * kSobolDims;
+        const uint32_t seed = (py * P.width + px) ^ (P.seed * 0x9E3779B9u);
+        RandomSampler rs{point, B.camDimOffset + 2u, seed};
+        const float2 lensR = rs.r2();
+        const uint32_t g = slotInFrame / kGroupSize, j = slotInFrame % kGroupSize;
+        const uint32_t hc = B.validCount[f];
+        uint32_t path = kNoLightPath, count = 0;
+        float hero;
         if (hc == 0)
         {
-            sCount = 0;
-            sPath = 0;
-            sHero = S.lambdaMin + rs.r1() * (S.lambdaMax - S.lambdaMin);
+            // the group's first pixel draws the wavelength with its next dimension
+            const uint32_t pix0 = B.perm[(size_t)g * kGroupSize];
+            const uint32_t px0 = P.cropX + pix0 % P.cropW, py0 = P.cropY + pix0 / P.cropW;
+            RandomSampler r0{point, B.camDimOffset + 4u, (py0 * P.width + px0) ^ (P.seed * 0x9E3779B9u)};
+            hero = S.lambdaMin + r0.r1() * (S.lambdaMax - S.lambdaMin);
+            if (j == 0) rs.r1();
         }
         else
         {
             RandomSampler rt{point, 2u, g ^ (P.seed * 0x9E3779B9u)};
             uint32_t h = (uint32_t)fminf(floorf(rt.r1() * (float)hc), (float)(hc - 1u));
-            uint32_t l = B.valid[(size_t)f * B.lightPaths + h];
-            sPath = l;
-            sCount = B.counts[(size_t)f * B.lightPaths + l];
-            sHero = B.heroes[(size_t)f * B.lightPaths + l];
+            path = B.valid[(size_t)f * B.lightPaths + h];
+            count = B.counts[(size_t)f * B.lightPaths + path];
+            hero = B.heroes[(size_t)f * B.lightPaths + path];
         }
-    }
-    __syncthreads();
-    const uint32_t count = sCount;
-    Spectral sp;
-    spectralOf(S, sHero, sp);
-    if (threadIdx.x < count)
-    {
-        const LightNode* src = B.nodes + ((size_t)f * B.lightPaths + sPath) * B.maxLightVerts;
-        uint32_t k = threadIdx.x;
-        prepareSharedNode(S, P, sp, src[k], k ? src[k - 1].pos : src[0].pos, k, nodes[k]);
-    }
-    __syncthreads();
-    if (!active) return;
-
-    // generateCameraRay (raytraceCommonResources.hlsl:113-137) with the group's wavelength
-    float invW = 1.0f / (float)P.width, invH = 1.0f / (float)P.height;
-    float2 uv = make_float2((float)px * invW + 0.5f * invW, (float)py * invH + 0.5f * invH);
-    float2 texel = make_float2(sampleDim(point, 0, seed), sampleDim(point, 1, seed));
-    float2 to = make_float2(0.f, 0.f);
-    if ((P.flags & 2u) == 0) to = make_float2(texel.x - 0.5f, texel.y - 0.5f);
-    to = make_float2(to.x * invW, to.y * invH);
-    float4 pn = mul44(S.cam.uvToView, mk4(uv.x + to.x, uv.y + to.y, 0.0f, 1.0f));
-    pn = pn / pn.w;
-    float3 pin = mk3(pn.x, pn.y, pn.z);
-    float3 focusP = pin * safeDiv(S.cam.focusDistance, fabsf(pin.z));
-    float2 disk = sampleConcentricDisk(lensR);
-    float3 lensP = mk3(disk.x * S.cam.apertureRadius, disk.y * S.cam.apertureRadius, 0.0f);
-    float4 ow = mul44(S.cam.viewToWorld, mk4(lensP.x, lensP.y, lensP.z, 1.0f));
-    float4 dw = mul44(S.cam.viewToWorld, mk4(focusP.x - lensP.x, focusP.y - lensP.y, focusP.z - lensP.z, 0.0f));
-    float3 rayOrigin = mk3(ow.x, ow.y, ow.z);
-    float3 rayDir = normalize(mk3(dw.x, dw.y, dw.z));
-
-    float4 total = splat4(0.0f);
-    FirstHit fh;
-    fh.albedo = mk3(0.f, 0.f, 0.f);
-    fh.normal = mk3(0.f, 0.f, 0.f);
-    fh.depth = 0.0f;
-    PathState st;
-    initState(st);
-    CamVertex cv;
-    cv.pdfRatioSum = 0.0f;
-    cv.prevPdfFwd = 0.0f;
-    cv.prevPos = mk3(0.f, 0.f, 0.f);
-    cv.prevNormal = mk3(0.f, 0.f, 0.f);
-    float pdfFwdCam = cameraDirectionalPdf(S, P, rayDir);
-    float deferredRI = 0.0f;
-    for (uint32_t ci = 0; ci < P.maxDepth; ++ci)
-    {
-        Hit hit;
-        bool found = traceClosest<false>(S, rayOrigin, rayDir, kRayMinT, __int_as_float(0x7f800000), hit, nullptr);
-        float4 rv = rs.r4();
-        if (!found)
+        // generateCameraRay (raytraceCommonResources.hlsl:113-137) with the group's wavelength
+        float invW = 1.0f / (float)P.width, invH = 1.0f / (float)P.height;
+        float2 uv = make_float2((float)px * invW + 0.5f * invW, (float)py * invH + 0.5f * invH);
+        float2 texel = make_float2(sampleDim(point, 0, seed), sampleDim(point, 1, seed));
+        float2 to = make_float2(0.f, 0.f);
+        if ((P.flags & 2u) == 0) to = make_float2(texel.x - 0.5f, texel.y - 0.5f);
+        to = make_float2(to.x * invW, to.y * invH);
+        float4 pn = mul44(S.cam.uvToView, mk4(uv.x + to.x, uv.y + to.y, 0.0f, 1.0f));
+        pn = pn / pn.w;
+        float3 pin = mk3(pn.x, pn.y, pn.z);
+        float3 focusP = pin * safeDiv(S.cam.focusDistance, fabsf(pin.z));
+        float2 disk = sampleConcentricDisk(lensR);
+        float3 lensP = mk3(disk.x * S.cam.apertureRadius, disk.y * S.cam.apertureRadius, 0.0f);
+        float4 ow = mul44(S.cam.viewToWorld, mk4(lensP.x, lensP.y, lensP.z, 1.0f));
+        float4 dw = mul44(S.cam.viewToWorld, mk4(focusP.x - lensP.x, focusP.y - lensP.y, focusP.z - lensP.z, 0.0f));
+        float3 rayOrigin = mk3(ow.x, ow.y, ow.z);
+        float3 rayDir = normalize(mk3(dw.x, dw.y, dw.z));
+        W.thr[s] = splat4(1.0f);
+        W.tot[s] = splat4(0.0f);
+        W.cv0[s] = splat4(0.0f);
+        W.cv1[s] = splat4(0.0f);
+        W.cv2[s] = mk4(0.0f, cameraDirectionalPdf(S, P, rayDir), hero, 0.0f);
+        W.misc[s] = make_uint4(0u, rs.dim, rs.seed, f);
+        W.misc2[s] = make_uint4(pix, path, count, 0u);
+        if (P.featAlbedo)
         {
-            // calculateMISWeightOnCameraPathMissing (BDPTCommon.hlsl:1039-1059)
-            cv.curPdfFwd = pdfFwdCam;
-            float mis = 1.0f;
-            if (ci > 0)
-            {
-                float ri = accumulateRISum(cv.pdfRatioSum, pdfEnvPosition(B) * fabsf(dot(cv.prevNormal, rayDir)), cv.prevPdfFwd);
-                ri = accumulateRISum(ri, envSelectionPdf(S) * pdfEnvDirection(-rayDir), cv.curPdfFwd);
-                mis = 1.0f / (1.0f + ri);
-            }
-            total = total + st.throughput * skyRadiance(S, P, sp, rayDir) * mis;
-            break;
+            W.fhAlb[s] = splat4(0.0f);
+            W.fhNrm[s] = splat4(0.0f);
         }
-        const GpuInstance& I = S.instances[hit.instance];
-        if (P.regularizeEnable && ci >= P.regularizeAfter) st.flags |= kFlagRegularize;
+        Q.o[s] = mk4(rayOrigin.x, rayOrigin.y, rayOrigin.z, __uint_as_float(s));
+        Q.d[s] = mk4(rayDir.x, rayDir.y, rayDir.z, 0.0f);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = W.n;
+}
+
+__global__ void __launch_bounds__(128) wbTrace(const SceneView S, RayQueue Q, HitQueue H)
+{
+    TraversalCount tc{0, 0};
+    uint32_t rays = 0;
+    traceGrid<false>(
+        *Q.count,
+        [&](TraceState& t, uint32_t i) {
+            const float4 o = Q.o[i], d = Q.d[i];
+            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000));
+        },
+        [&](const TraceState& t, uint32_t i) {
+            H.a[i] = mk4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.instance));
+            H.b[i] = t.found ? (t.h.prim | (t.h.front ? 0x80000000u : 0u)) : 0xffffffffu;
+        },
+        tc, rays);
+}
+
+// one camera vertex per queued path (the body of the bounce loop of traceCameraRays)
+__global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchParams P, BdptParams B, BdptWave W,
+                                              RayQueue Qin, HitQueue H, RayQueue Qout, uint32_t ci)
+{
+    const Luts Lt = bdptLuts(S);
+    const uint32_t n = *Qin.count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        const uint32_t i = first + r * stride;
+        const bool active = i < n;
+        uint32_t s = 0, count = 0, path = kNoLightPath, f = 0;
+        bool connect = false, alive = false;
+        PathState st;
+        RandomSampler rs;
+        Spectral sp;
+        CamVertex cv;
+        float deferredRI = 0.0f, pdfFwdCam = 0.0f;
+        float3 rayOrigin = mk3(0.f, 0.f, 0.f), rayDir = mk3(0.f, 0.f, 1.f);
+        Hit hit;
         HitSurface hs;
         SurfaceCtx c;
-        vertexSurface(S, P, sp, hit, I, rayDir, st, hs, c);
-        const Surface& s = hs.s;
-        cv.pos = rayOrigin + rayDir * hit.t;
-        cv.normal = normalize(xformVectorT(I.w2o, s.geometryNormal));
-        const float3 wo = -hs.rayDirOS;
-        if (ci == 0)
+        const GpuInstance* I = nullptr;
+        bool delta = true;
+        float4 total = splat4(0.0f);
+        float4 rv = splat4(0.0f);
+        if (active)
         {
-            fh.albedo = hs.albedoRGB;
-            fh.normal = normalize(xformVectorT(I.w2o, s.baseLayerNormal));
-            float4 vp = mul44(S.cam.worldToView, mk4(cv.pos.x, cv.pos.y, cv.pos.z, 1.0f));
-            fh.depth = vp.z * S.cam.forwardZSign;
-        }
-        const bool delta = isDeltaDistribution(c.a2, s);
-        cv.curPdfFwd = pdfFwdCam < 0.0f ? -1.0f : pdfFwdCam * solidAngleToArea(cv.pos - rayOrigin, cv.normal);
-        float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
-        if (!allEqual4(ab, 0.0f)) st.throughput = st.throughput * transmittance(ab, hit.t);
-        if (!allEqual4(s.emissive, 0.0f))
-        {
-            // calculateMISWeightOnCameraPathHittingLight (BDPTCommon.hlsl:1008-1035)
-            float mis = 1.0f;
-            if (ci > 0)
+            const float4 qo = Qin.o[i], qd = Qin.d[i];
+            s = __float_as_uint(qo.w);
+            rayOrigin = mk3(qo.x, qo.y, qo.z);
+            rayDir = mk3(qd.x, qd.y, qd.z);
+            const uint4 m = W.misc[s], m2 = W.misc2[s];
+            f = m.w;
+            path = m2.y;
+            count = m2.z;
+            initState(st);
+            st.throughput = W.thr[s];
+            st.flags = m.x & 0xffffu;
+            st.nVol = m.x >> 16;
+            wbLoadVolumes(W, s, st);
+            rs = RandomSampler{S.sobol + (size_t)f * kSobolDims, m.y, m.z};
+            const float4 a = W.cv0[s], b = W.cv1[s], e = W.cv2[s];
+            cv.prevPos = mk3(a.x, a.y, a.z);
+            cv.pdfRatioSum = a.w;
+            cv.prevNormal = mk3(b.x, b.y, b.z);
+            cv.prevPdfFwd = b.w;
+            deferredRI = e.x;
+            pdfFwdCam = e.y;
+            spectralOf(S, e.z, sp);
+            total = W.tot[s];
+            const float4 ha = H.a[i];
+            const uint32_t hb = H.b[i];
+            const bool found = hb != 0xffffffffu;
+            hit.t = ha.x;
+            hit.b1 = ha.y;
+            hit.b2 = ha.z;
+            hit.instance = __float_as_uint(ha.w);
+            hit.prim = hb & 0x7fffffffu;
+            hit.front = (hb & 0x80000000u) != 0;
+            rv = rs.r4();
+            if (!found)
             {
-                float3 towards = cv.prevPos - cv.pos;
-                float pick, posPdf, dirPdf;
-                pdfForSamplingLight(S, hit.instance, hit.prim, cv.normal, normalize(towards), pick, posPdf, dirPdf);
-                float ri = accumulateRISum(cv.pdfRatioSum, dirPdf * solidAngleToArea(towards, cv.prevNormal), cv.prevPdfFwd);
-                ri = accumulateRISum(ri, pick * posPdf, cv.curPdfFwd);
-                mis = 1.0f / (1.0f + ri);
+                // calculateMISWeightOnCameraPathMissing (BDPTCommon.hlsl:1039-1059)
+                cv.curPdfFwd = pdfFwdCam;
+                float mis = 1.0f;
+                if (ci > 0)
+                {
+                    float ri = accumulateRISum(cv.pdfRatioSum, pdfEnvPosition(B) * fabsf(dot(cv.prevNormal, rayDir)), cv.prevPdfFwd);
+                    ri = accumulateRISum(ri, envSelectionPdf(S) * pdfEnvDirection(-rayDir), cv.curPdfFwd);
+                    mis = 1.0f / (1.0f + ri);
+                }
+                total = total + st.throughput * skyRadiance(S, P, sp, rayDir) * mis;
             }
-            if (isTwoSided(s.flags) || dot(s.geometryNormal, wo) > 0.0f)
+            else
             {
-                float profile = evaluateEmissionProfile(dot(cv.normal, -rayDir), s.emissionFocus);
-                total = total + st.throughput * s.emissive * mis * profile;
+                I = &S.instances[hit.instance];
+                if (P.regularizeEnable && ci >= P.regularizeAfter) st.flags |= kFlagRegularize;
+                vertexSurface(S, P, sp, hit, *I, rayDir, st, hs, c);
+                const Surface& sf = hs.s;
+                cv.pos = rayOrigin + rayDir * hit.t;
+                cv.normal = normalize(xformVectorT(I->w2o, sf.geometryNormal));
+                if (ci == 0 && P.featAlbedo)
+                {
+                    float3 nn = normalize(xformVectorT(I->w2o, sf.baseLayerNormal));
+                    float4 vp = mul44(S.cam.worldToView, mk4(cv.pos.x, cv.pos.y, cv.pos.z, 1.0f));
+                    W.fhAlb[s] = mk4(hs.albedoRGB.x, hs.albedoRGB.y, hs.albedoRGB.z, 0.0f);
+                    W.fhNrm[s] = mk4(nn.x, nn.y, nn.z, vp.z * S.cam.forwardZSign);
+                }
+                delta = isDeltaDistribution(c.a2, sf);
+                cv.curPdfFwd = pdfFwdCam < 0.0f ? -1.0f : pdfFwdCam * solidAngleToArea(cv.pos - rayOrigin, cv.normal);
+                float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
+                if (!allEqual4(ab, 0.0f)) st.throughput = st.throughput * transmittance(ab, hit.t);
+                if (!allEqual4(sf.emissive, 0.0f))
+                {
+                    // calculateMISWeightOnCameraPathHittingLight (BDPTCommon.hlsl:1008-1035)
+                    float mis = 1.0f;
+                    if (ci > 0)
+                    {
+                        float3 towards = cv.prevPos - cv.pos;
+                        float pick, posPdf, dirPdf;
+                        pdfForSamplingLight(S, hit.instance, hit.prim, cv.normal, normalize(towards), pick, posPdf, dirPdf);
+                        float ri = accumulateRISum(cv.pdfRatioSum, dirPdf * solidAngleToArea(towards, cv.prevNormal), cv.prevPdfFwd);
+                        ri = accumulateRISum(ri, pick * posPdf, cv.curPdfFwd);
+                        mis = 1.0f / (1.0f + ri);
+                    }
+                    if (isTwoSided(sf.flags) || dot(sf.geometryNormal, -hs.rayDirOS) > 0.0f)
+                    {
+                        float profile = evaluateEmissionProfile(dot(cv.normal, -rayDir), sf.emissionFocus);
+                        total = total + st.throughput * sf.emissive * mis * profile;
+                    }
+                }
+                else
+                {
+                    connect = !delta && !allEqual4(st.throughput, 0.0f) && count > 0;
+                    alive = true;
+                }
             }
-            break;
+            if (!alive) W.tot[s] = total; // the path ends at this vertex
         }
-        if (!delta && !allEqual4(st.throughput, 0.0f))
+        // connection records: count per connecting path, consecutive per path
+        const uint32_t base = warpReserve(W.connCount, connect ? count : 0u);
+        if (active) W.conn[s] = make_uint2(base, connect ? count : 0u);
+        if (connect)
         {
-            // connect to every vertex of the group's light path (BDPTTraceCameraPath.comp:240-282)
+            const Surface& sf = hs.s;
+            const float3 wo = -hs.rayDirOS;
+            const SharedNode* nodes = W.prep + (((size_t)(f - W.fBase)) * B.lightPaths + path) * B.maxLightVerts;
             LightVertexCtx lv;
             lv.riSum = 0.0f;
             lv.originFlags = 0;
@@ -813,6 +981,9 @@ __global__ void __launch_bounds__(kGroupSize) bdptCamera(const SceneView S, cons
             {
                 const SharedNode& sn = nodes[li];
                 const LightNode& ln = sn.n;
+                const uint32_t e = base + li;
+                float4 ro = mk4(0.f, 0.f, 0.f, __uint_as_float(s)), rd = mk4(0.f, 0.f, 0.f, -1.0f), contrib = splat4(0.0f);
+                uint2 target = make_uint2(0u, 0u);
                 if (!(ln.flags & NF_DELTA))
                 {
                     // getLightNodeConnection + calculateLightPathRadiance (BDPTCommon.hlsl:622-635, 1062-1215)
@@ -830,10 +1001,10 @@ __global__ void __launch_bounds__(kGroupSize) bdptCamera(const SceneView S, cons
                         dist = length(toLight);
                         toLightDir = toLight / dist;
                     }
-                    const float3 wi = normalize(xformVector(I.w2o, toLightDir));
+                    const float3 wi = normalize(xformVector(I->w2o, toLightDir));
                     const bool lightTerminated = (ln.flags & NF_TERMINATED) != 0;
                     const bool terminatedBefore = camTerminated || lightTerminated;
-                    ScatterEval ce = evaluateBoth(Lt, sp, s, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, false, false);
+                    ScatterEval ce = evaluateBoth(Lt, sp, sf, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, false, false);
                     if ((ce.transmission & kTransDispersed) && !terminatedBefore) terminateSecondary(ce.weight);
                     if (ce.pdfFwd != 0.0f && !allEqual4(ce.weight, 0.0f))
                     {
@@ -842,28 +1013,28 @@ __global__ void __launch_bounds__(kGroupSize) bdptCamera(const SceneView S, cons
                         float fwdLight;
                         if (lightEndOfConnection(S, B, Lt, sp, sn, li, cv.pos, terminatedNow, le, fwdLight))
                         {
-                            float3 start = spawnRayOrigin(cv.pos, cv.normal, toLightDir);
-                            Hit vh;
-                            float tmax = atInfinity ? __int_as_float(0x7f800000) : kRayMinT + dist + kVisibilityEps;
-                            bool any = traceClosest<false>(S, start, toLightDir, kRayMinT, tmax, vh, nullptr);
-                            bool visible = atInfinity ? !any : (any && vh.instance == ln.instance && vh.prim == ln.prim);
-                            if (visible)
+                            float mis = misWeight(S, ci, cv, li, lv, ln, ce.pdfFwd, ce.pdfBwd, fwdLight, le.pdfBwd);
+                            float G = li > 0 ? 1.0f / (dist * dist) : 1.0f;
+                            float4 wc = ce.weight;
+                            if (!atInfinity)
                             {
-                                float mis = misWeight(S, ci, cv, li, lv, ln, ce.pdfFwd, ce.pdfBwd, fwdLight, le.pdfBwd);
-                                float G = li > 0 ? 1.0f / (dist * dist) : 1.0f;
-                                float4 wc = ce.weight;
-                                if (!atInfinity)
-                                {
-                                    float4 cab = absorptionAfter(st, ce.transmission, s, hs.material);
-                                    if (!allEqual4(cab, 0.0f)) wc = wc * transmittance(cab, dist);
-                                }
-                                float4 r = le.weight * wc * st.throughput * ln.radiance * G * mis;
-                                if (camTerminated && lightTerminated) r.x *= 0.25f; // undoSecondaryWavelengthRescale
-                                total = total + r;
+                                float4 cab = absorptionAfter(st, ce.transmission, sf, hs.material);
+                                if (!allEqual4(cab, 0.0f)) wc = wc * transmittance(cab, dist);
                             }
+                            contrib = le.weight * wc * st.throughput * ln.radiance * G * mis;
+                            if (camTerminated && lightTerminated) contrib.x *= 0.25f; // undoSecondaryWavelengthRescale
+                            const float3 start = spawnRayOrigin(cv.pos, cv.normal, toLightDir);
+                            ro = mk4(start.x, start.y, start.z, __uint_as_float(s));
+                            rd = mk4(toLightDir.x, toLightDir.y, toLightDir.z,
+                                     atInfinity ? __int_as_float(0x7f800000) : kRayMinT + dist + kVisibilityEps);
+                            target = atInfinity ? make_uint2(0xffffffffu, 0xffffffffu) : make_uint2(ln.instance, ln.prim);
                         }
                     }
                 }
+                W.C.o[e] = ro;
+                W.C.d[e] = rd;
+                W.C.target[e] = target;
+                W.C.contrib[e] = contrib;
                 lv.riSum = deferredLight;
                 deferredLight = accumulateRISum(deferredLight, ln.pdfBwd, ln.pdfFwd);
                 lv.prevNormal = ln.normal;
@@ -872,48 +1043,130 @@ __global__ void __launch_bounds__(kGroupSize) bdptCamera(const SceneView S, cons
                 if (li == 0) lv.originFlags = ln.flags;
             }
         }
-        bool isDiffuse, sDelta;
-        float3 wiS = sampleScatter(Lt, sp, s, c, rv, isDiffuse, sDelta);
-        if (isZero3(wiS)) break;
-        if (isDiffuse) st.flags |= kFlagRegularize;
-        ScatterEval ev = evaluateBoth(Lt, sp, s, c, currentIOR(st), previousIOR(st), wo, wiS, hit.front, false, sDelta);
-        bool dispersed = applyTransmission(st, ev.transmission, s, hs.material);
-        float4 w = ev.weight * safeDiv(1.0f, ev.pdfFwd);
-        if (dispersed) terminateSecondary(st.throughput);
-        if (russianRoulette(st.throughput, rs.r1())) break;
-        if (ci > 0)
+        bool cont = false;
+        if (alive)
         {
-            float bwdPrev = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - cv.pos, cv.prevNormal);
-            deferredRI = accumulateRISum(deferredRI, bwdPrev, cv.prevPdfFwd);
-            cv.pdfRatioSum = deferredRI;
+            // the scattered continuation (rv was drawn right after the trace)
+            const Surface& sf = hs.s;
+            const float3 wo = -hs.rayDirOS;
+            bool isDiffuse, sDelta;
+            float3 wiS = sampleScatter(Lt, sp, sf, c, rv, isDiffuse, sDelta);
+            if (!isZero3(wiS))
+            {
+                if (isDiffuse) st.flags |= kFlagRegularize;
+                ScatterEval ev = evaluateBoth(Lt, sp, sf, c, currentIOR(st), previousIOR(st), wo, wiS, hit.front, false, sDelta);
+                bool dispersed = applyTransmission(st, ev.transmission, sf, hs.material);
+                float4 w = ev.weight * safeDiv(1.0f, ev.pdfFwd);
+                if (dispersed) terminateSecondary(st.throughput);
+                if (!russianRoulette(st.throughput, rs.r1()))
+                {
+                    if (ci > 0)
+                    {
+                        float bwdPrev = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - cv.pos, cv.prevNormal);
+                        deferredRI = accumulateRISum(deferredRI, bwdPrev, cv.prevPdfFwd);
+                        cv.pdfRatioSum = deferredRI;
+                    }
+                    cv.prevNormal = cv.normal;
+                    cv.prevPos = cv.pos;
+                    cv.prevPdfFwd = cv.curPdfFwd;
+                    pdfFwdCam = sDelta ? -1.0f : ev.pdfFwd;
+                    st.throughput = st.throughput * w;
+                    rayDir = normalize(xformVectorT(I->w2o, wiS));
+                    rayOrigin = spawnRayOrigin(cv.pos, cv.normal, rayDir);
+                    cont = ci + 1 < P.maxDepth;
+                }
+            }
+            W.tot[s] = total;
+            if (cont)
+            {
+                W.thr[s] = st.throughput;
+                W.cv0[s] = mk4(cv.prevPos.x, cv.prevPos.y, cv.prevPos.z, cv.pdfRatioSum);
+                W.cv1[s] = mk4(cv.prevNormal.x, cv.prevNormal.y, cv.prevNormal.z, cv.prevPdfFwd);
+                W.cv2[s] = mk4(deferredRI, pdfFwdCam, sp.hero, 0.0f);
+                W.misc[s] = make_uint4(st.flags | (st.nVol << 16), rs.dim, rs.seed, f);
+                wbStoreVolumes(W, s, st);
+            }
         }
-        cv.prevNormal = cv.normal;
-        cv.prevPos = cv.pos;
-        cv.prevPdfFwd = cv.curPdfFwd;
-        pdfFwdCam = sDelta ? -1.0f : ev.pdfFwd;
-        st.throughput = st.throughput * w;
-        rayDir = normalize(xformVectorT(I.w2o, wiS));
-        rayOrigin = spawnRayOrigin(cv.pos, cv.normal, rayDir);
+        const uint32_t o = warpAppend(Qout.count, cont);
+        if (cont)
+        {
+            Qout.o[o] = mk4(rayOrigin.x, rayOrigin.y, rayOrigin.z, __uint_as_float(s));
+            Qout.d[o] = mk4(rayDir.x, rayDir.y, rayDir.z, 0.0f);
+        }
     }
-    const uint64_t idx = (uint64_t)f * cropPix + pix;
-    float3 X = toXYZ(S, sp, total);
-    P.sampleXYZ[idx] = mk4(X.x, X.y, X.z, 1.0f);
-    if (P.dump)
+}
+
+// visibility of the connection records (checkVisibility: the segment must reach the light
+// vertex's own triangle first; toward the environment nothing may be hit)
+__global__ void __launch_bounds__(128) wbVisibility(const SceneView S, BdptWave W)
+{
+    TraversalCount tc{0, 0};
+    uint32_t rays = 0;
+    const uint32_t n = *W.connCount;
+    TraceState t;
+    TraceStack st;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
     {
-        float* d = P.dump + idx * 8;
-        d[0] = sp.hero;
-        d[1] = total.x;
-        d[2] = total.y;
-        d[3] = total.z;
-        d[4] = total.w;
-        d[5] = X.x;
-        d[6] = X.y;
-        d[7] = X.z;
+        const float4 d = W.C.d[e];
+        if (d.w < 0.0f)
+        {
+            W.vis[e] = 0;
+            continue;
+        }
+        const float4 o = W.C.o[e];
+        traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w);
+        while (traceStep<false>(t, st, &tc)) {}
+        const uint2 tg = W.C.target[e];
+        W.vis[e] = tg.x == 0xffffffffu ? !t.found : shadowVisible(t.found, t.h, tg.x, tg.y);
+        ++rays;
     }
-    if (P.featAlbedo)
+}
+
+// adds each path's visible connections of this bounce, in light-vertex order
+__global__ void __launch_bounds__(256) wbAccumulate(BdptWave W, RayQueue Qin)
+{
+    const uint32_t n = *Qin.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
-        P.featAlbedo[idx] = mk4(fh.albedo.x, fh.albedo.y, fh.albedo.z, 0.0f);
-        P.featNormalDepth[idx] = mk4(fh.normal.x, fh.normal.y, fh.normal.z, fh.depth);
+        const uint32_t s = __float_as_uint(Qin.o[i].w);
+        const uint2 cr = W.conn[s];
+        if (cr.y == 0) continue;
+        float4 total = W.tot[s];
+        for (uint32_t j = 0; j < cr.y; ++j)
+            if (W.vis[cr.x + j]) total = total + W.C.contrib[cr.x + j];
+        W.tot[s] = total;
+    }
+}
+
+__global__ void __launch_bounds__(256) wbFinalize(const SceneView S, const LaunchParams P, BdptWave W)
+{
+    const uint64_t cropPix = (uint64_t)P.cropW * P.cropH;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < W.n; s += gridDim.x * blockDim.x)
+    {
+        const uint4 m = W.misc[s], m2 = W.misc2[s];
+        const uint64_t idx = (uint64_t)m.w * cropPix + m2.x;
+        Spectral sp;
+        spectralOf(S, W.cv2[s].z, sp);
+        const float4 total = W.tot[s];
+        float3 X = toXYZ(S, sp, total);
+        P.sampleXYZ[idx] = mk4(X.x, X.y, X.z, 1.0f);
+        if (P.dump)
+        {
+            float* d = P.dump + idx * 8;
+            d[0] = sp.hero;
+            d[1] = total.x;
+            d[2] = total.y;
+            d[3] = total.z;
+            d[4] = total.w;
+            d[5] = X.x;
+            d[6] = X.y;
+            d[7] = X.z;
+        }
+        if (P.featAlbedo)
+        {
+            P.featAlbedo[idx] = W.fhAlb[s];
+            P.featNormalDepth[idx] = W.fhNrm[s];
+        }
     }
 }
 
@@ -1045,12 +1298,37 @@ namespace
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 } // namespace
 
+constexpr uint32_t kBdptWave = 1u << 20; // camera paths per wave
+
+namespace
+{
+struct WaveShape
+{
+    uint32_t capacity;   // camera paths per wave
+    uint32_t spanFrames; // frames one wave can touch
+};
+WaveShape waveShape(uint32_t frames, uint64_t cropPixels)
+{
+    const uint64_t total = (uint64_t)frames * cropPixels;
+    WaveShape w;
+    w.capacity = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(total, kBdptWave));
+    w.spanFrames = (uint32_t)std::min<uint64_t>(frames, w.capacity / std::max<uint64_t>(cropPixels, 1) + 2);
+    return w;
+}
+size_t waveSlotBytes() { return 5 * 16 + 2 * 16 + 8 + 16 + 16 + 64 + 2 * 16 + 2 * 32 + 20; }
+} // namespace
+
 size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVerts, uint64_t cropPixels)
 {
     size_t b = align256((size_t)frames * lightPaths * maxLightVerts * sizeof(LightNode));
     b += 3 * align256((size_t)frames * lightPaths * 4);
     b += align256((size_t)frames * 4);
     b += align256((size_t)frames * cropPixels * 24);
+    const WaveShape w = waveShape(frames, cropPixels);
+    b += align256((size_t)w.spanFrames * lightPaths * maxLightVerts * sizeof(SharedNode));
+    b += (size_t)w.capacity * waveSlotBytes() + 32 * 256;
+    b += (size_t)w.capacity * maxLightVerts * (56 + 1) + 8 * 256;
+    b += 256;
     return b;
 }
 
@@ -1080,16 +1358,80 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
     B.valid = reinterpret_cast<uint32_t*>(take((size_t)B.frames * lightPaths * 4));
     B.validCount = reinterpret_cast<uint32_t*>(take((size_t)B.frames * 4));
     B.splat = reinterpret_cast<unsigned long long*>(take((size_t)B.frames * cropPix * 24));
+    // the camera wave
+    const WaveShape ws = waveShape(B.frames, cropPix);
+    const size_t C = ws.capacity;
+    BdptWave W;
+    W.capacity = ws.capacity;
+    W.prep = reinterpret_cast<SharedNode*>(take((size_t)ws.spanFrames * lightPaths * maxLightVerts * sizeof(SharedNode)));
+    W.thr = reinterpret_cast<float4*>(take(C * 16));
+    W.tot = reinterpret_cast<float4*>(take(C * 16));
+    W.cv0 = reinterpret_cast<float4*>(take(C * 16));
+    W.cv1 = reinterpret_cast<float4*>(take(C * 16));
+    W.cv2 = reinterpret_cast<float4*>(take(C * 16));
+    W.misc = reinterpret_cast<uint4*>(take(C * 16));
+    W.misc2 = reinterpret_cast<uint4*>(take(C * 16));
+    W.conn = reinterpret_cast<uint2*>(take(C * 8));
+    W.volIOR = reinterpret_cast<float4*>(take(C * 16));
+    W.volMat = reinterpret_cast<uint4*>(take(C * 16));
+    W.volAbs = reinterpret_cast<float4*>(take(C * 64));
+    W.fhAlb = reinterpret_cast<float4*>(take(C * 16));
+    W.fhNrm = reinterpret_cast<float4*>(take(C * 16));
+    uint32_t* counters = reinterpret_cast<uint32_t*>(take(256));
+    RayQueue QA{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<float4*>(take(C * 16)), counters + 0};
+    RayQueue QB{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<float4*>(take(C * 16)), counters + 1};
+    HitQueue H{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<uint32_t*>(take(C * 4))};
+    const size_t CR = C * maxLightVerts;
+    W.C = ShadowQueue{reinterpret_cast<float4*>(take(CR * 16)), reinterpret_cast<float4*>(take(CR * 16)),
+                      reinterpret_cast<uint2*>(take(CR * 8)), reinterpret_cast<float4*>(take(CR * 16)), counters + 2};
+    W.vis = reinterpret_cast<uint8_t*>(take(CR));
+    W.connCount = counters + 2;
+
     cudaMemsetAsync(B.splat, 0, (size_t)B.frames * cropPix * 24, stream);
     const uint32_t lp = B.frames * lightPaths;
     int lb = (int)std::min<uint64_t>((lp + 127) / 128, (uint64_t)smCount * 16);
+    int launches = 0;
     bdptLightPaths<<<lb, 128, 0, stream>>>(S, P, B);
     bdptHeaders<<<B.frames, 1024, 0, stream>>>(B);
-    bdptCamera<<<dim3(B.groups, B.frames), kGroupSize, 0, stream>>>(S, P, B);
+    launches += 2;
+    const uint64_t total = (uint64_t)B.frames * cropPix;
+    const int traceBlocks = smCount * 16, shadeBlocks = smCount * 8;
+    for (uint64_t c0 = 0; c0 < total; c0 += C)
+    {
+        W.c0 = c0;
+        W.n = (uint32_t)std::min<uint64_t>(C, total - c0);
+        W.fBase = (uint32_t)(c0 / cropPix);
+        const uint32_t waveFrames = (uint32_t)((c0 + W.n - 1) / cropPix) - W.fBase + 1;
+        const uint64_t prepItems = (uint64_t)waveFrames * lightPaths * maxLightVerts;
+        int pb = (int)std::min<uint64_t>((prepItems + 127) / 128, (uint64_t)smCount * 16);
+        wbPrepare<<<pb, 128, 0, stream>>>(S, P, B, W, waveFrames);
+        int gb = (int)std::min<uint64_t>((W.n + 127) / 128, (uint64_t)smCount * 16);
+        wbGenerate<<<gb, 128, 0, stream>>>(S, P, B, W, QA);
+        launches += 2;
+        RayQueue* cur = &QA;
+        RayQueue* nxt = &QB;
+        for (uint32_t ci = 0; ci < P.maxDepth; ++ci)
+        {
+            wbTrace<<<traceBlocks, 128, 0, stream>>>(S, *cur, H);
+            cudaMemsetAsync(nxt->count, 0, 4, stream);
+            cudaMemsetAsync(W.connCount, 0, 4, stream);
+            wbShade<<<shadeBlocks, 128, 0, stream>>>(S, P, B, W, *cur, H, *nxt, ci);
+            wbVisibility<<<traceBlocks, 128, 0, stream>>>(S, W);
+            wbAccumulate<<<smCount * 4, 256, 0, stream>>>(W, *cur);
+            launches += 4;
+            RayQueue* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+        int fb = (int)std::min<uint64_t>((W.n + 255) / 256, (uint64_t)smCount * 8);
+        wbFinalize<<<fb, 256, 0, stream>>>(S, P, W);
+        ++launches;
+    }
     bdptLightTrace<<<lb, 128, 0, stream>>>(S, P, B);
     int rb = (int)std::min<uint64_t>((B.frames * cropPix + 255) / 256, (uint64_t)smCount * 8);
     bdptResolveSplats<<<rb, 256, 0, stream>>>(P, B);
-    return 5;
+    launches += 2;
+    return launches;
 }
 
 } // namespace yg
