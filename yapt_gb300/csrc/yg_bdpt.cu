@@ -183,8 +183,11 @@ struct ScatterEval
 };
 
 // evaluateSurfaceAndPDFs (BDPTCommon.hlsl:377-443) without the ray-state update: the forward
-// evaluation, and the density of sampling wo from wi with the frame rebuilt for wi
-YG_DEV ScatterEval evaluateBoth(const Luts& L, const Spectral& sp, const Surface& s, const SurfaceCtx& c, float curIOR,
+// evaluation, and the density of sampling wo from wi with the frame rebuilt for wi. Kept out
+// of line: the camera-vertex kernel calls it for the connection's camera end, its light end
+// and the continuation, and one shared copy of the layered BSDF keeps the kernel's code
+// within the instruction cache.
+__device__ __noinline__ ScatterEval evaluateBoth(const Luts& L, const Spectral& sp, const Surface& s, const SurfaceCtx& c, float curIOR,
                                 float prevIOR, float3 wo, float3 wi, bool front, bool fromLight, bool treatAsDelta)
 {
     ScatterEval r;
@@ -1315,7 +1318,9 @@ WaveShape waveShape(uint32_t frames, uint64_t cropPixels)
     w.spanFrames = (uint32_t)std::min<uint64_t>(frames, w.capacity / std::max<uint64_t>(cropPixels, 1) + 2);
     return w;
 }
-size_t waveSlotBytes() { return 5 * 16 + 2 * 16 + 8 + 16 + 16 + 64 + 2 * 16 + 2 * 32 + 20; }
+// per path: state (5 x 16 + 2 x 16 + 8 + volumes 96 + features 32), two ray queues (64), hits
+// (20), the regrouped ray and hit queues (52) and the class key (1)
+size_t waveSlotBytes() { return 5 * 16 + 2 * 16 + 8 + 16 + 16 + 64 + 2 * 16 + 2 * 32 + 20 + 52 + 1; }
 } // namespace
 
 size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVerts, uint64_t cropPixels)
@@ -1381,6 +1386,10 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
     RayQueue QA{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<float4*>(take(C * 16)), counters + 0};
     RayQueue QB{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<float4*>(take(C * 16)), counters + 1};
     HitQueue H{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<uint32_t*>(take(C * 4))};
+    RayQueue QS{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<float4*>(take(C * 16)), counters + 3};
+    HitQueue HS{reinterpret_cast<float4*>(take(C * 16)), reinterpret_cast<uint32_t*>(take(C * 4))};
+    uint8_t* keys = reinterpret_cast<uint8_t*>(take(C));
+    uint32_t* classCounts = counters + 8; // [kShadeClasses] counts, then [kShadeClasses] cursors
     const size_t CR = C * maxLightVerts;
     W.C = ShadowQueue{reinterpret_cast<float4*>(take(CR * 16)), reinterpret_cast<float4*>(take(CR * 16)),
                       reinterpret_cast<uint2*>(take(CR * 8)), reinterpret_cast<float4*>(take(CR * 16)), counters + 2};
@@ -1415,10 +1424,14 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
             wbTrace<<<traceBlocks, 128, 0, stream>>>(S, *cur, H);
             cudaMemsetAsync(nxt->count, 0, 4, stream);
             cudaMemsetAsync(W.connCount, 0, 4, stream);
-            wbShade<<<shadeBlocks, 128, 0, stream>>>(S, P, B, W, *cur, H, *nxt, ci);
+            // shading coherence: hits grouped by material class before the vertex pass
+            cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
+            wfClassify<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
+            wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
+            wbShade<<<shadeBlocks, 128, 0, stream>>>(S, P, B, W, QS, HS, *nxt, ci);
             wbVisibility<<<traceBlocks, 128, 0, stream>>>(S, W);
-            wbAccumulate<<<smCount * 4, 256, 0, stream>>>(W, *cur);
-            launches += 4;
+            wbAccumulate<<<smCount * 4, 256, 0, stream>>>(W, QS);
+            launches += 6;
             RayQueue* t = cur;
             cur = nxt;
             nxt = t;

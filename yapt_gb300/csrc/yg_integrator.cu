@@ -103,25 +103,6 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, Hi
     }
 }
 
-__global__ void __launch_bounds__(256) wfClassify(const SceneView S, RayQueue Q, HitQueue H, uint8_t* keys, uint32_t* counts)
-{
-    const uint32_t n = *Q.count;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (n + stride - 1) / stride;
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t r = 0; r < rounds; ++r)
-    {
-        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
-        bool active = i < n;
-        uint32_t key = active ? shadeClass(S, H.a[i], H.b[i]) : 0xffu;
-        if (active) keys[i] = (uint8_t)key;
-        for (uint32_t c = 0; c < (uint32_t)kShadeClasses; ++c)
-        {
-            uint32_t m = __ballot_sync(0xffffffffu, key == c);
-            if (lane == 0 && m) atomicAdd(&counts[c], (uint32_t)__popc(m));
-        }
-    }
-}
 
 template <bool NEE>
 __global__ void __launch_bounds__(128, 4) wfShade(const SceneView S, const LaunchParams P, WaveState W, RayQueue Qin,
@@ -396,7 +377,7 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
             cudaMemsetAsync(SQ.count, 0, 4, stream);
             cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
             if (T) T->begin(stream);
-            wfClassify<<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
+            wfClassify<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
             wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
             if (T) T->end(kKernelRegroup, stream);
             if (T) T->begin(stream);

@@ -171,6 +171,28 @@ YG_DEV uint32_t shadeClass(const SceneView& S, float4 ha, uint32_t hb)
     return 2;
 }
 
+// shading-class key of every queued hit and the class counts
+template <int CLASSES>
+__global__ void __launch_bounds__(256) wfClassify(const SceneView S, RayQueue Q, HitQueue H, uint8_t* keys, uint32_t* counts)
+{
+    const uint32_t n = *Q.count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
+        bool active = i < n;
+        uint32_t key = active ? shadeClass(S, H.a[i], H.b[i]) : 0xffu;
+        if (active) keys[i] = (uint8_t)key;
+        for (uint32_t c = 0; c < (uint32_t)CLASSES; ++c)
+        {
+            uint32_t m = __ballot_sync(0xffffffffu, key == c);
+            if (lane == 0 && m) atomicAdd(&counts[c], (uint32_t)__popc(m));
+        }
+    }
+}
+
 template <int CLASSES>
 __global__ void __launch_bounds__(256) wfRegroup(RayQueue Q, HitQueue H, const uint8_t* keys, const uint32_t* counts,
                                                  uint32_t* cursors, RayQueue Qs, HitQueue Hs)
