@@ -242,6 +242,10 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* params, yg_sample_
 /* Film readback: mean XYZ per pixel (width*height*3) and per-pixel sample counts
  * (width*height, may be NULL). Synchronises the context stream. */
 YG_API int yg_film_read(yg_context* ctx, float* xyz_mean, float* counts);
+/* The same means written to DEVICE buffers (any may be NULL: xyz_mean and albedo/normal
+ * W*H*3 floats, depth W*H); the call returns when they are written. Features need a render
+ * with YG_FLAG_FEATURES since the last yg_film_clear. */
+YG_API int yg_film_resolve_device(yg_context* ctx, float* xyz_mean, float* albedo, float* normal, float* depth);
 /* First-hit feature means (YG_FLAG_FEATURES): albedo RGB, normal xyz, depth per pixel. */
 YG_API int yg_features_read(yg_context* ctx, float* albedo, float* normal, float* depth);
 /* relMSE of the film mean against a reference image (host, width*height*3 floats),
@@ -432,6 +436,14 @@ YG_API int yg_nn_adam(float* params, const float* grads, float* m, float* v, voi
 /* 16-channel network input: log1p(linear sRGB of the mean XYZ), albedo, normal, depth / depth_scale, zeros. */
 YG_API int yg_nn_pack_input(const float* xyz, const float* albedo, const float* normal, const float* depth, float depth_scale,
                             long pixels, const yg_nn_tensor* out, void* stream);
+/* Per-tile error estimate of a denoised image `out` (height x width x 3, FP32) from the denoised
+ * images a and b of two independent half renders: the tile mean of ((a-b)^2/4)/(out^2+eps) into
+ * tile_err, and tile_flags = err > threshold (tiles of `tile` pixels, row-major). */
+YG_API int yg_nn_tile_error(const float* a, const float* b, const float* out, int height, int width, int tile, float eps,
+                            float threshold, float* tile_err, uint32_t* tile_flags, void* stream);
+/* Replaces the flagged tiles of out by the linear sRGB of film_xyz (the plain film mean). */
+YG_API int yg_nn_tile_fallback(float* out, const float* film_xyz, const uint32_t* tile_flags, int height, int width, int tile,
+                               void* stream);
 
 #ifdef __cplusplus
 }

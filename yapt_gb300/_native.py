@@ -155,6 +155,10 @@ SIGNATURES = [
     ("yg_host_table", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     ("yg_upload_mesh", C.c_int, [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(C.c_uint32)]),
     ("yg_clear_meshes", C.c_int, [C.c_void_p]),
+    ("yg_film_resolve_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("yg_nn_tile_error", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                                   C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("yg_nn_tile_fallback", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     ("yg_bvh_check", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("yg_upload_materials", C.c_int, [C.c_void_p, C.POINTER(Material), C.c_uint32]),
     ("yg_upload_spectra", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.c_float, C.c_float]),

@@ -896,12 +896,13 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         timer = yg::KernelTimer{ctx->kernelEvents.data(), ctx->kernelKinds.data(), (uint32_t)ctx->kernelKinds.size(), 0};
     }
     ctx->kernelTimed = 0;
-    // Sobol points of every sample index of the request (RaytraceCommonResources.cpp:623-627)
-    std::vector<uint32_t> pts((size_t)p->spp_count * yg::kSobolDims);
-    for (uint32_t s = 0; s < p->spp_count; ++s)
-        for (uint32_t d = 0; d < (uint32_t)yg::kSobolDims; ++d)
-            pts[(size_t)s * yg::kSobolDims + d] = yg::sobolUint(ctx->sobolMatrices.data(), p->spp_start + s, d);
-    if ((r = upload(ctx, ctx->dSobol, pts.data(), pts.size()))) return r;
+    // Sobol points of every sample index of the request (RaytraceCommonResources.cpp:623-627),
+    // generated on the device from the generator matrices
+    if (!ctx->dSobolMat.p)
+        if ((r = upload(ctx, ctx->dSobolMat, ctx->sobolMatrices.data(), ctx->sobolMatrices.size()))) return r;
+    YG_CUDA(ctx->dSobol.ensure((size_t)p->spp_count * yg::kSobolDims * 4));
+    yg::launchSobolPoints(ctx->dSobolMat.as<uint32_t>(), p->spp_start, p->spp_count, ctx->dSobol.as<uint32_t>(), ctx->smCount,
+                          ctx->stream);
 
     yg::SceneView S;
     fillSceneView(ctx, lminf, lmaxf, needRgb, S);
@@ -1040,6 +1041,21 @@ YG_API int yg_film_read(yg_context* ctx, float* xyz, float* counts)
         xyz[3 * i + 2] = s[i].z * inv;
         if (counts) counts[i] = c;
     }
+    return YG_OK;
+}
+
+YG_API int yg_film_resolve_device(yg_context* ctx, float* xyz, float* albedo, float* normal, float* depth)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "film resolve: null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t n = (size_t)ctx->filmW * ctx->filmH;
+    if (n == 0) return fail(YG_ERR_NOT_READY, "film: not allocated");
+    if ((albedo || normal || depth) && !ctx->dAccA.p)
+        return fail(YG_ERR_NOT_READY, "film resolve: no feature accumulators");
+    yg::launchFilmResolve(ctx->dFilmSum.as<float4>(), ctx->dAccA.as<float4>(), ctx->dAccN.as<float4>(), n, xyz, albedo, normal,
+                          depth, ctx->smCount, ctx->stream);
+    YG_CUDA(cudaGetLastError());
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
     return YG_OK;
 }
 

@@ -9,6 +9,8 @@
 // film in sample order, so the film does not depend on thread scheduling.
 #include "yg_wave.cuh"
 
+#include <algorithm>
+
 namespace yg
 {
 
@@ -294,7 +296,77 @@ __global__ void relmseKernel(const float4* __restrict__ sum, const float* __rest
     }
 }
 
+// Sobol points of sample indices [start, start + count), kSobolDims each: the XOR of the
+// generator-matrix columns of the set bits of the index (sobolUint, RandUtility.inl:34-46)
+__global__ void sobolPointsKernel(const uint32_t* __restrict__ matrices, uint32_t start, uint32_t count,
+                                  uint32_t* __restrict__ out)
+{
+    const uint64_t total = (uint64_t)count * kSobolDims;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint32_t dim = (uint32_t)(i % kSobolDims);
+        uint32_t index = start + (uint32_t)(i / kSobolDims);
+        const uint32_t* m = matrices + dim * 32;
+        uint32_t v = 0;
+        for (int b = 0; index != 0; index >>= 1, ++b)
+            if (index & 1u) v ^= m[b];
+        out[i] = v;
+    }
+}
+
+int launchSobolPoints(const uint32_t* matrices, uint32_t start, uint32_t count, uint32_t* out, int smCount, cudaStream_t stream)
+{
+    const uint64_t total = (uint64_t)count * kSobolDims;
+    int blocks = (int)std::min<uint64_t>((total + 255) / 256, (uint64_t)smCount * 8);
+    sobolPointsKernel<<<std::max(blocks, 1), 256, 0, stream>>>(matrices, start, count, out);
+    return 1;
+}
+
+// film means on the device: XYZ (and first-hit features) divided by the sample count
+__global__ void filmResolveKernel(const float4* __restrict__ sum, const float4* __restrict__ accA,
+                                  const float4* __restrict__ accN, uint64_t n, float* __restrict__ xyz,
+                                  float* __restrict__ albedo, float* __restrict__ normal, float* __restrict__ depth)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const float4 s = sum[i];
+        const float c = s.w > 0.0f ? 1.0f / s.w : 0.0f;
+        if (xyz)
+        {
+            xyz[3 * i] = s.x * c;
+            xyz[3 * i + 1] = s.y * c;
+            xyz[3 * i + 2] = s.z * c;
+        }
+        if (albedo)
+        {
+            const float4 a = accA[i];
+            albedo[3 * i] = a.x * c;
+            albedo[3 * i + 1] = a.y * c;
+            albedo[3 * i + 2] = a.z * c;
+        }
+        if (normal || depth)
+        {
+            const float4 nd = accN[i];
+            if (normal)
+            {
+                normal[3 * i] = nd.x * c;
+                normal[3 * i + 1] = nd.y * c;
+                normal[3 * i + 2] = nd.z * c;
+            }
+            if (depth) depth[i] = nd.w * c;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- launchers
+int launchFilmResolve(const float4* sum, const float4* accA, const float4* accN, uint64_t n, float* xyz, float* albedo,
+                      float* normal, float* depth, int smCount, cudaStream_t stream)
+{
+    int blocks = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)smCount * 8);
+    filmResolveKernel<<<std::max(blocks, 1), 256, 0, stream>>>(sum, accA, accN, n, xyz, albedo, normal, depth);
+    return 1;
+}
+
 int launchPathKernel(const SceneView& S, const LaunchParams& P, int smCount, cudaStream_t stream)
 {
     const int threads = 128;

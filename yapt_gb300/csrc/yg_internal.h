@@ -104,7 +104,7 @@ struct yg_context
     // device
     DevBuf dTris, dNodes, dInst, dMat, dLights, dPos, dNrm, dTan, dUV, dIdx, dSpec;
     DevBuf dLut[9];
-    DevBuf dCie, dRgb, dSobol, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
+    DevBuf dCie, dRgb, dSobol, dSobolMat, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
     DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena, dPerm;
     uint32_t nLights = 0;
     float worldCenter[3] = {0, 0, 0}; // getWorldCenterAndRadiusSqr (raytraceCommonResources.hlsl:99-104)
@@ -123,7 +123,7 @@ struct yg_context
     ~yg_context()
     {
         DevBuf* all[] = {&dTris, &dNodes, &dInst, &dMat, &dLights, &dPos, &dNrm, &dTan, &dUV, &dIdx, &dSpec, &dCie, &dRgb,
-                         &dSobol, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
+                         &dSobol, &dSobolMat, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
                          &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm};
         for (DevBuf* b : all) b->release();
         for (auto& b : dLut) b.release();

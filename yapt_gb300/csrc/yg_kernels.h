@@ -70,6 +70,9 @@ int launchFilm(float4* sum, float4* comp, const float4* samples, uint32_t width,
                uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
 int launchFeatures(float4* accA, float4* accN, const float4* fa, const float4* fn, uint32_t width, uint32_t cx, uint32_t cy,
                    uint32_t cw, uint32_t ch, uint32_t nspp, int smCount, cudaStream_t stream);
+int launchSobolPoints(const uint32_t* matrices, uint32_t start, uint32_t count, uint32_t* out, int smCount, cudaStream_t stream);
+int launchFilmResolve(const float4* sum, const float4* accA, const float4* accN, uint64_t n, float* xyz, float* albedo,
+                      float* normal, float* depth, int smCount, cudaStream_t stream);
 int launchRelmse(const float4* sum, const float* ref, uint32_t npix, double eps, double* out, int smCount,
                  cudaStream_t stream);
 // Merged wavefront of several requests (serving). All tables live in device memory and are

@@ -561,6 +561,59 @@ __global__ void packInput(const float* __restrict__ xyz, const float* __restrict
     }
 }
 
+// per-tile error estimate of a denoised image from the denoised images a and b of two
+// independent half renders: mean over the tile's pixels and channels of
+// ((a - b)^2 / 4) / (out^2 + eps), one block per tile (FP64 sums); flags tiles above threshold
+__global__ void tileError(const float* __restrict__ a, const float* __restrict__ b, const float* __restrict__ out, int H, int W,
+                          int tile, float eps, float threshold, float* __restrict__ err, uint32_t* __restrict__ flags)
+{
+    const int tx = (W + tile - 1) / tile;
+    const int t = blockIdx.x;
+    const int y0 = (t / tx) * tile, x0 = (t % tx) * tile;
+    const int th = min(tile, H - y0), tw = min(tile, W - x0);
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < th * tw; k += blockDim.x)
+    {
+        const long q = (long)(y0 + k / tw) * W + (x0 + k % tw);
+        for (int c = 0; c < 3; ++c)
+        {
+            const float d = a[3 * q + c] - b[3 * q + c], o = out[3 * q + c];
+            acc += (double)(d * d * 0.25f) / (double)(o * o + eps);
+        }
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1)
+    {
+        if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        const float e = (float)(red[0] / (3.0 * th * tw));
+        err[t] = e;
+        flags[t] = e > threshold ? 1u : 0u;
+    }
+}
+
+// flagged tiles of out replaced by the linear sRGB of a film mean (XYZ)
+__global__ void tileFallback(float* __restrict__ out, const float* __restrict__ xyz, const uint32_t* __restrict__ flags, int H,
+                             int W, int tile)
+{
+    const int tx = (W + tile - 1) / tile;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < (long)H * W; q += (long)gridDim.x * blockDim.x)
+    {
+        const int y = (int)(q / W), x = (int)(q % W);
+        if (!flags[(y / tile) * tx + x / tile]) continue;
+        const float X = xyz[3 * q], Y = xyz[3 * q + 1], Z = xyz[3 * q + 2];
+        // c_srgbXYZToRGB (colorSpaces.hlsl:18-23)
+        out[3 * q] = 3.2406f * X - 1.5372f * Y - 0.4986f * Z;
+        out[3 * q + 1] = -0.9689f * X + 1.8758f * Y + 0.0415f * Z;
+        out[3 * q + 2] = 0.0557f * X - 0.2040f * Y + 1.0570f * Z;
+    }
+}
+
 int gridFor(long n, int threads = 256)
 {
     long b = (n + threads - 1) / threads;
@@ -714,6 +767,25 @@ YG_API int yg_nn_adam(float* params, const float* grads, float* m, float* v, voi
     cudaStream_t st = (cudaStream_t)stream;
     float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
     adamKernel<<<gridFor(n), 256, 0, st>>>(params, grads, m, v, (bf16*)params_bf16, n, lr, beta1, beta2, eps, c1, c2);
+    return status(st);
+}
+
+YG_API int yg_nn_tile_error(const float* a, const float* b, const float* out, int height, int width, int tile, float eps,
+                            float threshold, float* tile_err, uint32_t* tile_flags, void* stream)
+{
+    if (!a || !b || !out || !tile_err || !tile_flags || height <= 0 || width <= 0 || tile <= 0) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int tiles = ((height + tile - 1) / tile) * ((width + tile - 1) / tile);
+    tileError<<<tiles, 256, 0, st>>>(a, b, out, height, width, tile, eps, threshold, tile_err, tile_flags);
+    return status(st);
+}
+
+YG_API int yg_nn_tile_fallback(float* out, const float* film_xyz, const uint32_t* tile_flags, int height, int width, int tile,
+                               void* stream)
+{
+    if (!out || !film_xyz || !tile_flags || height <= 0 || width <= 0 || tile <= 0) return YG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    tileFallback<<<gridFor((long)height * width), 256, 0, st>>>(out, film_xyz, tile_flags, height, width, tile);
     return status(st);
 }
 

@@ -338,9 +338,10 @@ def relmse(y, ref, eps=EPS):
     return float(np.mean((y - r) ** 2 / (r * r + eps)))
 
 
-def train(net, images, steps, batch=8, crop=128, lr=1e-3, seed=0, log_every=0):
+def train(net, images, steps, batch=8, crop=128, lr=1e-3, seed=0, log_every=0, lr_final=None):
     """images: list of (packed input (h*w*16 BF16 device tensor), target (h*w*3 FP32 device tensor), h, w).
-    Random crops (with flips) per step; Adam on the relMSE loss. Returns the loss history."""
+    Random crops (with flips) per step; Adam on the relMSE loss, the learning rate decaying from lr
+    to lr_final on a cosine when lr_final is given. Returns the loss history."""
     torch = net.torch
     rng = np.random.Generator(np.random.PCG64(seed))
     xb = torch.zeros(batch * crop * crop * 16, dtype=torch.bfloat16, device=net.dev)
@@ -360,11 +361,76 @@ def train(net, images, steps, batch=8, crop=128, lr=1e-3, seed=0, log_every=0):
             xv[b].copy_(xs)
             tv[b].copy_(ts)
         loss = net.loss_and_gradients(xb, tb, batch, crop, crop)
-        net.adam_step(lr)
+        step_lr = lr if lr_final is None else lr_final + 0.5 * (lr - lr_final) * (1.0 + np.cos(np.pi * s / max(1, steps)))
+        net.adam_step(step_lr)
         hist.append(loss)
         if log_every and s % log_every == 0:
             print("step %d loss %.5f" % (s, loss), flush=True)
     return hist
+
+
+class DenoisePipeline:
+    """The denoised render on the device: half render A, then B into the same film (so the
+    film holds the full mean), the network on A and on the full input, the per-tile error
+    estimate ((D(A) - D(full))^2 relative, equal to (D(A) - D(B))^2 / 4 for a linear
+    denoiser), and plain accumulation of the tiles above the threshold. Film means, features
+    and the packed input never leave the device."""
+
+    def __init__(self, net, ctx, height, width, tile=64, depth_scale=4.0):
+        torch = net.torch
+        self.net, self.ctx, self.h, self.w, self.tile, self.depth_scale = net, ctx, height, width, tile, depth_scale
+        n = height * width
+        f32 = dict(dtype=torch.float32, device=net.dev)
+        self.xyz, self.alb, self.nrm = (torch.zeros(n * 3, **f32) for _ in range(3))
+        self.dep = torch.zeros(n, **f32)
+        self.packed = torch.zeros(n * 16, dtype=torch.bfloat16, device=net.dev)
+        self.den_a = torch.zeros(n * 3, **f32)
+        self.tiles = ((height + tile - 1) // tile) * ((width + tile - 1) // tile)
+        self.tile_err = torch.zeros(self.tiles, **f32)
+        self.tile_flags = torch.zeros(self.tiles, dtype=torch.int32, device=net.dev)
+
+    def _ptr(self, t):
+        return C.c_void_p(t.data_ptr())
+
+    def _resolve_and_pack(self):
+        lib = self.net.lib
+        N.check(lib.yg_film_resolve_device(self.ctx.h, self._ptr(self.xyz), self._ptr(self.alb), self._ptr(self.nrm),
+                                           self._ptr(self.dep)))
+        fp = lambda t: C.cast(self._ptr(t), C.POINTER(C.c_float))  # noqa: E731
+        _check(lib.yg_nn_pack_input(fp(self.xyz), fp(self.alb), fp(self.nrm), fp(self.dep), C.c_float(self.depth_scale),
+                                    self.h * self.w, C.byref(view(self.packed, 16, 0, 16)), self.net.stream()), "pack")
+
+    def run(self, spp, spp_plain, target, integrator="uni", max_depth=8, lambda_range=(380, 780), fallback_start=1 << 16):
+        """Returns (linear sRGB image h x w x 3 on the host, fallback tile count)."""
+        ctx, net, lib, h, w = self.ctx, self.net, self.net.lib, self.h, self.w
+        half = max(1, spp // 2)
+        kw = dict(max_depth=max_depth, lambda_range=lambda_range, flags=N.YG_FLAG_FEATURES)
+        ctx.film_clear(w, h)
+        ctx.render(ctx.params(integrator, w, h, spp_start=0, spp=half, **kw))
+        self._resolve_and_pack()
+        self.den_a.copy_(net.forward(self.packed, 1, h, w))
+        net.torch.cuda.current_stream().synchronize()  # the next resolve rewrites the inputs on the context stream
+        ctx.render(ctx.params(integrator, w, h, spp_start=half, spp=spp - half, **kw))
+        self._resolve_and_pack()
+        out = net.forward(self.packed, 1, h, w)
+        # threshold / 4: the kernel estimates (a - b)^2 / 4 and here b - a is half of B - A
+        _check(lib.yg_nn_tile_error(self._ptr(self.den_a), self._ptr(out), self._ptr(out), h, w, self.tile, C.c_float(EPS),
+                                    C.c_float(target / 4.0), self._ptr(self.tile_err), self._ptr(self.tile_flags),
+                                    net.stream()), "tile error")
+        flags = self.tile_flags.cpu().numpy()
+        bad = np.nonzero(flags)[0]
+        if len(bad):
+            tx = (w + self.tile - 1) // self.tile
+            ctx.film_clear(w, h)
+            for t in bad:
+                y0, x0 = (int(t) // tx) * self.tile, (int(t) % tx) * self.tile
+                ctx.render(ctx.params(integrator, w, h, spp_start=fallback_start, spp=spp_plain,
+                                      crop=(x0, y0, min(self.tile, w - x0), min(self.tile, h - y0)),
+                                      max_depth=max_depth, lambda_range=lambda_range))
+            N.check(lib.yg_film_resolve_device(ctx.h, self._ptr(self.xyz), None, None, None))
+            _check(lib.yg_nn_tile_fallback(self._ptr(out), self._ptr(self.xyz), self._ptr(self.tile_flags), h, w, self.tile,
+                                           net.stream()), "tile fallback")
+        return out.view(h, w, 3).cpu().numpy(), int(len(bad))
 
 
 def denoise_image(net, packed, h, w):
