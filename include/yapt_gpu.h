@@ -401,6 +401,13 @@ typedef struct yg_nn_tensor
     uint32_t reserved;
 } yg_nn_tensor;
 
+/* The tensor-core path of yg_nn_conv3x3: YG_NN_CONV_TCGEN05 (tcgen05.mma with the accumulator in
+ * tensor memory) or YG_NN_CONV_MMA_SYNC (warp-level mma.sync). Process-wide. */
+#define YG_NN_CONV_MMA_SYNC 0
+#define YG_NN_CONV_TCGEN05 1
+YG_API int yg_nn_set_conv_impl(int impl);
+/* Bounded waits of the tcgen05 convolution that ran out since load (0 on a healthy device). */
+YG_API int yg_nn_tc_timeouts(uint32_t* count);
 /* y = relu?(conv3x3(x, w) + bias), times (mask > 0) where mask is given, added to y when
  * accumulate; y->channels must be a multiple of 32. Zero padding, stride 1. */
 YG_API int yg_nn_conv3x3(const yg_nn_tensor* x, const void* weights, const float* bias, const yg_nn_tensor* y,

@@ -32,8 +32,25 @@ def stream(torch):
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-@pytest.mark.parametrize("cin,cout,off", [(16, 32, 0), (32, 64, 0), (96, 32, 32), (64, 128, 0)])
-def test_conv3x3_forward_and_data_gradient(torch_cuda, cin, cout, off):
+IMPLS = {"mma_sync": 0, "tcgen05": 1}
+
+
+@pytest.fixture(params=list(IMPLS))
+def conv_impl(request, torch_cuda):
+    """Runs a test with each tensor-core path of yg_nn_conv3x3, then restores the default."""
+    from yapt_gb300 import _native as N
+    lib = N.load()
+    assert lib.yg_nn_set_conv_impl(IMPLS[request.param]) == 0
+    yield request.param
+    torch_cuda.cuda.synchronize()
+    import ctypes as C
+    t = C.c_uint32()
+    assert lib.yg_nn_tc_timeouts(C.byref(t)) == 0 and t.value == 0, "tcgen05 waits ran out"
+    assert lib.yg_nn_set_conv_impl(0) == 0
+
+
+@pytest.mark.parametrize("cin,cout,off", [(16, 32, 0), (32, 64, 0), (96, 32, 32), (64, 128, 0), (64, 256, 0), (128, 384, 0)])
+def test_conv3x3_forward_and_data_gradient(torch_cuda, conv_impl, cin, cout, off):
     import ctypes as C
     import unet_ref as R
     from yapt_gb300 import _native as N
@@ -138,7 +155,7 @@ def test_pool_and_upsample_and_their_gradients(torch_cuda):
     np.testing.assert_allclose(host(o2).reshape(n, h, w, c), R.bf16(R.up_bwd(g2) * (x > 0)), rtol=2 ** -7, atol=0)
 
 
-def test_unet_loss_and_gradients_match_the_oracle(torch_cuda):
+def test_unet_loss_and_gradients_match_the_oracle(torch_cuda, conv_impl):
     import unet_ref as R
     from yapt_gb300 import denoise as D
     torch = torch_cuda

@@ -22,6 +22,8 @@ YG_FLAG_FEATURES = 1 << 9
 YG_FLAG_COUNT_TRAVERSAL = 1 << 10
 YG_FLAG_MEGAKERNEL = 1 << 11
 YG_FLAG_TIME_KERNELS = 1 << 12
+YG_NN_CONV_MMA_SYNC = 0
+YG_NN_CONV_TCGEN05 = 1
 
 TABLES = {
     "sobol": 0, "ss": 1, "ss_avg": 2, "ssms": 3, "ssms_avg": 4, "trans_denser": 5, "trans_lighter": 6,
@@ -156,6 +158,8 @@ SIGNATURES = [
     ("yg_upload_mesh", C.c_int, [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(C.c_uint32)]),
     ("yg_clear_meshes", C.c_int, [C.c_void_p]),
     ("yg_film_resolve_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("yg_nn_set_conv_impl", C.c_int, [C.c_int]),
+    ("yg_nn_tc_timeouts", C.c_int, [C.POINTER(C.c_uint32)]),
     ("yg_nn_tile_error", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
                                    C.c_void_p, C.c_void_p, C.c_void_p]),
     ("yg_nn_tile_fallback", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),

@@ -5,13 +5,15 @@
 // channel offset so that a U-Net skip concatenation is just two writers into one buffer.
 // Channel counts are multiples of 16.
 //
-// conv3x3: implicit GEMM, M = pixels, N = output channels, K = 9 taps x input channels.
-// A 128 x 64 output tile per 256-thread block; K advances in chunks of KC channels of one tap,
-// staged in shared memory by a 3-stage cp.async pipeline (zero-filled outside the image) and
-// fed to mma.sync m16n8k16 (BF16 in, FP32 accumulate) through ldmatrix. The epilogue adds the
-// bias, applies ReLU or a ReLU-derivative mask, optionally accumulates into the destination,
-// and stores BF16. The data gradient is the same kernel on spatially flipped, transposed
-// weights; the weight gradient is a split-K GEMM over pixels with a deterministic reduction.
+// conv3x3: implicit GEMM, M = pixels, N = output channels, K = 9 taps x input channels, on the
+// tcgen05 tensor cores with the accumulator in tensor memory (conv3x3Tc, the default): one CTA
+// per 128 pixels of an image row and up to 256 output channels; the input halo of each channel
+// chunk is staged once and every tap reads it through a shifted matrix descriptor. A warp-level
+// mma.sync m16n8k16 version (conv3x3Kernel: 128 x 64 tiles, cp.async + ldmatrix) is kept
+// selectable (yg_nn_set_conv_impl). Both epilogues add the bias, apply ReLU or a
+// ReLU-derivative mask, optionally accumulate into the destination, and store BF16. The data
+// gradient is the same kernel on spatially flipped, transposed weights; the weight gradient is
+// a split-K GEMM over pixels (mma.sync) with a deterministic reduction.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -207,6 +209,330 @@ __global__ void __launch_bounds__(256) conv3x3Kernel(Act x, const bf16* __restri
             }
         }
 }
+
+// ------------------------------------------------------------------ 3x3 convolution on tcgen05
+// The same implicit GEMM on the 5th-generation tensor cores: one CTA of 128 threads per 128
+// output pixels and up to 256 output channels (N). The FP32 accumulator [128 x N] lives in
+// tensor memory (TMEM, one column per output channel, one lane per pixel). Per K block (one
+// tap, KC input channels) all threads stage the im2col A tile [128 x KC] and the weight tile
+// B [N x KC] in shared memory with cp.async (zero fill outside the image), in the no-swizzle
+// K-major layout of 8-row x 16-byte core matrices (core (g, k) at g * SBO + k * 128 bytes).
+// One thread issues the tcgen05.mma instructions (kind::f16, BF16 x BF16 -> FP32, K = 16
+// each) and commits them to the stage's mbarrier. Two stages: a stage is reloaded once the
+// MMAs that read it have completed. The epilogue reads TMEM with tcgen05.ld (warp w owns
+// lanes 32w..32w+31), adds the bias, applies ReLU / mask / accumulation and stores BF16.
+// Every mbarrier wait is bounded; on a timeout the kernel records it, waits (bounded) for
+// its MMAs, frees its TMEM and returns.
+namespace tc
+{
+__device__ uint32_t g_timeouts; // waits that ran out (read by yg_nn_tc_timeouts)
+constexpr uint32_t kSpinLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading (K) and stride (M/N) byte offsets in
+// 16-byte units, descriptor version 1 (bits 46-47), base offset 0, no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t smemDesc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+// instruction descriptor of kind::f16: FP32 accumulator (bits 4-5), BF16 A (bits 7-9) and B
+// (bits 10-12), both K-major, N >> 3 (bits 17-22), M >> 4 (bits 24-28)
+__host__ __device__ constexpr uint32_t idescBf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbarInit(uint32_t addr, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbarWait(uint32_t addr, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kSpinLimit; ++i)
+    {
+        uint32_t ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(ok)
+                     : "r"(addr), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void fenceBeforeSync() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fenceAfterSync() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+template <int KC, int NT>
+struct TcShape
+{
+    static constexpr int HALO = 130;                          // input pixels per halo row (128 + 2)
+    static constexpr uint32_t A_LBO = 3u * HALO * 16u;        // bytes between 8-channel groups of the halo
+    static constexpr int A_BYTES = (int)A_LBO * (KC / 8);     // one channel chunk of the 3 halo rows
+    static constexpr int TAP_BYTES = NT * KC * 2;             // one tap's weights for the chunk
+    // taps per K block (9, 3 or 1): as many as fit beside the two halo buffers, so that one
+    // synchronisation round issues enough MMAs
+    static constexpr int FREE = 200704 - 2 * A_BYTES;
+    static constexpr int TB = 2 * 9 * TAP_BYTES <= FREE ? 9 : (3 * 3 * TAP_BYTES <= FREE ? 3 : 1);
+    static constexpr int B_BYTES = TB * TAP_BYTES;
+    static constexpr int B_STAGES = TB == 9 ? 2 : 3;
+    static constexpr int SMEM = 2 * A_BYTES + B_STAGES * B_BYTES;
+    static constexpr uint32_t TCOLS = NT < 32 ? 32 : NT;
+};
+
+// One CTA computes 128 consecutive output pixels of one image row (x0..x0+127 of row y) for NT
+// output channels. The three input rows y-1..y+1, columns x0-1..x0+128, of one chunk of KC
+// input channels are staged once: 8-channel group g of halo pixel (r, c) at
+// g * A_LBO + (r * 130 + c) * 16. Rows then sit 16 bytes apart within a group, so the A
+// operand of tap (dy, dx) is the same buffer with its start shifted by
+// ((1 + dy) * 130 + 1 + dx) * 16 bytes (SBO 128, LBO A_LBO): the nine taps read one copy of the
+// input. B (the tap's NT x KC weights) goes through a three-deep ring; the MMAs of one K block
+// (a chunk and a tap) are committed to that B stage's mbarrier.
+template <int KC, int NT>
+__global__ void __launch_bounds__(128) conv3x3Tc(Act x, const bf16* __restrict__ w, const float* __restrict__ bias, Act y,
+                                                 Act mask, int relu, int accumulate, int nImg, int H, int W)
+{
+    using T = TcShape<KC, NT>;
+    constexpr uint32_t IDESC = idescBf16(128, NT);
+    constexpr uint32_t SBO_B = (KC / 8) * 128;
+    constexpr int SEGS = KC / 8;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar[T::B_STAGES];
+    __shared__ uint32_t tmemSlot;
+    __shared__ int abortFlag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tilesPerRow = (W + 127) / 128;
+    const int rowTile = blockIdx.x % tilesPerRow;
+    const int rowIdx = blockIdx.x / tilesPerRow; // image * H + y
+    const int img = rowIdx / H, yy0 = rowIdx % H;
+    const int x0 = rowTile * 128;
+    const int n0 = blockIdx.y * NT;
+    const int Cin = (int)x.ch;
+    constexpr int GROUPS = 9 / T::TB; // K blocks per chunk
+    const int chunks = Cin / KC, kBlocks = GROUPS * chunks;
+    uint8_t* sA[2] = {smem, smem + T::A_BYTES};
+    uint8_t* sBring = smem + 2 * T::A_BYTES;
+
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(&tmemSlot)),
+                     "r"(T::TCOLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0)
+    {
+        for (int k = 0; k < T::B_STAGES; ++k) mbarInit(smemAddr(&mbar[k]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        abortFlag = 0;
+    }
+    fenceBeforeSync();
+    __syncthreads();
+    fenceAfterSync();
+    const uint32_t tmem = tmemSlot;
+
+    auto loadA = [&](int c) {
+        uint8_t* dst = sA[c & 1];
+        const int c0 = c * KC;
+        for (int i = tid; i < 3 * T::HALO * SEGS; i += 128)
+        {
+            const int sg = i % SEGS, px = i / SEGS;
+            const int r = px / T::HALO, cc = px % T::HALO;
+            const int yy = yy0 + r - 1, xx = x0 + cc - 1;
+            const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
+            const bf16* src = ok ? x.p + ((long)(img * H + yy) * W + xx) * x.stride + x.off + c0 + sg * 8 : x.p;
+            cpAsync16(dst + sg * T::A_LBO + px * 16, src, ok);
+        }
+    };
+    auto loadB = [&](int kb) {
+        uint8_t* dst = sBring + (kb % T::B_STAGES) * T::B_BYTES;
+        const int c0 = (kb / GROUPS) * KC, tap0 = (kb % GROUPS) * T::TB;
+        for (int i = tid; i < T::TB * NT * SEGS; i += 128)
+        {
+            const int t = i / (NT * SEGS), rs = i % (NT * SEGS);
+            const int r = rs / SEGS, sg = rs % SEGS;
+            const bf16* src = w + ((long)(n0 + r) * 9 + tap0 + t) * Cin + c0 + sg * 8;
+            cpAsync16(dst + t * T::TAP_BYTES + (r >> 3) * SBO_B + sg * 128 + (r & 7) * 16, src, true);
+        }
+    };
+    uint32_t parity[T::B_STAGES] = {};
+    // waits for the MMAs of K block kb (its B stage's mbarrier); in order, so earlier blocks are done too
+    auto waitBlock = [&](int kb) {
+        const int stg = kb % T::B_STAGES;
+        if (!mbarWait(smemAddr(&mbar[stg]), parity[stg])) abortFlag = 1;
+        parity[stg] ^= 1u;
+    };
+
+    // prologue: A of chunk 0 and B of block 0
+    loadA(0);
+    loadB(0);
+    cpAsyncCommit();
+    int waitedUpTo = -1; // highest K block whose MMAs are known complete
+    for (int kb = 0; kb < kBlocks; ++kb)
+    {
+        const int c = kb / GROUPS, grp = kb % GROUPS;
+        // prefetch B of kb + 1 (its stage last served kb + 1 - B_STAGES) and, in the middle of
+        // a chunk, A of the next chunk (its buffer last served chunk c - 1, done by then)
+        const int nb = kb + 1;
+        if (nb < kBlocks)
+        {
+            const int reuse = nb - T::B_STAGES;
+            while (waitedUpTo < reuse) waitBlock(++waitedUpTo);
+            loadB(nb);
+        }
+        if (grp == GROUPS / 2 && c + 1 < chunks)
+        {
+            const int lastOfPrev = GROUPS * c - 1;
+            while (waitedUpTo < lastOfPrev) waitBlock(++waitedUpTo);
+            loadA(c + 1);
+        }
+        cpAsyncCommit();
+        if (__syncthreads_or(abortFlag)) break;
+        cpAsyncWait<1>(); // everything but the group just issued
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0)
+        {
+            fenceAfterSync();
+            const uint32_t aBase = smemAddr(sA[c & 1]);
+            const uint32_t bBase = smemAddr(sBring + (kb % T::B_STAGES) * T::B_BYTES);
+#pragma unroll
+            for (int t = 0; t < T::TB; ++t)
+            {
+                const int tap = grp * T::TB + t;
+                const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+                const uint32_t a0 = aBase + (uint32_t)(((1 + dy) * T::HALO + 1 + dx) * 16);
+                const uint32_t b0 = bBase + t * T::TAP_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < KC / 16; ++kk)
+                {
+                    const uint64_t ad = smemDesc(a0 + kk * 2 * T::A_LBO, T::A_LBO, 128);
+                    const uint64_t bd = smemDesc(b0 + kk * 2 * 128, 128, SBO_B);
+                    const uint32_t acc = (kb | t | kk) != 0 ? 1u : 0u;
+                    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                                 "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                                 : "memory");
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smemAddr(&mbar[kb % T::B_STAGES]))
+                         : "memory");
+        }
+    }
+    cpAsyncWait<0>();
+    bool ok = !abortFlag;
+    if (ok)
+    {
+        while (waitedUpTo < kBlocks - 1) waitBlock(++waitedUpTo);
+        ok = !abortFlag;
+    }
+    else
+    {
+        // a wait ran out: drain what may still be in flight (bounded) before TMEM is freed
+        for (int k = 0; k < T::B_STAGES; ++k) mbarWait(smemAddr(&mbar[k]), parity[k]);
+    }
+    if (__syncthreads_or(!ok))
+    {
+        if (tid == 0) atomicAdd(&g_timeouts, 1u);
+    }
+    else
+    {
+        fenceAfterSync();
+        const int xo = x0 + warp * 32 + lane;
+        const long q = ((long)(img * H + yy0)) * W + xo;
+#pragma unroll 1
+        for (int cc = 0; cc < NT; cc += 16)
+        {
+            uint32_t r[16];
+            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                         : "r"(ta)
+                         : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (xo >= W) continue;
+#pragma unroll
+            for (int j = 0; j < 16; j += 2)
+            {
+                const int co = n0 + cc + j;
+                float v0 = __uint_as_float(r[j]), v1 = __uint_as_float(r[j + 1]);
+                if (bias)
+                {
+                    v0 += bias[co];
+                    v1 += bias[co + 1];
+                }
+                if (relu)
+                {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                }
+                if (mask.p)
+                {
+                    __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask.p + q * mask.stride + mask.off + co);
+                    if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
+                    if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
+                }
+                __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(y.p + q * y.stride + y.off + co);
+                if (accumulate)
+                {
+                    __nv_bfloat162 old = *dst;
+                    v0 += __bfloat162float(old.x);
+                    v1 += __bfloat162float(old.y);
+                }
+                *dst = __floats2bfloat162_rn(v0, v1);
+            }
+        }
+    }
+    fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0)
+    {
+        fenceAfterSync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(T::TCOLS) : "memory");
+    }
+}
+
+template <int KC, int NT>
+int launchTc(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate, int n,
+             int h, int wd, cudaStream_t st)
+{
+    using T = TcShape<KC, NT>;
+    // at most 512 / TCOLS CTAs per SM may hold tensor memory at once, so the shared-memory
+    // request is raised until no more CTAs than that fit on an SM (228 KB each): an
+    // allocation then never waits for another CTA's columns
+    constexpr int floorBytes = 233472 / (512 / (int)T::TCOLS) - 2047;
+    constexpr int smemBytes = T::SMEM > floorBytes ? T::SMEM : floorBytes;
+    static_assert(smemBytes <= 232448, "shared memory");
+    static bool configured = false;
+    if (!configured)
+    {
+        if (cudaFuncSetAttribute(conv3x3Tc<KC, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes) != cudaSuccess)
+            return YG_ERR_CUDA;
+        configured = true;
+    }
+    dim3 grid((unsigned)(n * h * ((wd + 127) / 128)), (unsigned)(y.ch / NT));
+    conv3x3Tc<KC, NT><<<grid, 128, smemBytes, st>>>(x, w, bias, y, m, relu, accumulate, n, h, wd);
+    return YG_OK;
+}
+
+template <int KC>
+int launchTcN(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate, int n,
+              int h, int wd, cudaStream_t st)
+{
+    const int c = (int)y.ch;
+    if (c % 256 == 0) return launchTc<KC, 256>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    if (c % 128 == 0) return launchTc<KC, 128>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    if (c % 64 == 0) return launchTc<KC, 64>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    if (c % 32 == 0) return launchTc<KC, 32>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    return YG_ERR_INVALID_ARGUMENT;
+}
+} // namespace tc
 
 // ------------------------------------------------------------------ 3x3 weight gradient
 // dW[co][tap][ci] = sum_q dY[q][co] * X[q shifted by tap][ci]: M = Cout (64 per block),
@@ -634,6 +960,8 @@ Act act(const yg_nn_tensor* t)
     a.ch = t ? t->channels : 0;
     return a;
 }
+int g_convImpl = YG_NN_CONV_TCGEN05;
+
 bool okTensor(const yg_nn_tensor* t)
 {
     return t && t->data && t->channels % 16 == 0 && t->stride % 8 == 0 && t->offset % 8 == 0 &&
@@ -649,6 +977,19 @@ int status(cudaStream_t s)
 
 extern "C" {
 
+YG_API int yg_nn_set_conv_impl(int impl)
+{
+    if (impl != YG_NN_CONV_MMA_SYNC && impl != YG_NN_CONV_TCGEN05) return YG_ERR_INVALID_ARGUMENT;
+    g_convImpl = impl;
+    return YG_OK;
+}
+
+YG_API int yg_nn_tc_timeouts(uint32_t* count)
+{
+    if (!count) return YG_ERR_INVALID_ARGUMENT;
+    return cudaMemcpyFromSymbol(count, tc::g_timeouts, sizeof(uint32_t)) == cudaSuccess ? YG_OK : YG_ERR_CUDA;
+}
+
 YG_API int yg_nn_conv3x3(const yg_nn_tensor* x, const void* weights, const float* bias, const yg_nn_tensor* y,
                          const yg_nn_tensor* mask, int relu, int accumulate, int n, int h, int w, void* stream)
 {
@@ -659,6 +1000,14 @@ YG_API int yg_nn_conv3x3(const yg_nn_tensor* x, const void* weights, const float
     long P = (long)n * h * w;
     dim3 grid((unsigned)((P + CM - 1) / CM), (unsigned)((y->channels + CN - 1) / CN));
     Act m = act(mask && mask->data ? mask : nullptr);
+    if (g_convImpl == YG_NN_CONV_TCGEN05)
+    {
+        int r;
+        if (x->channels % 64 == 0) r = tc::launchTcN<64>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
+        else if (x->channels % 32 == 0) r = tc::launchTcN<32>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
+        else r = tc::launchTcN<16>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
+        return r != YG_OK ? r : status(st);
+    }
     if (x->channels % 32 == 0)
         conv3x3Kernel<32><<<grid, 256, 0, st>>>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w);
     else
