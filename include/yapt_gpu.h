@@ -405,6 +405,7 @@ typedef struct yg_nn_tensor
  * tensor memory) or YG_NN_CONV_MMA_SYNC (warp-level mma.sync). Process-wide. */
 #define YG_NN_CONV_MMA_SYNC 0
 #define YG_NN_CONV_TCGEN05 1
+#define YG_NN_CONV_TCGEN05_TMA 2 /* tcgen05 with the operands loaded by TMA (cp.async.bulk.tensor) */
 YG_API int yg_nn_set_conv_impl(int impl);
 /* Bounded waits of the tcgen05 convolution that ran out since load (0 on a healthy device). */
 YG_API int yg_nn_tc_timeouts(uint32_t* count);

@@ -32,7 +32,7 @@ def stream(torch):
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-IMPLS = {"mma_sync": 0, "tcgen05": 1}
+IMPLS = {"mma_sync": 0, "tcgen05": 1, "tcgen05_tma": 2}
 
 
 @pytest.fixture(params=list(IMPLS))

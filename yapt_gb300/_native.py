@@ -24,6 +24,7 @@ YG_FLAG_MEGAKERNEL = 1 << 11
 YG_FLAG_TIME_KERNELS = 1 << 12
 YG_NN_CONV_MMA_SYNC = 0
 YG_NN_CONV_TCGEN05 = 1
+YG_NN_CONV_TCGEN05_TMA = 2
 
 TABLES = {
     "sobol": 0, "ss": 1, "ss_avg": 2, "ssms": 3, "ssms_avg": 4, "trans_denser": 5, "trans_lighter": 6,

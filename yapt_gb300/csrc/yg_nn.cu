@@ -6,14 +6,17 @@
 // Channel counts are multiples of 16.
 //
 // conv3x3: implicit GEMM, M = pixels, N = output channels, K = 9 taps x input channels, on the
-// tcgen05 tensor cores with the accumulator in tensor memory (conv3x3Tc, the default): one CTA
-// per 128 pixels of an image row and up to 256 output channels; the input halo of each channel
-// chunk is staged once and every tap reads it through a shifted matrix descriptor. A warp-level
-// mma.sync m16n8k16 version (conv3x3Kernel: 128 x 64 tiles, cp.async + ldmatrix) is kept
-// selectable (yg_nn_set_conv_impl). Both epilogues add the bias, apply ReLU or a
+// tcgen05 tensor cores with the accumulator in tensor memory: one CTA per 128 pixels of an
+// image row and up to 256 output channels; the input halo of each channel chunk is staged once
+// and every tap reads it through a shifted matrix descriptor. The default (conv3x3Tma) loads
+// the operands with TMA boxes tracked by mbarrier transaction counts, one producer thread and
+// one MMA thread; conv3x3Tc stages them with cp.async by all threads; a warp-level mma.sync
+// m16n8k16 version (conv3x3Kernel: 128 x 64 tiles, cp.async + ldmatrix) is kept for
+// comparison. The path is selectable (yg_nn_set_conv_impl). Both epilogues add the bias, apply ReLU or a
 // ReLU-derivative mask, optionally accumulate into the destination, and store BF16. The data
 // gradient is the same kernel on spatially flipped, transposed weights; the weight gradient is
 // a split-K GEMM over pixels (mma.sync) with a deterministic reduction.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -498,6 +501,302 @@ __global__ void __launch_bounds__(128) conv3x3Tc(Act x, const bf16* __restrict__
     }
 }
 
+// ------------------------------------------------------------------ the same convolution fed by TMA
+// Operands arrive by the Tensor Memory Accelerator: one thread (warp 0) is the producer, one
+// (warp 1) issues the MMAs, and the four warps share the epilogue. For every 8-channel group the
+// producer loads the 3 x 130 halo as one 4-D box (channels, x, y, image; out-of-image pixels
+// read as zero) into that group's block of the A buffer, and each tap's weights as one 3-D box
+// (channels, tap, output channel) of NT rows; the stage's "full" mbarrier expects the bytes.
+// The MMA thread waits for "full", issues the block's MMAs and commits them to the stage's
+// "empty" mbarrier, which the producer waits for before reloading the stage. No thread
+// barrier in the main loop. Layouts: A as in conv3x3Tc (groups padded to 128-byte
+// multiples); B group-major, 8-channel group g of a tap at g * NT * 16 bytes (SBO 128,
+// LBO NT * 16).
+template <int KC, int NT>
+struct TmaShape
+{
+    static constexpr int HALO = 130;
+    static constexpr uint32_t A_GROUP = 3u * HALO * 16u;               // bytes the box writes
+    static constexpr uint32_t A_LBO = (A_GROUP + 127u) / 128u * 128u;   // group pitch
+    static constexpr int A_BYTES = (int)A_LBO * (KC / 8);
+    static constexpr int TAP_BYTES = NT * KC * 2;
+    static constexpr int FREE = 200704 - 2 * A_BYTES;
+    static constexpr int TB = 2 * 9 * TAP_BYTES <= FREE ? 9 : (3 * 3 * TAP_BYTES <= FREE ? 3 : 1);
+    static constexpr int B_BYTES = TB * TAP_BYTES;
+    static constexpr int B_STAGES = TB == 9 ? 2 : 3;
+    static constexpr int SMEM = 2 * A_BYTES + B_STAGES * B_BYTES;
+    static constexpr uint32_t TCOLS = NT < 32 ? 32 : NT;
+};
+
+__device__ __forceinline__ void expectTx(uint32_t mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tmaLoad4(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(
+                     dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ void tmaLoad3(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+                     dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(mbar)
+                 : "memory");
+}
+
+template <int KC, int NT>
+__global__ void __launch_bounds__(128) conv3x3Tma(const __grid_constant__ CUtensorMap mapX, const __grid_constant__ CUtensorMap mapW,
+                                                  const float* __restrict__ bias, Act x, Act y, Act mask, int relu,
+                                                  int accumulate, int nImg, int H, int W)
+{
+    using T = TmaShape<KC, NT>;
+    constexpr uint32_t IDESC = idescBf16(128, NT);
+    constexpr int G = KC / 8;                 // 8-channel groups per chunk
+    constexpr int GROUPS = 9 / T::TB;         // K blocks per chunk
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t full[T::B_STAGES], empty[T::B_STAGES], done;
+    __shared__ uint32_t tmemSlot;
+    __shared__ int abortFlag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tilesPerRow = (W + 127) / 128;
+    const int rowTile = blockIdx.x % tilesPerRow;
+    const int rowIdx = blockIdx.x / tilesPerRow;
+    const int img = rowIdx / H, yy0 = rowIdx % H;
+    const int x0 = rowTile * 128;
+    const int n0 = blockIdx.y * NT;
+    const int chunks = (int)x.ch / KC, kBlocks = GROUPS * chunks;
+    const uint32_t sBase = smemAddr(smem);
+    const uint32_t aBuf[2] = {sBase, sBase + T::A_BYTES};
+    const uint32_t bRing = sBase + 2 * T::A_BYTES;
+
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(&tmemSlot)),
+                     "r"(T::TCOLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0)
+    {
+        for (int k = 0; k < T::B_STAGES; ++k)
+        {
+            mbarInit(smemAddr(&full[k]), 1);
+            mbarInit(smemAddr(&empty[k]), 1);
+        }
+        mbarInit(smemAddr(&done), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        abortFlag = 0;
+    }
+    fenceBeforeSync();
+    __syncthreads();
+    fenceAfterSync();
+    const uint32_t tmem = tmemSlot;
+
+    if (warp == 0 && lane == 0)
+    {
+        // producer
+        int last = -1;
+        for (int kb = 0; kb < kBlocks && !abortFlag; ++kb)
+        {
+            const int st = kb % T::B_STAGES, use = kb / T::B_STAGES;
+            if (!mbarWait(smemAddr(&empty[st]), (uint32_t)(use & 1) ^ 1u))
+            {
+                abortFlag = 1;
+                break;
+            }
+            const int c = kb / GROUPS, grp = kb % GROUPS;
+            const uint32_t fb = smemAddr(&full[st]);
+            expectTx(fb, (uint32_t)(T::TB * G * NT * 16) + (grp == 0 ? (uint32_t)(G * T::A_GROUP) : 0u));
+            if (grp == 0)
+                for (int g = 0; g < G; ++g)
+                    tmaLoad4(aBuf[c & 1] + g * T::A_LBO, &mapX, (int)x.off + c * KC + 8 * g, x0 - 1, yy0 - 1, img, fb);
+            const uint32_t sb = bRing + st * T::B_BYTES;
+            for (int t = 0; t < T::TB; ++t)
+                for (int g = 0; g < G; ++g)
+                    tmaLoad3(sb + (t * G + g) * NT * 16, &mapW, c * KC + 8 * g, grp * T::TB + t, n0, fb);
+            last = kb;
+        }
+        // on an abort, let the loads already issued land before the CTA can exit
+        if (abortFlag && last >= 0) mbarWait(smemAddr(&full[last % T::B_STAGES]), (uint32_t)((last / T::B_STAGES) & 1));
+    }
+    else if (warp == 1 && lane == 0)
+    {
+        // MMA issue
+        for (int kb = 0; kb < kBlocks && !abortFlag; ++kb)
+        {
+            const int st = kb % T::B_STAGES, use = kb / T::B_STAGES;
+            if (!mbarWait(smemAddr(&full[st]), (uint32_t)(use & 1)))
+            {
+                abortFlag = 1;
+                break;
+            }
+            fenceAfterSync();
+            const int c = kb / GROUPS, grp = kb % GROUPS;
+            const uint32_t sb = bRing + st * T::B_BYTES;
+#pragma unroll
+            for (int t = 0; t < T::TB; ++t)
+            {
+                const int tap = grp * T::TB + t;
+                const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+                const uint32_t a0 = aBuf[c & 1] + (uint32_t)(((1 + dy) * T::HALO + 1 + dx) * 16);
+                const uint32_t b0 = sb + t * G * NT * 16;
+#pragma unroll
+                for (int kk = 0; kk < KC / 16; ++kk)
+                {
+                    const uint64_t ad = smemDesc(a0 + kk * 2 * T::A_LBO, T::A_LBO, 128);
+                    const uint64_t bd = smemDesc(b0 + kk * 2 * NT * 16, NT * 16, 128);
+                    const uint32_t acc = (kb | t | kk) != 0 ? 1u : 0u;
+                    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                                 "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                                 : "memory");
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smemAddr(&empty[st]))
+                         : "memory");
+        }
+        // completes when every MMA issued above has
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smemAddr(&done))
+                     : "memory");
+    }
+    __syncwarp();
+    const bool ok = mbarWait(smemAddr(&done), 0u);
+    if (__syncthreads_or(!ok || abortFlag))
+    {
+        if (tid == 0) atomicAdd(&g_timeouts, 1u);
+    }
+    else
+    {
+        fenceAfterSync();
+        const int xo = x0 + warp * 32 + lane;
+        const long q = ((long)(img * H + yy0)) * W + xo;
+#pragma unroll 1
+        for (int cc = 0; cc < NT; cc += 16)
+        {
+            uint32_t r[16];
+            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                         : "r"(ta)
+                         : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (xo >= W) continue;
+#pragma unroll
+            for (int j = 0; j < 16; j += 2)
+            {
+                const int co = n0 + cc + j;
+                float v0 = __uint_as_float(r[j]), v1 = __uint_as_float(r[j + 1]);
+                if (bias)
+                {
+                    v0 += bias[co];
+                    v1 += bias[co + 1];
+                }
+                if (relu)
+                {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                }
+                if (mask.p)
+                {
+                    __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask.p + q * mask.stride + mask.off + co);
+                    if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
+                    if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
+                }
+                __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(y.p + q * y.stride + y.off + co);
+                if (accumulate)
+                {
+                    __nv_bfloat162 old = *dst;
+                    v0 += __bfloat162float(old.x);
+                    v1 += __bfloat162float(old.y);
+                }
+                *dst = __floats2bfloat162_rn(v0, v1);
+            }
+        }
+    }
+    fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0)
+    {
+        fenceAfterSync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(T::TCOLS) : "memory");
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                  const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encodeTiled()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried)
+    {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+template <int KC, int NT>
+int launchTma(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate, int n,
+              int h, int wd, cudaStream_t st)
+{
+    using T = TmaShape<KC, NT>;
+    EncodeTiledFn enc = encodeTiled();
+    if (!enc) return YG_ERR_CUDA;
+    alignas(64) CUtensorMap mapX, mapW;
+    // activations: (channels of the buffer, x, y, image); boxes of 8 channels x 130 x 3 x 1
+    const cuuint64_t dimX[4] = {x.stride, (cuuint64_t)wd, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strideX[3] = {(cuuint64_t)x.stride * 2, (cuuint64_t)x.stride * 2 * wd, (cuuint64_t)x.stride * 2 * wd * h};
+    const cuuint32_t boxX[4] = {8, (cuuint32_t)T::HALO, 3, 1};
+    const cuuint32_t ones[4] = {1, 1, 1, 1};
+    if (enc(&mapX, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)x.p, dimX, strideX, boxX, ones, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return YG_ERR_CUDA;
+    // weights [Cout][3][3][Cin]: (input channel, tap, output channel); boxes of 8 x 1 x NT
+    const cuuint64_t dimW[3] = {x.ch, 9, y.ch};
+    const cuuint64_t strideW[2] = {(cuuint64_t)x.ch * 2, (cuuint64_t)x.ch * 2 * 9};
+    const cuuint32_t boxW[3] = {8, 1, (cuuint32_t)NT};
+    if (enc(&mapW, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)w, dimW, strideW, boxW, ones, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return YG_ERR_CUDA;
+    constexpr int floorBytes = 233472 / (512 / (int)T::TCOLS) - 2047;
+    constexpr int smemBytes = T::SMEM > floorBytes ? T::SMEM : floorBytes;
+    static_assert(smemBytes <= 232448, "shared memory");
+    static bool configured = false;
+    if (!configured)
+    {
+        if (cudaFuncSetAttribute(conv3x3Tma<KC, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes) != cudaSuccess)
+            return YG_ERR_CUDA;
+        configured = true;
+    }
+    dim3 grid((unsigned)(n * h * ((wd + 127) / 128)), (unsigned)(y.ch / NT));
+    conv3x3Tma<KC, NT><<<grid, 128, smemBytes, st>>>(mapX, mapW, bias, x, y, m, relu, accumulate, n, h, wd);
+    return YG_OK;
+}
+
+template <int KC>
+int launchTmaN(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate, int n,
+               int h, int wd, cudaStream_t st)
+{
+    const int c = (int)y.ch;
+    if (c % 256 == 0) return launchTma<KC, 256>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    if (c % 128 == 0) return launchTma<KC, 128>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    if (c % 64 == 0) return launchTma<KC, 64>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    if (c % 32 == 0) return launchTma<KC, 32>(x, w, bias, y, m, relu, accumulate, n, h, wd, st);
+    return YG_ERR_INVALID_ARGUMENT;
+}
+
 template <int KC, int NT>
 int launchTc(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate, int n,
              int h, int wd, cudaStream_t st)
@@ -960,7 +1259,7 @@ Act act(const yg_nn_tensor* t)
     a.ch = t ? t->channels : 0;
     return a;
 }
-int g_convImpl = YG_NN_CONV_TCGEN05;
+int g_convImpl = YG_NN_CONV_TCGEN05_TMA;
 
 bool okTensor(const yg_nn_tensor* t)
 {
@@ -979,7 +1278,7 @@ extern "C" {
 
 YG_API int yg_nn_set_conv_impl(int impl)
 {
-    if (impl != YG_NN_CONV_MMA_SYNC && impl != YG_NN_CONV_TCGEN05) return YG_ERR_INVALID_ARGUMENT;
+    if (impl != YG_NN_CONV_MMA_SYNC && impl != YG_NN_CONV_TCGEN05 && impl != YG_NN_CONV_TCGEN05_TMA) return YG_ERR_INVALID_ARGUMENT;
     g_convImpl = impl;
     return YG_OK;
 }
@@ -1000,6 +1299,14 @@ YG_API int yg_nn_conv3x3(const yg_nn_tensor* x, const void* weights, const float
     long P = (long)n * h * w;
     dim3 grid((unsigned)((P + CM - 1) / CM), (unsigned)((y->channels + CN - 1) / CN));
     Act m = act(mask && mask->data ? mask : nullptr);
+    if (g_convImpl == YG_NN_CONV_TCGEN05_TMA)
+    {
+        int r;
+        if (x->channels % 64 == 0) r = tc::launchTmaN<64>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
+        else if (x->channels % 32 == 0) r = tc::launchTmaN<32>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
+        else r = tc::launchTmaN<16>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
+        return r != YG_OK ? r : status(st);
+    }
     if (g_convImpl == YG_NN_CONV_TCGEN05)
     {
         int r;

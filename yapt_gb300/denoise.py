@@ -462,7 +462,8 @@ if __name__ == "__main__":
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--reps", type=int, default=3)
-    ap.add_argument("--impl", default="tcgen05", choices=["tcgen05", "mma_sync"])
+    ap.add_argument("--impl", default="tcgen05_tma", choices=["tcgen05", "tcgen05_tma", "mma_sync"])
     a = ap.parse_args()
-    N.check(N.load().yg_nn_set_conv_impl(N.YG_NN_CONV_TCGEN05 if a.impl == "tcgen05" else N.YG_NN_CONV_MMA_SYNC))
+    impls = {"tcgen05": N.YG_NN_CONV_TCGEN05, "tcgen05_tma": N.YG_NN_CONV_TCGEN05_TMA, "mma_sync": N.YG_NN_CONV_MMA_SYNC}
+    N.check(N.load().yg_nn_set_conv_impl(impls[a.impl]))
     _profile_forward(a.width, a.height, a.reps)
