@@ -513,6 +513,42 @@ def run_denoise(args, world, rank, local):
         # time to the target: the fastest operating point (samples per pixel) that reaches it
         if r <= W["target_relmse"] and (best is None or dt < best["seconds"]):
             best = den_curve[-1]
+    # the reference's own denoiser (edge-stopping a-trous, 5 passes) on the same renders: the
+    # render gathers its features, the filter runs on the device, the image is read back
+    from yapt_gb300 import _native as N
+    from yapt_gb300.runtime import atrous_params
+    ap_ = atrous_params()
+
+    def atrous(spp):
+        torch.cuda.synchronize()
+        t = time.time()
+        ctx.film_clear(EW, EH)
+        ctx.render(ctx.params(W["integrator"], EW, EH, spp_start=0, spp=spp, max_depth=W["max_depth"], lambda_range=lam,
+                              flags=N.YG_FLAG_ATROUS_FEATURES))
+        out, _ = ctx.atrous_denoise(ap_)
+        return out[..., :3] @ D.SRGB_FROM_XYZ.T, time.time() - t
+
+    atrous(8)  # warm-up
+    at_curve, at_best = [], None
+    for spp in (4, 16, 64, 256, 1024):
+        img, dt = atrous(spp)
+        r = D.relmse(img, ref)
+        at_curve.append({"spp": spp, "relmse": r, "seconds": dt})
+        if r <= W["target_relmse"] and (at_best is None or dt < at_best["seconds"]):
+            at_best = at_curve[-1]
+    # filter time alone at 1080p (prefilter + 5 passes), device events
+    ctx.film_clear(EW, EH)
+    ctx.render(ctx.params(W["integrator"], EW, EH, spp=4, max_depth=W["max_depth"], lambda_range=lam,
+                          flags=N.YG_FLAG_ATROUS_FEATURES))
+    a_out = torch.empty((EH, EW, 4), dtype=torch.float32, device="cuda")
+    a_var = torch.empty((EH, EW), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        N.check(ctx.lib.yg_atrous_denoise(ctx.h, ap_, a_out.data_ptr(), a_var.data_ptr()))
+    torch.cuda.synchronize()
+    t = time.time()
+    for _ in range(10):
+        N.check(ctx.lib.yg_atrous_denoise(ctx.h, ap_, a_out.data_ptr(), a_var.data_ptr()))
+    atrous_ms = (time.time() - t) * 1e2
     # network throughput at 1080p (3 forward passes measured above; time one more with events)
     packed = D.to_device_input(net, *D.render_features(ctx, EW, EH, 4, **kw), depth_scale=4.0)
     for _ in range(3):
@@ -541,6 +577,9 @@ def run_denoise(args, world, rank, local):
             "plain": {"spp": spp_plain, "seconds": t_plain, "relmse": r_plain,
                       "curve": [{"spp": s_, "relmse": r_, "seconds": d_} for (s_, r_, d_) in plain_curve]},
             "denoised": {"best": best, "curve": den_curve},
+            "atrous_baseline": {"best": at_best, "curve": at_curve, "filter_ms_1080p": atrous_ms,
+                                "speedup_to_target": (t_plain / at_best["seconds"]) if at_best else None,
+                                "unet_speedup_over_atrous": (at_best["seconds"] / best["seconds"]) if (at_best and best) else None},
             "training": {"data_seconds": data_s, "train_seconds": train_s, "first_loss": float(np.mean(hist[:20])),
                          "last_loss": float(np.mean(hist[-20:]))},
             "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,

@@ -138,6 +138,7 @@ typedef struct yg_camera
 #define YG_FLAG_COUNT_TRAVERSAL (1u << 10) /* count BVH nodes visited / triangles tested (slower) */
 #define YG_FLAG_MEGAKERNEL (1u << 11)      /* one-thread-per-path kernel instead of the wavefront */
 #define YG_FLAG_TIME_KERNELS (1u << 12)    /* time each wavefront kernel kind with CUDA events */
+#define YG_FLAG_ATROUS_FEATURES (1u << 13) /* gather the a-trous denoiser's feature moments and odd-sample film */
 
 typedef struct yg_render_params
 {
@@ -247,6 +248,45 @@ YG_API int yg_film_read(yg_context* ctx, float* xyz_mean, float* counts);
  * with YG_FLAG_FEATURES since the last yg_film_clear. */
 YG_API int yg_film_resolve_device(yg_context* ctx, float* xyz_mean, float* albedo, float* normal, float* depth);
 /* First-hit feature means (YG_FLAG_FEATURES): albedo RGB, normal xyz, depth per pixel. */
+
+/* The reference's edge-stopping a-trous denoiser (CombineSamplesSubStage.cpp:305-313,
+ * 689-698 running prefilterFeatures.comp and denoise.comp; knobs RendererVarsList.h:25-32),
+ * kept as the baseline the learned denoiser is measured against. Defaults are the
+ * reference's: depth sigma scale 0.02, normal sigma 0.06, material sigma 0.05, colour sigma
+ * 3, feature variance scale 1, prefilter on, 5 passes. */
+typedef struct yg_atrous_params
+{
+    float depth_sigma_scale;      /* Denoise.DepthSigmaScale */
+    float normal_sigma;           /* Denoise.NormalSigma */
+    float material_sigma;         /* Denoise.MaterialDifferenceSigma */
+    float color_sigma;            /* Denoise.ColorDifferenceSigma */
+    float feature_variance_scale; /* Denoise.FeatureVarianceScale */
+    uint32_t prefilter;           /* Denoise.FeaturePrefilter: 0 off, 1 on */
+    uint32_t passes;              /* a-trous passes, steps 1, 2, 4, ... (reference: 5) */
+    uint32_t reserved;
+} yg_atrous_params;
+YG_API void yg_atrous_default_params(yg_atrous_params* params);
+/* Denoises the context's film. Every film render since the last yg_film_clear must have
+ * carried YG_FLAG_ATROUS_FEATURES (else YG_ERR_NOT_READY). out_xyzw: DEVICE buffer of
+ * W*H*4 floats (XYZ, 1) and out_variance DEVICE W*H floats; either may be NULL, and the
+ * result then stays in the context for yg_atrous_read. Returns when the output is written. */
+YG_API int yg_atrous_denoise(yg_context* ctx, const yg_atrous_params* params, float* out_xyzw, float* out_variance);
+/* Host copies of the context's a-trous state (any pointer may be NULL): the last
+ * yg_atrous_denoise output kept in the context (W*H*4, W*H), the filter's inputs -- the film's
+ * XYZ sums and counts (W*H float4), the odd-sample XYZ sums and counts (W*H float4), the
+ * gathered feature-moment sums (4 planes of W*H float4: albedo.rgb, |albedo|^2; normal.xyz,
+ * hits; roughness, metalness, transparency, anisotropy; IOR/2, |material|^2 + (IOR/2)^2,
+ * depth, depth^2) -- and the packed prefiltered features (2 planes of W*H uint4, the
+ * reference's two RGBA32_UINT feature textures). Synchronous. */
+YG_API int yg_atrous_read(yg_context* ctx, float* xyzw, float* variance, float* film_sum, float* odd_sum, float* moments,
+                          uint32_t* features);
+/* The same filter on caller data, all HOST buffers of W*H pixels row major (copied to the
+ * device and back inside the call): film_sum XYZ sums and sample count (float4), odd_sum
+ * the odd-indexed samples' XYZ sums and count (float4), moments as for yg_atrous_read;
+ * outputs out_xyzw (W*H*4), out_variance (W*H) and, if not NULL, features_out (2*W*H uint4). */
+YG_API int yg_atrous_run(uint32_t width, uint32_t height, const float* film_sum, const float* odd_sum,
+                         const float* moments, const yg_camera* camera, const yg_atrous_params* params,
+                         float* out_xyzw, float* out_variance, uint32_t* features_out);
 YG_API int yg_features_read(yg_context* ctx, float* albedo, float* normal, float* depth);
 /* relMSE of the film mean against a reference image (host, width*height*3 floats),
  * reduced in FP64 on the device: mean over pixels and channels of

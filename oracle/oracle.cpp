@@ -1699,15 +1699,12 @@ template <typename T> void fillSurf(const Ctx<T>& c, const Spec<T>& s4, uint32_t
     s.sheenColor = s.sheenAmount > T(0) ? setFromRGB(c, s4, v3(T(M.sheen_tint[0]), T(M.sheen_tint[1]), T(M.sheen_tint[2]))) : sp(T(0));
 }
 
-template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P, const uint32_t* point, uint32_t px, uint32_t py,
-                                     float* rec, V3<T>& xyzOut, uint64_t& rays)
+// The hero wavelength and camera ray of a sample (rayGenPrimaryRays.hlsl:13-37,
+// generateCameraRay in raytraceCommonResources.hlsl:113-137); rs starts at dimension 2.
+template <typename T> void cameraSample(const Ctx<T>& c, const yg_render_params& P, uint32_t px, uint32_t py, Sampler& rs,
+                                        Spec<T>& s4, V3<T>& rayO, V3<T>& rayD)
 {
     const oracle_scene* sc = c.sc;
-    LutSet<T> L{{sc->luts[0], sc->luts[1], sc->luts[2], sc->luts[3], sc->luts[4], sc->luts[5], sc->luts[6], sc->luts[7], sc->luts[8]}};
-    uint32_t rayIndex = py * P.width + px;
-    uint32_t seed = rayIndex ^ (P.seed * 0x9E3779B9u);
-    Sampler rs{point, 2u, seed};
-    Spec<T> s4;
     s4.hero = c.lmin + T(rs.r1()) * (c.lmax - c.lmin);
     {
         // getSpectralSampleLambdas (spectralDistribution.hlsl:21-43)
@@ -1748,12 +1745,23 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
     T o4[4] = {lp.x, lp.y, lp.z, T(1)}, d4[4] = {fp.x - lp.x, fp.y - lp.y, fp.z - lp.z, T(0)}, ow[4], dw[4];
     mul44(cam.view_to_world, o4, ow);
     mul44(cam.view_to_world, d4, dw);
+    rayO = v3(ow[0], ow[1], ow[2]);
+    rayD = normalize(v3(dw[0], dw[1], dw[2]));
+}
 
+template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P, const uint32_t* point, uint32_t px, uint32_t py,
+                                     float* rec, V3<T>& xyzOut, uint64_t& rays)
+{
+    const oracle_scene* sc = c.sc;
+    LutSet<T> L{{sc->luts[0], sc->luts[1], sc->luts[2], sc->luts[3], sc->luts[4], sc->luts[5], sc->luts[6], sc->luts[7], sc->luts[8]}};
+    uint32_t rayIndex = py * P.width + px;
+    uint32_t seed = rayIndex ^ (P.seed * 0x9E3779B9u);
+    Sampler rs{point, 2u, seed};
+    Spec<T> s4;
     Path<T> ps;
+    cameraSample(c, P, px, py, rs, s4, ps.o, ps.d);
     ps.thr = sp(T(1));
     ps.total = sp(T(0));
-    ps.o = v3(ow[0], ow[1], ow[2]);
-    ps.d = normalize(v3(dw[0], dw[1], dw[2]));
     ps.pdfRay = 0;
     ps.flags = 0;
     ps.len = 0;
@@ -2059,6 +2067,7 @@ template <typename T> int run(const oracle_scene* sc, const yg_render_params* P,
 }
 
 #include "oracle_bdpt.inc"
+#include "oracle_atrous.inc"
 
 } // namespace orc
 
@@ -2077,6 +2086,24 @@ int oracle_render(const oracle_scene* sc, const yg_render_params* P, int precisi
     }
     if (precision == 64) return orc::run<double>(sc, P, threads, records, film, stats);
     return orc::run<float>(sc, P, threads, records, film, stats);
+}
+
+int oracle_atrous_moments(const oracle_scene* sc, const yg_render_params* P, int threads, float* moments)
+{
+    if (!sc || !P || !moments) return -1;
+    if (!sc->rgb_to_spd && orc::needsRgbTable(sc, P)) return -6;
+    return orc::gatherMoments(sc, P, threads, moments);
+}
+
+int oracle_atrous(uint32_t width, uint32_t height, const float* film_sum, const float* odd_sum, const float* moments,
+                  const yg_camera* camera, const yg_atrous_params* params, int threads, float* out_xyzw, float* out_variance,
+                  uint32_t* features)
+{
+    if (!film_sum || !odd_sum || !moments || !camera || !params || !out_xyzw || !out_variance || !width || !height) return -1;
+    orc::ASettings A{params->depth_sigma_scale, params->normal_sigma, params->material_sigma, params->color_sigma,
+                     params->feature_variance_scale, params->prefilter != 0, params->passes};
+    orc::atrousFilter(width, height, film_sum, odd_sum, moments, *camera, A, threads, out_xyzw, out_variance, features);
+    return 0;
 }
 
 int oracle_sobol_matrices(const char* dir, uint32_t* out)

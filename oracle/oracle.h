@@ -69,6 +69,15 @@ int oracle_render(const oracle_scene* scene, const yg_render_params* params, int
 /* Sobol generator matrices derived here from the Joe-Kuo file (256 x 32 uint32). */
 int oracle_sobol_matrices(const char* data_dir, uint32_t* out);
 
+/* The a-trous denoiser (the reference's baseline denoiser), FP32 in the device order.
+ * oracle_atrous_moments adds the first-camera-vertex feature moments of every sample of the
+ * request onto `moments` (4 planes of width*height float4, layout of yg_atrous_read).
+ * oracle_atrous runs the prefilter and the passes on the same inputs as yg_atrous_run. */
+int oracle_atrous_moments(const oracle_scene* scene, const yg_render_params* params, int threads, float* moments);
+int oracle_atrous(uint32_t width, uint32_t height, const float* film_sum, const float* odd_sum, const float* moments,
+                  const yg_camera* camera, const yg_atrous_params* params, int threads, float* out_xyzw,
+                  float* out_variance, uint32_t* features);
+
 /* Per-function checks (BSDF known-answer tests): evaluate a material at (wo, wi) for
  * the given hero wavelength; returns weight[4] and pdf. Object space, normal (0,1,0). */
 int oracle_eval_bsdf(const oracle_scene* scene, uint32_t material, float hero, const float* wo, const float* wi,

@@ -55,6 +55,11 @@ def load():
         lib.oracle_render.restype = C.c_int
         lib.oracle_render.argtypes = [C.POINTER(OracleScene), C.POINTER(N.RenderParams), C.c_int, C.c_int, C.c_void_p,
                                       C.c_void_p, C.POINTER(OracleStats)]
+        lib.oracle_atrous_moments.restype = C.c_int
+        lib.oracle_atrous_moments.argtypes = [C.POINTER(OracleScene), C.POINTER(N.RenderParams), C.c_int, C.c_void_p]
+        lib.oracle_atrous.restype = C.c_int
+        lib.oracle_atrous.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(N.Camera),
+                                      C.POINTER(N.AtrousParams), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.oracle_sobol_matrices.restype = C.c_int
         lib.oracle_sobol_matrices.argtypes = [C.c_char_p, C.c_void_p]
         _lib = lib
@@ -132,6 +137,33 @@ class OracleSceneHandle:
         if rc != 0:
             raise RuntimeError("oracle_render failed: %d" % rc)
         return dict(records=rec, film=fil, rays=st.rays, seconds=st.seconds)
+
+    def atrous_moments(self, params, moments, threads=None):
+        """Adds the first-camera-vertex feature moments of the request's samples onto
+        `moments` (float32 (4, H, W, 4), layout of yg_atrous_read), in sample order."""
+        assert moments.dtype == np.float32 and moments.flags.c_contiguous
+        assert moments.shape == (4, params.height, params.width, 4)
+        rc = load().oracle_atrous_moments(C.byref(self.s), C.byref(params), threads or os.cpu_count() or 1,
+                                          moments.ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise RuntimeError("oracle_atrous_moments failed: %d" % rc)
+        return moments
+
+
+def atrous(film_sum, odd_sum, moments, camera, params, threads=None):
+    """The a-trous filter on float32 arrays film_sum/odd_sum (H, W, 4) and moments
+    (4, H, W, 4); returns (xyzw (H, W, 4), variance (H, W), features (2, H, W, 4) uint32)."""
+    h, w = film_sum.shape[:2]
+    f = [np.ascontiguousarray(a, np.float32) for a in (film_sum, odd_sum, moments)]
+    out = np.zeros((h, w, 4), np.float32)
+    var = np.zeros((h, w), np.float32)
+    feat = np.zeros((2, h, w, 4), np.uint32)
+    rc = load().oracle_atrous(w, h, *[a.ctypes.data_as(C.c_void_p) for a in f], C.byref(camera), C.byref(params),
+                              threads or os.cpu_count() or 1, out.ctypes.data_as(C.c_void_p),
+                              var.ctypes.data_as(C.c_void_p), feat.ctypes.data_as(C.c_void_p))
+    if rc != 0:
+        raise RuntimeError("oracle_atrous failed: %d" % rc)
+    return out, var, feat
 
 
 def luts_from_context(ctx):

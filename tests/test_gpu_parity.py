@@ -86,6 +86,30 @@ def test_rgb_colours_and_environment_use_the_spectral_fit(host_luts, built):
         compare(gpu, orc)
 
 
+@pytest.mark.parametrize("integrator", ["uni", "nee", "bdpt"])
+def test_layered_materials_per_sample(integrator, host_luts, built):
+    """Sheen, clear coat over plastic, anisotropic metal with a rotated tangent frame and a
+    thin film under a clear coat: every layer of the principled BSDF, per sample."""
+    import pyoracle
+    from yapt_gb300 import _native as N
+    sc = configs.layered_box_scene(4)
+    p = Context.params(integrator, 48, 40, spp=4, max_depth=8, lambda_range=(380, 780), flags=256,
+                       light_vertices=8 if integrator == "bdpt" else 0)
+    with Context(0) as c:
+        c.upload_scene(sc)
+        gpu = c.render(p, dump=True)
+        c.upload_scene(configs.box_scene(4))
+        plain = c.render(p, dump=True)
+    rgb = N.host_table("rgb_to_spd", (380, 780))  # sheen tint and specular colours are RGB
+    orc = pyoracle.OracleSceneHandle(sc, host_luts, rgb).render(p, precision=32)["records"]
+    compare(gpu, orc, min_within=0.999)
+    if integrator == "bdpt":  # the light-tracing splats land in XYZ
+        rel = np.abs(gpu[..., 5:8] - orc[..., 5:8]) / np.maximum(np.abs(orc[..., 5:8]), 1e-6)
+        assert float(np.mean(np.all(rel <= REL_TOL, axis=-1))) >= 0.999
+    # the layers change the image: a large share of samples differ from the plain box
+    assert float(np.mean(np.any(gpu[..., 1:5] != plain[..., 1:5], axis=-1))) > 0.2
+
+
 def test_film_is_the_ordered_mean_of_the_samples(host_luts, built):
     with Context(0) as c:
         sc = configs.box_scene(0)

@@ -22,6 +22,7 @@ YG_FLAG_FEATURES = 1 << 9
 YG_FLAG_COUNT_TRAVERSAL = 1 << 10
 YG_FLAG_MEGAKERNEL = 1 << 11
 YG_FLAG_TIME_KERNELS = 1 << 12
+YG_FLAG_ATROUS_FEATURES = 1 << 13
 YG_NN_CONV_MMA_SYNC = 0
 YG_NN_CONV_TCGEN05 = 1
 YG_NN_CONV_TCGEN05_TMA = 2
@@ -73,6 +74,14 @@ class Camera(C.Structure):
         ("world_to_view", C.c_float * 16), ("view_to_world", C.c_float * 16),
         ("aperture_radius", C.c_float), ("focus_distance", C.c_float),
         ("view_forward_z_sign", C.c_float), ("reserved", C.c_float),
+    ]
+
+
+class AtrousParams(C.Structure):
+    _fields_ = [
+        ("depth_sigma_scale", C.c_float), ("normal_sigma", C.c_float), ("material_sigma", C.c_float),
+        ("color_sigma", C.c_float), ("feature_variance_scale", C.c_float), ("prefilter", C.c_uint32),
+        ("passes", C.c_uint32), ("reserved", C.c_uint32),
     ]
 
 
@@ -159,6 +168,11 @@ SIGNATURES = [
     ("yg_upload_mesh", C.c_int, [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(C.c_uint32)]),
     ("yg_clear_meshes", C.c_int, [C.c_void_p]),
     ("yg_film_resolve_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("yg_atrous_default_params", None, [C.POINTER(AtrousParams)]),
+    ("yg_atrous_denoise", C.c_int, [C.c_void_p, C.POINTER(AtrousParams), C.c_void_p, C.c_void_p]),
+    ("yg_atrous_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("yg_atrous_run", C.c_int, [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Camera),
+                                C.POINTER(AtrousParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("yg_nn_set_conv_impl", C.c_int, [C.c_int]),
     ("yg_nn_tc_timeouts", C.c_int, [C.POINTER(C.c_uint32)]),
     ("yg_nn_tile_error", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,

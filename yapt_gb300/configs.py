@@ -160,6 +160,27 @@ def box_scene(seed=0, light_intensity=12.0, aspect=1.0):
     return sc
 
 
+def layered_box_scene(seed=0, light_intensity=12.0, aspect=1.0):
+    """``box_scene`` with the principled BSDF's layered lobes switched on: a sheen floor, a
+    clear-coated plastic back wall, a brushed (anisotropic, rotated tangent frame) metal
+    block and a clear-coated metal block under a thin film, so that every layer of the
+    reference's BSDF (Shaders/Bsdfs/layeredBsdf.hlsl, miscBrdf.hlsl, thinFilm.hlsl) carries
+    energy into the image. Materials 0..4 are the walls, 5 and 6 the blocks, 7 the light."""
+    sc = box_scene(seed, light_intensity, aspect)
+    sc.name = "layered_box(seed=%d)" % seed
+    m = sc.materials
+    m[0].update(sheen_amount=0.8, sheen_tint=(0.9, 0.6, 0.3), sheen_roughness=0.35)
+    m[2].update(clear_coat_amount=1.0, clear_coat_ior=1.6, clear_coat_roughness=0.05, roughness=0.6)
+    m[5].update(metalness=1.0, roughness=0.35, specular=(0.95, 0.8, 0.6), specular_amount=1.0,
+                anisotropy=0.7, anisotropy_rotation=0.2)
+    m[6].update(metalness=1.0, roughness=0.2, specular=(0.9, 0.9, 0.9), specular_amount=1.0,
+                clear_coat_amount=1.0, clear_coat_ior=1.45, clear_coat_roughness=0.1, thin_film_thickness_nm=420.0)
+    # the blocks need tangents for the anisotropic lobe: one per vertex along the mesh's +x
+    cube = sc.meshes[sc.instances[5][1]]
+    cube["tangents"] = np.tile(np.float32([1, 0, 0, 1]), (len(cube["positions"]), 1))
+    return sc
+
+
 def random_shapes_scene(seed=0, n_spheres=500, light_intensity=25.0, aspect=1.0):
     rng = np.random.Generator(np.random.PCG64(seed))
     sc = Scene()

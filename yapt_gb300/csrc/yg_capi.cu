@@ -806,6 +806,7 @@ YG_API int yg_film_clear(yg_context* ctx, uint32_t w, uint32_t h)
     YG_CUDA(cudaMemsetAsync(ctx->dAccN.p, 0, bytes, ctx->stream));
     ctx->filmW = w;
     ctx->filmH = h;
+    ctx->atrousState = 0;
     return YG_OK;
 }
 
@@ -864,6 +865,24 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         }
     }
     bool feats = (p->flags & YG_FLAG_FEATURES) != 0;
+    const bool atrous = (p->flags & YG_FLAG_ATROUS_FEATURES) != 0;
+    if (atrous && !film) return fail(YG_ERR_INVALID_ARGUMENT, "render: YG_FLAG_ATROUS_FEATURES needs the film");
+    if (film)
+    {
+        const size_t plane = (size_t)p->width * p->height;
+        if (atrous)
+        {
+            YG_CUDA(ctx->dAtrousMom.ensure(4 * plane * sizeof(float4)));
+            YG_CUDA(ctx->dAtrousOdd.ensure(plane * sizeof(float4)));
+            if (ctx->atrousState == 0)
+            {
+                YG_CUDA(cudaMemsetAsync(ctx->dAtrousMom.p, 0, 4 * plane * sizeof(float4), ctx->stream));
+                YG_CUDA(cudaMemsetAsync(ctx->dAtrousOdd.p, 0, plane * sizeof(float4), ctx->stream));
+            }
+        }
+        const int st = atrous ? 1 : 2;
+        ctx->atrousState = (ctx->atrousState == 0 || ctx->atrousState == st) ? st : 3;
+    }
     YG_CUDA(ctx->dSamples.ensure(npix * chunkSpp * sizeof(float4)));
     if (feats)
     {
@@ -947,6 +966,9 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         if (film)
             launches += yg::launchFilm(ctx->dFilmSum.as<float4>(), ctx->dFilmComp.as<float4>(), L.sampleXYZ, p->width, cx,
                                        cy, cw, ch, ns, ctx->smCount, ctx->stream);
+        if (film && atrous)
+            launches += yg::launchAtrousGather(S, L, ctx->dAtrousMom.as<float4>(), ctx->dAtrousOdd.as<float4>(), L.sampleXYZ, ns,
+                                               ctx->smCount, ctx->stream);
         if (film && feats)
             launches += yg::launchFeatures(ctx->dAccA.as<float4>(), ctx->dAccN.as<float4>(), L.featAlbedo, L.featNormalDepth,
                                            p->width, cx, cy, cw, ch, ns, ctx->smCount, ctx->stream);
@@ -1056,6 +1078,168 @@ YG_API int yg_film_resolve_device(yg_context* ctx, float* xyz, float* albedo, fl
                           depth, ctx->smCount, ctx->stream);
     YG_CUDA(cudaGetLastError());
     YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return YG_OK;
+}
+
+YG_API void yg_atrous_default_params(yg_atrous_params* p)
+{
+    if (!p) return;
+    p->depth_sigma_scale = 0.02f;
+    p->normal_sigma = 0.06f;
+    p->material_sigma = 0.05f;
+    p->color_sigma = 3.0f;
+    p->feature_variance_scale = 1.0f;
+    p->prefilter = 1;
+    p->passes = 5;
+    p->reserved = 0;
+}
+
+extern "C++"
+{
+namespace
+{
+int atrousSettings(const yg_atrous_params* p, yg::AtrousSettings& A)
+{
+    if (!p) return fail(YG_ERR_INVALID_ARGUMENT, "a-trous: null parameters");
+    const float v[5] = {p->depth_sigma_scale, p->normal_sigma, p->material_sigma, p->color_sigma, p->feature_variance_scale};
+    for (int i = 0; i < 5; ++i)
+        if (!(v[i] >= 0.0f) || !std::isfinite(v[i])) return fail(YG_ERR_INVALID_ARGUMENT, "a-trous: sigmas must be finite and >= 0");
+    if (p->passes > 12) return fail(YG_ERR_INVALID_ARGUMENT, "a-trous: at most 12 passes");
+    A = yg::AtrousSettings{p->depth_sigma_scale, p->normal_sigma, p->material_sigma, p->color_sigma, p->feature_variance_scale,
+                           p->prefilter ? 1u : 0u, p->passes};
+    return YG_OK;
+}
+
+void atrousCamera(const float* uvToView, const float* viewToWorld, uint32_t w, uint32_t h, yg::AtrousBuffers& B)
+{
+    B.width = w;
+    B.height = h;
+    B.invW = 1.0f / (float)w;
+    B.invH = 1.0f / (float)h;
+    std::memcpy(B.uvToView, uvToView, sizeof(B.uvToView));
+    std::memcpy(B.viewToWorld, viewToWorld, sizeof(B.viewToWorld));
+}
+} // namespace
+}
+
+YG_API int yg_atrous_denoise(yg_context* ctx, const yg_atrous_params* params, float* out_xyzw, float* out_variance)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "a-trous: null context");
+    yg::AtrousSettings A;
+    int r = atrousSettings(params, A);
+    if (r) return r;
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t n = (size_t)ctx->filmW * ctx->filmH;
+    if (n == 0) return fail(YG_ERR_NOT_READY, "a-trous: film not allocated");
+    if (ctx->atrousState != 1)
+        return fail(YG_ERR_NOT_READY, "a-trous: every film render since yg_film_clear needs YG_FLAG_ATROUS_FEATURES");
+    if (!ctx->cameraSet) return fail(YG_ERR_NOT_READY, "a-trous: camera not set");
+    cudaSetDevice(ctx->device);
+    // planes: colour and variance ping-pong [0], [1] and the kept output [2]
+    YG_CUDA(ctx->dAtrousFeat.ensure(2 * n * sizeof(uint4)));
+    YG_CUDA(ctx->dAtrousCol.ensure(3 * n * sizeof(float4)));
+    YG_CUDA(ctx->dAtrousVar.ensure(3 * n * sizeof(float)));
+    yg::AtrousBuffers B;
+    atrousCamera(ctx->camera.uvToView, ctx->camera.viewToWorld, ctx->filmW, ctx->filmH, B);
+    B.film = ctx->dFilmSum.as<float4>();
+    B.odd = ctx->dAtrousOdd.as<float4>();
+    B.moments = ctx->dAtrousMom.as<float4>();
+    B.feat0 = ctx->dAtrousFeat.as<uint4>();
+    B.feat1 = B.feat0 + n;
+    B.colour[0] = ctx->dAtrousCol.as<float4>();
+    B.colour[1] = B.colour[0] + n;
+    B.variance[0] = ctx->dAtrousVar.as<float>();
+    B.variance[1] = B.variance[0] + n;
+    float4* oc = out_xyzw ? reinterpret_cast<float4*>(out_xyzw) : B.colour[0] + 2 * n;
+    float* ov = out_variance ? out_variance : B.variance[0] + 2 * n;
+    yg::launchAtrous(B, A, oc, ov, ctx->stream);
+    YG_CUDA(cudaGetLastError());
+    if (out_xyzw && !out_variance)
+    {
+        // keep the context's copy complete for yg_atrous_read
+        YG_CUDA(cudaMemcpyAsync(B.colour[0] + 2 * n, oc, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    else if (out_xyzw)
+    {
+        YG_CUDA(cudaMemcpyAsync(B.colour[0] + 2 * n, oc, n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+        YG_CUDA(cudaMemcpyAsync(B.variance[0] + 2 * n, ov, n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    else if (out_variance)
+    {
+        YG_CUDA(cudaMemcpyAsync(B.variance[0] + 2 * n, ov, n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return YG_OK;
+}
+
+YG_API int yg_atrous_read(yg_context* ctx, float* xyzw, float* variance, float* film_sum, float* odd_sum, float* moments,
+                          uint32_t* features)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "a-trous read: null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t n = (size_t)ctx->filmW * ctx->filmH;
+    if (n == 0) return fail(YG_ERR_NOT_READY, "a-trous read: film not allocated");
+    if ((moments || odd_sum) && ctx->atrousState != 1)
+        return fail(YG_ERR_NOT_READY, "a-trous read: no complete gather since yg_film_clear");
+    if ((xyzw || variance || features) && ctx->dAtrousCol.bytes < 3 * n * sizeof(float4))
+        return fail(YG_ERR_NOT_READY, "a-trous read: call yg_atrous_denoise first");
+    cudaSetDevice(ctx->device);
+    auto d2h = [&](void* dst, const void* src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    };
+    if (xyzw) YG_CUDA(d2h(xyzw, ctx->dAtrousCol.as<float4>() + 2 * n, n * sizeof(float4)));
+    if (variance) YG_CUDA(d2h(variance, ctx->dAtrousVar.as<float>() + 2 * n, n * sizeof(float)));
+    if (film_sum) YG_CUDA(d2h(film_sum, ctx->dFilmSum.p, n * sizeof(float4)));
+    if (moments) YG_CUDA(d2h(moments, ctx->dAtrousMom.p, 4 * n * sizeof(float4)));
+    if (odd_sum) YG_CUDA(d2h(odd_sum, ctx->dAtrousOdd.p, n * sizeof(float4)));
+    if (features) YG_CUDA(d2h(features, ctx->dAtrousFeat.p, 2 * n * sizeof(uint4)));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return YG_OK;
+}
+
+YG_API int yg_atrous_run(uint32_t width, uint32_t height, const float* film_sum, const float* odd_sum, const float* moments,
+                         const yg_camera* camera, const yg_atrous_params* params, float* out_xyzw, float* out_variance,
+                         uint32_t* features_out)
+{
+    if (!film_sum || !odd_sum || !moments || !camera || !out_xyzw || !out_variance)
+        return fail(YG_ERR_INVALID_ARGUMENT, "a-trous: null argument");
+    if (width == 0 || height == 0) return fail(YG_ERR_INVALID_ARGUMENT, "a-trous: empty image");
+    yg::AtrousSettings A;
+    int r = atrousSettings(params, A);
+    if (r) return r;
+    const size_t n = (size_t)width * height;
+    yg::AtrousBuffers B;
+    atrousCamera(camera->uv_to_view, camera->view_to_world, width, height, B);
+    // device layout: film, odd, 4 moment planes, 3 colour planes (float4); 2 feature planes
+    // (uint4); 3 variance planes (float)
+    const size_t f4 = n * sizeof(float4);
+    void* mem = nullptr;
+    YG_CUDA(cudaMalloc(&mem, 9 * f4 + 2 * n * sizeof(uint4) + 3 * n * sizeof(float)));
+    float4* base = static_cast<float4*>(mem);
+    cudaError_t e = cudaMemcpy(base, film_sum, f4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(base + n, odd_sum, f4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(base + 2 * n, moments, 4 * f4, cudaMemcpyHostToDevice);
+    B.film = base;
+    B.odd = base + n;
+    B.moments = base + 2 * n;
+    B.colour[0] = base + 6 * n;
+    B.colour[1] = base + 7 * n;
+    float4* oc = base + 8 * n;
+    B.feat0 = reinterpret_cast<uint4*>(base + 9 * n);
+    B.feat1 = B.feat0 + n;
+    B.variance[0] = reinterpret_cast<float*>(B.feat1 + n);
+    B.variance[1] = B.variance[0] + n;
+    float* ov = B.variance[1] + n;
+    if (e == cudaSuccess)
+    {
+        yg::launchAtrous(B, A, oc, ov, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out_xyzw, oc, f4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_variance, ov, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && features_out) e = cudaMemcpy(features_out, B.feat0, 2 * n * sizeof(uint4), cudaMemcpyDeviceToHost);
+    cudaFree(mem);
+    if (e != cudaSuccess) return fail(YG_ERR_CUDA, std::string("a-trous: ") + cudaGetErrorString(e));
     return YG_OK;
 }
 

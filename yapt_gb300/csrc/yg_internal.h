@@ -106,6 +106,7 @@ struct yg_context
     DevBuf dLut[9];
     DevBuf dCie, dRgb, dSobol, dSobolMat, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
     DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena, dPerm;
+    DevBuf dAtrousMom, dAtrousOdd, dAtrousFeat, dAtrousCol, dAtrousVar; // a-trous denoiser state
     uint32_t nLights = 0;
     float worldCenter[3] = {0, 0, 0}; // getWorldCenterAndRadiusSqr (raytraceCommonResources.hlsl:99-104)
     float worldRadiusSqr = 0;
@@ -115,6 +116,9 @@ struct yg_context
     float cieYSumInv = 0, d65SumInv = 0;
     uint32_t filmW = 0, filmH = 0;
     bool featuresOn = false;
+    // a-trous gather over the film renders since yg_film_clear: 0 none yet, 1 all gathered,
+    // 2 none gathered, 3 mixed
+    int atrousState = 0;
     // stats
     float lastMs = 0;
     uint64_t lastRays = 0;
@@ -124,7 +128,8 @@ struct yg_context
     {
         DevBuf* all[] = {&dTris, &dNodes, &dInst, &dMat, &dLights, &dPos, &dNrm, &dTan, &dUV, &dIdx, &dSpec, &dCie, &dRgb,
                          &dSobol, &dSobolMat, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
-                         &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm};
+                         &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm, &dAtrousMom, &dAtrousOdd,
+                         &dAtrousFeat, &dAtrousCol, &dAtrousVar};
         for (DevBuf* b : all) b->release();
         for (auto& b : dLut) b.release();
         for (cudaEvent_t e : kernelEvents) cudaEventDestroy(e);

@@ -75,6 +75,28 @@ int launchFilmResolve(const float4* sum, const float4* accA, const float4* accN,
                       float* normal, float* depth, int smCount, cudaStream_t stream);
 int launchRelmse(const float4* sum, const float* ref, uint32_t npix, double eps, double* out, int smCount,
                  cudaStream_t stream);
+// Edge-stopping a-trous denoiser (the reference's denoiser, kept as a baseline).
+struct AtrousSettings
+{
+    float depthSigmaScale, normalSigma, materialSigma, colorSigma, featureVarianceScale;
+    uint32_t prefilter, passes;
+};
+struct AtrousBuffers
+{
+    uint32_t width, height;
+    float invW, invH;
+    float uvToView[16], viewToWorld[16]; // row-major camera matrices
+    const float4* film;    // [pixel] XYZ sums and sample count
+    const float4* odd;     // [pixel] XYZ sums and count of the odd-indexed samples
+    const float4* moments; // [4][pixel] feature moment sums
+    uint4* feat0;          // [pixel] packed prefiltered features, two halves
+    uint4* feat1;
+    float4* colour[2];     // ping-pong colour planes; [0] receives the merged input colour
+    float* variance[2];
+};
+int launchAtrousGather(const SceneView& S, const LaunchParams& P, float4* moments, float4* odd, const float4* samples,
+                       uint32_t nspp, int smCount, cudaStream_t stream);
+int launchAtrous(const AtrousBuffers& B, const AtrousSettings& A, float4* outColour, float* outVar, cudaStream_t stream);
 // Merged wavefront of several requests (serving). All tables live in device memory and are
 // read by the kernels, so a captured launch sequence can be replayed round after round.
 struct MultiTables

@@ -101,6 +101,30 @@ class Context:
                                       cnt.ctypes.data_as(C.POINTER(C.c_float))))
         return xyz, cnt
 
+    def atrous_denoise(self, params=None):
+        """Runs the a-trous denoiser on the film (every film render since film_clear must
+        carry YG_FLAG_ATROUS_FEATURES); returns (xyzw (H, W, 4), variance (H, W))."""
+        p = params or atrous_params()
+        N.check(self.lib.yg_atrous_denoise(self.h, C.byref(p), None, None))
+        out = np.zeros((self.height, self.width, 4), np.float32)
+        var = np.zeros((self.height, self.width), np.float32)
+        N.check(self.lib.yg_atrous_read(self.h, out.ctypes.data_as(C.c_void_p), var.ctypes.data_as(C.c_void_p),
+                                        None, None, None, None))
+        return out, var
+
+    def atrous_state(self, features=False):
+        """The filter's inputs gathered on the device: film sums, odd-sample sums (H, W, 4),
+        moment sums (4, H, W, 4) and, after atrous_denoise, the packed features (2, H, W, 4)."""
+        H, W = self.height, self.width
+        film = np.zeros((H, W, 4), np.float32)
+        odd = np.zeros((H, W, 4), np.float32)
+        mom = np.zeros((4, H, W, 4), np.float32)
+        feat = np.zeros((2, H, W, 4), np.uint32) if features else None
+        N.check(self.lib.yg_atrous_read(self.h, None, None, film.ctypes.data_as(C.c_void_p), odd.ctypes.data_as(C.c_void_p),
+                                        mom.ctypes.data_as(C.c_void_p),
+                                        feat.ctypes.data_as(C.c_void_p) if feat is not None else None))
+        return dict(film=film, odd=odd, moments=mom, features=feat)
+
     def features(self):
         a = np.zeros((self.height, self.width, 3), np.float32)
         n = np.zeros((self.height, self.width, 3), np.float32)
@@ -255,3 +279,29 @@ def plan_round(items, budget_bytes, bytes_in_use=0, max_active=64, wave_capacity
     if total < 0:
         raise N.YaptError(lib.yg_last_error().decode())
     return [int(adm[i]) for i in range(n)], [int(pl[i]) for i in range(n)], int(total)
+
+
+def atrous_params(**kw):
+    """yg_atrous_params with the reference's defaults, overridden by keyword."""
+    p = N.AtrousParams()
+    N.load().yg_atrous_default_params(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise ValueError("unknown a-trous parameter %r" % k)
+        setattr(p, k, v)
+    return p
+
+
+def atrous_run(film_sum, odd_sum, moments, camera, params=None):
+    """The a-trous filter on host arrays through the C ABI (yg_atrous_run): film_sum, odd_sum
+    (H, W, 4) and moments (4, H, W, 4) float32 -> (xyzw, variance, features)."""
+    h, w = film_sum.shape[:2]
+    f = [np.ascontiguousarray(a, np.float32) for a in (film_sum, odd_sum, moments)]
+    out = np.zeros((h, w, 4), np.float32)
+    var = np.zeros((h, w), np.float32)
+    feat = np.zeros((2, h, w, 4), np.uint32)
+    p = params or atrous_params()
+    N.check(N.load().yg_atrous_run(w, h, *[a.ctypes.data_as(C.c_void_p) for a in f], C.byref(camera), C.byref(p),
+                                   out.ctypes.data_as(C.c_void_p), var.ctypes.data_as(C.c_void_p),
+                                   feat.ctypes.data_as(C.c_void_p)))
+    return out, var, feat
