@@ -140,6 +140,26 @@ typedef struct yg_camera
 #define YG_FLAG_TIME_KERNELS (1u << 12)    /* time each wavefront kernel kind with CUDA events */
 #define YG_FLAG_ATROUS_FEATURES (1u << 13) /* gather the a-trous denoiser's feature moments and odd-sample film */
 
+/* Punctual lights (PunctualLightParameters; LightEntryGPU in materialsCommonResources.hlsl):
+ * point and spot lights emit RGB intensity from a position (spot: within the cone of
+ * direction, full inside cos_inner, smoothstep to zero at cos_outer); a directional light
+ * delivers RGB irradiance travelling along direction. They have no geometry: BSDF
+ * sampling never hits them, so they are sampled explicitly by every integrator (uni: the
+ * punctual lights only; NEE: all lights). */
+#define YG_LIGHT_POINT 1
+#define YG_LIGHT_SPOT 2
+#define YG_LIGHT_DIRECTIONAL 3
+typedef struct yg_punctual_light
+{
+    uint32_t type;       /* YG_LIGHT_* */
+    float position[3];   /* world space (point, spot) */
+    float direction[3];  /* world space, direction of emission (spot axis, directional); normalised on upload */
+    float intensity[3];  /* RGB */
+    float cos_inner;     /* spot: cosine of the inner (full intensity) angle */
+    float cos_outer;     /* spot: cosine of the outer (zero intensity) angle */
+    float reserved[2];
+} yg_punctual_light;
+
 typedef struct yg_render_params
 {
     uint32_t integrator; /* YG_INTEGRATOR_* */
@@ -220,6 +240,9 @@ YG_API int yg_upload_materials(yg_context* ctx, const yg_material* materials, ui
 YG_API int yg_upload_spectra(yg_context* ctx, const float* values, uint32_t n_curves, uint32_t n_points,
                              float lambda_min, float lambda_max);
 YG_API int yg_set_instances(yg_context* ctx, const yg_instance* instances, uint32_t count);
+/* Replaces the punctual lights (count 0 removes them). The light tables are rebuilt at once
+ * when the scene is built, else by yg_build_scene. */
+YG_API int yg_set_punctual_lights(yg_context* ctx, const yg_punctual_light* lights, uint32_t count);
 YG_API int yg_set_camera(yg_context* ctx, const yg_camera* camera);
 /* Builds the acceleration structure and the light tables (alias tables over mesh
  * lights, RaytraceCommonResources.cpp:325-547) for the current meshes/instances/materials. */

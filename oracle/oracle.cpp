@@ -296,7 +296,13 @@ struct Ctx
         uint32_t inst;
         float pdf, thr;
         uint32_t alias;
+        // punctual lights (type != 0): their own table over the punctual lights alone
+        uint32_t type;
+        float ppdf, pthr;
+        uint32_t palias;
+        float pos[3], dir[3], inten[3], cosIn, cosOut;
     };
+    uint32_t nPunctual = 0;
     std::vector<Light> lights;
     std::vector<float> instLightPdf;
     // world triangles and BVH
@@ -1492,19 +1498,43 @@ template <typename T> bool setup(Ctx<T>& c, const oracle_scene* sc, const Tables
             lightInst.push_back(i);
         }
     }
-    if (!lightInst.empty())
+    if (c.tris.empty())
+        for (int k = 0; k < 3; ++k) c.wlo[k] = c.whi[k] = 0.0f;
+    // punctual lights after the mesh lights (uploadLightData, RaytraceCommonResources.cpp:426-543),
+    // power of estimatePunctualLightPower (:407-424)
+    std::vector<float> pun;
+    for (uint32_t i = 0; i < sc->n_punctual; ++i)
     {
-        // calculateSelectionPDFs + buildAliasTable (RaytraceCommonResources.cpp:325-383)
-        size_t cnt = power.size();
+        const yg_punctual_light& L = sc->punctual[i];
+        float in = 0.2126f * L.intensity[0] + 0.7152f * L.intensity[1] + 0.0722f * L.intensity[2];
+        const float pi = 3.14159274f;
+        float pw;
+        if (L.type == YG_LIGHT_POINT)
+            pw = 4.f * pi * in;
+        else if (L.type == YG_LIGHT_SPOT)
+            pw = 2.f * pi * (1.f - 0.5f * (L.cos_inner + L.cos_outer)) * in;
+        else
+        {
+            float ex = (c.whi[0] - c.wlo[0]) * 0.5f, ey = (c.whi[1] - c.wlo[1]) * 0.5f, ez = (c.whi[2] - c.wlo[2]) * 0.5f;
+            pw = pi * (ex * ex + ey * ey + ez * ez) * in;
+        }
+        pun.push_back(pw);
+        power.push_back(pw);
+    }
+    // calculateSelectionPDFs + buildAliasTable (RaytraceCommonResources.cpp:325-383)
+    auto table = [](std::vector<float>& pw, std::vector<float>& thr, std::vector<uint32_t>& alias) {
+        size_t cnt = pw.size();
         double total = 0;
-        for (float w : power) total += w;
+        for (float w : pw) total += w;
         float share = total > 0 ? 0.1f : 1.f;
-        for (float& w : power) w = (1.f - share) * (total > 0 ? float(w / total) : 0.f) + share / cnt;
-        std::vector<float> scaled(cnt), thr(cnt);
-        std::vector<uint32_t> alias(cnt), small, large;
+        for (float& w : pw) w = (1.f - share) * (total > 0 ? float(w / total) : 0.f) + share / cnt;
+        std::vector<float> scaled(cnt);
+        thr.assign(cnt, 0.f);
+        alias.assign(cnt, 0);
+        std::vector<uint32_t> small, large;
         for (size_t i = 0; i < cnt; ++i)
         {
-            scaled[i] = power[i] * cnt;
+            scaled[i] = pw[i] * cnt;
             (scaled[i] < 1.f ? small : large).push_back((uint32_t)i);
         }
         while (!small.empty() && !large.empty())
@@ -1520,14 +1550,51 @@ template <typename T> bool setup(Ctx<T>& c, const oracle_scene* sc, const Tables
         }
         for (uint32_t i : large) { thr[i] = 1.f; alias[i] = i; }
         for (uint32_t i : small) { thr[i] = 1.f; alias[i] = i; }
-        for (size_t l = 0; l < cnt; ++l)
+    };
+    std::vector<float> thr, pthr;
+    std::vector<uint32_t> alias, palias;
+    if (!power.empty()) table(power, thr, alias);
+    if (!pun.empty()) table(pun, pthr, palias);
+    const size_t nMesh = lightInst.size();
+    for (size_t l = 0; l < power.size(); ++l)
+    {
+        typename Ctx<T>::Light e{};
+        e.pdf = power[l];
+        e.thr = thr[l];
+        e.alias = alias[l];
+        if (l < nMesh)
         {
-            c.lights.push_back({lightInst[l], power[l], thr[l], alias[l]});
+            e.inst = lightInst[l];
             c.instLightPdf[lightInst[l]] = power[l];
         }
+        else
+        {
+            const size_t i = l - nMesh;
+            yg_punctual_light L = sc->punctual[i];
+            if (L.type != YG_LIGHT_POINT)
+            {
+                // normalised as yg_set_punctual_lights does
+                float d = std::sqrt(L.direction[0] * L.direction[0] + L.direction[1] * L.direction[1] + L.direction[2] * L.direction[2]);
+                for (int k = 0; k < 3; ++k) L.direction[k] = L.direction[k] / d;
+            }
+            e.inst = 0xffffffffu;
+            e.type = L.type;
+            e.ppdf = pun[i];
+            e.pthr = pthr[i];
+            e.palias = palias[i];
+            for (int k = 0; k < 3; ++k)
+            {
+                e.pos[k] = L.position[k];
+                e.dir[k] = L.direction[k];
+                e.inten[k] = L.intensity[k];
+            }
+            e.cosIn = L.cos_inner;
+            e.cosOut = L.cos_outer;
+        }
+        c.lights.push_back(e);
     }
-    if (c.tris.empty())
-        for (int k = 0; k < 3; ++k) c.wlo[k] = c.whi[k] = 0.0f;
+    c.nPunctual = sc->n_punctual;
+
     buildBvh(c);
     return true;
 }
@@ -1831,18 +1898,98 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                 T cur = ps.nVol ? ps.volIOR[ps.nVol - 1] : T(1), prev = ps.nVol > 1 ? ps.volIOR[ps.nVol - 2] : T(1);
                 makeCtx(s, cur, prev, wo, h.front, sctx);
                 V3<T> nWS = normalize(xVecT<T>(I.w2o, s.geoN));
-                if (P.integrator == YG_INTEGRATOR_NEE && !c.lights.empty() && !isDeltaDistr(sctx, s))
+                const bool nee = P.integrator == YG_INTEGRATOR_NEE;
+                // hasExplicitlySampledLights (rayHitDefault.hlsl:26-34): without NEE only the punctual lights
+                if ((nee ? !c.lights.empty() : c.nPunctual > 0) && !isDeltaDistr(sctx, s))
                 {
                     // connectToExplicitLight (rayHitDefault.hlsl:204-257)
                     T rl[4];
                     for (int k = 0; k < 4; ++k) rl[k] = T(rs.r1());
-                    // sampleLightIndex (lightSampling.hlsl:31-37)
-                    uint32_t nL = (uint32_t)c.lights.size();
-                    float scaled = (float)rl[3] * (float)nL;
-                    if (!std::is_same<T, float>::value) scaled = (float)(rl[3] * T(nL));
-                    uint32_t li = std::min((uint32_t)scaled, nL - 1);
-                    li = (scaled - (float)li) < c.lights[li].thr ? li : c.lights[li].alias;
+                    // sampleLightIndex / samplePunctualLightIndex (lightSampling.hlsl:31-53)
+                    uint32_t nL = (uint32_t)c.lights.size(), li;
+                    float pick;
+                    if (nee)
+                    {
+                        float scaled = (float)rl[3] * (float)nL;
+                        if (!std::is_same<T, float>::value) scaled = (float)(rl[3] * T(nL));
+                        li = std::min((uint32_t)scaled, nL - 1);
+                        li = (scaled - (float)li) < c.lights[li].thr ? li : c.lights[li].alias;
+                        pick = c.lights[li].pdf;
+                    }
+                    else
+                    {
+                        uint32_t nP = c.nPunctual, first = nL - nP;
+                        float scaled = (float)rl[3] * (float)nP;
+                        if (!std::is_same<T, float>::value) scaled = (float)(rl[3] * T(nP));
+                        uint32_t idx = std::min((uint32_t)scaled, nP - 1);
+                        const auto& E = c.lights[first + idx];
+                        li = first + ((scaled - (float)idx) < E.pthr ? idx : E.palias);
+                        pick = c.lights[li].ppdf;
+                    }
                     const auto& Lt = c.lights[li];
+                    if (Lt.type != 0)
+                    {
+                        // evaluatePunctualLightIncidence (lightSampling.hlsl:255-275)
+                        V3<T> toL, I3;
+                        T dist;
+                        if (Lt.type == YG_LIGHT_DIRECTIONAL)
+                        {
+                            toL = v3(-T(Lt.dir[0]), -T(Lt.dir[1]), -T(Lt.dir[2]));
+                            dist = T(INFINITY);
+                            I3 = v3(T(Lt.inten[0]), T(Lt.inten[1]), T(Lt.inten[2]));
+                        }
+                        else
+                        {
+                            V3<T> v = v3(T(Lt.pos[0]), T(Lt.pos[1]), T(Lt.pos[2])) - hitPos;
+                            T d2 = std::fmax(dot(v, v), T(1e-10f));
+                            dist = Mth<T>::sqrt(d2);
+                            toL = v / dist;
+                            T fall = T(1);
+                            if (Lt.type == YG_LIGHT_SPOT)
+                            {
+                                // spotFalloff (lightSampling.hlsl:228-236)
+                                V3<T> from = -toL;
+                                T ct = dot(from, v3(T(Lt.dir[0]), T(Lt.dir[1]), T(Lt.dir[2])));
+                                T ci = T(Lt.cosIn), co = T(Lt.cosOut);
+                                if (ci <= co)
+                                    fall = ct >= co ? T(1) : T(0);
+                                else
+                                {
+                                    T t = saturate((ct - co) / (ci - co));
+                                    fall = t * t * (T(3) - T(2) * t);
+                                }
+                            }
+                            T f = fall / d2;
+                            I3 = v3(T(Lt.inten[0]) * f, T(Lt.inten[1]) * f, T(Lt.inten[2]) * f);
+                        }
+                        S4<T> emis = isZero(I3) ? sp(T(0)) : setFromRGBUnbounded(c, s4, I3);
+                        if (!allEq(emis, T(0)) && T(pick) > T(0))
+                        {
+                            V3<T> toLOS = normalize(xVec<T>(I.w2o, toL));
+                            EvalR<T> ev = evalSurface(L, s, sctx, wo, toLOS, false, s4);
+                            S4<T> wl = ev.w;
+                            if ((ev.trans & 4) && !(ps.flags & F_SEC))
+                            {
+                                wl[0] *= T(4);
+                                wl[1] = wl[2] = wl[3] = 0;
+                            }
+                            if (!allEq(wl, T(0)))
+                            {
+                                V3<T> st = spawn(hitPos, nWS, toL);
+                                TriHit<float> sh;
+                                rays++;
+                                // checkUnoccluded (rayHitDefault.hlsl:114-133)
+                                bool any = trace(c, st, toL, 5e-4f, (float)dist - 5e-4f, sh);
+                                if (!any)
+                                {
+                                    wl = (wl / T(pick)) * T(1);
+                                    ps.total = ps.total + ps.thr * wl * emis;
+                                }
+                            }
+                        }
+                    }
+                    else
+                    {
                     const oracle_instance& LI = sc->instances[Lt.inst];
                     const yg_material& LM = sc->materials[LI.material];
                     uint32_t pc = LI.prim_count;
@@ -1871,7 +2018,7 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                     T dist = len(toL);
                     T cosE = -dot(g, toL / dist);
                     S4<T> emis = rad * emissionProfile(cosE, T(LM.emission_focus));
-                    T lpdf = T(Lt.pdf) * pdfPos * area2solid(toL, g);
+                    T lpdf = T(pick) * pdfPos * area2solid(toL, g);
                     V3<T> toLWS = toL / dist;
                     if (!two && dot(toL, g) >= T(0))
                     {
@@ -1902,6 +2049,7 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                                 ps.total = ps.total + ps.thr * wl * emis;
                             }
                         }
+                    }
                     }
                 }
                 // sampleScatteringEvent (scatteringSample.hlsl:30-65)
@@ -1998,6 +2146,8 @@ inline bool needsRgbTable(const oracle_scene* sc, const yg_render_params* P)
             (m.sheen_amount > 0.0f && nonGrey(m.sheen_tint)))
             return true;
     }
+    for (uint32_t i = 0; i < sc->n_punctual; ++i)
+        if (nonGrey(sc->punctual[i].intensity)) return true;
     return false;
 }
 
@@ -2081,6 +2231,7 @@ int oracle_render(const oracle_scene* sc, const yg_render_params* P, int precisi
     if (!sc->rgb_to_spd && orc::needsRgbTable(sc, P)) return -6; // the RGB -> spectrum table was not given
     if (P->integrator == YG_INTEGRATOR_BDPT)
     {
+        if (sc->n_punctual) return -7; // punctual lights are not built for BDPT
         if (precision == 64) return orc::runBdpt<double>(sc, P, threads, records, film, stats);
         return orc::runBdpt<float>(sc, P, threads, records, film, stats);
     }

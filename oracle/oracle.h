@@ -52,6 +52,8 @@ typedef struct oracle_scene
     const float* luts[9];     /* YG_TABLE_LUT_* in order */
     const float* rgb_to_spd;  /* 64^3 x 3 or NULL */
     const char* data_dir;     /* CIE + Joe-Kuo data files */
+    const yg_punctual_light* punctual; /* may be NULL when n_punctual is 0 */
+    uint32_t n_punctual;
 } oracle_scene;
 
 typedef struct oracle_stats

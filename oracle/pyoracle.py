@@ -32,7 +32,8 @@ class OracleScene(C.Structure):
                 ("materials", C.POINTER(N.Material)), ("n_materials", C.c_uint32),
                 ("spectra", C.POINTER(C.c_float)), ("spec_points", C.c_uint32), ("spec_lmin", C.c_float),
                 ("spec_lmax", C.c_float), ("camera", C.POINTER(N.Camera)), ("luts", C.POINTER(C.c_float) * 9),
-                ("rgb_to_spd", C.POINTER(C.c_float)), ("data_dir", C.c_char_p)]
+                ("rgb_to_spd", C.POINTER(C.c_float)), ("data_dir", C.c_char_p),
+                ("punctual", C.POINTER(N.PunctualLight)), ("n_punctual", C.c_uint32)]
 
 
 class OracleStats(C.Structure):
@@ -121,7 +122,10 @@ class OracleSceneHandle:
             s.luts[i] = fp(luts[name]).ctypes.data_as(C.POINTER(C.c_float))
         s.rgb_to_spd = fp(rgb_to_spd).ctypes.data_as(C.POINTER(C.c_float)) if rgb_to_spd is not None else None
         s.data_dir = N.DATA_DIR.encode()
-        self.keep += [inst, mats, cam]
+        pl = scene.punctual_structs()
+        s.punctual = pl
+        s.n_punctual = len(scene.punctual_lights)
+        self.keep += [inst, mats, cam, pl]
         self.s = s
 
     def render(self, params, precision=32, threads=None, records=True, film=False):

@@ -160,8 +160,8 @@ def test_bdpt_pipeline_and_unsupported_features_raise(built, py_yapt):
     assert np.all(np.isfinite(xyz)) and float(xyz[..., 1].mean()) > 0.0
     light = sc.createLight("point", Y.Light.LightType.POINT)
     with pytest.raises(Y.YaptError):
-        sc.update(0.0)  # punctual lights are not built
-    light.setIntensity(0.0)
+        sc.update(0.0)  # BDPT with punctual lights is not built
+    light.setIntensity(0.0)  # a dark light is left out
     sc.update(0.0)
     r.getRendererVariable("RenderPipeline").setSelectedOption(3)
     with pytest.raises(Y.YaptError):

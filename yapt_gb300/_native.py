@@ -77,6 +77,16 @@ class Camera(C.Structure):
     ]
 
 
+YG_LIGHT_POINT, YG_LIGHT_SPOT, YG_LIGHT_DIRECTIONAL = 1, 2, 3
+
+
+class PunctualLight(C.Structure):
+    _fields_ = [
+        ("type", C.c_uint32), ("position", C.c_float * 3), ("direction", C.c_float * 3), ("intensity", C.c_float * 3),
+        ("cos_inner", C.c_float), ("cos_outer", C.c_float), ("reserved", C.c_float * 2),
+    ]
+
+
 class AtrousParams(C.Structure):
     _fields_ = [
         ("depth_sigma_scale", C.c_float), ("normal_sigma", C.c_float), ("material_sigma", C.c_float),
@@ -168,6 +178,7 @@ SIGNATURES = [
     ("yg_upload_mesh", C.c_int, [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(C.c_uint32)]),
     ("yg_clear_meshes", C.c_int, [C.c_void_p]),
     ("yg_film_resolve_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("yg_set_punctual_lights", C.c_int, [C.c_void_p, C.POINTER(PunctualLight), C.c_uint32]),
     ("yg_atrous_default_params", None, [C.POINTER(AtrousParams)]),
     ("yg_atrous_denoise", C.c_int, [C.c_void_p, C.POINTER(AtrousParams), C.c_void_p, C.c_void_p]),
     ("yg_atrous_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -181,6 +181,22 @@ def layered_box_scene(seed=0, light_intensity=12.0, aspect=1.0):
     return sc
 
 
+def punctual_box_scene(seed=0, area_light=True, aspect=1.0):
+    """``box_scene`` lit by punctual lights (LightManager's point, spot and directional
+    lights): a point light in the upper left, a spot light under the ceiling aimed at the
+    floor (inner 20, outer 35 degrees) and a directional light entering through the open
+    front; the ceiling's area light stays unless ``area_light`` is False."""
+    sc = box_scene(seed, aspect=aspect)
+    sc.name = "punctual_box(seed=%d%s)" % (seed, "" if area_light else ", no area light")
+    if not area_light:
+        sc.instances.pop()  # the ceiling light quad is the last instance
+    sc.add_punctual_light("point", position=(0.25, 0.8, 0.6), intensity=(0.35, 0.3, 0.22))
+    sc.add_punctual_light("spot", position=(0.7, 0.95, 0.45), direction=(0.0, -1.0, 0.1), intensity=(1.2, 1.1, 0.9),
+                          cos_inner=float(np.cos(np.radians(20.0))), cos_outer=float(np.cos(np.radians(35.0))))
+    sc.add_punctual_light("directional", direction=(-0.3, -0.45, -1.0), intensity=(0.5, 0.55, 0.65))
+    return sc
+
+
 def random_shapes_scene(seed=0, n_spheres=500, light_intensity=25.0, aspect=1.0):
     rng = np.random.Generator(np.random.PCG64(seed))
     sc = Scene()

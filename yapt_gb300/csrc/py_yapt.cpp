@@ -12,8 +12,12 @@
 // camera or renderer variables restarts the accumulation. readback() returns the film
 // synchronously (state Ready). There is no window: setRenderOutputToSurface raises.
 //
-// Not built (they raise): textures, debug render pipelines, punctual lights with
-// non-zero intensity, orthographic cameras.
+// Punctual lights follow LightManager::fillParameters (LightManager.cpp:97-107): position is
+// the node's world translation, direction the world forward axis (0, 0, -1) rotated by the
+// node's transform, intensity colour x max(0, intensity); lights with zero intensity are
+// left out. BDPT renders with punctual lights raise.
+//
+// Not built (they raise): textures, debug render pipelines, orthographic cameras.
 #include <pybind11/operators.h>
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
@@ -990,6 +994,7 @@ struct RendererState
     std::vector<uint8_t> lastScene;  // instances, materials, spectra
     std::vector<uint64_t> lastMeshes; // (mesh identity, content version) of the uploaded meshes
     std::vector<uint8_t> lastCamera;
+    std::vector<uint8_t> lastLights;
     std::vector<uint8_t> lastParams;
     std::vector<yg_instance> instances; // the records of the last commit
     std::vector<yg_material> materials;
@@ -1337,11 +1342,28 @@ bool Scene::sync()
 {
     requireInit();
     RendererState& S = *R;
+    std::vector<yg_punctual_light> punctual;
     for (auto& w : lights)
-        if (auto l = w.lock())
-            if (l->intensity > 0.f)
-                throw YaptError("punctual lights are not supported by the GB300 integrators (light '" + l->node->name +
-                                "')");
+    {
+        auto l = w.lock();
+        if (!l) continue;
+        const float k = std::max(0.f, l->intensity);
+        yg_punctual_light P{};
+        P.type = (uint32_t)l->type + 1u; // POINT, SPOT, DIRECTIONAL -> YG_LIGHT_*
+        for (int c = 0; c < 3; ++c) P.intensity[c] = l->color.v[c] * k;
+        if (P.intensity[0] == 0.f && P.intensity[1] == 0.f && P.intensity[2] == 0.f) continue;
+        M4 t = l->node->transform->world();
+        double d[3] = {-t.a[0][2], -t.a[1][2], -t.a[2][2]};
+        double dl = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int c = 0; c < 3; ++c)
+        {
+            P.position[c] = (float)t.a[c][3];
+            P.direction[c] = dl > 0.0 ? (float)(d[c] / dl) : (c == 2 ? -1.f : 0.f);
+        }
+        P.cos_inner = std::cos(l->inner);
+        P.cos_outer = std::cos(l->outer);
+        punctual.push_back(P);
+    }
     // gather instances in creation order (RaytraceCommonResources::sceneChanged: one instance
     // per (render object, submesh), the last material serving the submeshes beyond the list)
     std::vector<std::shared_ptr<MeshData>> meshes;
@@ -1449,6 +1471,15 @@ bool Scene::sync()
         check(yg_set_instances(S.ctx, inst.data(), (uint32_t)inst.size()), "scene update");
         check(yg_build_scene(S.ctx), "scene update");
         S.lastScene = sceneSig;
+        changed = true;
+    }
+    std::vector<uint8_t> lightSig;
+    for (auto& P : punctual) appendBytes(lightSig, P);
+    if (lightSig != S.lastLights || changed)
+    {
+        check(yg_set_punctual_lights(S.ctx, punctual.empty() ? nullptr : punctual.data(), (uint32_t)punctual.size()),
+              "scene update");
+        S.lastLights = lightSig;
         changed = true;
     }
     yg_camera cam = Camera{camera}.constants((float)S.var("Camera.ApertureRadius")->val[0],

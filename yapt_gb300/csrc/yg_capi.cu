@@ -56,6 +56,19 @@ yg::GpuMaterial packMaterial(const yg_material& m)
 
 bool isGreyOrZero(const float* c) { return c[0] == c[1] && c[0] == c[2]; }
 
+// estimatePunctualLightPower (RaytraceCommonResources.cpp:407-424); directional lights cover
+// the world bounds' half diagonal
+float punctualPower(const yg_context* ctx, const yg_punctual_light& L)
+{
+    float intensity = 0.2126f * L.intensity[0] + 0.7152f * L.intensity[1] + 0.0722f * L.intensity[2];
+    const float pi = 3.14159274f;
+    if (L.type == YG_LIGHT_POINT) return 4.f * pi * intensity;
+    if (L.type == YG_LIGHT_SPOT) return 2.f * pi * (1.f - 0.5f * (L.cos_inner + L.cos_outer)) * intensity;
+    float ex = (ctx->worldHi[0] - ctx->worldLo[0]) * 0.5f, ey = (ctx->worldHi[1] - ctx->worldLo[1]) * 0.5f,
+          ez = (ctx->worldHi[2] - ctx->worldLo[2]) * 0.5f;
+    return pi * (ex * ex + ey * ey + ez * ez) * intensity;
+}
+
 // Vose alias table (RaytraceCommonResources.cpp:325-383)
 void selectionPdfs(std::vector<float>& w)
 {
@@ -105,6 +118,65 @@ void aliasTable(const std::vector<float>& pdfs, std::vector<float>& thr, std::ve
     }
 }
 
+// uploadLightData (RaytraceCommonResources.cpp:426-543): selection pdfs and alias tables over
+// the mesh lights then the punctual lights, and over the punctual lights alone; the
+// instances' light pdfs are rewritten to match
+int uploadLightTable(yg_context* ctx)
+{
+    const size_t nMesh = ctx->meshLightInst.size(), nP = ctx->punctual.size(), n = nMesh + nP;
+    std::vector<float> all(ctx->meshLightPower), pun(nP);
+    for (size_t i = 0; i < nP; ++i)
+    {
+        pun[i] = punctualPower(ctx, ctx->punctual[i]);
+        all.push_back(pun[i]);
+    }
+    std::vector<yg::GpuLight> lights(std::max<size_t>(n, 1));
+    std::memset(lights.data(), 0, lights.size() * sizeof(yg::GpuLight));
+    for (yg::GpuInstance& G : ctx->hostInst) G.lightPdf = 0.0f;
+    std::vector<float> thr, pthr;
+    std::vector<uint32_t> alias, palias;
+    if (n)
+    {
+        selectionPdfs(all);
+        aliasTable(all, thr, alias);
+    }
+    if (nP)
+    {
+        selectionPdfs(pun);
+        aliasTable(pun, pthr, palias);
+    }
+    for (size_t l = 0; l < n; ++l)
+    {
+        yg::GpuLight& G = lights[l];
+        G.selectionPdf = all[l];
+        G.aliasThreshold = thr[l];
+        G.aliasIndex = alias[l];
+        if (l < nMesh)
+        {
+            G.instance = ctx->meshLightInst[l];
+            G.type = yg::kLightMesh;
+            ctx->hostInst[G.instance].lightPdf = all[l];
+            continue;
+        }
+        const size_t i = l - nMesh;
+        const yg_punctual_light& P = ctx->punctual[i];
+        G.instance = 0xffffffffu;
+        G.type = P.type;
+        G.punctualSelectionPdf = pun[i];
+        G.punctualAliasThreshold = pthr[i];
+        G.punctualAliasIndex = palias[i];
+        G.positionCosInner = make_float4(P.position[0], P.position[1], P.position[2], P.cos_inner);
+        G.directionCosOuter = make_float4(P.direction[0], P.direction[1], P.direction[2], P.cos_outer);
+        G.intensity = make_float4(P.intensity[0], P.intensity[1], P.intensity[2], 0.0f);
+    }
+    int r;
+    if ((r = upload(ctx, ctx->dLights, lights.data(), lights.size()))) return r;
+    if (!ctx->hostInst.empty() && (r = upload(ctx, ctx->dInst, ctx->hostInst.data(), ctx->hostInst.size()))) return r;
+    ctx->nLights = (uint32_t)n;
+    ctx->nPunctual = (uint32_t)nP;
+    return YG_OK;
+}
+
 int ensureCie(yg_context* c, int lmin, int lmax)
 {
     if (c->cieLmin == lmin && c->cieLmax == lmax) return YG_OK;
@@ -133,6 +205,8 @@ bool sceneNeedsRgbLut(const yg_context* c, float envScale)
         if (!isGreyOrZero(m.absorption)) return true;
         if (m.sheen_amount > 0.0f && !isGreyOrZero(m.sheen_tint)) return true;
     }
+    for (const yg_punctual_light& L : c->punctual)
+        if (!isGreyOrZero(L.intensity)) return true;
     return false;
 }
 
@@ -191,6 +265,7 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.rgbToSpd = needRgb ? ctx->dRgb.as<float>() : nullptr;
     S.cam = ctx->camera;
     S.nLights = ctx->nLights;
+    S.nPunctual = ctx->nPunctual;
     S.nInstances = (uint32_t)ctx->instances.size();
     S.specPoints = ctx->specPoints;
     S.specLmin = ctx->specLmin;
@@ -715,25 +790,10 @@ YG_API int yg_build_scene(yg_context* ctx)
             lightInst.push_back((uint32_t)i);
         }
     }
-    std::vector<yg::GpuLight> lights(lightInst.size());
-    if (!lightInst.empty())
-    {
-        std::vector<float> thr;
-        std::vector<uint32_t> alias;
-        selectionPdfs(power);
-        aliasTable(power, thr, alias);
-        for (size_t l = 0; l < lightInst.size(); ++l)
-        {
-            lights[l].instance = lightInst[l];
-            lights[l].selectionPdf = power[l];
-            lights[l].aliasThreshold = thr[l];
-            lights[l].aliasIndex = alias[l];
-            gi[lightInst[l]].lightPdf = power[l];
-        }
-    }
+    ctx->meshLightInst = lightInst;
+    ctx->meshLightPower = power;
     int r;
     if ((r = upload(ctx, ctx->dInst, gi.data(), gi.size()))) return r;
-    if ((r = upload(ctx, ctx->dLights, lights.data(), lights.size()))) return r;
     if ((r = upload(ctx, ctx->dPos, ctx->positions.data(), ctx->positions.size()))) return r;
     if ((r = upload(ctx, ctx->dNrm, ctx->normals.data(), ctx->normals.size()))) return r;
     if ((r = upload(ctx, ctx->dTan, ctx->tangents.data(), ctx->tangents.size()))) return r;
@@ -755,7 +815,7 @@ YG_API int yg_build_scene(yg_context* ctx)
     ctx->nTris = primStart[nInst];
     ctx->nNodes = bout.nNodes;
     ctx->bvhDepth = bout.depth;
-    ctx->nLights = (uint32_t)lights.size();
+    ctx->hostInst = gi;
     // every inner node reachable exactly once and every triangle referenced exactly once,
     // checked before any ray can traverse the tree
     if ((r = checkWideBvhStructure(ctx))) return r;
@@ -768,8 +828,44 @@ YG_API int yg_build_scene(yg_context* ctx)
         ext2 += e * e;
     }
     ctx->worldRadiusSqr = ext2;
+    for (int k = 0; k < 3; ++k)
+    {
+        ctx->worldLo[k] = bout.lo[k];
+        ctx->worldHi[k] = bout.hi[k];
+    }
+    if ((r = uploadLightTable(ctx))) return r;
     YG_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->sceneBuilt = true;
+    return YG_OK;
+}
+
+YG_API int yg_set_punctual_lights(yg_context* ctx, const yg_punctual_light* lights, uint32_t count)
+{
+    if (!ctx || (!lights && count)) return fail(YG_ERR_INVALID_ARGUMENT, "punctual lights: null argument");
+    std::vector<yg_punctual_light> v(lights, lights + count);
+    for (yg_punctual_light& L : v)
+    {
+        if (L.type < YG_LIGHT_POINT || L.type > YG_LIGHT_DIRECTIONAL)
+            return fail(YG_ERR_INVALID_ARGUMENT, "punctual lights: unknown type");
+        const float* f = &L.position[0];
+        for (int k = 0; k < 11; ++k)
+            if (!std::isfinite(f[k])) return fail(YG_ERR_INVALID_ARGUMENT, "punctual lights: non-finite parameter");
+        if (L.intensity[0] < 0.f || L.intensity[1] < 0.f || L.intensity[2] < 0.f)
+            return fail(YG_ERR_INVALID_ARGUMENT, "punctual lights: negative intensity");
+        if (L.type != YG_LIGHT_POINT)
+        {
+            float d = std::sqrt(L.direction[0] * L.direction[0] + L.direction[1] * L.direction[1] + L.direction[2] * L.direction[2]);
+            if (!(d > 0.0f)) return fail(YG_ERR_INVALID_ARGUMENT, "punctual lights: zero direction");
+            for (int k = 0; k < 3; ++k) L.direction[k] = L.direction[k] / d;
+        }
+    }
+    std::lock_guard<std::mutex> g(ctx->lock);
+    ctx->punctual = v;
+    if (!ctx->sceneBuilt) return YG_OK;
+    cudaSetDevice(ctx->device);
+    int r = uploadLightTable(ctx);
+    if (r) return r;
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
     return YG_OK;
 }
 
@@ -848,6 +944,7 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     const uint64_t maxSamplesPerChunk = bdpt ? (1ull << 24) : (1ull << 26);
     uint32_t chunkSpp = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->spp_count, maxSamplesPerChunk / npix));
     if (bdpt && (p->flags & YG_FLAG_MEGAKERNEL)) return fail(YG_ERR_INVALID_ARGUMENT, "render: BDPT has no megakernel variant");
+    if (bdpt && ctx->nPunctual) return fail(YG_ERR_INVALID_ARGUMENT, "render: BDPT with punctual lights is not available");
     const uint32_t lightVerts = p->bdpt_light_vertices ? p->bdpt_light_vertices : yg::kBdptMaxLightVertices;
     if (bdpt && (lightVerts < 2 || lightVerts > yg::kBdptMaxLightVertices))
         return fail(YG_ERR_INVALID_ARGUMENT, "render: bdpt_light_vertices must be 2..16");

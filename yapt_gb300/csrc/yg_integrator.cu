@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(128, 4) wfShade(const SceneView S, const Launc
             Qout.o[k] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, __uint_as_float(slot));
             Qout.d[k] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, 0.0f);
         }
-        if (NEE)
+        if (NEE || S.nPunctual > 0)
         {
             uint32_t j = warpAppend(SQ.count, sr.valid);
             if (sr.valid)
@@ -457,7 +457,7 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
             else wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ);
             if (T) T->end(kKernelShade, stream);
             launches += 4;
-            if (P.integrator == 1)
+            if (P.integrator == 1 || S.nPunctual > 0)
             {
                 if (T) T->begin(stream);
                 if (count) wfShadow<true><<<traceBlocks, 128, 0, stream>>>(S, W, SQ, P.rayCounter, P.traversalCounter);

@@ -107,7 +107,13 @@ struct yg_context
     DevBuf dCie, dRgb, dSobol, dSobolMat, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
     DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena, dPerm;
     DevBuf dAtrousMom, dAtrousOdd, dAtrousFeat, dAtrousCol, dAtrousVar; // a-trous denoiser state
-    uint32_t nLights = 0;
+    uint32_t nLights = 0;   // mesh and punctual
+    uint32_t nPunctual = 0;
+    std::vector<yg_punctual_light> punctual;
+    std::vector<yg::GpuInstance> hostInst;  // as uploaded; lightPdf rewritten with the light table
+    std::vector<uint32_t> meshLightInst;    // emissive instances and their power estimates
+    std::vector<float> meshLightPower;
+    float worldLo[3] = {0, 0, 0}, worldHi[3] = {0, 0, 0};
     float worldCenter[3] = {0, 0, 0}; // getWorldCenterAndRadiusSqr (raytraceCommonResources.hlsl:99-104)
     float worldRadiusSqr = 0;
     uint32_t permW = 0, permH = 0;    // size of the BDPT pixel permutation in dPerm

@@ -255,8 +255,8 @@ struct LightPoint
 };
 YG_DEV void sampleMeshLight(const SceneView& S, const Spectral& sp, uint32_t li, float3 r, LightPoint& out)
 {
-    GpuLight L = S.lights[li];
-    const GpuInstance& I = S.instances[L.instance];
+    const uint32_t inst = S.lights[li].instance;
+    const GpuInstance& I = S.instances[inst];
     uint32_t primCount = I.primCount;
     uint32_t prim = (uint32_t)fminf((float)primCount * r.z, (float)(primCount - 1u));
     float bx = r.x, by = r.y;
@@ -279,7 +279,7 @@ YG_DEV void sampleMeshLight(const SceneView& S, const Spectral& sp, uint32_t li,
     out.radiance = emissionSpectrum(S, sp, mk3(e.x, e.y, e.z), M.emissionSpectrum);
     out.pdfPos = 1.0f / ((float)primCount * area);
     out.focus = M.emissionFocus;
-    out.instance = L.instance;
+    out.instance = inst;
     out.prim = prim;
     out.twoSided = (M.mask & 1u) != 0;
 }
@@ -288,8 +288,29 @@ YG_DEV uint32_t sampleLightIndex(const SceneView& S, float u)
 {
     float scaled = u * (float)S.nLights;
     uint32_t index = min((uint32_t)scaled, S.nLights - 1u);
-    GpuLight e = S.lights[index];
+    const GpuLight& e = S.lights[index];
     return (scaled - (float)index) < e.aliasThreshold ? index : e.aliasIndex;
+}
+
+// samplePunctualLightIndex (lightSampling.hlsl:46-53): the alias table over the punctual lights
+YG_DEV uint32_t samplePunctualLightIndex(const SceneView& S, float u)
+{
+    const uint32_t first = S.nLights - S.nPunctual;
+    float scaled = u * (float)S.nPunctual;
+    uint32_t index = min((uint32_t)scaled, S.nPunctual - 1u);
+    const GpuLight& e = S.lights[first + index];
+    return first + ((scaled - (float)index) < e.punctualAliasThreshold ? index : e.punctualAliasIndex);
+}
+
+// spotFalloff + punctualLightAngularFalloff (lightSampling.hlsl:228-246)
+YG_DEV float punctualFalloff(const GpuLight& L, float3 dirFromLight)
+{
+    if (L.type != kLightSpot) return 1.0f;
+    float cosTheta = dot(dirFromLight, mk3(L.directionCosOuter.x, L.directionCosOuter.y, L.directionCosOuter.z));
+    float cosInner = L.positionCosInner.w, cosOuter = L.directionCosOuter.w;
+    if (cosInner <= cosOuter) return cosTheta >= cosOuter ? 1.0f : 0.0f;
+    float t = saturate((cosTheta - cosOuter) / (cosInner - cosOuter));
+    return t * t * (3.0f - 2.0f * t); // smoothstep
 }
 
 // calculateExplicitLightConnectionPDF (rayHitDefault.hlsl:137-166)
@@ -325,13 +346,66 @@ struct ShadowRequest
     bool valid;
 };
 
+// With NEE every light is sampled; without it only the punctual lights, which BSDF sampling
+// can never hit (hasExplicitlySampledLights / sampleExplicitLight, rayHitDefault.hlsl:26-81).
+// A punctual light is visible when nothing is hit before it (checkUnoccluded) and its
+// connection has no MIS weight.
+template <bool NEE>
 YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, const Surface& s, const SurfaceCtx& c,
                        float3 woOS, float3 posWS, float3 normalWS, const float4* w2o, const PathState& ps,
                        RandomSampler& rs, ShadowRequest& sr)
 {
     float4 r = rs.r4();
-    uint32_t li = sampleLightIndex(S, r.w);
-    float pick = S.lights[li].selectionPdf;
+    uint32_t li;
+    float pick;
+    if (NEE)
+    {
+        li = sampleLightIndex(S, r.w);
+        pick = S.lights[li].selectionPdf;
+    }
+    else
+    {
+        li = samplePunctualLightIndex(S, r.w);
+        pick = S.lights[li].punctualSelectionPdf;
+    }
+    const GpuLight& PL = S.lights[li];
+    if (PL.type != kLightMesh)
+    {
+        // evaluatePunctualLightIncidence (lightSampling.hlsl:255-275)
+        float3 toL, I3;
+        float dist;
+        if (PL.type == kLightDirectional)
+        {
+            toL = mk3(-PL.directionCosOuter.x, -PL.directionCosOuter.y, -PL.directionCosOuter.z);
+            dist = __int_as_float(0x7f800000);
+            I3 = mk3(PL.intensity.x, PL.intensity.y, PL.intensity.z);
+        }
+        else
+        {
+            float3 v = mk3(PL.positionCosInner.x, PL.positionCosInner.y, PL.positionCosInner.z) - posWS;
+            float d2 = fmaxf(dot(v, v), 1e-10f);
+            dist = sqrtf(d2);
+            toL = v / dist;
+            float f = punctualFalloff(PL, -toL) / d2;
+            I3 = mk3(PL.intensity.x * f, PL.intensity.y * f, PL.intensity.z * f);
+        }
+        float4 emission = emissionSpectrum(S, sp, I3, -1);
+        if (allEqual4(emission, 0.0f) || !(pick > 0.0f)) return;
+        float3 toLightOS = normalize(xformVector(w2o, toL));
+        Eval ev = evaluateSurface(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
+        float4 w = ev.weight;
+        if ((ev.transmission & kTransDispersed) != 0 && !(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(w);
+        if (allEqual4(w, 0.0f)) return;
+        w = (w / pick) * 1.0f;
+        sr.origin = spawnRayOrigin(posWS, normalWS, toL);
+        sr.dir = toL;
+        sr.tmax = dist - kRayMinT;
+        sr.instance = kPunctualShadow;
+        sr.prim = li;
+        sr.contrib = ps.throughput * w * emission;
+        sr.valid = true;
+        return;
+    }
     LightPoint lp;
     sampleMeshLight(S, sp, li, mk3(r.x, r.y, r.z), lp);
     float3 toLight = lp.pos - posWS;
@@ -363,8 +437,10 @@ YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, c
 }
 
 // checkLightVisibility (rayHitDefault.hlsl:83-112): the closest hit must be the sampled light triangle
+// checkUnoccluded (rayHitDefault.hlsl:114-133) for punctual lights: nothing may be hit
 YG_DEV bool shadowVisible(bool any, const Hit& h, uint32_t inst, uint32_t prim)
 {
+    if (inst == kPunctualShadow) return !any;
     return any && h.instance == inst && h.prim == prim;
 }
 
@@ -479,8 +555,8 @@ YG_DEV bool shadeSegment(const SceneView& S, const LaunchParams& P, const Luts& 
             SurfaceCtx c;
             makeSurfaceCtx(s, currentIOR(ps), previousIOR(ps), wo, hit.front, c);
             float3 normalWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
-            if (NEE && S.nLights > 0 && !isDeltaDistribution(c.a2, s))
-                prepareNee(S, Lt, sp, s, c, wo, hitPos, normalWS, I.w2o, ps, rs, sr);
+            if ((NEE ? S.nLights > 0 : S.nPunctual > 0) && !isDeltaDistribution(c.a2, s))
+                prepareNee<NEE>(S, Lt, sp, s, c, wo, hitPos, normalWS, I.w2o, ps, rs, sr);
             // sampleScatteringEvent (scatteringSample.hlsl:30-65)
             int layer = selectMaterialLayer(rB.x, c.probs);
             float3 wi = mk3(0.f, 0.f, 0.f);

@@ -58,13 +58,24 @@ struct alignas(16) GpuInstance
     uint32_t pad;
 };
 
-// LightEntryGPU (materialsCommonResources.hlsl:51-71), mesh lights only.
+// LightEntryGPU (materialsCommonResources.hlsl:51-71): the mesh lights first, then the
+// punctual lights, which also carry a second alias table over the punctual lights alone
+// (used when they are the only explicitly sampled lights, i.e. without NEE).
+constexpr uint32_t kLightMesh = 0, kLightPoint = 1, kLightSpot = 2, kLightDirectional = 3;
+constexpr uint32_t kPunctualShadow = 0xffffffffu; // shadow-ray target of a punctual light: nothing may be hit
 struct alignas(16) GpuLight
 {
-    uint32_t instance;
+    uint32_t instance; // mesh lights
     float selectionPdf;
     float aliasThreshold;
     uint32_t aliasIndex;
+    uint32_t type;     // kLight*
+    float punctualSelectionPdf;
+    float punctualAliasThreshold;
+    uint32_t punctualAliasIndex;
+    float4 positionCosInner;  // punctual: world position, cos of the spot's inner angle
+    float4 directionCosOuter; // punctual: world direction of emission, cos of the outer angle
+    float4 intensity;         // punctual: RGB intensity (irradiance for directional lights)
 };
 
 struct alignas(16) GpuCamera
@@ -97,7 +108,8 @@ struct SceneView
     const float* rgbToSpd; // 64^3 x 3, may be null
     const uint32_t* sobol; // [spp_count][kSobolDims] points of this launch
     GpuCamera cam;
-    uint32_t nLights;
+    uint32_t nLights;      // mesh and punctual
+    uint32_t nPunctual;    // the last nPunctual entries of lights
     uint32_t nInstances;
     uint32_t specPoints;
     float specLmin, specLmax;

@@ -138,6 +138,7 @@ class Scene:
         self.instances = []   # (o2w 4x4 float64, mesh, submesh, material)
         self.camera = None
         self.name = "scene"
+        self.punctual_lights = []  # dict(type, position, direction, intensity, cos_inner, cos_outer)
 
     # -- building --------------------------------------------------------
     def add_mesh(self, positions, normals, indices, submeshes=None, tangents=None):
@@ -160,6 +161,26 @@ class Scene:
             raise ValueError("spectra are stored on %d points (380..780 nm)" % SPECTRUM_POINTS)
         self.spectra.append(v)
         return len(self.spectra) - 1
+
+    def add_punctual_light(self, kind, position=(0, 0, 0), direction=(0, -1, 0), intensity=(1, 1, 1), cos_inner=1.0,
+                           cos_outer=0.0):
+        """kind: "point", "spot" or "directional" (RGB intensity; irradiance for directional)."""
+        t = {"point": N.YG_LIGHT_POINT, "spot": N.YG_LIGHT_SPOT, "directional": N.YG_LIGHT_DIRECTIONAL}[kind]
+        self.punctual_lights.append(dict(type=t, position=tuple(position), direction=tuple(direction),
+                                         intensity=tuple(intensity), cos_inner=float(cos_inner),
+                                         cos_outer=float(cos_outer)))
+        return len(self.punctual_lights) - 1
+
+    def punctual_structs(self):
+        arr = (N.PunctualLight * max(1, len(self.punctual_lights)))()
+        for i, L in enumerate(self.punctual_lights):
+            arr[i].type = L["type"]
+            for k in range(3):
+                arr[i].position[k] = float(L["position"][k])
+                arr[i].direction[k] = float(L["direction"][k])
+                arr[i].intensity[k] = float(L["intensity"][k])
+            arr[i].cos_inner, arr[i].cos_outer = L["cos_inner"], L["cos_outer"]
+        return arr
 
     def add_instance(self, mesh, material, o2w=None, submesh=0):
         o2w = np.eye(4) if o2w is None else np.asarray(o2w, dtype=np.float64)
@@ -221,6 +242,7 @@ class Scene:
         if self.camera is not None:
             cam = self.camera.struct()
             N.check(lib.yg_set_camera(ctx, C.byref(cam)))
+        N.check(lib.yg_set_punctual_lights(ctx, self.punctual_structs(), len(self.punctual_lights)))
         N.check(lib.yg_build_scene(ctx))
 
     def pooled(self):
