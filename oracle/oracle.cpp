@@ -1766,6 +1766,16 @@ template <typename T> void fillSurf(const Ctx<T>& c, const Spec<T>& s4, uint32_t
     s.sheenColor = s.sheenAmount > T(0) ? setFromRGB(c, s4, v3(T(M.sheen_tint[0]), T(M.sheen_tint[1]), T(M.sheen_tint[2]))) : sp(T(0));
 }
 
+// spotFalloff / punctualLightAngularFalloff (lightSampling.hlsl:228-246) towards dirFromLight
+template <typename T> T spotFalloff(V3<T> dirFromLight, const float* axis, float cosIn, float cosOut)
+{
+    T ct = dot(dirFromLight, v3(T(axis[0]), T(axis[1]), T(axis[2])));
+    T ci = T(cosIn), co = T(cosOut);
+    if (ci <= co) return ct >= co ? T(1) : T(0);
+    T t = saturate((ct - co) / (ci - co));
+    return t * t * (T(3) - T(2) * t);
+}
+
 // The hero wavelength and camera ray of a sample (rayGenPrimaryRays.hlsl:13-37,
 // generateCameraRay in raytraceCommonResources.hlsl:113-137); rs starts at dimension 2.
 template <typename T> void cameraSample(const Ctx<T>& c, const yg_render_params& P, uint32_t px, uint32_t py, Sampler& rs,
@@ -1944,21 +1954,7 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                             T d2 = std::fmax(dot(v, v), T(1e-10f));
                             dist = Mth<T>::sqrt(d2);
                             toL = v / dist;
-                            T fall = T(1);
-                            if (Lt.type == YG_LIGHT_SPOT)
-                            {
-                                // spotFalloff (lightSampling.hlsl:228-236)
-                                V3<T> from = -toL;
-                                T ct = dot(from, v3(T(Lt.dir[0]), T(Lt.dir[1]), T(Lt.dir[2])));
-                                T ci = T(Lt.cosIn), co = T(Lt.cosOut);
-                                if (ci <= co)
-                                    fall = ct >= co ? T(1) : T(0);
-                                else
-                                {
-                                    T t = saturate((ct - co) / (ci - co));
-                                    fall = t * t * (T(3) - T(2) * t);
-                                }
-                            }
+                            T fall = Lt.type == YG_LIGHT_SPOT ? spotFalloff(-toL, Lt.dir, Lt.cosIn, Lt.cosOut) : T(1);
                             T f = fall / d2;
                             I3 = v3(T(Lt.inten[0]) * f, T(Lt.inten[1]) * f, T(Lt.inten[2]) * f);
                         }
@@ -2231,7 +2227,6 @@ int oracle_render(const oracle_scene* sc, const yg_render_params* P, int precisi
     if (!sc->rgb_to_spd && orc::needsRgbTable(sc, P)) return -6; // the RGB -> spectrum table was not given
     if (P->integrator == YG_INTEGRATOR_BDPT)
     {
-        if (sc->n_punctual) return -7; // punctual lights are not built for BDPT
         if (precision == 64) return orc::runBdpt<double>(sc, P, threads, records, film, stats);
         return orc::runBdpt<float>(sc, P, threads, records, film, stats);
     }

@@ -1,12 +1,13 @@
 """Punctual lights (point, spot, directional; LightManager / lightSampling.hlsl:210-358) on
 the GPU through the C ABI.
 
-They have no geometry, so both integrators sample them explicitly: NEE picks from the one
-alias table over all lights, the unidirectional integrator from the table over the
-punctual lights alone (rayHitDefault.hlsl:26-81). Checks: per-sample parity with the FP32
-oracle within 1e-4 relative (the same tolerance as the other integrator tests), the
-wavefront and the megakernel giving identical samples, uni and NEE agreeing block by block
-within their combined standard error (both unbiased for the same image), and the
+They have no geometry, so the path integrators sample them explicitly: NEE picks from the
+one alias table over all lights, the unidirectional integrator from the table over the
+punctual lights alone (rayHitDefault.hlsl:26-81); BDPT starts light subpaths at them
+(samplePunctualLightEmission, BDPTCommon.hlsl:697-760). Checks: per-sample parity with the
+FP32 oracle within 1e-4 relative (the same tolerance as the other integrator tests), the
+wavefront and the megakernel giving identical samples, uni and BDPT agreeing with NEE block
+by block within their combined standard error (all unbiased for the same image), and the
 boundary's validation."""
 import ctypes as C
 
@@ -23,36 +24,45 @@ import test_gpu_parity as T
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("integrator", ["uni", "nee"])
+@pytest.mark.parametrize("integrator", ["uni", "nee", "bdpt"])
 @pytest.mark.parametrize("area_light", [True, False])
 def test_per_sample_parity_with_the_oracle(built, host_luts, integrator, area_light):
     import pyoracle
     sc = configs.punctual_box_scene(3, area_light=area_light)
-    p = Context.params(integrator, 48, 40, spp=4, max_depth=8, lambda_range=(380, 780), flags=256)
+    bdpt = integrator == "bdpt"
+    p = Context.params(integrator, 48, 40, spp=4, max_depth=8, lambda_range=(380, 780), flags=256,
+                       light_vertices=8 if bdpt else 0)
     with Context(0) as c:
         c.upload_scene(sc)
         gpu = c.render(p, dump=True)
-        p.flags = 256 | N.YG_FLAG_MEGAKERNEL
-        mega = c.render(p, dump=True)
-    assert np.array_equal(gpu, mega)
+        if not bdpt:
+            p.flags = 256 | N.YG_FLAG_MEGAKERNEL
+            mega = c.render(p, dump=True)
+            p.flags = 256
+            assert np.array_equal(gpu, mega)
     rgb = N.host_table("rgb_to_spd", (380, 780))  # the lights' intensities are RGB
     orc = pyoracle.OracleSceneHandle(sc, host_luts, rgb).render(p, precision=32)["records"]
     T.compare(gpu, orc, min_within=0.999)
+    if bdpt:  # light-tracing splats (point and spot light paths reach the camera) land in XYZ
+        rel = np.abs(gpu[..., 5:8] - orc[..., 5:8]) / np.maximum(np.abs(orc[..., 5:8]), 1e-6)
+        assert float(np.mean(np.all(rel <= T.REL_TOL, axis=-1))) >= 0.999
 
 
+@pytest.mark.parametrize("other", ["uni", "bdpt"])
 @pytest.mark.parametrize("area_light", [True, False])
-def test_uni_and_nee_estimate_the_same_image(built, area_light):
+def test_integrators_estimate_the_same_image(built, other, area_light):
     sc = configs.punctual_box_scene(1, area_light=area_light)
     W = H = 32
     with Context(0) as c:
         c.upload_scene(sc)
         common = dict(spp=512, max_depth=16, regularize=False, lambda_range=(380, 780), flags=256)
-        uni = c.render(c.params("uni", W, H, **common), dump=True)
+        oth = c.render(c.params(other, W, H, **common), dump=True)
         nee = c.render(c.params("nee", W, H, **common), dump=True)
-    mu, su = B.block_stats(uni, 8)
+    assert np.all(np.isfinite(oth))
+    mu, su = B.block_stats(oth, 8)
     mn, sn = B.block_stats(nee, 8)
     z = np.abs(mu - mn) / np.sqrt(su ** 2 + sn ** 2 + 1e-30)
-    gu, gn = float(uni[..., 6].mean()), float(nee[..., 6].mean())
+    gu, gn = float(oth[..., 6].mean()), float(nee[..., 6].mean())
     assert gn > 0
     assert abs(gu - gn) / gn < B.MEAN_REL_TOL, (gu, gn)
     assert float(z.max()) < B.Z_MAX, float(z.max())
@@ -77,8 +87,8 @@ def test_lights_update_without_a_rebuild_and_validation(built):
         bad[0].type = N.YG_LIGHT_SPOT  # zero direction
         with pytest.raises(N.YaptError):
             N.check(c.lib.yg_set_punctual_lights(c.h, bad, 1))
-        with pytest.raises(N.YaptError):
-            c.render(c.params("bdpt", 24, 24, spp=1, flags=256))  # BDPT with punctual lights is not built
+        bd = c.render(c.params("bdpt", 24, 24, spp=2, max_depth=6, lambda_range=(380, 780), flags=256), dump=True)
+        assert float(bd[..., 6].sum()) > 0.0  # BDPT light subpaths start at the punctual lights
         N.check(c.lib.yg_set_punctual_lights(c.h, None, 0))
         dark = c.render(p, dump=True)
         assert float(dark[..., 6].sum()) == 0.0  # no area light and no punctual light left

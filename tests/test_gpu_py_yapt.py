@@ -159,8 +159,9 @@ def test_bdpt_pipeline_and_unsupported_features_raise(built, py_yapt):
     xyz = film_of(Y, r)
     assert np.all(np.isfinite(xyz)) and float(xyz[..., 1].mean()) > 0.0
     light = sc.createLight("point", Y.Light.LightType.POINT)
-    with pytest.raises(Y.YaptError):
-        sc.update(0.0)  # BDPT with punctual lights is not built
+    light.getTransform().setTranslation(Y.vec3([0.5, 0.8, 0.5]))
+    sc.update(0.0)  # BDPT light subpaths from the point light
+    assert r.getAccumulatedFrames() == 1
     light.setIntensity(0.0)  # a dark light is left out
     sc.update(0.0)
     r.getRendererVariable("RenderPipeline").setSelectedOption(3)

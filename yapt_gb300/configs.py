@@ -74,6 +74,32 @@ def cuboid():
     return np.array(pos, np.float32), np.array(nrm, np.float32), np.array(idx, np.uint32)
 
 
+def flat_tangents(normals):
+    """One unit tangent per vertex, perpendicular to its normal (w = 1). The shading frame is
+    built from the normal and the tangent (constructBasisTransform, commonMath.hlsl:124-129);
+    a mesh without tangents gets (1, 0, 0) (hitShadersCommon.hlsl:197), which is parallel to
+    a face whose normal is +-x and leaves that frame degenerate (NaN), so the box walls and
+    cuboids carry tangents, as meshes loaded by the reference's asset scripts do
+    (pythonScripts/yapt/mesh_utils.py:12-60)."""
+    n = np.asarray(normals, np.float64).reshape(-1, 3)
+    a = np.where(np.abs(n[:, 1:2]) < 0.9, [[0.0, 1.0, 0.0]], [[0.0, 0.0, 1.0]])
+    t = np.cross(a, n)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    return np.concatenate([t, np.ones((len(t), 1))], 1).astype(np.float32)
+
+
+def scaled_cuboid(sc, size):
+    """A cuboid mesh with its extent in the vertices, so that its instance transform stays a
+    rotation and translation. The reference samples and evaluates BSDFs in object space and
+    maps directions with the object-to-world matrix in the path tracers
+    (rayHitDefault.hlsl:429-431) but with the normal matrix in BDPT
+    (BDPTTraceLightPath.comp:182-185, 324); under a non-uniform scale the integrators then
+    estimate slightly different images, so the synthetic scenes keep instance scales uniform."""
+    p, n, i = cuboid()
+    p = (p * np.asarray(size, np.float32)).astype(np.float32)
+    return sc.add_mesh(p, n, i, tangents=flat_tangents(n))
+
+
 def icosphere(subdiv=2):
     """Unit icosphere: 20 * 4^subdiv triangles, outward winding, smooth normals."""
     t = (1.0 + 5 ** 0.5) / 2.0
@@ -136,12 +162,12 @@ def box_scene(seed=0, light_intensity=12.0, aspect=1.0):
         if np.dot(np.cross(cs[1] - cs[0], cs[2] - cs[0]), n) < 0:
             tri = [b, b + 2, b + 1, b, b + 3, b + 2]
         idx.extend(tri)
-    walls = sc.add_mesh(np.array(pos), np.array(nrm), np.array(idx), submeshes=[(6 * i, 6) for i in range(5)])
+    walls = sc.add_mesh(np.array(pos), np.array(nrm), np.array(idx), submeshes=[(6 * i, 6) for i in range(5)],
+                        tangents=flat_tangents(nrm))
     for i in range(5):
         sid = sc.add_spectrum(control_point_spectrum(rng))
         mat = sc.add_material(**diffuse(sid))
         sc.add_instance(walls, mat, submesh=i)
-    cube = sc.add_mesh(*cuboid())
     for k in range(2):
         sid = sc.add_spectrum(control_point_spectrum(rng))
         mat = sc.add_material(**diffuse(sid))
@@ -149,8 +175,8 @@ def box_scene(seed=0, light_intensity=12.0, aspect=1.0):
         w = rng.uniform(0.18, 0.3)
         x = 0.3 if k == 0 else 0.7
         z = rng.uniform(0.3, 0.6)
-        o2w = affine(translation=(x, h / 2, z), rotation=rotation_y(rng.uniform(0, np.pi)), scale=(w, h, w))
-        sc.add_instance(cube, mat, o2w)
+        o2w = affine(translation=(x, h / 2, z), rotation=rotation_y(rng.uniform(0, np.pi)))
+        sc.add_instance(scaled_cuboid(sc, (w, h, w)), mat, o2w)
     qp, qn, qi = quad(0.25, 0.25)
     light = sc.add_mesh(qp, qn, qi)
     lmat = sc.add_material(albedo=(0.0, 0.0, 0.0), emissive=(light_intensity,) * 3, metalness=0.0, specular_amount=0.0,
@@ -175,9 +201,6 @@ def layered_box_scene(seed=0, light_intensity=12.0, aspect=1.0):
                 anisotropy=0.7, anisotropy_rotation=0.2)
     m[6].update(metalness=1.0, roughness=0.2, specular=(0.9, 0.9, 0.9), specular_amount=1.0,
                 clear_coat_amount=1.0, clear_coat_ior=1.45, clear_coat_roughness=0.1, thin_film_thickness_nm=420.0)
-    # the blocks need tangents for the anisotropic lobe: one per vertex along the mesh's +x
-    cube = sc.meshes[sc.instances[5][1]]
-    cube["tangents"] = np.tile(np.float32([1, 0, 0, 1]), (len(cube["positions"]), 1))
     return sc
 
 
@@ -279,13 +302,11 @@ def sky_scene(seed=0, aspect=1.0):
     gi = gi[[0, 2, 1, 3, 5, 4]]
     ground = sc.add_mesh(gp, gn, gi)
     sc.add_instance(ground, sc.add_material(**diffuse(sc.add_spectrum(control_point_spectrum(rng)))))
-    cube = sc.add_mesh(*cuboid())
     for k in range(3):
         mat = sc.add_material(**diffuse(sc.add_spectrum(control_point_spectrum(rng))))
         h = rng.uniform(0.5, 1.5)
-        o2w = affine(translation=(-1.2 + 1.2 * k, h / 2, rng.uniform(-0.5, 0.5)),
-                     rotation=rotation_y(rng.uniform(0, np.pi)), scale=(0.6, h, 0.6))
-        sc.add_instance(cube, mat, o2w)
+        o2w = affine(translation=(-1.2 + 1.2 * k, h / 2, rng.uniform(-0.5, 0.5)), rotation=rotation_y(rng.uniform(0, np.pi)))
+        sc.add_instance(scaled_cuboid(sc, (0.6, h, 0.6)), mat, o2w)
     sc.camera = CameraDesc(eye=(0.0, 2.5, 5.0), target=(0.0, 0.5, 0.0), fovy=np.pi * 0.3, aspect=aspect)
     return sc
 

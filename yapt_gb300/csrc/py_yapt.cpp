@@ -15,7 +15,7 @@
 // Punctual lights follow LightManager::fillParameters (LightManager.cpp:97-107): position is
 // the node's world translation, direction the world forward axis (0, 0, -1) rotated by the
 // node's transform, intensity colour x max(0, intensity); lights with zero intensity are
-// left out. BDPT renders with punctual lights raise.
+// left out.
 //
 // Not built (they raise): textures, debug render pipelines, orthographic cameras.
 #include <pybind11/operators.h>

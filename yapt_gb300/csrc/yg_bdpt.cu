@@ -32,6 +32,9 @@ constexpr uint32_t NF_FRONT = 1u << 1;
 constexpr uint32_t NF_ENV = 1u << 2;
 constexpr uint32_t NF_DELTA = 1u << 3;
 constexpr uint32_t NF_REGULARIZED = 1u << 4;
+constexpr uint32_t NF_PUNCTUAL = 1u << 6;    // origin at a punctual light; prim holds the light index
+constexpr uint32_t NF_DIRECTIONAL = 1u << 7; // origin at a directional light (a point on its emitting disk)
+constexpr uint32_t NF_INFINITE = NF_ENV | NF_DIRECTIONAL; // isInfiniteLightNode: the normal holds the direction
 constexpr float kMaxPdfRatioSum = 1e16f;    // MAX_PDF_RATIO_SUM
 constexpr float kVisibilityEps = 0.001f;    // VISIBILITY_RAY_EPSILON
 constexpr double kSplatScale = 16777216.0;  // fixed-point units per XYZ unit (2^24)
@@ -118,6 +121,25 @@ YG_DEV float3 sampleCosPowSphere(float2 s, float e)
 }
 YG_DEV float pdfCosPowHemi(float d, float e) { return (e + 2.0f) * kINVPI * 0.5f * ygm_powf(saturate(d), e + 1.0f); }
 YG_DEV float pdfCosPowSphere(float d, float e) { return (e + 2.0f) * kINVPI * 0.25f * ygm_powf(fabsf(d), e + 1.0f); }
+
+// sampleSphere, sampleUniformCone (around +y), pdfUniformCone (miscBrdf.hlsl:70-94)
+YG_DEV float3 sampleSphere(float2 r)
+{
+    float y = 1.0f - 2.0f * r.x;
+    float rr = sqrtf(1.0f - y * y);
+    float s, c;
+    ygm_sincosf(2.0f * kPI * r.y, &s, &c);
+    return mk3(rr * c, y, rr * s);
+}
+YG_DEV float3 sampleUniformCone(float2 r, float cosMax)
+{
+    float y = 1.0f - r.x * (1.0f - cosMax);
+    float rr = sqrtf(fmaxf(0.0f, 1.0f - y * y));
+    float s, c;
+    ygm_sincosf(2.0f * kPI * r.y, &s, &c);
+    return mk3(rr * c, y, rr * s);
+}
+YG_DEV float pdfUniformCone(float cosMax) { return safeDiv(1.0f, 2.0f * kPI * (1.0f - cosMax)); }
 
 // environmentSelectionPDF / pdfEnvironmentDirection / pdfEnvironmentPosition (lightSampling.hlsl:23-76);
 // ENV_LIGHT_SELECTION_PROBABILITY is 0, so the environment starts light paths only without lights
@@ -324,6 +346,51 @@ YG_DEV bool startLightPath(const SceneView& S, const LaunchParams& P, const Bdpt
     {
         uint32_t li = sampleLightIndex(S, (pickR - envPdf) / (1.0f - envPdf));
         sel = (1.0f - envPdf) * S.lights[li].selectionPdf;
+        const GpuLight& PL = S.lights[li];
+        if (PL.type != kLightMesh)
+        {
+            // samplePunctualLightEmission (lightSampling.hlsl:290-336) with random values (r1, r0.xy)
+            Le = emissionSpectrum(S, sp, mk3(PL.intensity.x, PL.intensity.y, PL.intensity.z), -1);
+            const float3 ax = mk3(PL.directionCosOuter.x, PL.directionCosOuter.y, PL.directionCosOuter.z);
+            profile = 1.0f;
+            if (PL.type == kLightDirectional)
+            {
+                float3 v1, v2;
+                vectorBase(ax, v1, v2);
+                float2 cd = sampleConcentricDisk(r1);
+                float radius = sqrtf(B.worldRadiusSqr);
+                pos = B.worldCenter - ax * radius + (v1 * cd.x + v2 * cd.y) * radius;
+                dir = ax;
+                pdfPos = pdfEnvPosition(B);
+                pdfDir = 1.0f;
+                n0.flags = NF_PUNCTUAL | NF_DIRECTIONAL;
+            }
+            else
+            {
+                pos = mk3(PL.positionCosInner.x, PL.positionCosInner.y, PL.positionCosInner.z);
+                pdfPos = 1.0f;
+                if (PL.type == kLightSpot)
+                {
+                    float3 v1, v2;
+                    vectorBase(ax, v1, v2);
+                    float3 loc = sampleUniformCone(r1, PL.directionCosOuter.w);
+                    dir = normalize(v1 * loc.x + ax * loc.y + v2 * loc.z);
+                    pdfDir = pdfUniformCone(PL.directionCosOuter.w);
+                    profile = punctualFalloff(PL, dir);
+                }
+                else
+                {
+                    dir = sampleSphere(r1);
+                    pdfDir = 1.0f / (4.0f * kPI);
+                }
+                n0.flags = NF_PUNCTUAL;
+            }
+            n = dir;
+            n0.instance = 0xffffffffu;
+            n0.prim = li;
+        }
+        else
+        {
         LightPoint lp;
         sampleMeshLight(S, sp, li, mk3(r0.x, r0.y, r0.z), lp);
         const GpuInstance& LI = S.instances[lp.instance];
@@ -354,6 +421,7 @@ YG_DEV bool startLightPath(const SceneView& S, const LaunchParams& P, const Bdpt
         n0.instance = lp.instance;
         n0.prim = lp.prim;
         n0.flags = 0;
+        }
     }
     if (allEqual4(Le, 0.0f) || pdfPos == 0.0f || pdfDir == 0.0f || sel == 0.0f) return false;
     n0.bary = make_float2(-1.0f, -1.0f);
@@ -394,6 +462,8 @@ __global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const L
                             originPosPdf))
             continue;
         const bool originEnv = (nodes[0].flags & NF_ENV) != 0;
+        const bool originInfinite = (nodes[0].flags & NF_INFINITE) != 0;
+        const bool originPunctual = (nodes[0].flags & NF_PUNCTUAL) != 0;
         const float maxRadiance = max4(radiance);
         uint32_t stored = 0;
         bool prevDelta = false;
@@ -419,7 +489,7 @@ __global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const L
             float3 normalWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
             float3 posWS = rayOrigin + rayDir * hit.t;
             float pdfFwdMIS;
-            if (i == 1 && originEnv) pdfFwdMIS = originPosPdf * fabsf(dot(rayDir, normalWS));
+            if (i == 1 && originInfinite) pdfFwdMIS = originPosPdf * fabsf(dot(rayDir, normalWS));
             else pdfFwdMIS = prevDelta ? -1.0f : pdfForward * solidAngleToArea(posWS - rayOrigin, normalWS);
             float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
             if (!allEqual4(ab, 0.0f)) radiance = radiance * transmittance(ab, hit.t);
@@ -445,7 +515,8 @@ __global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const L
             pdfForward = ev.pdfFwd;
             float4 w = ev.weight * safeDiv(1.0f, pdfForward);
             prev.pdfBwd = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - posWS, prev.normal);
-            if (i == 1 && originEnv && !sDelta) prev.pdfBwd = ev.pdfBwd;
+            if (i == 1 && originPunctual) prev.pdfBwd = 0.0f; // a camera path never hits a delta light
+            else if (i == 1 && originEnv && !sDelta) prev.pdfBwd = ev.pdfBwd;
             out[stored++] = prev;
             radiance = radiance * w;
             if (dispersed) terminateSecondary(radiance);
@@ -527,7 +598,7 @@ YG_DEV void prepareSharedNode(const SceneView& S, const LaunchParams& P, const S
                               float3 prevPos, uint32_t index, SharedNode& d)
 {
     d.n = src;
-    if (src.flags & NF_ENV) return;
+    if (src.flags & (NF_ENV | NF_PUNCTUAL)) return; // light origins without a surface
     const GpuInstance& I = S.instances[src.instance];
     d.w2o[0] = I.w2o[0];
     d.w2o[1] = I.w2o[1];
@@ -571,6 +642,41 @@ YG_DEV bool lightEndOfConnection(const SceneView& S, const BdptParams& B, const 
     ev.pdfFwd = 0.0f;
     ev.pdfBwd = 0.0f;
     ev.transmission = 0;
+    if (index == 0 && (n.flags & NF_PUNCTUAL))
+    {
+        // node radiance is intensity (point, spot) or irradiance (directional): no area density
+        const GpuLight& L = S.lights[n.prim];
+        const float pick = (1.0f - envSelectionPdf(S)) * L.selectionPdf;
+        if (L.type == kLightDirectional)
+        {
+            ev.pdfFwd = pick;
+            ev.weight = splat4(1.0f / pick);
+            pdfFwdMIS = pdfEnvPosition(B); // planar density; the cosine at the next vertex is the caller's
+        }
+        else
+        {
+            float3 fl = nextPos - n.pos;
+            float d2 = fmaxf(dot(fl, fl), 1e-10f);
+            float3 fd = fl * (1.0f / sqrtf(d2));
+            float fall = punctualFalloff(L, fd);
+            if (fall <= 0.0f)
+            {
+                pdfFwdMIS = 0.0f;
+                return false;
+            }
+            ev.pdfFwd = pick * d2;
+            ev.weight = splat4(fall / ev.pdfFwd);
+            // pdfPunctualLightEmissionDirection (lightSampling.hlsl:280-288)
+            if (L.type == kLightSpot)
+                pdfFwdMIS = dot(fd, mk3(L.directionCosOuter.x, L.directionCosOuter.y, L.directionCosOuter.z)) >= L.directionCosOuter.w
+                                ? pdfUniformCone(L.directionCosOuter.w)
+                                : 0.0f;
+            else
+                pdfFwdMIS = 1.0f / (4.0f * kPI);
+        }
+        ev.pdfBwd = 0.0f;
+        return true;
+    }
     if (index == 0 && (n.flags & NF_ENV))
     {
         float pdfDir = envSelectionPdf(S) * pdfEnvDirection(n.normal);
@@ -630,13 +736,21 @@ YG_DEV float misWeight(const SceneView& S, uint32_t camIndex, const CamVertex& c
     if (camIndex > 0)
         riCam = accumulateRISum(riCam, bwdCam * solidAngleToArea(cv.prevPos - cv.pos, cv.prevNormal), cv.prevPdfFwd);
     const bool env0 = lightIndex == 0 && (ln.flags & NF_ENV);
-    float toCamArea = env0 ? fwdLight * fabsf(dot(cv.normal, ln.normal)) : fwdLight * solidAngleToArea(cv.pos - ln.pos, cv.normal);
+    const bool inf0 = lightIndex == 0 && (ln.flags & NF_INFINITE);
+    float toCamArea = inf0 ? fwdLight * fabsf(dot(cv.normal, ln.normal)) : fwdLight * solidAngleToArea(cv.pos - ln.pos, cv.normal);
     riCam = accumulateRISum(riCam, toCamArea, cv.curPdfFwd);
     float riLight = lv.riSum;
     if (lightIndex == 0)
     {
         float pick, posPdf, dirPdf, toLight;
-        if (env0)
+        if (ln.flags & NF_PUNCTUAL)
+        {
+            // a camera path never hits a delta light
+            pick = 1.0f;
+            posPdf = 1.0f;
+            toLight = 0.0f;
+        }
+        else if (env0)
         {
             pick = envSelectionPdf(S);
             posPdf = pdfEnvDirection(ln.normal);
@@ -655,7 +769,9 @@ YG_DEV float misWeight(const SceneView& S, uint32_t camIndex, const CamVertex& c
     {
         float bwdPrev = bwdLight;
         bool prevEnv = lightIndex == 1 && (lv.originFlags & NF_ENV);
-        if (!prevEnv) bwdPrev *= solidAngleToArea(lv.prevPos - ln.pos, lv.prevNormal);
+        bool prevPunctual = lightIndex == 1 && (lv.originFlags & NF_PUNCTUAL);
+        if (prevPunctual) bwdPrev = 0.0f;
+        else if (!prevEnv) bwdPrev *= solidAngleToArea(lv.prevPos - ln.pos, lv.prevNormal);
         riLight = accumulateRISum(riLight, bwdPrev, lv.prevPdfFwd);
         riLight = accumulateRISum(riLight, fwdCam * solidAngleToArea(ln.pos - cv.pos, ln.normal), ln.pdfFwd);
     }
@@ -786,6 +902,11 @@ __global__ void __launch_bounds__(128) wbGenerate(const SceneView S, const Launc
         {
             RandomSampler rt{point, 2u, g ^ (P.seed * 0x9E3779B9u)};
             uint32_t h = (uint32_t)fminf(floorf(rt.r1() * (float)hc), (float)(hc - 1u));
+            // the headers are in light-path order, so header h would be the path whose hero
+            // wavelength was drawn from the same Sobol dimension with the seed h: a per-sample
+            // rotation (a hash of the sample index) keeps the chosen wavelength uniform, as the
+            // reference's atomically ordered headers do
+            h = (h + hash2(P.sppStart + f, P.seed ^ 0x2545F491u) % hc) % hc;
             path = B.valid[(size_t)f * B.lightPaths + h];
             count = B.counts[(size_t)f * B.lightPaths + path];
             hero = B.heroes[(size_t)f * B.lightPaths + path];
@@ -990,7 +1111,8 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                 if (!(ln.flags & NF_DELTA))
                 {
                     // getLightNodeConnection + calculateLightPathRadiance (BDPTCommon.hlsl:622-635, 1062-1215)
-                    const bool atInfinity = li == 0 && (ln.flags & NF_ENV);
+                    const bool atInfinity = li == 0 && (ln.flags & NF_INFINITE);
+                    const bool noGeometry = li == 0 && (ln.flags & (NF_ENV | NF_PUNCTUAL));
                     float3 toLightDir;
                     float dist;
                     if (atInfinity)
@@ -1029,8 +1151,9 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                             const float3 start = spawnRayOrigin(cv.pos, cv.normal, toLightDir);
                             ro = mk4(start.x, start.y, start.z, __uint_as_float(s));
                             rd = mk4(toLightDir.x, toLightDir.y, toLightDir.z,
-                                     atInfinity ? __int_as_float(0x7f800000) : kRayMinT + dist + kVisibilityEps);
-                            target = atInfinity ? make_uint2(0xffffffffu, 0xffffffffu) : make_uint2(ln.instance, ln.prim);
+                                     atInfinity ? __int_as_float(0x7f800000)
+                                                : (noGeometry ? dist - kRayMinT : kRayMinT + dist + kVisibilityEps));
+                            target = noGeometry ? make_uint2(0xffffffffu, 0xffffffffu) : make_uint2(ln.instance, ln.prim);
                         }
                     }
                 }
@@ -1241,6 +1364,7 @@ __global__ void __launch_bounds__(128) bdptLightTrace(const SceneView S, const L
                     {
                         bool prevEnv = i == 1 && (originFlags & NF_ENV);
                         float bwdPrev = ev.pdfBwd * (prevEnv ? 1.0f : solidAngleToArea(prevPos - n.pos, prevNormal));
+                        if (i == 1 && (originFlags & NF_PUNCTUAL)) bwdPrev = 0.0f; // a camera path never hits a delta light
                         float3 camToNode = n.pos - lensWS;
                         float pdfCam = cameraDirectionalPdf(S, P, camToNode);
                         float ri = accumulateRISum(riSum, bwdPrev, prevPdfFwd);

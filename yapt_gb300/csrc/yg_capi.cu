@@ -944,7 +944,6 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     const uint64_t maxSamplesPerChunk = bdpt ? (1ull << 24) : (1ull << 26);
     uint32_t chunkSpp = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->spp_count, maxSamplesPerChunk / npix));
     if (bdpt && (p->flags & YG_FLAG_MEGAKERNEL)) return fail(YG_ERR_INVALID_ARGUMENT, "render: BDPT has no megakernel variant");
-    if (bdpt && ctx->nPunctual) return fail(YG_ERR_INVALID_ARGUMENT, "render: BDPT with punctual lights is not available");
     const uint32_t lightVerts = p->bdpt_light_vertices ? p->bdpt_light_vertices : yg::kBdptMaxLightVertices;
     if (bdpt && (lightVerts < 2 || lightVerts > yg::kBdptMaxLightVertices))
         return fail(YG_ERR_INVALID_ARGUMENT, "render: bdpt_light_vertices must be 2..16");
