@@ -46,9 +46,9 @@ SERVE_METRIC = "serve: Msamples/s at full load with p50/p99 latency (Poisson arr
 # reach relMSE 1e-3: plain accumulation vs few-spp renders + the network, with a per-tile
 # fallback to plain accumulation where the two-half error estimate exceeds a threshold.
 DENOISE_WORKLOAD = dict(workload="denoise_unet_box_scenes_1080p", train_scenes=48, train_width=384, train_height=216,
-                        train_input_spp=[2, 4, 8, 16, 32], train_target_spp=2048, train_steps=12000, batch=8, crop=128, lr=1e-3,
+                        train_input_spp=[2, 4, 8, 16, 32], train_target_spp=8192, train_steps=12000, batch=8, crop=128, lr=1e-3,
                         lr_final=1e-5,
-                        eval_width=1920, eval_height=1080, eval_reference_spp=4096, eval_seed=100000, integrator="uni",
+                        eval_width=1920, eval_height=1080, eval_reference_spp=65536, eval_seed=100000, integrator="uni",
                         max_depth=8, tile=64, target_relmse=1e-3, lambda_nm=[380, 780])
 DENOISE_METRIC = "denoise: wall-time speed-up to relMSE 1e-3 at 1920x1080 (plain accumulation time / denoised time)"
 UNET_FLOP_PER_PIXEL = 2 * 9 * (16 * 32 + 32 * 32 + (32 * 64 + 64 * 64) / 4 + (64 * 128 + 128 * 128) / 16 +

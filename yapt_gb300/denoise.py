@@ -373,8 +373,9 @@ class DenoisePipeline:
     """The denoised render on the device: half render A, then B into the same film (so the
     film holds the full mean), the network on A and on the full input, the per-tile error
     estimate ((D(A) - D(full))^2 relative, equal to (D(A) - D(B))^2 / 4 for a linear
-    denoiser), and plain accumulation of the tiles above the threshold. Film means, features
-    and the packed input never leave the device."""
+    denoiser), and plain accumulation of the worst tiles until the estimated image error fits
+    the budget. Film means, features and the packed input never leave the device; only the
+    per-tile error estimates (one float a tile) come back to choose the tiles."""
 
     def __init__(self, net, ctx, height, width, tile=64, depth_scale=4.0):
         torch = net.torch
@@ -400,7 +401,29 @@ class DenoisePipeline:
         _check(lib.yg_nn_pack_input(fp(self.xyz), fp(self.alb), fp(self.nrm), fp(self.dep), C.c_float(self.depth_scale),
                                     self.h * self.w, C.byref(view(self.packed, 16, 0, 16)), self.net.stream()), "pack")
 
-    def run(self, spp, spp_plain, target, integrator="uni", max_depth=8, lambda_range=(380, 780), fallback_start=1 << 16):
+    def fallback_tiles(self, target, budget):
+        """Tiles to replace by plain accumulation. 4 x tile error estimates the variance part of
+        a tile's relMSE; a replaced tile is counted at the target (plain accumulation is run at
+        the sample count that reaches it). The worst tiles are replaced until the estimated
+        image relMSE is within budget x target; a tile that is not worse than the target is never
+        replaced."""
+        err = 4.0 * self.tile_err.cpu().numpy().astype(np.float64)
+        tx = (self.w + self.tile - 1) // self.tile
+        ty = (self.h + self.tile - 1) // self.tile
+        npx = np.array([min(self.tile, self.h - (t // tx) * self.tile) * min(self.tile, self.w - (t % tx) * self.tile)
+                        for t in range(tx * ty)], np.float64)
+        total = float(npx.sum())
+        cur = float((err * npx).sum() / total)
+        flags = np.zeros(len(err), np.int32)
+        for t in np.argsort(-err * npx):
+            if cur <= budget * target or err[t] <= target:
+                break
+            flags[t] = 1
+            cur += (target - err[t]) * npx[t] / total
+        return flags
+
+    def run(self, spp, spp_plain, target, integrator="uni", max_depth=8, lambda_range=(380, 780), fallback_start=1 << 16,
+            budget=0.5):
         """Returns (linear sRGB image h x w x 3 on the host, fallback tile count)."""
         ctx, net, lib, h, w = self.ctx, self.net, self.net.lib, self.h, self.w
         half = max(1, spp // 2)
@@ -417,7 +440,8 @@ class DenoisePipeline:
         _check(lib.yg_nn_tile_error(self._ptr(self.den_a), self._ptr(out), self._ptr(out), h, w, self.tile, C.c_float(EPS),
                                     C.c_float(target / 4.0), self._ptr(self.tile_err), self._ptr(self.tile_flags),
                                     net.stream()), "tile error")
-        flags = self.tile_flags.cpu().numpy()
+        flags = self.fallback_tiles(target, budget)
+        self.tile_flags.copy_(net.torch.from_numpy(flags))
         bad = np.nonzero(flags)[0]
         if len(bad):
             tx = (w + self.tile - 1) // self.tile
