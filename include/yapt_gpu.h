@@ -89,6 +89,19 @@ typedef struct yg_material
     int32_t specular_spectrum; /* -1: RGB specular */
     int32_t emission_spectrum; /* -1: RGB emission (times D65, as in the reference) */
     int32_t reserved;
+    /* Textures (MaterialEntryGPU *TexIndexAndScale, materialsCommon.hlsl:354-397): texture id
+     * + 1 from yg_upload_texture, 0 for none. Albedo multiplies the RGB albedo (alpha sets the
+     * transparency of alpha-blended materials), normal is a tangent-space normal map, ORM holds
+     * occlusion, roughness and metalness factors (glTF), emissive multiplies the RGB emission.
+     * Each texture's uv is multiplied by its scale. */
+    uint32_t albedo_texture;
+    uint32_t normal_texture;
+    uint32_t orm_texture;
+    uint32_t emissive_texture;
+    float albedo_uv_scale[2];
+    float normal_uv_scale[2];
+    float orm_uv_scale[2];
+    float emissive_uv_scale[2];
 } yg_material;
 
 /* Mesh upload (BindlessMeshManager + Mesh.setVertexBuffer/setIndexBuffer/setSubmesh). */
@@ -240,6 +253,19 @@ YG_API int yg_upload_materials(yg_context* ctx, const yg_material* materials, ui
 YG_API int yg_upload_spectra(yg_context* ctx, const float* values, uint32_t n_curves, uint32_t n_points,
                              float lambda_min, float lambda_max);
 YG_API int yg_set_instances(yg_context* ctx, const yg_instance* instances, uint32_t count);
+/* 2D textures (g_textures2D): decoded at upload to linear float RGBA and sampled bilinearly with
+ * wrapping at mip 0. RGBA8_UNORM: v / 255; RGBA8_SRGB: the sRGB transfer function on RGB (alpha
+ * linear); RGBA32_FLOAT as given. The id (0, 1, ...) is in upload order; materials refer to id + 1.
+ * yg_clear_textures drops them all (the materials' references must be updated too). */
+#define YG_TEXTURE_RGBA8_UNORM 0
+#define YG_TEXTURE_RGBA8_SRGB 1
+#define YG_TEXTURE_RGBA32_FLOAT 2
+YG_API int yg_upload_texture(yg_context* ctx, uint32_t width, uint32_t height, uint32_t format, const void* data,
+                             uint32_t* texture_id);
+YG_API int yg_clear_textures(yg_context* ctx);
+/* The environment (RVARNAME_SKYBOX with a longitude-latitude map): texture id + 1, or 0 for the
+ * reference's analytic |dir| sky. Scaled by env_intensity_scale of each request. */
+YG_API int yg_set_environment_texture(yg_context* ctx, uint32_t texture);
 /* Replaces the punctual lights (count 0 removes them). The light tables are rebuilt at once
  * when the scene is built, else by yg_build_scene. */
 YG_API int yg_set_punctual_lights(yg_context* ctx, const yg_punctual_light* lights, uint32_t count);

@@ -125,6 +125,53 @@ template <typename T> V3<T> refract(V3<T> i, V3<T> n, T eta)
 }
 
 // float3x3(t, n, b) rows (constructBasisTransform, commonMath.hlsl:128-133)
+// IEEE binary32 -> binary16, round to nearest, ties to even (HLSL f32tof16); subnormal
+// halves kept, overflow to infinity.
+inline uint16_t halfFromFloat(float f)
+{
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    x &= 0x7fffffffu;
+    if (x >= 0x7f800000u) return (uint16_t)(sign | (x > 0x7f800000u ? 0x7e00u : 0x7c00u));
+    if (x >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u); // >= 65520 rounds past the largest half
+    if (x >= 0x38800000u)                                   // normal half
+    {
+        uint32_t h = (((x >> 23) - 112u) << 10) | ((x & 0x7fffffu) >> 13);
+        const uint32_t rem = x & 0x1fffu;
+        if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+        return (uint16_t)(sign | h);
+    }
+    if (x < 0x33000000u) return (uint16_t)sign; // below half of the smallest subnormal
+    const uint32_t e = x >> 23, mant = (x & 0x7fffffu) | 0x800000u, shift = 126u - e;
+    uint32_t h = mant >> shift;
+    const uint32_t rem = mant & ((1u << shift) - 1u), halfway = 1u << (shift - 1u);
+    if (rem > halfway || (rem == halfway && (h & 1u))) ++h;
+    return (uint16_t)(sign | h);
+}
+
+inline float floatFromHalf(uint16_t h)
+{
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16, e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+    uint32_t x;
+    if (e == 0x1fu)
+        x = sign | 0x7f800000u | (m << 13);
+    else if (e != 0)
+        x = sign | ((e + 112u) << 23) | (m << 13);
+    else if (m == 0)
+        x = sign;
+    else
+    {
+        // subnormal: m * 2^-24, exact in binary32
+        float v = (float)m * 5.9604644775390625e-08f;
+        std::memcpy(&x, &v, 4);
+        x |= sign;
+    }
+    float f;
+    std::memcpy(&f, &x, 4);
+    return f;
+}
+
 template <typename T>
 struct Basis
 {
@@ -304,6 +351,9 @@ struct Ctx
     };
     uint32_t nPunctual = 0;
     std::vector<Light> lights;
+    // textures decoded to linear float RGBA (yg_upload_texture)
+    std::vector<std::vector<float>> tex;
+    std::vector<uint32_t> texW, texH;
     std::vector<float> instLightPdf;
     // world triangles and BVH
     struct Tri
@@ -912,6 +962,7 @@ struct Surf
     V3<T> coatN, baseN, geoN, tangent;
     T transparency, metalness, ior, roughness, cauchyA, cauchyB, specAmount, ccAmount, ccIOR, ccRough;
     T aniso, anisoRot, thinFilm, sheenRough, sheenAmount, focus, sssAmount;
+    T diffOcc = T(1), specOcc = T(1); // unpackOcclusion of the ORM texture's occlusion
     uint32_t flags;
 };
 template <typename T>
@@ -1044,7 +1095,7 @@ template <typename T, bool R> EvalR<T> evalSurfaceF(const LutSet<T>& L, const Su
                     T fms = fmsDielM<T, R>(L, eta, s.ccRough, std::fabs(dot(woC, wm)));
                     w += energyCompM<T, R>(L, fms, std::fabs(woC.y), std::fabs(wiC.y), s.ccRough, w);
                 }
-                S4<T> weight = sp(w) * (s.ccAmount * eLeft) * compC;
+                S4<T> weight = sp(w) * (s.ccAmount * eLeft) * compC * s.specOcc;
                 if (infer) coatAmp = weight;
                 else ws = ws + weight;
                 pdfSum += c.probs[0] * pdf;
@@ -1061,7 +1112,7 @@ template <typename T, bool R> EvalR<T> evalSurfaceF(const LutSet<T>& L, const Su
             if (pdf > 0 && bRefl)
             {
                 S4<T> w = sameHemi(woB, wiB) ? evalSheen(s.sheenColor, s.sheenRough, woB, wiB) * std::fabs(wiB.y) : sp(T(0));
-                ws = ws + w * (s.sheenAmount * eLeft) * compB;
+                ws = ws + w * (s.sheenAmount * eLeft) * compB * s.specOcc;
                 pdfSum += c.probs[1] * pdf;
             }
         }
@@ -1103,7 +1154,7 @@ template <typename T, bool R> EvalR<T> evalSurfaceF(const LutSet<T>& L, const Su
                         w[i] = (ss + ms) * std::fabs(wiB.y);
                     }
                 }
-                S4<T> weight = w * (s.metalness * eLeft) * compB;
+                S4<T> weight = w * (s.metalness * eLeft) * compB * s.specOcc;
                 if (infer)
                 {
                     T etaC = s.ccIOR / fromIOR;
@@ -1130,7 +1181,7 @@ template <typename T, bool R> EvalR<T> evalSurfaceF(const LutSet<T>& L, const Su
             T pdf = specPdf<T, R>(L, sl, woB, wiB);
             if (pdf > 0)
             {
-                S4<T> weight = sp(specEval<T, R>(L, sl, woB, wiB)) * (specAmount * eLeft) * compB;
+                S4<T> weight = sp(specEval<T, R>(L, sl, woB, wiB)) * (specAmount * eLeft) * compB * s.specOcc;
                 if (infer)
                 {
                     T etaC = s.ccIOR / fromIOR;
@@ -1153,7 +1204,7 @@ template <typename T, bool R> EvalR<T> evalSurfaceF(const LutSet<T>& L, const Su
         {
             S4<T> alb = s.albedo / C<T>::PI;
             S4<T> w = sameHemi(woB, wiB) ? alb * std::fabs(wiB.y) : sp(T(0));
-            ws = ws + w * (diffAmount * eLeft) * compB;
+            ws = ws + w * (diffAmount * eLeft) * compB * s.diffOcc;
             pdfSum += c.probs[4] * pdf;
         }
     }
@@ -1179,7 +1230,7 @@ template <typename T, bool R> EvalR<T> evalSurfaceF(const LutSet<T>& L, const Su
                 r.trans |= c.exiting ? 2u : 1u;
             }
             else r.trans |= 3u;
-            ws = ws + sp(specEval<T, R>(L, sl, woB, wiB)) * (transAmount * eLeft) * comp * compB;
+            ws = ws + sp(specEval<T, R>(L, sl, woB, wiB)) * (transAmount * eLeft) * comp * compB * s.specOcc;
         }
     }
     r.pdf = pdfSum;
@@ -1445,6 +1496,35 @@ template <typename T> bool setup(Ctx<T>& c, const oracle_scene* sc, const Tables
     c.tb = tb;
     c.lmin = lmin;
     c.lmax = lmax;
+    // textures as yg_upload_texture decodes them (8-bit: v / 255, or the sRGB transfer function
+    // of IEC 61966-2-1 in double on RGB)
+    for (uint32_t t = 0; t < sc->n_textures; ++t)
+    {
+        const oracle_texture& X = sc->textures[t];
+        const size_t n = (size_t)X.width * X.height;
+        std::vector<float> v(4 * n);
+        if (X.format == YG_TEXTURE_RGBA32_FLOAT)
+            std::memcpy(v.data(), X.data, 4 * n * sizeof(float));
+        else
+        {
+            float lut[256];
+            for (int k = 0; k < 256; ++k)
+            {
+                double x = k / 255.0;
+                lut[k] = X.format == YG_TEXTURE_RGBA8_SRGB ? (float)(x <= 0.04045 ? x / 12.92 : std::pow((x + 0.055) / 1.055, 2.4))
+                                                           : (float)x;
+            }
+            const uint8_t* b = static_cast<const uint8_t*>(X.data);
+            for (size_t i = 0; i < n; ++i)
+            {
+                for (int k = 0; k < 3; ++k) v[4 * i + k] = lut[b[4 * i + k]];
+                v[4 * i + 3] = (float)(b[4 * i + 3] / 255.0);
+            }
+        }
+        c.tex.push_back(std::move(v));
+        c.texW.push_back(X.width);
+        c.texH.push_back(X.height);
+    }
     int a = (int)lmin, b = (int)lmax;
     double ys = 0, ds = 0;
     for (int l = a; l <= b; ++l)
@@ -1688,6 +1768,54 @@ template <typename T> T regularizeR(T lr, bool sq)
     return lr;
 }
 
+// Texture2D.SampleLevel(LINEAR_REPEAT, uv, 0) restated: bilinear between the four nearest
+// texel centres with wrapped coordinates, in the same arithmetic order as the device
+template <typename T> void sampleTex(const Ctx<T>& c, int id, T u0, T v0, T out[4])
+{
+    const std::vector<float>& tx = c.tex[id];
+    const int W = (int)c.texW[id], H = (int)c.texH[id];
+    T u = u0 - std::floor(u0), v = v0 - std::floor(v0);
+    T x = u * T(W) - T(0.5f), y = v * T(H) - T(0.5f);
+    T fx = std::floor(x), fy = std::floor(y);
+    T ax = x - fx, ay = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    x0 = x0 < 0 ? x0 + W : (x0 >= W ? x0 - W : x0);
+    y0 = y0 < 0 ? y0 + H : (y0 >= H ? y0 - H : y0);
+    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    const float* c00 = &tx[4 * ((size_t)y0 * W + x0)];
+    const float* c10 = &tx[4 * ((size_t)y0 * W + x1)];
+    const float* c01 = &tx[4 * ((size_t)y1 * W + x0)];
+    const float* c11 = &tx[4 * ((size_t)y1 * W + x1)];
+    const T sx = T(1) - ax, sy = T(1) - ay;
+    for (int k = 0; k < 4; ++k)
+        out[k] = (T(c00[k]) * sx + T(c10[k]) * ax) * sy + (T(c01[k]) * sx + T(c11[k]) * ax) * ay;
+}
+
+// fetchMeshUV or (0.5, 0.5) without texture coordinates
+template <typename T> void meshUV(const oracle_scene* sc, const oracle_instance& I, const uint32_t id[3], T b0, T b1, T b2,
+                                  T& u, T& v)
+{
+    if (!I.has_uvs || !sc->uvs)
+    {
+        u = v = T(0.5f);
+        return;
+    }
+    const float* U = sc->uvs;
+    u = T(U[2 * id[0]]) * b0 + T(U[2 * id[1]]) * b1 + T(U[2 * id[2]]) * b2;
+    v = T(U[2 * id[0] + 1]) * b0 + T(U[2 * id[1] + 1]) * b1 + T(U[2 * id[2] + 1]) * b2;
+}
+
+// getSkyBoxColor (materialsCommonResources.hlsl:181-224) times the intensity scale
+template <typename T> V3<T> skyColor(const Ctx<T>& c, V3<T> d, T scale)
+{
+    if (!c.sc->env_texture) return v3(std::fabs(d.x) * scale, std::fabs(d.y) * scale, std::fabs(d.z) * scale);
+    V3<T> v = normalize(d);
+    T theta = std::atan2(v.z, v.x), phi = std::acos(clampT(v.y, T(-1), T(1)));
+    T t[4];
+    sampleTex(c, (int)c.sc->env_texture - 1, theta * C<T>::INVPI * T(0.5f) + T(0.5f), phi * C<T>::INVPI, t);
+    return v3(t[0] * scale, t[1] * scale, t[2] * scale);
+}
+
 // fetch + fetchSurfaceMaterialParameters (with the BindlessMaterialManager clamps) +
 // handleTwoSidedMaterialOrientation (when orient) + setupSurfaceOrientation + regularisation (when
 // regularize) + convertSurfaceDefinitionFromRGB (rayHitDefault.hlsl:470-520, hitShadersCommon.hlsl:51-91)
@@ -1752,6 +1880,39 @@ template <typename T> void fillSurf(const Ctx<T>& c, const Spec<T>& s4, uint32_t
         V3<T> t = s.tangent;
         s.tangent = v3(ca * t.x + T(0) * t.y + sa * t.z, T(0) * t.x + T(1) * t.y + T(0) * t.z, -sa * t.x + T(0) * t.y + ca * t.z);
     }
+    // modifySurfaceMaterialParametersWithTextures (materialsCommon.hlsl:354-397)
+    float alb[3] = {M.albedo[0], M.albedo[1], M.albedo[2]}, emi[3] = {M.emissive[0], M.emissive[1], M.emissive[2]};
+    s.diffOcc = s.specOcc = T(1);
+    if (M.albedo_texture || M.normal_texture || M.orm_texture || M.emissive_texture)
+    {
+        T u, v, t[4];
+        meshUV(sc, I, id, b0, b1, b2, u, v);
+        if (M.albedo_texture)
+        {
+            sampleTex(c, (int)M.albedo_texture - 1, u * T(M.albedo_uv_scale[0]), v * T(M.albedo_uv_scale[1]), t);
+            for (int k = 0; k < 3; ++k) alb[k] = (float)(T(M.albedo[k]) * t[k]);
+            if (s.flags & YG_MATERIAL_ALPHA_BLEND) s.transparency = T(1) - t[3] * (T(1) - s.transparency);
+        }
+        if (M.normal_texture)
+        {
+            sampleTex(c, (int)M.normal_texture - 1, u * T(M.normal_uv_scale[0]), v * T(M.normal_uv_scale[1]), t);
+            V3<T> nn = normalize(v3(t[0] * T(2) - T(1), t[1] * T(2) - T(1), t[2] * T(2) - T(1)));
+            s.baseN = mulvM(v3(nn.x, nn.z, nn.y), basis(s.baseN, s.tangent));
+        }
+        if (M.orm_texture)
+        {
+            sampleTex(c, (int)M.orm_texture - 1, u * T(M.orm_uv_scale[0]), v * T(M.orm_uv_scale[1]), t);
+            T occ = T(floatFromHalf(halfFromFloat((float)t[0]))); // packOcclusion: a half
+            s.diffOcc = s.specOcc = occ;
+            s.roughness = s.roughness * t[1];
+            s.metalness = s.metalness * t[2];
+        }
+        if (M.emissive_texture)
+        {
+            sampleTex(c, (int)M.emissive_texture - 1, u * T(M.emissive_uv_scale[0]), v * T(M.emissive_uv_scale[1]), t);
+            for (int k = 0; k < 3; ++k) emi[k] = (float)(T(M.emissive[k]) * t[k]);
+        }
+    }
     if (regularize)
     {
         s.roughness = regularizeR(s.roughness, true);
@@ -1759,10 +1920,10 @@ template <typename T> void fillSurf(const Ctx<T>& c, const Spec<T>& s4, uint32_t
         s.ccRough = regularizeR(s.ccRough, true);
     }
     s.specular = reflectance(c, s4, M.specular, M.specular_spectrum);
-    s.albedo = reflectance(c, s4, M.albedo, M.albedo_spectrum);
+    s.albedo = reflectance(c, s4, alb, M.albedo_spectrum);
     bool absZero = M.absorption[0] == 0 && M.absorption[1] == 0 && M.absorption[2] == 0;
     s.absorption = absZero ? sp(T(0)) : setFromRGBUnboundedNoIllum(c, s4, v3(T(M.absorption[0]), T(M.absorption[1]), T(M.absorption[2])));
-    s.emissive = emission(c, s4, M.emissive, M.emission_spectrum);
+    s.emissive = emission(c, s4, emi, M.emission_spectrum);
     s.sheenColor = s.sheenAmount > T(0) ? setFromRGB(c, s4, v3(T(M.sheen_tint[0]), T(M.sheen_tint[1]), T(M.sheen_tint[2]))) : sp(T(0));
 }
 
@@ -1855,7 +2016,7 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
         {
             // rayMissEnvironment (rayMissEnvironment.hlsl:13-31)
             T sc4 = T(P.env_intensity_scale);
-            V3<T> col = v3(std::fabs(ps.d.x) * sc4, std::fabs(ps.d.y) * sc4, std::fabs(ps.d.z) * sc4);
+            V3<T> col = skyColor(c, ps.d, sc4);
             S4<T> Le = isZero(col) ? sp(T(0)) : setFromRGBUnbounded(c, s4, col);
             ps.total = ps.total + ps.thr * Le;
             alive = false;
@@ -2007,7 +2168,16 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                     g = g / gl;
                     T area = gl * T(0.5f);
                     V3<T> lpos = p1 * lb0 + p2 * bx + p3 * by;
-                    S4<T> rad = emission(c, s4, LM.emissive, LM.emission_spectrum);
+                    float lem[3] = {LM.emissive[0], LM.emissive[1], LM.emissive[2]};
+                    if (LM.emissive_texture)
+                    {
+                        // modifySurfaceEmissionWithTexture at the sampled point
+                        T u, v, t[4];
+                        meshUV(sc, LI, qi, lb0, bx, by, u, v);
+                        sampleTex(c, (int)LM.emissive_texture - 1, u * T(LM.emissive_uv_scale[0]), v * T(LM.emissive_uv_scale[1]), t);
+                        for (int k = 0; k < 3; ++k) lem[k] = (float)(T(LM.emissive[k]) * t[k]);
+                    }
+                    S4<T> rad = emission(c, s4, lem, LM.emission_spectrum);
                     T pdfPos = T(1) / (T(pc) * area);
                     bool two = (LM.material_mask & YG_MATERIAL_TWO_SIDED) != 0;
                     V3<T> toL = lpos - hitPos;
@@ -2139,7 +2309,7 @@ inline bool needsRgbTable(const oracle_scene* sc, const yg_render_params* P)
         const yg_material& m = sc->materials[i];
         if ((m.albedo_spectrum < 0 && nonGrey(m.albedo)) || (m.specular_spectrum < 0 && nonGrey(m.specular)) ||
             (m.emission_spectrum < 0 && nonGrey(m.emissive)) || (nonZero(m.absorption) && nonGrey(m.absorption)) ||
-            (m.sheen_amount > 0.0f && nonGrey(m.sheen_tint)))
+            (m.sheen_amount > 0.0f && nonGrey(m.sheen_tint)) || m.albedo_texture || m.emissive_texture)
             return true;
     }
     for (uint32_t i = 0; i < sc->n_punctual; ++i)

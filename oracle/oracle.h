@@ -31,8 +31,15 @@ typedef struct oracle_instance
     uint32_t vertex_base;
     uint32_t material;
     uint32_t has_tangents;
-    uint32_t reserved[3];
+    uint32_t has_uvs;
+    uint32_t reserved[2];
 } oracle_instance;
+
+typedef struct oracle_texture
+{
+    const void* data; /* width*height RGBA texels in the yg_upload_texture format */
+    uint32_t width, height, format, reserved;
+} oracle_texture;
 
 typedef struct oracle_scene
 {
@@ -54,6 +61,10 @@ typedef struct oracle_scene
     const char* data_dir;     /* CIE + Joe-Kuo data files */
     const yg_punctual_light* punctual; /* may be NULL when n_punctual is 0 */
     uint32_t n_punctual;
+    const float* uvs;                  /* 2 per vertex (may be NULL when no instance has uvs) */
+    const oracle_texture* textures;    /* materials refer to id + 1 */
+    uint32_t n_textures;
+    uint32_t env_texture;              /* id + 1 of a longitude-latitude environment, 0: |dir| */
 } oracle_scene;
 
 typedef struct oracle_stats

@@ -22,7 +22,12 @@ from yapt_gb300 import _native as N  # noqa: E402  (struct layouts of include/ya
 class OracleInstance(C.Structure):
     _fields_ = [("o2w", C.c_float * 12), ("w2o", C.c_float * 12), ("first_index", C.c_uint32),
                 ("prim_count", C.c_uint32), ("vertex_base", C.c_uint32), ("material", C.c_uint32),
-                ("has_tangents", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("has_tangents", C.c_uint32), ("has_uvs", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+
+
+class OracleTexture(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("format", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class OracleScene(C.Structure):
@@ -33,7 +38,9 @@ class OracleScene(C.Structure):
                 ("spectra", C.POINTER(C.c_float)), ("spec_points", C.c_uint32), ("spec_lmin", C.c_float),
                 ("spec_lmax", C.c_float), ("camera", C.POINTER(N.Camera)), ("luts", C.POINTER(C.c_float) * 9),
                 ("rgb_to_spd", C.POINTER(C.c_float)), ("data_dir", C.c_char_p),
-                ("punctual", C.POINTER(N.PunctualLight)), ("n_punctual", C.c_uint32)]
+                ("punctual", C.POINTER(N.PunctualLight)), ("n_punctual", C.c_uint32),
+                ("uvs", C.POINTER(C.c_float)), ("textures", C.POINTER(OracleTexture)), ("n_textures", C.c_uint32),
+                ("env_texture", C.c_uint32)]
 
 
 class OracleStats(C.Structure):
@@ -101,6 +108,7 @@ class OracleSceneHandle:
             inst[i].vertex_base = d["vertex_base"]
             inst[i].material = d["material"]
             inst[i].has_tangents = 1 if d["has_tangents"] else 0
+            inst[i].has_uvs = 1 if d["has_uvs"] else 0
         mats = scene.material_structs()
         spec = fp(scene.spectra_array() if len(scene.spectra) else np.zeros((1, 81), np.float32))
         cam = scene.camera.struct()
@@ -125,7 +133,16 @@ class OracleSceneHandle:
         pl = scene.punctual_structs()
         s.punctual = pl
         s.n_punctual = len(scene.punctual_lights)
-        self.keep += [inst, mats, cam, pl]
+        s.uvs = fp(pool["uvs"]).ctypes.data_as(C.POINTER(C.c_float))
+        tx = (OracleTexture * max(1, len(scene.textures)))()
+        for i, (w, h, fmt, a) in enumerate(scene.textures):
+            self.keep.append(a)
+            tx[i].data = a.ctypes.data_as(C.c_void_p)
+            tx[i].width, tx[i].height, tx[i].format = w, h, fmt
+        s.textures = tx
+        s.n_textures = len(scene.textures)
+        s.env_texture = scene.env_texture
+        self.keep += [inst, mats, cam, pl, tx]
         self.s = s
 
     def render(self, params, precision=32, threads=None, records=True, film=False):

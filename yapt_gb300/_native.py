@@ -23,6 +23,7 @@ YG_FLAG_COUNT_TRAVERSAL = 1 << 10
 YG_FLAG_MEGAKERNEL = 1 << 11
 YG_FLAG_TIME_KERNELS = 1 << 12
 YG_FLAG_ATROUS_FEATURES = 1 << 13
+YG_TEXTURE_RGBA8_UNORM, YG_TEXTURE_RGBA8_SRGB, YG_TEXTURE_RGBA32_FLOAT = 0, 1, 2
 YG_NN_CONV_MMA_SYNC = 0
 YG_NN_CONV_TCGEN05 = 1
 YG_NN_CONV_TCGEN05_TMA = 2
@@ -49,6 +50,9 @@ class Material(C.Structure):
         ("subsurface_radius_scale", C.c_float), ("alpha_cutoff", C.c_float),
         ("albedo_spectrum", C.c_int32), ("specular_spectrum", C.c_int32),
         ("emission_spectrum", C.c_int32), ("reserved", C.c_int32),
+        ("albedo_texture", C.c_uint32), ("normal_texture", C.c_uint32), ("orm_texture", C.c_uint32),
+        ("emissive_texture", C.c_uint32), ("albedo_uv_scale", C.c_float * 2), ("normal_uv_scale", C.c_float * 2),
+        ("orm_uv_scale", C.c_float * 2), ("emissive_uv_scale", C.c_float * 2),
     ]
 
 
@@ -179,6 +183,9 @@ SIGNATURES = [
     ("yg_clear_meshes", C.c_int, [C.c_void_p]),
     ("yg_film_resolve_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("yg_set_punctual_lights", C.c_int, [C.c_void_p, C.POINTER(PunctualLight), C.c_uint32]),
+    ("yg_upload_texture", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32)]),
+    ("yg_clear_textures", C.c_int, [C.c_void_p]),
+    ("yg_set_environment_texture", C.c_int, [C.c_void_p, C.c_uint32]),
     ("yg_atrous_default_params", None, [C.POINTER(AtrousParams)]),
     ("yg_atrous_denoise", C.c_int, [C.c_void_p, C.POINTER(AtrousParams), C.c_void_p, C.c_void_p]),
     ("yg_atrous_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

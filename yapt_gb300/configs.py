@@ -17,6 +17,7 @@ distributions of the benchmark definitions:
 """
 import numpy as np
 
+from . import _native as N
 from .scene import (SPECTRUM_LMAX, SPECTRUM_LMIN, SPECTRUM_POINTS, CameraDesc, Scene, affine, rotation_y)
 
 GRID = np.linspace(SPECTRUM_LMIN, SPECTRUM_LMAX, SPECTRUM_POINTS)
@@ -201,6 +202,53 @@ def layered_box_scene(seed=0, light_intensity=12.0, aspect=1.0):
                 anisotropy=0.7, anisotropy_rotation=0.2)
     m[6].update(metalness=1.0, roughness=0.2, specular=(0.9, 0.9, 0.9), specular_amount=1.0,
                 clear_coat_amount=1.0, clear_coat_ior=1.45, clear_coat_roughness=0.1, thin_film_thickness_nm=420.0)
+    return sc
+
+
+def textured_box_scene(seed=0, aspect=1.0):
+    """``box_scene`` with textures in every material slot the reference has
+    (materialsCommon.hlsl:354-397): an 8 x 8 checker albedo (sRGB, uv scale 3) on the floor,
+    a bump normal map plus an occlusion/roughness/metalness map (linear) on a metallic back
+    wall, and an emission gradient on the ceiling light. Quad faces get uv (0,0)-(1,1)."""
+    rng = np.random.Generator(np.random.PCG64(1000 + seed))
+    sc = box_scene(seed, aspect=aspect)
+    sc.name = "textured_box(seed=%d)" % seed
+    for m in sc.meshes:
+        m["uvs"] = np.tile(np.float32([[0, 0], [1, 0], [1, 1], [0, 1]]), (len(m["positions"]) // 4, 1))
+    ij = np.indices((64, 64)).sum(axis=0) // 8
+    c0, c1 = rng.integers(40, 250, 3), rng.integers(40, 250, 3)
+    checker = np.where((ij % 2 == 0)[..., None], c0, c1).astype(np.uint8)
+    checker = np.concatenate([checker, np.full((64, 64, 1), 255, np.uint8)], axis=2)
+    y, x = np.mgrid[0:32, 0:32] / 32.0
+    nx, ny = 0.35 * np.cos(2 * np.pi * 3 * x), 0.35 * np.sin(2 * np.pi * 2 * y)
+    n = np.stack([nx, ny, np.ones_like(nx)], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    normal = np.concatenate([np.round((n * 0.5 + 0.5) * 255), np.full((32, 32, 1), 255)], -1).astype(np.uint8)
+    orm = np.stack([0.5 + 0.5 * x, 0.3 + 0.7 * y, (x > 0.5).astype(float), np.ones_like(x)], -1)
+    orm = np.round(orm * 255).astype(np.uint8)
+    glow = np.stack([0.3 + 0.7 * x[:16, :16] * 2, np.full((16, 16), 0.8), 0.5 + 0.5 * y[:16, :16] * 2, np.ones((16, 16))], -1)
+    glow = np.round(np.clip(glow, 0, 1) * 255).astype(np.uint8)
+    t_checker = sc.add_texture(checker)
+    t_normal = sc.add_texture(normal, N.YG_TEXTURE_RGBA8_UNORM)
+    t_orm = sc.add_texture(orm, N.YG_TEXTURE_RGBA8_UNORM)
+    t_glow = sc.add_texture(glow, N.YG_TEXTURE_RGBA8_UNORM)
+    m = sc.materials
+    m[0].update(albedo_spectrum=-1, albedo=(0.9, 0.9, 0.9), albedo_texture=t_checker, albedo_uv_scale=(3.0, 3.0))
+    m[2].update(metalness=1.0, specular=(0.9, 0.85, 0.8), specular_amount=1.0, roughness=0.6, normal_texture=t_normal,
+                orm_texture=t_orm)
+    m[7].update(emissive_texture=t_glow)
+    return sc
+
+
+def environment_sky_scene(seed=0, aspect=1.0):
+    """``sky_scene`` under a longitude-latitude environment map (getSkyBoxColor with
+    ENVIRONMENT_TYPE_LONGLAT): a float RGBA gradient sky with a warm band near the horizon."""
+    sc = sky_scene(seed, aspect=aspect)
+    sc.name = "environment_sky(seed=%d)" % seed
+    v, u = np.mgrid[0:32, 0:64] / np.array([32.0, 64.0])[:, None, None]
+    sky = np.stack([0.4 + 0.6 * np.exp(-((v - 0.5) / 0.1) ** 2) + 0.2 * u, 0.5 + 0.3 * (1 - v), 0.9 - 0.5 * v, np.ones_like(u)],
+                   -1).astype(np.float32)
+    sc.env_texture = sc.add_texture(sky)
     return sc
 
 

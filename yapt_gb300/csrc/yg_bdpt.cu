@@ -154,7 +154,7 @@ YG_DEV float pdfEnvPosition(const BdptParams& B) { return safeDiv(1.0f, kPI * B.
 // getSkyBoxColor without an environment map (|dir|) as an unbounded RGB emitter
 YG_DEV float4 skyRadiance(const SceneView& S, const LaunchParams& P, const Spectral& sp, float3 d)
 {
-    float3 col = mk3(fabsf(d.x) * P.envScale, fabsf(d.y) * P.envScale, fabsf(d.z) * P.envScale);
+    float3 col = skyColor(S, d, P.envScale);
     return isZero3(col) ? splat4(0.0f) : fromRGBUnbounded(S, sp, col);
 }
 // constructVectorBase (commonMath.hlsl:87-93)

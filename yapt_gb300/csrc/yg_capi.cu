@@ -51,6 +51,10 @@ yg::GpuMaterial packMaterial(const yg_material& m)
     g.albedoSpectrum = m.albedo_spectrum;
     g.specularSpectrum = m.specular_spectrum;
     g.emissionSpectrum = m.emission_spectrum;
+    g.textures = make_int4((int)m.albedo_texture - 1, (int)m.normal_texture - 1, (int)m.orm_texture - 1,
+                           (int)m.emissive_texture - 1);
+    g.albedoNormalScale = make_float4(m.albedo_uv_scale[0], m.albedo_uv_scale[1], m.normal_uv_scale[0], m.normal_uv_scale[1]);
+    g.ormEmissiveScale = make_float4(m.orm_uv_scale[0], m.orm_uv_scale[1], m.emissive_uv_scale[0], m.emissive_uv_scale[1]);
     return g;
 }
 
@@ -207,6 +211,8 @@ bool sceneNeedsRgbLut(const yg_context* c, float envScale)
     }
     for (const yg_punctual_light& L : c->punctual)
         if (!isGreyOrZero(L.intensity)) return true;
+    for (const yg_material& m : c->materials)
+        if (m.albedo_texture || m.emissive_texture) return true; // texels may be coloured
     return false;
 }
 
@@ -250,6 +256,8 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.normals = ctx->dNrm.as<float>();
     S.tangents = ctx->dTan.as<float4>();
     S.uvs = ctx->dUV.as<float2>();
+    S.textures = ctx->dTexTable.as<yg::GpuTexture>();
+    S.envTexture = ctx->envTexture;
     S.indices = ctx->dIdx.as<uint32_t>();
     S.spectra = ctx->dSpec.as<float>();
     S.lutSS = ctx->dLut[0].as<float>();
@@ -531,6 +539,68 @@ YG_API int yg_upload_materials(yg_context* ctx, const yg_material* mats, uint32_
     for (uint32_t i = 0; i < count; ++i) ctx->gpuMaterials[i] = packMaterial(mats[i]);
     ctx->sceneBuilt = false;
     return upload(ctx, ctx->dMat, ctx->gpuMaterials.data(), ctx->gpuMaterials.size());
+}
+
+// sRGB electro-optical transfer function (IEC 61966-2-1), in double
+static double srgbToLinear(double c) { return c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4); }
+
+YG_API int yg_upload_texture(yg_context* ctx, uint32_t width, uint32_t height, uint32_t format, const void* data,
+                             uint32_t* texture_id)
+{
+    if (!ctx || !data || !texture_id) return fail(YG_ERR_INVALID_ARGUMENT, "texture: null argument");
+    if (width == 0 || height == 0 || width > 32768 || height > 32768) return fail(YG_ERR_INVALID_ARGUMENT, "texture: bad size");
+    if (format > YG_TEXTURE_RGBA32_FLOAT) return fail(YG_ERR_INVALID_ARGUMENT, "texture: unknown format");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t n = (size_t)width * height;
+    std::vector<float4> texels(n);
+    if (format == YG_TEXTURE_RGBA32_FLOAT)
+    {
+        const float* f = static_cast<const float*>(data);
+        for (size_t i = 0; i < 4 * n; ++i)
+            if (!std::isfinite(f[i])) return fail(YG_ERR_INVALID_ARGUMENT, "texture: non-finite texel");
+        std::memcpy(texels.data(), f, n * sizeof(float4));
+    }
+    else
+    {
+        float lut[256];
+        for (int v = 0; v < 256; ++v)
+            lut[v] = format == YG_TEXTURE_RGBA8_SRGB ? (float)srgbToLinear(v / 255.0) : (float)(v / 255.0);
+        const uint8_t* b = static_cast<const uint8_t*>(data);
+        for (size_t i = 0; i < n; ++i)
+            texels[i] = make_float4(lut[b[4 * i]], lut[b[4 * i + 1]], lut[b[4 * i + 2]], (float)(b[4 * i + 3] / 255.0));
+    }
+    cudaSetDevice(ctx->device);
+    DevBuf buf;
+    int r = upload(ctx, buf, texels.data(), n);
+    if (r) return r;
+    ctx->texBufs.push_back(buf);
+    ctx->texTable.push_back(yg::GpuTexture{buf.as<float4>(), width, height});
+    if ((r = upload(ctx, ctx->dTexTable, ctx->texTable.data(), ctx->texTable.size()))) return r;
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    *texture_id = (uint32_t)ctx->texTable.size() - 1;
+    return YG_OK;
+}
+
+YG_API int yg_clear_textures(yg_context* ctx)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "textures: null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    cudaSetDevice(ctx->device);
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (DevBuf& b : ctx->texBufs) b.release();
+    ctx->texBufs.clear();
+    ctx->texTable.clear();
+    ctx->envTexture = -1;
+    return YG_OK;
+}
+
+YG_API int yg_set_environment_texture(yg_context* ctx, uint32_t texture)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "environment: null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    if (texture > ctx->texTable.size()) return fail(YG_ERR_INVALID_ARGUMENT, "environment: unknown texture");
+    ctx->envTexture = (int)texture - 1;
+    return YG_OK;
 }
 
 YG_API int yg_upload_spectra(yg_context* ctx, const float* values, uint32_t n_curves, uint32_t n_points, float lmin,
@@ -938,6 +1008,10 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     if (r) return r;
     bool needRgb = sceneNeedsRgbLut(ctx, p->env_intensity_scale);
     if (needRgb && (r = ensureRgbLut(ctx, lmin, lmax))) return r;
+    const size_t nTex = ctx->texTable.size();
+    for (const yg_material& m : ctx->materials)
+        if (m.albedo_texture > nTex || m.normal_texture > nTex || m.orm_texture > nTex || m.emissive_texture > nTex)
+            return fail(YG_ERR_INVALID_ARGUMENT, "render: a material refers to a texture that was not uploaded");
 
     const uint64_t npix = (uint64_t)cw * ch;
     const bool bdpt = p->integrator == YG_INTEGRATOR_BDPT;

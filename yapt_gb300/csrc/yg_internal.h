@@ -107,6 +107,10 @@ struct yg_context
     DevBuf dCie, dRgb, dSobol, dSobolMat, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
     DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena, dPerm;
     DevBuf dAtrousMom, dAtrousOdd, dAtrousFeat, dAtrousCol, dAtrousVar; // a-trous denoiser state
+    std::vector<DevBuf> texBufs;          // decoded texels of each texture
+    std::vector<yg::GpuTexture> texTable; // device pointers and sizes, mirrored in dTexTable
+    DevBuf dTexTable;
+    int envTexture = -1;
     uint32_t nLights = 0;   // mesh and punctual
     uint32_t nPunctual = 0;
     std::vector<yg_punctual_light> punctual;
@@ -137,6 +141,8 @@ struct yg_context
                          &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm, &dAtrousMom, &dAtrousOdd,
                          &dAtrousFeat, &dAtrousCol, &dAtrousVar};
         for (DevBuf* b : all) b->release();
+        for (DevBuf& b : texBufs) b.release();
+        dTexTable.release();
         for (auto& b : dLut) b.release();
         for (cudaEvent_t e : kernelEvents) cudaEventDestroy(e);
         if (evStart) cudaEventDestroy(evStart);

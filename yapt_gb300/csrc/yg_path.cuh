@@ -11,6 +11,7 @@
 // wavefront and the megakernel give bit-identical samples.
 #pragma once
 #include "yg_shading.cuh"
+#include <cuda_fp16.h>
 #include "yg_trace.cuh"
 
 namespace yg
@@ -113,6 +114,49 @@ YG_DEV float3 interp3(const float* A, const TriGeom& g, float b0, float b1, floa
     float3 b = mk3(__ldg(A + 3 * g.i2), __ldg(A + 3 * g.i2 + 1), __ldg(A + 3 * g.i2 + 2));
     float3 c = mk3(__ldg(A + 3 * g.i3), __ldg(A + 3 * g.i3 + 1), __ldg(A + 3 * g.i3 + 2));
     return a * b0 + b * b1 + c * b2;
+}
+
+// Texture2D.SampleLevel(LINEAR_REPEAT, uv, 0): bilinear between the four nearest texel
+// centres, coordinates wrapped. Done in FP32 arithmetic (not the texture unit's 8-bit
+// fraction) so that a CPU restatement computes the same value.
+YG_DEV float4 sampleTexture(const SceneView& S, int id, float2 uv)
+{
+    const GpuTexture T = S.textures[id];
+    const float w = (float)T.width, h = (float)T.height;
+    float u = uv.x - floorf(uv.x), v = uv.y - floorf(uv.y);
+    float x = u * w - 0.5f, y = v * h - 0.5f;
+    float fx = floorf(x), fy = floorf(y);
+    float tx = x - fx, ty = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    const int W = (int)T.width, H = (int)T.height;
+    x0 = x0 < 0 ? x0 + W : (x0 >= W ? x0 - W : x0);
+    y0 = y0 < 0 ? y0 + H : (y0 >= H ? y0 - H : y0);
+    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    const float4 c00 = __ldg(T.texels + (size_t)y0 * W + x0), c10 = __ldg(T.texels + (size_t)y0 * W + x1);
+    const float4 c01 = __ldg(T.texels + (size_t)y1 * W + x0), c11 = __ldg(T.texels + (size_t)y1 * W + x1);
+    const float sx = 1.0f - tx, sy = 1.0f - ty;
+    return (c00 * sx + c10 * tx) * sy + (c01 * sx + c11 * tx) * ty;
+}
+
+// fetchMeshUV, or (0.5, 0.5) for a mesh without texture coordinates (hitShadersCommon.hlsl:198)
+YG_DEV float2 meshUV(const SceneView& S, const GpuInstance& I, const TriGeom& g, float b0, float b1, float b2)
+{
+    if (!I.hasUVs) return make_float2(0.5f, 0.5f);
+    const float2 a = __ldg(S.uvs + g.i1), b = __ldg(S.uvs + g.i2), c = __ldg(S.uvs + g.i3);
+    return make_float2(a.x * b0 + b.x * b1 + c.x * b2, a.y * b0 + b.y * b1 + c.y * b2);
+}
+
+YG_DEV float2 scaleUV(float2 uv, float sx, float sy) { return make_float2(uv.x * sx, uv.y * sy); }
+
+// getSkyBoxColor (materialsCommonResources.hlsl:181-224): a longitude-latitude texture
+// (cartesianToSpherical, commonMath.hlsl:144-151) or, without one, |dir|; times the scale
+YG_DEV float3 skyColor(const SceneView& S, float3 dir, float scale)
+{
+    if (S.envTexture < 0) return mk3(fabsf(dir.x) * scale, fabsf(dir.y) * scale, fabsf(dir.z) * scale);
+    float3 v = normalize(dir);
+    float theta = atan2f(v.z, v.x), phi = acosf(clampf(v.y, -1.0f, 1.0f));
+    float4 c = sampleTexture(S, S.envTexture, make_float2(theta * kINVPI * 0.5f + 0.5f, phi * kINVPI));
+    return mk3(c.x * scale, c.y * scale, c.z * scale);
 }
 
 // Scalar material parameters before the spectral conversion (SurfaceDefinitionRGB)
@@ -224,6 +268,42 @@ YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectr
         float3 t = s.tangent;
         s.tangent = mk3(ca * t.x + 0.0f * t.y + sa * t.z, 0.0f * t.x + 1.0f * t.y + 0.0f * t.z, -sa * t.x + 0.0f * t.y + ca * t.z);
     }
+    // modifySurfaceMaterialParametersWithTextures (materialsCommon.hlsl:354-397)
+    s.diffOcclusion = 1.0f;
+    s.specOcclusion = 1.0f;
+    const int4 tex = M.textures;
+    if ((tex.x & tex.y & tex.z & tex.w) >= 0) // some index is not -1
+    {
+        const float2 uv = meshUV(S, I, g, b0, hit.b1, hit.b2);
+        const float4 sa = M.albedoNormalScale, so = M.ormEmissiveScale;
+        if (tex.x >= 0)
+        {
+            float4 a = sampleTexture(S, tex.x, scaleUV(uv, sa.x, sa.y));
+            rgb.albedo = mk3(rgb.albedo.x * a.x, rgb.albedo.y * a.y, rgb.albedo.z * a.z);
+            if (s.flags & 4u) s.transparency = 1.0f - a.w * (1.0f - s.transparency); // alpha blended
+        }
+        if (tex.y >= 0)
+        {
+            float4 t = sampleTexture(S, tex.y, scaleUV(uv, sa.z, sa.w));
+            float3 n = normalize(mk3(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f));
+            s.baseLayerNormal = fromLocal(constructBasis(s.baseLayerNormal, s.tangent), mk3(n.x, n.z, n.y));
+        }
+        if (tex.z >= 0)
+        {
+            float4 o = sampleTexture(S, tex.z, scaleUV(uv, so.x, so.y));
+            // packOcclusion / unpackOcclusion: the occlusion travels as a half
+            float occ = __half2float(__float2half_rn(o.x));
+            s.diffOcclusion = occ;
+            s.specOcclusion = occ;
+            s.roughness = s.roughness * o.y;
+            s.metalness = s.metalness * o.z;
+        }
+        if (tex.w >= 0)
+        {
+            float4 e = sampleTexture(S, tex.w, scaleUV(uv, so.z, so.w));
+            rgb.emissive = mk3(rgb.emissive.x * e.x, rgb.emissive.y * e.y, rgb.emissive.z * e.z);
+        }
+    }
     // regularisation (rayHitDefault.hlsl:494-502)
     if (P.regularizeEnable)
     {
@@ -276,7 +356,15 @@ YG_DEV void sampleMeshLight(const SceneView& S, const Spectral& sp, uint32_t li,
     out.n = gn;
     const GpuMaterial& M = S.materials[I.material];
     float4 e = M.emissive_roughness;
-    out.radiance = emissionSpectrum(S, sp, mk3(e.x, e.y, e.z), M.emissionSpectrum);
+    float3 erg = mk3(e.x, e.y, e.z);
+    if (M.textures.w >= 0)
+    {
+        // modifySurfaceEmissionWithTexture (materialsCommon.hlsl:420-428) at the sampled point
+        const float2 uv = meshUV(S, I, g, b0, bx, by);
+        float4 t = sampleTexture(S, M.textures.w, scaleUV(uv, M.ormEmissiveScale.z, M.ormEmissiveScale.w));
+        erg = mk3(erg.x * t.x, erg.y * t.y, erg.z * t.z);
+    }
+    out.radiance = emissionSpectrum(S, sp, erg, M.emissionSpectrum);
     out.pdfPos = 1.0f / ((float)primCount * area);
     out.focus = M.emissionFocus;
     out.instance = inst;
@@ -500,7 +588,7 @@ YG_DEV bool shadeSegment(const SceneView& S, const LaunchParams& P, const Luts& 
     if (!found)
     {
         // rayMissEnvironment: |dir| * Env.IntensityScale, as an unbounded RGB emitter
-        float3 col = mk3(fabsf(ps.dir.x) * P.envScale, fabsf(ps.dir.y) * P.envScale, fabsf(ps.dir.z) * P.envScale);
+        float3 col = skyColor(S, ps.dir, P.envScale);
         float4 Le = isZero3(col) ? splat4(0.0f) : fromRGBUnbounded(S, sp, col);
         ps.total = ps.total + ps.throughput * Le;
         alive = false;

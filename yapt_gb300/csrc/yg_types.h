@@ -41,6 +41,17 @@ struct alignas(16) GpuMaterial
     float4 sheenColor_roughness;
     float4 subsurfaceRadius_amount;
     int albedoSpectrum, specularSpectrum, emissionSpectrum, pad;
+    int4 textures;            // albedo, normal, ORM, emissive texture index (-1: none)
+    float4 albedoNormalScale; // uv scales of the albedo (xy) and normal (zw) textures
+    float4 ormEmissiveScale;  // uv scales of the ORM (xy) and emissive (zw) textures
+};
+
+// A 2D texture, decoded to linear float RGBA at upload, sampled bilinearly with wrapping
+// (the reference's LINEAR_REPEAT colour sampler at mip 0)
+struct alignas(16) GpuTexture
+{
+    const float4* texels; // row major, width x height
+    uint32_t width, height;
 };
 
 // Per (render object, submesh) instance: RenderObjectTransformDataGPU + MeshEntryGPU refs.
@@ -108,6 +119,8 @@ struct SceneView
     const float* rgbToSpd; // 64^3 x 3, may be null
     const uint32_t* sobol; // [spp_count][kSobolDims] points of this launch
     GpuCamera cam;
+    const GpuTexture* textures;
+    int envTexture;        // longitude-latitude environment texture, -1: the analytic sky
     uint32_t nLights;      // mesh and punctual
     uint32_t nPunctual;    // the last nPunctual entries of lights
     uint32_t nInstances;

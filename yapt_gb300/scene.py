@@ -27,6 +27,9 @@ MATERIAL_DEFAULTS = dict(
     clear_coat_roughness=0.1, subsurface_radius=(1.0, 0.2, 0.1), subsurface_amount=0.0,
     subsurface_radius_scale=1.0, alpha_cutoff=0.0, albedo_spectrum=-1, specular_spectrum=-1,
     emission_spectrum=-1,
+    # texture id + 1 (0: none) and uv scale per slot
+    albedo_texture=0, normal_texture=0, orm_texture=0, emissive_texture=0,
+    albedo_uv_scale=(1.0, 1.0), normal_uv_scale=(1.0, 1.0), orm_uv_scale=(1.0, 1.0), emissive_uv_scale=(1.0, 1.0),
 )
 
 # the spectral grid every tabulated curve is stored on (5 nm steps)
@@ -47,7 +50,7 @@ def material_struct(params):
                 arr[i] = float(x)
         elif k in ("material_mask",):
             setattr(m, k, int(v))
-        elif k.endswith("_spectrum"):
+        elif k.endswith("_spectrum") or k.endswith("_texture"):
             setattr(m, k, int(v))
         else:
             setattr(m, k, float(v))
@@ -139,16 +142,32 @@ class Scene:
         self.camera = None
         self.name = "scene"
         self.punctual_lights = []  # dict(type, position, direction, intensity, cos_inner, cos_outer)
+        self.textures = []         # (width, height, format, texel array)
+        self.env_texture = 0       # texture id + 1 of a longitude-latitude environment
 
     # -- building --------------------------------------------------------
-    def add_mesh(self, positions, normals, indices, submeshes=None, tangents=None):
+    def add_texture(self, texels, fmt=None):
+        """texels: (h, w, 4) uint8 (fmt RGBA8_UNORM or RGBA8_SRGB, default sRGB) or float32
+        (RGBA32_FLOAT). Returns the id + 1 that materials and env_texture refer to."""
+        a = np.ascontiguousarray(texels)
+        assert a.ndim == 3 and a.shape[2] == 4
+        if a.dtype == np.uint8:
+            fmt = N.YG_TEXTURE_RGBA8_SRGB if fmt is None else fmt
+        else:
+            a = np.ascontiguousarray(a, np.float32)
+            fmt = N.YG_TEXTURE_RGBA32_FLOAT
+        self.textures.append((a.shape[1], a.shape[0], fmt, a))
+        return len(self.textures)
+
+    def add_mesh(self, positions, normals, indices, submeshes=None, tangents=None, uvs=None):
         pos = _f32(positions).reshape(-1, 3)
         nrm = _f32(normals).reshape(-1, 3)
         idx = np.ascontiguousarray(np.asarray(indices, dtype=np.uint32).reshape(-1))
         if submeshes is None:
             submeshes = [(0, len(idx))]
         tan = None if tangents is None else _f32(tangents).reshape(-1, 4)
-        self.meshes.append(dict(positions=pos, normals=nrm, indices=idx, submeshes=list(submeshes), tangents=tan))
+        uv = None if uvs is None else _f32(uvs).reshape(-1, 2)
+        self.meshes.append(dict(positions=pos, normals=nrm, indices=idx, submeshes=list(submeshes), tangents=tan, uvs=uv))
         return len(self.meshes) - 1
 
     def add_material(self, **params):
@@ -221,7 +240,7 @@ class Scene:
             d.positions = m["positions"].ctypes.data_as(C.POINTER(C.c_float))
             d.normals = m["normals"].ctypes.data_as(C.POINTER(C.c_float))
             d.tangents = m["tangents"].ctypes.data_as(C.POINTER(C.c_float)) if m["tangents"] is not None else None
-            d.uvs = None
+            d.uvs = m["uvs"].ctypes.data_as(C.POINTER(C.c_float)) if m.get("uvs") is not None else None
             d.vertex_count = len(m["positions"])
             d.indices = m["indices"].ctypes.data_as(C.c_void_p)
             d.index_count = len(m["indices"])
@@ -243,11 +262,16 @@ class Scene:
             cam = self.camera.struct()
             N.check(lib.yg_set_camera(ctx, C.byref(cam)))
         N.check(lib.yg_set_punctual_lights(ctx, self.punctual_structs(), len(self.punctual_lights)))
+        N.check(lib.yg_clear_textures(ctx))
+        for (w, h, fmt, a) in self.textures:
+            tid = C.c_uint32()
+            N.check(lib.yg_upload_texture(ctx, w, h, fmt, a.ctypes.data_as(C.c_void_p), C.byref(tid)))
+        N.check(lib.yg_set_environment_texture(ctx, self.env_texture))
         N.check(lib.yg_build_scene(ctx))
 
     def pooled(self):
         """Vertex/index pools and per-instance records (first index, prim count, vertex base)."""
-        pos, nrm, tan, idx = [], [], [], []
+        pos, nrm, tan, idx, uvs = [], [], [], [], []
         vbase, ibase = [], []
         nv = ni = 0
         for m in self.meshes:
@@ -257,6 +281,7 @@ class Scene:
             nrm.append(m["normals"])
             t = m["tangents"] if m["tangents"] is not None else np.tile(np.float32([1, 0, 0, 1]), (len(m["positions"]), 1))
             tan.append(t)
+            uvs.append(m["uvs"] if m.get("uvs") is not None else np.full((len(m["positions"]), 2), 0.5, np.float32))
             idx.append(m["indices"])
             nv += len(m["positions"])
             ni += len(m["indices"])
@@ -264,6 +289,7 @@ class Scene:
         for (o2w, mesh, sub, mat) in self.instances:
             first, count = self.meshes[mesh]["submeshes"][sub]
             inst.append(dict(o2w=o2w, first_index=ibase[mesh] + first, prim_count=count // 3, vertex_base=vbase[mesh],
-                             material=mat, has_tangents=self.meshes[mesh]["tangents"] is not None))
+                             material=mat, has_tangents=self.meshes[mesh]["tangents"] is not None,
+                             has_uvs=self.meshes[mesh].get("uvs") is not None))
         return dict(positions=np.concatenate(pos), normals=np.concatenate(nrm), tangents=np.concatenate(tan),
-                    indices=np.concatenate(idx), instances=inst)
+                    uvs=np.concatenate(uvs), indices=np.concatenate(idx), instances=inst)
