@@ -170,6 +170,57 @@ def test_bdpt_pipeline_and_unsupported_features_raise(built, py_yapt):
     assert r.getRendererVariable("No.Such.Variable") is None
     assert "RenderPipeline" in r.getAllRendererVariableNames()
     with pytest.raises(Y.YaptError):
-        r.createTexture("t", Y.ResourceDimension.TEXTURE_2D, Y.ResourceFormat.RGBA8_UNORM, 0, 4, 4, 1, 1)
+        r.createTexture("t", Y.ResourceDimension.TEXTURE_3D, Y.ResourceFormat.RGBA8_UNORM, 0, 4, 4, 1, 1)
+    with pytest.raises(Y.YaptError):
+        r.createTexture("t", Y.ResourceDimension.TEXTURE_2D, Y.ResourceFormat.R32_SFLOAT, 0, 4, 4, 1, 1)
+    sc.shutdown()
+    r.shutdown()
+
+
+def test_textures_and_skybox(built, py_yapt):
+    """A white albedo texture leaves the film bit for bit unchanged (albedo x 1); a coloured one
+    and a skybox change it; every texture change restarts the accumulation."""
+    Y = py_yapt
+    r = setup_renderer(Y, 32, 24)
+    sc = Y.Scene()
+    sc.init(r)
+    meshes, mats, objs = U.build_scene(Y, r, sc, U.box(2))
+    # an RGB-albedo material on the walls (a texture modulates the RGB albedo; materials whose
+    # albedo is a tabulated curve ignore it)
+    wall = r.createMaterial("wall")
+    wall.setAlbedo(Y.vec3([0.7, 0.7, 0.7]))
+    wall.setMetalness(0.0)
+    wall.setRoughness(1.0)
+    objs[0].setMaterials([wall] * len(objs[0].getMaterials()))
+    mats = [wall]
+    sc.update(0.0, 2)
+    base = film_of(Y, r)
+    white = np.full((4, 4, 4), 255, np.uint8)
+    t = r.createTexture("white", Y.ResourceDimension.TEXTURE_2D, Y.ResourceFormat.RGBA8_UNORM, 0, 4, 4, 1, 1)
+    t.upload(0, 0, 1, 1, 16, white.ctypes.data, 0)
+    assert t.getName() == "white"
+    mats[0].setAlbedoTexture(t, Y.vec2([2.0, 2.0]))
+    sc.update(0.0, 2)
+    assert r.getAccumulatedFrames() == 2
+    same = film_of(Y, r)
+    assert np.array_equal(same, base)
+    red = np.zeros((4, 4, 4), np.uint8)
+    red[..., 0] = 255
+    red[..., 3] = 255
+    t.upload(0, 0, 1, 1, 16, red.ctypes.data, 0)  # new content: a new upload
+    sc.update(0.0, 2)
+    assert r.getAccumulatedFrames() == 2
+    assert not np.array_equal(film_of(Y, r), base)
+    sky = np.ones((8, 16, 4), np.float32)
+    k = r.createTexture("sky", Y.ResourceDimension.TEXTURE_2D, Y.ResourceFormat.RGBA32_SFLOAT, 0, 16, 8, 1, 1)
+    k.upload(0, 0, 1, 1, 16 * 16, sky.ctypes.data, 0)
+    var = r.getRendererVariable("World.Skycube")
+    assert var.getTexture() is None
+    var.setTexture(k)
+    assert var.getTexture().getName() == "sky"
+    r.getRendererVariable("World.EnvIntensityScale").setFromFloatArray([1.0])
+    sc.update(0.0, 2)
+    img = film_of(Y, r)
+    assert np.all(np.isfinite(img)) and float(img[..., 1].mean()) > 0.0
     sc.shutdown()
     r.shutdown()

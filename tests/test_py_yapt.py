@@ -245,7 +245,7 @@ def test_material_presets_defaults_and_spectra(py_yapt):
     m.setEmissionBlackbody(3000.0)
     from yapt_gb300.configs import blackbody_spectrum
     np.testing.assert_allclose(m.getEmissionSpectrum(), blackbody_spectrum(3000.0), rtol=1e-6)
-    with pytest.raises(Y.YaptError):
+    with pytest.raises(TypeError):  # a Texture from Renderer.createTexture is required
         m.setAlbedoTexture(None, Y.vec2(1.0))
 
 

@@ -17,7 +17,11 @@
 // node's transform, intensity colour x max(0, intensity); lights with zero intensity are
 // left out.
 //
-// Not built (they raise): textures, debug render pipelines, orthographic cameras.
+// Textures: Renderer.createTexture (2D; RGBA8_UNORM, RGBA8_SRGB or RGBA32_SFLOAT), Texture.upload of
+// mip 0, Material.set{Albedo,Normal,ORM,Emissive}Texture(texture, uv scale) and the
+// World.Skycube variable (a longitude-latitude map).
+//
+// Not built (they raise): other texture kinds, debug render pipelines, orthographic cameras.
 #include <pybind11/operators.h>
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
@@ -664,10 +668,22 @@ py::tuple calculateBounds(uintptr_t vertexData, uintptr_t indexData, size_t inde
 constexpr float kSpecLmin = 380.f, kSpecLmax = 780.f;
 constexpr int kSpecPoints = 81; // 5 nm grid
 
+// Texture (PyTexture.cpp): a 2D texture held on the host until a scene update uploads the
+// textures its materials and the skybox use (yg_upload_texture)
+struct TextureData
+{
+    std::string name;
+    uint32_t format = YG_TEXTURE_RGBA8_UNORM; // YG_TEXTURE_*
+    uint32_t width = 0, height = 0;
+    std::vector<uint8_t> texels; // mip 0, rows packed
+    uint64_t version = 0;
+};
+
 struct MaterialData
 {
     std::string name;
     yg_material m{};
+    std::shared_ptr<TextureData> tex[4]; // albedo, normal, ORM, emissive
     bool twoSided = false, dispersion = false, alphaBlend = false;
     std::vector<float> albedoSpec, specularSpec, emissionSpec; // empty: RGB
     uint64_t version = 0;
@@ -839,7 +855,15 @@ struct Material
         r.v = {d->m.cauchy[0], d->m.cauchy[1]};
         return r;
     }
-    [[noreturn]] void setTexture(py::args) { throw YaptError("textures are not supported by the GB300 integrators"); }
+    // PyMaterial::set*Texture (PyMaterial.cpp:299-326): the texture and its uv scale
+    void setSlot(int k, const std::shared_ptr<TextureData>& t, const vec2& scale)
+    {
+        d->tex[k] = t;
+        float* s = k == 0 ? d->m.albedo_uv_scale : k == 1 ? d->m.normal_uv_scale : k == 2 ? d->m.orm_uv_scale : d->m.emissive_uv_scale;
+        s[0] = scale.v[0];
+        s[1] = scale.v[1];
+        touch();
+    }
 
     // spectral extension: tabulated curves instead of the RGB -> spectrum conversion
     void setAlbedoSpectrum(const std::vector<double>& lam, const std::vector<double>& val)
@@ -887,6 +911,27 @@ struct VarData
     std::array<double, 4> val{}, lo{}, hi{};
     std::vector<std::string> options;
     int selected = 0;
+    std::shared_ptr<TextureData> texture; // TEXTURE variables
+};
+
+struct Texture
+{
+    std::shared_ptr<TextureData> d;
+    // PyTexture::upload: mip 0 of one 2D texture; rows rowPitchInBytes apart in host memory at
+    // data + dataPtrOffset (a numpy array's ctypes.data, as the reference scripts pass it)
+    void upload(uint32_t mipOffset, uint32_t arrayOffset, uint32_t mipCount, uint32_t arrayCount, size_t rowPitch,
+                uintptr_t data, size_t offset)
+    {
+        if (mipOffset != 0 || arrayOffset != 0 || arrayCount > 1 || mipCount < 1)
+            throw YaptError("texture '" + d->name + "': only mip 0 of a 2D texture is used");
+        const size_t texel = d->format == YG_TEXTURE_RGBA32_FLOAT ? 16 : 4, row = texel * d->width;
+        if (rowPitch < row) throw YaptError("texture '" + d->name + "': row pitch smaller than a row");
+        const uint8_t* src = reinterpret_cast<const uint8_t*>(data) + offset;
+        d->texels.resize(row * d->height);
+        for (uint32_t y = 0; y < d->height; ++y) std::memcpy(d->texels.data() + y * row, src + y * rowPitch, row);
+        ++d->version;
+    }
+    std::string getName() const { return d->name; }
 };
 
 struct RendererVariable
@@ -907,6 +952,18 @@ struct RendererVariable
         if ((int)v.size() != d->comps) throw YaptError(d->name + ": expected " + std::to_string(d->comps) + " values");
         for (int i = 0; i < d->comps; ++i) d->val[i] = std::clamp((double)v[i], d->lo[i], d->hi[i]);
         ++*serial;
+    }
+    void setTexture(const Texture& t)
+    {
+        if (d->type != RendererVariableType::TEXTURE) throw YaptError(d->name + ": not a TEXTURE variable");
+        d->texture = t.d;
+        ++*serial;
+    }
+    py::object getTexture() const
+    {
+        if (d->type != RendererVariableType::TEXTURE) throw YaptError(d->name + ": not a TEXTURE variable");
+        if (!d->texture) return py::none();
+        return py::cast(Texture{d->texture});
     }
     std::vector<double> getAsFloatArray() const
     {
@@ -995,6 +1052,7 @@ struct RendererState
     std::vector<uint64_t> lastMeshes; // (mesh identity, content version) of the uploaded meshes
     std::vector<uint8_t> lastCamera;
     std::vector<uint8_t> lastLights;
+    std::vector<uint64_t> lastTextures; // (pointer, version) of the uploaded textures
     std::vector<uint8_t> lastParams;
     std::vector<yg_instance> instances; // the records of the last commit
     std::vector<yg_material> materials;
@@ -1028,6 +1086,13 @@ struct RendererState
         addFloat(n, def, lo, hi);
         vars.back()->type = RendererVariableType::INT;
     }
+    void addTexture(const std::string& n)
+    {
+        auto v = std::make_shared<VarData>();
+        v->name = n;
+        v->type = RendererVariableType::TEXTURE;
+        vars.push_back(v);
+    }
     void addOptions(const std::string& n, int sel, std::vector<std::string> opts)
     {
         auto v = std::make_shared<VarData>();
@@ -1046,6 +1111,7 @@ void registerVariables(RendererState& R)
 {
     R.addInt("Generic.RenderResolution", {1920, 1080}, 2, 99999999);
     R.addFloat("World.EnvIntensityScale", {1.0}, 0.0, 100000.0);
+    R.addTexture("World.Skycube"); // RVARNAME_SKYBOX: a longitude-latitude RGBA texture here
     R.addOptions("RenderPipeline", 1, {"BPT", "BPT_WITH_NEE", "BDPT", "DBG_Normals", "DBG_Tangents", "DBG_UV"});
     R.addFloat("Camera.ApertureRadius", {0.0}, 0.0, 1000.0);
     R.addFloat("Camera.FocusDistance", {10.0}, 0.001, 1000000.0);
@@ -1293,7 +1359,26 @@ struct Renderer
         throw YaptError("setRenderOutputToSurface: this renderer is headless; use readback()");
     }
     void resetRenderOutput() {}
-    [[noreturn]] void createTexture(py::args) { throw YaptError("textures are not supported by the GB300 integrators"); }
+    // PyRenderer::createTexture (PyRenderer.cpp:84-94): 2D, RGBA8 (UNORM / sRGB) or RGBA32 float
+    Texture createTexture(const std::string& name, ResourceDimension dim, ResourceFormat fmt, uint32_t usage, uint32_t width,
+                          uint32_t height, uint32_t mips, uint32_t depthOrSlices)
+    {
+        (void)usage;
+        (void)mips;
+        if (dim != ResourceDimension::TEXTURE_2D || depthOrSlices > 1)
+            throw YaptError("createTexture '" + name + "': only 2D textures are used by the GB300 integrators");
+        auto t = std::make_shared<TextureData>();
+        t->name = name;
+        if (fmt == ResourceFormat::RGBA8_UNORM) t->format = YG_TEXTURE_RGBA8_UNORM;
+        else if (fmt == ResourceFormat::RGBA8_SRGB) t->format = YG_TEXTURE_RGBA8_SRGB;
+        else if (fmt == ResourceFormat::RGBA32_SFLOAT) t->format = YG_TEXTURE_RGBA32_FLOAT;
+        else throw YaptError("createTexture '" + name + "': format must be RGBA8_UNORM, RGBA8_SRGB or RGBA32_SFLOAT");
+        if (width == 0 || height == 0) throw YaptError("createTexture '" + name + "': empty texture");
+        t->width = width;
+        t->height = height;
+        t->texels.assign((size_t)width * height * (t->format == YG_TEXTURE_RGBA32_FLOAT ? 16 : 4), 0);
+        return Texture{t};
+    }
     Buffer createBuffer(const std::string& name, uint32_t usage, size_t size)
     {
         auto b = std::make_shared<BufferData>();
@@ -1413,6 +1498,15 @@ bool Scene::sync()
         spectra.insert(spectra.end(), v.begin(), v.end());
         return (int)(spectra.size() / kSpecPoints) - 1;
     };
+    // textures in first-use order (materials, then the skybox); materials refer to id + 1
+    std::vector<std::shared_ptr<TextureData>> texs;
+    auto texId = [&](const std::shared_ptr<TextureData>& t) -> uint32_t {
+        if (!t) return 0;
+        for (size_t i = 0; i < texs.size(); ++i)
+            if (texs[i] == t) return (uint32_t)i + 1;
+        texs.push_back(t);
+        return (uint32_t)texs.size();
+    };
     for (auto& m : mats)
     {
         yg_material x = m->m;
@@ -1421,7 +1515,31 @@ bool Scene::sync()
         x.albedo_spectrum = addSpec(m->albedoSpec);
         x.specular_spectrum = addSpec(m->specularSpec);
         x.emission_spectrum = addSpec(m->emissionSpec);
+        x.albedo_texture = texId(m->tex[0]);
+        x.normal_texture = texId(m->tex[1]);
+        x.orm_texture = texId(m->tex[2]);
+        x.emissive_texture = texId(m->tex[3]);
         gm.push_back(x);
+    }
+    const uint32_t envTex = texId(S.var("World.Skycube")->texture);
+    bool texturesChanged = false;
+    std::vector<uint64_t> texSig{envTex};
+    for (auto& t : texs)
+    {
+        texSig.push_back(reinterpret_cast<uintptr_t>(t.get()));
+        texSig.push_back(t->version);
+    }
+    if (texSig != S.lastTextures)
+    {
+        check(yg_clear_textures(S.ctx), "scene update");
+        for (auto& t : texs)
+        {
+            uint32_t id = 0;
+            check(yg_upload_texture(S.ctx, t->width, t->height, t->format, t->texels.data(), &id), "scene update");
+        }
+        check(yg_set_environment_texture(S.ctx, envTex), "scene update");
+        S.lastTextures = texSig;
+        texturesChanged = true;
     }
     std::vector<uint64_t> meshSig;
     for (auto& m : meshes)
@@ -1433,7 +1551,7 @@ bool Scene::sync()
     for (auto& i : inst) appendBytes(sceneSig, i);
     for (auto& m : gm) appendBytes(sceneSig, m);
     for (float f : spectra) appendBytes(sceneSig, f);
-    bool changed = false;
+    bool changed = texturesChanged;
     if (meshSig != S.lastMeshes)
     {
         check(yg_clear_meshes(S.ctx), "scene update");
@@ -1745,10 +1863,14 @@ PYBIND11_MODULE(py_yapt, m)
         YG_PROP(CauchysCoefficients) YG_PROP(EnableDispersion) YG_PROP(SubsurfaceAmount) YG_PROP(SubsurfaceRadius)
         YG_PROP(SubsurfaceRadiusScale)
 #undef YG_PROP
-        .def("setAlbedoTexture", &Material::setTexture)
-        .def("setNormalTexture", &Material::setTexture)
-        .def("setORMTexture", &Material::setTexture)
-        .def("setEmissiveTexture", &Material::setTexture)
+        .def("setAlbedoTexture", [](Material& m, const Texture& t, const vec2& s) { m.setSlot(0, t.d, s); }, py::arg("texture"),
+             py::arg("scale") = vec2{{1.f, 1.f}})
+        .def("setNormalTexture", [](Material& m, const Texture& t, const vec2& s) { m.setSlot(1, t.d, s); }, py::arg("texture"),
+             py::arg("scale") = vec2{{1.f, 1.f}})
+        .def("setORMTexture", [](Material& m, const Texture& t, const vec2& s) { m.setSlot(2, t.d, s); }, py::arg("texture"),
+             py::arg("scale") = vec2{{1.f, 1.f}})
+        .def("setEmissiveTexture", [](Material& m, const Texture& t, const vec2& s) { m.setSlot(3, t.d, s); },
+             py::arg("texture"), py::arg("scale") = vec2{{1.f, 1.f}})
         .def("setAlbedoSpectrum", &Material::setAlbedoSpectrum)
         .def("setSpecularSpectrum", &Material::setSpecularSpectrum)
         .def("setEmissionSpectrum", &Material::setEmissionSpectrum)
@@ -1840,7 +1962,10 @@ PYBIND11_MODULE(py_yapt, m)
         .def("getOptions", &RendererVariable::getOptions)
         .def("getSelectedOption", &RendererVariable::getSelectedOption)
         .def("setSelectedOption", &RendererVariable::setSelectedOption)
-        .def("getType", &RendererVariable::getType);
+        .def("getType", &RendererVariable::getType)
+        .def("setTexture", &RendererVariable::setTexture)
+        .def("getTexture", &RendererVariable::getTexture);
+    py::class_<Texture>(m, "Texture").def("upload", &Texture::upload).def("getName", &Texture::getName);
 
     py::enum_<ReadbackTarget>(m, "ReadbackTarget")
         .value("FinalColor", ReadbackTarget::FinalColor)

@@ -53,6 +53,7 @@ yg::GpuMaterial packMaterial(const yg_material& m)
     g.emissionSpectrum = m.emission_spectrum;
     g.textures = make_int4((int)m.albedo_texture - 1, (int)m.normal_texture - 1, (int)m.orm_texture - 1,
                            (int)m.emissive_texture - 1);
+    if (m.albedo_texture || m.normal_texture || m.orm_texture || m.emissive_texture) g.mask |= yg::kMaterialTextured;
     g.albedoNormalScale = make_float4(m.albedo_uv_scale[0], m.albedo_uv_scale[1], m.normal_uv_scale[0], m.normal_uv_scale[1]);
     g.ormEmissiveScale = make_float4(m.orm_uv_scale[0], m.orm_uv_scale[1], m.emissive_uv_scale[0], m.emissive_uv_scale[1]);
     return g;

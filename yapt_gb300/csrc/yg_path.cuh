@@ -150,13 +150,17 @@ YG_DEV float2 scaleUV(float2 uv, float sx, float sy) { return make_float2(uv.x *
 
 // getSkyBoxColor (materialsCommonResources.hlsl:181-224): a longitude-latitude texture
 // (cartesianToSpherical, commonMath.hlsl:144-151) or, without one, |dir|; times the scale
-YG_DEV float3 skyColor(const SceneView& S, float3 dir, float scale)
+YG_DEV __noinline__ float3 skyTexture(const SceneView& S, float3 dir, float scale)
 {
-    if (S.envTexture < 0) return mk3(fabsf(dir.x) * scale, fabsf(dir.y) * scale, fabsf(dir.z) * scale);
     float3 v = normalize(dir);
     float theta = atan2f(v.z, v.x), phi = acosf(clampf(v.y, -1.0f, 1.0f));
     float4 c = sampleTexture(S, S.envTexture, make_float2(theta * kINVPI * 0.5f + 0.5f, phi * kINVPI));
     return mk3(c.x * scale, c.y * scale, c.z * scale);
+}
+YG_DEV float3 skyColor(const SceneView& S, float3 dir, float scale)
+{
+    if (S.envTexture < 0) return mk3(fabsf(dir.x) * scale, fabsf(dir.y) * scale, fabsf(dir.z) * scale);
+    return skyTexture(S, dir, scale);
 }
 
 // Scalar material parameters before the spectral conversion (SurfaceDefinitionRGB)
@@ -196,6 +200,51 @@ struct HitSurface
     uint32_t material;
     float3 albedoRGB; // first-hit features
 };
+
+// modifySurfaceMaterialParametersWithTextures (materialsCommon.hlsl:354-397), out of line so
+// that untextured shading keeps its instruction footprint
+YG_DEV __noinline__ void applyTextures(const SceneView& S, const GpuMaterial& M, const GpuInstance& I, const TriGeom& g,
+                                       float b0, float b1, float b2, SurfaceRGB& rgb, Surface& s)
+{
+    const int4 tex = M.textures;
+    const float2 uv = meshUV(S, I, g, b0, b1, b2);
+    const float4 sa = M.albedoNormalScale, so = M.ormEmissiveScale;
+    if (tex.x >= 0)
+    {
+        float4 a = sampleTexture(S, tex.x, scaleUV(uv, sa.x, sa.y));
+        rgb.albedo = mk3(rgb.albedo.x * a.x, rgb.albedo.y * a.y, rgb.albedo.z * a.z);
+        if (s.flags & 4u) s.transparency = 1.0f - a.w * (1.0f - s.transparency); // alpha blended
+    }
+    if (tex.y >= 0)
+    {
+        float4 t = sampleTexture(S, tex.y, scaleUV(uv, sa.z, sa.w));
+        float3 n = normalize(mk3(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f));
+        s.baseLayerNormal = fromLocal(constructBasis(s.baseLayerNormal, s.tangent), mk3(n.x, n.z, n.y));
+    }
+    if (tex.z >= 0)
+    {
+        float4 o = sampleTexture(S, tex.z, scaleUV(uv, so.x, so.y));
+        // packOcclusion / unpackOcclusion: the occlusion travels as a half
+        float occ = __half2float(__float2half_rn(o.x));
+        s.occlusion = occ;
+        s.roughness = s.roughness * o.y;
+        s.metalness = s.metalness * o.z;
+    }
+    if (tex.w >= 0)
+    {
+        float4 e = sampleTexture(S, tex.w, scaleUV(uv, so.z, so.w));
+        rgb.emissive = mk3(rgb.emissive.x * e.x, rgb.emissive.y * e.y, rgb.emissive.z * e.z);
+    }
+}
+
+// modifySurfaceEmissionWithTexture (materialsCommon.hlsl:420-428) at a sampled light point
+YG_DEV __noinline__ float3 emissionTextured(const SceneView& S, const GpuMaterial& M, const GpuInstance& I, const TriGeom& g,
+                                           float b0, float b1, float b2, float3 erg)
+{
+    const float2 uv = meshUV(S, I, g, b0, b1, b2);
+    float4 t = sampleTexture(S, M.textures.w, scaleUV(uv, M.ormEmissiveScale.z, M.ormEmissiveScale.w));
+    return mk3(erg.x * t.x, erg.y * t.y, erg.z * t.z);
+}
 
 // fetch + fetchSurfaceMaterialParameters + two-sided orientation + tangent rotation +
 // regularisation + RGB -> spectral conversion (rayHitDefault.hlsl:470-520)
@@ -269,41 +318,8 @@ YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectr
         s.tangent = mk3(ca * t.x + 0.0f * t.y + sa * t.z, 0.0f * t.x + 1.0f * t.y + 0.0f * t.z, -sa * t.x + 0.0f * t.y + ca * t.z);
     }
     // modifySurfaceMaterialParametersWithTextures (materialsCommon.hlsl:354-397)
-    s.diffOcclusion = 1.0f;
-    s.specOcclusion = 1.0f;
-    const int4 tex = M.textures;
-    if ((tex.x & tex.y & tex.z & tex.w) >= 0) // some index is not -1
-    {
-        const float2 uv = meshUV(S, I, g, b0, hit.b1, hit.b2);
-        const float4 sa = M.albedoNormalScale, so = M.ormEmissiveScale;
-        if (tex.x >= 0)
-        {
-            float4 a = sampleTexture(S, tex.x, scaleUV(uv, sa.x, sa.y));
-            rgb.albedo = mk3(rgb.albedo.x * a.x, rgb.albedo.y * a.y, rgb.albedo.z * a.z);
-            if (s.flags & 4u) s.transparency = 1.0f - a.w * (1.0f - s.transparency); // alpha blended
-        }
-        if (tex.y >= 0)
-        {
-            float4 t = sampleTexture(S, tex.y, scaleUV(uv, sa.z, sa.w));
-            float3 n = normalize(mk3(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f));
-            s.baseLayerNormal = fromLocal(constructBasis(s.baseLayerNormal, s.tangent), mk3(n.x, n.z, n.y));
-        }
-        if (tex.z >= 0)
-        {
-            float4 o = sampleTexture(S, tex.z, scaleUV(uv, so.x, so.y));
-            // packOcclusion / unpackOcclusion: the occlusion travels as a half
-            float occ = __half2float(__float2half_rn(o.x));
-            s.diffOcclusion = occ;
-            s.specOcclusion = occ;
-            s.roughness = s.roughness * o.y;
-            s.metalness = s.metalness * o.z;
-        }
-        if (tex.w >= 0)
-        {
-            float4 e = sampleTexture(S, tex.w, scaleUV(uv, so.z, so.w));
-            rgb.emissive = mk3(rgb.emissive.x * e.x, rgb.emissive.y * e.y, rgb.emissive.z * e.z);
-        }
-    }
+    s.occlusion = 1.0f;
+    if (M.mask & kMaterialTextured) applyTextures(S, M, I, g, b0, hit.b1, hit.b2, rgb, s);
     // regularisation (rayHitDefault.hlsl:494-502)
     if (P.regularizeEnable)
     {
@@ -357,13 +373,7 @@ YG_DEV void sampleMeshLight(const SceneView& S, const Spectral& sp, uint32_t li,
     const GpuMaterial& M = S.materials[I.material];
     float4 e = M.emissive_roughness;
     float3 erg = mk3(e.x, e.y, e.z);
-    if (M.textures.w >= 0)
-    {
-        // modifySurfaceEmissionWithTexture (materialsCommon.hlsl:420-428) at the sampled point
-        const float2 uv = meshUV(S, I, g, b0, bx, by);
-        float4 t = sampleTexture(S, M.textures.w, scaleUV(uv, M.ormEmissiveScale.z, M.ormEmissiveScale.w));
-        erg = mk3(erg.x * t.x, erg.y * t.y, erg.z * t.z);
-    }
+    if (M.textures.w >= 0) erg = emissionTextured(S, M, I, g, b0, bx, by, erg);
     out.radiance = emissionSpectrum(S, sp, erg, M.emissionSpectrum);
     out.pdfPos = 1.0f / ((float)primCount * area);
     out.focus = M.emissionFocus;

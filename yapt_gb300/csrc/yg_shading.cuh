@@ -826,7 +826,7 @@ struct Surface
     float clearCoatIOR, clearCoatRoughness, anisotropy, anisotropyRotation;
     float thinFilmNM, sheenRoughness, sheenAmount, emissionFocus;
     float subsurfaceAmount;
-    float diffOcclusion, specOcclusion; // unpackOcclusion of the ORM texture's occlusion (1 without one)
+    float occlusion; // unpackOcclusion of the ORM texture's occlusion, diffuse = specular (1 without one)
     uint32_t flags;
 };
 
@@ -1076,7 +1076,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
                         float fms = fmsDielectric<RECIP>(L, etaR, s.clearCoatRoughness, fabsf(dot(woC, wm)));
                         w += energyComp<RECIP>(L, fms, fabsf(woC.y), fabsf(wiC.y), s.clearCoatRoughness, w);
                     }
-                    float4 weight = splat4(w) * (s.clearCoatAmount * energyLeft) * compC * s.specOcclusion;
+                    float4 weight = splat4(w) * (s.clearCoatAmount * energyLeft) * compC * s.occlusion;
                     if (applyInference) coatAmp = weight;
                     else wsum = wsum + weight;
                 }
@@ -1095,7 +1095,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
                 if (!onlyPDF)
                 {
                     float4 w = onSameHemisphere(woB, wiB) ? evaluateSheen(s.sheenColor, s.sheenRoughness, woB, wiB) * fabsf(wiB.y) : splat4(0.0f);
-                    wsum = wsum + w * (s.sheenAmount * energyLeft) * compB * s.specOcclusion;
+                    wsum = wsum + w * (s.sheenAmount * energyLeft) * compB * s.occlusion;
                 }
                 pdfSum += c.probs[LAYER_SHEEN] * pdf;
             }
@@ -1143,7 +1143,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
                             setLane(w, i, (ss + ms) * fabsf(wiB.y));
                         }
                     }
-                    float4 weight = w * (s.metalness * energyLeft) * compB * s.specOcclusion;
+                    float4 weight = w * (s.metalness * energyLeft) * compB * s.occlusion;
                     if (applyInference)
                     {
                         float etaRC = s.clearCoatIOR / fromIOR;
@@ -1176,7 +1176,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
             {
                 if (!onlyPDF)
                 {
-                    float4 weight = splat4(specEvaluate<RECIP>(L, sl, woB, wiB)) * (specAmount * energyLeft) * compB * s.specOcclusion;
+                    float4 weight = splat4(specEvaluate<RECIP>(L, sl, woB, wiB)) * (specAmount * energyLeft) * compB * s.occlusion;
                     if (applyInference)
                     {
                         float etaRC = s.clearCoatIOR / fromIOR;
@@ -1203,7 +1203,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
             if (!onlyPDF)
             {
                 float4 w = onSameHemisphere(woB, wiB) ? (s.albedo / kPI) * fabsf(wiB.y) : splat4(0.0f);
-                wsum = wsum + w * (diffAmount * energyLeft) * compB * s.diffOcclusion;
+                wsum = wsum + w * (diffAmount * energyLeft) * compB * s.occlusion;
             }
             pdfSum += c.probs[LAYER_DIFF] * pdf;
         }
@@ -1238,7 +1238,7 @@ YG_DEV Eval evaluateSurface(const Luts& L, const Surface& s, const SurfaceCtx& c
             }
             if (!onlyPDF)
             {
-                wsum = wsum + splat4(specEvaluate<RECIP>(L, sl, woB, wiB)) * (transAmount * energyLeft) * compression * compB * s.specOcclusion;
+                wsum = wsum + splat4(specEvaluate<RECIP>(L, sl, woB, wiB)) * (transAmount * energyLeft) * compression * compB * s.occlusion;
             }
         }
     }

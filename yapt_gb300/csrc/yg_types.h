@@ -46,6 +46,8 @@ struct alignas(16) GpuMaterial
     float4 ormEmissiveScale;  // uv scales of the ORM (xy) and emissive (zw) textures
 };
 
+constexpr uint32_t kMaterialTextured = 1u << 8; // GpuMaterial::mask: some texture slot is bound
+
 // A 2D texture, decoded to linear float RGBA at upload, sampled bilinearly with wrapping
 // (the reference's LINEAR_REPEAT colour sampler at mip 0)
 struct alignas(16) GpuTexture
