@@ -266,6 +266,25 @@ YG_API int yg_clear_textures(yg_context* ctx);
 /* The environment (RVARNAME_SKYBOX with a longitude-latitude map): texture id + 1, or 0 for the
  * reference's analytic |dir| sky. Scaled by env_intensity_scale of each request. */
 YG_API int yg_set_environment_texture(yg_context* ctx, uint32_t texture);
+/* The tonemap stage (TonemapStage.cpp; knobs Tonemap.* of RendererVarsList.h:50-57): the film
+ * mean or the last a-trous output in linear sRGB, a 128-bucket EV histogram from EV -12, auto
+ * exposure (key 0.18 over the mean luminance, exposure compensation in EV, approached with
+ * 1 - exp(-dt * speed) each frame from the first frame's value) or a manual exposure, the ACES
+ * fitted operator when enabled, and the sRGB transfer function to RGBA8. rgba8: HOST buffer of
+ * W*H*4 bytes; exposure (may be NULL) receives the exposure used. Synchronous. */
+typedef struct yg_tonemap_params
+{
+    uint32_t enable;             /* Tonemap.Enable: the ACES fitted operator */
+    uint32_t auto_exposure;      /* Tonemap.UseAutoExposure */
+    float manual_exposure;       /* Tonemap.ManualExposure */
+    float exposure_compensation; /* Tonemap.ExposureCompensation (EV) */
+    float eye_adaptation_speed;  /* Tonemap.EyeAdaptationSpeed */
+    float delta_time;            /* seconds since the previous frame */
+    uint32_t reset;              /* first frame: the exposure starts at its parameter value */
+    uint32_t source;             /* 0: the film mean, 1: the last yg_atrous_denoise output */
+} yg_tonemap_params;
+YG_API void yg_tonemap_default_params(yg_tonemap_params* params);
+YG_API int yg_tonemap(yg_context* ctx, const yg_tonemap_params* params, uint8_t* rgba8, float* exposure);
 /* Replaces the punctual lights (count 0 removes them). The light tables are rebuilt at once
  * when the scene is built, else by yg_build_scene. */
 YG_API int yg_set_punctual_lights(yg_context* ctx, const yg_punctual_light* lights, uint32_t count);

@@ -91,6 +91,14 @@ class PunctualLight(C.Structure):
     ]
 
 
+class TonemapParams(C.Structure):
+    _fields_ = [
+        ("enable", C.c_uint32), ("auto_exposure", C.c_uint32), ("manual_exposure", C.c_float),
+        ("exposure_compensation", C.c_float), ("eye_adaptation_speed", C.c_float), ("delta_time", C.c_float),
+        ("reset", C.c_uint32), ("source", C.c_uint32),
+    ]
+
+
 class AtrousParams(C.Structure):
     _fields_ = [
         ("depth_sigma_scale", C.c_float), ("normal_sigma", C.c_float), ("material_sigma", C.c_float),
@@ -187,6 +195,8 @@ SIGNATURES = [
     ("yg_clear_textures", C.c_int, [C.c_void_p]),
     ("yg_set_environment_texture", C.c_int, [C.c_void_p, C.c_uint32]),
     ("yg_atrous_default_params", None, [C.POINTER(AtrousParams)]),
+    ("yg_tonemap_default_params", None, [C.POINTER(TonemapParams)]),
+    ("yg_tonemap", C.c_int, [C.c_void_p, C.POINTER(TonemapParams), C.c_void_p, C.POINTER(C.c_float)]),
     ("yg_atrous_denoise", C.c_int, [C.c_void_p, C.POINTER(AtrousParams), C.c_void_p, C.c_void_p]),
     ("yg_atrous_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("yg_atrous_run", C.c_int, [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(Camera),

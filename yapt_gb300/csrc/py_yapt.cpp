@@ -1054,6 +1054,8 @@ struct RendererState
     std::vector<uint8_t> lastLights;
     std::vector<uint64_t> lastTextures; // (pointer, version) of the uploaded textures
     std::vector<uint8_t> lastParams;
+    float lastDeltaTime = 0.f;  // Scene.update's deltaTime, the tonemap's eye adaptation step
+    bool tonemapStarted = false;
     std::vector<yg_instance> instances; // the records of the last commit
     std::vector<yg_material> materials;
     std::vector<float> spectra;
@@ -1117,7 +1119,23 @@ void registerVariables(RendererState& R)
     R.addFloat("Camera.FocusDistance", {10.0}, 0.001, 1000000.0);
     R.addInt("Firefly.RegularizeAfterVertices", {8}, 0, 64);
     R.addOptions("Firefly.Regularize", 1, {"OFF", "ON"});
+    // tonemap stage (RendererVarsList.h:50-57) and the a-trous denoiser (RendererVarsList.h:25-32)
+    R.addOptions("Tonemap.Enable", 1, {"OFF", "ON"});
+    R.addFloat("Tonemap.Toe", {1.0}, 0.0, 100.0);
+    R.addFloat("Tonemap.Mid", {1.0}, 0.0, 100.0);
+    R.addFloat("Tonemap.Shoulder", {1.0}, 0.0, 100.0);
+    R.addOptions("Tonemap.UseAutoExposure", 1, {"OFF", "ON"});
+    R.addFloat("Tonemap.ExposureCompensation", {0.0}, -10000.0, 10000.0);
+    R.addFloat("Tonemap.EyeAdaptationSpeed", {1.0}, 0.0, 1000.0);
     R.addFloat("Tonemap.ManualExposure", {1.0}, 0.0, 1e16);
+    R.addOptions("Denoise.Mode", 0, {"OFF", "ON", "DEBUG_MAT_PARAMS", "DEBUG_VARIANCE", "DEBUG_SHOW_SAMPLE_SOURCES",
+                                     "DEBUG_FEATURE_VARIANCE"});
+    R.addFloat("Denoise.DepthSigmaScale", {0.02}, 0.00001, 10.0);
+    R.addFloat("Denoise.NormalSigma", {0.06}, 0.00001, 1000.0);
+    R.addFloat("Denoise.MaterialDifferenceSigma", {0.05}, 0.00001, 1000.0);
+    R.addFloat("Denoise.ColorDifferenceSigma", {3.0}, 0.00001, 1000.0);
+    R.addFloat("Denoise.FeatureVarianceScale", {1.0}, 0.0, 1000.0);
+    R.addOptions("Denoise.FeaturePrefilter", 1, {"OFF", "ON"});
     R.addInt("Generic.MaxDepth", {32}, 1, 64);
     R.addInt("Generic.Seed", {0}, 0, 4294967295.0);
     R.addFloat("Generic.SpectralRange", {380.0, 700.0}, 360.0, 830.0);
@@ -1635,7 +1653,10 @@ void Scene::update(float deltaTime, uint32_t samples)
     p.bdpt_light_vertices = (uint32_t)S.var("BDPT.LightVertices")->val[0];
     p.bdpt_light_paths = (uint32_t)S.var("BDPT.LightPaths")->val[0];
     bool feats = S.var("Generic.Features")->selected == 1;
-    p.flags = feats ? YG_FLAG_FEATURES : 0u;
+    const int denoise = S.var("Denoise.Mode")->selected;
+    if (denoise > 1) throw YaptError("Denoise.Mode: only OFF and ON are built (the debug views are not)");
+    p.flags = (feats ? YG_FLAG_FEATURES : 0u) | (denoise == 1 ? YG_FLAG_ATROUS_FEATURES : 0u);
+    S.lastDeltaTime = deltaTime;
     std::vector<uint8_t> sig;
     appendBytes(sig, p);
     if (changed || sig != S.lastParams || p.width != S.filmW || p.height != S.filmH)
@@ -1714,21 +1735,34 @@ std::shared_ptr<ReadbackObject> Renderer::readback(ReadbackTarget target)
     };
     if (target == ReadbackTarget::FinalColor)
     {
+        // the combine stage's a-trous denoiser when Denoise.Mode is ON, then the tonemap stage
         data->format = ResourceFormat::RGBA8_UNORM;
         data->bytes.resize(n * 4);
-        const float ex = (float)S.var("Tonemap.ManualExposure")->val[0];
-        for (size_t i = 0; i < n; ++i)
+        const bool denoise = S.var("Denoise.Mode")->selected == 1;
+        if (denoise)
         {
-            float c[3];
-            rgbOf(i, c);
-            for (int k = 0; k < 3; ++k)
-            {
-                float v = std::clamp(c[k] * ex, 0.f, 1.f);
-                float e = v <= 0.0031308f ? 12.92f * v : 1.055f * std::pow(v, 1.f / 2.4f) - 0.055f; // sRGB encoding
-                data->bytes[4 * i + k] = (uint8_t)std::lround(std::clamp(e, 0.f, 1.f) * 255.f);
-            }
-            data->bytes[4 * i + 3] = 255;
+            yg_atrous_params a;
+            yg_atrous_default_params(&a);
+            a.depth_sigma_scale = (float)S.var("Denoise.DepthSigmaScale")->val[0];
+            a.normal_sigma = (float)S.var("Denoise.NormalSigma")->val[0];
+            a.material_sigma = (float)S.var("Denoise.MaterialDifferenceSigma")->val[0];
+            a.color_sigma = (float)S.var("Denoise.ColorDifferenceSigma")->val[0];
+            a.feature_variance_scale = (float)S.var("Denoise.FeatureVarianceScale")->val[0];
+            a.prefilter = (uint32_t)S.var("Denoise.FeaturePrefilter")->selected;
+            check(yg_atrous_denoise(S.ctx, &a, nullptr, nullptr), "readback");
         }
+        yg_tonemap_params t;
+        yg_tonemap_default_params(&t);
+        t.enable = (uint32_t)S.var("Tonemap.Enable")->selected;
+        t.auto_exposure = (uint32_t)S.var("Tonemap.UseAutoExposure")->selected;
+        t.manual_exposure = (float)S.var("Tonemap.ManualExposure")->val[0];
+        t.exposure_compensation = (float)S.var("Tonemap.ExposureCompensation")->val[0];
+        t.eye_adaptation_speed = (float)S.var("Tonemap.EyeAdaptationSpeed")->val[0];
+        t.delta_time = S.lastDeltaTime;
+        t.reset = S.tonemapStarted ? 0u : 1u;
+        t.source = denoise ? 1u : 0u;
+        check(yg_tonemap(S.ctx, &t, data->bytes.data(), nullptr), "readback");
+        S.tonemapStarted = true;
     }
     else
     {

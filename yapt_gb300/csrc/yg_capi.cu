@@ -1343,6 +1343,57 @@ YG_API int yg_atrous_denoise(yg_context* ctx, const yg_atrous_params* params, fl
     return YG_OK;
 }
 
+YG_API void yg_tonemap_default_params(yg_tonemap_params* p)
+{
+    if (!p) return;
+    p->enable = 1;
+    p->auto_exposure = 1;
+    p->manual_exposure = 1.0f;
+    p->exposure_compensation = 0.0f;
+    p->eye_adaptation_speed = 1.0f;
+    p->delta_time = 0.0f;
+    p->reset = 0;
+    p->source = 0;
+}
+
+YG_API int yg_tonemap(yg_context* ctx, const yg_tonemap_params* p, uint8_t* rgba8, float* exposure)
+{
+    if (!ctx || !p || !rgba8) return fail(YG_ERR_INVALID_ARGUMENT, "tonemap: null argument");
+    if (!std::isfinite(p->manual_exposure) || !std::isfinite(p->exposure_compensation) || !std::isfinite(p->delta_time) ||
+        !std::isfinite(p->eye_adaptation_speed) || p->delta_time < 0.0f || p->eye_adaptation_speed < 0.0f)
+        return fail(YG_ERR_INVALID_ARGUMENT, "tonemap: non-finite or negative parameter");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    const size_t n = (size_t)ctx->filmW * ctx->filmH;
+    if (n == 0) return fail(YG_ERR_NOT_READY, "tonemap: film not allocated");
+    if (p->source == 1 && ctx->dAtrousCol.bytes < 3 * n * sizeof(float4))
+        return fail(YG_ERR_NOT_READY, "tonemap: no a-trous output (call yg_atrous_denoise first)");
+    cudaSetDevice(ctx->device);
+    const bool fresh = ctx->dDisplay.p == nullptr;
+    YG_CUDA(ctx->dDisplay.ensure(128 * sizeof(uint32_t) + 4 * sizeof(float)));
+    YG_CUDA(ctx->dDisplayOut.ensure(n * sizeof(uint32_t)));
+    yg::DisplayArgs A{};
+    A.width = ctx->filmW;
+    A.height = ctx->filmH;
+    A.film = ctx->dFilmSum.as<float4>();
+    A.atrous = p->source == 1 ? ctx->dAtrousCol.as<float4>() + 2 * n : nullptr;
+    A.histogram = ctx->dDisplay.as<uint32_t>();
+    A.exposure = reinterpret_cast<float*>(A.histogram + 128);
+    A.stats = A.exposure + 1;
+    A.out = ctx->dDisplayOut.as<uint32_t>();
+    A.tonemap = p->enable ? 1u : 0u;
+    A.autoExposure = p->auto_exposure ? 1u : 0u;
+    A.init = (p->reset || fresh) ? 1u : 0u;
+    A.exposureParam = p->auto_exposure ? p->exposure_compensation : p->manual_exposure;
+    A.deltaTime = p->delta_time;
+    A.adaptSpeed = p->eye_adaptation_speed;
+    yg::launchDisplay(A, ctx->smCount, ctx->stream);
+    YG_CUDA(cudaGetLastError());
+    YG_CUDA(cudaMemcpyAsync(rgba8, A.out, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (exposure) YG_CUDA(cudaMemcpyAsync(exposure, A.exposure, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return YG_OK;
+}
+
 YG_API int yg_atrous_read(yg_context* ctx, float* xyzw, float* variance, float* film_sum, float* odd_sum, float* moments,
                           uint32_t* features)
 {

@@ -110,6 +110,7 @@ struct yg_context
     std::vector<DevBuf> texBufs;          // decoded texels of each texture
     std::vector<yg::GpuTexture> texTable; // device pointers and sizes, mirrored in dTexTable
     DevBuf dTexTable;
+    DevBuf dDisplay, dDisplayOut; // tonemap histogram, exposure state, RGBA8 image
     int envTexture = -1;
     uint32_t nLights = 0;   // mesh and punctual
     uint32_t nPunctual = 0;
@@ -143,6 +144,8 @@ struct yg_context
         for (DevBuf* b : all) b->release();
         for (DevBuf& b : texBufs) b.release();
         dTexTable.release();
+        dDisplay.release();
+        dDisplayOut.release();
         for (auto& b : dLut) b.release();
         for (cudaEvent_t e : kernelEvents) cudaEventDestroy(e);
         if (evStart) cudaEventDestroy(evStart);

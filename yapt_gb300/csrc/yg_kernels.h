@@ -97,6 +97,21 @@ struct AtrousBuffers
 int launchAtrousGather(const SceneView& S, const LaunchParams& P, float4* moments, float4* odd, const float4* samples,
                        uint32_t nspp, int smCount, cudaStream_t stream);
 int launchAtrous(const AtrousBuffers& B, const AtrousSettings& A, float4* outColour, float* outVar, cudaStream_t stream);
+// The tonemap stage's display path: histogram auto-exposure and the ACES fitted curve to RGBA8.
+struct DisplayArgs
+{
+    uint32_t width, height;
+    const float4* film;   // film sums and counts (used when atrous is null)
+    const float4* atrous; // the a-trous filter's XYZ output, or null
+    uint32_t* histogram;  // 128 buckets
+    float* exposure;      // persistent device state
+    float* stats;         // [0] mean luminance of the frame
+    uint32_t* out;        // RGBA8, one word a pixel
+    uint32_t tonemap, autoExposure, init;
+    float exposureParam;  // the manual exposure, or the compensation (EV) with auto exposure
+    float deltaTime, adaptSpeed;
+};
+int launchDisplay(const DisplayArgs& A, int smCount, cudaStream_t stream);
 // Merged wavefront of several requests (serving). All tables live in device memory and are
 // read by the kernels, so a captured launch sequence can be replayed round after round.
 struct MultiTables

@@ -112,6 +112,21 @@ class Context:
                                         None, None, None, None))
         return out, var
 
+    def tonemap(self, params=None, **kw):
+        """The tonemap stage on the film (source 0) or the last a-trous output (source 1):
+        returns (RGBA8 (H, W, 4) uint8, the exposure used)."""
+        p = params or N.TonemapParams()
+        if params is None:
+            N.load().yg_tonemap_default_params(C.byref(p))
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise ValueError("unknown tonemap parameter %r" % k)
+            setattr(p, k, v)
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        e = C.c_float()
+        N.check(self.lib.yg_tonemap(self.h, C.byref(p), out.ctypes.data_as(C.c_void_p), C.byref(e)))
+        return out, e.value
+
     def atrous_state(self, features=False):
         """The filter's inputs gathered on the device: film sums, odd-sample sums (H, W, 4),
         moment sums (4, H, W, 4) and, after atrous_denoise, the packed features (2, H, W, 4)."""
