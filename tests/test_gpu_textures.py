@@ -87,3 +87,22 @@ def test_texture_validation(built):
         c.upload_scene(sc)
         with pytest.raises(N.YaptError):
             c.render(c.params("nee", 8, 8, spp=1, flags=256))
+
+
+@pytest.mark.parametrize("integrator", ["nee", "bdpt"])
+def test_gltf_scene_renders_with_parity(built, host_luts, tmp_path, integrator):
+    """A scene loaded from glTF (textured cube, emissive lamp, spot light) through the C ABI."""
+    import pyoracle
+    import gltf_util as G
+    from yapt_gb300 import gltf
+    path = str(tmp_path / "s.glb")
+    G.write_scene(path, binary=True)
+    sc = gltf.load(path)
+    p = Context.params(integrator, 40, 32, spp=4, max_depth=8, lambda_range=(380, 780), flags=256,
+                       light_vertices=8 if integrator == "bdpt" else 0)
+    with Context(0) as c:
+        c.upload_scene(sc)
+        gpu = c.render(p, dump=True)
+    rgb = N.host_table("rgb_to_spd", (380, 780))
+    orc = pyoracle.OracleSceneHandle(sc, host_luts, rgb).render(p, precision=32)["records"]
+    T.compare(gpu, orc, min_within=0.999)
