@@ -1417,9 +1417,54 @@ template <typename T> void buildBvh(Ctx<T>& c)
     }
 }
 
-// Moller-Trumbore in the same operation order as the device kernel
+// Texture2D.SampleLevel(LINEAR_REPEAT, uv, 0) restated: bilinear between the four nearest
+// texel centres with wrapped coordinates, in the same arithmetic order as the device
+template <typename T> void bilinearTexels(const float* tx, int W, int H, T u0, T v0, T out[4])
+{
+    T u = u0 - std::floor(u0), v = v0 - std::floor(v0);
+    T x = u * T(W) - T(0.5f), y = v * T(H) - T(0.5f);
+    T fx = std::floor(x), fy = std::floor(y);
+    T ax = x - fx, ay = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    x0 = x0 < 0 ? x0 + W : (x0 >= W ? x0 - W : x0);
+    y0 = y0 < 0 ? y0 + H : (y0 >= H ? y0 - H : y0);
+    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    const float* c00 = &tx[4 * ((size_t)y0 * W + x0)];
+    const float* c10 = &tx[4 * ((size_t)y0 * W + x1)];
+    const float* c01 = &tx[4 * ((size_t)y1 * W + x0)];
+    const float* c11 = &tx[4 * ((size_t)y1 * W + x1)];
+    const T sx = T(1) - ax, sy = T(1) - ay;
+    for (int k = 0; k < 4; ++k)
+        out[k] = (T(c00[k]) * sx + T(c10[k]) * ax) * sy + (T(c01[k]) * sx + T(c11[k]) * ax) * ay;
+}
+
+// alphaTestPasses (hitShadersCommon.hlsl:162-183): a hit on an instance whose material has an
+// alpha cutoff above 0 and an albedo texture, on a mesh with texture coordinates, counts only
+// where the albedo alpha at its uv (times the albedo uv scale) reaches the cutoff. FP32 for
+// both oracle precisions, like the traversal itself.
+template <typename T> bool cutoutPasses(const Ctx<T>& c, uint32_t inst, uint32_t prim, float b1, float b2)
+{
+    const oracle_scene* sc = c.sc;
+    const oracle_instance& I = sc->instances[inst];
+    const yg_material& M = sc->materials[I.material];
+    if (!(M.alpha_cutoff > 0.0f) || !M.albedo_texture || !I.has_uvs || !sc->uvs) return true;
+    uint32_t id[3];
+    for (int k = 0; k < 3; ++k) id[k] = sc->indices[I.first_index + 3 * prim + k] + I.vertex_base;
+    const float* U = sc->uvs;
+    const float b0 = 1.0f - b1 - b2;
+    const float u = U[2 * id[0]] * b0 + U[2 * id[1]] * b1 + U[2 * id[2]] * b2;
+    const float v = U[2 * id[0] + 1] * b0 + U[2 * id[1] + 1] * b1 + U[2 * id[2] + 1] * b2;
+    const int t = (int)M.albedo_texture - 1;
+    float a[4];
+    bilinearTexels(c.tex[t].data(), (int)c.texW[t], (int)c.texH[t], u * M.albedo_uv_scale[0], v * M.albedo_uv_scale[1], a);
+    return a[3] >= M.alpha_cutoff;
+}
+
+// Moller-Trumbore in the same operation order as the device kernel; a candidate that would
+// become the closest hit must also pass the cutout test
+template <typename Cut>
 inline void triTest(const V3<float>& o, const V3<float>& d, float tminv, const V3<float>& v0, const V3<float>& e1,
-                    const V3<float>& e2, uint32_t inst, uint32_t prim, TriHit<float>& h)
+                    const V3<float>& e2, uint32_t inst, uint32_t prim, TriHit<float>& h, Cut&& cut)
 {
     V3<float> pvec = cross(d, e2);
     float det = dot(e1, pvec);
@@ -1435,6 +1480,7 @@ inline void triTest(const V3<float>& o, const V3<float>& d, float tminv, const V
     if (!(t > tminv)) return;
     if (t < h.t || (t == h.t && h.found && keyLess(inst, prim, h.inst, h.prim)))
     {
+        if (!cut(u, v)) return;
         h.t = t;
         h.b1 = u;
         h.b2 = v;
@@ -1477,7 +1523,8 @@ template <typename T> bool trace(const Ctx<T>& c, V3<T> oT, V3<T> dT, float tmin
             for (int i = nd.first; i < nd.first + nd.count; ++i)
             {
                 const auto& t = c.tris[c.triIdx[i]];
-                triTest(o, d, tminv, t.v0, t.e1, t.e2, t.inst, t.prim, h);
+                triTest(o, d, tminv, t.v0, t.e1, t.e2, t.inst, t.prim, h,
+                        [&](float b1, float b2) { return cutoutPasses(c, t.inst, t.prim, b1, b2); });
             }
         }
         else
@@ -1768,27 +1815,10 @@ template <typename T> T regularizeR(T lr, bool sq)
     return lr;
 }
 
-// Texture2D.SampleLevel(LINEAR_REPEAT, uv, 0) restated: bilinear between the four nearest
-// texel centres with wrapped coordinates, in the same arithmetic order as the device
+// a scene texture, sampled as bilinearTexels does
 template <typename T> void sampleTex(const Ctx<T>& c, int id, T u0, T v0, T out[4])
 {
-    const std::vector<float>& tx = c.tex[id];
-    const int W = (int)c.texW[id], H = (int)c.texH[id];
-    T u = u0 - std::floor(u0), v = v0 - std::floor(v0);
-    T x = u * T(W) - T(0.5f), y = v * T(H) - T(0.5f);
-    T fx = std::floor(x), fy = std::floor(y);
-    T ax = x - fx, ay = y - fy;
-    int x0 = (int)fx, y0 = (int)fy;
-    x0 = x0 < 0 ? x0 + W : (x0 >= W ? x0 - W : x0);
-    y0 = y0 < 0 ? y0 + H : (y0 >= H ? y0 - H : y0);
-    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
-    const float* c00 = &tx[4 * ((size_t)y0 * W + x0)];
-    const float* c10 = &tx[4 * ((size_t)y0 * W + x1)];
-    const float* c01 = &tx[4 * ((size_t)y1 * W + x0)];
-    const float* c11 = &tx[4 * ((size_t)y1 * W + x1)];
-    const T sx = T(1) - ax, sy = T(1) - ay;
-    for (int k = 0; k < 4; ++k)
-        out[k] = (T(c00[k]) * sx + T(c10[k]) * ax) * sy + (T(c01[k]) * sx + T(c11[k]) * ax) * ay;
+    bilinearTexels(c.tex[id].data(), (int)c.texW[id], (int)c.texH[id], u0, v0, out);
 }
 
 // fetchMeshUV or (0.5, 0.5) without texture coordinates

@@ -18,7 +18,8 @@ distributions of the benchmark definitions:
 import numpy as np
 
 from . import _native as N
-from .scene import (SPECTRUM_LMAX, SPECTRUM_LMIN, SPECTRUM_POINTS, CameraDesc, Scene, affine, rotation_y)
+from .scene import (SPECTRUM_LMAX, SPECTRUM_LMIN, SPECTRUM_POINTS, CameraDesc, Scene, affine, rotation_x,
+                    rotation_y)
 
 GRID = np.linspace(SPECTRUM_LMIN, SPECTRUM_LMAX, SPECTRUM_POINTS)
 
@@ -237,6 +238,40 @@ def textured_box_scene(seed=0, aspect=1.0):
     m[2].update(metalness=1.0, specular=(0.9, 0.85, 0.8), specular_amount=1.0, roughness=0.6, normal_texture=t_normal,
                 orm_texture=t_orm)
     m[7].update(emissive_texture=t_glow)
+    return sc
+
+
+def cutout_box_scene(seed=0, cutoff=0.5, aspect=1.0):
+    """``box_scene`` with two alpha-tested panels (the reference's alpha cutoff, applied in the
+    any-hit stage by alphaTestPasses, hitShadersCommon.hlsl:162-183): a two-sided vertical
+    screen with round holes between the camera and the blocks, and a grate of slots just
+    under the ceiling light, so that camera, bounce and shadow rays all pass through
+    cutouts. Their albedo texture's alpha is 0 in the holes and 1 elsewhere, with a soft
+    edge; the panels are the last two instances, material ids 8 and 9."""
+    sc = box_scene(seed, aspect=aspect)
+    sc.name = "cutout_box(seed=%d, cutoff=%g)" % (seed, cutoff)
+    uv = np.float32([[0, 0], [1, 0], [1, 1], [0, 1]])
+    y, x = (np.mgrid[0:64, 0:64] + 0.5) / 64.0
+    r = np.hypot(x - 0.5, y - 0.5)
+    holes = np.clip((r - 0.3) / 0.06, 0.0, 1.0)
+    screen = np.stack([0.2 + 0.6 * x, 0.5 + 0.0 * x, 0.8 - 0.5 * y, holes], -1)
+    slots = np.clip(np.abs(x - 0.5) * 8.0 - 1.0, 0.0, 1.0)
+    grate = np.stack([0.6 + 0.0 * x, 0.6 + 0.0 * x, 0.6 + 0.0 * x, slots], -1)
+    t_screen = sc.add_texture(np.round(screen * 255).astype(np.uint8), N.YG_TEXTURE_RGBA8_UNORM)
+    t_grate = sc.add_texture(np.round(grate * 255).astype(np.uint8), N.YG_TEXTURE_RGBA8_UNORM)
+    qp, qn, qi = quad(0.7, 0.6)
+    screen_mesh = sc.add_mesh(qp, qn, qi, tangents=flat_tangents(qn), uvs=uv)
+    m_screen = sc.add_material(albedo=(0.8, 0.8, 0.8), metalness=0.0, transparency=0.0, specular_amount=0.0,
+                               roughness=1.0, albedo_texture=t_screen, albedo_uv_scale=(3.0, 2.0), alpha_cutoff=cutoff,
+                               material_mask=N.YG_MATERIAL_TWO_SIDED)
+    # the xz quad turned to face +z, at z = 0.85
+    sc.add_instance(screen_mesh, m_screen, affine(translation=(0.5, 0.45, 0.85), rotation=rotation_x(-np.pi / 2)))
+    qp, qn, qi = quad(0.4, 0.4)
+    grate_mesh = sc.add_mesh(qp, qn, qi, tangents=flat_tangents(qn), uvs=uv)
+    m_grate = sc.add_material(albedo=(0.6, 0.6, 0.6), metalness=0.0, transparency=0.0, specular_amount=0.0,
+                              roughness=1.0, albedo_texture=t_grate, albedo_uv_scale=(2.0, 1.0), alpha_cutoff=cutoff,
+                              material_mask=N.YG_MATERIAL_TWO_SIDED)
+    sc.add_instance(grate_mesh, m_grate, affine(translation=(0.5, 0.93, 0.5)))
     return sc
 
 

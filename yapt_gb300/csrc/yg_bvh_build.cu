@@ -70,7 +70,8 @@ __device__ __forceinline__ float halfArea(float4 lo, float4 hi)
 __global__ void worldTriangles(const GpuInstance* __restrict__ inst, const uint32_t* __restrict__ instStart,
                                uint32_t nInst, const float* __restrict__ pos, const uint32_t* __restrict__ idx,
                                uint32_t nPrims, float4* __restrict__ tris, float4* __restrict__ lo,
-                               float4* __restrict__ hi, uint32_t* __restrict__ bounds)
+                               float4* __restrict__ hi, uint32_t* __restrict__ bounds, const float2* __restrict__ uvs,
+                               const GpuAlphaSource* __restrict__ alpha, float4* __restrict__ cutouts)
 {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     float blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -87,16 +88,32 @@ __global__ void worldTriangles(const GpuInstance* __restrict__ inst, const uint3
         const GpuInstance& I = inst[a];
         uint32_t p = g - instStart[a];
         float3 w[3];
+        uint32_t vi[3];
         for (int k = 0; k < 3; ++k)
         {
-            uint32_t vi = idx[I.firstIndex + 3 * p + k] + I.vertexBase;
-            w[k] = xformPoint(I.o2w, mk3(pos[3 * vi], pos[3 * vi + 1], pos[3 * vi + 2]));
+            vi[k] = idx[I.firstIndex + 3 * p + k] + I.vertexBase;
+            w[k] = xformPoint(I.o2w, mk3(pos[3 * vi[k]], pos[3 * vi[k] + 1], pos[3 * vi[k] + 2]));
+        }
+        // the cutout record of an alpha-tested triangle, behind the reordered triangles; the
+        // triangle refers to it by its float4 offset from the start of the triangle array
+        uint32_t cut = 0;
+        if (cutouts && I.alphaSource)
+        {
+            const GpuAlphaSource A = alpha[I.alphaSource - 1];
+            const float2 t0 = uvs[vi[0]], t1 = uvs[vi[1]], t2 = uvs[vi[2]];
+            const uint64_t tp = reinterpret_cast<uint64_t>(A.texels);
+            float4* r = cutouts + 3 * (size_t)g;
+            r[0] = make_float4(t0.x, t0.y, t1.x, t1.y);
+            r[1] = make_float4(t2.x, t2.y, A.su, A.sv);
+            r[2] = make_float4(__uint_as_float((uint32_t)tp), __uint_as_float((uint32_t)(tp >> 32)), __uint_as_float(A.size),
+                               A.cutoff);
+            cut = 3 * nPrims + 3 * g;
         }
         float3 e1 = mk3(w[1].x - w[0].x, w[1].y - w[0].y, w[1].z - w[0].z);
         float3 e2 = mk3(w[2].x - w[0].x, w[2].y - w[0].y, w[2].z - w[0].z);
         tris[3 * (size_t)g] = make_float4(w[0].x, w[0].y, w[0].z, __uint_as_float(a));
         tris[3 * (size_t)g + 1] = make_float4(e1.x, e1.y, e1.z, __uint_as_float(p));
-        tris[3 * (size_t)g + 2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+        tris[3 * (size_t)g + 2] = make_float4(e2.x, e2.y, e2.z, __uint_as_float(cut));
         for (int k = 0; k < 3; ++k)
         {
             const float c[3] = {w[k].x, w[k].y, w[k].z};
@@ -711,9 +728,16 @@ int buildWideBvh(const WideBvhInput& in, WideBvhOutput& out, cudaStream_t s, std
     for (int k = 0; k < 12; ++k) init[k] = k % 6 < 3 ? 0xffffffffu : 0u;
     cudaMemcpyAsync(bounds, init, sizeof(init), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(instStart, in.instPrimStart.data(), in.instPrimStart.size() * 4, cudaMemcpyHostToDevice, s);
+    // the output triangles, with room for one cutout record per triangle when some instance
+    // is alpha-tested (record offsets are 32-bit)
+    const bool cutouts = in.alpha != nullptr && N > 0;
+    if (cutouts && 6ull * N > 0xffffffffull) return err = "bvh: too many triangles for cutout records", -1;
+    float4* trisOut = pool.get<float4>(3 * (size_t)std::max<uint32_t>(N, 1) * (cutouts ? 2 : 1), ce);
+    if (!cuda("bvh: allocation")) return -1;
     if (N)
         worldTriangles<<<blocksFor(N, 256), 256, 0, s>>>(in.instances, instStart, in.nInstances, in.positions, in.indices, N,
-                                                         trisIn, plo, phi, bounds);
+                                                         trisIn, plo, phi, bounds, in.uvs, in.alpha,
+                                                         cutouts ? trisOut + 3 * (size_t)N : nullptr);
     uint32_t hb[12];
     cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
     if (!cuda("bvh: triangles")) return -1;
@@ -732,8 +756,7 @@ int buildWideBvh(const WideBvhInput& in, WideBvhOutput& out, cudaStream_t s, std
     // the wide tree: at most one wide node per primitive, plus the root
     const size_t maxWide = (size_t)N + 1;
     float4* wide = pool.get<float4>(5 * maxWide, ce);
-    float4* trisOut = pool.get<float4>(3 * (size_t)std::max<uint32_t>(N, 1), ce);
-    if (!cuda("bvh: allocation")) return -1;
+
     if (N == 0)
     {
         // an empty root: no slot is ever hit

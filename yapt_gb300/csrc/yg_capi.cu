@@ -589,6 +589,8 @@ YG_API int yg_clear_textures(yg_context* ctx)
     cudaSetDevice(ctx->device);
     YG_CUDA(cudaStreamSynchronize(ctx->stream));
     for (DevBuf& b : ctx->texBufs) b.release();
+    // the cutout records of a built scene refer to texture memory: the scene is built again
+    if (ctx->nAlphaInstances) ctx->sceneBuilt = false;
     ctx->texBufs.clear();
     ctx->texTable.clear();
     ctx->envTexture = -1;
@@ -814,6 +816,7 @@ YG_API int yg_build_scene(yg_context* ctx)
     std::vector<float> power;
     std::vector<uint32_t> lightInst;
     std::vector<uint32_t> primStart(nInst + 1, 0);
+    std::vector<yg::GpuAlphaSource> alphaSrc;
     for (size_t i = 0; i < nInst; ++i)
     {
         const yg_instance& I = ctx->instances[i];
@@ -834,6 +837,24 @@ YG_API int yg_build_scene(yg_context* ctx)
         G.lightPdf = 0.0f;
         G.hasTangents = m.tangents ? 1u : 0u;
         G.hasUVs = m.uvs ? 1u : 0u;
+        G.alphaSource = 0;
+        // alpha-tested: a cutoff above 0, an albedo texture and texture coordinates
+        // (alphaTestPasses, hitShadersCommon.hlsl:162-175); the texture must be uploaded first
+        const yg_material& AM = ctx->materials[I.material];
+        if (AM.alpha_cutoff > 0.0f && AM.albedo_texture && m.uvs)
+        {
+            if (AM.albedo_texture > ctx->texTable.size())
+                return fail(YG_ERR_INVALID_ARGUMENT, "an alpha-tested material's albedo texture is not uploaded");
+            const yg::GpuTexture& T = ctx->texTable[AM.albedo_texture - 1];
+            yg::GpuAlphaSource A{};
+            A.texels = T.texels;
+            A.size = T.width | T.height << 16;
+            A.cutoff = AM.alpha_cutoff;
+            A.su = AM.albedo_uv_scale[0];
+            A.sv = AM.albedo_uv_scale[1];
+            alphaSrc.push_back(A);
+            G.alphaSource = (uint32_t)alphaSrc.size();
+        }
         if ((uint64_t)primStart[i] + G.primCount > 0xffffffffull) return fail(YG_ERR_INVALID_ARGUMENT, "scene: too many triangles");
         primStart[i + 1] = primStart[i] + G.primCount;
         // mesh lights: emissive materials (LightManager.cpp:145), power estimate of
@@ -876,12 +897,21 @@ YG_API int yg_build_scene(yg_context* ctx)
         if ((r = upload(ctx, ctx->dSpec, z, 4))) return r;
     }
     // the acceleration structure, built on the device
+    DevBuf dAlpha;
+    if (!alphaSrc.empty() && (r = upload(ctx, dAlpha, alphaSrc.data(), alphaSrc.size()))) return r;
     yg::WideBvhInput bin{ctx->dInst.as<yg::GpuInstance>(), (uint32_t)nInst, primStart, ctx->dPos.as<float>(),
-                         ctx->dIdx.as<uint32_t>(), primStart[nInst]};
+                         ctx->dIdx.as<uint32_t>(), primStart[nInst], ctx->dUV.as<float2>(),
+                         alphaSrc.empty() ? nullptr : dAlpha.as<yg::GpuAlphaSource>()};
     yg::WideBvhOutput bout{};
     std::string berr;
-    if (yg::buildWideBvh(bin, bout, ctx->stream, berr) != 0) return fail(YG_ERR_CUDA, berr);
-    ctx->dTris.adopt(bout.tris, 3 * sizeof(float4) * std::max<uint32_t>(primStart[nInst], 1));
+    const int built = yg::buildWideBvh(bin, bout, ctx->stream, berr);
+    const cudaError_t synced = cudaStreamSynchronize(ctx->stream); // the build reads the cutout sources
+    dAlpha.release();
+    if (built != 0) return fail(YG_ERR_CUDA, berr);
+    YG_CUDA(synced);
+    ctx->dTris.adopt(bout.tris, 3 * sizeof(float4) * std::max<uint32_t>(primStart[nInst], 1) *
+                                    (alphaSrc.empty() || primStart[nInst] == 0 ? 1 : 2));
+    ctx->nAlphaInstances = (uint32_t)alphaSrc.size();
     ctx->dNodes.adopt(bout.nodes, 5 * sizeof(float4) * (size_t)bout.nNodes);
     ctx->nTris = primStart[nInst];
     ctx->nNodes = bout.nNodes;

@@ -99,6 +99,8 @@ struct yg_context
     yg::GpuCamera camera{};
     bool cameraSet = false;
     bool sceneBuilt = false;
+    uint32_t nAlphaInstances = 0; // alpha-tested instances of the built scene (their cutout
+                                  // records point into texture memory)
     uint64_t nTris = 0, nNodes = 0;
     uint32_t bvhDepth = 0;
     // device

@@ -26,6 +26,8 @@ struct WideBvhInput
     const float* positions;
     const uint32_t* indices;
     uint32_t nPrims;
+    const float2* uvs;              // texture coordinates of the vertices (alpha-tested meshes)
+    const GpuAlphaSource* alpha;    // indexed by GpuInstance::alphaSource - 1; null: no cutouts
 };
 struct WideBvhOutput
 {

@@ -116,26 +116,11 @@ YG_DEV float3 interp3(const float* A, const TriGeom& g, float b0, float b1, floa
     return a * b0 + b * b1 + c * b2;
 }
 
-// Texture2D.SampleLevel(LINEAR_REPEAT, uv, 0): bilinear between the four nearest texel
-// centres, coordinates wrapped. Done in FP32 arithmetic (not the texture unit's 8-bit
-// fraction) so that a CPU restatement computes the same value.
+// a scene texture, sampled as bilinearWrap does
 YG_DEV float4 sampleTexture(const SceneView& S, int id, float2 uv)
 {
     const GpuTexture T = S.textures[id];
-    const float w = (float)T.width, h = (float)T.height;
-    float u = uv.x - floorf(uv.x), v = uv.y - floorf(uv.y);
-    float x = u * w - 0.5f, y = v * h - 0.5f;
-    float fx = floorf(x), fy = floorf(y);
-    float tx = x - fx, ty = y - fy;
-    int x0 = (int)fx, y0 = (int)fy;
-    const int W = (int)T.width, H = (int)T.height;
-    x0 = x0 < 0 ? x0 + W : (x0 >= W ? x0 - W : x0);
-    y0 = y0 < 0 ? y0 + H : (y0 >= H ? y0 - H : y0);
-    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
-    const float4 c00 = __ldg(T.texels + (size_t)y0 * W + x0), c10 = __ldg(T.texels + (size_t)y0 * W + x1);
-    const float4 c01 = __ldg(T.texels + (size_t)y1 * W + x0), c11 = __ldg(T.texels + (size_t)y1 * W + x1);
-    const float sx = 1.0f - tx, sy = 1.0f - ty;
-    return (c00 * sx + c10 * tx) * sy + (c01 * sx + c11 * tx) * ty;
+    return bilinearWrap(T.texels, T.width, T.height, uv);
 }
 
 // fetchMeshUV, or (0.5, 0.5) for a mesh without texture coordinates (hitShadersCommon.hlsl:198)

@@ -11,7 +11,13 @@
 // rounds outward and pads one quantum). imask bit i: slot i is an inner node, stored at
 // child base + (inner slots below i). Otherwise meta[i] = count << 5 | offset: a leaf of
 // `count` triangles at triangle base + offset; meta[i] == 0: empty slot.
-// Triangles (48 B): (v0.xyz, instance) (e1.xyz, primitive) (e2.xyz, 0), world space.
+// Triangles (48 B): (v0.xyz, instance) (e1.xyz, primitive) (e2.xyz, cutout), world space.
+// cutout = 0 for an opaque triangle; otherwise the float4 offset from the triangle array's
+// start of the triangle's cutout record (three float4 behind all the triangles):
+//   (uv0, uv1) (uv2, albedo uv scale) (texels pointer lo, hi, width | height << 16, cutoff)
+// A candidate hit that would become the closest one is dropped when the albedo alpha at its
+// uv is below the cutoff (PROCEED_ALPHA_TESTED / rayAnyHitAlphaTest.hlsl), for closest-hit
+// and shadow rays alike, so the result does not depend on the order the tree is visited in.
 //
 // Traversal keeps one group of unvisited inner children (child base, inner mask, hit mask
 // in near-to-far key order) and a stack of such groups. Children sit in slots by octant, so
@@ -44,6 +50,41 @@ YG_HD bool keyLess(uint32_t ia, uint32_t pa, uint32_t ib, uint32_t pb)
     return ia < ib || (ia == ib && pa < pb);
 }
 
+// Texture2D.SampleLevel(LINEAR_REPEAT, uv, 0): bilinear between the four nearest texel
+// centres, coordinates wrapped. Done in FP32 arithmetic (not the texture unit's 8-bit
+// fraction) so that a CPU restatement computes the same value.
+__device__ __forceinline__ float4 bilinearWrap(const float4* __restrict__ texels, uint32_t width, uint32_t height, float2 uv)
+{
+    const float w = (float)width, h = (float)height;
+    float u = uv.x - floorf(uv.x), v = uv.y - floorf(uv.y);
+    float x = u * w - 0.5f, y = v * h - 0.5f;
+    float fx = floorf(x), fy = floorf(y);
+    float tx = x - fx, ty = y - fy;
+    int x0 = (int)fx, y0 = (int)fy;
+    const int W = (int)width, H = (int)height;
+    x0 = x0 < 0 ? x0 + W : (x0 >= W ? x0 - W : x0);
+    y0 = y0 < 0 ? y0 + H : (y0 >= H ? y0 - H : y0);
+    const int x1 = x0 + 1 == W ? 0 : x0 + 1, y1 = y0 + 1 == H ? 0 : y0 + 1;
+    const float4 c00 = __ldg(texels + (size_t)y0 * W + x0), c10 = __ldg(texels + (size_t)y0 * W + x1);
+    const float4 c01 = __ldg(texels + (size_t)y1 * W + x0), c11 = __ldg(texels + (size_t)y1 * W + x1);
+    const float sx = 1.0f - tx, sy = 1.0f - ty;
+    return (c00 * sx + c10 * tx) * sy + (c01 * sx + c11 * tx) * ty;
+}
+
+// alphaTestPasses (hitShadersCommon.hlsl:162-183) on a triangle's cutout record, at the
+// barycentrics (b1, b2) of a candidate hit. Out of line: only alpha-tested triangles pay.
+static __device__ __noinline__ bool cutoutPasses(const float4* __restrict__ r, float b1, float b2)
+{
+    const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
+    const float b0 = 1.0f - b1 - b2;
+    const float u = a.x * b0 + a.z * b1 + b.x * b2, v = a.y * b0 + a.w * b1 + b.y * b2;
+    const uint64_t lo = __float_as_uint(c.x), hi = __float_as_uint(c.y);
+    const float4* texels = reinterpret_cast<const float4*>(lo | hi << 32);
+    const uint32_t size = __float_as_uint(c.z);
+    const float4 t = bilinearWrap(texels, size & 0xffffu, size >> 16, make_float2(u * b.z, v * b.w));
+    return t.w >= c.w;
+}
+
 __device__ __forceinline__ void intersectTri(const float4* __restrict__ tris, int ti, float3 o, float3 d, float tmin,
                                              Hit& h, bool& found)
 {
@@ -66,6 +107,8 @@ __device__ __forceinline__ void intersectTri(const float4* __restrict__ tris, in
     uint32_t inst = __float_as_uint(a.w), prim = __float_as_uint(b.w);
     if (t < h.t || (t == h.t && found && keyLess(inst, prim, h.instance, h.prim)))
     {
+        const uint32_t cut = __float_as_uint(c.w);
+        if (cut != 0u && !cutoutPasses(tris + cut, u, v)) return;
         h.t = t;
         h.b1 = u;
         h.b2 = v;

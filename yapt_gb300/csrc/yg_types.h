@@ -68,7 +68,21 @@ struct alignas(16) GpuInstance
     float lightPdf;       // g_instanceLightSelectionPDFs entry (0: not a light)
     uint32_t hasTangents;
     uint32_t hasUVs;
-    uint32_t pad;
+    uint32_t alphaSource; // id + 1 of the instance's GpuAlphaSource, 0: opaque
+};
+
+// The cutout of an alpha-tested instance (alphaTestPasses, hitShadersCommon.hlsl:162-183): a
+// material with an alpha cutoff above 0 and an albedo texture, on a mesh with texture
+// coordinates. Traversal rejects a candidate hit whose albedo alpha at the hit's uv (times
+// the albedo uv scale) is below the cutoff. Used by the scene build only, which copies it into
+// the per-triangle cutout records behind the triangles.
+struct alignas(16) GpuAlphaSource
+{
+    const float4* texels;
+    uint32_t size;   // width | height << 16 (textures are at most 32768 texels wide)
+    float cutoff;
+    float su, sv;    // albedo uv scale
+    uint32_t pad[2];
 };
 
 // LightEntryGPU (materialsCommonResources.hlsl:51-71): the mesh lights first, then the

@@ -70,6 +70,11 @@ def affine(translation=(0, 0, 0), rotation=None, scale=(1, 1, 1)):
     return M
 
 
+def rotation_x(angle):
+    c, s = np.cos(angle), np.sin(angle)
+    return np.array([[1, 0, 0], [0, c, -s], [0, s, c]])
+
+
 def rotation_y(angle):
     c, s = np.cos(angle), np.sin(angle)
     return np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
