@@ -266,6 +266,12 @@ YG_API int yg_clear_textures(yg_context* ctx);
 /* The environment (RVARNAME_SKYBOX with a longitude-latitude map): texture id + 1, or 0 for the
  * reference's analytic |dir| sky. Scaled by env_intensity_scale of each request. */
 YG_API int yg_set_environment_texture(yg_context* ctx, uint32_t texture);
+/* A cube-map environment (RVARNAME_SKYBOX holding a TEXTURE_CUBEMAP; envType
+ * ENVIRONMENT_TYPE_CUBE, RaytraceCommonResources.cpp:292-296 and getSkyBoxColor,
+ * materialsCommonResources.hlsl:196-199): texture id + 1 of an uploaded texture whose six square
+ * faces are stacked top to bottom in layer order +X, -X, +Y, -Y, +Z, -Z (height = 6 x width).
+ * yg_set_environment_texture switches back to a longitude-latitude map or the analytic sky. */
+YG_API int yg_set_environment_cube(yg_context* ctx, uint32_t texture);
 /* The tonemap stage (TonemapStage.cpp; knobs Tonemap.* of RendererVarsList.h:50-57): the film
  * mean or the last a-trous output in linear sRGB, a 128-bucket EV histogram from EV -12, auto
  * exposure (key 0.18 over the mean luminance, exposure compensation in EV, approached with

@@ -1836,10 +1836,63 @@ template <typename T> void meshUV(const oracle_scene* sc, const oracle_instance&
 }
 
 // getSkyBoxColor (materialsCommonResources.hlsl:181-224) times the intensity scale
+// TextureCube.SampleLevel(LINEAR, dir, 0) restated: the Vulkan cube map face selection (major
+// axis; sc, tc, ma per face, faces stacked +X, -X, +Y, -Y, +Z, -Z), then bilinear between texel
+// centres clamped to the face's edge texels, in the device's operation order
+template <typename T> void sampleCube(const Ctx<T>& c, int id, V3<T> d, T out[4])
+{
+    const T ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    int face;
+    T sc, tc, ma;
+    if (ax >= ay && ax >= az)
+    {
+        face = d.x >= T(0) ? 0 : 1;
+        sc = d.x >= T(0) ? -d.z : d.z;
+        tc = -d.y;
+        ma = ax;
+    }
+    else if (ay >= az)
+    {
+        face = d.y >= T(0) ? 2 : 3;
+        sc = d.x;
+        tc = d.y >= T(0) ? d.z : -d.z;
+        ma = ay;
+    }
+    else
+    {
+        face = d.z >= T(0) ? 4 : 5;
+        sc = d.z >= T(0) ? d.x : -d.x;
+        tc = -d.y;
+        ma = az;
+    }
+    const T s = T(0.5f) * (sc / ma + T(1)), t = T(0.5f) * (tc / ma + T(1));
+    const int W = (int)c.texW[id];
+    const T x = s * T(W) - T(0.5f), y = t * T(W) - T(0.5f);
+    const T fx = std::floor(x), fy = std::floor(y);
+    const T ax2 = x - fx, ay2 = y - fy;
+    const int xi = (int)fx, yi = (int)fy;
+    const int x0 = std::min(std::max(xi, 0), W - 1), x1 = std::min(std::max(xi + 1, 0), W - 1);
+    const int y0 = std::min(std::max(yi, 0), W - 1), y1 = std::min(std::max(yi + 1, 0), W - 1);
+    const float* F = c.tex[id].data() + 4 * (size_t)face * W * W;
+    const float* c00 = &F[4 * ((size_t)y0 * W + x0)];
+    const float* c10 = &F[4 * ((size_t)y0 * W + x1)];
+    const float* c01 = &F[4 * ((size_t)y1 * W + x0)];
+    const float* c11 = &F[4 * ((size_t)y1 * W + x1)];
+    const T sx = T(1) - ax2, sy = T(1) - ay2;
+    for (int k = 0; k < 4; ++k)
+        out[k] = (T(c00[k]) * sx + T(c10[k]) * ax2) * sy + (T(c01[k]) * sx + T(c11[k]) * ax2) * ay2;
+}
+
 template <typename T> V3<T> skyColor(const Ctx<T>& c, V3<T> d, T scale)
 {
     if (!c.sc->env_texture) return v3(std::fabs(d.x) * scale, std::fabs(d.y) * scale, std::fabs(d.z) * scale);
     V3<T> v = normalize(d);
+    if (c.sc->env_cube)
+    {
+        T t[4];
+        sampleCube(c, (int)c.sc->env_texture - 1, v, t);
+        return v3(t[0] * scale, t[1] * scale, t[2] * scale);
+    }
     T theta = std::atan2(v.z, v.x), phi = std::acos(clampT(v.y, T(-1), T(1)));
     T t[4];
     sampleTex(c, (int)c.sc->env_texture - 1, theta * C<T>::INVPI * T(0.5f) + T(0.5f), phi * C<T>::INVPI, t);

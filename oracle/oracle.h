@@ -64,7 +64,8 @@ typedef struct oracle_scene
     const float* uvs;                  /* 2 per vertex (may be NULL when no instance has uvs) */
     const oracle_texture* textures;    /* materials refer to id + 1 */
     uint32_t n_textures;
-    uint32_t env_texture;              /* id + 1 of a longitude-latitude environment, 0: |dir| */
+    uint32_t env_texture;              /* id + 1 of the environment texture, 0: |dir| */
+    uint32_t env_cube;                 /* 1: env_texture is a cube map (six faces stacked), 0: longitude-latitude */
 } oracle_scene;
 
 typedef struct oracle_stats

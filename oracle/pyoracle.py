@@ -40,7 +40,7 @@ class OracleScene(C.Structure):
                 ("rgb_to_spd", C.POINTER(C.c_float)), ("data_dir", C.c_char_p),
                 ("punctual", C.POINTER(N.PunctualLight)), ("n_punctual", C.c_uint32),
                 ("uvs", C.POINTER(C.c_float)), ("textures", C.POINTER(OracleTexture)), ("n_textures", C.c_uint32),
-                ("env_texture", C.c_uint32)]
+                ("env_texture", C.c_uint32), ("env_cube", C.c_uint32)]
 
 
 class OracleStats(C.Structure):
@@ -142,6 +142,7 @@ class OracleSceneHandle:
         s.textures = tx
         s.n_textures = len(scene.textures)
         s.env_texture = scene.env_texture
+        s.env_cube = 1 if getattr(scene, "env_cube", False) else 0
         self.keep += [inst, mats, cam, pl, tx]
         self.s = s
 

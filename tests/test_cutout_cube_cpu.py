@@ -4,7 +4,10 @@ for camera, bounce and shadow rays alike (PROCEED_ALPHA_TESTED, rayHitDefault.hl
 BDPTCommon.hlsl:1157).
 
 A cutoff above every alpha cuts a panel away completely, so the image must equal, sample by
-sample, the scene without the panels; a cutoff of 0 turns the test off (the panels are opaque)."""
+sample, the scene without the panels; a cutoff of 0 turns the test off (the panels are opaque).
+
+Also the cube-map environment (getSkyBoxColor with ENVIRONMENT_TYPE_CUBE) against a
+longitude-latitude map of the same constant colour."""
 import numpy as np
 import pytest
 
@@ -59,3 +62,21 @@ def test_scene_carries_the_cutout_materials():
     mats = sc.materials[-2:]
     assert all(m["alpha_cutoff"] == 0.5 and m["albedo_texture"] > 0 for m in mats)
     assert all(sc.meshes[mesh].get("uvs") is not None for (_, mesh, _, _) in sc.instances[-2:])
+
+
+def test_constant_cube_map_matches_a_constant_longitude_latitude_map(built, host_luts):
+    """A cube map and a longitude-latitude map of one colour light the scene alike (up to the
+    last-bit rounding of the bilinear weights); a cube map read from the wrong face or texel
+    would not."""
+    colour = np.array([0.7, 0.45, 0.3, 1.0], np.float32)
+    cube = configs.cube_sky_scene(1, face=8)
+    cube.textures[-1] = (8, 48, N.YG_TEXTURE_RGBA32_FLOAT, np.tile(colour, (48, 8, 1)))
+    flat = configs.environment_sky_scene(1)
+    flat.textures[-1] = (16, 8, N.YG_TEXTURE_RGBA32_FLOAT, np.tile(colour, (8, 16, 1)))
+    import pyoracle
+    p = Context.params("nee", 24, 20, spp=2, max_depth=6, lambda_range=(380, 780), flags=256, env_scale=1.0)
+    rgb = N.host_table("rgb_to_spd", (380, 780))
+    a = pyoracle.OracleSceneHandle(cube, host_luts, rgb).render(p, precision=32)["records"]
+    b = pyoracle.OracleSceneHandle(flat, host_luts, rgb).render(p, precision=32)["records"]
+    assert np.any(b[..., 1:5] > 0)
+    assert np.allclose(a[..., 1:5], b[..., 1:5], rtol=1e-5, atol=1e-7)

@@ -222,5 +222,20 @@ def test_textures_and_skybox(built, py_yapt):
     sc.update(0.0, 2)
     img = film_of(Y, r)
     assert np.all(np.isfinite(img)) and float(img[..., 1].mean()) > 0.0
+    # a cube map of the same constant sky, its faces uploaded in two ranges of slices, lights
+    # the scene alike (up to the last-bit rounding of the bilinear weights)
+    cube = r.createTexture("cube", Y.ResourceDimension.TEXTURE_CUBEMAP, Y.ResourceFormat.RGBA32_SFLOAT, 0, 8, 8, 1, 6)
+    faces = np.ones((6, 8, 8, 4), np.float32)
+    cube.upload(0, 0, 1, 2, 8 * 16, faces.ctypes.data, 0)
+    cube.upload(0, 2, 1, 4, 8 * 16, faces.ctypes.data, 2 * 8 * 8 * 16)
+    with pytest.raises(Y.YaptError):
+        cube.upload(0, 4, 1, 3, 8 * 16, faces.ctypes.data, 0)  # slices 4..6 of six
+    with pytest.raises(Y.YaptError):
+        mats[0].setAlbedoTexture(cube, Y.vec2([1.0, 1.0]))
+    with pytest.raises(Y.YaptError):
+        r.createTexture("c", Y.ResourceDimension.TEXTURE_CUBEMAP, Y.ResourceFormat.RGBA8_UNORM, 0, 8, 4, 1, 6)
+    var.setTexture(cube)
+    sc.update(0.0, 2)
+    assert np.allclose(film_of(Y, r), img, rtol=1e-5, atol=1e-7)
     sc.shutdown()
     r.shutdown()

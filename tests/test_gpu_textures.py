@@ -25,11 +25,13 @@ pytestmark = pytest.mark.gpu
 def scene(name):
     if name == "textured":
         return configs.textured_box_scene(1), 0.0
+    if name == "cube":
+        return configs.cube_sky_scene(3), 1.0
     return configs.environment_sky_scene(2), 1.0
 
 
 @pytest.mark.parametrize("integrator", ["uni", "nee", "bdpt"])
-@pytest.mark.parametrize("name", ["textured", "environment"])
+@pytest.mark.parametrize("name", ["textured", "environment", "cube"])
 def test_per_sample_parity_with_the_oracle(built, host_luts, integrator, name):
     import pyoracle
     sc, env = scene(name)

@@ -194,6 +194,7 @@ SIGNATURES = [
     ("yg_upload_texture", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32)]),
     ("yg_clear_textures", C.c_int, [C.c_void_p]),
     ("yg_set_environment_texture", C.c_int, [C.c_void_p, C.c_uint32]),
+    ("yg_set_environment_cube", C.c_int, [C.c_void_p, C.c_uint32]),
     ("yg_atrous_default_params", None, [C.POINTER(AtrousParams)]),
     ("yg_tonemap_default_params", None, [C.POINTER(TonemapParams)]),
     ("yg_tonemap", C.c_int, [C.c_void_p, C.POINTER(TonemapParams), C.c_void_p, C.POINTER(C.c_float)]),

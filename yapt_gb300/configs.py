@@ -287,6 +287,21 @@ def environment_sky_scene(seed=0, aspect=1.0):
     return sc
 
 
+def cube_sky_scene(seed=0, aspect=1.0, face=16):
+    """``sky_scene`` under a cube-map environment (getSkyBoxColor with ENVIRONMENT_TYPE_CUBE):
+    six float RGBA faces, each a distinct tint with a gradient across it, so that the face
+    selection and the in-face coordinates both show in the image."""
+    sc = sky_scene(seed, aspect=aspect)
+    sc.name = "cube_sky(seed=%d)" % seed
+    t, s = (np.mgrid[0:face, 0:face] + 0.5) / face
+    tints = [(1.0, 0.5, 0.4), (0.4, 1.0, 0.5), (0.9, 0.9, 1.2), (0.3, 0.25, 0.2), (0.5, 0.6, 1.0), (1.0, 0.8, 0.3)]
+    faces = [np.stack([r * (0.6 + 0.4 * s), g * (0.6 + 0.4 * t), b * (1.0 - 0.3 * s * t), np.ones_like(s)], -1)
+             for (r, g, b) in tints]
+    sc.env_texture = sc.add_texture(np.concatenate(faces, 0).astype(np.float32))
+    sc.env_cube = True
+    return sc
+
+
 def punctual_box_scene(seed=0, area_light=True, aspect=1.0):
     """``box_scene`` lit by punctual lights (LightManager's point, spot and directional
     lights): a point light in the upper left, a spot light under the ceiling aimed at the

@@ -17,9 +17,10 @@
 // node's transform, intensity colour x max(0, intensity); lights with zero intensity are
 // left out.
 //
-// Textures: Renderer.createTexture (2D; RGBA8_UNORM, RGBA8_SRGB or RGBA32_SFLOAT), Texture.upload of
-// mip 0, Material.set{Albedo,Normal,ORM,Emissive}Texture(texture, uv scale) and the
-// World.Skycube variable (a longitude-latitude map).
+// Textures: Renderer.createTexture (2D, or a cube map of six square slices; RGBA8_UNORM, RGBA8_SRGB
+// or RGBA32_SFLOAT), Texture.upload of mip 0 (any range of a cube map's faces),
+// Material.set{Albedo,Normal,ORM,Emissive}Texture(texture, uv scale) and the World.Skycube variable
+// (a longitude-latitude map, or a cube map: envType ENVIRONMENT_TYPE_CUBE).
 //
 // Not built (they raise): other texture kinds, debug render pipelines, orthographic cameras.
 #include <pybind11/operators.h>
@@ -675,7 +676,8 @@ struct TextureData
     std::string name;
     uint32_t format = YG_TEXTURE_RGBA8_UNORM; // YG_TEXTURE_*
     uint32_t width = 0, height = 0;
-    std::vector<uint8_t> texels; // mip 0, rows packed
+    uint32_t layers = 1;         // 6 for a cube map (faces +X, -X, +Y, -Y, +Z, -Z)
+    std::vector<uint8_t> texels; // mip 0, rows packed, layer after layer
     uint64_t version = 0;
 };
 
@@ -858,6 +860,7 @@ struct Material
     // PyMaterial::set*Texture (PyMaterial.cpp:299-326): the texture and its uv scale
     void setSlot(int k, const std::shared_ptr<TextureData>& t, const vec2& scale)
     {
+        if (t && t->layers != 1) throw YaptError("material '" + d->name + "': a material texture is 2D, not a cube map");
         d->tex[k] = t;
         float* s = k == 0 ? d->m.albedo_uv_scale : k == 1 ? d->m.normal_uv_scale : k == 2 ? d->m.orm_uv_scale : d->m.emissive_uv_scale;
         s[0] = scale.v[0];
@@ -917,18 +920,26 @@ struct VarData
 struct Texture
 {
     std::shared_ptr<TextureData> d;
-    // PyTexture::upload: mip 0 of one 2D texture; rows rowPitchInBytes apart in host memory at
-    // data + dataPtrOffset (a numpy array's ctypes.data, as the reference scripts pass it)
+    // PyTexture::upload: mip 0 of slices [arrayOffset, arrayOffset + arrayCount) (one for a 2D
+    // texture, up to six faces of a cube map); rows rowPitchInBytes apart in host memory at
+    // data + dataPtrOffset (a numpy array's ctypes.data, as the reference scripts pass it), one
+    // slice after the other
     void upload(uint32_t mipOffset, uint32_t arrayOffset, uint32_t mipCount, uint32_t arrayCount, size_t rowPitch,
                 uintptr_t data, size_t offset)
     {
-        if (mipOffset != 0 || arrayOffset != 0 || arrayCount > 1 || mipCount < 1)
-            throw YaptError("texture '" + d->name + "': only mip 0 of a 2D texture is used");
+        if (mipOffset != 0 || mipCount < 1) throw YaptError("texture '" + d->name + "': only mip 0 is used");
+        const uint32_t n = std::max<uint32_t>(arrayCount, 1);
+        if (arrayOffset >= d->layers || n > d->layers - arrayOffset)
+            throw YaptError("texture '" + d->name + "': slices outside the texture");
         const size_t texel = d->format == YG_TEXTURE_RGBA32_FLOAT ? 16 : 4, row = texel * d->width;
         if (rowPitch < row) throw YaptError("texture '" + d->name + "': row pitch smaller than a row");
+        if (!data) throw YaptError("texture '" + d->name + "': null data");
         const uint8_t* src = reinterpret_cast<const uint8_t*>(data) + offset;
-        d->texels.resize(row * d->height);
-        for (uint32_t y = 0; y < d->height; ++y) std::memcpy(d->texels.data() + y * row, src + y * rowPitch, row);
+        d->texels.resize(row * d->height * d->layers);
+        for (uint32_t l = 0; l < n; ++l)
+            for (uint32_t y = 0; y < d->height; ++y)
+                std::memcpy(d->texels.data() + ((size_t)(arrayOffset + l) * d->height + y) * row,
+                            src + ((size_t)l * d->height + y) * rowPitch, row);
         ++d->version;
     }
     std::string getName() const { return d->name; }
@@ -1383,9 +1394,12 @@ struct Renderer
     {
         (void)usage;
         (void)mips;
-        if (dim != ResourceDimension::TEXTURE_2D || depthOrSlices > 1)
-            throw YaptError("createTexture '" + name + "': only 2D textures are used by the GB300 integrators");
+        const bool cube = dim == ResourceDimension::TEXTURE_CUBEMAP;
+        if (cube ? (depthOrSlices != 6 || width != height) : (dim != ResourceDimension::TEXTURE_2D || depthOrSlices > 1))
+            throw YaptError("createTexture '" + name +
+                            "': 2D textures and cube maps of six square slices are used by the GB300 integrators");
         auto t = std::make_shared<TextureData>();
+        t->layers = cube ? 6 : 1;
         t->name = name;
         if (fmt == ResourceFormat::RGBA8_UNORM) t->format = YG_TEXTURE_RGBA8_UNORM;
         else if (fmt == ResourceFormat::RGBA8_SRGB) t->format = YG_TEXTURE_RGBA8_SRGB;
@@ -1394,7 +1408,7 @@ struct Renderer
         if (width == 0 || height == 0) throw YaptError("createTexture '" + name + "': empty texture");
         t->width = width;
         t->height = height;
-        t->texels.assign((size_t)width * height * (t->format == YG_TEXTURE_RGBA32_FLOAT ? 16 : 4), 0);
+        t->texels.assign((size_t)width * height * t->layers * (t->format == YG_TEXTURE_RGBA32_FLOAT ? 16 : 4), 0);
         return Texture{t};
     }
     Buffer createBuffer(const std::string& name, uint32_t usage, size_t size)
@@ -1553,9 +1567,12 @@ bool Scene::sync()
         for (auto& t : texs)
         {
             uint32_t id = 0;
-            check(yg_upload_texture(S.ctx, t->width, t->height, t->format, t->texels.data(), &id), "scene update");
+            check(yg_upload_texture(S.ctx, t->width, t->height * t->layers, t->format, t->texels.data(), &id),
+                  "scene update");
         }
-        check(yg_set_environment_texture(S.ctx, envTex), "scene update");
+        const auto& sky = S.var("World.Skycube")->texture;
+        if (envTex && sky && sky->layers == 6) check(yg_set_environment_cube(S.ctx, envTex), "scene update");
+        else check(yg_set_environment_texture(S.ctx, envTex), "scene update");
         S.lastTextures = texSig;
         texturesChanged = true;
     }

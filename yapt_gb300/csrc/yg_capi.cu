@@ -259,6 +259,7 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.uvs = ctx->dUV.as<float2>();
     S.textures = ctx->dTexTable.as<yg::GpuTexture>();
     S.envTexture = ctx->envTexture;
+    S.envCube = ctx->envCube ? 1u : 0u;
     S.indices = ctx->dIdx.as<uint32_t>();
     S.spectra = ctx->dSpec.as<float>();
     S.lutSS = ctx->dLut[0].as<float>();
@@ -594,6 +595,7 @@ YG_API int yg_clear_textures(yg_context* ctx)
     ctx->texBufs.clear();
     ctx->texTable.clear();
     ctx->envTexture = -1;
+    ctx->envCube = false;
     return YG_OK;
 }
 
@@ -603,6 +605,20 @@ YG_API int yg_set_environment_texture(yg_context* ctx, uint32_t texture)
     std::lock_guard<std::mutex> g(ctx->lock);
     if (texture > ctx->texTable.size()) return fail(YG_ERR_INVALID_ARGUMENT, "environment: unknown texture");
     ctx->envTexture = (int)texture - 1;
+    ctx->envCube = false;
+    return YG_OK;
+}
+
+YG_API int yg_set_environment_cube(yg_context* ctx, uint32_t texture)
+{
+    if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "environment: null context");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    if (texture == 0 || texture > ctx->texTable.size()) return fail(YG_ERR_INVALID_ARGUMENT, "environment: unknown texture");
+    const yg::GpuTexture& T = ctx->texTable[texture - 1];
+    if (T.height != 6 * T.width)
+        return fail(YG_ERR_INVALID_ARGUMENT, "environment: a cube map is six square faces stacked (height = 6 x width)");
+    ctx->envTexture = (int)texture - 1;
+    ctx->envCube = true;
     return YG_OK;
 }
 

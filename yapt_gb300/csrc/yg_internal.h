@@ -114,6 +114,7 @@ struct yg_context
     DevBuf dTexTable;
     DevBuf dDisplay, dDisplayOut; // tonemap histogram, exposure state, RGBA8 image
     int envTexture = -1;
+    bool envCube = false;
     uint32_t nLights = 0;   // mesh and punctual
     uint32_t nPunctual = 0;
     std::vector<yg_punctual_light> punctual;

@@ -133,11 +133,62 @@ YG_DEV float2 meshUV(const SceneView& S, const GpuInstance& I, const TriGeom& g,
 
 YG_DEV float2 scaleUV(float2 uv, float sx, float sy) { return make_float2(uv.x * sx, uv.y * sy); }
 
-// getSkyBoxColor (materialsCommonResources.hlsl:181-224): a longitude-latitude texture
-// (cartesianToSpherical, commonMath.hlsl:144-151) or, without one, |dir|; times the scale
+// TextureCube.SampleLevel(LINEAR, dir, 0) on six square faces stacked in layer order +X, -X,
+// +Y, -Y, +Z, -Z: the major axis picks the face and (sc, tc, ma) of the Vulkan cube map face
+// selection table give s = (sc / |ma| + 1) / 2, t = (tc / |ma| + 1) / 2; then bilinear between
+// texel centres in FP32, clamped to the face's edge texels (the hardware filters across the
+// seam into the neighbouring face; here the outer half texel repeats the edge).
+YG_DEV float4 sampleCube(const GpuTexture& T, float3 d)
+{
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    uint32_t face;
+    float sc, tc, ma;
+    if (ax >= ay && ax >= az)
+    {
+        face = d.x >= 0.0f ? 0u : 1u;
+        sc = d.x >= 0.0f ? -d.z : d.z;
+        tc = -d.y;
+        ma = ax;
+    }
+    else if (ay >= az)
+    {
+        face = d.y >= 0.0f ? 2u : 3u;
+        sc = d.x;
+        tc = d.y >= 0.0f ? d.z : -d.z;
+        ma = ay;
+    }
+    else
+    {
+        face = d.z >= 0.0f ? 4u : 5u;
+        sc = d.z >= 0.0f ? d.x : -d.x;
+        tc = -d.y;
+        ma = az;
+    }
+    const float s = 0.5f * (sc / ma + 1.0f), t = 0.5f * (tc / ma + 1.0f);
+    const int W = (int)T.width;
+    const float x = s * (float)W - 0.5f, y = t * (float)W - 0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float tx = x - fx, ty = y - fy;
+    const int xi = (int)fx, yi = (int)fy;
+    const int x0 = min(max(xi, 0), W - 1), x1 = min(max(xi + 1, 0), W - 1);
+    const int y0 = min(max(yi, 0), W - 1), y1 = min(max(yi + 1, 0), W - 1);
+    const float4* F = T.texels + (size_t)face * W * W;
+    const float4 c00 = __ldg(F + (size_t)y0 * W + x0), c10 = __ldg(F + (size_t)y0 * W + x1);
+    const float4 c01 = __ldg(F + (size_t)y1 * W + x0), c11 = __ldg(F + (size_t)y1 * W + x1);
+    const float sx = 1.0f - tx, sy = 1.0f - ty;
+    return (c00 * sx + c10 * tx) * sy + (c01 * sx + c11 * tx) * ty;
+}
+
+// getSkyBoxColor (materialsCommonResources.hlsl:181-224): a cube map, a longitude-latitude
+// texture (cartesianToSpherical, commonMath.hlsl:144-151) or, without one, |dir|; times the scale
 YG_DEV __noinline__ float3 skyTexture(const SceneView& S, float3 dir, float scale)
 {
     float3 v = normalize(dir);
+    if (S.envCube)
+    {
+        const float4 c = sampleCube(S.textures[S.envTexture], v);
+        return mk3(c.x * scale, c.y * scale, c.z * scale);
+    }
     float theta = atan2f(v.z, v.x), phi = acosf(clampf(v.y, -1.0f, 1.0f));
     float4 c = sampleTexture(S, S.envTexture, make_float2(theta * kINVPI * 0.5f + 0.5f, phi * kINVPI));
     return mk3(c.x * scale, c.y * scale, c.z * scale);

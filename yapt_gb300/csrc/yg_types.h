@@ -136,7 +136,8 @@ struct SceneView
     const uint32_t* sobol; // [spp_count][kSobolDims] points of this launch
     GpuCamera cam;
     const GpuTexture* textures;
-    int envTexture;        // longitude-latitude environment texture, -1: the analytic sky
+    int envTexture;        // environment texture, -1: the analytic sky
+    uint32_t envCube;      // 1: envTexture is a cube map (six square faces stacked), 0: longitude-latitude
     uint32_t nLights;      // mesh and punctual
     uint32_t nPunctual;    // the last nPunctual entries of lights
     uint32_t nInstances;

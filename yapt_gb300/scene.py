@@ -148,7 +148,8 @@ class Scene:
         self.name = "scene"
         self.punctual_lights = []  # dict(type, position, direction, intensity, cos_inner, cos_outer)
         self.textures = []         # (width, height, format, texel array)
-        self.env_texture = 0       # texture id + 1 of a longitude-latitude environment
+        self.env_texture = 0       # texture id + 1 of the environment (longitude-latitude map)
+        self.env_cube = False      # True: env_texture is a cube map, faces stacked +X, -X, +Y, -Y, +Z, -Z
 
     # -- building --------------------------------------------------------
     def add_texture(self, texels, fmt=None):
@@ -271,7 +272,10 @@ class Scene:
         for (w, h, fmt, a) in self.textures:
             tid = C.c_uint32()
             N.check(lib.yg_upload_texture(ctx, w, h, fmt, a.ctypes.data_as(C.c_void_p), C.byref(tid)))
-        N.check(lib.yg_set_environment_texture(ctx, self.env_texture))
+        if self.env_cube:
+            N.check(lib.yg_set_environment_cube(ctx, self.env_texture))
+        else:
+            N.check(lib.yg_set_environment_texture(ctx, self.env_texture))
         N.check(lib.yg_build_scene(ctx))
 
     def pooled(self):
