@@ -1572,6 +1572,10 @@ template <typename T> bool setup(Ctx<T>& c, const oracle_scene* sc, const Tables
         c.texW.push_back(X.width);
         c.texH.push_back(X.height);
     }
+    // the environment texture must exist, and a cube map is six square faces stacked (the
+    // checks yg_set_environment_texture / yg_set_environment_cube make)
+    if (sc->env_texture > sc->n_textures) return false;
+    if (sc->env_cube && sc->env_texture && c.texH[sc->env_texture - 1] != 6 * c.texW[sc->env_texture - 1]) return false;
     int a = (int)lmin, b = (int)lmax;
     double ys = 0, ds = 0;
     for (int l = a; l <= b; ++l)
@@ -2412,7 +2416,7 @@ template <typename T> int run(const oracle_scene* sc, const yg_render_params* P,
         lmaxf = 700;
     }
     Ctx<T> c;
-    setup(c, sc, &tb, T(lminf), T(lmaxf));
+    if (!setup(c, sc, &tb, T(lminf), T(lmaxf))) return -7; // a bad environment texture reference
     uint32_t cx = P->crop_x, cy = P->crop_y, cw = P->crop_w, ch = P->crop_h;
     if (cw == 0 || ch == 0)
     {
