@@ -5,12 +5,18 @@ Workload (one "step"): the NEE integrator over 500 icospheres (subdivision 2) on
 per pixel, path depth 12, spectral range 380..780 nm, seeded synthetic scene.
 Metric: Msamples/s (one sample = one camera path carrying 4 hero wavelengths).
 The GPU and the CPU baseline trace the identical samples (same Sobol index and
-pixel seed give the same radiance), so their images have equal relMSE at equal spp.
+pixel seed give the same radiance within 1e-4), so at equal spp their images have
+equal relMSE. That is measured, not assumed: both arms render the 128 x 128 centre
+crop at the step's 64 spp with sample indices 4096..4159 and report the crop's
+relMSE against the FP64 oracle fixture (4096 spp, indices 0..4095,
+tests/golden/nee_random_shapes_crop128_fp64_4096spp.npz).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the CPU restatement of the reference integrator (the
-oracle, all host threads) on a bounded crop of the same workload.
+oracle library alone, its own tables, all host threads) on a strided subsample of
+the same step: every 4th pixel in x and y of the 1024 x 1024 frame with all 64
+sample indices.
 """
 import argparse
 import json
@@ -28,7 +34,8 @@ WORKLOAD = dict(workload="nee_random_shapes_500_icospheres", width=1024, height=
 METRIC = "Msamples/s (NEE, random-shapes scene, 1024x1024, 64 spp, depth 12, equal relMSE)"
 # --workload bdpt: the bidirectional integrator on the caustic box (box layout, 150 icospheres of
 # which 60% dispersive dielectrics, 10 sphere lights; ~196k triangles), 512 x 512, 32 spp,
-# camera and light subpath depth 10. The CPU oracle has no BDPT, so that line has no CPU baseline.
+# camera and light subpath depth 10. Its CPU baseline is the oracle's BDPT on a centre crop (BDPT
+# couples the pixels of a camera group through their shared light path, so it is not strided).
 BDPT_WORKLOAD = dict(workload="bdpt_caustic_box_150_spheres_10_sphere_lights", width=512, height=512, spp=32,
                      max_depth=10, light_vertices=10, integrator="bdpt", lambda_nm=[380, 780], scene_seed=0)
 BDPT_METRIC = "Msamples/s (BDPT with MIS, caustic box scene, 512x512, 32 spp, depth 10)"
@@ -54,8 +61,10 @@ DENOISE_METRIC = "denoise: wall-time speed-up to relMSE 1e-3 at 1920x1080 (plain
 UNET_FLOP_PER_PIXEL = 2 * 9 * (16 * 32 + 32 * 32 + (32 * 64 + 64 * 64) / 4 + (64 * 128 + 128 * 128) / 16 +
                                (128 * 256 + 256 * 256) / 64 + (384 * 128 + 128 * 128) / 16 + (192 * 64 + 64 * 64) / 4 +
                                (96 * 32 + 32 * 32)) + 2 * 3 * 32
-CPU_CROP = (256, 256, 512, 512)  # bounded CPU sample: 512x512 centre crop
-CPU_SPP = 32
+CPU_STRIDE = 4  # bounded CPU sample: every 4th pixel in x and y of the frame, all of the step's spp
+BDPT_CPU_CROP = 64  # bounded CPU sample of the BDPT step: a 64 x 64 centre crop, all of the step's spp
+FP64_FIXTURE = os.path.join(ROOT, "tests", "golden", "nee_random_shapes_crop128_fp64_4096spp.npz")
+RELMSE_EPS = 1e-2  # relMSE = mean over pixels and channels of (x - r)^2 / (r^2 + eps), XYZ
 
 
 def read_peaks():
@@ -159,45 +168,121 @@ def allsum(world, v):
     return float(t.item())
 
 
-def cpu_port_rate(scene, seconds_hint=None, threads=None, spp=CPU_SPP, crop=CPU_CROP):
-    """The oracle (FP32 CPU restatement of the reference integrator) on a bounded crop."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def oracle_handle(scene, params):
+    """The oracle (FP32 CPU restatement of the reference integrator) on `scene` with the
+    oracle library's own tables: no GPU library is loaded."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    from yapt_gb300 import _native as N
-    from yapt_gb300.runtime import Context
-    names = ["ss", "ss_avg", "ssms", "ssms_avg", "trans_denser", "trans_lighter", "trans_avg_denser",
-             "trans_avg_lighter", "sheen"]
-    luts = {n: N.host_table(n) for n in names}
-    h = pyoracle.OracleSceneHandle(scene, luts)
+    return pyoracle.OracleSceneHandle(scene, pyoracle.own_luts()).ensure_rgb_table(params)
+
+
+def workload_params(spp_start=0, spp=None, crop=None):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    return pyoracle.render_params(WORKLOAD["integrator"], WORKLOAD["width"], WORKLOAD["height"], spp_start=spp_start,
+                                  spp=spp or WORKLOAD["spp"], max_depth=WORKLOAD["max_depth"],
+                                  lambda_range=WORKLOAD["lambda_nm"], crop=crop,
+                                  light_vertices=WORKLOAD.get("light_vertices", 0))
+
+
+def cpu_port_rate(handle, threads=None, spp=None):
+    """The oracle on a bounded sample of one step: uni/NEE every CPU_STRIDE-th pixel of the
+    frame in x and y; BDPT a centre crop. All of the step's sample indices."""
     threads = threads or os.cpu_count() or 1
-    side = min(crop[2], WORKLOAD["width"], WORKLOAD["height"])
-    crop = ((WORKLOAD["width"] - side) // 2, (WORKLOAD["height"] - side) // 2, side, side)
-    p = Context.params(WORKLOAD["integrator"], WORKLOAD["width"], WORKLOAD["height"], spp=spp,
-                       max_depth=WORKLOAD["max_depth"], lambda_range=WORKLOAD["lambda_nm"], crop=crop)
-    r = h.render(p, precision=32, threads=threads, records=False, film=False)
-    n = crop[2] * crop[3] * spp
-    return n / r["seconds"] / 1e6, threads, "%dx%d crop x %d spp of the workload (%d samples, %.1f s)" % (
-        crop[2], crop[3], spp, n, r["seconds"])
+    spp = spp or WORKLOAD["spp"]
+    W, H = WORKLOAD["width"], WORKLOAD["height"]
+    if WORKLOAD["integrator"] == "bdpt":
+        side = min(BDPT_CPU_CROP, W, H)
+        crop = ((W - side) // 2, (H - side) // 2, side, side)
+        r = handle.render(workload_params(spp=spp, crop=crop), precision=32, threads=threads, records=False, film=False)
+        n = side * side * spp
+        what = "%dx%d centre crop x %d spp of the step (%d samples, %.1f s)" % (side, side, spp, n, r["seconds"])
+    else:
+        r = handle.render_strided(workload_params(spp=spp), CPU_STRIDE, precision=32, threads=threads)
+        n = ((W + CPU_STRIDE - 1) // CPU_STRIDE) * ((H + CPU_STRIDE - 1) // CPU_STRIDE) * spp
+        what = ("every %dth pixel in x and y of the %dx%d frame x all %d spp of the step (%d samples, %.1f s)"
+                % (CPU_STRIDE, W, H, spp, n, r["seconds"]))
+    return n / r["seconds"] / 1e6, threads, what
+
+
+def load_fp64_fixture():
+    """(mean XYZ, variance of that mean, spec) of the FP64 oracle crop, or None when the
+    workload is not the one the fixture was made for."""
+    import numpy as np
+    if WORKLOAD["integrator"] != "nee" or (WORKLOAD["width"], WORKLOAD["height"]) != (1024, 1024):
+        return None
+    try:
+        z = np.load(FP64_FIXTURE)
+    except OSError:
+        return None
+    return z["mean"].astype(np.float64), z["var_of_mean"].astype(np.float64), json.loads(str(z["spec"]))
+
+
+def relmse(img, ref, eps=RELMSE_EPS):
+    import numpy as np
+    img = np.asarray(img, np.float64)
+    return float(np.mean((img - ref) ** 2 / (ref * ref + eps)))
+
+
+def fp64_judge_params(spec):
+    """The judged render: the fixture's crop at the step's spp, with sample indices just past
+    the fixture's (so the two estimates are independent)."""
+    return workload_params(spp_start=spec["spp_start"] + spec["spp"], spp=WORKLOAD["spp"], crop=spec["crop"])
+
+
+def cpu_relmse_vs_fp64(handle, threads=None):
+    fx = load_fp64_fixture()
+    if fx is None:
+        return None
+    mean, var, spec = fx
+    img = handle.render(fp64_judge_params(spec), precision=32, threads=threads or os.cpu_count() or 1, records=False,
+                        film=True)["film"]
+    return relmse(img, mean)
 
 
 def run_reference(args, world, rank):
     from yapt_gb300 import configs
     if rank != 0:
         return
-    scene = configs.random_shapes_scene(WORKLOAD["scene_seed"])
+    bdpt = WORKLOAD["integrator"] == "bdpt"
+    scene = configs.caustic_box_scene(WORKLOAD["scene_seed"]) if bdpt else configs.random_shapes_scene(WORKLOAD["scene_seed"])
+    h = oracle_handle(scene, workload_params())
     for _ in range(args.warmup):
-        cpu_port_rate(scene, spp=1)
+        cpu_port_rate(h, spp=1)
     rates = []
     t0 = time.time()
     for _ in range(args.steps):
-        r, threads, sample = cpu_port_rate(scene)
+        r, threads, sample = cpu_port_rate(h)
         rates.append(r)
     value = sum(rates) / len(rates)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": (time.time() - t0) * 1e3 / args.steps,
+    ms_per_step = (time.time() - t0) * 1e3 / args.steps
+    line = {"impl": "reference", "metric": BDPT_METRIC if bdpt else METRIC, "value": value, "unit": "Msamples/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(WORKLOAD),
-            "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample,
+                             "cpu_model": cpu_model(), "threads": threads},
+            "relmse_vs_fp64": cpu_relmse_vs_fp64(h),
             "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -323,10 +408,31 @@ def run_ours(args, world, rank, local):
         except (OSError, KeyError, ValueError):
             pass
     achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
+    # equal relMSE, measured: the GPU's and the CPU baseline's render of the FP64 fixture's crop
+    # at the step's spp (same sample indices, disjoint from the fixture's), each against the fixture
+    judged = None
+    fx = load_fp64_fixture()
+    if fx is not None and rank == 0:
+        mean, var, spec = fx
+        jp = fp64_judge_params(spec)
+        ctx.film_clear(W, H)
+        ctx.render(ctx.params(WORKLOAD["integrator"], W, H, spp_start=jp.spp_start, spp=jp.spp_count,
+                              max_depth=WORKLOAD["max_depth"], lambda_range=WORKLOAD["lambda_nm"], crop=spec["crop"]))
+        xyz, _ = ctx.film()
+        cx, cy, cw, ch = spec["crop"]
+        gpu_img = xyz[cy:cy + ch, cx:cx + cw, :3]
+        judged = {"gpu": relmse(gpu_img, mean), "cpu": None, "eps": RELMSE_EPS,
+                  "expected_noise_floor_fixture": float(np.mean(var / (mean * mean + RELMSE_EPS))),
+                  "crop": spec["crop"], "spp": int(jp.spp_count), "sample_indices": [int(jp.spp_start), int(jp.spp_start + jp.spp_count)],
+                  "fixture": os.path.relpath(FP64_FIXTURE, ROOT), "fixture_spp": spec["spp"]}
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu and not bdpt:
-        r, threads, sample = cpu_port_rate(scene)
-        cpu = {"value": r, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        h = oracle_handle(scene, workload_params())
+        r, threads, sample = cpu_port_rate(h)
+        cpu = {"value": r, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample,
+               "cpu_model": cpu_model(), "threads": threads}
+        if judged is not None:
+            judged["cpu"] = cpu_relmse_vs_fp64(h)
     if rank == 0:
         line = {"metric": BDPT_METRIC if bdpt else METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": sum(kernel_ms) / len(kernel_ms), "higher_is_better": True,
@@ -339,7 +445,7 @@ def run_ours(args, world, rank, local):
                              "algorithmic_bytes_per_launch": per_launch_bytes, "dominant": dominant,
                              "nodes_per_sample": tc["nodes"] / (W * H * spp),
                              "triangles_per_sample": tc["triangles"] / (W * H * spp)},
-                "cpu_baseline": cpu,
+                "cpu_baseline": cpu, "relmse_vs_fp64": judged,
                 "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "rays_per_sample": rays / (W * H * spp * args.steps),
                 "wall_s_timed": wall, "clocks": clocks.summary()}

@@ -378,9 +378,12 @@ YG_API int yg_film_relmse(yg_context* ctx, const float* reference_xyz, double ep
  * asynchronous on the context stream (ready after yg_synchronize).
  * Scratch: a file-scope device array of about 7 MB that every GPU loading the library holds
  * until exit; at most 256 sample indices per call (spp_count > 256 is rejected) and waves of
- * 16384 paths. The first call on a device looks up the array's device address; make that
- * first call before any stream capture. All calls share the one array: calls whose work
- * overlaps on the GPU (other contexts or threads, other streams) race on it. */
+ * 16384 paths. The first call on a device sets the array up: it looks up the array's device
+ * address and copies the constant Sobol generator matrices into it (a synchronous copy); make
+ * that first call before any stream capture. Later calls only launch kernels. All calls share
+ * the one array: calls whose work overlaps on the GPU (other contexts or threads, other
+ * streams) race on it. A material that refers to a texture that is no longer resident (after
+ * yg_clear_textures) is rejected, as by yg_render. */
 YG_API int yg_render_samples_noalloc(yg_context* ctx, const yg_render_params* params, float* device_sample_xyz);
 
 /* Device timing of the most recent yg_render: kernel milliseconds, rays traced. */

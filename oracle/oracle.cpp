@@ -16,6 +16,7 @@
 #include "oracle.h"
 
 #include "../include/yapt_fmath.h"
+#include "../yapt_gb300/csrc/yg_tables.h"
 
 #include <algorithm>
 #include <array>
@@ -25,6 +26,7 @@
 #include <cstring>
 #include <fstream>
 #include <limits>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -2404,8 +2406,11 @@ inline bool needsRgbTable(const oracle_scene* sc, const yg_render_params* P)
     return false;
 }
 
+// `stride` > 1 renders every stride-th pixel of the crop in x and y (a strided subsample of
+// the request, each pixel with its own sample indices); records and film are then laid out
+// over the ceil(crop_w / stride) x ceil(crop_h / stride) subsampled pixels.
 template <typename T> int run(const oracle_scene* sc, const yg_render_params* P, int threads, float* records, double* film,
-                              oracle_stats* stats)
+                              oracle_stats* stats, uint32_t stride = 1)
 {
     Tables tb;
     if (!loadCie(sc->data_dir, tb.cie) || !sobolMatrices(sc->data_dir, tb.sobol)) return -5;
@@ -2424,6 +2429,9 @@ template <typename T> int run(const oracle_scene* sc, const yg_render_params* P,
         cw = P->width;
         ch = P->height;
     }
+    const uint32_t px0 = cx, py0 = cy;
+    cw = (cw + stride - 1) / stride;
+    ch = (ch + stride - 1) / stride;
     std::vector<uint32_t> pts((size_t)P->spp_count * 256);
     for (uint32_t s = 0; s < P->spp_count; ++s)
         for (uint32_t d = 0; d < 256; ++d) pts[(size_t)s * 256 + d] = sobolUint(tb.sobol, P->spp_start + s, d);
@@ -2446,7 +2454,8 @@ template <typename T> int run(const oracle_scene* sc, const yg_render_params* P,
                     {
                         uint64_t idx = (uint64_t)s * npix + (uint64_t)y * cw + x;
                         V3<T> X;
-                        tracePath(c, *P, &pts[(size_t)s * 256], cx + x, cy + y, records ? records + idx * 8 : nullptr, X, rays);
+                        tracePath(c, *P, &pts[(size_t)s * 256], px0 + x * stride, py0 + y * stride,
+                                  records ? records + idx * 8 : nullptr, X, rays);
                         acc[0] += (double)X.x;
                         acc[1] += (double)X.y;
                         acc[2] += (double)X.z;
@@ -2491,6 +2500,22 @@ int oracle_render(const oracle_scene* sc, const yg_render_params* P, int precisi
     return orc::run<float>(sc, P, threads, records, film, stats);
 }
 
+int oracle_needs_rgb_table(const oracle_scene* sc, const yg_render_params* P)
+{
+    if (!sc || !P) return -1;
+    return orc::needsRgbTable(sc, P) ? 1 : 0;
+}
+
+int oracle_render_strided(const oracle_scene* sc, const yg_render_params* P, uint32_t stride, int precision, int threads,
+                          double* film, oracle_stats* stats)
+{
+    if (!sc || !P || stride == 0) return -1;
+    if (P->integrator > YG_INTEGRATOR_NEE) return -1; // uni and NEE (BDPT couples pixels through its light paths)
+    if (!sc->rgb_to_spd && orc::needsRgbTable(sc, P)) return -6;
+    if (precision == 64) return orc::run<double>(sc, P, threads, nullptr, film, stats, stride);
+    return orc::run<float>(sc, P, threads, nullptr, film, stats, stride);
+}
+
 int oracle_atrous_moments(const oracle_scene* sc, const yg_render_params* P, int threads, float* moments)
 {
     if (!sc || !P || !moments) return -1;
@@ -2514,6 +2539,51 @@ int oracle_sobol_matrices(const char* dir, uint32_t* out)
     std::vector<uint32_t> m;
     if (!orc::sobolMatrices(dir, m)) return -5;
     std::memcpy(out, m.data(), m.size() * 4);
+    return 0;
+}
+
+int oracle_host_table(const char* data_dir, int which, int lmin, int lmax, void* out, size_t capacity, size_t* count)
+{
+    if (!data_dir || !count) return -1;
+    std::string dir(data_dir), err;
+    std::vector<uint32_t> u;
+    std::vector<float> f;
+    std::vector<double> cie;
+    if (which == YG_TABLE_SOBOL_MATRICES)
+    {
+        if (!yg::buildSobolMatrices(dir + "/joe_kuo_6_21201_first256.txt", u, err)) return -5;
+    }
+    else if (which >= YG_TABLE_LUT_SS_NOFRESNEL && which <= YG_TABLE_LUT_SHEEN)
+    {
+        static std::mutex m;
+        static yg::MsLuts cache;
+        static bool built = false;
+        std::lock_guard<std::mutex> g(m);
+        if (!built)
+        {
+            yg::buildMsLuts(cache);
+            built = true;
+        }
+        const std::vector<float>* L[9] = {&cache.ss, &cache.ssAvg, &cache.ssms, &cache.ssmsAvg, &cache.transDenser,
+                                          &cache.transLighter, &cache.transAvgDenser, &cache.transAvgLighter, &cache.sheen};
+        f = *L[which - YG_TABLE_LUT_SS_NOFRESNEL];
+    }
+    else if (which == YG_TABLE_RGB_TO_SPD)
+    {
+        if (!yg::loadCie(dir + "/cie1931_2deg_d65_1nm.txt", cie, err)) return -5;
+        if (lmin < 360 || lmax > 830 || lmax <= lmin) return -1;
+        yg::buildRgbToSpd(cie, lmin, lmax, f);
+    }
+    else
+    {
+        return -1;
+    }
+    size_t n = u.empty() ? f.size() : u.size();
+    *count = n;
+    if (!out) return 0;
+    if (capacity < n) return -1;
+    if (u.empty()) std::memcpy(out, f.data(), n * sizeof(float));
+    else std::memcpy(out, u.data(), n * sizeof(uint32_t));
     return 0;
 }
 

@@ -15,6 +15,7 @@
 #ifndef YAPT_ORACLE_H
 #define YAPT_ORACLE_H
 
+#include <stddef.h>
 #include <stdint.h>
 #include "../include/yapt_gpu.h"
 
@@ -80,6 +81,17 @@ typedef struct oracle_stats
 int oracle_render(const oracle_scene* scene, const yg_render_params* params, int precision, int threads,
                   float* records, double* film_xyz, oracle_stats* stats);
 
+/* The uni/NEE render of every stride-th pixel of the crop in x and y (pixel (cx + i*stride,
+ * cy + j*stride) with its own sample indices and seeds); film_xyz (optional) holds the mean XYZ
+ * of the ceil(crop_w/stride) x ceil(crop_h/stride) rendered pixels. A bounded sample of a large
+ * request for timing. */
+int oracle_render_strided(const oracle_scene* scene, const yg_render_params* params, uint32_t stride, int precision,
+                          int threads, double* film_xyz, oracle_stats* stats);
+
+/* 1 when rendering params on the scene converts RGB colours to spectra (so the scene must
+ * carry rgb_to_spd), 0 when not, -1 on a null argument. */
+int oracle_needs_rgb_table(const oracle_scene* scene, const yg_render_params* params);
+
 /* Sobol generator matrices derived here from the Joe-Kuo file (256 x 32 uint32). */
 int oracle_sobol_matrices(const char* data_dir, uint32_t* out);
 
@@ -91,6 +103,14 @@ int oracle_atrous_moments(const oracle_scene* scene, const yg_render_params* par
 int oracle_atrous(uint32_t width, uint32_t height, const float* film_sum, const float* odd_sum, const float* moments,
                   const yg_camera* camera, const yg_atrous_params* params, int threads, float* out_xyzw,
                   float* out_variance, uint32_t* features);
+
+/* The precomputed tables the integrators read (YG_TABLE_SOBOL_MATRICES, YG_TABLE_LUT_*,
+ * YG_TABLE_RGB_TO_SPD for [lmin, lmax]), generated on the host without a GPU. The oracle and
+ * the device load the same tables by design: they are inputs of the integrator math, built by
+ * the shared generator (yapt_gb300/csrc/yg_tables.cpp, linked into this library) and checked
+ * on their own (brute-force integration of the LUTs, the reference's Sobol matrices). Same
+ * calling convention as yg_host_table: *count receives the element count; out may be NULL. */
+int oracle_host_table(const char* data_dir, int which, int lmin, int lmax, void* out, size_t capacity, size_t* count);
 
 /* Per-function checks (BSDF known-answer tests): evaluate a material at (wo, wi) for
  * the given hero wavelength; returns weight[4] and pdf. Object space, normal (0,1,0). */

@@ -68,6 +68,14 @@ def load():
         lib.oracle_atrous.restype = C.c_int
         lib.oracle_atrous.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(N.Camera),
                                       C.POINTER(N.AtrousParams), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.oracle_render_strided.restype = C.c_int
+        lib.oracle_render_strided.argtypes = [C.POINTER(OracleScene), C.POINTER(N.RenderParams), C.c_uint32, C.c_int,
+                                              C.c_int, C.c_void_p, C.POINTER(OracleStats)]
+        lib.oracle_needs_rgb_table.restype = C.c_int
+        lib.oracle_needs_rgb_table.argtypes = [C.POINTER(OracleScene), C.POINTER(N.RenderParams)]
+        lib.oracle_host_table.restype = C.c_int
+        lib.oracle_host_table.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t,
+                                          C.POINTER(C.c_size_t)]
         lib.oracle_sobol_matrices.restype = C.c_int
         lib.oracle_sobol_matrices.argtypes = [C.c_char_p, C.c_void_p]
         _lib = lib
@@ -79,6 +87,53 @@ def sobol_matrices():
     rc = load().oracle_sobol_matrices(N.DATA_DIR.encode(), out.ctypes.data_as(C.c_void_p))
     assert rc == 0
     return out
+
+
+LUT_NAMES = ["ss", "ss_avg", "ssms", "ssms_avg", "trans_denser", "trans_lighter", "trans_avg_denser",
+             "trans_avg_lighter", "sheen"]
+
+
+def host_table(name, lambda_range=(380, 700)):
+    """A precomputed table generated by the oracle library itself (no GPU library loaded):
+    "sobol", one of LUT_NAMES, or "rgb_to_spd" for the spectral range."""
+    which = N.TABLES[name]
+    n = C.c_size_t()
+    lib = load()
+    lo, hi = int(lambda_range[0]), int(lambda_range[1])
+    if lib.oracle_host_table(N.DATA_DIR.encode(), which, lo, hi, None, 0, C.byref(n)) != 0:
+        raise RuntimeError("oracle_host_table(%s) failed" % name)
+    out = np.zeros(n.value, dtype=np.uint32 if name == "sobol" else np.float32)
+    if lib.oracle_host_table(N.DATA_DIR.encode(), which, lo, hi, out.ctypes.data_as(C.c_void_p), out.size, C.byref(n)) != 0:
+        raise RuntimeError("oracle_host_table(%s) failed" % name)
+    return out
+
+
+def own_luts():
+    """The nine multiple-scattering / sheen LUTs, generated by the oracle library."""
+    return {n: host_table(n) for n in LUT_NAMES}
+
+
+def render_params(integrator="nee", width=64, height=64, spp_start=0, spp=1, max_depth=8, lambda_range=(380.0, 700.0),
+                  crop=None, regularize_after=8, regularize=True, env_scale=0.0, seed=0, flags=0, light_paths=0,
+                  light_vertices=0):
+    """A yg_render_params request (struct layout of include/yapt_gpu.h), built without the
+    GPU library."""
+    p = N.RenderParams()
+    p.integrator = N.INTEGRATORS[integrator] if isinstance(integrator, str) else int(integrator)
+    p.width, p.height = int(width), int(height)
+    p.spp_start, p.spp_count = int(spp_start), int(spp)
+    p.max_depth = int(max_depth)
+    p.regularize_after_vertices = int(regularize_after)
+    p.regularize_enable = 1 if regularize else 0
+    p.env_intensity_scale = float(env_scale)
+    p.seed = int(seed)
+    p.flags = int(flags)
+    if crop is not None:
+        p.crop_x, p.crop_y, p.crop_w, p.crop_h = [int(v) for v in crop]
+    p.lambda_min, p.lambda_max = float(lambda_range[0]), float(lambda_range[1])
+    p.bdpt_light_paths = int(light_paths)
+    p.bdpt_light_vertices = int(light_vertices)
+    return p
 
 
 class OracleSceneHandle:
@@ -125,8 +180,7 @@ class OracleSceneHandle:
         s.spec_points = 81
         s.spec_lmin, s.spec_lmax = 380.0, 780.0
         s.camera = C.pointer(cam)
-        for i, name in enumerate(["ss", "ss_avg", "ssms", "ssms_avg", "trans_denser", "trans_lighter",
-                                  "trans_avg_denser", "trans_avg_lighter", "sheen"]):
+        for i, name in enumerate(LUT_NAMES):
             s.luts[i] = fp(luts[name]).ctypes.data_as(C.POINTER(C.c_float))
         s.rgb_to_spd = fp(rgb_to_spd).ctypes.data_as(C.POINTER(C.c_float)) if rgb_to_spd is not None else None
         s.data_dir = N.DATA_DIR.encode()
@@ -160,6 +214,33 @@ class OracleSceneHandle:
             raise RuntimeError("oracle_render failed: %d" % rc)
         return dict(records=rec, film=fil, rays=st.rays, seconds=st.seconds)
 
+    def ensure_rgb_table(self, params):
+        """Gives the scene the oracle's own RGB -> spectrum fit for the request's range when the
+        request needs one (RGB colours, coloured lights or an environment)."""
+        if self.s.rgb_to_spd or load().oracle_needs_rgb_table(C.byref(self.s), C.byref(params)) != 1:
+            return self
+        lo, hi = params.lambda_min, params.lambda_max
+        if lo == 0.0 and hi == 0.0:
+            lo, hi = 380.0, 700.0
+        t = np.ascontiguousarray(host_table("rgb_to_spd", (lo, hi)), np.float32)
+        self.keep.append(t)
+        self.s.rgb_to_spd = t.ctypes.data_as(C.POINTER(C.c_float))
+        return self
+
+    def render_strided(self, params, stride, precision=32, threads=None, film=False):
+        """Every stride-th pixel of the crop in x and y (uni/NEE): a bounded sample of a large
+        request. film: mean XYZ (ceil(ch/stride), ceil(cw/stride), 3) in float64."""
+        threads = threads or os.cpu_count() or 1
+        cw = params.crop_w or params.width
+        ch = params.crop_h or params.height
+        fil = np.zeros(((ch + stride - 1) // stride, (cw + stride - 1) // stride, 3), np.float64) if film else None
+        st = OracleStats()
+        rc = load().oracle_render_strided(C.byref(self.s), C.byref(params), int(stride), precision, threads,
+                                          fil.ctypes.data_as(C.c_void_p) if fil is not None else None, C.byref(st))
+        if rc != 0:
+            raise RuntimeError("oracle_render_strided failed: %d" % rc)
+        return dict(film=fil, rays=st.rays, seconds=st.seconds)
+
     def atrous_moments(self, params, moments, threads=None):
         """Adds the first-camera-vertex feature moments of the request's samples onto
         `moments` (float32 (4, H, W, 4), layout of yg_atrous_read), in sample order."""
@@ -189,6 +270,4 @@ def atrous(film_sum, odd_sum, moments, camera, params, threads=None):
 
 
 def luts_from_context(ctx):
-    names = ["ss", "ss_avg", "ssms", "ssms_avg", "trans_denser", "trans_lighter", "trans_avg_denser",
-             "trans_avg_lighter", "sheen"]
-    return {n: ctx.table(n) for n in names}
+    return {n: ctx.table(n) for n in LUT_NAMES}

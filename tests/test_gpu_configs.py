@@ -1,0 +1,128 @@
+"""The benchmark configurations at their real sizes, through the C ABI.
+
+* Per-sample parity with the FP32 oracle (same Sobol index and pixel seed give the same
+  spectral radiance within 1e-4 relative) on the unidirectional box workload at its full
+  size (256 x 256, 16 spp, depth 8: 1,048,576 samples), on the NEE benchmark scene itself
+  (500 icospheres, 160,008 triangles) with sample indices spread over 0..65535, and on the
+  BDPT caustic-box benchmark scene.
+* The converged-image judgement: the GPU's 4096-spp render of the NEE benchmark crop
+  against the FP64 oracle fixture (tests/golden/make_fp64_crop.py), with sample indices
+  disjoint from the fixture's, so the two estimates are independent. The stated bound:
+  relMSE <= RELMSE_BOUND, and the measured relMSE must match what the two estimates'
+  own noise predicts (no bias beyond the noise). The reference's agreement measure
+  (block-averaged relative |difference|, Tests/IntegratorCompare/report.py:59-85) is
+  checked beside it.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from yapt_gb300 import configs
+from yapt_gb300.runtime import Context
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-4
+FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "nee_random_shapes_crop128_fp64_4096spp.npz")
+RELMSE_EPS = 1e-2
+# The stated bound: relMSE of the GPU's 4096-spp crop against the 4096-spp FP64 fixture. The
+# two estimates' noise alone predicts 1.39e-2 on this crop (the fixture's own term is 6.4e-3:
+# glass and dispersion make a few pixels very noisy); the FP32 oracle at the same disjoint
+# sample indices measures 1.38e-2, block-averaged rel|d| 0.48 % and a mean gap of -0.013 %.
+RELMSE_BOUND = 2.0e-2
+
+
+def compare(gpu, cpu, min_within=0.9995):
+    L_gpu, L_cpu = gpu[..., 1:5], cpu[..., 1:5]
+    assert np.array_equal(gpu[..., 0], cpu[..., 0]), "hero wavelengths differ"
+    rel = np.abs(L_gpu - L_cpu) / np.maximum(np.abs(L_cpu), 1e-6)
+    within = float(np.mean(np.all(rel <= REL_TOL, axis=-1)))
+    exact = float(np.mean(np.all(L_gpu == L_cpu, axis=-1)))
+    assert np.any(L_cpu > 0), "degenerate scene: no radiance"
+    assert within >= min_within, "only %.5f of samples within %g (exact %.5f)" % (within, REL_TOL, exact)
+    return within, exact
+
+
+def oracle_records(scene, params, host_luts):
+    import pyoracle
+    return pyoracle.OracleSceneHandle(scene, host_luts).render(params, precision=32)["records"]
+
+
+def test_uni_box_workload_at_full_size_per_sample(built, host_luts):
+    """256 x 256 pixels x 16 spp, depth 8, 4 hero wavelengths: every sample of the workload."""
+    sc = configs.box_scene(0)
+    p = Context.params("uni", 256, 256, spp_start=0, spp=16, max_depth=8, lambda_range=(380, 780), flags=256)
+    with Context(0) as c:
+        c.upload_scene(sc)
+        gpu = c.render(p, dump=True)
+    within, exact = compare(gpu, oracle_records(sc, p, host_luts))
+    assert gpu.shape[:3] == (16, 256, 256)
+
+
+@pytest.mark.parametrize("spp_start,spp", [(0, 2), (21, 2), (40, 3), (62, 2), (4093, 3), (65534, 2)])
+def test_nee_benchmark_scene_per_sample(built, host_luts, spp_start, spp):
+    """The 500-icosphere NEE benchmark scene itself, 64 x 64 centre crop of the 1024 x 1024
+    frame, depth 12, at sample indices across the step's 0..63 and well beyond it."""
+    sc = configs.random_shapes_scene(0)
+    p = Context.params("nee", 1024, 1024, spp_start=spp_start, spp=spp, max_depth=12, lambda_range=(380, 780),
+                       crop=(480, 480, 64, 64), flags=256)
+    with Context(0) as c:
+        c.upload_scene(sc)
+        gpu = c.render(p, dump=True)
+    compare(gpu, oracle_records(sc, p, host_luts))
+
+
+def test_bdpt_benchmark_scene_per_sample(built, host_luts):
+    """The caustic box of the BDPT benchmark (150 icospheres, 60 % dispersive dielectrics,
+    10 sphere lights), a 48 x 40 crop of the 512 x 512 frame, camera and light depth 10."""
+    sc = configs.caustic_box_scene(0)
+    p = Context.params("bdpt", 512, 512, spp_start=5, spp=2, max_depth=10, lambda_range=(380, 780),
+                       crop=(232, 240, 48, 40), light_vertices=10, flags=256)
+    with Context(0) as c:
+        c.upload_scene(sc)
+        gpu = c.render(p, dump=True)
+    compare(gpu, oracle_records(sc, p, host_luts), min_within=0.999)
+
+
+def relmse(img, ref, eps=RELMSE_EPS):
+    return float(np.mean((img - ref) ** 2 / (ref * ref + eps)))
+
+
+def block_mean(img, b):
+    h, w = img.shape[:2]
+    return img[:h - h % b, :w - w % b].reshape(h // b, b, w // b, b, -1).mean(axis=(1, 3))
+
+
+def test_converged_nee_crop_is_within_the_stated_relmse_of_the_fp64_oracle(built):
+    z = np.load(FIXTURE)
+    ref, var_ref = z["mean"].astype(np.float64), z["var_of_mean"].astype(np.float64)
+    spec = json.loads(str(z["spec"]))
+    cx, cy, cw, ch = spec["crop"]
+    W, H = spec["width"], spec["height"]
+    batches, per = 16, spec["spp"] // 16
+    first = spec["spp_start"] + spec["spp"]  # disjoint from the fixture's sample indices
+    means = []
+    with Context(0) as c:
+        c.upload_scene(configs.random_shapes_scene(0))
+        for b in range(batches):
+            c.film_clear(W, H)
+            c.render(c.params(spec["integrator"], W, H, spp_start=first + b * per, spp=per, max_depth=spec["max_depth"],
+                              lambda_range=spec["lambda_nm"], crop=spec["crop"]))
+            xyz, _ = c.film()
+            means.append(xyz[cy:cy + ch, cx:cx + cw, :3].astype(np.float64))
+    m = np.stack(means)
+    gpu = m.mean(axis=0)
+    var_gpu = m.var(axis=0, ddof=1) / batches
+    r = relmse(gpu, ref)
+    predicted = float(np.mean((var_gpu + var_ref) / (ref * ref + RELMSE_EPS)))
+    assert r <= RELMSE_BOUND, (r, predicted)
+    # no disagreement beyond the noise of the two estimates
+    assert 0.7 * predicted <= r <= 1.3 * predicted, (r, predicted)
+    # the reference's measure: 16x16 block averages, relative mean |difference| and mean gap
+    ga, ra = block_mean(gpu, 16), block_mean(ref, 16)
+    rel_down = float(np.abs(ga - ra).mean() / ((ga.mean() + ra.mean()) / 2))
+    gap = float((gpu.mean() - ref.mean()) / ref.mean())
+    assert rel_down < 0.01, rel_down
+    assert abs(gap) < 0.005, gap

@@ -75,3 +75,26 @@ def test_oracle_bdpt_and_nee_estimate_the_same_image_in_fp64(box):
         z = np.abs(mn.mean(axis=0) - mb.mean(axis=0)) / se
         assert z.max() < 5.0, (z.max(), mn.mean(), mb.mean())
     assert abs(bd.mean() - nee.mean()) / nee.mean() < 0.03
+
+
+def test_oracle_generates_the_same_tables_as_the_library(built):
+    """The oracle library builds its own copy of the precomputed tables, so the timed CPU
+    baseline loads no GPU library; the copies equal the library's bit for bit."""
+    import pyoracle
+    from yapt_gb300 import _native as N
+    for name in pyoracle.LUT_NAMES + ["sobol"]:
+        assert np.array_equal(pyoracle.host_table(name), N.host_table(name)), name
+    assert np.array_equal(pyoracle.host_table("rgb_to_spd", (380, 780)), N.host_table("rgb_to_spd", (380, 780)))
+
+
+def test_strided_subsample_renders_the_same_pixels_as_the_full_crop(box):
+    """oracle_render_strided (the bounded CPU sample of a large request) traces pixel
+    (cx + i*s, cy + j*s) exactly as the full render of the crop does."""
+    import pyoracle
+    _, h = box
+    p = pyoracle.render_params("nee", 40, 30, spp_start=3, spp=2, max_depth=8, lambda_range=(380, 780),
+                               crop=(5, 4, 23, 17))
+    full = h.render(p, precision=32, records=False, film=True)["film"]
+    sub = h.render_strided(p, 4, precision=32, film=True)["film"]
+    assert sub.shape == (5, 6, 3)
+    assert np.array_equal(sub, full[::4, ::4])

@@ -286,6 +286,16 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.cieYSumInv = ctx->cieYSumInv;
     S.d65SumInv = ctx->d65SumInv;
 }
+
+int checkMaterialTextures(const yg_context* c, const char* what)
+{
+    const size_t nTex = c->texTable.size();
+    for (const yg_material& m : c->materials)
+        if (m.albedo_texture > nTex || m.normal_texture > nTex || m.orm_texture > nTex || m.emissive_texture > nTex)
+            return fail(YG_ERR_INVALID_ARGUMENT,
+                        std::string(what) + ": a material refers to a texture that was not uploaded (or was cleared)");
+    return YG_OK;
+}
 } // namespace ygi
 
 using namespace ygi;
@@ -1055,10 +1065,7 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     if (r) return r;
     bool needRgb = sceneNeedsRgbLut(ctx, p->env_intensity_scale);
     if (needRgb && (r = ensureRgbLut(ctx, lmin, lmax))) return r;
-    const size_t nTex = ctx->texTable.size();
-    for (const yg_material& m : ctx->materials)
-        if (m.albedo_texture > nTex || m.normal_texture > nTex || m.orm_texture > nTex || m.emissive_texture > nTex)
-            return fail(YG_ERR_INVALID_ARGUMENT, "render: a material refers to a texture that was not uploaded");
+    if ((r = checkMaterialTextures(ctx, "render"))) return r;
 
     const uint64_t npix = (uint64_t)cw * ch;
     const bool bdpt = p->integrator == YG_INTEGRATOR_BDPT;
@@ -1571,8 +1578,10 @@ YG_API int yg_film_relmse(yg_context* ctx, const float* ref, double eps, double*
 // must not hit cudaMalloc's implicit device synchronisation in the middle of a frame.
 // yg_render_samples_noalloc renders with the wavefront kernels like yg_render, but its
 // scratch (path-state arena, Sobol points, generator matrices) is the file-scope device
-// array below, a fixed 6 MB that every GPU loading this library holds until exit. The
-// caller passes the scene (already built in the context) and the output buffer.
+// array below, kNoAllocScratchBytes = 256 KB of Sobol points + 32 KB of generator matrices
+// + 16384 paths x 416 B + 64 KB of slack, about 7 MB, that every GPU loading this library
+// holds until exit. The caller passes the scene (already built in the context) and the
+// output buffer.
 namespace
 {
 constexpr uint32_t kNoAllocWaveCapacity = 16384; // paths in flight per wave
@@ -1589,12 +1598,17 @@ std::mutex g_noallocMutex;
 void* g_noallocDevicePtr[256] = {};
 
 // Device address of the scratch array on `device` (which must be current). The host
-// symbol is only a stand-in, so the address is looked up once per device and cached.
-int noallocScratchAddress(int device, void** out)
+// symbol is only a stand-in, so the address is looked up once per device and cached. The
+// same one-time set-up copies the Sobol generator matrices (a constant table, identical in
+// every context) into their part of the array with a synchronous copy; later calls only
+// launch kernels.
+int noallocScratchAddress(int device, const std::vector<uint32_t>& sobolMatrices, void** out)
 {
     if (device < 0 || device >= 256) return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: device ordinal out of range");
     if (yg::wavefrontBytesPerSlot() > kNoAllocBytesPerSlot)
         return fail(YG_ERR_INVALID_ARGUMENT, "no-alloc render: scratch layout is smaller than the wavefront state");
+    if (sobolMatrices.size() * sizeof(uint32_t) != kNoAllocMatrixBytes)
+        return fail(YG_ERR_NOT_READY, "no-alloc render: Sobol generator matrices are not loaded");
     std::lock_guard<std::mutex> g(g_noallocMutex);
     if (!g_noallocDevicePtr[device])
     {
@@ -1602,6 +1616,10 @@ int noallocScratchAddress(int device, void** out)
         cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
         if (e != cudaSuccess || !p)
             return fail(YG_ERR_CUDA, std::string("no-alloc render: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        e = cudaMemcpy(static_cast<char*>(p) + kNoAllocSobolBytes, sobolMatrices.data(), kNoAllocMatrixBytes,
+                       cudaMemcpyHostToDevice);
+        if (e != cudaSuccess)
+            return fail(YG_ERR_CUDA, std::string("no-alloc render: generator matrix upload: ") + cudaGetErrorString(e));
         g_noallocDevicePtr[device] = p;
     }
     *out = g_noallocDevicePtr[device];
@@ -1664,15 +1682,15 @@ YG_API int yg_render_samples_noalloc(yg_context* ctx, const yg_render_params* p,
     if (needRgb && (ctx->rgbToSpd.empty() || ctx->rgbLmin != ctx->cieLmin || ctx->rgbLmax != ctx->cieLmax || !ctx->dRgb.p))
         return fail(YG_ERR_NOT_READY, "no-alloc render: the RGB spectral fit is not resident "
                                       "(render once with yg_render at this range first)");
+    int r = checkMaterialTextures(ctx, "no-alloc render");
+    if (r) return r;
     YG_CUDA(cudaSetDevice(ctx->device));
     void* scratch = nullptr;
-    int r = noallocScratchAddress(ctx->device, &scratch);
-    if (r) return r;
+    if ((r = noallocScratchAddress(ctx->device, ctx->sobolMatrices, &scratch))) return r;
     char* base = static_cast<char*>(scratch);
     uint32_t* sobolPts = reinterpret_cast<uint32_t*>(base);
-    uint32_t* matrices = reinterpret_cast<uint32_t*>(base + kNoAllocSobolBytes);
+    const uint32_t* matrices = reinterpret_cast<const uint32_t*>(base + kNoAllocSobolBytes);
     void* arena = base + kNoAllocSobolBytes + kNoAllocMatrixBytes;
-    YG_CUDA(cudaMemcpyAsync(matrices, ctx->sobolMatrices.data(), kNoAllocMatrixBytes, cudaMemcpyHostToDevice, ctx->stream));
     noallocSobolPoints<<<ctx->smCount, 256, 0, ctx->stream>>>(matrices, p->spp_start, p->spp_count, sobolPts);
 
     yg::SceneView S;

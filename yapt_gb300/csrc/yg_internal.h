@@ -175,6 +175,9 @@ int ensureRgbLut(yg_context* c, int lmin, int lmax);
 // CIE table of [lmin, lmax] (and the RGB table when needRgb) must be current.
 void fillSceneView(const yg_context* c, float lmin, float lmax, bool needRgb, yg::SceneView& S);
 int checkWideBvhStructure(yg_context* c);
+// Fails (naming `what`) when a material refers to a texture id that is not resident, e.g.
+// after yg_clear_textures: the device texture table then holds freed pointers.
+int checkMaterialTextures(const yg_context* c, const char* what);
 // the pixel order of the BDPT camera groups for a cw x ch crop
 void pixelPermutation(uint32_t cw, uint32_t ch, std::vector<uint32_t>& perm);
 } // namespace ygi

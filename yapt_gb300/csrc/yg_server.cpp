@@ -625,7 +625,9 @@ YG_API int yg_server_create(yg_context* const* scenes, uint32_t n, const yg_serv
         if (!c || c->device != s->device) return fail(YG_ERR_INVALID_ARGUMENT, "serve: scenes must share one device");
         std::lock_guard<std::mutex> g(c->lock);
         if (!c->sceneBuilt || !c->cameraSet) return fail(YG_ERR_NOT_READY, "serve: scene not built or camera not set");
-        int r = ensureCie(c, (int)s->lmin, (int)s->lmax);
+        int r = checkMaterialTextures(c, "serve");
+        if (r) return r;
+        r = ensureCie(c, (int)s->lmin, (int)s->lmax);
         if (r) return r;
         if (i > 0 && !scenes[0]->rgbToSpd.empty() && c->rgbToSpd.empty())
         {
