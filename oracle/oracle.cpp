@@ -2586,11 +2586,4 @@ int oracle_host_table(const char* data_dir, int which, int lmin, int lmax, void*
     else std::memcpy(out, u.data(), n * sizeof(uint32_t));
     return 0;
 }
-
-int oracle_eval_bsdf(const oracle_scene* sc, uint32_t material, float hero, const float* wo, const float* wi, int precision,
-                     double* weight4, double* pdf)
-{
-    (void)sc; (void)material; (void)hero; (void)wo; (void)wi; (void)precision; (void)weight4; (void)pdf;
-    return -1;
-}
 }

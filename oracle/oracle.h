@@ -7,10 +7,17 @@
  * reference images that relMSE is judged against). It is used by tests/, by
  * smoke() and by bench.py's CPU baseline, never by the product path.
  *
- * Parity status: the reference's hot path is HLSL for DX12/Vulkan ray tracing
- * and cannot be built or run here; its tests hold no golden vectors for this path
- * (only the Sobol generator matrices of SobolMatrices.h, which pin the sampler).
- * Integrator parity is therefore "unpinned" beyond the sampler table.
+ * Parity status: the reference's hot path is HLSL for DX12/Vulkan ray tracing and
+ * cannot run as a renderer here, and its tests hold no golden vectors for this path
+ * beyond the Sobol generator matrices of SobolMatrices.h. The shader math itself is
+ * pinned: oracle/ref_build.py compiles the reference's own .hlsl files as C++ (through
+ * oracle/hlsl_shim.h) into oracle/_ref/refcheck, which compares this oracle with them
+ * function by function on seeded inputs -- sampler and Owen scrambling bit for bit; the
+ * spectral conversions, ToXYZ, Russian roulette, GGX, Fresnel, sheen, every lobe, the
+ * multiple-scattering compensation (both models), layer probabilities, layer sampling and
+ * the layered evaluateSurface within 1e-4 (tests/test_reference_pin.py). Traversal, the
+ * bounce loop, NEE and the BDPT connection logic remain restatements checked against the
+ * device and against each other (uni/NEE/BDPT agreement), not against reference code.
  */
 #ifndef YAPT_ORACLE_H
 #define YAPT_ORACLE_H
@@ -111,11 +118,6 @@ int oracle_atrous(uint32_t width, uint32_t height, const float* film_sum, const 
  * on their own (brute-force integration of the LUTs, the reference's Sobol matrices). Same
  * calling convention as yg_host_table: *count receives the element count; out may be NULL. */
 int oracle_host_table(const char* data_dir, int which, int lmin, int lmax, void* out, size_t capacity, size_t* count);
-
-/* Per-function checks (BSDF known-answer tests): evaluate a material at (wo, wi) for
- * the given hero wavelength; returns weight[4] and pdf. Object space, normal (0,1,0). */
-int oracle_eval_bsdf(const oracle_scene* scene, uint32_t material, float hero, const float* wo, const float* wi,
-                     int precision, double* weight4, double* pdf);
 
 #ifdef __cplusplus
 }
