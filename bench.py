@@ -63,7 +63,8 @@ UNET_FLOP_PER_PIXEL = 2 * 9 * (16 * 32 + 32 * 32 + (32 * 64 + 64 * 64) / 4 + (64
                                (96 * 32 + 32 * 32)) + 2 * 3 * 32
 CPU_STRIDE = 4  # bounded CPU sample: every 4th pixel in x and y of the frame, all of the step's spp
 BDPT_CPU_CROP = 64  # bounded CPU sample of the BDPT step: a 64 x 64 centre crop, all of the step's spp
-FP64_FIXTURE = os.path.join(ROOT, "tests", "golden", "nee_random_shapes_crop128_fp64_4096spp.npz")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+FP64_FIXTURE = os.path.join(GOLDEN, "nee_random_shapes_crop128_fp64_4096spp.npz")
 RELMSE_EPS = 1e-2  # relMSE = mean over pixels and channels of (x - r)^2 / (r^2 + eps), XYZ
 
 
@@ -225,17 +226,30 @@ def cpu_port_rate(handle, threads=None, spp=None):
     return n / r["seconds"] / 1e6, threads, what
 
 
-def load_fp64_fixture():
-    """(mean XYZ, variance of that mean, spec) of the FP64 oracle crop, or None when the
-    workload is not the one the fixture was made for."""
+def fixture_name(integrator=None):
+    """The FP64 fixture of the current workload rendered with `integrator` (default: the
+    workload's own), or None."""
+    integrator = integrator or WORKLOAD["integrator"]
+    if WORKLOAD["workload"] == BDPT_WORKLOAD["workload"] and (WORKLOAD["width"], WORKLOAD["height"]) == (512, 512):
+        return "%s_caustic_box" % integrator
+    if WORKLOAD["workload"] == "nee_random_shapes_500_icospheres" and (WORKLOAD["width"], WORKLOAD["height"]) == (1024, 1024):
+        return "nee_random_shapes" if integrator == "nee" else None
+    return None
+
+
+def load_fp64_fixture(integrator=None):
+    """(mean XYZ, variance of that mean, spec, path) of the FP64 oracle crop of the workload,
+    or None when there is none for it."""
     import numpy as np
-    if WORKLOAD["integrator"] != "nee" or (WORKLOAD["width"], WORKLOAD["height"]) != (1024, 1024):
+    name = fixture_name(integrator)
+    if name is None:
         return None
+    path = os.path.join(GOLDEN, "%s_crop128_fp64_4096spp.npz" % name)
     try:
-        z = np.load(FP64_FIXTURE)
+        z = np.load(path)
     except OSError:
         return None
-    return z["mean"].astype(np.float64), z["var_of_mean"].astype(np.float64), json.loads(str(z["spec"]))
+    return z["mean"].astype(np.float64), z["var_of_mean"].astype(np.float64), json.loads(str(z["spec"])), path
 
 
 def relmse(img, ref, eps=RELMSE_EPS):
@@ -247,17 +261,44 @@ def relmse(img, ref, eps=RELMSE_EPS):
 def fp64_judge_params(spec):
     """The judged render: the fixture's crop at the step's spp, with sample indices just past
     the fixture's (so the two estimates are independent)."""
-    return workload_params(spp_start=spec["spp_start"] + spec["spp"], spp=WORKLOAD["spp"], crop=spec["crop"])
+    import copy
+    p = workload_params(spp_start=spec["spp_start"] + spec["spp"], spp=WORKLOAD["spp"], crop=spec["crop"])
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    p.integrator = pyoracle.N.INTEGRATORS[spec["integrator"]]
+    p.max_depth = spec["max_depth"]
+    return p
 
 
 def cpu_relmse_vs_fp64(handle, threads=None):
     fx = load_fp64_fixture()
     if fx is None:
         return None
-    mean, var, spec = fx
+    mean, var, spec, _ = fx
     img = handle.render(fp64_judge_params(spec), precision=32, threads=threads or os.cpu_count() or 1, records=False,
                         film=True)["film"]
     return relmse(img, mean)
+
+
+def gpu_relmse_vs_fp64(ctx, integrator=None):
+    """The GPU's render of the fixture's crop at the step's spp against the fixture."""
+    import numpy as np
+    fx = load_fp64_fixture(integrator)
+    if fx is None:
+        return None
+    mean, var, spec, path = fx
+    jp = fp64_judge_params(spec)
+    W, H = spec["width"], spec["height"]
+    ctx.film_clear(W, H)
+    ctx.render(ctx.params(spec["integrator"], W, H, spp_start=jp.spp_start, spp=jp.spp_count, max_depth=spec["max_depth"],
+                          lambda_range=spec["lambda_nm"], crop=spec["crop"], light_vertices=spec.get("light_vertices", 0)))
+    xyz, _ = ctx.film()
+    cx, cy, cw, ch = spec["crop"]
+    return {"gpu": relmse(xyz[cy:cy + ch, cx:cx + cw, :3], mean), "cpu": None, "eps": RELMSE_EPS,
+            "integrator": spec["integrator"],
+            "fixture_noise_term": float(np.mean(var / (mean * mean + RELMSE_EPS))), "crop": spec["crop"],
+            "spp": int(jp.spp_count), "sample_indices": [int(jp.spp_start), int(jp.spp_start + jp.spp_count)],
+            "fixture": os.path.relpath(path, ROOT), "fixture_spp": spec["spp"]}
 
 
 def run_reference(args, world, rank):
@@ -410,21 +451,28 @@ def run_ours(args, world, rank, local):
     achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9
     # equal relMSE, measured: the GPU's and the CPU baseline's render of the FP64 fixture's crop
     # at the step's spp (same sample indices, disjoint from the fixture's), each against the fixture
-    judged = None
-    fx = load_fp64_fixture()
-    if fx is not None and rank == 0:
-        mean, var, spec = fx
-        jp = fp64_judge_params(spec)
+    judged = gpu_relmse_vs_fp64(ctx) if rank == 0 else None
+    versus = None
+    if bdpt and rank == 0 and judged is not None:
+        # BDPT against NEE at equal relMSE on the caustic box: each integrator's crop at the
+        # step's spp against its own FP64 image (the two use different multiple-scattering models
+        # on rough dielectrics), and each integrator's device time per sample of the full frame;
+        # with relMSE proportional to 1/spp, the time to any common relMSE scales as
+        # (time per spp) x relMSE at the step's spp
+        nee_j = gpu_relmse_vs_fp64(ctx, "nee")
         ctx.film_clear(W, H)
-        ctx.render(ctx.params(WORKLOAD["integrator"], W, H, spp_start=jp.spp_start, spp=jp.spp_count,
-                              max_depth=WORKLOAD["max_depth"], lambda_range=WORKLOAD["lambda_nm"], crop=spec["crop"]))
-        xyz, _ = ctx.film()
-        cx, cy, cw, ch = spec["crop"]
-        gpu_img = xyz[cy:cy + ch, cx:cx + cw, :3]
-        judged = {"gpu": relmse(gpu_img, mean), "cpu": None, "eps": RELMSE_EPS,
-                  "expected_noise_floor_fixture": float(np.mean(var / (mean * mean + RELMSE_EPS))),
-                  "crop": spec["crop"], "spp": int(jp.spp_count), "sample_indices": [int(jp.spp_start), int(jp.spp_start + jp.spp_count)],
-                  "fixture": os.path.relpath(FP64_FIXTURE, ROOT), "fixture_spp": spec["spp"]}
+        nee_ms = []
+        for k in range(3):
+            ctx.render(ctx.params("nee", W, H, spp_start=base + k * spp, spp=spp, max_depth=WORKLOAD["max_depth"],
+                                  lambda_range=WORKLOAD["lambda_nm"]))
+            nee_ms.append(ctx.last_stats()["ms"])
+        ms_bdpt = sum(kernel_ms) / len(kernel_ms)
+        ms_nee = sorted(nee_ms)[1]
+        if nee_j is not None:
+            versus = {"relmse_bdpt": judged["gpu"], "relmse_nee": nee_j["gpu"], "spp": spp,
+                      "ms_per_frame_bdpt": ms_bdpt, "ms_per_frame_nee": ms_nee,
+                      "nee_fixture": nee_j["fixture"],
+                      "time_to_equal_relmse_bdpt_over_nee": (ms_bdpt * judged["gpu"]) / (ms_nee * nee_j["gpu"])}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         h = oracle_handle(scene, workload_params())
@@ -445,7 +493,7 @@ def run_ours(args, world, rank, local):
                              "algorithmic_bytes_per_launch": per_launch_bytes, "dominant": dominant,
                              "nodes_per_sample": tc["nodes"] / (W * H * spp),
                              "triangles_per_sample": tc["triangles"] / (W * H * spp)},
-                "cpu_baseline": cpu, "relmse_vs_fp64": judged,
+                "cpu_baseline": cpu, "relmse_vs_fp64": judged, "bdpt_vs_nee": versus,
                 "e2e": {"value": e2e_value, "unit": "Msamples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "rays_per_sample": rays / (W * H * spp * args.steps),
                 "wall_s_timed": wall, "clocks": clocks.summary()}

@@ -106,20 +106,33 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, Hi
 }
 
 
+// Shades the regrouped hits of shading classes [classLo, classHi): a contiguous range of the
+// regrouped queue, located from the class counts. The host launches one class group at a time,
+// so that the warps resident on an SM run one kind of surface and share its instructions.
+#ifndef YG_SHADE_MIN_BLOCKS
+#define YG_SHADE_MIN_BLOCKS 4
+#endif
 template <bool NEE>
-__global__ void __launch_bounds__(128, 4) wfShade(const SceneView S, const LaunchParams P, WaveState W, RayQueue Qin,
-                                               HitQueue H, RayQueue Qout, ShadowQueue SQ)
+__global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const SceneView S, const LaunchParams P, WaveState W, RayQueue Qin,
+                                               HitQueue H, RayQueue Qout, ShadowQueue SQ, const uint32_t* classCounts,
+                                               uint32_t classLo, uint32_t classHi)
 {
     Luts Lt = lutsOf(S);
-    const uint32_t n = *Qin.count;
+    uint32_t begin = 0, n = 0;
+    for (uint32_t c = 0; c < classHi; ++c)
+    {
+        if (c < classLo) begin += classCounts[c];
+        else n += classCounts[c];
+    }
     // uniform trip count per warp so that the warp-wide appends see every lane
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t rounds = (n + stride - 1) / stride;
     for (uint32_t r = 0; r < rounds; ++r)
     {
-        uint32_t i = first + r * stride;
-        bool active = i < n;
+        uint32_t j = first + r * stride;
+        bool active = j < n;
+        uint32_t i = begin + j;
         bool alive = false;
         ShadowRequest sr;
         sr.valid = false;
@@ -395,6 +408,14 @@ size_t wavefrontBytesPerSlot()
     return 5 * 16 + 16 + 16 + 64 + 32 + 64 + 20 + 56 + 52 + 1;
 }
 
+// Shading launches per bounce, by class ranges of the regrouped queue: misses and emitters
+// (short), opaque dielectric bases, conductors, transparent dielectrics.
+#ifndef YG_SHADE_ONE_LAUNCH
+constexpr uint32_t kShadeGroups[][2] = {{0, 2}, {2, 3}, {3, 4}, {4, kShadeClasses}};
+#else
+constexpr uint32_t kShadeGroups[][2] = {{0, kShadeClasses}};
+#endif
+
 int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint32_t capacity, int smCount,
                     cudaStream_t stream, KernelTimer* T)
 {
@@ -453,10 +474,16 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
             wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
             if (T) T->end(kKernelRegroup, stream);
             if (T) T->begin(stream);
-            if (P.integrator == 1) wfShade<true><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ);
-            else wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ);
+            for (const auto& g : kShadeGroups)
+            {
+                if (P.integrator == 1)
+                    wfShade<true><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ, classCounts, g[0], g[1]);
+                else
+                    wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ, classCounts, g[0], g[1]);
+                ++launches;
+            }
             if (T) T->end(kKernelShade, stream);
-            launches += 4;
+            launches += 3;
             if (P.integrator == 1 || S.nPunctual > 0)
             {
                 if (T) T->begin(stream);

@@ -480,6 +480,20 @@ struct ShadowRequest
     bool valid;
 };
 
+// The unidirectional integrators evaluate the layered BSDF at three places (the punctual and
+// the mesh light connection, and the sampled direction). One out-of-line copy keeps the
+// shading kernels' instruction footprint to a single copy of the layered evaluation, which
+// dominates their code; set YG_EVAL_INLINE to inline it at each site instead.
+#ifndef YG_EVAL_INLINE
+static __device__ __noinline__ Eval evaluateSurfaceOnce(const Luts& L, const Surface& s, const SurfaceCtx& c, float3 woOS,
+                                                        float3 wiOS, uint32_t flags, const Spectral& sp)
+{
+    return evaluateSurface(L, s, c, woOS, wiOS, flags, sp);
+}
+#else
+#define evaluateSurfaceOnce evaluateSurface
+#endif
+
 // With NEE every light is sampled; without it only the punctual lights, which BSDF sampling
 // can never hit (hasExplicitlySampledLights / sampleExplicitLight, rayHitDefault.hlsl:26-81).
 // A punctual light is visible when nothing is hit before it (checkUnoccluded) and its
@@ -526,7 +540,7 @@ YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, c
         float4 emission = emissionSpectrum(S, sp, I3, -1);
         if (allEqual4(emission, 0.0f) || !(pick > 0.0f)) return;
         float3 toLightOS = normalize(xformVector(w2o, toL));
-        Eval ev = evaluateSurface(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
+        Eval ev = evaluateSurfaceOnce(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
         float4 w = ev.weight;
         if ((ev.transmission & kTransDispersed) != 0 && !(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(w);
         if (allEqual4(w, 0.0f)) return;
@@ -555,7 +569,7 @@ YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, c
     }
     if (allEqual4(emission, 0.0f) || !(pdf > 0.0f)) return;
     float3 toLightOS = normalize(xformVector(w2o, toLightWS));
-    Eval ev = evaluateSurface(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
+    Eval ev = evaluateSurfaceOnce(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
     float4 w = ev.weight;
     if ((ev.transmission & kTransDispersed) != 0 && !(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(w);
     if (allEqual4(w, 0.0f)) return;
@@ -703,7 +717,7 @@ YG_DEV bool shadeSegment(const SceneView& S, const LaunchParams& P, const Luts& 
             ev.transmission = 0;
             if (!isZero3(wi))
             {
-                ev = evaluateSurface(Lt, s, c, wo, wi, isDelta ? kEvalTreatAsDelta : kEvalNone, sp);
+                ev = evaluateSurfaceOnce(Lt, s, c, wo, wi, isDelta ? kEvalTreatAsDelta : kEvalNone, sp);
                 if (isDiffuse) ps.flags |= kFlagRegularize;
             }
             ps.pdfThisRay = ev.pdf;

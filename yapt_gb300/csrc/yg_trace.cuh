@@ -153,10 +153,34 @@ struct TraceState
     int sp;
 };
 // the groups waiting below the current one (kept apart from TraceState so that the state's
-// scalars stay in registers)
+// scalars stay in registers), all in local memory
 struct TraceStack
 {
     uint2 e[kTraversalStack];
+    __device__ __forceinline__ void push(int sp, uint2 v) { e[sp] = v; }
+    __device__ __forceinline__ uint2 pop(int sp) const { return e[sp]; }
+};
+
+// The same stack with its top kSharedStack entries in the block's shared memory: one slice per
+// thread, laid out [entry][thread] so that a warp's entries fall in distinct banks. The wide
+// tree is shallow (a few levels for 10^5-10^6 triangles), so the deeper local-memory entries are
+// rarely touched and the node and triangle loads keep the L1 to themselves.
+constexpr int kSharedStack = 8;
+constexpr int kTraceBlock = 128; // the block size of every kernel that uses traceGrid
+struct SharedTraceStack
+{
+    uint2* sh; // this thread's slice (entry k at sh[k * kTraceBlock]), or null: local only
+    uint2 e[kTraversalStack];
+    __device__ __forceinline__ void push(int sp, uint2 v)
+    {
+        if (sh && sp < kSharedStack) sh[sp * kTraceBlock] = v;
+        else e[sp] = v;
+    }
+    __device__ __forceinline__ uint2 pop(int sp) const
+    {
+        if (sh && sp < kSharedStack) return sh[sp * kTraceBlock];
+        return e[sp];
+    }
 };
 
 __device__ __forceinline__ void traceBegin(TraceState& t, const SceneView& S, float3 o, float3 d, float tmin, float tmax)
@@ -180,13 +204,13 @@ __device__ __forceinline__ void traceBegin(TraceState& t, const SceneView& S, fl
 
 // Opens the next node (testing its eight child boxes and the triangles of the leaf slots
 // that are hit); returns false once nothing is left to visit.
-template <bool COUNT>
-__device__ __forceinline__ bool traceStep(TraceState& t, TraceStack& st, TraversalCount* tc)
+template <bool COUNT, typename Stack>
+__device__ __forceinline__ bool traceStep(TraceState& t, Stack& st, TraversalCount* tc)
 {
     if (t.gHits == 0)
     {
         if (t.sp == 0) return false;
-        const uint2 e = st.e[--t.sp];
+        const uint2 e = st.pop(--t.sp);
         t.gBase = e.x;
         t.gHits = e.y & 0xffu;
         t.gImask = e.y >> 8;
@@ -262,7 +286,7 @@ __device__ __forceinline__ bool traceStep(TraceState& t, TraceStack& st, Travers
     {
         // descend; the rest of the current group waits on the stack (one entry per
         // level, and the builder keeps the tree within kTraversalStack levels)
-        if (t.gHits && t.sp < kTraversalStack) st.e[t.sp++] = make_uint2(t.gBase, t.gHits | (t.gImask << 8));
+        if (t.gHits && t.sp < kTraversalStack) st.push(t.sp++, make_uint2(t.gBase, t.gHits | (t.gImask << 8)));
         t.gBase = __float_as_uint(n1.x);
         t.gImask = imask;
         t.gHits = hits;
@@ -290,7 +314,13 @@ template <bool COUNT, typename Begin, typename End>
 __device__ __forceinline__ void traceGrid(uint32_t n, Begin begin, End end, TraversalCount& tc, uint32_t& rays)
 {
     TraceState t;
+#ifndef YG_TRACE_LOCAL_STACK
+    __shared__ uint2 stackTop[kSharedStack * kTraceBlock];
+    SharedTraceStack st;
+    st.sh = threadIdx.x < (uint32_t)kTraceBlock ? stackTop + threadIdx.x : nullptr;
+#else
     TraceStack st;
+#endif
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         begin(t, i);
