@@ -411,25 +411,29 @@ def run_ours(args, world, rank, local):
         dominant = {"kernel": "whole render (bidirectional)", "avg_launch_ms": avg_ms}
     else:
         # per-kind device time from the timed steps; algorithmic bytes from one counting step
-        # of the same workload (same kernels, traversal counters on):
-        #  wfTrace: rays read (32 B), hits written (20 B), wide BVH nodes (80 B) and triangles (48 B)
-        #           its rays visit;
-        #  wfShade: per shaded path the regrouped ray and hit (52 B) and the path state (80 B)
-        #           read, the state written (80 B), a continuation ray (32 B) for every path
-        #           that continues and a shadow-queue entry (56 B) per light sample; volume
-        #           stacks are not counted (a lower bound).
+        # of the same workload (same kernels, traversal counters on), per bounce:
+        #  wfTrace:  rays read (origin and direction of the queued record, 32 B), hits written
+        #            (20 B), wide BVH nodes (80 B) and triangles (48 B) its rays visit;
+        #  regroup:  classification (hit read, 20 B; key written, 1 B) and the move of every
+        #            record with its hit (key 1 B + record 84 B + hit 20 B read, 104 B written);
+        #  wfShade:  (the four class-group launches of a bounce together) per shaded path the
+        #            regrouped record and hit read (104 B), the record of every continuing path
+        #            written (84 B), the radiance and hero wavelength of every ended path (20 B),
+        #            a shadow-queue entry (56 B) per light sample; volume stacks not counted.
         ctx.render(params(0, flags=N.YG_FLAG_COUNT_TRAVERSAL | N.YG_FLAG_NO_FILM | N.YG_FLAG_TIME_KERNELS))
         kp = ctx.kernel_profile()
         tc = {"nodes": kp["closest_nodes"] + kp["shadow_nodes"], "triangles": kp["closest_triangles"] + kp["shadow_triangles"]}
         samples_step = W * H * spp
+        R = kp["closest_rays"]
         algo = {
-            "trace": (kp["closest_rays"] * (32 + 20) + kp["closest_nodes"] * 80 + kp["closest_triangles"] * 48),
-            "shade": (kp["closest_rays"] * (52 + 80 + 80) + (kp["closest_rays"] - samples_step) * 32 + kp["shadow_rays"] * 56),
+            "trace": (R * (32 + 20) + kp["closest_nodes"] * 80 + kp["closest_triangles"] * 48),
+            "regroup": R * (20 + 1 + 1 + 104 + 104),
+            "shade": (R * 104 + (R - samples_step) * 84 + samples_step * 20 + kp["shadow_rays"] * 56),
         }
-        names = {"trace": "wfTrace", "shade": "wfShade"}
+        names = {"trace": "wfTrace", "regroup": "wfClassifyQ+wfRegroupQ", "shade": "wfShade"}
         total_ms = sum(v["ms"] for v in kinds.values())
         kernels = {}
-        for k in ("trace", "shade"):
+        for k in ("trace", "regroup", "shade"):
             nl = max(1, kp[k]["launches"])
             avg = kinds[k]["ms"] / max(1, kinds[k]["launches"])
             kernels[names[k]] = {"algorithmic_bytes_per_launch": algo[k] / nl, "avg_launch_ms": avg,
@@ -445,7 +449,8 @@ def run_ours(args, world, rank, local):
                 tj = json.load(f)
             traffic = tj[dom]["dram_bytes_per_launch"]
             for n in kernels:
-                kernels[n]["traffic"] = tj[n]["dram_bytes_per_launch"]
+                if n in tj:
+                    kernels[n]["traffic"] = tj[n]["dram_bytes_per_launch"]
         except (OSError, KeyError, ValueError):
             pass
     achieved = per_launch_bytes / (avg_ms / 1e3) / 1e9

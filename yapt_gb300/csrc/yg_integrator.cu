@@ -54,7 +54,82 @@ __global__ void __launch_bounds__(128) pathKernel(const SceneView S, const Launc
     if (COUNT) countTraversal(P.traversalCounter, tc);
 }
 
-__global__ void __launch_bounds__(256) wfGenerate(const SceneView S, const LaunchParams P, WaveState W, RayQueue Q,
+// ------------------------------------------------------------------ wavefront
+// The path state travels with its ray. A PathQueue holds the live paths of a wave in queue
+// order (structure of arrays): the regroup before shading moves each path's whole record with
+// its hit, so the shading kernel reads and writes contiguous records instead of gathering the
+// state of scattered slots. What stays per slot (sample): the volume stack (touched only inside
+// media), the first-hit features and the final radiance of paths that ended.
+struct PathQueue
+{
+    float4* thr;     // throughput
+    float4* tot;     // accumulated radiance
+    float4* orgPdf;  // ray origin, pdf of the ray
+    float4* dirHero; // ray direction, hero wavelength
+    uint4* misc;     // flags | pathLength << 8 | nVol << 16, dimension cursor, scramble seed, Sobol row
+    uint32_t* slot;  // the sample's slot in the wave
+    uint32_t* count;
+};
+struct SlotState
+{
+    float4* finalTot; // radiance of the ended path (x, y, z, w lanes); finalHero its hero wavelength
+    float* finalHero;
+    float4* volIOR;   // volume stack (RAY_MAX_VOLUMES_ENTERED = 4)
+    uint4* volMat;
+    float4* volAbs;   // [4][capacity]
+    float4* fhAlb;    // first-hit features
+    float4* fhNrm;
+    uint32_t capacity;
+};
+// shadow-queue target of a path that ended at this vertex: its slot, flagged
+constexpr uint32_t kShadowToSlot = 0x80000000u;
+
+YG_DEV void loadQueued(const PathQueue& Q, uint32_t i, const SlotState& W, uint32_t slot, PathState& ps,
+                       RandomSampler& rs, Spectral& sp, const SceneView& S)
+{
+    float4 t = Q.thr[i], a = Q.tot[i], o = Q.orgPdf[i], d = Q.dirHero[i];
+    uint4 m = Q.misc[i];
+    ps.throughput = t;
+    ps.total = a;
+    ps.origin = mk3(o.x, o.y, o.z);
+    ps.pdfThisRay = o.w;
+    ps.dir = mk3(d.x, d.y, d.z);
+    ps.flags = m.x & 0xffu;
+    ps.pathLength = (m.x >> 8) & 0xffu;
+    ps.nVol = (m.x >> 16) & 0xffu;
+    rs.dim = m.y;
+    rs.seed = m.z;
+    rs.point = S.sobol + (size_t)m.w * kSobolDims;
+    spectralOf(S, d.w, sp);
+    if (ps.nVol)
+    {
+        float4 vi = W.volIOR[slot];
+        uint4 vm = W.volMat[slot];
+        ps.volIOR[0] = vi.x; ps.volIOR[1] = vi.y; ps.volIOR[2] = vi.z; ps.volIOR[3] = vi.w;
+        ps.volMat[0] = vm.x; ps.volMat[1] = vm.y; ps.volMat[2] = vm.z; ps.volMat[3] = vm.w;
+        for (int k = 0; k < kMaxVolumes; ++k) ps.volAbs[k] = W.volAbs[(size_t)k * W.capacity + slot];
+    }
+}
+
+YG_DEV void storeQueued(const PathQueue& Q, uint32_t k, uint32_t slot, const PathState& ps, const RandomSampler& rs,
+                        float hero, uint32_t row)
+{
+    Q.thr[k] = ps.throughput;
+    Q.tot[k] = ps.total;
+    Q.orgPdf[k] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, ps.pdfThisRay);
+    Q.dirHero[k] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, hero);
+    Q.misc[k] = make_uint4(ps.flags | (ps.pathLength << 8) | (ps.nVol << 16), rs.dim, rs.seed, row);
+    Q.slot[k] = slot;
+}
+
+YG_DEV void storeVolumes(const SlotState& W, uint32_t slot, const PathState& ps)
+{
+    W.volIOR[slot] = mk4(ps.volIOR[0], ps.volIOR[1], ps.volIOR[2], ps.volIOR[3]);
+    W.volMat[slot] = make_uint4(ps.volMat[0], ps.volMat[1], ps.volMat[2], ps.volMat[3]);
+    for (int k = 0; k < kMaxVolumes; ++k) W.volAbs[(size_t)k * W.capacity + slot] = ps.volAbs[k];
+}
+
+__global__ void __launch_bounds__(256) wfGenerate(const SceneView S, const LaunchParams P, SlotState W, PathQueue Q,
                                                   uint64_t base, uint32_t n)
 {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
@@ -67,20 +142,18 @@ __global__ void __launch_bounds__(256) wfGenerate(const SceneView S, const Launc
         Spectral sp;
         PathState ps;
         beginPath(S, P, cx, cy, rs, sp, ps);
-        storePath(W, s, ps, rs, sp.hero, sl, false);
+        storeQueued(Q, s, s, ps, rs, sp.hero, sl);
         if (P.featAlbedo)
         {
             W.fhAlb[s] = splat4(0.0f);
             W.fhNrm[s] = splat4(0.0f);
         }
-        Q.o[s] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, __uint_as_float(s));
-        Q.d[s] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, 0.0f);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, HitQueue H, unsigned long long* rayCtr,
+__global__ void __launch_bounds__(128) wfTrace(const SceneView S, PathQueue Q, HitQueue H, unsigned long long* rayCtr,
                                                unsigned long long* travCtr)
 {
     const uint32_t n = *Q.count;
@@ -89,7 +162,7 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, Hi
     traceGrid<COUNT>(
         n,
         [&](TraceState& t, uint32_t i) {
-            const float4 o = Q.o[i], d = Q.d[i];
+            const float4 o = Q.orgPdf[i], d = Q.dirHero[i];
             traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000));
         },
         [&](const TraceState& t, uint32_t i) {
@@ -105,17 +178,87 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, RayQueue Q, Hi
     }
 }
 
+// shading-class key of every queued hit and the class counts (shadeClass of yg_wave.cuh)
+__global__ void __launch_bounds__(256) wfClassifyQ(const SceneView S, const uint32_t* count, HitQueue H, uint8_t* keys,
+                                                   uint32_t* counts)
+{
+    const uint32_t n = *count;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
+        bool active = i < n;
+        uint32_t key = active ? shadeClass(S, H.a[i], H.b[i]) : 0xffu;
+        if (active) keys[i] = (uint8_t)key;
+        for (uint32_t c = 0; c < (uint32_t)kShadeClasses; ++c)
+        {
+            uint32_t m = __ballot_sync(0xffffffffu, key == c);
+            if (lane == 0 && m) atomicAdd(&counts[c], (uint32_t)__popc(m));
+        }
+    }
+}
+
+// Moves every queued path (record and hit) to its class range: warp-aggregated cursors per class.
+__global__ void __launch_bounds__(256) wfRegroupQ(PathQueue A, HitQueue H, const uint8_t* keys, const uint32_t* counts,
+                                                  uint32_t* cursors, PathQueue B, HitQueue HB)
+{
+    const uint32_t n = *A.count;
+    uint32_t base[kShadeClasses];
+    uint32_t acc = 0;
+    for (int c = 0; c < kShadeClasses; ++c)
+    {
+        base[c] = acc;
+        acc += counts[c];
+    }
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t r = 0; r < rounds; ++r)
+    {
+        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
+        bool active = i < n;
+        uint32_t key = active ? keys[i] : 0xffu;
+        uint32_t pos = 0;
+        for (uint32_t c = 0; c < (uint32_t)kShadeClasses; ++c)
+        {
+            uint32_t m = __ballot_sync(0xffffffffu, key == c);
+            if (!m) continue;
+            uint32_t leader = (uint32_t)(__ffs(m) - 1);
+            uint32_t b0 = 0;
+            if (lane == leader) b0 = atomicAdd(&cursors[c], (uint32_t)__popc(m));
+            b0 = __shfl_sync(0xffffffffu, b0, leader);
+            if (key == c) pos = base[c] + b0 + __popc(m & ((1u << lane) - 1u));
+        }
+        if (active)
+        {
+            B.thr[pos] = A.thr[i];
+            B.tot[pos] = A.tot[i];
+            B.orgPdf[pos] = A.orgPdf[i];
+            B.dirHero[pos] = A.dirHero[i];
+            B.misc[pos] = A.misc[i];
+            B.slot[pos] = A.slot[i];
+            HB.a[pos] = H.a[i];
+            HB.b[pos] = H.b[i];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *B.count = n;
+}
 
 // Shades the regrouped hits of shading classes [classLo, classHi): a contiguous range of the
 // regrouped queue, located from the class counts. The host launches one class group at a time,
 // so that the warps resident on an SM run one kind of surface and share its instructions.
+// Continuing paths are appended to Qout (record by record), ended ones leave their radiance in
+// their slot.
 #ifndef YG_SHADE_MIN_BLOCKS
 #define YG_SHADE_MIN_BLOCKS 4
 #endif
 template <bool NEE>
-__global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const SceneView S, const LaunchParams P, WaveState W, RayQueue Qin,
-                                               HitQueue H, RayQueue Qout, ShadowQueue SQ, const uint32_t* classCounts,
-                                               uint32_t classLo, uint32_t classHi)
+__global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const SceneView S, const LaunchParams P, SlotState W,
+                                                                   PathQueue Qin, HitQueue H, PathQueue Qout, ShadowQueue SQ,
+                                                                   const uint32_t* classCounts, uint32_t classLo,
+                                                                   uint32_t classHi)
 {
     Luts Lt = lutsOf(S);
     uint32_t begin = 0, n = 0;
@@ -142,8 +285,8 @@ __global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const SceneV
         Spectral sp;
         if (active)
         {
-            slot = __float_as_uint(Qin.o[i].w);
-            loadPath(W, slot, ps, rs, sp, S);
+            slot = Qin.slot[i];
+            loadQueued(Qin, i, W, slot, ps, rs, sp, S);
             uint32_t nVol0 = ps.nVol;
             float4 ha = H.a[i];
             uint32_t hb = H.b[i];
@@ -164,31 +307,34 @@ __global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const SceneV
                 W.fhNrm[slot] = mk4(fh.normal.x, fh.normal.y, fh.normal.z, fh.depth);
             }
             alive = alive && ps.pathLength < P.maxDepth;
-            storePath(W, slot, ps, rs, sp.hero, (uint32_t)(rs.point - S.sobol) / kSobolDims, ps.nVol != 0 || nVol0 != 0);
+            if (ps.nVol != 0 || nVol0 != 0) storeVolumes(W, slot, ps);
+            if (!alive)
+            {
+                W.finalTot[slot] = ps.total;
+                W.finalHero[slot] = sp.hero;
+            }
         }
         uint32_t k = warpAppend(Qout.count, alive);
-        if (alive)
-        {
-            Qout.o[k] = mk4(ps.origin.x, ps.origin.y, ps.origin.z, __uint_as_float(slot));
-            Qout.d[k] = mk4(ps.dir.x, ps.dir.y, ps.dir.z, 0.0f);
-        }
+        if (alive) storeQueued(Qout, k, slot, ps, rs, sp.hero, (uint32_t)(rs.point - S.sobol) / kSobolDims);
         if (NEE || S.nPunctual > 0)
         {
-            uint32_t j = warpAppend(SQ.count, sr.valid);
+            uint32_t q = warpAppend(SQ.count, sr.valid);
             if (sr.valid)
             {
-                SQ.o[j] = mk4(sr.origin.x, sr.origin.y, sr.origin.z, __uint_as_float(slot));
-                SQ.d[j] = mk4(sr.dir.x, sr.dir.y, sr.dir.z, sr.tmax);
-                SQ.target[j] = make_uint2(sr.instance, sr.prim);
-                SQ.contrib[j] = sr.contrib;
+                SQ.o[q] = mk4(sr.origin.x, sr.origin.y, sr.origin.z, __uint_as_float(alive ? k : (slot | kShadowToSlot)));
+                SQ.d[q] = mk4(sr.dir.x, sr.dir.y, sr.dir.z, sr.tmax);
+                SQ.target[q] = make_uint2(sr.instance, sr.prim);
+                SQ.contrib[q] = sr.contrib;
             }
         }
     }
 }
 
+// Shadow rays: a visible light adds its contribution to the path's record in the next queue, or
+// to the slot of a path that ended at this vertex.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) wfShadow(const SceneView S, WaveState W, ShadowQueue SQ, unsigned long long* rayCtr,
-                                                unsigned long long* travCtr)
+__global__ void __launch_bounds__(128) wfShadow(const SceneView S, SlotState W, PathQueue Qnext, ShadowQueue SQ,
+                                                unsigned long long* rayCtr, unsigned long long* travCtr)
 {
     const uint32_t n = *SQ.count;
     TraversalCount tc{0, 0};
@@ -203,8 +349,16 @@ __global__ void __launch_bounds__(128) wfShadow(const SceneView S, WaveState W, 
             const uint2 tg = SQ.target[i];
             if (shadowVisible(t.found, t.h, tg.x, tg.y))
             {
-                const uint32_t s = __float_as_uint(SQ.o[i].w);
-                W.tot[s] = W.tot[s] + SQ.contrib[i];
+                const uint32_t to = __float_as_uint(SQ.o[i].w);
+                if (to & kShadowToSlot)
+                {
+                    const uint32_t s = to & ~kShadowToSlot;
+                    W.finalTot[s] = W.finalTot[s] + SQ.contrib[i];
+                }
+                else
+                {
+                    Qnext.tot[to] = Qnext.tot[to] + SQ.contrib[i];
+                }
             }
         },
         tc, rays);
@@ -216,13 +370,13 @@ __global__ void __launch_bounds__(128) wfShadow(const SceneView S, WaveState W, 
     }
 }
 
-__global__ void __launch_bounds__(256) wfFinalize(const SceneView S, const LaunchParams P, WaveState W, uint64_t base,
+__global__ void __launch_bounds__(256) wfFinalize(const SceneView S, const LaunchParams P, SlotState W, uint64_t base,
                                                   uint32_t n)
 {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
         Spectral sp;
-        spectralOf(S, W.dirHero[s].w, sp);
+        spectralOf(S, W.finalHero[s], sp);
         FirstHit fh{mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), 0.0f};
         if (P.featAlbedo)
         {
@@ -231,7 +385,7 @@ __global__ void __launch_bounds__(256) wfFinalize(const SceneView S, const Launc
             fh.normal = mk3(nd.x, nd.y, nd.z);
             fh.depth = nd.w;
         }
-        writeSample(S, P, base + s, sp, W.tot[s], fh);
+        writeSample(S, P, base + s, sp, W.finalTot[s], fh);
     }
 }
 
@@ -403,9 +557,10 @@ int launchPathKernel(const SceneView& S, const LaunchParams& P, int smCount, cud
 
 size_t wavefrontBytesPerSlot()
 {
-    // state (5 x 16 + 16 + 16 + 64) + features (32) + 2 ray queues (64) + hits (20) + shadow queue (56)
-    // + the regrouped ray and hit queues (32 + 20) and the class keys (1)
-    return 5 * 16 + 16 + 16 + 64 + 32 + 64 + 20 + 56 + 52 + 1;
+    // two path queues (5 x 16 + 4 each), per slot the final radiance (16 + 4), the volume stack
+    // (16 + 16 + 64) and the features (32); hits and regrouped hits (20 + 20), the shadow queue
+    // (56) and the class keys (1)
+    return 2 * (5 * 16 + 4) + 16 + 4 + 16 + 16 + 64 + 32 + 2 * 20 + 56 + 1;
 }
 
 // Shading launches per bounce, by class ranges of the regrouped queue: misses and emitters
@@ -426,28 +581,34 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
         return r;
     };
     size_t C = capacity;
-    WaveState W;
+    uint32_t* counters = (uint32_t*)take(256);
+    auto queue = [&](uint32_t* count) {
+        PathQueue q;
+        q.thr = (float4*)take(C * 16);
+        q.tot = (float4*)take(C * 16);
+        q.orgPdf = (float4*)take(C * 16);
+        q.dirHero = (float4*)take(C * 16);
+        q.misc = (uint4*)take(C * 16);
+        q.slot = (uint32_t*)take(C * 4);
+        q.count = count;
+        return q;
+    };
+    PathQueue QA = queue(counters + 0), QB = queue(counters + 1);
+    SlotState W;
     W.capacity = capacity;
-    W.thr = (float4*)take(C * 16);
-    W.tot = (float4*)take(C * 16);
-    W.orgPdf = (float4*)take(C * 16);
-    W.dirHero = (float4*)take(C * 16);
-    W.misc = (uint4*)take(C * 16);
+    W.finalTot = (float4*)take(C * 16);
+    W.finalHero = (float*)take(C * 4);
     W.volIOR = (float4*)take(C * 16);
     W.volMat = (uint4*)take(C * 16);
     W.volAbs = (float4*)take(C * 64);
     W.fhAlb = (float4*)take(C * 16);
     W.fhNrm = (float4*)take(C * 16);
-    uint32_t* counters = (uint32_t*)take(256);
-    RayQueue QA{(float4*)take(C * 16), (float4*)take(C * 16), counters + 0};
-    RayQueue QB{(float4*)take(C * 16), (float4*)take(C * 16), counters + 1};
     HitQueue H{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
+    HitQueue HS{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
     ShadowQueue SQ{(float4*)take(C * 16), (float4*)take(C * 16), (uint2*)take(C * 8), (float4*)take(C * 16),
                    counters + 2};
-    RayQueue QS{(float4*)take(C * 16), (float4*)take(C * 16), counters + 3};
-    HitQueue HS{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
     uint8_t* keys = (uint8_t*)take(C);
-    uint32_t* classCounts = counters + 8;  // [kShadeClasses] counts, then [kShadeClasses] cursors
+    uint32_t* classCounts = counters + 8; // [kShadeClasses] counts, then [kShadeClasses] cursors
     bool count = P.traversalCounter != nullptr;
     int launches = 0;
     const int traceBlocks = smCount * 16, shadeBlocks = smCount * 8;
@@ -458,28 +619,28 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
         if (gblocks > smCount * 8) gblocks = smCount * 8;
         wfGenerate<<<gblocks, 256, 0, stream>>>(S, P, W, QA, base, n);
         ++launches;
-        RayQueue* cur = &QA;
-        RayQueue* nxt = &QB;
+        // QA: the live paths in trace order; QB: the same paths regrouped by shading class.
+        // Shading reads QB and appends the continuing paths to QA again.
         for (uint32_t b = 0; b < P.maxDepth; ++b)
         {
             if (T) T->begin(stream);
-            if (count) wfTrace<true><<<traceBlocks, 128, 0, stream>>>(S, *cur, H, P.rayCounter, P.traversalCounter);
-            else wfTrace<false><<<traceBlocks, 128, 0, stream>>>(S, *cur, H, P.rayCounter, nullptr);
+            if (count) wfTrace<true><<<traceBlocks, 128, 0, stream>>>(S, QA, H, P.rayCounter, P.traversalCounter);
+            else wfTrace<false><<<traceBlocks, 128, 0, stream>>>(S, QA, H, P.rayCounter, nullptr);
             if (T) T->end(kKernelTrace, stream);
-            cudaMemsetAsync(nxt->count, 0, 4, stream);
-            cudaMemsetAsync(SQ.count, 0, 4, stream);
             cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
             if (T) T->begin(stream);
-            wfClassify<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
-            wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
+            wfClassifyQ<<<smCount * 4, 256, 0, stream>>>(S, QA.count, H, keys, classCounts);
+            wfRegroupQ<<<smCount * 4, 256, 0, stream>>>(QA, H, keys, classCounts, classCounts + kShadeClasses, QB, HS);
             if (T) T->end(kKernelRegroup, stream);
+            cudaMemsetAsync(QA.count, 0, 4, stream);
+            cudaMemsetAsync(SQ.count, 0, 4, stream);
             if (T) T->begin(stream);
             for (const auto& g : kShadeGroups)
             {
                 if (P.integrator == 1)
-                    wfShade<true><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ, classCounts, g[0], g[1]);
+                    wfShade<true><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QB, HS, QA, SQ, classCounts, g[0], g[1]);
                 else
-                    wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QS, HS, *nxt, SQ, classCounts, g[0], g[1]);
+                    wfShade<false><<<shadeBlocks, 128, 0, stream>>>(S, P, W, QB, HS, QA, SQ, classCounts, g[0], g[1]);
                 ++launches;
             }
             if (T) T->end(kKernelShade, stream);
@@ -487,14 +648,11 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
             if (P.integrator == 1 || S.nPunctual > 0)
             {
                 if (T) T->begin(stream);
-                if (count) wfShadow<true><<<traceBlocks, 128, 0, stream>>>(S, W, SQ, P.rayCounter, P.traversalCounter);
-                else wfShadow<false><<<traceBlocks, 128, 0, stream>>>(S, W, SQ, P.rayCounter, nullptr);
+                if (count) wfShadow<true><<<traceBlocks, 128, 0, stream>>>(S, W, QA, SQ, P.rayCounter, P.traversalCounter);
+                else wfShadow<false><<<traceBlocks, 128, 0, stream>>>(S, W, QA, SQ, P.rayCounter, nullptr);
                 if (T) T->end(kKernelShadow, stream);
                 ++launches;
             }
-            RayQueue* t = cur;
-            cur = nxt;
-            nxt = t;
         }
         wfFinalize<<<gblocks, 256, 0, stream>>>(S, P, W, base, n);
         ++launches;
