@@ -45,6 +45,7 @@ struct Mth<float>
     static void sincos(float x, float& s, float& c) { ygm_sincosf(x, &s, &c); }
     static float cos(float x) { return ygm_cosf(x); }
     static float exp(float x) { return ygm_expf(x); }
+    static float log(float x) { return ygm_logf(x); }
     static float pow(float x, float y) { return ygm_powf(x, y); }
 };
 template <>
@@ -58,6 +59,7 @@ struct Mth<double>
     }
     static double cos(double x) { return std::cos(x); }
     static double exp(double x) { return std::exp(x); }
+    static double log(double x) { return std::log(x); }
     static double pow(double x, double y) { return std::pow(x, y); }
 };
 
@@ -966,6 +968,7 @@ struct Surf
     T aniso, anisoRot, thinFilm, sheenRough, sheenAmount, focus, sssAmount;
     T diffOcc = T(1), specOcc = T(1); // unpackOcclusion of the ORM texture's occlusion
     uint32_t flags;
+    S4<T> sssRadius; // subsurface radius per lane (setFromRGBUnboundedNoIlluminant), when sssAmount > 0
 };
 template <typename T>
 struct SCtx
@@ -1495,7 +1498,9 @@ inline void triTest(const V3<float>& o, const V3<float>& d, float tminv, const V
 
 // Closest hit. The FP64 oracle traces in FP32 geometry too (the scene is FP32 data);
 // only shading runs in T.
-template <typename T> bool trace(const Ctx<T>& c, V3<T> oT, V3<T> dT, float tminv, float tmaxv, TriHit<float>& h)
+// onlyInst restricts the hits to one instance (the subsurface probe rays)
+template <typename T>
+bool trace(const Ctx<T>& c, V3<T> oT, V3<T> dT, float tminv, float tmaxv, TriHit<float>& h, uint32_t onlyInst = 0xffffffffu)
 {
     V3<float> o = v3((float)oT.x, (float)oT.y, (float)oT.z), d = v3((float)dT.x, (float)dT.y, (float)dT.z);
     h.t = tmaxv;
@@ -1525,6 +1530,7 @@ template <typename T> bool trace(const Ctx<T>& c, V3<T> oT, V3<T> dT, float tmin
             for (int i = nd.first; i < nd.first + nd.count; ++i)
             {
                 const auto& t = c.tris[c.triIdx[i]];
+                if (onlyInst != 0xffffffffu && t.inst != onlyInst) continue;
                 triTest(o, d, tminv, t.v0, t.e1, t.e2, t.inst, t.prim, h,
                         [&](float b1, float b2) { return cutoutPasses(c, t.inst, t.prim, b1, b2); });
             }
@@ -2014,6 +2020,121 @@ template <typename T> void fillSurf(const Ctx<T>& c, const Spec<T>& s4, uint32_t
     s.absorption = absZero ? sp(T(0)) : setFromRGBUnboundedNoIllum(c, s4, v3(T(M.absorption[0]), T(M.absorption[1]), T(M.absorption[2])));
     s.emissive = emission(c, s4, emi, M.emission_spectrum);
     s.sheenColor = s.sheenAmount > T(0) ? setFromRGB(c, s4, v3(T(M.sheen_tint[0]), T(M.sheen_tint[1]), T(M.sheen_tint[2]))) : sp(T(0));
+    // subsurfaceRadiusAmount.xyz = radius * scale, in FP32 as the material packing computes it
+    const float sr[3] = {M.subsurface_radius[0] * M.subsurface_radius_scale, M.subsurface_radius[1] * M.subsurface_radius_scale,
+                         M.subsurface_radius[2] * M.subsurface_radius_scale};
+    s.sssRadius = s.sssAmount > T(0) ? setFromRGBUnboundedNoIllum(c, s4, v3(T(sr[0]), T(sr[1]), T(sr[2]))) : sp(T(0));
+}
+
+// ---------------------------------------------------------------- subsurface (subsurface.hlsl)
+// The Christensen-Burley profile as a separable BSSRDF (subsurface.hlsl:88-394): profile, radius
+// sampling, probe frame, exit density, the energy that reaches the diffuse base, the exit lobe.
+template <typename T> T burleyScale(T albedo)
+{
+    T x = std::fabs(albedo - T(0.8f));
+    return T(1.85f) - albedo + T(7) * x * x * x;
+}
+template <typename T> T burleyD(T radius, T albedo) { return tmax(radius, T(1e-6f)) / burleyScale(albedo); }
+template <typename T> T burleyRMax(T d) { return T(20.7232658f) * d; }
+template <typename T> T burleyProfileArea(T r, T d)
+{
+    r = tmax(r, d * T(1e-4f));
+    return (Mth<T>::exp(-r / d) + Mth<T>::exp(-r / (T(3) * d))) / (T(8) * C<T>::PI * d * r);
+}
+template <typename T> T burleySampleRadius(T u, T d)
+{
+    T scale = d;
+    if (u < T(0.25f)) u *= T(4);
+    else
+    {
+        u = (u - T(0.25f)) / T(0.75f);
+        scale = T(3) * d;
+    }
+    return -scale * Mth<T>::log(tmax(T(1) - u, T(1e-7f)));
+}
+template <typename T> S4<T> subsurfaceRd(const Surf<T>& s, T dist)
+{
+    S4<T> rd;
+    for (int l = 0; l < 4; ++l) rd[l] = s.albedo[l] * burleyProfileArea(dist, burleyD(s.sssRadius[l], s.albedo[l]));
+    return rd;
+}
+// constructVectorBase (commonMath.hlsl:84-90)
+template <typename T> void vectorBase(V3<T> v, V3<T>& v2, V3<T>& v3o)
+{
+    if (std::fabs(v.x) > std::fabs(v.y)) v2 = v3(-v.z, T(0), v.x) / Mth<T>::sqrt(v.x * v.x + v.z * v.z);
+    else v2 = v3(T(0), v.z, -v.y) / Mth<T>::sqrt(v.y * v.y + v.z * v.z);
+    v3o = cross(v, v2);
+}
+template <typename T> void probeFrame(V3<T> n, uint32_t k, V3<T>& axis, V3<T>& u, V3<T>& v)
+{
+    V3<T> t, b;
+    vectorBase(n, t, b);
+    if (k == 0) { axis = n; u = t; v = b; }
+    else if (k == 1) { axis = t; u = b; v = n; }
+    else { axis = b; u = n; v = t; }
+}
+template <typename T> T pdfSssExit(const Surf<T>& s, V3<T> fromP, V3<T> fromN, V3<T> toP, V3<T> toN)
+{
+    V3<T> d = toP - fromP;
+    T pdf = 0;
+    for (uint32_t k = 0; k < 3; ++k)
+    {
+        V3<T> axis, pu, pv;
+        probeFrame(fromN, k, axis, pu, pv);
+        T du = dot(d, pu), dv = dot(d, pv);
+        T rProj = Mth<T>::sqrt(du * du + dv * dv);
+        T axisPdf = 0;
+        for (int l = 0; l < 4; ++l)
+        {
+            T dl = burleyD(s.sssRadius[l], s.albedo[l]);
+            if (rProj < burleyRMax(dl)) axisPdf += burleyProfileArea(rProj, dl);
+        }
+        pdf += (k == 0 ? T(0.5f) : T(0.25f)) * (T(1) / T(4)) * axisPdf * std::fabs(dot(toN, axis));
+    }
+    return pdf;
+}
+// getSubsurfaceEntryFactor (subsurface.hlsl:25-85)
+template <typename T> T sssEntryFactor(const LutSet<T>& L, const Surf<T>& s, const SCtx<T>& c, T hero)
+{
+    T left = 1;
+    T fromIOR = c.fromIOR, toIOR = c.toIOR;
+    if (s.ccAmount > T(0)) left *= energyAfterSpec(L, s.ccIOR / fromIOR, c.woC.y, s.ccRough, s.ccAmount);
+    if (s.sheenAmount > T(0)) left *= T(1) - L.sheen(std::fabs(c.woB.y), s.sheenRough) * s.sheenAmount;
+    if (s.metalness > T(0)) left *= T(1) - s.metalness;
+    T specAmount = (T(1) - s.metalness) * s.specAmount;
+    if (specAmount > T(0))
+    {
+        if (s.flags & YG_MATERIAL_DISPERSION)
+        {
+            if (c.exiting) fromIOR = cauchy(s, hero);
+            else toIOR = cauchy(s, hero);
+        }
+        left *= energyAfterSpec(L, toIOR / fromIOR, c.woB.y, s.roughness, specAmount);
+    }
+    T layer = (T(1) - s.metalness) * (T(1) - s.transparency) * s.sssAmount;
+    return layer * left * s.diffOcc;
+}
+// sampleSubsurfaceExitLobe / evaluateSubsurfaceExitLobe (subsurface.hlsl:340-392)
+template <typename T> V3<T> exitLobeSample(const Surf<T>& s, const SCtx<T>& c, V3<T> wo, T r0, T r1)
+{
+    V3<T> wi = mulvM(cosHemi(r0, r1), c.baseB);
+    if (dot(wi, s.geoN) * dot(wo, s.geoN) <= T(0)) return v3(T(0), T(0), T(0));
+    return wi;
+}
+template <typename T> void exitLobeEval(const Surf<T>& s, const SCtx<T>& c, V3<T> wo, V3<T> wi, uint32_t flags, S4<T>& w, T& pdf)
+{
+    w = sp(T(0));
+    pdf = 0;
+    T dWo = dot(wo, s.geoN), dWi = dot(wi, s.geoN);
+    if (dWo * dWi <= T(0)) return;
+    V3<T> wiB = normalize(mulMv(c.baseB, wi));
+    if (wiB.y <= T(0)) return;
+    pdf = pdfCosHemi(wiB.y);
+    if ((flags & EV_PDF_ONLY) == 0)
+    {
+        T cosine = (flags & EV_LIGHT_PATH) ? std::fabs(dWi) : wiB.y;
+        w = sp(C<T>::INVPI * cosine);
+    }
 }
 
 // spotFalloff / punctualLightAngularFalloff (lightSampling.hlsl:228-246) towards dirFromLight
@@ -2159,9 +2280,17 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                 makeCtx(s, cur, prev, wo, h.front, sctx);
                 V3<T> nWS = normalize(xVecT<T>(I.w2o, s.geoN));
                 const bool nee = P.integrator == YG_INTEGRATOR_NEE;
-                // hasExplicitlySampledLights (rayHitDefault.hlsl:26-34): without NEE only the punctual lights
-                if ((nee ? !c.lights.empty() : c.nPunctual > 0) && !isDeltaDistr(sctx, s))
-                {
+                // connectToExplicitLight (rayHitDefault.hlsl:204-257) from a vertex; at a subsurface exit
+                // point (exitLobe) the light is weighed by the exit lobe instead of the BSDF
+                auto connectLight = [&](const Surf<T>& s, const SCtx<T>& sctx, V3<T> wo, V3<T> hitPos, V3<T> nWS,
+                                        const oracle_instance& I, bool exitLobe) {
+                    auto evalToLight = [&](V3<T> toLOS) {
+                        if (!exitLobe) return evalSurface(L, s, sctx, wo, toLOS, false, s4);
+                        EvalR<T> e;
+                        exitLobeEval(s, sctx, wo, toLOS, EV_NONE, e.w, e.pdf);
+                        e.trans = 0;
+                        return e;
+                    };
                     // connectToExplicitLight (rayHitDefault.hlsl:204-257)
                     T rl[4];
                     for (int k = 0; k < 4; ++k) rl[k] = T(rs.r1());
@@ -2212,7 +2341,7 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                         if (!allEq(emis, T(0)) && T(pick) > T(0))
                         {
                             V3<T> toLOS = normalize(xVec<T>(I.w2o, toL));
-                            EvalR<T> ev = evalSurface(L, s, sctx, wo, toLOS, false, s4);
+                            EvalR<T> ev = evalToLight(toLOS);
                             S4<T> wl = ev.w;
                             if ((ev.trans & 4) && !(ps.flags & F_SEC))
                             {
@@ -2283,7 +2412,7 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                     if (!allEq(emis, T(0)) && lpdf > T(0))
                     {
                         V3<T> toLOS = normalize(xVec<T>(I.w2o, toLWS));
-                        EvalR<T> ev = evalSurface(L, s, sctx, wo, toLOS, false, s4);
+                        EvalR<T> ev = evalToLight(toLOS);
                         S4<T> wl = ev.w;
                         if ((ev.trans & 4) && !(ps.flags & F_SEC))
                         {
@@ -2306,7 +2435,10 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                         }
                     }
                     }
-                }
+                                };
+                // hasExplicitlySampledLights (rayHitDefault.hlsl:26-34): without NEE only the punctual lights
+                if ((nee ? !c.lights.empty() : c.nPunctual > 0) && !isDeltaDistr(sctx, s))
+                    connectLight(s, sctx, wo, hitPos, nWS, I, false);
                 // sampleScatteringEvent (scatteringSample.hlsl:30-65)
                 T r = tmax(T(0), rB[0] + T(0.00001f));
                 int layer;
@@ -2315,51 +2447,174 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                     if (r < sctx.probs[layer] && sctx.probs[layer] > T(0)) break;
                     r -= sctx.probs[layer];
                 }
-                V3<T> wi = v3(T(0), T(0), T(0));
-                bool diff = false, delta = false;
-                if (layer < 5) wi = sampleLayer<T, false>(&L, s, sctx, layer, rB[1], rB[2], rB[3], s4.hero, diff, delta);
-                EvalR<T> ev;
-                ev.w = sp(T(0));
-                ev.pdf = 0;
-                ev.trans = 0;
-                if (!isZero(wi))
+                if (layer == 5)
                 {
-                    ev = evalSurface(L, s, sctx, wo, wi, delta, s4);
-                    if (diff) ps.flags |= F_REG;
-                }
-                ps.pdfRay = ev.pdf;
-                if (delta) ps.flags |= F_DELTA;
-                else ps.flags &= ~F_DELTA;
-                if (ev.pdf > T(0))
-                {
-                    if (ev.trans)
+                    // the subsurface event (scatteringSample.hlsl:45-54; rayHitDefault.hlsl:261-320, 349-355);
+                    // the entry vertex's light connection was added above
+                    alive = false;
+                    const V3<T> ep = hitPos;
+                    const V3<T> en = dot(-ps.d, nWS) < T(0) ? -nWS : nWS; // orientToSameSide
+                    // sampleSubsurfaceExit (subsurface.hlsl:212-337)
+                    T u = rB[1];
+                    uint32_t axisIndex;
+                    if (u < T(0.5f)) { axisIndex = 0; u *= T(2); }
+                    else if (u < T(0.75f)) { axisIndex = 1; u = (u - T(0.5f)) * T(4); }
+                    else { axisIndex = 2; u = (u - T(0.75f)) * T(4); }
+                    uint32_t lane = std::min((uint32_t)(u * T(4)), 3u);
+                    T uSel = saturate(u * T(4) - T(lane));
+                    const T dLane = burleyD(s.sssRadius[lane], s.albedo[lane]);
+                    const T rMax = burleyRMax(dLane);
+                    const T r = burleySampleRadius(rB[2], dLane);
+                    bool ok = r < rMax;
+                    V3<T> exitPos, exitN;
+                    S4<T> exitW;
+                    T pdfPos = 0;
+                    TriHit<float> sel;
+                    if (ok)
                     {
-                        if (ev.trans & 4)
+                        V3<T> axis, pu, pv;
+                        probeFrame(en, axisIndex, axis, pu, pv);
+                        T sinPhi, cosPhi;
+                        Mth<T>::sincos(T(2) * C<T>::PI * rB[3], sinPhi, cosPhi);
+                        const T maxCoord = tmax(tmax(std::fabs(ep.x), std::fabs(ep.y)), std::fabs(ep.z));
+                        const T halfLength = tmax(Mth<T>::sqrt(rMax * rMax - r * r), T(1e-3f) + T(1e-5f) * maxCoord);
+                        const V3<T> po = ep + (pu * cosPhi + pv * sinPhi) * r - axis * halfLength;
+                        T wSum = 0, selW = 0;
+                        S4<T> selRd = sp(T(0));
+                        float tMin = 0.f;
+                        for (int k = 0; k < 8; ++k)
                         {
-                            if (!(ps.flags & F_SEC))
+                            TriHit<float> th;
+                            rays++;
+                            if (!trace(c, po, axis, tMin, (float)(T(2) * halfLength), th, h.inst)) break;
+                            const S4<T> rd = subsurfaceRd(s, len(po + axis * T(th.t) - ep));
+                            const T w = rd[0] + rd[1] + rd[2] + rd[3];
+                            wSum += w;
+                            const T keep = wSum > T(0) ? w / wSum : T(0);
+                            if (keep >= T(1) || uSel < keep)
                             {
-                                ev.w[0] *= T(4);
-                                ev.w[1] = ev.w[2] = ev.w[3] = 0;
+                                uSel = keep >= T(1) ? uSel : uSel / keep;
+                                selW = w;
+                                selRd = rd;
+                                sel = th;
                             }
-                            ps.flags |= F_SEC;
+                            else
+                            {
+                                uSel = (uSel - keep) / (T(1) - keep);
+                            }
+                            tMin = th.t + 5e-4f;
                         }
-                        bool en = (ev.trans & 1) != 0, ex = (ev.trans & 2) != 0;
-                        if (en != ex)
+                        ok = selW > T(0);
+                        if (ok)
                         {
-                            if (ex) exitVol(ps, I.material);
-                            else enterVol(ps, s.ior, s.absorption, I.material);
+                            V3<T> q[3];
+                            uint32_t qi[3];
+                            triPositions(c, I, sel.prim, q, qi);
+                            const V3<T> nOS = normalize(cross(q[1] - q[0], q[2] - q[0]));
+                            const V3<T> nW = normalize(xVecT<T>(I.w2o, nOS));
+                            const V3<T> frontN = ((dot(nW, axis) < T(0)) == sel.front) ? nW : -nW;
+                            exitPos = po + axis * T(sel.t);
+                            exitN = h.front ? frontN : -frontN;
+                            pdfPos = pdfSssExit(s, ep, en, exitPos, exitN);
+                            ok = pdfPos > T(0);
+                            if (ok) exitW = selRd / (pdfPos * (selW / wSum));
                         }
                     }
-                    ev.w = ev.w / ev.pdf;
+                    if (!ok)
+                    {
+                        // no exit point: the event has no direction, the path ends
+                        ps.pdfRay = 0;
+                        ps.flags &= ~F_DELTA;
+                        ps.thr = ps.thr * sp(T(0));
+                    }
+                    else
+                    {
+                        // evaluateSubsurfaceEntry, then continueFromSubsurfaceExit
+                        S4<T> entryW = exitW * (sssEntryFactor(L, s, sctx, s4.hero) * pdfPos);
+                        T pdfFwd = sctx.probs[5] * pdfPos;
+                        ps.thr = ps.thr * entryW * safeDiv(T(1), pdfFwd);
+                        V3<T> xrd = normalize(xVec<T>(I.w2o, -exitN));
+                        Surf<T> xs;
+                        fillSurf(c, s4, h.inst, sel.prim, T(sel.b1), T(sel.b2), xrd, true,
+                                 P.regularize_enable && (ps.flags & F_REG), xs);
+                        V3<T> xwo = -xrd;
+                        SCtx<T> xc;
+                        makeCtx(xs, cur, prev, xwo, h.front, xc);
+                        if (nee ? !c.lights.empty() : c.nPunctual > 0) connectLight(xs, xc, xwo, exitPos, exitN, I, true);
+                        T rX[4];
+                        for (int k = 0; k < 4; ++k) rX[k] = T(rs.r1());
+                        V3<T> xwi = exitLobeSample(xs, xc, xwo, rX[2], rX[3]);
+                        S4<T> xw = sp(T(0));
+                        T xpdf = 0;
+                        bool dirSet = false;
+                        if (!isZero(xwi))
+                        {
+                            exitLobeEval(xs, xc, xwo, xwi, EV_NONE, xw, xpdf);
+                            if (xpdf > T(0))
+                            {
+                                xw = xw / xpdf;
+                                V3<T> dW = normalize(xVec<T>(I.o2w, xwi));
+                                ps.o = spawn(exitPos, exitN, dW);
+                                ps.d = dW;
+                                dirSet = true;
+                            }
+                            else xw = sp(T(0));
+                        }
+                        ps.flags |= F_REG;
+                        ps.flags &= ~F_DELTA;
+                        ps.pdfRay = xpdf;
+                        ps.thr = ps.thr * xw;
+                        alive = dirSet && xpdf != T(0);
+                    }
                 }
-                ps.thr = ps.thr * ev.w;
-                if (isZero(wi) || ps.pdfRay == T(0)) alive = false;
                 else
                 {
-                    V3<T> nW = normalize(xVec<T>(I.o2w, s.geoN));
-                    V3<T> dW = normalize(xVec<T>(I.o2w, wi));
-                    ps.o = spawn(hitPos, nW, dW);
-                    ps.d = dW;
+                    V3<T> wi = v3(T(0), T(0), T(0));
+                    bool diff = false, delta = false;
+                    if (layer < 5) wi = sampleLayer<T, false>(&L, s, sctx, layer, rB[1], rB[2], rB[3], s4.hero, diff, delta);
+                    EvalR<T> ev;
+                    ev.w = sp(T(0));
+                    ev.pdf = 0;
+                    ev.trans = 0;
+                    if (!isZero(wi))
+                    {
+                        ev = evalSurface(L, s, sctx, wo, wi, delta, s4);
+                        if (diff) ps.flags |= F_REG;
+                    }
+                    ps.pdfRay = ev.pdf;
+                    if (delta) ps.flags |= F_DELTA;
+                    else ps.flags &= ~F_DELTA;
+                    if (ev.pdf > T(0))
+                    {
+                        if (ev.trans)
+                        {
+                            if (ev.trans & 4)
+                            {
+                                if (!(ps.flags & F_SEC))
+                                {
+                                    ev.w[0] *= T(4);
+                                    ev.w[1] = ev.w[2] = ev.w[3] = 0;
+                                }
+                                ps.flags |= F_SEC;
+                            }
+                            bool en = (ev.trans & 1) != 0, ex = (ev.trans & 2) != 0;
+                            if (en != ex)
+                            {
+                                if (ex) exitVol(ps, I.material);
+                                else enterVol(ps, s.ior, s.absorption, I.material);
+                            }
+                        }
+                        ev.w = ev.w / ev.pdf;
+                    }
+                    ps.thr = ps.thr * ev.w;
+                    if (isZero(wi) || ps.pdfRay == T(0)) alive = false;
+                    else
+                    {
+                        V3<T> nW = normalize(xVec<T>(I.o2w, s.geoN));
+                        V3<T> dW = normalize(xVec<T>(I.o2w, wi));
+                        ps.o = spawn(hitPos, nW, dW);
+                        ps.d = dW;
+                    }
                 }
             }
         }
@@ -2398,7 +2653,8 @@ inline bool needsRgbTable(const oracle_scene* sc, const yg_render_params* P)
         const yg_material& m = sc->materials[i];
         if ((m.albedo_spectrum < 0 && nonGrey(m.albedo)) || (m.specular_spectrum < 0 && nonGrey(m.specular)) ||
             (m.emission_spectrum < 0 && nonGrey(m.emissive)) || (nonZero(m.absorption) && nonGrey(m.absorption)) ||
-            (m.sheen_amount > 0.0f && nonGrey(m.sheen_tint)) || m.albedo_texture || m.emissive_texture)
+            (m.sheen_amount > 0.0f && nonGrey(m.sheen_tint)) || (m.subsurface_amount > 0.0f && nonGrey(m.subsurface_radius)) ||
+            m.albedo_texture || m.emissive_texture)
             return true;
     }
     for (uint32_t i = 0; i < sc->n_punctual; ++i)

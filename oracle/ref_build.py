@@ -15,8 +15,9 @@ copies and the binary into oracle/_ref/ only (git-ignored; never committed):
     a scalar to a struct member by member);
   * include directives are resolved case-insensitively (the shaders were written on Windows).
 
-The struct SurfaceDefinition (raytracing/hitShadersCommon.hlsl) is extracted on its own, so
-the ray-tracing resources that file pulls in are not needed.
+The struct SurfaceDefinition (raytracing/hitShadersCommon.hlsl) and the subsurface functions of
+raytracing/subsurface.hlsl other than its probe-ray sampler are extracted on their own, so the
+ray-tracing resources those files pull in are not needed.
 
   python oracle/ref_build.py            # build (skips quietly when the shaders are absent)
   python oracle/ref_build.py --run      # build and run the comparison, print its JSON
@@ -109,6 +110,27 @@ def extract_struct(text, name):
     return text[m.start():j + 1]
 
 
+def extract_function(text, name):
+    """The definition of function `name` (return type through the closing brace)."""
+    m = re.search(r"^[ \t]*[A-Za-z_][\w<>]*[ \t]+%s[ \t]*\(" % re.escape(name), text, re.M)
+    if not m:
+        raise RuntimeError("function %s not found" % name)
+    i = text.index("{", m.end())
+    depth, j = 1, i + 1
+    while depth:
+        depth += {"{": 1, "}": -1}.get(text[j], 0)
+        j += 1
+    return text[m.start():j]
+
+
+# the subsurface functions compared (subsurface.hlsl); its probe-ray sampler needs the ray-query
+# pipeline and stays out
+SUBSURFACE_FUNCTIONS = ["getSubsurfaceLayerWeight", "getEnergyLeftForBaseLayer", "getSubsurfaceEntryFactor", "burleyScale",
+                        "burleyD", "burleyRMax", "burleyProfileArea", "burleySampleRadius", "evaluateSubsurfaceRd",
+                        "getSubsurfaceProbeFrame", "getSubsurfaceProbeAxisProbability", "pdfSubsurfaceExit",
+                        "sampleSubsurfaceExitLobe", "evaluateSubsurfaceExitLobe"]
+
+
 def convert_tree():
     for dirpath, _, files in os.walk(SHADERS):
         for f in files:
@@ -126,6 +148,13 @@ def convert_tree():
         piece = extract_struct(fh.read(), "SurfaceDefinition")
     with open(os.path.join(HLSL_OUT, "SurfaceDefinition.inc"), "w") as fh:
         fh.write(transform(piece, hsc) + "\n")
+    sss = os.path.join(SHADERS, "raytracing", "subsurface.hlsl")
+    with open(sss, encoding="utf-8", errors="replace") as fh:
+        text = fh.read()
+    defines = "\n".join(ln for ln in text.split("\n") if ln.startswith("#define SUBSURFACE_"))
+    parts = [defines] + [extract_function(text, f) for f in SUBSURFACE_FUNCTIONS]
+    with open(os.path.join(HLSL_OUT, "subsurface_math.inc"), "w") as fh:
+        fh.write(transform("\n\n".join(parts), sss) + "\n")
 
 
 def build():

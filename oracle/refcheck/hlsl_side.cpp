@@ -34,6 +34,7 @@ static ByteAddressBuffer g_randomSamples;
 #include "../_ref/hlsl/raytracing/spectralDistribution.hlsl"
 #include "../_ref/hlsl/SurfaceDefinition.inc"
 #include "../_ref/hlsl/raytracing/materialSample.hlsl"
+#include "../_ref/hlsl/subsurface_math.inc"
 #undef interface
 } // namespace REFCHECK_NS
 
@@ -68,7 +69,7 @@ SurfaceDefinition surfaceOf(const Surface& s)
     d.absorption = spec(s.absorption);
     d.emissive = spec(s.emissive);
     d.sheenColor = spec(s.sheenColor);
-    d.subsurfaceRadius.set(1.0f);
+    d.subsurfaceRadius = spec(s.sssRadius);
     d.coatingLayerNormal = v3(s.coatN);
     d.baseLayerNormal = v3(s.baseN);
     d.geometryNormal = v3(s.geoN);
@@ -301,5 +302,39 @@ void FN(sample_layer)(const Surface& s, float hero, float cur, float prev, const
     put3(getSampleDirectionOSForLayer(c, (uint)layer, sel, float2(r0, r1), d, dl), out);
     *diffuse = d ? 1 : 0;
     *delta = dl ? 1 : 0;
+}
+// the Burley profile: 0 burleyProfileArea(r = a, d = b), 1 burleySampleRadius(u = a, d = b),
+// 2 burleyD(radius = a, albedo = b)
+float FN(sss)(int fn, float a, float b)
+{
+    switch (fn)
+    {
+    case 0: return burleyProfileArea(a, b);
+    case 1: return burleySampleRadius(a, b);
+    case 2: return burleyD(a, b);
+    }
+    return 0.0f;
+}
+float FN(sss_pdf)(const Surface& s, const float fromP[3], const float fromN[3], const float toP[3], const float toN[3])
+{
+    return pdfSubsurfaceExit(surfaceOf(s), v3(fromP), v3(fromN), v3(toP), v3(toN));
+}
+float FN(sss_entry)(const Surface& s, float hero, float cur, float prev, const float wo[3], int front)
+{
+    g_checkHeroLambda = hero;
+    SurfaceSamplingContext c = makeSurfaceSamplingContext(surfaceOf(s), cur, prev, v3(wo), front != 0);
+    return getSubsurfaceEntryFactor(c.surfaceDef, c.precalculatedSurfaceData);
+}
+// out: sampled direction (3), weight (4) and pdf of the exit lobe at wi
+void FN(sss_exit_lobe)(const Surface& s, float cur, float prev, const float wo[3], int front, float r0, float r1,
+                       const float wi[3], uint32_t flags, float out[8])
+{
+    SurfaceSamplingContext c = makeSurfaceSamplingContext(surfaceOf(s), cur, prev, v3(wo), front != 0);
+    put3(sampleSubsurfaceExitLobe(c.surfaceDef, c.precalculatedSurfaceData, v3(wo), float2(r0, r1)), out);
+    SpectralSamples w;
+    float pdf = 0.0f;
+    evaluateSubsurfaceExitLobe(c.surfaceDef, c.precalculatedSurfaceData, v3(wo), v3(wi), flags, w, pdf);
+    for (int k = 0; k < 4; ++k) out[3 + k] = w.samples[k];
+    out[7] = pdf;
 }
 } // namespace refcheck

@@ -154,7 +154,8 @@ Surface randomSurface(Rng& r)
     s.sheenRough = r.rough();
     s.sheenAmount = pick(0.6f, 0.1f);
     s.focus = 0.0f;
-    s.sssAmount = 0.0f; // subsurface is outside the compared integrators
+    s.sssAmount = pick(0.6f, 0.2f);
+    for (int k = 0; k < 4; ++k) s.sssRadius[k] = r.range(0.002f, 0.3f);
     s.diffOcc = r.uni() < 0.7f ? 1.0f : r.range(0.3f, 1.0f);
     s.specOcc = r.uni() < 0.7f ? 1.0f : r.range(0.3f, 1.0f);
     s.flags = (r.uni() < 0.5f ? 1u : 0u) | (r.uni() < 0.3f ? 2u : 0u);
@@ -383,6 +384,34 @@ int main(int argc, char** argv)
         }
         compare1(check("evaluateSurface (pdf)", 1e-4), ev1[4], ev2[4]);
         compare1(check("evaluateSurface (transmission type)", 0, 0.999, true), ev1[5], ev2[5]);
+        // subsurface (subsurface.hlsl): the Burley profile, radius sampling, the exit density, the
+        // entry factor and the exit lobe
+        {
+            float dd = r.range(1e-4f, 0.2f), rr = r.range(0.f, 2.f) * dd, uu = r.uni();
+            compare1(check("burleyProfileArea", 1e-4), ref_sss(0, rr, dd), orc_sss(0, rr, dd));
+            compare1(check("burleySampleRadius", 1e-4), ref_sss(1, uu, dd), orc_sss(1, uu, dd));
+            float rad = r.range(0.f, 0.3f), alb = r.uni();
+            compare1(check("burleyD", 1e-5), ref_sss(2, rad, alb), orc_sss(2, rad, alb));
+            float fp[3], fnrm[3], tp[3], tn[3], off[3];
+            r.dir(fnrm);
+            r.dir(tn);
+            r.dir(off);
+            float dist = r.range(0.f, 0.5f);
+            for (int k = 0; k < 3; ++k)
+            {
+                fp[k] = r.range(-2.f, 2.f);
+                tp[k] = fp[k] + dist * off[k];
+            }
+            compare1(check("pdfSubsurfaceExit", 1e-4), ref_sss_pdf(S, fp, fnrm, tp, tn), orc_sss_pdf(S, fp, fnrm, tp, tn));
+            compare1(check("getSubsurfaceEntryFactor", 1e-4), ref_sss_entry(S, shero, cur, prev, swo, front),
+                     orc_sss_entry(S, shero, cur, prev, swo, front));
+            float xo1[8], xo2[8], xr0 = r.uni(), xr1 = r.uni();
+            uint32_t xfl = r.uni() < 0.5f ? 1u : 4u;
+            ref_sss_exit_lobe(S, cur, prev, swo, front, xr0, xr1, swi, xfl, xo1);
+            orc_sss_exit_lobe(S, cur, prev, swo, front, xr0, xr1, swi, xfl, xo2);
+            compare(check("sampleSubsurfaceExitLobe", 1e-4), xo1, xo2, 3);
+            compare(check("evaluateSubsurfaceExitLobe", 1e-4), xo1 + 3, xo2 + 3, 5);
+        }
         // the bidirectional integrator's model (RECIPROCAL_MULTISCATTER): layer sampling with the
         // multiple-scattering lobe, and evaluation on camera and light paths
         refK_sample_layer(S, shero, cur, prev, swo, front, layer, sel, r0, r1, sd1, &df1, &dl1);

@@ -69,6 +69,7 @@ Surf<float> surfOf(const Surface& x)
     s.diffOcc = floatFromHalf(halfFromFloat(x.diffOcc));
     s.specOcc = floatFromHalf(halfFromFloat(x.specOcc));
     s.flags = x.flags;
+    s.sssRadius = s4(x.sssRadius);
     return s;
 }
 } // namespace
@@ -259,5 +260,39 @@ void orcK_sample_layer(const Surface& s, float hero, float cur, float prev, cons
                        float r0, float r1, float out[3], int* diffuse, int* delta)
 {
     sampleLayerOf<true>(s, hero, cur, prev, wo, front, layer, sel, r0, r1, out, diffuse, delta);
+}
+float orc_sss(int fn, float a, float b)
+{
+    switch (fn)
+    {
+    case 0: return burleyProfileArea(a, b);
+    case 1: return burleySampleRadius(a, b);
+    case 2: return burleyD(a, b);
+    }
+    return 0.0f;
+}
+float orc_sss_pdf(const Surface& s, const float fromP[3], const float fromN[3], const float toP[3], const float toN[3])
+{
+    return pdfSssExit(surfOf(s), v(fromP), v(fromN), v(toP), v(toN));
+}
+float orc_sss_entry(const Surface& s, float hero, float cur, float prev, const float wo[3], int front)
+{
+    Surf<float> sf = surfOf(s);
+    SCtx<float> c;
+    makeCtx(sf, cur, prev, v(wo), front != 0, c);
+    return sssEntryFactor(g_luts, sf, c, hero);
+}
+void orc_sss_exit_lobe(const Surface& s, float cur, float prev, const float wo[3], int front, float r0, float r1,
+                       const float wi[3], uint32_t flags, float out[8])
+{
+    Surf<float> sf = surfOf(s);
+    SCtx<float> c;
+    makeCtx(sf, cur, prev, v(wo), front != 0, c);
+    put(exitLobeSample(sf, c, v(wo), r0, r1), out);
+    S4<float> w;
+    float pdf = 0.0f;
+    exitLobeEval(sf, c, v(wo), v(wi), flags, w, pdf);
+    for (int k = 0; k < 4; ++k) out[3 + k] = w[k];
+    out[7] = pdf;
 }
 } // namespace refcheck

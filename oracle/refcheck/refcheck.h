@@ -26,6 +26,7 @@ struct Surface
     float aniso, anisoRot, thinFilm, sheenRough, sheenAmount, focus, sssAmount;
     float diffOcc, specOcc;
     uint32_t flags;
+    float sssRadius[4]; // subsurfaceRadius per lane
 };
 struct Eval
 {
@@ -68,7 +69,13 @@ struct Eval
     Eval P##eval_surface(const Surface& s, float hero, float cur, float prev, const float wo[3], int front,      \
                          const float wi[3], uint32_t flags);                                                     \
     void P##sample_layer(const Surface& s, float hero, float cur, float prev, const float wo[3], int front,      \
-                         int layer, float sel, float r0, float r1, float out[3], int* diffuse, int* delta);
+                         int layer, float sel, float r0, float r1, float out[3], int* diffuse, int* delta);        \
+    float P##sss(int fn, float a, float b);                                                                      \
+    float P##sss_pdf(const Surface& s, const float fromP[3], const float fromN[3], const float toP[3],          \
+                     const float toN[3]);                                                                        \
+    float P##sss_entry(const Surface& s, float hero, float cur, float prev, const float wo[3], int front);      \
+    void P##sss_exit_lobe(const Surface& s, float cur, float prev, const float wo[3], int front, float r0,      \
+                          float r1, const float wi[3], uint32_t flags, float out[8]);
 
 REFCHECK_API(ref_)
 REFCHECK_API(refK_)

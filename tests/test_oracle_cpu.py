@@ -98,3 +98,23 @@ def test_strided_subsample_renders_the_same_pixels_as_the_full_crop(box):
     sub = h.render_strided(p, 4, precision=32, film=True)["film"]
     assert sub.shape == (5, 6, 3)
     assert np.array_equal(sub, full[::4, ::4])
+
+
+def test_subsurface_oracle_is_deterministic_and_estimators_agree():
+    """The subsurface layer in the oracle: thread-independent samples, finite values, FP32 and
+    FP64 per-sample agreement, and the unidirectional and NEE estimators agree on the image."""
+    import pyoracle
+    sc = configs.subsurface_box_scene(0)
+    h = pyoracle.OracleSceneHandle(sc, pyoracle.own_luts())
+    kw = dict(max_depth=8, lambda_range=(380, 780))
+    p = pyoracle.render_params("nee", 24, 24, spp=2, **kw)
+    h.ensure_rgb_table(p)
+    a = h.render(p, precision=32, threads=1)["records"]
+    b = h.render(p, precision=32, threads=6)["records"]
+    assert np.array_equal(a, b) and np.all(np.isfinite(a))
+    d = h.render(p, precision=64)["records"]
+    rel = np.abs(a[..., 1:5] - d[..., 1:5]) / np.maximum(np.abs(d[..., 1:5]), 1e-6)
+    assert np.mean(rel < 1e-3) > 0.99
+    fu = h.render(pyoracle.render_params("uni", 16, 16, spp=256, **kw), precision=32, records=False, film=True)["film"]
+    fn = h.render(pyoracle.render_params("nee", 16, 16, spp=256, **kw), precision=32, records=False, film=True)["film"]
+    assert abs(fu[..., 1].mean() - fn[..., 1].mean()) / fn[..., 1].mean() < 0.08

@@ -2,7 +2,8 @@
 
 oracle/ref_build.py compiles the reference's HLSL shader math (random.hlsl,
 randomSampler.hlsl, spectralDistribution.hlsl, ggx.hlsl, fresnel.hlsl, miscBrdf.hlsl,
-bsdfSample.hlsl, multiScatter.hlsl, materialLayers.hlsl, materialSample.hlsl ...) as C++
+bsdfSample.hlsl, multiScatter.hlsl, materialLayers.hlsl, materialSample.hlsl and the
+subsurface functions of subsurface.hlsl) as C++
 through oracle/hlsl_shim.h into oracle/_ref/refcheck, once as the unidirectional
 integrators compile it and once with RECIPROCAL_MULTISCATTER as the bidirectional one does,
 and runs it beside the oracle's restatement on the same seeded inputs. The sampler is
@@ -37,6 +38,8 @@ EXPECTED = [
     "getDirectionalAlbedoTranslucent", "getAverageAlbedoTranslucent",
     "calculateNormalizedMaterialLayerSamplingProbabilities", "getSampleDirectionOSForLayer",
     "evaluateSurface (weight)", "evaluateSurface (pdf)", "evaluateSurface (transmission type)",
+    "burleyProfileArea", "burleySampleRadius", "burleyD", "pdfSubsurfaceExit", "getSubsurfaceEntryFactor",
+    "sampleSubsurfaceExitLobe", "evaluateSubsurfaceExitLobe",
     "getSampleDirectionOSForLayer (RECIPROCAL_MULTISCATTER)", "evaluateSurface (RECIPROCAL_MULTISCATTER, weight)",
     "evaluateSurface (RECIPROCAL_MULTISCATTER, pdf)", "evaluateSurface (RECIPROCAL_MULTISCATTER, transmission type)",
 ]

@@ -206,6 +206,31 @@ def layered_box_scene(seed=0, light_intensity=12.0, aspect=1.0):
     return sc
 
 
+def subsurface_box_scene(seed=0, light_intensity=12.0, aspect=1.0):
+    """``box_scene`` whose two blocks scatter below their surfaces (the Christensen-Burley
+    subsurface layer of subsurface.hlsl): one a pale, fully subsurface block with an RGB mean
+    free path of (1.0, 0.5, 0.25) x 0.06 under a glossy specular layer, the other a half
+    subsurface, half diffuse block with a clear coat and sheen and a grey radius of 0.02, plus
+    three subsurface icospheres (subdivision 3) on the floor. Closed meshes, so every probe ray
+    finds the surface it starts in."""
+    sc = box_scene(seed, light_intensity, aspect)
+    sc.name = "subsurface_box(seed=%d)" % seed
+    m = sc.materials
+    m[5].update(albedo_spectrum=-1, albedo=(0.85, 0.55, 0.4), subsurface_amount=1.0, subsurface_radius=(1.0, 0.5, 0.25),
+                subsurface_radius_scale=0.06, specular_amount=0.5, roughness=0.35, dielectric_ior=1.4)
+    m[6].update(subsurface_amount=0.5, subsurface_radius=(1.0, 1.0, 1.0), subsurface_radius_scale=0.02,
+                clear_coat_amount=0.6, clear_coat_roughness=0.2, sheen_amount=0.4, sheen_roughness=0.5)
+    rng = np.random.Generator(np.random.PCG64(2000 + seed))
+    ball = sc.add_mesh(*icosphere(3))
+    for k in range(3):
+        mat = sc.add_material(**diffuse(sc.add_spectrum(control_point_spectrum(rng))))
+        sc.materials[mat].update(subsurface_amount=1.0, subsurface_radius=tuple(rng.uniform(0.3, 1.0, 3)),
+                                 subsurface_radius_scale=0.04, specular_amount=0.3, roughness=0.5)
+        r = 0.07
+        sc.add_instance(ball, mat, affine(translation=(0.2 + 0.3 * k, r, 0.8), scale=(r, r, r)))
+    return sc
+
+
 def textured_box_scene(seed=0, aspect=1.0):
     """``box_scene`` with textures in every material slot the reference has
     (materialsCommon.hlsl:354-397): an 8 x 8 checker albedo (sRGB, uv scale 3) on the floor,

@@ -209,6 +209,7 @@ bool sceneNeedsRgbLut(const yg_context* c, float envScale)
         if (m.emission_spectrum < 0 && !isGreyOrZero(m.emissive)) return true;
         if (!isGreyOrZero(m.absorption)) return true;
         if (m.sheen_amount > 0.0f && !isGreyOrZero(m.sheen_tint)) return true;
+        if (m.subsurface_amount > 0.0f && !isGreyOrZero(m.subsurface_radius)) return true;
     }
     for (const yg_punctual_light& L : c->punctual)
         if (!isGreyOrZero(L.intensity)) return true;
@@ -285,6 +286,13 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.lambdaMax = lmaxf;
     S.cieYSumInv = ctx->cieYSumInv;
     S.d65SumInv = ctx->d65SumInv;
+}
+
+bool sceneHasSubsurface(const yg_context* c)
+{
+    for (const yg_material& m : c->materials)
+        if (m.subsurface_amount > 0.0f) return true;
+    return false;
 }
 
 int checkMaterialTextures(const yg_context* c, const char* what)
@@ -541,11 +549,6 @@ YG_API int yg_upload_materials(yg_context* ctx, const yg_material* mats, uint32_
 {
     if (!ctx || (!mats && count)) return fail(YG_ERR_INVALID_ARGUMENT, "materials: null argument");
     std::lock_guard<std::mutex> g(ctx->lock);
-    for (uint32_t i = 0; i < count; ++i)
-    {
-        if (mats[i].subsurface_amount > 0.0f)
-            return fail(YG_ERR_INVALID_ARGUMENT, "materials: subsurface scattering is not supported by this build");
-    }
     ctx->materials.assign(mats, mats + count);
     ctx->gpuMaterials.resize(count);
     for (uint32_t i = 0; i < count; ++i) ctx->gpuMaterials[i] = packMaterial(mats[i]);
@@ -1069,6 +1072,9 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
 
     const uint64_t npix = (uint64_t)cw * ch;
     const bool bdpt = p->integrator == YG_INTEGRATOR_BDPT;
+    if (bdpt && sceneHasSubsurface(ctx))
+        return fail(YG_ERR_INVALID_ARGUMENT, "render: the bidirectional integrator does not handle subsurface materials "
+                                             "(render them with the unidirectional or NEE integrator)");
     const uint64_t maxSamplesPerChunk = bdpt ? (1ull << 24) : (1ull << 26);
     uint32_t chunkSpp = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->spp_count, maxSamplesPerChunk / npix));
     if (bdpt && (p->flags & YG_FLAG_MEGAKERNEL)) return fail(YG_ERR_INVALID_ARGUMENT, "render: BDPT has no megakernel variant");

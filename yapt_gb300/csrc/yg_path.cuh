@@ -12,6 +12,7 @@
 #pragma once
 #include "yg_shading.cuh"
 #include <cuda_fp16.h>
+#include "yg_subsurface.cuh"
 #include "yg_trace.cuh"
 
 namespace yg
@@ -374,6 +375,9 @@ YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectr
     s.absorption = isZero3(rgb.absorption) ? splat4(0.0f) : fromRGBUnboundedNoIllum(S, sp, rgb.absorption);
     s.emissive = emissionSpectrum(S, sp, rgb.emissive, M.emissionSpectrum);
     s.sheenColor = s.sheenAmount > 0.0f ? fromRGB(S, sp, rgb.sheenColor) : splat4(0.0f);
+    // distances, not limited to [0, 1] (setFromRGBUnboundedNoIlluminant)
+    const float4 sr = M.subsurfaceRadius_amount;
+    s.subsurfaceRadius = s.subsurfaceAmount > 0.0f ? fromRGBUnboundedNoIllum(S, sp, mk3(sr.x, sr.y, sr.z)) : splat4(0.0f);
 }
 
 // sampleLight for mesh lights (lightSampling.hlsl:122-188), position part only
@@ -480,6 +484,95 @@ struct ShadowRequest
     bool valid;
 };
 
+// sampleSubsurfaceExit (subsurface.hlsl:212-337)
+YG_DEV bool sampleSubsurfaceExit(const SceneView& S, const Surface& s, const SurfacePoint& entry, float3 rnd,
+                                 SubsurfaceExit& out)
+{
+    float u = rnd.x;
+    uint32_t axisIndex;
+    if (u < 0.5f)
+    {
+        axisIndex = 0;
+        u *= 2.f;
+    }
+    else if (u < 0.75f)
+    {
+        axisIndex = 1;
+        u = (u - 0.5f) * 4.f;
+    }
+    else
+    {
+        axisIndex = 2;
+        u = (u - 0.75f) * 4.f;
+    }
+    uint32_t lane = min((uint32_t)(u * kSssLanes), (uint32_t)kSssLanes - 1u);
+    float uSelect = saturate(u * kSssLanes - (float)lane);
+    const float dLane = burleyD((&s.subsurfaceRadius.x)[lane], (&s.albedo.x)[lane]);
+    const float rMax = burleyRMax(dLane);
+    const float r = burleySampleRadius(rnd.y, dLane);
+    if (r >= rMax) return false;
+    float3 axis, pu, pv;
+    subsurfaceProbeFrame(entry.normal, axisIndex, axis, pu, pv);
+    float sinPhi, cosPhi;
+    ygm_sincosf(2.f * kPI * rnd.z, &sinPhi, &cosPhi);
+    // chord of the r_max sphere through the disk point, with a minimum length
+    const float3 ep = entry.pos;
+    const float maxCoord = fmaxf(fmaxf(fabsf(ep.x), fabsf(ep.y)), fabsf(ep.z));
+    const float halfLength = fmaxf(sqrtf(rMax * rMax - r * r), 1e-3f + 1e-5f * maxCoord);
+    const float3 probeOrigin = ep + (pu * cosPhi + pv * sinPhi) * r - axis * halfLength;
+    float weightSum = 0.f, selectedWeight = 0.f;
+    float4 selectedRd = splat4(0.0f);
+    Hit sel;
+    sel.t = 0.f;
+    sel.b1 = sel.b2 = 0.f;
+    sel.instance = entry.instance;
+    sel.prim = 0;
+    sel.front = false;
+    float tMin = 0.f;
+    for (int i = 0; i < kSssMaxProbeHits; ++i)
+    {
+        Hit h;
+        if (!traceInstanceClosest(S, probeOrigin, axis, tMin, 2.f * halfLength, entry.instance, h)) break;
+        // keep the k-th hit with probability w_k / (w_1 + ... + w_k)
+        const float4 rd = subsurfaceRd(s, length(probeOrigin + axis * h.t - ep));
+        const float w = rd.x + rd.y + rd.z + rd.w;
+        weightSum += w;
+        const float keep = weightSum > 0.f ? w / weightSum : 0.f;
+        if (keep >= 1.f || uSelect < keep)
+        {
+            uSelect = keep >= 1.f ? uSelect : uSelect / keep;
+            selectedWeight = w;
+            selectedRd = rd;
+            sel = h;
+        }
+        else
+        {
+            uSelect = (uSelect - keep) / (1.f - keep);
+        }
+        tMin = h.t + kRayMinT;
+    }
+    if (!(selectedWeight > 0.f)) return false;
+    const GpuInstance& I = S.instances[entry.instance];
+    TriGeom g = fetchTri(S, I, sel.prim);
+    const float3 nOS = normalize(cross(g.p2 - g.p1, g.p3 - g.p1));
+    const float3 nWS = normalize(xformVectorT(I.w2o, nOS));
+    // the front face faces against the probe
+    const float3 frontN = ((dot(nWS, axis) < 0.f) == sel.front) ? nWS : -nWS;
+    out.exit.pos = probeOrigin + axis * sel.t;
+    out.exit.instance = entry.instance;
+    out.exit.normal = entry.front ? frontN : -frontN;
+    out.exit.prim = sel.prim;
+    out.exit.b1 = sel.b1;
+    out.exit.b2 = sel.b2;
+    out.exit.front = entry.front;
+    const float pdf = pdfSubsurfaceExit(s, ep, entry.normal, out.exit.pos, out.exit.normal);
+    if (!(pdf > 0.f)) return false;
+    const float selection = selectedWeight / weightSum;
+    out.weight = selectedRd / (pdf * selection);
+    out.pdfPosition = pdf;
+    return true;
+}
+
 // The unidirectional integrators evaluate the layered BSDF at three places (the punctual and
 // the mesh light connection, and the sampled direction). One out-of-line copy keeps the
 // shading kernels' instruction footprint to a single copy of the layered evaluation, which
@@ -498,11 +591,26 @@ static __device__ __noinline__ Eval evaluateSurfaceOnce(const Luts& L, const Sur
 // can never hit (hasExplicitlySampledLights / sampleExplicitLight, rayHitDefault.hlsl:26-81).
 // A punctual light is visible when nothing is hit before it (checkUnoccluded) and its
 // connection has no MIS weight.
+// At a subsurface exit point (exitLobe) the light is weighed by the exit lobe instead of the BSDF
+// (connectToExplicitLight, rayHitDefault.hlsl:203-257).
 template <bool NEE>
 YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, const Surface& s, const SurfaceCtx& c,
                        float3 woOS, float3 posWS, float3 normalWS, const float4* w2o, const PathState& ps,
-                       RandomSampler& rs, ShadowRequest& sr)
+                       RandomSampler& rs, ShadowRequest& sr, bool exitLobe = false)
 {
+    auto evalToLight = [&](float3 toLightOS) {
+        Eval ev;
+        if (exitLobe)
+        {
+            evaluateSubsurfaceExitLobe(s, c, woOS, toLightOS, kEvalNone, ev.weight, ev.pdf);
+            ev.transmission = 0;
+        }
+        else
+        {
+            ev = evaluateSurfaceOnce(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
+        }
+        return ev;
+    };
     float4 r = rs.r4();
     uint32_t li;
     float pick;
@@ -540,7 +648,7 @@ YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, c
         float4 emission = emissionSpectrum(S, sp, I3, -1);
         if (allEqual4(emission, 0.0f) || !(pick > 0.0f)) return;
         float3 toLightOS = normalize(xformVector(w2o, toL));
-        Eval ev = evaluateSurfaceOnce(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
+        Eval ev = evalToLight(toLightOS);
         float4 w = ev.weight;
         if ((ev.transmission & kTransDispersed) != 0 && !(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(w);
         if (allEqual4(w, 0.0f)) return;
@@ -569,7 +677,7 @@ YG_DEV void prepareNee(const SceneView& S, const Luts& Lt, const Spectral& sp, c
     }
     if (allEqual4(emission, 0.0f) || !(pdf > 0.0f)) return;
     float3 toLightOS = normalize(xformVector(w2o, toLightWS));
-    Eval ev = evaluateSurfaceOnce(Lt, s, c, woOS, toLightOS, kEvalNone, sp);
+    Eval ev = evalToLight(toLightOS);
     float4 w = ev.weight;
     if ((ev.transmission & kTransDispersed) != 0 && !(ps.flags & kFlagSecondaryTerminated)) terminateSecondary(w);
     if (allEqual4(w, 0.0f)) return;
@@ -635,6 +743,89 @@ struct FirstHit
     float3 albedo, normal;
     float depth;
 };
+
+// The subsurface event at an entry vertex (scatteringSample.hlsl:45-54; rayHitDefault.hlsl:261-320,
+// 349-355): probe for the exit point, weigh the throughput by the entry, set the exit surface up
+// and continue from it with its light connection and the exit lobe. The entry vertex's light
+// connection (sr, prepared before the layer was chosen) is resolved here, so that it is added
+// before the exit's and each path keeps one deferred shadow ray. Returns whether the path
+// continues (before Russian roulette). Out of line: only paths on subsurface materials run it.
+template <bool NEE>
+static __device__ __noinline__ bool subsurfaceEvent(const SceneView& S, const LaunchParams& P, const Luts& Lt, const Spectral& sp, const Hit& hit,
+                            const GpuInstance& I, const Surface& s, const SurfaceCtx& c, float3 hitPos, float3 normalWS,
+                            float4 rB, PathState& ps, RandomSampler& rs, ShadowRequest& sr)
+{
+    if (sr.valid)
+    {
+        Hit h;
+        bool any = traceClosest<false>(S, sr.origin, sr.dir, kRayMinT, sr.tmax, h, nullptr);
+        if (shadowVisible(any, h, sr.instance, sr.prim)) ps.total = ps.total + sr.contrib;
+        sr.valid = false;
+    }
+    SurfacePoint entry;
+    entry.pos = hitPos;
+    entry.normal = dot(-ps.dir, normalWS) < 0.0f ? -normalWS : normalWS; // orientToSameSide
+    entry.instance = hit.instance;
+    entry.prim = hit.prim;
+    entry.b1 = hit.b1;
+    entry.b2 = hit.b2;
+    entry.front = hit.front;
+    SubsurfaceExit ex;
+    if (!sampleSubsurfaceExit(S, s, entry, mk3(rB.y, rB.z, rB.w), ex))
+    {
+        // no exit point: the event has no direction, the path ends
+        ps.pdfThisRay = 0.0f;
+        ps.flags &= ~kFlagDelta;
+        ps.throughput = ps.throughput * splat4(0.0f);
+        return false;
+    }
+    // evaluateSubsurfaceEntry: the edge's area density cancels against the weight's
+    float4 entryWeight = ex.weight * (subsurfaceEntryFactor(Lt, s, c, sp.hero) * ex.pdfPosition);
+    float pdfForward = c.probs[LAYER_SSS] * ex.pdfPosition;
+    ps.throughput = ps.throughput * entryWeight * safeDiv(1.0f, pdfForward);
+    // continueFromSubsurfaceExit: the exit surface seen from the outside
+    Hit xh;
+    xh.t = 0.0f;
+    xh.b1 = ex.exit.b1;
+    xh.b2 = ex.exit.b2;
+    xh.instance = ex.exit.instance;
+    xh.prim = ex.exit.prim;
+    xh.front = ex.exit.front;
+    const GpuInstance& XI = S.instances[ex.exit.instance];
+    HitSurface xs;
+    setupSurface(S, P, sp, xh, XI, -ex.exit.normal, ps, xs);
+    const float3 xwo = -xs.rayDirOS;
+    SurfaceCtx xc;
+    makeSurfaceCtx(xs.s, currentIOR(ps), previousIOR(ps), xwo, ex.exit.front, xc);
+    if (NEE ? S.nLights > 0 : S.nPunctual > 0)
+        prepareNee<NEE>(S, Lt, sp, xs.s, xc, xwo, ex.exit.pos, ex.exit.normal, XI.w2o, ps, rs, sr, true);
+    const float4 rX = rs.r4();
+    const float3 xwi = sampleSubsurfaceExitLobe(xs.s, xc, xwo, make_float2(rX.z, rX.w));
+    float4 w = splat4(0.0f);
+    float pdf = 0.0f;
+    bool dirSet = false;
+    if (!isZero3(xwi))
+    {
+        evaluateSubsurfaceExitLobe(xs.s, xc, xwo, xwi, kEvalNone, w, pdf);
+        if (pdf > 0.0f)
+        {
+            w = w / pdf;
+            float3 dW = normalize(xformVector(XI.o2w, xwi));
+            ps.origin = spawnRayOrigin(ex.exit.pos, ex.exit.normal, dW);
+            ps.dir = dW;
+            dirSet = true;
+        }
+        else
+        {
+            w = splat4(0.0f);
+        }
+    }
+    ps.flags |= kFlagRegularize;
+    ps.flags &= ~kFlagDelta;
+    ps.pdfThisRay = pdf;
+    ps.throughput = ps.throughput * w;
+    return dirSet && pdf != 0.0f;
+}
 
 // One traced segment: the miss shader, or the closest-hit shader at the vertex, then
 // Russian roulette. Returns whether the path continues; the NEE shadow request (if
@@ -707,9 +898,16 @@ YG_DEV bool shadeSegment(const SceneView& S, const LaunchParams& P, const Luts& 
                 prepareNee<NEE>(S, Lt, sp, s, c, wo, hitPos, normalWS, I.w2o, ps, rs, sr);
             // sampleScatteringEvent (scatteringSample.hlsl:30-65)
             int layer = selectMaterialLayer(rB.x, c.probs);
+            if (layer == LAYER_SSS)
+            {
+                alive = subsurfaceEvent<NEE>(S, P, Lt, sp, hit, I, s, c, hitPos, normalWS, rB, ps, rs, sr);
+                ps.pathLength += 1;
+                if (alive && russianRoulette(ps.throughput, rs.r1())) alive = false;
+                return alive;
+            }
             float3 wi = mk3(0.f, 0.f, 0.f);
             bool isDiffuse = false, isDelta = false;
-            if (layer != LAYER_SSS && layer < LAYER_COUNT)
+            if (layer < LAYER_COUNT)
                 wi = sampleLayerDirection(Lt, s, c, layer, rB.y, make_float2(rB.z, rB.w), sp.hero, isDiffuse, isDelta);
             Eval ev;
             ev.weight = splat4(0.0f);

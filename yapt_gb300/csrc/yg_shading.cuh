@@ -828,6 +828,7 @@ struct Surface
     float subsurfaceAmount;
     float occlusion; // unpackOcclusion of the ORM texture's occlusion, diffuse = specular (1 without one)
     uint32_t flags;
+    float4 subsurfaceRadius; // diffuse mean free path per lane (world units); set when subsurfaceAmount > 0
 };
 
 constexpr int LAYER_COAT = 0, LAYER_SHEEN = 1, LAYER_COND = 2, LAYER_DIEL = 3, LAYER_DIFF = 4, LAYER_SSS = 5;

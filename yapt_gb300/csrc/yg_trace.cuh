@@ -85,10 +85,14 @@ static __device__ __noinline__ bool cutoutPasses(const float4* __restrict__ r, f
     return t.w >= c.w;
 }
 
+// onlyInst: with FILTER, triangles of every other instance are ignored (the subsurface probe
+// rays, which look for the surface of the instance they started in)
+template <bool FILTER = false>
 __device__ __forceinline__ void intersectTri(const float4* __restrict__ tris, int ti, float3 o, float3 d, float tmin,
-                                             Hit& h, bool& found)
+                                             Hit& h, bool& found, uint32_t onlyInst = 0)
 {
     float4 a = __ldg(tris + 3 * ti);
+    if (FILTER && __float_as_uint(a.w) != onlyInst) return;
     float4 b = __ldg(tris + 3 * ti + 1);
     float4 c = __ldg(tris + 3 * ti + 2);
     float3 v0 = mk3(a.x, a.y, a.z), e1 = mk3(b.x, b.y, b.z), e2 = mk3(c.x, c.y, c.z);
@@ -151,6 +155,7 @@ struct TraceState
     bool found;
     uint32_t gBase, gImask, gHits, visits;
     int sp;
+    uint32_t onlyInst; // the instance a filtered traversal is restricted to
 };
 // the groups waiting below the current one (kept apart from TraceState so that the state's
 // scalars stay in registers), all in local memory
@@ -204,7 +209,7 @@ __device__ __forceinline__ void traceBegin(TraceState& t, const SceneView& S, fl
 
 // Opens the next node (testing its eight child boxes and the triangles of the leaf slots
 // that are hit); returns false once nothing is left to visit.
-template <bool COUNT, typename Stack>
+template <bool COUNT, typename Stack, bool FILTER = false>
 __device__ __forceinline__ bool traceStep(TraceState& t, Stack& st, TraversalCount* tc)
 {
     if (t.gHits == 0)
@@ -279,7 +284,7 @@ __device__ __forceinline__ bool traceStep(TraceState& t, Stack& st, TraversalCou
         {
             const uint32_t j = __ffs(triHits) - 1;
             triHits &= triHits - 1;
-            intersectTri(t.tris, (int)(triBase + j), t.o, t.d, t.tmin, t.h, t.found);
+            intersectTri<FILTER>(t.tris, (int)(triBase + j), t.o, t.d, t.tmin, t.h, t.found, t.onlyInst);
         }
     }
     if (hits)
@@ -303,6 +308,20 @@ __device__ __noinline__ bool traceClosest(const SceneView& S, float3 o, float3 d
     TraceStack st;
     traceBegin(t, S, o, d, tmin, tmax);
     while (traceStep<COUNT>(t, st, tc)) {}
+    h = t.h;
+    return t.found;
+}
+
+// The closest hit in (tmin, tmax) on the triangles of instance `inst` alone, as the reference's
+// subsurface probe query commits only that instance's hits (subsurface.hlsl:265-274).
+static __device__ __noinline__ bool traceInstanceClosest(const SceneView& S, float3 o, float3 d, float tmin, float tmax,
+                                                  uint32_t inst, Hit& h)
+{
+    TraceState t;
+    TraceStack st;
+    traceBegin(t, S, o, d, tmin, tmax);
+    t.onlyInst = inst;
+    while (traceStep<false, TraceStack, true>(t, st, nullptr)) {}
     h = t.h;
     return t.found;
 }
