@@ -45,7 +45,7 @@ BDPT_METRIC = "Msamples/s (BDPT with MIS, caustic box scene, 512x512, 32 spp, de
 # each rate; every request is also run alone to give its isolated latency.
 SERVE_WORKLOAD = dict(workload="serve_poisson_8_box_variants_10k_to_2M_triangles", resolutions=[128, 256, 512, 1024],
                       spp=[1, 4, 16, 64], integrators=["uni", "nee", "bdpt"], rates_per_s=[50, 100, 200, 400, 800],
-                      requests=24, max_depth=8, light_vertices=8, lambda_nm=[380, 780], seed=0)
+                      loads=[0.5, 0.8, 1.0], requests=200, max_depth=8, light_vertices=8, lambda_nm=[380, 780], seed=0)
 SERVE_METRIC = "serve: Msamples/s at full load with p50/p99 latency (Poisson arrivals, mixed sizes/spp/integrators)"
 # --workload denoise: the learned denoiser. Training pairs are rendered by the tracer from seeded
 # box scenes (256x256, 4 spp + first-hit features -> a high-spp target), the U-Net is trained
@@ -512,7 +512,10 @@ def run_serve(args, world, rank, local):
     from yapt_gb300.runtime import Context, Server
     if rank != 0:
         return
-    W = SERVE_WORKLOAD
+    W = dict(SERVE_WORKLOAD)
+    if args.serve_requests:
+        W["requests"] = args.serve_requests
+    W["round"] = args.serve_round
     t0 = time.time()
     scenes = [configs.serve_scene(v) for v in range(8)]
     ctxs = []
@@ -532,7 +535,8 @@ def run_serve(args, world, rank, local):
                            lambda_range=W["lambda_nm"], seed=i, light_vertices=W["light_vertices"])
         trace.append((scene, p, integ, res, spp))
     total_samples = sum(res * res * spp for (_, _, _, res, spp) in trace)
-    srv = Server(ctxs, lambda_range=W["lambda_nm"], max_depth=W["max_depth"], memory_budget_bytes=64 << 30)
+    srv = Server(ctxs, lambda_range=W["lambda_nm"], max_depth=W["max_depth"], memory_budget_bytes=64 << 30,
+                 persistent=W["round"] == "persistent")
     # warm-up: compile the merged round's graph and touch every scene
     for s in range(8):
         srv.wait(srv.submit(s, Context.params("nee", 64, 64, spp=1, max_depth=W["max_depth"], lambda_range=W["lambda_nm"])))
@@ -549,10 +553,11 @@ def run_serve(args, world, rank, local):
     per_rate = []
     identical = 0
     compared = 0
-    # the rate at which the trace's offered work equals the GPU's capacity (full load), then the
-    # configuration's rates (all of them beyond capacity for this trace)
+    # offered load rho = rate x mean isolated latency: rates at rho 0.5, 0.8 and 1 (full load: the
+    # trace's work equals the GPU's capacity), then the configuration's rates (beyond capacity for
+    # this trace, whose BDPT requests dominate the work)
     full_load_rate = len(trace) / float(np.sum(iso))
-    for rate in [full_load_rate] + list(W["rates_per_s"]):
+    for rate in [full_load_rate * rho for rho in W["loads"]] + list(W["rates_per_s"]):
         arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(trace)))
         start = time.time()
         ids = []
@@ -569,7 +574,8 @@ def run_serve(args, world, rank, local):
             compared += 1
             identical += int(np.array_equal(srv.result(r)[0], iso_res[k]))
             srv.release(r)
-        per_rate.append({"rate_per_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
+        per_rate.append({"rate_per_s": rate, "offered_load": rate / full_load_rate,
+                         "p50_latency_s": float(np.percentile(lat, 50)),
                          "p99_latency_s": float(np.percentile(lat, 99)),
                          "p99_latency_over_isolated_p99": float(np.percentile(lat, 99) / np.percentile(iso, 99)),
                          "p50_slowdown": float(np.percentile(slow, 50)), "p99_slowdown": float(np.percentile(slow, 99)),
@@ -578,7 +584,7 @@ def run_serve(args, world, rank, local):
     srv.close()
     for c in ctxs:
         c.close()
-    best = per_rate[0]
+    best = per_rate[len(W["loads"]) - 1]  # full load
     line = {"metric": SERVE_METRIC, "value": best["msamples_per_s"], "unit": "Msamples/s", "n_gpus": 1,
             "steps": len(per_rate), "warmup": 9, "full_load_rate_per_s": full_load_rate, "ms_per_step": best["makespan_s"] * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -587,7 +593,8 @@ def run_serve(args, world, rank, local):
             "serve": per_rate, "isolated_latency_s": {"p50": float(np.percentile(iso, 50)), "p99": float(np.percentile(iso, 99)),
                                                       "sum": float(np.sum(iso))},
             "results_identical_alone_and_in_mix": "%d/%d" % (identical, compared),
-            "server": {k: st[k] for k in ("rounds", "graph_replays", "bdpt_slices", "peak_bytes_in_use")}}
+            "server": {k: st[k] for k in ("rounds", "graph_replays", "persistent_rounds", "bdpt_slices", "failed",
+                                          "peak_bytes_in_use")}}
     print(json.dumps(line), flush=True)
 
 
@@ -758,6 +765,9 @@ def main():
     ap.add_argument("--size", type=int, default=0, help="image side for a smaller profiling case")
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel for a smaller profiling case")
     ap.add_argument("--workload", default="nee", choices=["nee", "bdpt", "serve", "denoise"])
+    ap.add_argument("--serve-round", default="graph", choices=["graph", "persistent"],
+                    help="serve: merged rounds as a captured graph of launches or as one persistent kernel")
+    ap.add_argument("--serve-requests", type=int, default=0, help="serve: requests in the trace (0: the workload's)")
     args = ap.parse_args()
     if args.workload == "bdpt":
         WORKLOAD.clear()

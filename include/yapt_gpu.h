@@ -428,7 +428,12 @@ typedef struct yg_server_options
     uint32_t max_depth;           /* largest uni/NEE max_depth accepted (0: 16) */
     float lambda_min, lambda_max; /* spectral range of every request (0, 0: 380..700) */
     uint32_t use_graphs;          /* 1: replay the merged round as a captured CUDA graph; 0: plain launches */
-    uint32_t reserved[5];
+    uint32_t persistent;          /* 1: run the merged round as one persistent cooperative kernel whose
+                                     stages meet at bounded grid barriers (captured as a graph when
+                                     use_graphs is set and the driver captures cooperative launches) */
+    uint32_t barrier_polls;       /* polls of ~128 ns a block waits at a barrier before the round fails
+                                     with YG_ERR_DEVICE_TIMEOUT (0: 2^24) */
+    uint32_t reserved[3];
 } yg_server_options;
 
 typedef struct yg_request
@@ -460,6 +465,7 @@ typedef struct yg_server_stats
 {
     uint64_t submitted, completed, failed, cancelled;
     uint64_t rounds, graph_replays, bdpt_slices, samples;
+    uint64_t persistent_rounds;   /* merged rounds run as one persistent kernel */
     uint64_t bytes_in_use, peak_bytes_in_use;
     uint32_t active, queued;
     double seconds;
@@ -480,6 +486,13 @@ YG_API int yg_server_release(yg_server* server, uint64_t id);
 YG_API int yg_server_stats_get(yg_server* server, yg_server_stats* stats);
 /* Cancels what is queued, finishes nothing further, waits for the device and frees it all. */
 YG_API int yg_server_destroy(yg_server* server);
+/* Self-check of the bounded grid barrier the persistent merged round uses: one cooperative
+ * kernel on the context's stream whose blocks pass the barrier three times while `missing`
+ * blocks never arrive (0: all arrive). *blocks: the grid; *passes: barriers passed summed over
+ * blocks (3 x blocks when all arrive); *timed_out: 1 when a wait ran out of `poll_limit`
+ * polls, after which every block returned and the context stays usable. */
+YG_API int yg_grid_barrier_selftest(yg_context* ctx, uint32_t missing, uint32_t poll_limit, uint32_t* blocks,
+                                    uint32_t* passes, uint32_t* timed_out);
 
 /* One scheduling decision of the serving loop on host data only (no device work), so the
  * policy can be checked without a GPU. items[i]: pixels, planes still to render, film

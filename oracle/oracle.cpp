@@ -2470,6 +2470,11 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                     S4<T> exitW;
                     T pdfPos = 0;
                     TriHit<float> sel;
+                    sel.t = sel.b1 = sel.b2 = 0.f;
+                    sel.inst = h.inst;
+                    sel.prim = 0;
+                    sel.front = false;
+                    sel.found = false;
                     if (ok)
                     {
                         V3<T> axis, pu, pv;

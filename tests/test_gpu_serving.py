@@ -44,7 +44,8 @@ def alone(scene, params):
         return c.film()
 
 
-def test_results_are_identical_alone_and_in_the_mix(built):
+@pytest.mark.parametrize("persistent", [False, True], ids=["graph", "persistent"])
+def test_results_are_identical_alone_and_in_the_mix(built, persistent):
     scs = scenes()
     reqs = request_set()
     expected = [alone(scs[s], p) for (s, p) in reqs]
@@ -52,7 +53,7 @@ def test_results_are_identical_alone_and_in_the_mix(built):
     for c, sc in zip(ctxs, scs):
         c.upload_scene(sc)
     try:
-        with Server(ctxs, lambda_range=LAMBDA, max_depth=12, round_samples=1 << 14) as srv:
+        with Server(ctxs, lambda_range=LAMBDA, max_depth=12, round_samples=1 << 14, persistent=persistent) as srv:
             ids = [srv.submit(s, p) for (s, p) in reqs]
             for rid in ids:
                 info = srv.wait(rid, timeout=120.0)
@@ -68,7 +69,10 @@ def test_results_are_identical_alone_and_in_the_mix(built):
             # continuous batching: several requests shared rounds
             planes = sum(p.spp_count for _, p in reqs if p.integrator != 2)
             assert st["rounds"] < planes
-            assert st["graph_replays"] == st["rounds"]
+            if persistent:
+                assert st["persistent_rounds"] == st["rounds"] and st["graph_replays"] in (0, st["rounds"])
+            else:
+                assert st["graph_replays"] == st["rounds"] and st["persistent_rounds"] == 0
     finally:
         for c in ctxs:
             c.close()
@@ -129,3 +133,51 @@ def test_shutdown_with_work_in_flight_returns_promptly(built):
         t = time.time()
         srv.close()
         assert time.time() - t < 30.0
+
+
+def test_grid_barrier_wait_is_bounded_and_the_context_survives(built):
+    """The persistent round's grid barrier: with every block arriving, each block passes it
+    three times; with one block that never arrives (the barrier expects one more block than the
+    grid), every wait runs out after its poll limit, the kernel reports the time-out and returns,
+    and the context renders correctly afterwards."""
+    scene = configs.box_scene(0)
+    p = Context.params("nee", 32, 32, spp_start=0, spp=2, max_depth=6, lambda_range=LAMBDA)
+    xyz_e, cnt_e = alone(scene, p)
+    with Context(0) as c:
+        blocks, passes, timed = c.grid_barrier_selftest(missing=0, poll_limit=1 << 22)
+        assert blocks > 0 and not timed and passes == 3 * blocks
+        t = time.time()
+        blocks, passes, timed = c.grid_barrier_selftest(missing=1, poll_limit=4096)
+        assert timed and passes == 0
+        assert time.time() - t < 30.0
+        c.upload_scene(scene)
+        c.film_clear(32, 32)
+        c.render(p)
+        xyz, cnt = c.film()
+        assert np.array_equal(cnt, cnt_e) and np.array_equal(xyz, xyz_e)
+
+
+def test_persistent_round_barrier_time_out_fails_only_that_round(built):
+    """A persistent round whose barrier waits are allowed a single poll: whether or not the
+    barriers time out, every request ends (done with the film yg_render gives, or failed with
+    YG_ERR_DEVICE_TIMEOUT); a new server on the same context then completes the request."""
+    scene = configs.box_scene(0)
+    p = Context.params("nee", 48, 32, spp_start=0, spp=2, max_depth=6, lambda_range=LAMBDA)
+    xyz_e, cnt_e = alone(scene, p)
+    with Context(0) as c:
+        c.upload_scene(scene)
+        with Server([c], lambda_range=LAMBDA, max_depth=8, persistent=True, barrier_polls=1) as srv:
+            ids = [srv.submit(0, p) for _ in range(3)]
+            for rid in ids:
+                info = srv.wait(rid, timeout=60.0)
+                assert info["state"] in ("done", "failed"), info
+                if info["state"] == "failed":
+                    assert info["error"] == -6
+                else:
+                    xyz, cnt = srv.result(rid)
+                    assert np.array_equal(cnt, cnt_e) and np.array_equal(xyz, xyz_e)
+        with Server([c], lambda_range=LAMBDA, max_depth=8, persistent=True) as srv:
+            rid = srv.submit(0, p)
+            assert srv.wait(rid, timeout=60.0)["state"] == "done"
+            xyz, cnt = srv.result(rid)
+            assert np.array_equal(cnt, cnt_e) and np.array_equal(xyz, xyz_e)

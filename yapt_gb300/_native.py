@@ -137,7 +137,8 @@ class ServerOptions(C.Structure):
     _fields_ = [
         ("memory_budget_bytes", C.c_uint64), ("max_active", C.c_uint32), ("wave_capacity", C.c_uint32),
         ("round_samples", C.c_uint32), ("max_depth", C.c_uint32), ("lambda_min", C.c_float),
-        ("lambda_max", C.c_float), ("use_graphs", C.c_uint32), ("reserved", C.c_uint32 * 5),
+        ("lambda_max", C.c_float), ("use_graphs", C.c_uint32), ("persistent", C.c_uint32),
+        ("barrier_polls", C.c_uint32), ("reserved", C.c_uint32 * 3),
     ]
 
 
@@ -156,7 +157,7 @@ class ServerStats(C.Structure):
     _fields_ = [
         ("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64), ("cancelled", C.c_uint64),
         ("rounds", C.c_uint64), ("graph_replays", C.c_uint64), ("bdpt_slices", C.c_uint64), ("samples", C.c_uint64),
-        ("bytes_in_use", C.c_uint64), ("peak_bytes_in_use", C.c_uint64), ("active", C.c_uint32),
+        ("persistent_rounds", C.c_uint64), ("bytes_in_use", C.c_uint64), ("peak_bytes_in_use", C.c_uint64), ("active", C.c_uint32),
         ("queued", C.c_uint32), ("seconds", C.c_double),
     ]
 
@@ -233,6 +234,8 @@ SIGNATURES = [
     ("yg_server_cancel", C.c_int, [C.c_void_p, C.c_uint64]),
     ("yg_server_release", C.c_int, [C.c_void_p, C.c_uint64]),
     ("yg_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("yg_grid_barrier_selftest", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
+                                           C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("yg_server_destroy", C.c_int, [C.c_void_p]),
     ("yg_nn_conv3x3", C.c_int, [C.POINTER(NNTensor), C.c_void_p, C.POINTER(C.c_float), C.POINTER(NNTensor),
                                 C.POINTER(NNTensor), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),

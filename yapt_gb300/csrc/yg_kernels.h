@@ -132,6 +132,17 @@ struct MultiTables
 size_t multiWaveBytes(uint32_t capacity);
 int launchWavefrontMulti(const MultiTables& M, void* arena, uint32_t capacity, uint32_t maxDepth,
                          unsigned long long* rayCounter, int smCount, cudaStream_t stream);
+// The same round as one persistent cooperative kernel with bounded grid barriers (`barrier`:
+// 16 bytes of device memory; its third word is nonzero after a barrier ran out of `pollLimit`
+// polls). Returns the launch count, or minus the CUDA error of the launch.
+struct GridBarrier;
+int launchWavefrontMultiPersistent(const MultiTables& M, void* arena, uint32_t capacity, uint32_t maxDepth,
+                                   unsigned long long* rayCounter, int smCount, cudaStream_t stream, GridBarrier* barrier,
+                                   uint32_t pollLimit);
+// Cooperative probe of the grid barrier: `missing` blocks never arrive. *passes counts the
+// barriers each block passed; the barrier's error word tells whether the wait ran out.
+int gridBarrierCheck(GridBarrier* barrier, uint32_t* passes, uint32_t missing, uint32_t pollLimit, int smCount,
+                     cudaStream_t stream, uint32_t* blocks);
 // Bidirectional integrator over P.sppCount sample indices. `arena` holds
 // bdptArenaBytes(P.sppCount, lightPaths, maxLightVerts, cropW*cropH) bytes; `perm` is a
 // permutation of the crop's pixel indices (camera groups take 64 consecutive entries).

@@ -27,7 +27,7 @@ YG_DEV uint32_t segmentOf(const MultiTables& M, uint32_t nSeg, uint32_t s)
     return lo;
 }
 
-__global__ void __launch_bounds__(256) wfmGenerate(MultiTables M, WaveState W, RayQueue Q)
+__device__ __forceinline__ void generateBody(const MultiTables& M, const WaveState& W, const RayQueue& Q)
 {
     const uint32_t nSeg = *M.nSeg;
     const uint32_t total = M.segStart[nSeg];
@@ -53,8 +53,10 @@ __global__ void __launch_bounds__(256) wfmGenerate(MultiTables M, WaveState W, R
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = total;
 }
+__global__ void __launch_bounds__(256) wfmGenerate(MultiTables M, WaveState W, RayQueue Q) { generateBody(M, W, Q); }
 
-__global__ void __launch_bounds__(128) wfmTrace(MultiTables M, RayQueue Q, HitQueue H, unsigned long long* rayCtr)
+__device__ __forceinline__ void traceBody(const MultiTables& M, const RayQueue& Q, const HitQueue& H,
+                                          unsigned long long* rayCtr)
 {
     const uint32_t n = *Q.count;
     uint32_t rays = 0;
@@ -73,8 +75,13 @@ __global__ void __launch_bounds__(128) wfmTrace(MultiTables M, RayQueue Q, HitQu
         tc, rays);
     countRays(rayCtr, rays);
 }
+__global__ void __launch_bounds__(128) wfmTrace(MultiTables M, RayQueue Q, HitQueue H, unsigned long long* rayCtr)
+{
+    traceBody(M, Q, H, rayCtr);
+}
 
-__global__ void __launch_bounds__(256) wfmClassify(MultiTables M, RayQueue Q, HitQueue H, uint8_t* keys, uint32_t* counts)
+__device__ __forceinline__ void classifyBody(const MultiTables& M, const RayQueue& Q, const HitQueue& H, uint8_t* keys,
+                                             uint32_t* counts)
 {
     const uint32_t n = *Q.count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -99,8 +106,13 @@ __global__ void __launch_bounds__(256) wfmClassify(MultiTables M, RayQueue Q, Hi
     }
 }
 
-__global__ void __launch_bounds__(128, 4) wfmShade(MultiTables M, WaveState W, RayQueue Qin, HitQueue H, RayQueue Qout,
-                                                ShadowQueue SQ)
+__global__ void __launch_bounds__(256) wfmClassify(MultiTables M, RayQueue Q, HitQueue H, uint8_t* keys, uint32_t* counts)
+{
+    classifyBody(M, Q, H, keys, counts);
+}
+
+__device__ __forceinline__ void shadeBody(const MultiTables& M, const WaveState& W, const RayQueue& Qin, const HitQueue& H,
+                                          const RayQueue& Qout, const ShadowQueue& SQ)
 {
     const uint32_t n = *Qin.count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -157,8 +169,14 @@ __global__ void __launch_bounds__(128, 4) wfmShade(MultiTables M, WaveState W, R
         }
     }
 }
+__global__ void __launch_bounds__(128, 4) wfmShade(MultiTables M, WaveState W, RayQueue Qin, HitQueue H, RayQueue Qout,
+                                                ShadowQueue SQ)
+{
+    shadeBody(M, W, Qin, H, Qout, SQ);
+}
 
-__global__ void __launch_bounds__(128) wfmShadow(MultiTables M, WaveState W, ShadowQueue SQ, unsigned long long* rayCtr)
+__device__ __forceinline__ void shadowBody(const MultiTables& M, const WaveState& W, const ShadowQueue& SQ,
+                                           unsigned long long* rayCtr)
 {
     const uint32_t n = *SQ.count;
     uint32_t rays = 0;
@@ -182,7 +200,12 @@ __global__ void __launch_bounds__(128) wfmShadow(MultiTables M, WaveState W, Sha
     countRays(rayCtr, rays);
 }
 
-__global__ void __launch_bounds__(256) wfmFinalize(MultiTables M, WaveState W)
+__global__ void __launch_bounds__(128) wfmShadow(MultiTables M, WaveState W, ShadowQueue SQ, unsigned long long* rayCtr)
+{
+    shadowBody(M, W, SQ, rayCtr);
+}
+
+__device__ __forceinline__ void finalizeBody(const MultiTables& M, const WaveState& W)
 {
     const uint32_t total = M.segStart[*M.nSeg];
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < total; s += gridDim.x * blockDim.x)
@@ -197,8 +220,10 @@ __global__ void __launch_bounds__(256) wfmFinalize(MultiTables M, WaveState W)
     }
 }
 
+__global__ void __launch_bounds__(256) wfmFinalize(MultiTables M, WaveState W) { finalizeBody(M, W); }
+
 // Kahan film of every segment: the request's pixels, its planes of this round in order
-__global__ void __launch_bounds__(256) wfmFilm(MultiTables M)
+__device__ __forceinline__ void filmBody(const MultiTables& M)
 {
     const uint32_t nSeg = *M.nSeg;
     const uint32_t totalPix = M.segPixStart[nSeg];
@@ -233,14 +258,99 @@ __global__ void __launch_bounds__(256) wfmFilm(MultiTables M)
         comp[fi] = c;
     }
 }
+__global__ void __launch_bounds__(256) wfmFilm(MultiTables M) { filmBody(M); }
+
+// The queues of a merged round, carved from the round's arena
+struct RoundQueues
+{
+    WaveState W;
+    RayQueue QA, QB, QS;
+    HitQueue H, HS;
+    ShadowQueue SQ;
+    uint8_t* keys;
+    uint32_t* classCounts;
+};
+
+// One merged round as one persistent cooperative kernel: every stage of the multi-kernel round
+// (generate; per bounce trace, classify, regroup, shade, shadow; finalize; film), each a
+// grid-stride loop over the stage's queue, separated by grid barriers instead of launches. The
+// paths compute what they compute in the multi-kernel round. A barrier that does not complete
+// within `pollLimit` polls stops every block (the round reports the time-out through the
+// barrier's error word) instead of hanging.
+__global__ void __launch_bounds__(128, 4) wfmRound(MultiTables M, RoundQueues R, uint32_t maxDepth, GridBarrier* bar,
+                                                   uint32_t pollLimit, unsigned long long* rayCtr)
+{
+    generateBody(M, R.W, R.QA);
+    if (!gridSync(bar, pollLimit)) return;
+    RayQueue cur = R.QA, nxt = R.QB;
+    for (uint32_t b = 0; b < maxDepth; ++b)
+    {
+        // the same count in every block (written before the last barrier): no path left
+        if (*(volatile uint32_t*)cur.count == 0) break;
+        // nothing reads these counters between here and the next barrier
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+        {
+            *nxt.count = 0;
+            *R.SQ.count = 0;
+            for (int c = 0; c < 2 * kShadeClasses; ++c) R.classCounts[c] = 0;
+        }
+        traceBody(M, cur, R.H, rayCtr);
+        if (!gridSync(bar, pollLimit)) return;
+        classifyBody(M, cur, R.H, R.keys, R.classCounts);
+        if (!gridSync(bar, pollLimit)) return;
+        regroupBody<kShadeClasses>(cur, R.H, R.keys, R.classCounts, R.classCounts + kShadeClasses, R.QS, R.HS);
+        if (!gridSync(bar, pollLimit)) return;
+        shadeBody(M, R.W, R.QS, R.HS, nxt, R.SQ);
+        if (!gridSync(bar, pollLimit)) return;
+        shadowBody(M, R.W, R.SQ, rayCtr);
+        if (!gridSync(bar, pollLimit)) return;
+        RayQueue t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    finalizeBody(M, R.W);
+    if (!gridSync(bar, pollLimit)) return;
+    filmBody(M);
+}
+
+__global__ void gridBarrierInit(GridBarrier* bar, uint32_t expected)
+{
+    bar->count = 0;
+    bar->gen = 0;
+    bar->error = 0;
+    bar->expected = expected;
+}
+
+// Every block passes the barrier three times; with `missing` blocks that never arrive the first
+// barrier runs out of polls and every block returns.
+__global__ void __launch_bounds__(128) gridBarrierProbe(GridBarrier* bar, uint32_t pollLimit, uint32_t* passes)
+{
+    for (int k = 0; k < 3; ++k)
+    {
+        if (!gridSync(bar, pollLimit)) return;
+        if (threadIdx.x == 0) atomicAdd(passes, 1u);
+    }
+}
+
+int gridBarrierCheck(GridBarrier* bar, uint32_t* passes, uint32_t missing, uint32_t pollLimit, int smCount,
+                     cudaStream_t stream, uint32_t* blocks)
+{
+    int perSm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, gridBarrierProbe, 128, 0);
+    if (e != cudaSuccess) return (int)e;
+    const uint32_t grid = (uint32_t)std::max(1, std::min(perSm, 2) * smCount);
+    *blocks = grid;
+    gridBarrierInit<<<1, 1, 0, stream>>>(bar, grid + missing);
+    void* args[] = {&bar, &pollLimit, &passes};
+    return (int)cudaLaunchCooperativeKernel((const void*)gridBarrierProbe, dim3(grid), dim3(128), args, 0, stream);
+}
 
 size_t multiWaveBytes(uint32_t capacity)
 {
     return (size_t)capacity * (wavefrontBytesPerSlot() + 8) + (64u << 10);
 }
 
-int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, uint32_t maxDepth,
-                         unsigned long long* rayCounter, int smCount, cudaStream_t stream)
+static RoundQueues carveRound(MultiTables& M, void* arena, uint32_t capacity)
 {
     char* p = static_cast<char*>(arena);
     auto take = [&](size_t bytes) {
@@ -249,8 +359,8 @@ int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, 
         return r;
     };
     const size_t C = capacity;
-    MultiTables M = M0;
-    WaveState W;
+    RoundQueues R;
+    WaveState& W = R.W;
     W.capacity = capacity;
     W.thr = (float4*)take(C * 16);
     W.tot = (float4*)take(C * 16);
@@ -265,15 +375,33 @@ int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, 
     M.req = (uint32_t*)take(C * 4);
     M.local = (uint32_t*)take(C * 4);
     uint32_t* counters = (uint32_t*)take(256);
-    RayQueue QA{(float4*)take(C * 16), (float4*)take(C * 16), counters + 0};
-    RayQueue QB{(float4*)take(C * 16), (float4*)take(C * 16), counters + 1};
-    HitQueue H{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
-    ShadowQueue SQ{(float4*)take(C * 16), (float4*)take(C * 16), (uint2*)take(C * 8), (float4*)take(C * 16),
-                   counters + 2};
-    RayQueue QS{(float4*)take(C * 16), (float4*)take(C * 16), counters + 3};
-    HitQueue HS{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
-    uint8_t* keys = (uint8_t*)take(C);
-    uint32_t* classCounts = counters + 8;
+    R.QA = RayQueue{(float4*)take(C * 16), (float4*)take(C * 16), counters + 0};
+    R.QB = RayQueue{(float4*)take(C * 16), (float4*)take(C * 16), counters + 1};
+    R.H = HitQueue{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
+    R.SQ = ShadowQueue{(float4*)take(C * 16), (float4*)take(C * 16), (uint2*)take(C * 8), (float4*)take(C * 16),
+                       counters + 2};
+    R.QS = RayQueue{(float4*)take(C * 16), (float4*)take(C * 16), counters + 3};
+    R.HS = HitQueue{(float4*)take(C * 16), (uint32_t*)take(C * 4)};
+    R.keys = (uint8_t*)take(C);
+    R.classCounts = counters + 8;
+    return R;
+}
+
+int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, uint32_t maxDepth,
+                         unsigned long long* rayCounter, int smCount, cudaStream_t stream)
+{
+    MultiTables M = M0;
+    RoundQueues R = carveRound(M, arena, capacity);
+    WaveState& W = R.W;
+    RayQueue& QA = R.QA;
+    RayQueue& QB = R.QB;
+    RayQueue& QS = R.QS;
+    HitQueue& H = R.H;
+    HitQueue& HS = R.HS;
+    ShadowQueue& SQ = R.SQ;
+    uint8_t* keys = R.keys;
+    uint32_t* classCounts = R.classCounts;
+    const size_t C = capacity;
     const int traceBlocks = smCount * 16, shadeBlocks = smCount * 8;
     int gblocks = (int)std::min<uint64_t>((C + 255) / 256, (uint64_t)smCount * 8);
     int launches = 0;
@@ -300,6 +428,24 @@ int launchWavefrontMulti(const MultiTables& M0, void* arena, uint32_t capacity, 
     wfmFilm<<<gblocks, 256, 0, stream>>>(M);
     launches += 2;
     return launches;
+}
+
+int launchWavefrontMultiPersistent(const MultiTables& M0, void* arena, uint32_t capacity, uint32_t maxDepth,
+                                   unsigned long long* rayCounter, int smCount, cudaStream_t stream, GridBarrier* barrier,
+                                   uint32_t pollLimit)
+{
+    MultiTables M = M0;
+    RoundQueues R = carveRound(M, arena, capacity);
+    int perSm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, wfmRound, 128, 0);
+    if (e != cudaSuccess) return -(int)e;
+    if (perSm < 1) return -(int)cudaErrorCooperativeLaunchTooLarge;
+    const uint32_t grid = (uint32_t)(perSm * smCount);
+    gridBarrierInit<<<1, 1, 0, stream>>>(barrier, grid);
+    void* args[] = {&M, &R, &maxDepth, &barrier, &pollLimit, &rayCounter};
+    e = cudaLaunchCooperativeKernel((const void*)wfmRound, dim3(grid), dim3(128), args, 0, stream);
+    if (e != cudaSuccess) return -(int)e;
+    return 2;
 }
 
 } // namespace yg

@@ -149,6 +149,9 @@ struct yg_server
     uint32_t sobolPlanes = 0;
     yg::MultiTables M{};
     cudaGraphExec_t graph = nullptr;
+    yg::GridBarrier* barrier = nullptr; // persistent round: 4 words of device memory
+    bool persistentUncaptured = false;   // the cooperative round could not be captured
+    uint32_t* barrierErrHost = nullptr; // pinned copy of the barrier's error word after a round
     std::vector<Segment> inFlightA;
     // BDPT slice
     Req* inFlightB = nullptr;
@@ -344,7 +347,45 @@ int launchMerged(yg_server* s, std::vector<Segment>& segs)
     *nSeg = (uint32_t)segs.size();
     YG_CUDA(cudaMemcpyAsync(s->tablesDev, s->tablesHost, T.total, cudaMemcpyHostToDevice, s->sA));
     YG_CUDA(cudaMemcpyAsync(s->sobolDev, s->sobolHost, (size_t)plane * yg::kSobolDims * 4, cudaMemcpyHostToDevice, s->sA));
-    if (s->opt.use_graphs)
+    if (s->opt.persistent)
+    {
+        // the barrier set-up and the cooperative round, captured once when graphs are on
+        // (replayed like the multi-kernel round), else launched directly
+        if (s->opt.use_graphs && !s->graph && !s->persistentUncaptured)
+        {
+            cudaGraph_t g = nullptr;
+            YG_CUDA(cudaStreamBeginCapture(s->sA, cudaStreamCaptureModeThreadLocal));
+            int n = yg::launchWavefrontMultiPersistent(s->M, s->waveArena, s->opt.wave_capacity, s->opt.max_depth, nullptr,
+                                                      s->smCount, s->sA, s->barrier, s->opt.barrier_polls);
+            cudaError_t e = cudaStreamEndCapture(s->sA, &g);
+            if (n >= 0 && e == cudaSuccess) e = cudaGraphInstantiate(&s->graph, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (n < 0 || e != cudaSuccess)
+            {
+                // this driver does not capture cooperative launches: launch them directly
+                if (s->graph) cudaGraphExecDestroy(s->graph);
+                s->graph = nullptr;
+                s->persistentUncaptured = true;
+                cudaGetLastError();
+            }
+        }
+        if (s->graph)
+        {
+            YG_CUDA(cudaGraphLaunch(s->graph, s->sA));
+            ++s->st.graph_replays;
+        }
+        else
+        {
+            int n = yg::launchWavefrontMultiPersistent(s->M, s->waveArena, s->opt.wave_capacity, s->opt.max_depth, nullptr,
+                                                      s->smCount, s->sA, s->barrier, s->opt.barrier_polls);
+            if (n < 0)
+                return fail(YG_ERR_CUDA, std::string("serve: persistent round: ") + cudaGetErrorString((cudaError_t)(-n)));
+        }
+        YG_CUDA(cudaMemcpyAsync(s->barrierErrHost, reinterpret_cast<char*>(s->barrier) + 8, 4, cudaMemcpyDeviceToHost,
+                                s->sA));
+        ++s->st.persistent_rounds;
+    }
+    else if (s->opt.use_graphs)
     {
         if (!s->graph)
         {
@@ -448,6 +489,20 @@ void workerLoop(yg_server* s)
             {
                 failAll(s, std::string("serve: merged round: ") + cudaGetErrorString(e));
                 s->inFlightA.clear();
+            }
+            else if (s->opt.persistent && *s->barrierErrHost != 0)
+            {
+                // a grid barrier ran out of polls: the round's films are incomplete, the
+                // context is intact; the requests of the round fail, the server goes on
+                for (Segment& g : s->inFlightA)
+                {
+                    g.r->inFlight = false;
+                    releaseActive(s, g.r, s->sA);
+                    markDone(s, g.r, YG_REQ_FAILED, YG_ERR_DEVICE_TIMEOUT,
+                             "serve: persistent round: a grid barrier wait ran out");
+                }
+                s->inFlightA.clear();
+                *s->barrierErrHost = 0;
             }
             for (Segment& g : s->inFlightA)
             {
@@ -613,6 +668,7 @@ YG_API int yg_server_create(yg_context* const* scenes, uint32_t n, const yg_serv
     if (o.wave_capacity == 0) o.wave_capacity = 1u << 21;
     if (o.round_samples == 0) o.round_samples = 1u << 19;
     if (o.max_depth == 0) o.max_depth = 16;
+    if (o.barrier_polls == 0) o.barrier_polls = 1u << 24;
     if (o.lambda_min != 0.0f || o.lambda_max != 0.0f)
     {
         s->lmin = o.lambda_min;
@@ -644,6 +700,12 @@ YG_API int yg_server_create(yg_context* const* scenes, uint32_t n, const yg_serv
     }
     YG_CUDA(cudaSetDevice(s->device));
     cudaDeviceGetAttribute(&s->smCount, cudaDevAttrMultiProcessorCount, s->device);
+    if (o.persistent)
+    {
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
+        if (!coop) return fail(YG_ERR_INVALID_ARGUMENT, "serve: persistent rounds need cooperative launch");
+    }
     // merged rounds are short and carry most requests: their stream gets the higher priority,
     // so their blocks are scheduled ahead of the long BDPT kernels on the other stream
     int prLeast = 0, prGreatest = 0;
@@ -664,6 +726,9 @@ YG_API int yg_server_create(yg_context* const* scenes, uint32_t n, const yg_serv
     YG_CUDA(cudaMalloc((void**)&s->sobolDevB, sobolBytes));
     YG_CUDA(cudaMallocHost((void**)&s->sobolHostB, sobolBytes));
     YG_CUDA(cudaMalloc(&s->waveArena, yg::multiWaveBytes(o.wave_capacity)));
+    YG_CUDA(cudaMalloc((void**)&s->barrier, 16));
+    YG_CUDA(cudaMallocHost((void**)&s->barrierErrHost, 4));
+    *s->barrierErrHost = 0;
     YG_CUDA(cudaMalloc((void**)&s->roundSamples, (size_t)o.wave_capacity * 16));
     s->M.views = reinterpret_cast<const yg::SceneView*>(s->tablesDev + T.views);
     s->M.params = reinterpret_cast<const yg::LaunchParams*>(s->tablesDev + T.params);
@@ -776,6 +841,33 @@ YG_API int yg_server_release(yg_server* s, uint64_t id)
     return YG_OK;
 }
 
+YG_API int yg_grid_barrier_selftest(yg_context* ctx, uint32_t missing, uint32_t pollLimit, uint32_t* blocks,
+                                    uint32_t* passes, uint32_t* timedOut)
+{
+    if (!ctx || !blocks || !passes || !timedOut) return fail(YG_ERR_INVALID_ARGUMENT, "barrier selftest: null argument");
+    if (missing > 1024 || pollLimit == 0)
+        return fail(YG_ERR_INVALID_ARGUMENT, "barrier selftest: missing <= 1024 and poll_limit > 0");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    YG_CUDA(cudaSetDevice(ctx->device));
+    char* d = nullptr;
+    YG_CUDA(cudaMalloc((void**)&d, 32));
+    uint32_t h[8] = {};
+    cudaError_t e = cudaMemsetAsync(d, 0, 32, ctx->stream);
+    if (e == cudaSuccess)
+    {
+        int r = yg::gridBarrierCheck(reinterpret_cast<yg::GridBarrier*>(d), reinterpret_cast<uint32_t*>(d + 16), missing,
+                                     pollLimit, ctx->smCount, ctx->stream, blocks);
+        e = (cudaError_t)r;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 32, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(YG_ERR_CUDA, std::string("barrier selftest: ") + cudaGetErrorString(e));
+    *passes = h[4];
+    *timedOut = h[2] != 0 ? 1u : 0u;
+    return YG_OK;
+}
+
 YG_API int yg_server_stats_get(yg_server* s, yg_server_stats* out)
 {
     if (!s || !out) return fail(YG_ERR_INVALID_ARGUMENT, "serve: null argument");
@@ -814,6 +906,8 @@ YG_API int yg_server_destroy(yg_server* s)
     if (s->sobolDevB) cudaFree(s->sobolDevB);
     if (s->sobolHostB) cudaFreeHost(s->sobolHostB);
     if (s->waveArena) cudaFree(s->waveArena);
+    if (s->barrier) cudaFree(s->barrier);
+    if (s->barrierErrHost) cudaFreeHost(s->barrierErrHost);
     if (s->roundSamples) cudaFree(s->roundSamples);
     if (s->evA) cudaEventDestroy(s->evA);
     if (s->evB) cudaEventDestroy(s->evB);

@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(256) wfClassify(const SceneView S, RayQueue Q,
 }
 
 template <int CLASSES>
-__global__ void __launch_bounds__(256) wfRegroup(RayQueue Q, HitQueue H, const uint8_t* keys, const uint32_t* counts,
-                                                 uint32_t* cursors, RayQueue Qs, HitQueue Hs)
+__device__ __forceinline__ void regroupBody(RayQueue Q, HitQueue H, const uint8_t* keys, const uint32_t* counts,
+                                            uint32_t* cursors, RayQueue Qs, HitQueue Hs)
 {
     const uint32_t n = *Q.count;
     uint32_t base[CLASSES];
@@ -233,6 +233,58 @@ __global__ void __launch_bounds__(256) wfRegroup(RayQueue Q, HitQueue H, const u
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *Qs.count = n;
+}
+template <int CLASSES>
+__global__ void __launch_bounds__(256) wfRegroup(RayQueue Q, HitQueue H, const uint8_t* keys, const uint32_t* counts,
+                                                 uint32_t* cursors, RayQueue Qs, HitQueue Hs)
+{
+    regroupBody<CLASSES>(Q, H, keys, counts, cursors, Qs, Hs);
+}
+
+// A barrier over every block of a cooperative launch, with a bounded wait: generation counting
+// in device memory; the last block to arrive starts the next generation. A block that waits
+// longer than `limit` polls records the time-out in `error` and every block returns false, so
+// a kernel never hangs on a block that does not arrive. `expected` is normally gridDim.x.
+struct GridBarrier
+{
+    unsigned int count, gen, error, expected;
+};
+__device__ __forceinline__ bool gridSync(GridBarrier* b, uint32_t limit)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        ok = 1;
+        volatile unsigned int* vgen = &b->gen;
+        volatile unsigned int* verr = &b->error;
+        const unsigned int g = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&b->count, 1u) + 1u;
+        if (arrived == b->expected)
+        {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        }
+        else
+        {
+            uint32_t polls = 0;
+            while (*vgen == g)
+            {
+                if (*verr != 0u || ++polls > limit)
+                {
+                    atomicExch(&b->error, 1u);
+                    break;
+                }
+                __nanosleep(128);
+            }
+        }
+        __threadfence();
+        if (*verr != 0u) ok = 0;
+    }
+    __syncthreads();
+    return ok != 0;
 }
 
 } // namespace yg

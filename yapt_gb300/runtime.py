@@ -169,6 +169,15 @@ class Context:
             out[f] = getattr(kp, f)
         return out
 
+    def grid_barrier_selftest(self, missing=0, poll_limit=1 << 20):
+        """Runs the bounded grid barrier of the persistent serving round once as a cooperative
+        kernel whose blocks pass it three times, with `missing` blocks that never arrive.
+        Returns (blocks, barriers passed summed over blocks, timed out)."""
+        blocks, passes, timed = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        N.check(self.lib.yg_grid_barrier_selftest(self.h, int(missing), int(poll_limit), C.byref(blocks),
+                                                  C.byref(passes), C.byref(timed)))
+        return blocks.value, passes.value, bool(timed.value)
+
     def traversal_counts(self):
         n, t = C.c_uint64(), C.c_uint64()
         N.check(self.lib.yg_last_traversal_counts(self.h, C.byref(n), C.byref(t)))
@@ -188,7 +197,7 @@ class Server:
     directly while the server lives). Options as yg_server_options."""
 
     def __init__(self, contexts, memory_budget_bytes=0, max_active=0, wave_capacity=0, round_samples=0, max_depth=0,
-                 lambda_range=(380.0, 700.0), use_graphs=True):
+                 lambda_range=(380.0, 700.0), use_graphs=True, persistent=False, barrier_polls=0):
         self.lib = N.load()
         self.contexts = list(contexts)
         arr = (C.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
@@ -200,6 +209,8 @@ class Server:
         o.max_depth = int(max_depth)
         o.lambda_min, o.lambda_max = float(lambda_range[0]), float(lambda_range[1])
         o.use_graphs = 1 if use_graphs else 0
+        o.persistent = 1 if persistent else 0
+        o.barrier_polls = int(barrier_polls)
         h = C.c_void_p()
         N.check(self.lib.yg_server_create(arr, len(self.contexts), C.byref(o), C.byref(h)))
         self.h = h
