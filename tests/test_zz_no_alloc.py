@@ -58,19 +58,25 @@ def test_noalloc_matches_the_allocating_entry_point_on_consecutive_calls(built, 
                 assert_same_samples(got, orc)
 
 
-@pytest.mark.parametrize("case", ["several_waves", "crop"])
+@pytest.mark.parametrize("case", ["several_waves", "crop", "waves_split_planes"])
 def test_noalloc_over_several_waves_and_on_a_crop(built, case):
     """128 x 128 x 4 samples run as four waves of the fixed 16,384-path arena; the crop case
-    renders a ragged window of a larger image. Both against yg_render's per-sample dump."""
+    renders a ragged window of a larger image; 96 x 102 x 3 samples split a sample plane and a
+    four-row band between two waves and end each plane with a partial band (the slots there keep
+    scanline order, the others cover 8 x 4 tiles). All against yg_render's per-sample dump, which
+    renders each request as one wave."""
     lib = N.load()
     with Context(0) as c:
         c.upload_scene(configs.box_scene(2))
         if case == "several_waves":
             p = c.params("uni", 128, 128, spp_start=5, spp=4, max_depth=8, lambda_range=(380, 700),
                          flags=N.YG_FLAG_NO_FILM)
-        else:
+        elif case == "crop":
             p = c.params("nee", 200, 120, spp_start=17, spp=3, max_depth=8, lambda_range=(380, 700),
                          flags=N.YG_FLAG_NO_FILM, crop=(37, 21, 61, 43))
+        else:
+            p = c.params("nee", 96, 102, spp_start=2, spp=3, max_depth=8, lambda_range=(380, 700),
+                         flags=N.YG_FLAG_NO_FILM)
         ref = c.render(p, dump=True)[..., 5:8]
         for _ in range(2):  # twice in a row: the array keeps the last call's contents
             assert_same_samples(render_noalloc(lib, c, p), ref)

@@ -13,6 +13,12 @@
 #include <string>
 #include <vector>
 
+// paths per wavefront wave of yg_render (log2); the path state takes wavefrontBytesPerSlot()
+// bytes per path
+#ifndef YG_WAVE_CAPACITY_LOG2
+#define YG_WAVE_CAPACITY_LOG2 24
+#endif
+
 namespace ygi
 {
 thread_local std::string g_lastError;
@@ -1121,7 +1127,7 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     }
     if (dump) YG_CUDA(ctx->dDump.ensure(npix * chunkSpp * 8 * sizeof(float)));
     const bool mega = (p->flags & YG_FLAG_MEGAKERNEL) != 0;
-    uint32_t waveCap = (uint32_t)std::min<uint64_t>(npix * chunkSpp, 1ull << 22);
+    uint32_t waveCap = (uint32_t)std::min<uint64_t>(npix * chunkSpp, 1ull << YG_WAVE_CAPACITY_LOG2);
     if (!mega && !bdpt) YG_CUDA(ctx->dArena.ensure(waveCap * yg::wavefrontBytesPerSlot() + (64u << 10)));
     const size_t counterBytes = 8 * (1 + yg::kTraversalCounters);
     YG_CUDA(ctx->dRayCount.ensure(counterBytes));

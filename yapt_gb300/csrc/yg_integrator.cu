@@ -16,7 +16,7 @@ namespace yg
 
 // ------------------------------------------------------------------ megakernel
 template <bool NEE, bool COUNT>
-__global__ void __launch_bounds__(128) pathKernel(const SceneView S, const LaunchParams P)
+__global__ void __launch_bounds__(128) pathKernel(const __grid_constant__ SceneView S, const __grid_constant__ LaunchParams P)
 {
     Luts Lt = lutsOf(S);
     TraversalCount tc{0, 0};
@@ -129,12 +129,12 @@ YG_DEV void storeVolumes(const SlotState& W, uint32_t slot, const PathState& ps)
     for (int k = 0; k < kMaxVolumes; ++k) W.volAbs[(size_t)k * W.capacity + slot] = ps.volAbs[k];
 }
 
-__global__ void __launch_bounds__(256) wfGenerate(const SceneView S, const LaunchParams P, SlotState W, PathQueue Q,
+__global__ void __launch_bounds__(256) wfGenerate(const __grid_constant__ SceneView S, const __grid_constant__ LaunchParams P, SlotState W, PathQueue Q,
                                                   uint64_t base, uint32_t n)
 {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
-        uint64_t idx = base + s;
+        uint64_t idx = sampleOfSlot(P, base, n, s);
         uint32_t sl, cx, cy;
         pixelOf(P, idx, sl, cx, cy);
         uint32_t seed = (cy * P.width + cx) ^ (P.seed * 0x9E3779B9u);
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256) wfGenerate(const SceneView S, const Launc
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) wfTrace(const SceneView S, PathQueue Q, HitQueue H, unsigned long long* rayCtr,
+__global__ void __launch_bounds__(128) wfTrace(const __grid_constant__ SceneView S, PathQueue Q, HitQueue H, unsigned long long* rayCtr,
                                                unsigned long long* travCtr)
 {
     const uint32_t n = *Q.count;
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(128) wfTrace(const SceneView S, PathQueue Q, H
 }
 
 // shading-class key of every queued hit and the class counts (shadeClass of yg_wave.cuh)
-__global__ void __launch_bounds__(256) wfClassifyQ(const SceneView S, const uint32_t* count, HitQueue H, uint8_t* keys,
+__global__ void __launch_bounds__(256) wfClassifyQ(const __grid_constant__ SceneView S, const uint32_t* count, HitQueue H, uint8_t* keys,
                                                    uint32_t* counts)
 {
     const uint32_t n = *count;
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256) wfRegroupQ(PathQueue A, HitQueue H, const
 #define YG_SHADE_MIN_BLOCKS 4
 #endif
 template <bool NEE>
-__global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const SceneView S, const LaunchParams P, SlotState W,
+__global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const __grid_constant__ SceneView S, const __grid_constant__ LaunchParams P, SlotState W,
                                                                    PathQueue Qin, HitQueue H, PathQueue Qout, ShadowQueue SQ,
                                                                    const uint32_t* classCounts, uint32_t classLo,
                                                                    uint32_t classHi)
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const SceneV
 // Shadow rays: a visible light adds its contribution to the path's record in the next queue, or
 // to the slot of a path that ended at this vertex.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) wfShadow(const SceneView S, SlotState W, PathQueue Qnext, ShadowQueue SQ,
+__global__ void __launch_bounds__(128) wfShadow(const __grid_constant__ SceneView S, SlotState W, PathQueue Qnext, ShadowQueue SQ,
                                                 unsigned long long* rayCtr, unsigned long long* travCtr)
 {
     const uint32_t n = *SQ.count;
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(128) wfShadow(const SceneView S, SlotState W, 
     }
 }
 
-__global__ void __launch_bounds__(256) wfFinalize(const SceneView S, const LaunchParams P, SlotState W, uint64_t base,
+__global__ void __launch_bounds__(256) wfFinalize(const __grid_constant__ SceneView S, const __grid_constant__ LaunchParams P, SlotState W, uint64_t base,
                                                   uint32_t n)
 {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(256) wfFinalize(const SceneView S, const Launc
             fh.normal = mk3(nd.x, nd.y, nd.z);
             fh.depth = nd.w;
         }
-        writeSample(S, P, base + s, sp, W.finalTot[s], fh);
+        writeSample(S, P, sampleOfSlot(P, base, n, s), sp, W.finalTot[s], fh);
     }
 }
 

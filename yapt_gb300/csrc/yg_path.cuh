@@ -356,7 +356,20 @@ YG_DEV void setupSurface(const SceneView& S, const LaunchParams& P, const Spectr
     }
     // modifySurfaceMaterialParametersWithTextures (materialsCommon.hlsl:354-397)
     s.occlusion = 1.0f;
+#ifdef YG_COLD_COPIES
+    if (M.mask & kMaterialTextured)
+    {
+        // the out-of-line call works on copies, so that the surface itself never has its
+        // address taken
+        SurfaceRGB rgbX = rgb;
+        Surface sX = s;
+        applyTextures(S, M, I, g, b0, hit.b1, hit.b2, rgbX, sX);
+        rgb = rgbX;
+        s = sX;
+    }
+#else
     if (M.mask & kMaterialTextured) applyTextures(S, M, I, g, b0, hit.b1, hit.b2, rgb, s);
+#endif
     // regularisation (rayHitDefault.hlsl:494-502)
     if (P.regularizeEnable)
     {
@@ -900,7 +913,22 @@ YG_DEV bool shadeSegment(const SceneView& S, const LaunchParams& P, const Luts& 
             int layer = selectMaterialLayer(rB.x, c.probs);
             if (layer == LAYER_SSS)
             {
+#ifdef YG_COLD_COPIES
+                PathState psX = ps;
+                RandomSampler rsX = rs;
+                ShadowRequest srX = sr;
+                const Hit hitX = hit;
+                const Spectral spX = sp;
+                const Luts ltX = Lt;
+                const Surface sX = s;
+                const SurfaceCtx cX = c;
+                alive = subsurfaceEvent<NEE>(S, P, ltX, spX, hitX, I, sX, cX, hitPos, normalWS, rB, psX, rsX, srX);
+                ps = psX;
+                rs = rsX;
+                sr = srX;
+#else
                 alive = subsurfaceEvent<NEE>(S, P, Lt, sp, hit, I, s, c, hitPos, normalWS, rB, ps, rs, sr);
+#endif
                 ps.pathLength += 1;
                 if (alive && russianRoulette(ps.throughput, rs.r1())) alive = false;
                 return alive;

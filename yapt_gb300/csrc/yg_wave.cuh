@@ -52,6 +52,29 @@ YG_DEV void pixelOf(const LaunchParams& P, uint64_t idx, uint32_t& sl, uint32_t&
     cy = P.cropY + pl / P.cropW;
 }
 
+// The sample a wave slot renders (the wave holds samples base .. base + n - 1). Within every
+// band of four full rows of a sample plane that lies wholly in the wave, 32 consecutive slots
+// cover an 8x4 pixel tile, so the primary rays of a warp (and their shadow rays) start close
+// together and point nearly the same way; elsewhere slots follow scanline order. A bijection
+// on the wave: the film still receives every sample at its own index.
+YG_DEV uint64_t sampleOfSlot(const LaunchParams& P, uint64_t base, uint32_t n, uint32_t s)
+{
+    const uint64_t idx = base + s;
+    const uint32_t W = P.cropW;
+    if ((W & 7u) != 0u) return idx;
+    const uint64_t npix = (uint64_t)W * P.cropH;
+    const uint64_t sl = idx / npix;
+    const uint64_t pl = idx - sl * npix;
+    const uint64_t band = 4ull * W;
+    const uint64_t b0 = (pl / band) * band; // the band's first pixel
+    if (b0 + band > npix) return idx;      // the partial band at the bottom of the plane
+    const uint64_t g0 = sl * npix + b0;     // its first sample
+    if (g0 < base || g0 + band > base + n) return idx;
+    const uint32_t local = (uint32_t)(pl - b0);
+    const uint32_t x = (local >> 5) * 8u + (local & 7u), y = (local >> 3) & 3u;
+    return g0 + (uint64_t)y * W + x;
+}
+
 YG_DEV Luts lutsOf(const SceneView& S)
 {
     return Luts{S.lutSS, S.lutSSAvg, S.lutSSMS, S.lutSSMSAvg, S.lutTransDenser, S.lutTransLighter,
