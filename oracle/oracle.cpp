@@ -2137,6 +2137,89 @@ template <typename T> void exitLobeEval(const Surf<T>& s, const SCtx<T>& c, V3<T
     }
 }
 
+// sampleSubsurfaceExit (subsurface.hlsl:212-337): an exit point for the entry point ep (normal en
+// on the side the path arrived from) of instance inst, by up to eight probe rays along one axis of
+// the entry frame at a radius drawn from one spectral lane's profile, one hit kept in proportion
+// to the profile; the exit normal faces out of the geometry, the exit keeps the entry's face
+template <typename T>
+struct SssExit
+{
+    V3<T> pos, normal;
+    TriHit<float> hit; // the probe hit (its face flag is the probe's)
+    bool front;        // the exit's face flag: the entry's
+    S4<T> w;  // Rd / (area density * probe-hit selection probability)
+    T pdfPos; // area density of the exit point
+};
+template <typename T> bool sssSampleExit(const Ctx<T>& c, const Surf<T>& s, const oracle_instance& I, uint32_t inst, bool entryFront,
+                                         V3<T> ep, V3<T> en, T r1, T r2, T r3, SssExit<T>& out, uint64_t& rays)
+{
+    T u = r1;
+    uint32_t axisIndex;
+    if (u < T(0.5f)) { axisIndex = 0; u *= T(2); }
+    else if (u < T(0.75f)) { axisIndex = 1; u = (u - T(0.5f)) * T(4); }
+    else { axisIndex = 2; u = (u - T(0.75f)) * T(4); }
+    uint32_t lane = std::min((uint32_t)(u * T(4)), 3u);
+    T uSel = saturate(u * T(4) - T(lane));
+    const T dLane = burleyD(s.sssRadius[lane], s.albedo[lane]);
+    const T rMax = burleyRMax(dLane);
+    const T r = burleySampleRadius(r2, dLane);
+    out.pdfPos = 0;
+    out.w = sp(T(0));
+    out.front = entryFront;
+    TriHit<float>& sel = out.hit;
+    sel.t = sel.b1 = sel.b2 = 0.f;
+    sel.inst = inst;
+    sel.prim = 0;
+    sel.front = false;
+    sel.found = false;
+    if (!(r < rMax)) return false;
+    V3<T> axis, pu, pv;
+    probeFrame(en, axisIndex, axis, pu, pv);
+    T sinPhi, cosPhi;
+    Mth<T>::sincos(T(2) * C<T>::PI * r3, sinPhi, cosPhi);
+    const T maxCoord = tmax(tmax(std::fabs(ep.x), std::fabs(ep.y)), std::fabs(ep.z));
+    const T halfLength = tmax(Mth<T>::sqrt(rMax * rMax - r * r), T(1e-3f) + T(1e-5f) * maxCoord);
+    const V3<T> po = ep + (pu * cosPhi + pv * sinPhi) * r - axis * halfLength;
+    T wSum = 0, selW = 0;
+    S4<T> selRd = sp(T(0));
+    float tMin = 0.f;
+    for (int k = 0; k < 8; ++k)
+    {
+        TriHit<float> th;
+        rays++;
+        if (!trace(c, po, axis, tMin, (float)(T(2) * halfLength), th, inst)) break;
+        const S4<T> rd = subsurfaceRd(s, len(po + axis * T(th.t) - ep));
+        const T w = rd[0] + rd[1] + rd[2] + rd[3];
+        wSum += w;
+        const T keep = wSum > T(0) ? w / wSum : T(0);
+        if (keep >= T(1) || uSel < keep)
+        {
+            uSel = keep >= T(1) ? uSel : uSel / keep;
+            selW = w;
+            selRd = rd;
+            sel = th;
+        }
+        else
+        {
+            uSel = (uSel - keep) / (T(1) - keep);
+        }
+        tMin = th.t + 5e-4f;
+    }
+    if (!(selW > T(0))) return false;
+    V3<T> q[3];
+    uint32_t qi[3];
+    triPositions(c, I, sel.prim, q, qi);
+    const V3<T> nOS = normalize(cross(q[1] - q[0], q[2] - q[0]));
+    const V3<T> nW = normalize(xVecT<T>(I.w2o, nOS));
+    const V3<T> frontN = ((dot(nW, axis) < T(0)) == sel.front) ? nW : -nW;
+    out.pos = po + axis * T(sel.t);
+    out.normal = entryFront ? frontN : -frontN;
+    out.pdfPos = pdfSssExit(s, ep, en, out.pos, out.normal);
+    if (!(out.pdfPos > T(0))) return false;
+    out.w = selRd / (out.pdfPos * (selW / wSum));
+    return true;
+}
+
 // spotFalloff / punctualLightAngularFalloff (lightSampling.hlsl:228-246) towards dirFromLight
 template <typename T> T spotFalloff(V3<T> dirFromLight, const float* axis, float cosIn, float cosOut)
 {
@@ -2454,77 +2537,12 @@ template <typename T> void tracePath(const Ctx<T>& c, const yg_render_params& P,
                     alive = false;
                     const V3<T> ep = hitPos;
                     const V3<T> en = dot(-ps.d, nWS) < T(0) ? -nWS : nWS; // orientToSameSide
-                    // sampleSubsurfaceExit (subsurface.hlsl:212-337)
-                    T u = rB[1];
-                    uint32_t axisIndex;
-                    if (u < T(0.5f)) { axisIndex = 0; u *= T(2); }
-                    else if (u < T(0.75f)) { axisIndex = 1; u = (u - T(0.5f)) * T(4); }
-                    else { axisIndex = 2; u = (u - T(0.75f)) * T(4); }
-                    uint32_t lane = std::min((uint32_t)(u * T(4)), 3u);
-                    T uSel = saturate(u * T(4) - T(lane));
-                    const T dLane = burleyD(s.sssRadius[lane], s.albedo[lane]);
-                    const T rMax = burleyRMax(dLane);
-                    const T r = burleySampleRadius(rB[2], dLane);
-                    bool ok = r < rMax;
-                    V3<T> exitPos, exitN;
-                    S4<T> exitW;
-                    T pdfPos = 0;
-                    TriHit<float> sel;
-                    sel.t = sel.b1 = sel.b2 = 0.f;
-                    sel.inst = h.inst;
-                    sel.prim = 0;
-                    sel.front = false;
-                    sel.found = false;
-                    if (ok)
-                    {
-                        V3<T> axis, pu, pv;
-                        probeFrame(en, axisIndex, axis, pu, pv);
-                        T sinPhi, cosPhi;
-                        Mth<T>::sincos(T(2) * C<T>::PI * rB[3], sinPhi, cosPhi);
-                        const T maxCoord = tmax(tmax(std::fabs(ep.x), std::fabs(ep.y)), std::fabs(ep.z));
-                        const T halfLength = tmax(Mth<T>::sqrt(rMax * rMax - r * r), T(1e-3f) + T(1e-5f) * maxCoord);
-                        const V3<T> po = ep + (pu * cosPhi + pv * sinPhi) * r - axis * halfLength;
-                        T wSum = 0, selW = 0;
-                        S4<T> selRd = sp(T(0));
-                        float tMin = 0.f;
-                        for (int k = 0; k < 8; ++k)
-                        {
-                            TriHit<float> th;
-                            rays++;
-                            if (!trace(c, po, axis, tMin, (float)(T(2) * halfLength), th, h.inst)) break;
-                            const S4<T> rd = subsurfaceRd(s, len(po + axis * T(th.t) - ep));
-                            const T w = rd[0] + rd[1] + rd[2] + rd[3];
-                            wSum += w;
-                            const T keep = wSum > T(0) ? w / wSum : T(0);
-                            if (keep >= T(1) || uSel < keep)
-                            {
-                                uSel = keep >= T(1) ? uSel : uSel / keep;
-                                selW = w;
-                                selRd = rd;
-                                sel = th;
-                            }
-                            else
-                            {
-                                uSel = (uSel - keep) / (T(1) - keep);
-                            }
-                            tMin = th.t + 5e-4f;
-                        }
-                        ok = selW > T(0);
-                        if (ok)
-                        {
-                            V3<T> q[3];
-                            uint32_t qi[3];
-                            triPositions(c, I, sel.prim, q, qi);
-                            const V3<T> nOS = normalize(cross(q[1] - q[0], q[2] - q[0]));
-                            const V3<T> nW = normalize(xVecT<T>(I.w2o, nOS));
-                            const V3<T> frontN = ((dot(nW, axis) < T(0)) == sel.front) ? nW : -nW;
-                            exitPos = po + axis * T(sel.t);
-                            exitN = h.front ? frontN : -frontN;
-                            pdfPos = pdfSssExit(s, ep, en, exitPos, exitN);
-                            ok = pdfPos > T(0);
-                            if (ok) exitW = selRd / (pdfPos * (selW / wSum));
-                        }
-                    }
+                    SssExit<T> ex;
+                    bool ok = sssSampleExit(c, s, I, h.inst, h.front, ep, en, rB[1], rB[2], rB[3], ex, rays);
+                    const V3<T> exitPos = ex.pos, exitN = ex.normal;
+                    const S4<T> exitW = ex.w;
+                    const T pdfPos = ex.pdfPos;
+                    const TriHit<float>& sel = ex.hit;
                     if (!ok)
                     {
                         // no exit point: the event has no direction, the path ends

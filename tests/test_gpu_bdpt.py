@@ -29,10 +29,12 @@ def bdpt_scene(name):
         return configs.box_scene(0), 0.0
     if name == "caustic":
         return configs.caustic_box_scene(1, n_spheres=24, n_lights=4, sphere_subdiv=2), 0.0
+    if name == "subsurface":
+        return configs.subsurface_box_scene(0), 0.0
     return configs.sky_scene(2), 1.0
 
 
-@pytest.mark.parametrize("name", ["box", "caustic", "sky"])
+@pytest.mark.parametrize("name", ["box", "caustic", "sky", "subsurface"])
 def test_bdpt_per_sample_parity_with_the_oracle(name, host_luts, built):
     import pyoracle
     sc, env = bdpt_scene(name)
@@ -42,7 +44,8 @@ def test_bdpt_per_sample_parity_with_the_oracle(name, host_luts, built):
                      light_vertices=10)
         gpu = c.render(p, dump=True)
     from yapt_gb300 import _native as N
-    rgb = N.host_table("rgb_to_spd", (380, 780)) if env > 0 else None  # the sky is an RGB emitter
+    # the sky is an RGB emitter; subsurface radii are RGB distances turned into spectra
+    rgb = N.host_table("rgb_to_spd", (380, 780)) if (env > 0 or name == "subsurface") else None
     orc = pyoracle.OracleSceneHandle(sc, host_luts, rgb_to_spd=rgb).render(p, precision=32)["records"]
     assert np.array_equal(gpu[..., 0], orc[..., 0]), "hero wavelengths differ"
     assert np.any(orc[..., 6] > 0), "degenerate scene"
@@ -84,6 +87,14 @@ def test_bdpt_agrees_with_nee_on_the_diffuse_box(built):
     with Context(0) as c:
         zmax, rel, se_b, se_n = compare_integrators(c, configs.box_scene(0), 32, 32, 256, 8)
         assert se_b < 1.5 * se_n, (se_b, se_n)
+
+
+def test_bdpt_agrees_with_nee_on_subsurface_materials(built):
+    # subsurface exits are path vertices of both subpaths (reached without a ray), connected
+    # through the exit lobe, and excluded from the MIS sums as connection points; NEE takes the
+    # whole subsurface event at the entry vertex. Both estimate the same image.
+    with Context(0) as c:
+        compare_integrators(c, configs.subsurface_box_scene(0), 32, 32, 512, 8, depth=8)
 
 
 def test_bdpt_agrees_with_nee_under_the_sky_without_lights(built):

@@ -3,8 +3,8 @@
 Per-sample parity with the FP32 oracle for the unidirectional and NEE integrators on a box
 whose blocks and three icospheres scatter below their surfaces: probe rays against the
 entry instance, the exit point's light connection and exit lobe. The megakernel and the
-wavefront give the same samples. The bidirectional integrator rejects subsurface materials
-with an error instead of rendering them without the subsurface layer.
+wavefront give the same samples. The bidirectional integrator's subsurface vertices are
+covered in test_gpu_bdpt.py (per-sample parity and agreement with NEE).
 """
 import numpy as np
 import pytest
@@ -49,11 +49,3 @@ def test_subsurface_megakernel_equals_wavefront(built):
         b = c.render(c.params("nee", 48, 40, spp=3, max_depth=8, lambda_range=(380, 780),
                               flags=256 | N.YG_FLAG_MEGAKERNEL), dump=True)
     assert np.array_equal(a, b)
-
-
-def test_bdpt_rejects_subsurface_materials(built):
-    with Context(0) as c:
-        c.upload_scene(configs.subsurface_box_scene(0))
-        c.film_clear(16, 16)
-        with pytest.raises(N.YaptError, match="subsurface"):
-            c.render(c.params("bdpt", 16, 16, spp=1, max_depth=4, lambda_range=(380, 780)))

@@ -118,3 +118,25 @@ def test_subsurface_oracle_is_deterministic_and_estimators_agree():
     fu = h.render(pyoracle.render_params("uni", 16, 16, spp=256, **kw), precision=32, records=False, film=True)["film"]
     fn = h.render(pyoracle.render_params("nee", 16, 16, spp=256, **kw), precision=32, records=False, film=True)["film"]
     assert abs(fu[..., 1].mean() - fn[..., 1].mean()) / fn[..., 1].mean() < 0.08
+
+
+def test_bdpt_subsurface_oracle_agrees_with_nee():
+    """Subsurface exits as BDPT vertices in the oracle: thread-independent, FP32 and FP64 agree
+    per sample, and the bidirectional image agrees with NEE's, which takes the whole subsurface
+    event at the entry vertex (a wrong MIS sum over the exit vertices would bias it)."""
+    import pyoracle
+    sc = configs.subsurface_box_scene(0)
+    h = pyoracle.OracleSceneHandle(sc, pyoracle.own_luts())
+    kw = dict(max_depth=8, lambda_range=(380, 780))
+    p = pyoracle.render_params("bdpt", 24, 24, spp=2, light_vertices=8, **kw)
+    h.ensure_rgb_table(p)
+    a = h.render(p, precision=32, threads=1)["records"]
+    b = h.render(p, precision=32, threads=6)["records"]
+    assert np.array_equal(a, b) and np.all(np.isfinite(a))
+    d = h.render(p, precision=64)["records"]
+    rel = np.abs(a[..., 5:8] - d[..., 5:8]) / np.maximum(np.abs(d[..., 5:8]), 1e-6)
+    assert np.mean(rel < 1e-3) > 0.99
+    fb = h.render(pyoracle.render_params("bdpt", 32, 32, spp=512, light_vertices=8, **kw), precision=32, records=False,
+                  film=True)["film"]
+    fn = h.render(pyoracle.render_params("nee", 32, 32, spp=512, **kw), precision=32, records=False, film=True)["film"]
+    assert abs(fb[..., 1].mean() - fn[..., 1].mean()) / fn[..., 1].mean() < 0.01

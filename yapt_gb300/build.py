@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I" + os.path.join(CUDA_HOME, "include"),
              "-Wall", "-Wno-unused-function"]
 
-# extra nvcc flags for experiments on variants (e.g. YG_NVCC_EXTRA="-DYG_EVAL_INLINE"); empty normally
+# extra nvcc flags for experiments on variants (e.g. YG_NVCC_EXTRA="-DYG_EVAL_OUTLINE"); empty normally
 NVCC_FLAGS += os.environ.get("YG_NVCC_EXTRA", "").split()
 
 CUDA_SOURCES = ["yg_integrator.cu", "yg_bdpt.cu", "yg_serve_kernels.cu", "yg_nn.cu", "yg_bvh_build.cu", "yg_atrous.cu", "yg_display.cu", "yg_capi.cu"]

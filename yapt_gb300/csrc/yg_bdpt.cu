@@ -32,6 +32,7 @@ constexpr uint32_t NF_FRONT = 1u << 1;
 constexpr uint32_t NF_ENV = 1u << 2;
 constexpr uint32_t NF_DELTA = 1u << 3;
 constexpr uint32_t NF_REGULARIZED = 1u << 4;
+constexpr uint32_t NF_SSS_EXIT = 1u << 5;   // reached through the subsurface from the previous node (no ray between)
 constexpr uint32_t NF_PUNCTUAL = 1u << 6;    // origin at a punctual light; prim holds the light index
 constexpr uint32_t NF_DIRECTIONAL = 1u << 7; // origin at a directional light (a point on its emitting disk)
 constexpr uint32_t NF_INFINITE = NF_ENV | NF_DIRECTIONAL; // isInfiniteLightNode: the normal holds the direction
@@ -39,6 +40,8 @@ constexpr float kMaxPdfRatioSum = 1e16f;    // MAX_PDF_RATIO_SUM
 constexpr float kVisibilityEps = 0.001f;    // VISIBILITY_RAY_EPSILON
 constexpr double kSplatScale = 16777216.0;  // fixed-point units per XYZ unit (2^24)
 constexpr int kGroupSize = 64;              // THREAD_GROUP_DIM_SIZE_CAM_RAY^2
+constexpr uint32_t kWbAtExit = 1u << 12;    // camera wave flags: this vertex is a subsurface exit,
+constexpr uint32_t kWbPrevExit = 1u << 13;  // the previous vertex was one
 
 // LightPathNode (BDPTCommon.hlsl:52-67): 80 bytes, the normal kept in FP32 (the reference
 // packs it to FP16 and spends the 4 bytes on a linked-list index instead).
@@ -230,6 +233,42 @@ __device__ __noinline__ ScatterEval evaluateBoth(const Luts& L, const Spectral& 
     return r;
 }
 
+// evaluateSubsurfaceExitAndPDFs (BDPTCommon.hlsl:463-472): forward the exit lobe; backward the
+// density of reaching the entry point from the exit through the subsurface, an area density
+// (the subsurface layer's probability for the reversed direction times the probe density)
+YG_DEV ScatterEval evaluateExitBoth(const Surface& s, const SurfaceCtx& c, float curIOR, float prevIOR, float3 wo, float3 wi,
+                                    bool front, bool fromLight, float3 exitPos, float3 exitN, float3 entryPos, float3 entryN)
+{
+    ScatterEval r;
+    evaluateSubsurfaceExitLobe(s, c, wo, wi, fromLight ? kEvalLightPath : kEvalNone, r.weight, r.pdfFwd);
+    SurfaceCtx rc;
+    makeSurfaceCtx(s, curIOR, prevIOR, wi, front, rc);
+    r.pdfBwd = rc.probs[LAYER_SSS] * pdfSubsurfaceExit(s, exitPos, exitN, entryPos, entryN);
+    r.transmission = 0;
+    return r;
+}
+
+// evaluateSubsurfaceEntry (scatteringSample.hlsl:67-79): forward an area density over the
+// subsurface edge (used as is by the exit vertex), backward the exit lobe's density of wo
+YG_DEV ScatterEval evaluateEntry(const Luts& L, const Spectral& sp, const Surface& s, const SurfaceCtx& c, float3 wo,
+                                 const SubsurfaceExit& ex)
+{
+    ScatterEval r;
+    r.weight = ex.weight * (subsurfaceEntryFactor(L, s, c, sp.hero) * ex.pdfPosition);
+    r.pdfFwd = c.probs[LAYER_SSS] * ex.pdfPosition;
+    float4 unused;
+    evaluateSubsurfaceExitLobe(s, c, wo, wo, kEvalPdfOnly, unused, r.pdfBwd);
+    r.transmission = 0;
+    return r;
+}
+
+// the probe rays of a subsurface entry, out of line: only vertices on subsurface materials run it
+static __device__ __noinline__ bool sampleExitOutOfLine(const SceneView& S, const Surface& s, const SurfacePoint& entry,
+                                                        float4 r, SubsurfaceExit& out)
+{
+    return sampleSubsurfaceExit(S, s, entry, mk3(r.y, r.z, r.w), out);
+}
+
 // the ray-state part of evaluateSurfaceAndPDFs; returns whether this event dispersed first
 YG_DEV bool applyTransmission(PathState& st, uint32_t trans, const Surface& s, uint32_t material)
 {
@@ -273,16 +312,51 @@ YG_DEV float4 transmittance(float4 ab, float d)
     return mk4(ygm_expf(-ab.x * d), ygm_expf(-ab.y * d), ygm_expf(-ab.z * d), ygm_expf(-ab.w * d));
 }
 
-// sampleScatteringEvent (scatteringSample.hlsl:30-65) for the local lobes; the subsurface
-// lobe ends the path as it does in the unidirectional integrators of this library
-YG_DEV float3 sampleScatter(const Luts& L, const Spectral& sp, const Surface& s, const SurfaceCtx& c, float4 r,
+// sampleScatteringEvent (scatteringSample.hlsl:30-65): at a subsurface exit only the exit lobe;
+// elsewhere a layer, and for the subsurface layer an exit point found by probe rays
+enum : uint32_t
+{
+    kEventNone = 0,
+    kEventLocal = 1,
+    kEventEntry = 2,
+    kEventExitLobe = 3
+};
+YG_DEV uint32_t sampleEvent(const SceneView& S, const Luts& L, const Spectral& sp, const Surface& s, const SurfaceCtx& c,
+                            float3 wo, float4 r, bool atExit, const SurfacePoint& vertex, float3& wi, SubsurfaceExit& ex,
                             bool& isDiffuse, bool& isDelta)
 {
-    int layer = selectMaterialLayer(r.x, c.probs);
+    wi = mk3(0.f, 0.f, 0.f);
     isDiffuse = false;
     isDelta = false;
-    if (layer == LAYER_SSS || layer >= LAYER_COUNT) return mk3(0.f, 0.f, 0.f);
-    return sampleLayerDirection<true>(L, s, c, layer, r.y, make_float2(r.z, r.w), sp.hero, isDiffuse, isDelta);
+    if (atExit)
+    {
+        wi = sampleSubsurfaceExitLobe(s, c, wo, make_float2(r.z, r.w));
+        isDiffuse = true;
+        return isZero3(wi) ? kEventNone : kEventExitLobe;
+    }
+    int layer = selectMaterialLayer(r.x, c.probs);
+    if (layer == LAYER_SSS)
+    {
+        isDiffuse = true;
+        return sampleExitOutOfLine(S, s, vertex, r, ex) ? kEventEntry : kEventNone;
+    }
+    if (layer >= LAYER_COUNT) return kEventNone;
+    wi = sampleLayerDirection<true>(L, s, c, layer, r.y, make_float2(r.z, r.w), sp.hero, isDiffuse, isDelta);
+    return isZero3(wi) ? kEventNone : kEventLocal;
+}
+
+// makeSurfacePoint (BDPTCommon.hlsl:523-533): the vertex with its normal on the side of wo
+YG_DEV SurfacePoint vertexPoint(float3 pos, float3 normalWS, float3 woWS, const Hit& hit)
+{
+    SurfacePoint p;
+    p.pos = pos;
+    p.normal = dot(woWS, normalWS) < 0.0f ? -normalWS : normalWS;
+    p.instance = hit.instance;
+    p.prim = hit.prim;
+    p.b1 = hit.b1;
+    p.b2 = hit.b2;
+    p.front = hit.front;
+    return p;
 }
 
 // calculateCommonSurfaceParams (BDPTCommon.hlsl:653-684) at a ray hit; the regularisation flag
@@ -469,11 +543,28 @@ __global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const L
         bool prevDelta = false;
         PathState st;
         initState(st);
+        // set when the previous vertex took the subsurface event: the next vertex is its exit
+        // point, reached without a ray (rayOrigin then holds the exit point, rayDir its inward
+        // normal, so that wo is the outward normal)
+        bool pendingExit = false;
+        SubsurfaceExit pex;
         for (uint32_t i = 1; i < B.maxLightVerts; ++i)
         {
             float4 rv = rs.r4();
             Hit hit;
-            if (!traceClosest<false>(S, rayOrigin, rayDir, kRayMinT, __int_as_float(0x7f800000), hit, nullptr)) break;
+            const bool atExit = pendingExit;
+            if (atExit)
+            {
+                hit.t = 0.0f;
+                hit.b1 = pex.exit.b1;
+                hit.b2 = pex.exit.b2;
+                hit.instance = pex.exit.instance;
+                hit.prim = pex.exit.prim;
+                hit.front = pex.exit.front;
+                pendingExit = false;
+            }
+            else if (!traceClosest<false>(S, rayOrigin, rayDir, kRayMinT, __int_as_float(0x7f800000), hit, nullptr))
+                break;
             LightNode& cur = nodes[i & 1];
             LightNode& prev = nodes[(i - 1) & 1];
             const GpuInstance& I = S.instances[hit.instance];
@@ -481,18 +572,29 @@ __global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const L
             uint32_t nflags = hit.front ? NF_FRONT : 0u;
             nflags |= (st.flags & kFlagSecondaryTerminated) ? NF_TERMINATED : 0u;
             nflags |= (st.flags & kFlagRegularize) ? NF_REGULARIZED : 0u;
+            nflags |= atExit ? NF_SSS_EXIT : 0u;
             HitSurface hs;
             SurfaceCtx c;
             vertexSurface(S, P, sp, hit, I, rayDir, st, hs, c);
             const Surface& s = hs.s;
-            if (isDeltaDistribution(c.a2, s)) nflags |= NF_DELTA;
+            // a subsurface exit has only the exit lobe
+            if (!atExit && isDeltaDistribution(c.a2, s)) nflags |= NF_DELTA;
             float3 normalWS = normalize(xformVectorT(I.w2o, s.geometryNormal));
+            // exit nodes keep the outward normal; connections set their surface up from it
+            if (atExit && dot(-rayDir, normalWS) < 0.0f) normalWS = -normalWS;
             float3 posWS = rayOrigin + rayDir * hit.t;
             float pdfFwdMIS;
-            if (i == 1 && originInfinite) pdfFwdMIS = originPosPdf * fabsf(dot(rayDir, normalWS));
-            else pdfFwdMIS = prevDelta ? -1.0f : pdfForward * solidAngleToArea(posWS - rayOrigin, normalWS);
-            float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
-            if (!allEqual4(ab, 0.0f)) radiance = radiance * transmittance(ab, hit.t);
+            if (atExit)
+            {
+                pdfFwdMIS = pdfForward; // the subsurface edge's density is an area density already
+            }
+            else
+            {
+                if (i == 1 && originInfinite) pdfFwdMIS = originPosPdf * fabsf(dot(rayDir, normalWS));
+                else pdfFwdMIS = prevDelta ? -1.0f : pdfForward * solidAngleToArea(posWS - rayOrigin, normalWS);
+                float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
+                if (!allEqual4(ab, 0.0f)) radiance = radiance * transmittance(ab, hit.t);
+            }
             cur.instance = hit.instance;
             cur.prim = hit.prim;
             cur.bary = make_float2(hit.b1, hit.b2);
@@ -507,14 +609,23 @@ __global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const L
             cur.pad = 0.0f;
             bool isDiffuse, sDelta;
             float3 wo = -hs.rayDirOS;
-            float3 wi = sampleScatter(Lt, sp, s, c, rv, isDiffuse, sDelta);
-            if (isZero3(wi)) break;
+            float3 wi;
+            SubsurfaceExit nex;
+            const uint32_t event = sampleEvent(S, Lt, sp, s, c, wo, rv, atExit, vertexPoint(posWS, normalWS, -rayDir, hit), wi, nex,
+                                               isDiffuse, sDelta);
+            if (event == kEventNone) break;
             if (isDiffuse) st.flags |= kFlagRegularize;
-            ScatterEval ev = evaluateBoth(Lt, sp, s, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, true, sDelta);
+            ScatterEval ev;
+            if (event == kEventEntry) ev = evaluateEntry(Lt, sp, s, c, wo, nex);
+            else if (event == kEventExitLobe)
+                ev = evaluateExitBoth(s, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, true, posWS, normalWS, prev.pos,
+                                      prev.normal);
+            else ev = evaluateBoth(Lt, sp, s, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, true, sDelta);
             bool dispersed = applyTransmission(st, ev.transmission, s, hs.material);
             pdfForward = ev.pdfFwd;
             float4 w = ev.weight * safeDiv(1.0f, pdfForward);
-            prev.pdfBwd = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - posWS, prev.normal);
+            if (event == kEventExitLobe) prev.pdfBwd = ev.pdfBwd; // an area density
+            else prev.pdfBwd = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - posWS, prev.normal);
             if (i == 1 && originPunctual) prev.pdfBwd = 0.0f; // a camera path never hits a delta light
             else if (i == 1 && originEnv && !sDelta) prev.pdfBwd = ev.pdfBwd;
             out[stored++] = prev;
@@ -525,8 +636,18 @@ __global__ void __launch_bounds__(128) bdptLightPaths(const SceneView S, const L
             if (rs.r1() > p) break;
             radiance = radiance * (1.0f / p);
             if (allEqual4(radiance, 0.0f)) break;
-            rayDir = normalize(xformVectorT(I.w2o, wi));
-            rayOrigin = spawnRayOrigin(posWS, normalWS, rayDir);
+            if (event == kEventEntry)
+            {
+                pendingExit = true;
+                pex = nex;
+                rayOrigin = nex.exit.pos;
+                rayDir = -nex.exit.normal;
+            }
+            else
+            {
+                rayDir = normalize(xformVectorT(I.w2o, wi));
+                rayOrigin = spawnRayOrigin(posWS, normalWS, rayDir);
+            }
             prevDelta = sDelta;
         }
         // the last vertex reached (BDPTTraceLightPath.comp:335-352)
@@ -588,6 +709,7 @@ struct SharedNode
     Surface s;
     SurfaceCtx c;
     float4 w2o[3];
+    float3 prevPos, prevNormal; // the previous vertex (the entry point of a subsurface exit)
     float3 woOS;
     uint32_t material;
     float emissionFocus;
@@ -595,9 +717,11 @@ struct SharedNode
 };
 
 YG_DEV void prepareSharedNode(const SceneView& S, const LaunchParams& P, const Spectral& sp, const LightNode& src,
-                              float3 prevPos, uint32_t index, SharedNode& d)
+                              float3 prevPos, float3 prevNormal, uint32_t index, SharedNode& d)
 {
     d.n = src;
+    d.prevPos = prevPos;
+    d.prevNormal = prevNormal;
     if (src.flags & (NF_ENV | NF_PUNCTUAL)) return; // light origins without a surface
     const GpuInstance& I = S.instances[src.instance];
     d.w2o[0] = I.w2o[0];
@@ -609,7 +733,8 @@ YG_DEV void prepareSharedNode(const SceneView& S, const LaunchParams& P, const S
     d.twoSided = M.mask & 1u;
     if (index == 0) return;
     // fillSurfaceDefRGB + regularizeMaterial + convertSurfaceDefinitionFromRGB, no two-sided
-    // orientation (BDPTCommon.hlsl:845-869)
+    // orientation (BDPTCommon.hlsl:845-869); a subsurface exit is oriented to wo, its stored
+    // outward normal (BDPTCommon.hlsl:800-823)
     Hit h;
     h.instance = src.instance;
     h.prim = src.prim;
@@ -623,11 +748,19 @@ YG_DEV void prepareSharedNode(const SceneView& S, const LaunchParams& P, const S
     LaunchParams Pn = P;
     Pn.regularizeAfter = 0xffffffffu;
     HitSurface hs;
-    setupSurface(S, Pn, sp, h, I, src.normal, st, hs, false);
+    const bool exitNode = (src.flags & NF_SSS_EXIT) != 0;
+    setupSurface(S, Pn, sp, h, I, exitNode ? -src.normal : src.normal, st, hs, exitNode);
     d.s = hs.s;
-    float3 lpos = xformPoint(I.w2o, src.pos);
-    float3 ppos = xformPoint(I.w2o, prevPos);
-    d.woOS = normalize(ppos - lpos);
+    if (exitNode)
+    {
+        d.woOS = normalize(xformVector(I.w2o, src.normal));
+    }
+    else
+    {
+        float3 lpos = xformPoint(I.w2o, src.pos);
+        float3 ppos = xformPoint(I.w2o, prevPos);
+        d.woOS = normalize(ppos - lpos);
+    }
     makeSurfaceCtx(d.s, src.iorCur, src.iorPrev, d.woOS, h.front, d.c);
 }
 
@@ -709,6 +842,14 @@ YG_DEV bool lightEndOfConnection(const SceneView& S, const BdptParams& B, const 
     float3 cpos = xformPoint(sn.w2o, nextPos);
     float3 wi = normalize(cpos - lpos);
     bool front = (n.flags & NF_FRONT) != 0;
+    if (n.flags & NF_SSS_EXIT)
+    {
+        // the exit lobe; the backward density is an area density over the subsurface edge
+        ev = evaluateExitBoth(sn.s, sn.c, n.iorCur, n.iorPrev, sn.woOS, wi, front, true, n.pos, n.normal, sn.prevPos,
+                              sn.prevNormal);
+        pdfFwdMIS = ev.pdfFwd;
+        return !(ev.pdfBwd == 0.0f || allEqual4(ev.weight, 0.0f));
+    }
     ev = evaluateBoth(Lt, sp, sn.s, sn.c, n.iorCur, n.iorPrev, sn.woOS, wi, front, true, false);
     bool terminated = alreadyTerminated || (n.flags & NF_TERMINATED);
     if ((ev.transmission & kTransDispersed) && !terminated) terminateSecondary(ev.weight);
@@ -720,12 +861,13 @@ struct CamVertex
 {
     float3 pos, normal, prevPos, prevNormal;
     float pdfRatioSum, prevPdfFwd, curPdfFwd;
+    bool isExit, prevIsExit; // reached through the subsurface (no ray led to the vertex)
 };
 struct LightVertexCtx
 {
     float3 prevPos, prevNormal;
     float prevPdfFwd, riSum;
-    uint32_t originFlags;
+    uint32_t originFlags, prevFlags;
 };
 
 // calculateMISWeight (BDPTCommon.hlsl:918-1006)
@@ -734,11 +876,15 @@ YG_DEV float misWeight(const SceneView& S, uint32_t camIndex, const CamVertex& c
 {
     float riCam = cv.pdfRatioSum;
     if (camIndex > 0)
-        riCam = accumulateRISum(riCam, bwdCam * solidAngleToArea(cv.prevPos - cv.pos, cv.prevNormal), cv.prevPdfFwd);
+    {
+        // from a subsurface exit the backward density is an area density already
+        float bwd = cv.isExit ? bwdCam : bwdCam * solidAngleToArea(cv.prevPos - cv.pos, cv.prevNormal);
+        riCam = accumulateRISum(riCam, bwd, cv.prevPdfFwd, !cv.prevIsExit);
+    }
     const bool env0 = lightIndex == 0 && (ln.flags & NF_ENV);
     const bool inf0 = lightIndex == 0 && (ln.flags & NF_INFINITE);
     float toCamArea = inf0 ? fwdLight * fabsf(dot(cv.normal, ln.normal)) : fwdLight * solidAngleToArea(cv.pos - ln.pos, cv.normal);
-    riCam = accumulateRISum(riCam, toCamArea, cv.curPdfFwd);
+    riCam = accumulateRISum(riCam, toCamArea, cv.curPdfFwd, !cv.isExit);
     float riLight = lv.riSum;
     if (lightIndex == 0)
     {
@@ -768,12 +914,14 @@ YG_DEV float misWeight(const SceneView& S, uint32_t camIndex, const CamVertex& c
     else
     {
         float bwdPrev = bwdLight;
+        const bool lnExit = (ln.flags & NF_SSS_EXIT) != 0;
+        const bool prevExit = (lv.prevFlags & NF_SSS_EXIT) != 0;
         bool prevEnv = lightIndex == 1 && (lv.originFlags & NF_ENV);
         bool prevPunctual = lightIndex == 1 && (lv.originFlags & NF_PUNCTUAL);
         if (prevPunctual) bwdPrev = 0.0f;
-        else if (!prevEnv) bwdPrev *= solidAngleToArea(lv.prevPos - ln.pos, lv.prevNormal);
-        riLight = accumulateRISum(riLight, bwdPrev, lv.prevPdfFwd);
-        riLight = accumulateRISum(riLight, fwdCam * solidAngleToArea(ln.pos - cv.pos, ln.normal), ln.pdfFwd);
+        else if (!prevEnv && !lnExit) bwdPrev *= solidAngleToArea(lv.prevPos - ln.pos, lv.prevNormal);
+        riLight = accumulateRISum(riLight, bwdPrev, lv.prevPdfFwd, !prevExit);
+        riLight = accumulateRISum(riLight, fwdCam * solidAngleToArea(ln.pos - cv.pos, ln.normal), ln.pdfFwd, !lnExit);
     }
     return 1.0f / (1.0f + riCam + riLight);
 }
@@ -806,6 +954,7 @@ struct BdptWave
     uint4* misc;         // flags | volumes << 16, sampler dimension, sampler seed, frame
     uint4* misc2;        // permutation slot pixel, light path, light vertex count
     uint2* conn;         // this bounce's connection records: first, count
+    float4* exitHit;     // a pending subsurface exit: barycentrics, instance, primitive | front << 31
     float4* volIOR;
     uint4* volMat;
     float4* volAbs;      // [k * capacity + slot]
@@ -867,7 +1016,8 @@ __global__ void __launch_bounds__(128) wbPrepare(const SceneView S, const Launch
         Spectral sp;
         spectralOf(S, B.heroes[pl], sp);
         const LightNode* src = B.nodes + pl * B.maxLightVerts;
-        prepareSharedNode(S, P, sp, src[k], k ? src[k - 1].pos : src[0].pos, k, W.prep[i]);
+        prepareSharedNode(S, P, sp, src[k], k ? src[k - 1].pos : src[0].pos, k ? src[k - 1].normal : src[0].normal, k,
+                          W.prep[i]);
     }
 }
 
@@ -946,7 +1096,9 @@ __global__ void __launch_bounds__(128) wbGenerate(const SceneView S, const Launc
     if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = W.n;
 }
 
-__global__ void __launch_bounds__(128) wbTrace(const SceneView S, RayQueue Q, HitQueue H)
+// closest hits of the queued camera rays; a queued subsurface exit (d.w = 1) is not traced, its
+// hit is the exit point stored by the vertex that took the subsurface event
+__global__ void __launch_bounds__(128) wbTrace(const SceneView S, RayQueue Q, HitQueue H, const float4* exitHit)
 {
     TraversalCount tc{0, 0};
     uint32_t rays = 0;
@@ -954,9 +1106,16 @@ __global__ void __launch_bounds__(128) wbTrace(const SceneView S, RayQueue Q, Hi
         *Q.count,
         [&](TraceState& t, uint32_t i) {
             const float4 o = Q.o[i], d = Q.d[i];
-            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000));
+            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w != 0.0f ? 0.0f : __int_as_float(0x7f800000));
         },
         [&](const TraceState& t, uint32_t i) {
+            if (Q.d[i].w != 0.0f)
+            {
+                const float4 e = exitHit[__float_as_uint(Q.o[i].w)];
+                H.a[i] = mk4(0.0f, e.x, e.y, e.z);
+                H.b[i] = __float_as_uint(e.w);
+                return;
+            }
             H.a[i] = mk4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.instance));
             H.b[i] = t.found ? (t.h.prim | (t.h.front ? 0x80000000u : 0u)) : 0xffffffffu;
         },
@@ -1003,8 +1162,10 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
             count = m2.z;
             initState(st);
             st.throughput = W.thr[s];
-            st.flags = m.x & 0xffffu;
+            st.flags = m.x & 0x0fffu;
             st.nVol = m.x >> 16;
+            cv.isExit = (m.x & kWbAtExit) != 0;
+            cv.prevIsExit = (m.x & kWbPrevExit) != 0;
             wbLoadVolumes(W, s, st);
             rs = RandomSampler{S.sobol + (size_t)f * kSobolDims, m.y, m.z};
             const float4 a = W.cv0[s], b = W.cv1[s], e = W.cv2[s];
@@ -1033,7 +1194,8 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                 float mis = 1.0f;
                 if (ci > 0)
                 {
-                    float ri = accumulateRISum(cv.pdfRatioSum, pdfEnvPosition(B) * fabsf(dot(cv.prevNormal, rayDir)), cv.prevPdfFwd);
+                    float ri = accumulateRISum(cv.pdfRatioSum, pdfEnvPosition(B) * fabsf(dot(cv.prevNormal, rayDir)), cv.prevPdfFwd,
+                                               !cv.prevIsExit);
                     ri = accumulateRISum(ri, envSelectionPdf(S) * pdfEnvDirection(-rayDir), cv.curPdfFwd);
                     mis = 1.0f / (1.0f + ri);
                 }
@@ -1054,11 +1216,20 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                     W.fhAlb[s] = mk4(hs.albedoRGB.x, hs.albedoRGB.y, hs.albedoRGB.z, 0.0f);
                     W.fhNrm[s] = mk4(nn.x, nn.y, nn.z, vp.z * S.cam.forwardZSign);
                 }
-                delta = isDeltaDistribution(c.a2, sf);
-                cv.curPdfFwd = pdfFwdCam < 0.0f ? -1.0f : pdfFwdCam * solidAngleToArea(cv.pos - rayOrigin, cv.normal);
-                float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
-                if (!allEqual4(ab, 0.0f)) st.throughput = st.throughput * transmittance(ab, hit.t);
-                if (!allEqual4(sf.emissive, 0.0f))
+                // a subsurface exit has only the exit lobe, and the density of reaching it is an
+                // area density already; its emission was accounted for at the entry point
+                delta = !cv.isExit && isDeltaDistribution(c.a2, sf);
+                if (cv.isExit)
+                {
+                    cv.curPdfFwd = pdfFwdCam;
+                }
+                else
+                {
+                    cv.curPdfFwd = pdfFwdCam < 0.0f ? -1.0f : pdfFwdCam * solidAngleToArea(cv.pos - rayOrigin, cv.normal);
+                    float4 ab = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
+                    if (!allEqual4(ab, 0.0f)) st.throughput = st.throughput * transmittance(ab, hit.t);
+                }
+                if (!cv.isExit && !allEqual4(sf.emissive, 0.0f))
                 {
                     // calculateMISWeightOnCameraPathHittingLight (BDPTCommon.hlsl:1008-1035)
                     float mis = 1.0f;
@@ -1067,7 +1238,8 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                         float3 towards = cv.prevPos - cv.pos;
                         float pick, posPdf, dirPdf;
                         pdfForSamplingLight(S, hit.instance, hit.prim, cv.normal, normalize(towards), pick, posPdf, dirPdf);
-                        float ri = accumulateRISum(cv.pdfRatioSum, dirPdf * solidAngleToArea(towards, cv.prevNormal), cv.prevPdfFwd);
+                        float ri = accumulateRISum(cv.pdfRatioSum, dirPdf * solidAngleToArea(towards, cv.prevNormal), cv.prevPdfFwd,
+                                                   !cv.prevIsExit);
                         ri = accumulateRISum(ri, pick * posPdf, cv.curPdfFwd);
                         mis = 1.0f / (1.0f + ri);
                     }
@@ -1099,6 +1271,7 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
             lv.prevPos = mk3(0.f, 0.f, 0.f);
             lv.prevNormal = mk3(0.f, 0.f, 0.f);
             lv.prevPdfFwd = 0.0f;
+            lv.prevFlags = 0;
             float deferredLight = 0.0f;
             const bool camTerminated = (st.flags & kFlagSecondaryTerminated) != 0;
             for (uint32_t li = 0; li < count; ++li)
@@ -1129,7 +1302,10 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                     const float3 wi = normalize(xformVector(I->w2o, toLightDir));
                     const bool lightTerminated = (ln.flags & NF_TERMINATED) != 0;
                     const bool terminatedBefore = camTerminated || lightTerminated;
-                    ScatterEval ce = evaluateBoth(Lt, sp, sf, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, false, false);
+                    ScatterEval ce = cv.isExit ? evaluateExitBoth(sf, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, false,
+                                                                  cv.pos, cv.normal, cv.prevPos, cv.prevNormal)
+                                               : evaluateBoth(Lt, sp, sf, c, currentIOR(st), previousIOR(st), wo, wi, hit.front,
+                                                              false, false);
                     if ((ce.transmission & kTransDispersed) && !terminatedBefore) terminateSecondary(ce.weight);
                     if (ce.pdfFwd != 0.0f && !allEqual4(ce.weight, 0.0f))
                     {
@@ -1162,25 +1338,34 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                 W.C.target[e] = target;
                 W.C.contrib[e] = contrib;
                 lv.riSum = deferredLight;
-                deferredLight = accumulateRISum(deferredLight, ln.pdfBwd, ln.pdfFwd);
+                deferredLight = accumulateRISum(deferredLight, ln.pdfBwd, ln.pdfFwd, !(ln.flags & NF_SSS_EXIT));
                 lv.prevNormal = ln.normal;
                 lv.prevPos = ln.pos;
                 lv.prevPdfFwd = ln.pdfFwd;
+                lv.prevFlags = ln.flags;
                 if (li == 0) lv.originFlags = ln.flags;
             }
         }
-        bool cont = false;
+        bool cont = false, toExit = false;
         if (alive)
         {
             // the scattered continuation (rv was drawn right after the trace)
             const Surface& sf = hs.s;
             const float3 wo = -hs.rayDirOS;
             bool isDiffuse, sDelta;
-            float3 wiS = sampleScatter(Lt, sp, sf, c, rv, isDiffuse, sDelta);
-            if (!isZero3(wiS))
+            float3 wiS;
+            SubsurfaceExit ex;
+            const uint32_t event = sampleEvent(S, Lt, sp, sf, c, wo, rv, cv.isExit, vertexPoint(cv.pos, cv.normal, -rayDir, hit), wiS,
+                                               ex, isDiffuse, sDelta);
+            if (event != kEventNone)
             {
                 if (isDiffuse) st.flags |= kFlagRegularize;
-                ScatterEval ev = evaluateBoth(Lt, sp, sf, c, currentIOR(st), previousIOR(st), wo, wiS, hit.front, false, sDelta);
+                ScatterEval ev;
+                if (event == kEventEntry) ev = evaluateEntry(Lt, sp, sf, c, wo, ex);
+                else if (event == kEventExitLobe)
+                    ev = evaluateExitBoth(sf, c, currentIOR(st), previousIOR(st), wo, wiS, hit.front, false, cv.pos, cv.normal,
+                                          cv.prevPos, cv.prevNormal);
+                else ev = evaluateBoth(Lt, sp, sf, c, currentIOR(st), previousIOR(st), wo, wiS, hit.front, false, sDelta);
                 bool dispersed = applyTransmission(st, ev.transmission, sf, hs.material);
                 float4 w = ev.weight * safeDiv(1.0f, ev.pdfFwd);
                 if (dispersed) terminateSecondary(st.throughput);
@@ -1188,8 +1373,10 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                 {
                     if (ci > 0)
                     {
-                        float bwdPrev = sDelta ? -1.0f : ev.pdfBwd * solidAngleToArea(rayOrigin - cv.pos, cv.prevNormal);
-                        deferredRI = accumulateRISum(deferredRI, bwdPrev, cv.prevPdfFwd);
+                        float bwdPrev = sDelta ? -1.0f
+                                               : (event == kEventExitLobe ? ev.pdfBwd
+                                                                          : ev.pdfBwd * solidAngleToArea(rayOrigin - cv.pos, cv.prevNormal));
+                        deferredRI = accumulateRISum(deferredRI, bwdPrev, cv.prevPdfFwd, !cv.prevIsExit);
                         cv.pdfRatioSum = deferredRI;
                     }
                     cv.prevNormal = cv.normal;
@@ -1197,8 +1384,20 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                     cv.prevPdfFwd = cv.curPdfFwd;
                     pdfFwdCam = sDelta ? -1.0f : ev.pdfFwd;
                     st.throughput = st.throughput * w;
-                    rayDir = normalize(xformVectorT(I->w2o, wiS));
-                    rayOrigin = spawnRayOrigin(cv.pos, cv.normal, rayDir);
+                    if (event == kEventEntry)
+                    {
+                        // the next vertex is the exit point: queued without a ray to trace
+                        toExit = true;
+                        rayOrigin = ex.exit.pos;
+                        rayDir = -ex.exit.normal;
+                        W.exitHit[s] = mk4(ex.exit.b1, ex.exit.b2, __uint_as_float(ex.exit.instance),
+                                           __uint_as_float(ex.exit.prim | (ex.exit.front ? 0x80000000u : 0u)));
+                    }
+                    else
+                    {
+                        rayDir = normalize(xformVectorT(I->w2o, wiS));
+                        rayOrigin = spawnRayOrigin(cv.pos, cv.normal, rayDir);
+                    }
                     cont = ci + 1 < P.maxDepth;
                 }
             }
@@ -1209,7 +1408,8 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
                 W.cv0[s] = mk4(cv.prevPos.x, cv.prevPos.y, cv.prevPos.z, cv.pdfRatioSum);
                 W.cv1[s] = mk4(cv.prevNormal.x, cv.prevNormal.y, cv.prevNormal.z, cv.prevPdfFwd);
                 W.cv2[s] = mk4(deferredRI, pdfFwdCam, sp.hero, 0.0f);
-                W.misc[s] = make_uint4(st.flags | (st.nVol << 16), rs.dim, rs.seed, f);
+                W.misc[s] = make_uint4(st.flags | (toExit ? kWbAtExit : 0u) | (cv.isExit ? kWbPrevExit : 0u) | (st.nVol << 16),
+                                       rs.dim, rs.seed, f);
                 wbStoreVolumes(W, s, st);
             }
         }
@@ -1217,7 +1417,7 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
         if (cont)
         {
             Qout.o[o] = mk4(rayOrigin.x, rayOrigin.y, rayOrigin.z, __uint_as_float(s));
-            Qout.d[o] = mk4(rayDir.x, rayDir.y, rayDir.z, 0.0f);
+            Qout.d[o] = mk4(rayDir.x, rayDir.y, rayDir.z, toExit ? 1.0f : 0.0f);
         }
     }
 }
@@ -1323,6 +1523,7 @@ __global__ void __launch_bounds__(128) bdptLightTrace(const SceneView S, const L
         float3 prevPos = n0.pos, prevNormal = n0.normal;
         float prevPdfFwd = n0.pdfFwd;
         const uint32_t originFlags = n0.flags;
+        uint32_t prevFlags = n0.flags;
         float riSum = 0.0f;
         float deferred = accumulateRISum(0.0f, n0.pdfBwd, n0.pdfFwd);
         for (uint32_t i = 1; i < vCount; ++i)
@@ -1347,7 +1548,7 @@ __global__ void __launch_bounds__(128) bdptLightTrace(const SceneView S, const L
             if (onScreen && inCrop && !(n.flags & NF_DELTA))
             {
                 SharedNode sn;
-                prepareSharedNode(S, P, sp, n, prevPos, i, sn);
+                prepareSharedNode(S, P, sp, n, prevPos, prevNormal, i, sn);
                 ScatterEval ev;
                 float unused;
                 if (lightEndOfConnection(S, B, Lt, sp, sn, i, lensWS, false, ev, unused) && !isZero4(ev.weight))
@@ -1363,12 +1564,14 @@ __global__ void __launch_bounds__(128) bdptLightTrace(const SceneView S, const L
                     if (visible)
                     {
                         bool prevEnv = i == 1 && (originFlags & NF_ENV);
-                        float bwdPrev = ev.pdfBwd * (prevEnv ? 1.0f : solidAngleToArea(prevPos - n.pos, prevNormal));
+                        const bool nodeExit = (n.flags & NF_SSS_EXIT) != 0;
+                        // from a subsurface exit the backward density is an area density already
+                        float bwdPrev = ev.pdfBwd * ((prevEnv || nodeExit) ? 1.0f : solidAngleToArea(prevPos - n.pos, prevNormal));
                         if (i == 1 && (originFlags & NF_PUNCTUAL)) bwdPrev = 0.0f; // a camera path never hits a delta light
                         float3 camToNode = n.pos - lensWS;
                         float pdfCam = cameraDirectionalPdf(S, P, camToNode);
-                        float ri = accumulateRISum(riSum, bwdPrev, prevPdfFwd);
-                        ri = accumulateRISum(ri, pdfCam * solidAngleToArea(camToNode, n.normal), n.pdfFwd);
+                        float ri = accumulateRISum(riSum, bwdPrev, prevPdfFwd, !(prevFlags & NF_SSS_EXIT));
+                        ri = accumulateRISum(ri, pdfCam * solidAngleToArea(camToNode, n.normal), n.pdfFwd, !nodeExit);
                         float mis = 1.0f / (1.0f + ri);
                         float G = 1.0f / fmaxf(0.0001f, dot(camToNode, camToNode));
                         float importance = safeDiv(pdfCam, (float)hc);
@@ -1387,7 +1590,8 @@ __global__ void __launch_bounds__(128) bdptLightTrace(const SceneView S, const L
                 }
             }
             riSum = deferred;
-            deferred = accumulateRISum(deferred, n.pdfBwd, n.pdfFwd);
+            deferred = accumulateRISum(deferred, n.pdfBwd, n.pdfFwd, !(n.flags & NF_SSS_EXIT));
+            prevFlags = n.flags;
             prevPos = n.pos;
             prevNormal = n.normal;
             prevPdfFwd = n.pdfFwd;
@@ -1444,7 +1648,7 @@ WaveShape waveShape(uint32_t frames, uint64_t cropPixels)
 }
 // per path: state (5 x 16 + 2 x 16 + 8 + volumes 96 + features 32), two ray queues (64), hits
 // (20), the regrouped ray and hit queues (52) and the class key (1)
-size_t waveSlotBytes() { return 5 * 16 + 2 * 16 + 8 + 16 + 16 + 64 + 2 * 16 + 2 * 32 + 20 + 52 + 1; }
+size_t waveSlotBytes() { return 5 * 16 + 2 * 16 + 8 + 16 + 16 + 16 + 64 + 2 * 16 + 2 * 32 + 20 + 52 + 1; }
 } // namespace
 
 size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVerts, uint64_t cropPixels)
@@ -1501,6 +1705,7 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
     W.misc = reinterpret_cast<uint4*>(take(C * 16));
     W.misc2 = reinterpret_cast<uint4*>(take(C * 16));
     W.conn = reinterpret_cast<uint2*>(take(C * 8));
+    W.exitHit = reinterpret_cast<float4*>(take(C * 16));
     W.volIOR = reinterpret_cast<float4*>(take(C * 16));
     W.volMat = reinterpret_cast<uint4*>(take(C * 16));
     W.volAbs = reinterpret_cast<float4*>(take(C * 64));
@@ -1545,7 +1750,7 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
         RayQueue* nxt = &QB;
         for (uint32_t ci = 0; ci < P.maxDepth; ++ci)
         {
-            wbTrace<<<traceBlocks, 128, 0, stream>>>(S, *cur, H);
+            wbTrace<<<traceBlocks, 128, 0, stream>>>(S, *cur, H, W.exitHit);
             cudaMemsetAsync(nxt->count, 0, 4, stream);
             cudaMemsetAsync(W.connCount, 0, 4, stream);
             // shading coherence: hits grouped by material class before the vertex pass

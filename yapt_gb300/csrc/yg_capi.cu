@@ -294,13 +294,6 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.d65SumInv = ctx->d65SumInv;
 }
 
-bool sceneHasSubsurface(const yg_context* c)
-{
-    for (const yg_material& m : c->materials)
-        if (m.subsurface_amount > 0.0f) return true;
-    return false;
-}
-
 int checkMaterialTextures(const yg_context* c, const char* what)
 {
     const size_t nTex = c->texTable.size();
@@ -1078,9 +1071,6 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
 
     const uint64_t npix = (uint64_t)cw * ch;
     const bool bdpt = p->integrator == YG_INTEGRATOR_BDPT;
-    if (bdpt && sceneHasSubsurface(ctx))
-        return fail(YG_ERR_INVALID_ARGUMENT, "render: the bidirectional integrator does not handle subsurface materials "
-                                             "(render them with the unidirectional or NEE integrator)");
     const uint64_t maxSamplesPerChunk = bdpt ? (1ull << 24) : (1ull << 26);
     uint32_t chunkSpp = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(p->spp_count, maxSamplesPerChunk / npix));
     if (bdpt && (p->flags & YG_FLAG_MEGAKERNEL)) return fail(YG_ERR_INVALID_ARGUMENT, "render: BDPT has no megakernel variant");

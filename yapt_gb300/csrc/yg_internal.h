@@ -178,8 +178,6 @@ int checkWideBvhStructure(yg_context* c);
 // Fails (naming `what`) when a material refers to a texture id that is not resident, e.g.
 // after yg_clear_textures: the device texture table then holds freed pointers.
 int checkMaterialTextures(const yg_context* c, const char* what);
-// whether a material of the context scatters below the surface (subsurface amount above 0)
-bool sceneHasSubsurface(const yg_context* c);
 // the pixel order of the BDPT camera groups for a cw x ch crop
 void pixelPermutation(uint32_t cw, uint32_t ch, std::vector<uint32_t>& perm);
 } // namespace ygi

@@ -220,8 +220,6 @@ int validate(yg_server* s, const yg_request* q, Req& r)
     r.bdpt = p.integrator == YG_INTEGRATOR_BDPT;
     if (!r.bdpt && p.max_depth > s->opt.max_depth) return fail(YG_ERR_INVALID_ARGUMENT, "serve: max_depth above the server's");
     yg_context* ctx = s->scenes[q->scene];
-    if (r.bdpt && sceneHasSubsurface(ctx))
-        return fail(YG_ERR_INVALID_ARGUMENT, "serve: the bidirectional integrator does not handle subsurface materials");
     r.needRgb = sceneNeedsRgbLut(ctx, p.env_intensity_scale);
     r.scene = q->scene;
     r.p = p;
