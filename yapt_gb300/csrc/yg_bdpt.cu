@@ -714,6 +714,12 @@ struct SharedNode
     uint32_t material;
     float emissionFocus;
     uint32_t twoSided;
+    // the light subpath's MIS context of a connection to this vertex (LightVertexContext of
+    // traceCameraRays, which depends on the light path only): the ratio sum of the vertices
+    // before the previous one, the previous vertex, and the flags of the path's origin
+    float lvRiSum, lvPrevPdfFwd;
+    float3 lvPrevPos, lvPrevNormal;
+    uint32_t lvPrevFlags, lvOriginFlags;
 };
 
 YG_DEV void prepareSharedNode(const SceneView& S, const LaunchParams& P, const Spectral& sp, const LightNode& src,
@@ -939,6 +945,27 @@ YG_DEV float misWeight(const SceneView& S, uint32_t camIndex, const CamVertex& c
 // picked per (sample index, group) as in the reference. The light vertices' spectral surfaces
 // and forward frames are prepared once per wave in global memory (they depend only on the
 // light path and its hero wavelength, which the group shares).
+// a connecting camera vertex as its connections read it (calculateLightPathRadiance's camera
+// side: CameraVertexContext and the ray state at the vertex)
+struct alignas(16) ConnVertex
+{
+    float4 thr;       // throughput at the vertex
+    float4 absNone;   // absorption along a connection that stays in the current medium
+    float4 absExited; // and along one whose camera end leaves it
+    float3 pos;
+    uint32_t flags; // path flags at the vertex, kWbAtExit / kWbPrevExit
+    float3 normal;
+    float curPdfFwd;
+    float3 prevPos;
+    float pdfRatioSum;
+    float3 prevNormal;
+    float prevPdfFwd;
+    float3 wo; // object space
+    float hero;
+    float curIOR, prevIOR;
+    uint32_t instance, front;
+};
+
 struct BdptWave
 {
     uint64_t c0;         // first camera path (frame * cropPixels + permutation slot) of the wave
@@ -955,6 +982,10 @@ struct BdptWave
     uint4* misc2;        // permutation slot pixel, light path, light vertex count
     uint2* conn;         // this bounce's connection records: first, count
     float4* exitHit;     // a pending subsurface exit: barycentrics, instance, primitive | front << 31
+    Surface* camSurf;    // a connecting camera vertex: its surface and frames,
+    SurfaceCtx* camCtx;
+    struct ConnVertex* cvx; // and the rest of its state the connections read
+    uint2* connSlot;     // per connection record: camera path slot, light vertex
     float4* volIOR;
     uint4* volMat;
     float4* volAbs;      // [k * capacity + slot]
@@ -1016,8 +1047,16 @@ __global__ void __launch_bounds__(128) wbPrepare(const SceneView S, const Launch
         Spectral sp;
         spectralOf(S, B.heroes[pl], sp);
         const LightNode* src = B.nodes + pl * B.maxLightVerts;
-        prepareSharedNode(S, P, sp, src[k], k ? src[k - 1].pos : src[0].pos, k ? src[k - 1].normal : src[0].normal, k,
-                          W.prep[i]);
+        SharedNode& d = W.prep[i];
+        prepareSharedNode(S, P, sp, src[k], k ? src[k - 1].pos : src[0].pos, k ? src[k - 1].normal : src[0].normal, k, d);
+        float ri = 0.0f;
+        for (uint32_t j = 0; j + 1 < k; ++j) ri = accumulateRISum(ri, src[j].pdfBwd, src[j].pdfFwd, !(src[j].flags & NF_SSS_EXIT));
+        d.lvRiSum = ri;
+        d.lvPrevPos = k ? src[k - 1].pos : mk3(0.f, 0.f, 0.f);
+        d.lvPrevNormal = k ? src[k - 1].normal : mk3(0.f, 0.f, 0.f);
+        d.lvPrevPdfFwd = k ? src[k - 1].pdfFwd : 0.0f;
+        d.lvPrevFlags = k ? src[k - 1].flags : 0u;
+        d.lvOriginFlags = k ? src[0].flags : 0u;
     }
 }
 
@@ -1135,7 +1174,7 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
     {
         const uint32_t i = first + r * stride;
         const bool active = i < n;
-        uint32_t s = 0, count = 0, path = kNoLightPath, f = 0;
+        uint32_t s = 0, count = 0, f = 0;
         bool connect = false, alive = false;
         PathState st;
         RandomSampler rs;
@@ -1158,7 +1197,6 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
             rayDir = mk3(qd.x, qd.y, qd.z);
             const uint4 m = W.misc[s], m2 = W.misc2[s];
             f = m.w;
-            path = m2.y;
             count = m2.z;
             initState(st);
             st.throughput = W.thr[s];
@@ -1257,94 +1295,34 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
             }
             if (!alive) W.tot[s] = total; // the path ends at this vertex
         }
-        // connection records: count per connecting path, consecutive per path
+        // connection records: count per connecting path, consecutive per path; the
+        // connections themselves are evaluated by wbConnect, one thread per record
         const uint32_t base = warpReserve(W.connCount, connect ? count : 0u);
         if (active) W.conn[s] = make_uint2(base, connect ? count : 0u);
         if (connect)
         {
-            const Surface& sf = hs.s;
-            const float3 wo = -hs.rayDirOS;
-            const SharedNode* nodes = W.prep + (((size_t)(f - W.fBase)) * B.lightPaths + path) * B.maxLightVerts;
-            LightVertexCtx lv;
-            lv.riSum = 0.0f;
-            lv.originFlags = 0;
-            lv.prevPos = mk3(0.f, 0.f, 0.f);
-            lv.prevNormal = mk3(0.f, 0.f, 0.f);
-            lv.prevPdfFwd = 0.0f;
-            lv.prevFlags = 0;
-            float deferredLight = 0.0f;
-            const bool camTerminated = (st.flags & kFlagSecondaryTerminated) != 0;
-            for (uint32_t li = 0; li < count; ++li)
-            {
-                const SharedNode& sn = nodes[li];
-                const LightNode& ln = sn.n;
-                const uint32_t e = base + li;
-                float4 ro = mk4(0.f, 0.f, 0.f, __uint_as_float(s)), rd = mk4(0.f, 0.f, 0.f, -1.0f), contrib = splat4(0.0f);
-                uint2 target = make_uint2(0u, 0u);
-                if (!(ln.flags & NF_DELTA))
-                {
-                    // getLightNodeConnection + calculateLightPathRadiance (BDPTCommon.hlsl:622-635, 1062-1215)
-                    const bool atInfinity = li == 0 && (ln.flags & NF_INFINITE);
-                    const bool noGeometry = li == 0 && (ln.flags & (NF_ENV | NF_PUNCTUAL));
-                    float3 toLightDir;
-                    float dist;
-                    if (atInfinity)
-                    {
-                        toLightDir = -ln.normal;
-                        dist = __int_as_float(0x7f800000);
-                    }
-                    else
-                    {
-                        float3 toLight = ln.pos - cv.pos;
-                        dist = length(toLight);
-                        toLightDir = toLight / dist;
-                    }
-                    const float3 wi = normalize(xformVector(I->w2o, toLightDir));
-                    const bool lightTerminated = (ln.flags & NF_TERMINATED) != 0;
-                    const bool terminatedBefore = camTerminated || lightTerminated;
-                    ScatterEval ce = cv.isExit ? evaluateExitBoth(sf, c, currentIOR(st), previousIOR(st), wo, wi, hit.front, false,
-                                                                  cv.pos, cv.normal, cv.prevPos, cv.prevNormal)
-                                               : evaluateBoth(Lt, sp, sf, c, currentIOR(st), previousIOR(st), wo, wi, hit.front,
-                                                              false, false);
-                    if ((ce.transmission & kTransDispersed) && !terminatedBefore) terminateSecondary(ce.weight);
-                    if (ce.pdfFwd != 0.0f && !allEqual4(ce.weight, 0.0f))
-                    {
-                        const bool terminatedNow = terminatedBefore || (ce.transmission & kTransDispersed);
-                        ScatterEval le;
-                        float fwdLight;
-                        if (lightEndOfConnection(S, B, Lt, sp, sn, li, cv.pos, terminatedNow, le, fwdLight))
-                        {
-                            float mis = misWeight(S, ci, cv, li, lv, ln, ce.pdfFwd, ce.pdfBwd, fwdLight, le.pdfBwd);
-                            float G = li > 0 ? 1.0f / (dist * dist) : 1.0f;
-                            float4 wc = ce.weight;
-                            if (!atInfinity)
-                            {
-                                float4 cab = absorptionAfter(st, ce.transmission, sf, hs.material);
-                                if (!allEqual4(cab, 0.0f)) wc = wc * transmittance(cab, dist);
-                            }
-                            contrib = le.weight * wc * st.throughput * ln.radiance * G * mis;
-                            if (camTerminated && lightTerminated) contrib.x *= 0.25f; // undoSecondaryWavelengthRescale
-                            const float3 start = spawnRayOrigin(cv.pos, cv.normal, toLightDir);
-                            ro = mk4(start.x, start.y, start.z, __uint_as_float(s));
-                            rd = mk4(toLightDir.x, toLightDir.y, toLightDir.z,
-                                     atInfinity ? __int_as_float(0x7f800000)
-                                                : (noGeometry ? dist - kRayMinT : kRayMinT + dist + kVisibilityEps));
-                            target = noGeometry ? make_uint2(0xffffffffu, 0xffffffffu) : make_uint2(ln.instance, ln.prim);
-                        }
-                    }
-                }
-                W.C.o[e] = ro;
-                W.C.d[e] = rd;
-                W.C.target[e] = target;
-                W.C.contrib[e] = contrib;
-                lv.riSum = deferredLight;
-                deferredLight = accumulateRISum(deferredLight, ln.pdfBwd, ln.pdfFwd, !(ln.flags & NF_SSS_EXIT));
-                lv.prevNormal = ln.normal;
-                lv.prevPos = ln.pos;
-                lv.prevPdfFwd = ln.pdfFwd;
-                lv.prevFlags = ln.flags;
-                if (li == 0) lv.originFlags = ln.flags;
-            }
+            W.camSurf[s] = hs.s;
+            W.camCtx[s] = c;
+            ConnVertex v;
+            v.thr = st.throughput;
+            v.absNone = st.nVol ? st.volAbs[st.nVol - 1] : splat4(0.0f);
+            v.absExited = absorptionAfter(st, kTransExited, hs.s, hs.material);
+            v.pos = cv.pos;
+            v.flags = st.flags | (cv.isExit ? kWbAtExit : 0u) | (cv.prevIsExit ? kWbPrevExit : 0u);
+            v.normal = cv.normal;
+            v.curPdfFwd = cv.curPdfFwd;
+            v.prevPos = cv.prevPos;
+            v.pdfRatioSum = cv.pdfRatioSum;
+            v.prevNormal = cv.prevNormal;
+            v.prevPdfFwd = cv.prevPdfFwd;
+            v.wo = -hs.rayDirOS;
+            v.hero = sp.hero;
+            v.curIOR = currentIOR(st);
+            v.prevIOR = previousIOR(st);
+            v.instance = hit.instance;
+            v.front = hit.front ? 1u : 0u;
+            W.cvx[s] = v;
+            for (uint32_t li = 0; li < count; ++li) W.connSlot[base + li] = make_uint2(s, li);
         }
         bool cont = false, toExit = false;
         if (alive)
@@ -1419,6 +1397,108 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
             Qout.o[o] = mk4(rayOrigin.x, rayOrigin.y, rayOrigin.z, __uint_as_float(s));
             Qout.d[o] = mk4(rayDir.x, rayDir.y, rayDir.z, toExit ? 1.0f : 0.0f);
         }
+    }
+}
+
+// the connections of this bounce's camera vertices, one thread per (camera vertex, light
+// vertex) record (getLightNodeConnection + calculateLightPathRadiance, BDPTCommon.hlsl:622-635,
+// 1062-1215): the contribution and the visibility ray of each, summed later in light-vertex
+// order. The light side's MIS context comes prepared with the light vertex.
+__global__ void __launch_bounds__(128) wbConnect(const SceneView S, BdptParams B, BdptWave W, uint32_t ci)
+{
+    const Luts Lt = bdptLuts(S);
+    const uint32_t n = *W.connCount;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    {
+        const uint2 sl = W.connSlot[e];
+        const uint32_t s = sl.x, li = sl.y;
+        const uint32_t f = W.misc[s].w, path = W.misc2[s].y;
+        const SharedNode& sn = W.prep[(((size_t)(f - W.fBase)) * B.lightPaths + path) * B.maxLightVerts + li];
+        const LightNode& ln = sn.n;
+        float4 ro = mk4(0.f, 0.f, 0.f, __uint_as_float(s)), rd = mk4(0.f, 0.f, 0.f, -1.0f), contrib = splat4(0.0f);
+        uint2 target = make_uint2(0u, 0u);
+        if (!(ln.flags & NF_DELTA))
+        {
+            const ConnVertex v = W.cvx[s];
+            const Surface sf = W.camSurf[s];
+            const SurfaceCtx c = W.camCtx[s];
+            const GpuInstance& I = S.instances[v.instance];
+            Spectral sp;
+            spectralOf(S, v.hero, sp);
+            CamVertex cv;
+            cv.pos = v.pos;
+            cv.normal = v.normal;
+            cv.prevPos = v.prevPos;
+            cv.prevNormal = v.prevNormal;
+            cv.pdfRatioSum = v.pdfRatioSum;
+            cv.prevPdfFwd = v.prevPdfFwd;
+            cv.curPdfFwd = v.curPdfFwd;
+            cv.isExit = (v.flags & kWbAtExit) != 0;
+            cv.prevIsExit = (v.flags & kWbPrevExit) != 0;
+            LightVertexCtx lv;
+            lv.riSum = sn.lvRiSum;
+            lv.prevPos = sn.lvPrevPos;
+            lv.prevNormal = sn.lvPrevNormal;
+            lv.prevPdfFwd = sn.lvPrevPdfFwd;
+            lv.prevFlags = sn.lvPrevFlags;
+            lv.originFlags = sn.lvOriginFlags;
+            const bool front = v.front != 0;
+            const bool camTerminated = (v.flags & kFlagSecondaryTerminated) != 0;
+            const bool atInfinity = li == 0 && (ln.flags & NF_INFINITE);
+            const bool noGeometry = li == 0 && (ln.flags & (NF_ENV | NF_PUNCTUAL));
+            float3 toLightDir;
+            float dist;
+            if (atInfinity)
+            {
+                toLightDir = -ln.normal;
+                dist = __int_as_float(0x7f800000);
+            }
+            else
+            {
+                float3 toLight = ln.pos - cv.pos;
+                dist = length(toLight);
+                toLightDir = toLight / dist;
+            }
+            const float3 wi = normalize(xformVector(I.w2o, toLightDir));
+            const bool lightTerminated = (ln.flags & NF_TERMINATED) != 0;
+            const bool terminatedBefore = camTerminated || lightTerminated;
+            ScatterEval ce = cv.isExit ? evaluateExitBoth(sf, c, v.curIOR, v.prevIOR, v.wo, wi, front, false, cv.pos, cv.normal,
+                                                          cv.prevPos, cv.prevNormal)
+                                       : evaluateBoth(Lt, sp, sf, c, v.curIOR, v.prevIOR, v.wo, wi, front, false, false);
+            if ((ce.transmission & kTransDispersed) && !terminatedBefore) terminateSecondary(ce.weight);
+            if (ce.pdfFwd != 0.0f && !allEqual4(ce.weight, 0.0f))
+            {
+                const bool terminatedNow = terminatedBefore || (ce.transmission & kTransDispersed);
+                ScatterEval le;
+                float fwdLight;
+                if (lightEndOfConnection(S, B, Lt, sp, sn, li, cv.pos, terminatedNow, le, fwdLight))
+                {
+                    float mis = misWeight(S, ci, cv, li, lv, ln, ce.pdfFwd, ce.pdfBwd, fwdLight, le.pdfBwd);
+                    float G = li > 0 ? 1.0f / (dist * dist) : 1.0f;
+                    float4 wc = ce.weight;
+                    if (!atInfinity)
+                    {
+                        // absorptionAfter: the medium the connection runs through
+                        float4 cab = (ce.transmission & kTransExited)    ? v.absExited
+                                     : (ce.transmission & kTransEntered) ? sf.absorption
+                                                                          : v.absNone;
+                        if (!allEqual4(cab, 0.0f)) wc = wc * transmittance(cab, dist);
+                    }
+                    contrib = le.weight * wc * v.thr * ln.radiance * G * mis;
+                    if (camTerminated && lightTerminated) contrib.x *= 0.25f; // undoSecondaryWavelengthRescale
+                    const float3 start = spawnRayOrigin(cv.pos, cv.normal, toLightDir);
+                    ro = mk4(start.x, start.y, start.z, __uint_as_float(s));
+                    rd = mk4(toLightDir.x, toLightDir.y, toLightDir.z,
+                             atInfinity ? __int_as_float(0x7f800000)
+                                        : (noGeometry ? dist - kRayMinT : kRayMinT + dist + kVisibilityEps));
+                    target = noGeometry ? make_uint2(0xffffffffu, 0xffffffffu) : make_uint2(ln.instance, ln.prim);
+                }
+            }
+        }
+        W.C.o[e] = ro;
+        W.C.d[e] = rd;
+        W.C.target[e] = target;
+        W.C.contrib[e] = contrib;
     }
 }
 
@@ -1648,7 +1728,11 @@ WaveShape waveShape(uint32_t frames, uint64_t cropPixels)
 }
 // per path: state (5 x 16 + 2 x 16 + 8 + volumes 96 + features 32), two ray queues (64), hits
 // (20), the regrouped ray and hit queues (52) and the class key (1)
-size_t waveSlotBytes() { return 5 * 16 + 2 * 16 + 8 + 16 + 16 + 16 + 64 + 2 * 16 + 2 * 32 + 20 + 52 + 1; }
+size_t waveSlotBytes()
+{
+    return 5 * 16 + 2 * 16 + 8 + 16 + 16 + 16 + 64 + 2 * 16 + 2 * 32 + 20 + 52 + 1 + sizeof(Surface) + sizeof(SurfaceCtx) +
+           sizeof(ConnVertex);
+}
 } // namespace
 
 size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVerts, uint64_t cropPixels)
@@ -1659,8 +1743,8 @@ size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVer
     b += align256((size_t)frames * cropPixels * 24);
     const WaveShape w = waveShape(frames, cropPixels);
     b += align256((size_t)w.spanFrames * lightPaths * maxLightVerts * sizeof(SharedNode));
-    b += (size_t)w.capacity * waveSlotBytes() + 32 * 256;
-    b += (size_t)w.capacity * maxLightVerts * (56 + 1) + 8 * 256;
+    b += (size_t)w.capacity * waveSlotBytes() + 40 * 256;
+    b += (size_t)w.capacity * maxLightVerts * (56 + 1 + 8) + 8 * 256;
     b += 256;
     return b;
 }
@@ -1706,6 +1790,9 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
     W.misc2 = reinterpret_cast<uint4*>(take(C * 16));
     W.conn = reinterpret_cast<uint2*>(take(C * 8));
     W.exitHit = reinterpret_cast<float4*>(take(C * 16));
+    W.camSurf = reinterpret_cast<Surface*>(take(C * sizeof(Surface)));
+    W.camCtx = reinterpret_cast<SurfaceCtx*>(take(C * sizeof(SurfaceCtx)));
+    W.cvx = reinterpret_cast<ConnVertex*>(take(C * sizeof(ConnVertex)));
     W.volIOR = reinterpret_cast<float4*>(take(C * 16));
     W.volMat = reinterpret_cast<uint4*>(take(C * 16));
     W.volAbs = reinterpret_cast<float4*>(take(C * 64));
@@ -1723,6 +1810,7 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
     W.C = ShadowQueue{reinterpret_cast<float4*>(take(CR * 16)), reinterpret_cast<float4*>(take(CR * 16)),
                       reinterpret_cast<uint2*>(take(CR * 8)), reinterpret_cast<float4*>(take(CR * 16)), counters + 2};
     W.vis = reinterpret_cast<uint8_t*>(take(CR));
+    W.connSlot = reinterpret_cast<uint2*>(take(CR * 8));
     W.connCount = counters + 2;
 
     cudaMemsetAsync(B.splat, 0, (size_t)B.frames * cropPix * 24, stream);
@@ -1758,9 +1846,10 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
             wfClassify<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
             wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
             wbShade<<<shadeBlocks, 128, 0, stream>>>(S, P, B, W, QS, HS, *nxt, ci);
+            wbConnect<<<traceBlocks, 128, 0, stream>>>(S, B, W, ci);
             wbVisibility<<<traceBlocks, 128, 0, stream>>>(S, W);
             wbAccumulate<<<smCount * 4, 256, 0, stream>>>(W, QS);
-            launches += 6;
+            launches += 7;
             RayQueue* t = cur;
             cur = nxt;
             nxt = t;
