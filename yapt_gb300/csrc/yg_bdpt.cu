@@ -1295,8 +1295,9 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
             }
             if (!alive) W.tot[s] = total; // the path ends at this vertex
         }
-        // connection records: count per connecting path, consecutive per path; the
-        // connections themselves are evaluated by wbConnect, one thread per record
+        // connection records: count per connecting path, consecutive per path (neighbouring
+        // threads of wbConnect then read the same camera vertex); the connections themselves
+        // are evaluated by wbConnect, one thread per record
         const uint32_t base = warpReserve(W.connCount, connect ? count : 0u);
         if (active) W.conn[s] = make_uint2(base, connect ? count : 0u);
         if (connect)
@@ -1520,10 +1521,13 @@ __global__ void __launch_bounds__(128) wbVisibility(const SceneView S, BdptWave 
             continue;
         }
         const float4 o = W.C.o[e];
-        traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w);
-        while (traceStep<false>(t, st, &tc)) {}
+        // the light vertex's own triangle must be the first hit; toward a target without
+        // geometry (kPunctualShadow) nothing may be hit
         const uint2 tg = W.C.target[e];
-        W.vis[e] = tg.x == 0xffffffffu ? !t.found : shadowVisible(t.found, t.h, tg.x, tg.y);
+        const bool early = shadowBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, tg.x, tg.y);
+        while (traceStep<false>(t, st, &tc))
+            if (shadowStopped(t, early, tg.x, tg.y)) break;
+        W.vis[e] = shadowVisible(t.found, t.h, tg.x, tg.y);
         ++rays;
     }
 }

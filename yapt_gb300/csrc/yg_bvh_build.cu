@@ -703,6 +703,27 @@ cudaError_t readBack(T& v, const T* d, cudaStream_t s)
 
 } // namespace
 
+namespace
+{
+__global__ void triangleSlots(const float4* __restrict__ tris, uint32_t n, const uint32_t* __restrict__ primStart,
+                              uint32_t* __restrict__ out)
+{
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    {
+        const uint32_t inst = __float_as_uint(tris[3 * (size_t)j].w), prim = __float_as_uint(tris[3 * (size_t)j + 1].w);
+        out[primStart[inst] + prim] = j;
+    }
+}
+} // namespace
+
+int indexTrianglesByPrim(const float4* tris, uint32_t nTris, const uint32_t* primStart, uint32_t* out, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0xff, 4 * (size_t)std::max<uint32_t>(nTris, 1), s);
+    if (e != cudaSuccess || nTris == 0) return (int)e;
+    triangleSlots<<<(int)std::min<uint32_t>((nTris + 255) / 256, 4096), 256, 0, s>>>(tris, nTris, primStart, out);
+    return (int)cudaGetLastError();
+}
+
 int buildWideBvh(const WideBvhInput& in, WideBvhOutput& out, cudaStream_t s, std::string& err)
 {
     Pool pool;

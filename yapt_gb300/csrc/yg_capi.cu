@@ -265,6 +265,8 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.tangents = ctx->dTan.as<float4>();
     S.uvs = ctx->dUV.as<float2>();
     S.textures = ctx->dTexTable.as<yg::GpuTexture>();
+    S.instPrimStart = ctx->dPrimStart.as<uint32_t>();
+    S.triOfPrim = ctx->dTriOfPrim.as<uint32_t>();
     S.envTexture = ctx->envTexture;
     S.envCube = ctx->envCube ? 1u : 0u;
     S.indices = ctx->dIdx.as<uint32_t>();
@@ -943,6 +945,12 @@ YG_API int yg_build_scene(yg_context* ctx)
     ctx->dNodes.adopt(bout.nodes, 5 * sizeof(float4) * (size_t)bout.nNodes);
     ctx->nTris = primStart[nInst];
     ctx->nNodes = bout.nNodes;
+    // each primitive's position in the triangle array, for visibility tests that intersect
+    // their target triangle before traversing
+    if ((r = upload(ctx, ctx->dPrimStart, primStart.data(), primStart.size()))) return r;
+    YG_CUDA(ctx->dTriOfPrim.ensure(4 * (size_t)std::max<uint32_t>(primStart[nInst], 1)));
+    YG_CUDA((cudaError_t)yg::indexTrianglesByPrim(bout.tris, primStart[nInst], ctx->dPrimStart.as<uint32_t>(),
+                                                    ctx->dTriOfPrim.as<uint32_t>(), ctx->stream));
     ctx->bvhDepth = bout.depth;
     ctx->hostInst = gi;
     // every inner node reachable exactly once and every triangle referenced exactly once,

@@ -42,10 +42,9 @@ __global__ void __launch_bounds__(128) pathKernel(const __grid_constant__ SceneV
             alive = shadeSegment<NEE>(S, P, Lt, sp, found, hit, ps, rs, sr, P.featAlbedo ? &fh : nullptr);
             if (sr.valid)
             {
-                Hit h;
                 rays++;
-                bool any = traceClosest<COUNT>(S, sr.origin, sr.dir, kRayMinT, sr.tmax, h, &tc);
-                if (shadowVisible(any, h, sr.instance, sr.prim)) ps.total = ps.total + sr.contrib;
+                if (traceShadow<COUNT>(S, sr.origin, sr.dir, kRayMinT, sr.tmax, sr.instance, sr.prim, &tc))
+                    ps.total = ps.total + sr.contrib;
             }
         }
         writeSample(S, P, idx, sp, ps.total, fh);
@@ -339,14 +338,16 @@ __global__ void __launch_bounds__(128) wfShadow(const __grid_constant__ SceneVie
     const uint32_t n = *SQ.count;
     TraversalCount tc{0, 0};
     uint32_t rays = 0;
-    traceGrid<COUNT>(
+    uint2 tg = make_uint2(0u, 0u);
+    bool early = false;
+    traceGridStop<COUNT>(
         n,
         [&](TraceState& t, uint32_t i) {
             const float4 o = SQ.o[i], d = SQ.d[i];
-            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w);
+            tg = SQ.target[i];
+            early = shadowBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, tg.x, tg.y);
         },
         [&](const TraceState& t, uint32_t i) {
-            const uint2 tg = SQ.target[i];
             if (shadowVisible(t.found, t.h, tg.x, tg.y))
             {
                 const uint32_t to = __float_as_uint(SQ.o[i].w);
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(128) wfShadow(const __grid_constant__ SceneVie
                 }
             }
         },
-        tc, rays);
+        [&](const TraceState& t) { return shadowStopped(t, early, tg.x, tg.y); }, tc, rays);
     countRays(rayCtr, rays);
     if (COUNT)
     {

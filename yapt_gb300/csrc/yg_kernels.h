@@ -38,6 +38,9 @@ struct WideBvhOutput
     float lo[3], hi[3]; // world bounds of all triangles
 };
 int buildWideBvh(const WideBvhInput& in, WideBvhOutput& out, cudaStream_t stream, std::string& error);
+// out[primStart[instance] + primitive] = position of that triangle in tris (nTris triangles of
+// 48 bytes in leaf order), 0xffffffff where none; returns a cudaError_t
+int indexTrianglesByPrim(const float4* tris, uint32_t nTris, const uint32_t* primStart, uint32_t* out, cudaStream_t stream);
 
 // Kernel kinds of the timer (the C-ABI's YG_KERNEL_* values).
 constexpr uint8_t kKernelTrace = 0, kKernelRegroup = 1, kKernelShade = 2, kKernelShadow = 3;

@@ -712,6 +712,40 @@ YG_DEV bool shadowVisible(bool any, const Hit& h, uint32_t inst, uint32_t prim)
     return any && h.instance == inst && h.prim == prim;
 }
 
+// The visibility test above as an any-hit traversal that gives the same answer. The target
+// triangle is intersected first (the same test the traversal would make, so the same t); the
+// closest hit starts as the target, and the first candidate the traversal finds that would
+// replace it (nearer, or equally near with a smaller key) proves the segment occluded. A target
+// without geometry (inst = kPunctualShadow) is occluded by any hit. shadowBegin returns whether
+// the traversal may stop at such a candidate (shadowStopped); with the target missed it leaves
+// nothing to traverse.
+YG_DEV bool shadowBegin(TraceState& t, const SceneView& S, float3 o, float3 d, float tmin, float tmax, uint32_t inst,
+                        uint32_t prim)
+{
+    traceBegin(t, S, o, d, tmin, tmax);
+    if (inst == kPunctualShadow) return true;
+    const uint32_t j = S.triOfPrim ? S.triOfPrim[S.instPrimStart[inst] + prim] : 0xffffffffu;
+    if (j == 0xffffffffu) return false; // no position known: the full closest-hit traversal
+    intersectTri<false>(t.tris, (int)j, o, d, tmin, t.h, t.found);
+    if (!t.found || t.h.instance != inst || t.h.prim != prim) t.gHits = 0; // the target is not hit: occluded
+    return true;
+}
+YG_DEV bool shadowStopped(const TraceState& t, bool early, uint32_t inst, uint32_t prim)
+{
+    return early && t.found && (inst == kPunctualShadow || t.h.instance != inst || t.h.prim != prim);
+}
+template <bool COUNT>
+__device__ __noinline__ bool traceShadow(const SceneView& S, float3 o, float3 d, float tmin, float tmax, uint32_t inst, uint32_t prim,
+                                         TraversalCount* tc)
+{
+    TraceState t;
+    TraceStack st;
+    const bool early = shadowBegin(t, S, o, d, tmin, tmax, inst, prim);
+    while (traceStep<COUNT>(t, st, tc))
+        if (shadowStopped(t, early, inst, prim)) break;
+    return shadowVisible(t.found, t.h, inst, prim);
+}
+
 // generateCameraRay (raytraceCommonResources.hlsl:113-137) and the sample set-up of
 // rayGenPrimaryRays.hlsl:13-37
 YG_DEV void beginPath(const SceneView& S, const LaunchParams& P, uint32_t cx, uint32_t cy, RandomSampler& rs, Spectral& sp,
@@ -769,9 +803,8 @@ static __device__ __noinline__ bool subsurfaceEvent(const SceneView& S, const La
 {
     if (sr.valid)
     {
-        Hit h;
-        bool any = traceClosest<false>(S, sr.origin, sr.dir, kRayMinT, sr.tmax, h, nullptr);
-        if (shadowVisible(any, h, sr.instance, sr.prim)) ps.total = ps.total + sr.contrib;
+        if (traceShadow<false>(S, sr.origin, sr.dir, kRayMinT, sr.tmax, sr.instance, sr.prim, nullptr))
+            ps.total = ps.total + sr.contrib;
         sr.valid = false;
     }
     SurfacePoint entry;

@@ -181,22 +181,24 @@ __device__ __forceinline__ void shadowBody(const MultiTables& M, const WaveState
     const uint32_t n = *SQ.count;
     uint32_t rays = 0;
     TraversalCount tc{0, 0};
-    traceGrid<false>(
+    uint2 tg = make_uint2(0u, 0u);
+    bool early = false;
+    traceGridStop<false>(
         n,
         [&](TraceState& t, uint32_t i) {
             const float4 o = SQ.o[i], d = SQ.d[i];
             const SceneView& S = M.views[M.req[__float_as_uint(o.w)]];
-            traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w);
+            tg = SQ.target[i];
+            early = shadowBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, tg.x, tg.y);
         },
         [&](const TraceState& t, uint32_t i) {
-            const uint2 tg = SQ.target[i];
             if (shadowVisible(t.found, t.h, tg.x, tg.y))
             {
                 const uint32_t s = __float_as_uint(SQ.o[i].w);
                 W.tot[s] = W.tot[s] + SQ.contrib[i];
             }
         },
-        tc, rays);
+        [&](const TraceState& t) { return shadowStopped(t, early, tg.x, tg.y); }, tc, rays);
     countRays(rayCtr, rays);
 }
 

@@ -332,6 +332,28 @@ static __device__ __noinline__ bool traceInstanceClosest(const SceneView& S, flo
 // The group stack stays in local memory: its top entries live in L1 anyway, and staging them
 // in shared memory (YG_TRACE_SHARED_STACK, 8 KB per block) measured 3 % slower on the NEE
 // workload's traversal, the smaller L1 costing more node hits than the stack saves.
+// With `stop`, a ray's traversal also ends as soon as stop(state) holds after a node.
+template <bool COUNT, typename Begin, typename End, typename Stop>
+__device__ __forceinline__ void traceGridStop(uint32_t n, Begin begin, End end, Stop stop, TraversalCount& tc,
+                                              uint32_t& rays)
+{
+    TraceState t;
+#ifdef YG_TRACE_SHARED_STACK
+    __shared__ uint2 stackTop[kSharedStack * kTraceBlock];
+    SharedTraceStack st;
+    st.sh = threadIdx.x < (uint32_t)kTraceBlock ? stackTop + threadIdx.x : nullptr;
+#else
+    TraceStack st;
+#endif
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        begin(t, i);
+        while (traceStep<COUNT>(t, st, &tc))
+            if (stop(t)) break;
+        end(t, i);
+        ++rays;
+    }
+}
 template <bool COUNT, typename Begin, typename End>
 __device__ __forceinline__ void traceGrid(uint32_t n, Begin begin, End end, TraversalCount& tc, uint32_t& rays)
 {

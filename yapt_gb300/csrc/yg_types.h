@@ -134,6 +134,8 @@ struct SceneView
     const float4* cie;     // (xbar, ybar, zbar, d65) per 1 nm over [lambdaMin, lambdaMax]
     const float* rgbToSpd; // 64^3 x 3, may be null
     const uint32_t* sobol; // [spp_count][kSobolDims] points of this launch
+    const uint32_t* instPrimStart; // first primitive of each instance in the scene's primitive order
+    const uint32_t* triOfPrim;     // position in `tris` of each primitive (0xffffffff: none)
     GpuCamera cam;
     const GpuTexture* textures;
     int envTexture;        // environment texture, -1: the analytic sky
