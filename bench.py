@@ -56,6 +56,7 @@ DENOISE_WORKLOAD = dict(workload="denoise_unet_box_scenes_1080p", train_scenes=4
                         train_input_spp=[2, 4, 8, 16, 32], train_target_spp=8192, train_steps=12000, batch=8, crop=128, lr=1e-3,
                         lr_final=1e-5,
                         eval_width=1920, eval_height=1080, eval_reference_spp=65536, eval_seed=100000, integrator="uni",
+                        extra_eval_seeds=[100001, 100002, 100003], extra_reference_spp=16384,
                         max_depth=8, tile=64, target_relmse=1e-3, lambda_nm=[380, 780])
 DENOISE_METRIC = "denoise: wall-time speed-up to relMSE 1e-3 at 1920x1080 (plain accumulation time / denoised time)"
 UNET_FLOP_PER_PIXEL = 2 * 9 * (16 * 32 + 32 * 32 + (32 * 64 + 64 * 64) / 4 + (64 * 128 + 128 * 128) / 16 +
@@ -412,10 +413,11 @@ def run_ours(args, world, rank, local):
     else:
         # per-kind device time from the timed steps; algorithmic bytes from one counting step
         # of the same workload (same kernels, traversal counters on), per bounce:
-        #  wfTrace:  rays read (origin and direction of the queued record, 32 B), hits written
-        #            (20 B), wide BVH nodes (80 B) and triangles (48 B) its rays visit;
-        #  regroup:  classification (hit read, 20 B; key written, 1 B) and the move of every
-        #            record with its hit (key 1 B + record 84 B + hit 20 B read, 104 B written);
+        #  wfTrace:  rays read (origin and direction of the queued record, 32 B), hits and their
+        #            shading-class keys written (20 B + 1 B), wide BVH nodes (80 B) and
+        #            triangles (48 B) its rays visit;
+        #  regroup:  the move of every record with its hit (key 1 B + record 84 B + hit 20 B read,
+        #            104 B written);
         #  wfShade:  (the four class-group launches of a bounce together) per shaded path the
         #            regrouped record and hit read (104 B), the record of every continuing path
         #            written (84 B), the radiance and hero wavelength of every ended path (20 B),
@@ -426,11 +428,11 @@ def run_ours(args, world, rank, local):
         samples_step = W * H * spp
         R = kp["closest_rays"]
         algo = {
-            "trace": (R * (32 + 20) + kp["closest_nodes"] * 80 + kp["closest_triangles"] * 48),
-            "regroup": R * (20 + 1 + 1 + 104 + 104),
+            "trace": (R * (32 + 20 + 1) + kp["closest_nodes"] * 80 + kp["closest_triangles"] * 48),
+            "regroup": R * (1 + 104 + 104),
             "shade": (R * 104 + (R - samples_step) * 84 + samples_step * 20 + kp["shadow_rays"] * 56),
         }
-        names = {"trace": "wfTrace", "regroup": "wfClassifyQ+wfRegroupQ", "shade": "wfShade"}
+        names = {"trace": "wfTrace", "regroup": "wfRegroupQ", "shade": "wfShade"}
         total_ms = sum(v["ms"] for v in kinds.values())
         kernels = {}
         for k in ("trace", "regroup", "shade"):
@@ -679,6 +681,26 @@ def run_denoise(args, world, rank, local):
         # time to the target: the fastest operating point (samples per pixel) that reaches it
         if r <= W["target_relmse"] and (best is None or dt < best["seconds"]):
             best = den_curve[-1]
+    # generalisation: further held-out scenes at 960x544 (sides multiples of 8, as the network's
+    # three pooling levels need) against 16,384-spp references, the denoised image at 8 and 32
+    # spp beside plain accumulation at the same spp
+    seeds_eval = []
+    SW, SH = 960, 544
+    for sd in W["extra_eval_seeds"]:
+        ctx.upload_scene(configs.box_scene(sd, aspect=SW / SH))
+        sref = D.render_reference(ctx, SW, SH, W["extra_reference_spp"], spp_start=1 << 20, **kw)
+        spipe = D.DenoisePipeline(net, ctx, SH, SW, tile=W["tile"], depth_scale=4.0)
+        row = {"seed": sd, "width": SW, "height": SH, "reference_spp": W["extra_reference_spp"]}
+        for spp in (8, 32):
+            out, _ = spipe.run(spp, spp_plain, W["target_relmse"], integrator=W["integrator"], max_depth=W["max_depth"],
+                               lambda_range=lam)
+            ctx.film_clear(SW, SH)
+            ctx.render(ctx.params(W["integrator"], SW, SH, spp=spp, max_depth=W["max_depth"], lambda_range=lam))
+            xyz, _ = ctx.film()
+            row["denoised_relmse_%dspp" % spp] = D.relmse(out, sref)
+            row["plain_relmse_%dspp" % spp] = D.relmse(xyz @ D.SRGB_FROM_XYZ.T, sref)
+        seeds_eval.append(row)
+    ctx.upload_scene(configs.box_scene(W["eval_seed"], aspect=EW / EH))
     # the reference's own denoiser (edge-stopping a-trous, 5 passes) on the same renders: the
     # render gathers its features, the filter runs on the device, the image is read back
     from yapt_gb300 import _native as N
@@ -742,7 +764,7 @@ def run_denoise(args, world, rank, local):
             "config": dict(W, plain_spp_for_target=spp_plain, relmse_constant_c=c_fit),
             "plain": {"spp": spp_plain, "seconds": t_plain, "relmse": r_plain,
                       "curve": [{"spp": s_, "relmse": r_, "seconds": d_} for (s_, r_, d_) in plain_curve]},
-            "denoised": {"best": best, "curve": den_curve},
+            "denoised": {"best": best, "curve": den_curve, "held_out_seeds": seeds_eval},
             "atrous_baseline": {"best": at_best, "curve": at_curve, "filter_ms_1080p": atrous_ms,
                                 "speedup_to_target": (t_plain / at_best["seconds"]) if at_best else None,
                                 "unet_speedup_over_atrous": (at_best["seconds"] / best["seconds"]) if (at_best and best) else None},

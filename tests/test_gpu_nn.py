@@ -93,6 +93,47 @@ def test_conv3x3_forward_and_data_gradient(torch_cuda, conv_impl, cin, cout, off
     np.testing.assert_allclose(host(dxd).reshape(n, h, w, cin), want, rtol=2 ** -7, atol=1e-3)
 
 
+@pytest.mark.parametrize("cin,cout,off,masked", [(16, 32, 0, False), (32, 32, 0, True), (32, 64, 0, False), (64, 64, 0, True),
+                                                  (96, 32, 32, False)])
+def test_persistent_conv_matches_mma_sync_on_large_images(torch_cuda, cin, cout, off, masked):
+    """Images of 65,536 pixels and more take the persistent TMA + tcgen05 kernel for these shapes
+    (several tiles per CTA, double-buffered halo and accumulator). It must give what the mma.sync
+    path gives to one BF16 rounding, with a ragged last tile (330 = 2 x 128 + 74 pixels), a ReLU
+    mask and accumulation into the output, and no wait may run out."""
+    import ctypes as C
+    from yapt_gb300 import _native as N
+    from yapt_gb300.denoise import view
+    torch = torch_cuda
+    lib = N.load()
+    rng = np.random.default_rng(7 * cin + cout)
+    n, h, w = 1, 200, 330
+    stride_y = cout + off
+    xd = dev_bf16(torch, rng.normal(0, 1, (n, h, w, cin)))
+    wd = dev_bf16(torch, rng.normal(0, 0.2, (cout, 3, 3, cin)))
+    bd = torch.from_numpy(rng.normal(0, 0.1, cout).astype(np.float32)).cuda()
+    md = dev_bf16(torch, rng.normal(0, 1, (n, h, w, stride_y))) if masked else None
+    y0 = dev_bf16(torch, rng.normal(0, 0.5, n * h * w * stride_y))
+    outs = {}
+    try:
+        for impl in (0, 2):
+            assert lib.yg_nn_set_conv_impl(impl) == 0
+            yd = y0.clone()
+            mv = C.byref(view(md, stride_y, off, cout)) if masked else None
+            rc = lib.yg_nn_conv3x3(C.byref(view(xd, cin, 0, cin)), C.c_void_p(wd.data_ptr()),
+                                   C.cast(C.c_void_p(bd.data_ptr()), C.POINTER(C.c_float)),
+                                   C.byref(view(yd, stride_y, off, cout)), mv, 1, 1, n, h, w, stream(torch))
+            assert rc == 0
+            torch.cuda.synchronize()
+            outs[impl] = host(yd).reshape(n, h, w, stride_y)
+    finally:
+        lib.yg_nn_set_conv_impl(0)
+    t = C.c_uint32()
+    assert lib.yg_nn_tc_timeouts(C.byref(t)) == 0 and t.value == 0, "tcgen05 waits ran out"
+    a, b = outs[2], outs[0]
+    assert np.array_equal(a[..., :off], host(y0).reshape(n, h, w, stride_y)[..., :off])  # other channels untouched
+    np.testing.assert_allclose(a[..., off:], b[..., off:], rtol=2 ** -6, atol=2e-2)
+
+
 @pytest.mark.parametrize("cin,cout", [(16, 32), (96, 32), (128, 256)])
 def test_conv3x3_weight_gradient(torch_cuda, cin, cout):
     import ctypes as C

@@ -151,9 +151,11 @@ __global__ void __launch_bounds__(256) wfGenerate(const __grid_constant__ SceneV
     if (blockIdx.x == 0 && threadIdx.x == 0) *Q.count = n;
 }
 
+// Closest hits of the queued paths, each with its shading-class key for the regroup (the class
+// counts are summed per group of lanes that finish together, one atomic per class and group).
 template <bool COUNT>
-__global__ void __launch_bounds__(128) wfTrace(const __grid_constant__ SceneView S, PathQueue Q, HitQueue H, unsigned long long* rayCtr,
-                                               unsigned long long* travCtr)
+__global__ void __launch_bounds__(128) wfTrace(const __grid_constant__ SceneView S, PathQueue Q, HitQueue H, uint8_t* keys,
+                                               uint32_t* classCounts, unsigned long long* rayCtr, unsigned long long* travCtr)
 {
     const uint32_t n = *Q.count;
     TraversalCount tc{0, 0};
@@ -165,8 +167,19 @@ __global__ void __launch_bounds__(128) wfTrace(const __grid_constant__ SceneView
             traceBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, __int_as_float(0x7f800000));
         },
         [&](const TraceState& t, uint32_t i) {
-            H.a[i] = mk4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.instance));
-            H.b[i] = t.found ? (t.h.prim | (t.h.front ? 0x80000000u : 0u)) : 0xffffffffu;
+            const float4 a = mk4(t.h.t, t.h.b1, t.h.b2, __uint_as_float(t.h.instance));
+            const uint32_t b = t.found ? (t.h.prim | (t.h.front ? 0x80000000u : 0u)) : 0xffffffffu;
+            H.a[i] = a;
+            H.b[i] = b;
+            const uint32_t key = shadeClass(S, a, b);
+            keys[i] = (uint8_t)key;
+            const uint32_t group = __activemask();
+            const uint32_t leader = (uint32_t)(__ffs(group) - 1);
+            for (uint32_t c = 0; c < (uint32_t)kShadeClasses; ++c)
+            {
+                const uint32_t m = __ballot_sync(group, key == c);
+                if ((threadIdx.x & 31u) == leader && m) atomicAdd(&classCounts[c], (uint32_t)__popc(m));
+            }
         },
         tc, rays);
     countRays(rayCtr, rays);
@@ -174,28 +187,6 @@ __global__ void __launch_bounds__(128) wfTrace(const __grid_constant__ SceneView
     {
         countTraversal(travCtr, tc);
         countRays(travCtr + 4, rays);
-    }
-}
-
-// shading-class key of every queued hit and the class counts (shadeClass of yg_wave.cuh)
-__global__ void __launch_bounds__(256) wfClassifyQ(const __grid_constant__ SceneView S, const uint32_t* count, HitQueue H, uint8_t* keys,
-                                                   uint32_t* counts)
-{
-    const uint32_t n = *count;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (n + stride - 1) / stride;
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t r = 0; r < rounds; ++r)
-    {
-        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
-        bool active = i < n;
-        uint32_t key = active ? shadeClass(S, H.a[i], H.b[i]) : 0xffu;
-        if (active) keys[i] = (uint8_t)key;
-        for (uint32_t c = 0; c < (uint32_t)kShadeClasses; ++c)
-        {
-            uint32_t m = __ballot_sync(0xffffffffu, key == c);
-            if (lane == 0 && m) atomicAdd(&counts[c], (uint32_t)__popc(m));
-        }
     }
 }
 
@@ -624,13 +615,12 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
         // Shading reads QB and appends the continuing paths to QA again.
         for (uint32_t b = 0; b < P.maxDepth; ++b)
         {
-            if (T) T->begin(stream);
-            if (count) wfTrace<true><<<traceBlocks, 128, 0, stream>>>(S, QA, H, P.rayCounter, P.traversalCounter);
-            else wfTrace<false><<<traceBlocks, 128, 0, stream>>>(S, QA, H, P.rayCounter, nullptr);
-            if (T) T->end(kKernelTrace, stream);
             cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
             if (T) T->begin(stream);
-            wfClassifyQ<<<smCount * 4, 256, 0, stream>>>(S, QA.count, H, keys, classCounts);
+            if (count) wfTrace<true><<<traceBlocks, 128, 0, stream>>>(S, QA, H, keys, classCounts, P.rayCounter, P.traversalCounter);
+            else wfTrace<false><<<traceBlocks, 128, 0, stream>>>(S, QA, H, keys, classCounts, P.rayCounter, nullptr);
+            if (T) T->end(kKernelTrace, stream);
+            if (T) T->begin(stream);
             wfRegroupQ<<<smCount * 4, 256, 0, stream>>>(QA, H, keys, classCounts, classCounts + kShadeClasses, QB, HS);
             if (T) T->end(kKernelRegroup, stream);
             cudaMemsetAsync(QA.count, 0, 4, stream);
@@ -645,7 +635,7 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
                 ++launches;
             }
             if (T) T->end(kKernelShade, stream);
-            launches += 3;
+            launches += 2;
             if (P.integrator == 1 || S.nPunctual > 0)
             {
                 if (T) T->begin(stream);

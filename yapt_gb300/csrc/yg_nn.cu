@@ -797,6 +797,302 @@ int launchTmaN(const Act& x, const bf16* w, const float* bias, const Act& y, con
     return YG_ERR_INVALID_ARGUMENT;
 }
 
+// ------------------------------------------------------------------ persistent TMA + tcgen05 convolution
+// For layers whose whole input window (all Cin channels of a 3 x 130-pixel halo, twice) and all
+// nine taps of weights fit in shared memory: Cin <= 96 and N <= 64, the full- and half-resolution
+// layers. Their few MMAs per 128-pixel tile left conv3x3Tma waiting on loads and set-up, so here a
+// persistent CTA walks a strided sequence of row tiles: the weights load once, the halo of the next
+// tile loads while the current one multiplies (two A buffers), and the accumulator alternates
+// between two TMEM buffers so that the epilogue of one tile overlaps the MMAs of the next.
+// Warps 0-3 run the epilogue (warp w reads TMEM lanes 32w..32w+31), warp 4 lane 0 issues the TMA
+// loads, warp 5 lane 0 the MMAs. Barriers: wFull (weights), aFull/aEmpty (A buffers), accFull
+// (MMAs of a tile complete) and accEmpty (its epilogue has read TMEM, one arrival per epilogue
+// warp). Every wait is bounded; a time-out stops every role, the producer waits for its issued
+// loads and every thread for the issued MMAs before TMEM is freed, and the time-out is counted.
+template <int CIN, int NT>
+struct PersistShape
+{
+    static constexpr int HALO = 130;
+    static constexpr int G = CIN / 8;
+    static constexpr uint32_t A_GROUP = 3u * HALO * 16u;
+    static constexpr uint32_t A_LBO = (A_GROUP + 127u) / 128u * 128u;
+    static constexpr int A_BYTES = (int)A_LBO * G;
+    static constexpr int W_BYTES = 9 * G * NT * 16;
+    static constexpr int SMEM = 2 * A_BYTES + W_BYTES;
+    static constexpr uint32_t TCOLS = 2 * NT;
+};
+
+__device__ __forceinline__ void mbarArrive(uint32_t addr)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
+}
+
+template <int CIN, int NT>
+__global__ void __launch_bounds__(192) conv3x3Persist(const __grid_constant__ CUtensorMap mapX,
+                                                      const __grid_constant__ CUtensorMap mapW, const float* __restrict__ bias,
+                                                      Act x, Act y, Act mask, int relu, int accumulate, int nImg, int H, int W)
+{
+    using T = PersistShape<CIN, NT>;
+    constexpr uint32_t IDESC = idescBf16(128, NT);
+    constexpr int G = T::G;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t wFull, aFull[2], aEmpty[2], accFull[2], accEmpty[2], done;
+    __shared__ uint32_t tmemSlot;
+    __shared__ volatile int abortFlag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tilesPerRow = (W + 127) / 128;
+    const int nTiles = nImg * H * tilesPerRow;
+    const int n0 = blockIdx.y * NT;
+    const uint32_t sBase = smemAddr(smem);
+    const uint32_t aBuf[2] = {sBase, sBase + T::A_BYTES};
+    const uint32_t wBuf = sBase + 2 * T::A_BYTES;
+
+    if (warp == 4)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smemAddr(&tmemSlot)),
+                     "r"(T::TCOLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0)
+    {
+        mbarInit(smemAddr(&wFull), 1);
+        for (int k = 0; k < 2; ++k)
+        {
+            mbarInit(smemAddr(&aFull[k]), 1);
+            mbarInit(smemAddr(&aEmpty[k]), 1);
+            mbarInit(smemAddr(&accFull[k]), 1);
+            mbarInit(smemAddr(&accEmpty[k]), 4);
+        }
+        mbarInit(smemAddr(&done), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        abortFlag = 0;
+    }
+    fenceBeforeSync();
+    __syncthreads();
+    fenceAfterSync();
+    const uint32_t tmem = tmemSlot;
+
+    if (warp == 4)
+    {
+        if (lane == 0)
+        {
+            // producer: the weights once, then the halo of every tile of this CTA
+            const uint32_t wf = smemAddr(&wFull);
+            expectTx(wf, (uint32_t)T::W_BYTES);
+            for (int t = 0; t < 9; ++t)
+                for (int g = 0; g < G; ++g) tmaLoad3(wBuf + (t * G + g) * NT * 16, &mapW, 8 * g, t, n0, wf);
+            int issued = 0;
+            for (int tile = blockIdx.x; tile < nTiles && !abortFlag; tile += gridDim.x, ++issued)
+            {
+                const int b = issued & 1, use = issued >> 1;
+                if (!mbarWait(smemAddr(&aEmpty[b]), (uint32_t)(use & 1) ^ 1u))
+                {
+                    abortFlag = 1;
+                    break;
+                }
+                const int rowIdx = tile / tilesPerRow, x0 = (tile % tilesPerRow) * 128;
+                const int img = rowIdx / H, yy0 = rowIdx % H;
+                const uint32_t fb = smemAddr(&aFull[b]);
+                expectTx(fb, (uint32_t)(G * T::A_GROUP));
+                for (int g = 0; g < G; ++g)
+                    tmaLoad4(aBuf[b] + g * T::A_LBO, &mapX, (int)x.off + 8 * g, x0 - 1, yy0 - 1, img, fb);
+            }
+            // the CTA may not exit before its loads have landed
+            mbarWait(wf, 0u);
+            if (issued > 0) mbarWait(smemAddr(&aFull[(issued - 1) & 1]), (uint32_t)(((issued - 1) >> 1) & 1));
+        }
+    }
+    else if (warp == 5)
+    {
+        if (lane == 0)
+        {
+            // MMA issue: nine taps x Cin / 16 MMAs per tile into the tile's TMEM buffer
+            if (!mbarWait(smemAddr(&wFull), 0u)) abortFlag = 1;
+            int it = 0;
+            for (int tile = blockIdx.x; tile < nTiles && !abortFlag; tile += gridDim.x, ++it)
+            {
+                const int b = it & 1, use = it >> 1;
+                if (!mbarWait(smemAddr(&aFull[b]), (uint32_t)(use & 1)) ||
+                    !mbarWait(smemAddr(&accEmpty[b]), (uint32_t)(use & 1) ^ 1u))
+                {
+                    abortFlag = 1;
+                    break;
+                }
+                fenceAfterSync();
+                const uint32_t d = tmem + (uint32_t)(b * NT);
+#pragma unroll
+                for (int t = 0; t < 9; ++t)
+                {
+                    const int dy = t / 3 - 1, dx = t % 3 - 1;
+                    const uint32_t a0 = aBuf[b] + (uint32_t)(((1 + dy) * T::HALO + 1 + dx) * 16);
+                    const uint32_t b0 = wBuf + t * G * NT * 16;
+#pragma unroll
+                    for (int kk = 0; kk < CIN / 16; ++kk)
+                    {
+                        const uint64_t ad = smemDesc(a0 + kk * 2 * T::A_LBO, T::A_LBO, 128);
+                        const uint64_t bd = smemDesc(b0 + kk * 2 * NT * 16, NT * 16, 128);
+                        const uint32_t acc = (t | kk) != 0 ? 1u : 0u;
+                        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                                     "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                                     : "memory");
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 smemAddr(&aEmpty[b]))
+                             : "memory");
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 smemAddr(&accFull[b]))
+                             : "memory");
+            }
+            // completes when every MMA issued above has
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smemAddr(&done))
+                         : "memory");
+        }
+    }
+    else
+    {
+        // epilogue: bias, ReLU, mask, accumulation, BF16 stores of the tile's 128 pixels x NT
+        int it = 0;
+        for (int tile = blockIdx.x; tile < nTiles; tile += gridDim.x, ++it)
+        {
+            const int b = it & 1, use = it >> 1;
+            const bool ready = mbarWait(smemAddr(&accFull[b]), (uint32_t)(use & 1));
+            if (!ready || abortFlag)
+            {
+                abortFlag = 1;
+                break;
+            }
+            fenceAfterSync();
+            const int rowIdx = tile / tilesPerRow, x0 = (tile % tilesPerRow) * 128;
+            const int img = rowIdx / H, yy0 = rowIdx % H;
+            const int xo = x0 + warp * 32 + lane;
+            const long q = ((long)(img * H + yy0)) * W + xo;
+#pragma unroll 1
+            for (int cc = 0; cc < NT; cc += 16)
+            {
+                uint32_t r[16];
+                const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * NT + cc);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                               "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                             : "r"(ta)
+                             : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                if (xo >= W) continue;
+#pragma unroll
+                for (int j = 0; j < 16; j += 2)
+                {
+                    const int co = n0 + cc + j;
+                    float v0 = __uint_as_float(r[j]), v1 = __uint_as_float(r[j + 1]);
+                    if (bias)
+                    {
+                        v0 += bias[co];
+                        v1 += bias[co + 1];
+                    }
+                    if (relu)
+                    {
+                        v0 = fmaxf(v0, 0.0f);
+                        v1 = fmaxf(v1, 0.0f);
+                    }
+                    if (mask.p)
+                    {
+                        __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(mask.p + q * mask.stride + mask.off + co);
+                        if (!(__bfloat162float(mk.x) > 0.0f)) v0 = 0.0f;
+                        if (!(__bfloat162float(mk.y) > 0.0f)) v1 = 0.0f;
+                    }
+                    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(y.p + q * y.stride + y.off + co);
+                    if (accumulate)
+                    {
+                        __nv_bfloat162 old = *dst;
+                        v0 += __bfloat162float(old.x);
+                        v1 += __bfloat162float(old.y);
+                    }
+                    *dst = __floats2bfloat162_rn(v0, v1);
+                }
+            }
+            // TMEM buffer b read: the MMAs of the tile after next may overwrite it
+            fenceBeforeSync();
+            __syncwarp();
+            if (lane == 0) mbarArrive(smemAddr(&accEmpty[b]));
+        }
+    }
+    __syncwarp();
+    const bool ok = mbarWait(smemAddr(&done), 0u);
+    if (__syncthreads_or(!ok || abortFlag))
+    {
+        if (tid == 0) atomicAdd(&g_timeouts, 1u);
+    }
+    fenceBeforeSync();
+    __syncthreads();
+    if (warp == 4)
+    {
+        fenceAfterSync();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(T::TCOLS) : "memory");
+    }
+}
+
+template <int CIN, int NT>
+int launchPersist(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate, int n,
+                  int h, int wd, int smCount, cudaStream_t st)
+{
+    using T = PersistShape<CIN, NT>;
+    EncodeTiledFn enc = encodeTiled();
+    if (!enc) return YG_ERR_CUDA;
+    alignas(64) CUtensorMap mapX, mapW;
+    const cuuint64_t dimX[4] = {x.stride, (cuuint64_t)wd, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strideX[3] = {(cuuint64_t)x.stride * 2, (cuuint64_t)x.stride * 2 * wd, (cuuint64_t)x.stride * 2 * wd * h};
+    const cuuint32_t boxX[4] = {8, (cuuint32_t)T::HALO, 3, 1};
+    const cuuint32_t ones[4] = {1, 1, 1, 1};
+    if (enc(&mapX, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)x.p, dimX, strideX, boxX, ones, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return YG_ERR_CUDA;
+    const cuuint64_t dimW[3] = {x.ch, 9, y.ch};
+    const cuuint64_t strideW[2] = {(cuuint64_t)x.ch * 2, (cuuint64_t)x.ch * 2 * 9};
+    const cuuint32_t boxW[3] = {8, 1, (cuuint32_t)NT};
+    if (enc(&mapW, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)w, dimW, strideW, boxW, ones, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return YG_ERR_CUDA;
+    // at most 512 / TCOLS CTAs per SM may hold tensor memory at once: the shared-memory request
+    // is raised until no more CTAs than that fit on an SM, so an allocation never waits
+    constexpr int floorBytes = 233472 / (512 / (int)T::TCOLS) - 2047;
+    constexpr int smemBytes = T::SMEM > floorBytes ? T::SMEM : floorBytes;
+    static_assert(smemBytes <= 232448, "shared memory");
+    static bool configured = false;
+    if (!configured)
+    {
+        if (cudaFuncSetAttribute(conv3x3Persist<CIN, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes) != cudaSuccess)
+            return YG_ERR_CUDA;
+        configured = true;
+    }
+    int perSm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, conv3x3Persist<CIN, NT>, 192, smemBytes) != cudaSuccess || perSm < 1)
+        return YG_ERR_CUDA;
+    const int nCols = (int)(y.ch / NT);
+    const long tiles = (long)n * h * ((wd + 127) / 128);
+    const long want = std::max<long>(1, (long)smCount * perSm / nCols);
+    dim3 grid((unsigned)std::min<long>(tiles, want), (unsigned)nCols);
+    conv3x3Persist<CIN, NT><<<grid, 192, smemBytes, st>>>(mapX, mapW, bias, x, y, m, relu, accumulate, n, h, wd);
+    return YG_OK;
+}
+
+// the persistent kernel where its shape is built; 1 where the layer takes conv3x3Tma instead
+int launchPersistAny(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate,
+                     int n, int h, int wd, int smCount, cudaStream_t st)
+{
+    const int ci = (int)x.ch, co = (int)y.ch;
+#define YG_PERSIST(CI, N)                                                                                                   \
+    if (ci == CI && co % N == 0) return launchPersist<CI, N>(x, w, bias, y, m, relu, accumulate, n, h, wd, smCount, st);
+    YG_PERSIST(16, 32)
+    YG_PERSIST(32, 64)
+    YG_PERSIST(32, 32)
+    YG_PERSIST(64, 64)
+    YG_PERSIST(96, 32)
+#undef YG_PERSIST
+    return 1;
+}
+
 template <int KC, int NT>
 int launchTc(const Act& x, const bf16* w, const float* bias, const Act& y, const Act& m, int relu, int accumulate, int n,
              int h, int wd, cudaStream_t st)
@@ -1301,7 +1597,16 @@ YG_API int yg_nn_conv3x3(const yg_nn_tensor* x, const void* weights, const float
     Act m = act(mask && mask->data ? mask : nullptr);
     if (g_convImpl == YG_NN_CONV_TCGEN05_TMA)
     {
-        int r;
+        int r = 1;
+        if (h * w >= (1 << 16))
+        {
+            int dev = 0, sms = 152;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            r = tc::launchPersistAny(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, sms, st);
+        }
+        if (r == YG_OK) return status(st);
+        if (r != 1) return r;
         if (x->channels % 64 == 0) r = tc::launchTmaN<64>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
         else if (x->channels % 32 == 0) r = tc::launchTmaN<32>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
         else r = tc::launchTmaN<16>(act(x), (const bf16*)weights, bias, act(y), m, relu, accumulate, n, h, w, st);
