@@ -1405,7 +1405,10 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
 // vertex) record (getLightNodeConnection + calculateLightPathRadiance, BDPTCommon.hlsl:622-635,
 // 1062-1215): the contribution and the visibility ray of each, summed later in light-vertex
 // order. The light side's MIS context comes prepared with the light vertex.
-__global__ void __launch_bounds__(128) wbConnect(const SceneView S, BdptParams B, BdptWave W, uint32_t ci)
+#ifndef YG_CONNECT_MIN_BLOCKS
+#define YG_CONNECT_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(128, YG_CONNECT_MIN_BLOCKS) wbConnect(const SceneView S, BdptParams B, BdptWave W, uint32_t ci)
 {
     const Luts Lt = bdptLuts(S);
     const uint32_t n = *W.connCount;
