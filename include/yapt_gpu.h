@@ -317,6 +317,19 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* params, yg_sample_
 /* Film readback: mean XYZ per pixel (width*height*3) and per-pixel sample counts
  * (width*height, may be NULL). Synchronises the context stream. */
 YG_API int yg_film_read(yg_context* ctx, float* xyz_mean, float* counts);
+/* Film checkpoints: the compensated XYZ sums and counts, the feature accumulators and the
+ * a-trous moments of the context's film, so that a preempted render can resume. Renders after a
+ * restore continue the accumulation exactly as if it had not stopped (same film, bit for bit).
+ * yg_film_state_size gives the bytes; yg_film_save copies the state to host memory;
+ * yg_film_restore makes it the context's film (YG_ERR_INVALID_ARGUMENT for a buffer that is not
+ * a saved state of this format). */
+YG_API int yg_film_state_size(yg_context* ctx, size_t* bytes);
+/* Debug build (compiled with -DYG_DEBUG_BOUNDS): out-of-range node, triangle and queue indices
+ * the kernels refused (counted and skipped instead of read) since the scene was built;
+ * YG_ERR_NOT_READY in a normal build. */
+YG_API int yg_debug_bounds_errors(yg_context* ctx, uint32_t* count);
+YG_API int yg_film_save(yg_context* ctx, void* host, size_t bytes);
+YG_API int yg_film_restore(yg_context* ctx, const void* host, size_t bytes);
 /* The same means written to DEVICE buffers (any may be NULL: xyz_mean and albedo/normal
  * W*H*3 floats, depth W*H); the call returns when they are written. Features need a render
  * with YG_FLAG_FEATURES since the last yg_film_clear. */

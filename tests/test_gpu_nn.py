@@ -256,3 +256,31 @@ def test_training_on_tracer_renders_beats_the_noisy_input(torch_cuda):
     r_noisy, r_den = D.relmse(noisy, ref), D.relmse(den, ref)
     assert np.all(np.isfinite(den))
     assert r_den < 0.7 * r_noisy, (r_den, r_noisy)  # three 64x64 training images: a sanity bound
+
+
+def test_training_checkpoint_resumes_the_same_updates(torch_cuda, tmp_path):
+    """A run restored from a checkpoint (FP32 weights, both Adam moments, step count) makes the
+    same updates as the run that wrote it: six steps straight equal three, save, load, three."""
+    from yapt_gb300 import denoise as D
+    torch = torch_cuda
+    n, h, w = 2, 32, 32
+    rng = np.random.default_rng(3)
+    x = dev_bf16(torch, rng.uniform(0, 1, (n * h * w * 16)))
+    target = torch.from_numpy(rng.uniform(0, 1, n * h * w * 3).astype(np.float32)).cuda()
+
+    def steps(net, k):
+        for _ in range(k):
+            net.loss_and_gradients(x, target, n, h, w)
+            net.adam_step(lr=1e-3)
+
+    a = D.UNet(seed=5)
+    steps(a, 6)
+    b = D.UNet(seed=5)
+    steps(b, 3)
+    path = str(tmp_path / "unet.npz")
+    b.save_checkpoint(path)
+    c = D.UNet.load_checkpoint(path)
+    assert c.step_count == 3
+    steps(c, 3)
+    torch.cuda.synchronize()
+    assert np.array_equal(a.parameters(), c.parameters())

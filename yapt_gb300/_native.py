@@ -219,6 +219,10 @@ SIGNATURES = [
     ("yg_film_clear", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     ("yg_render", C.c_int, [C.c_void_p, C.POINTER(RenderParams), C.c_void_p]),
     ("yg_film_read", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    ("yg_film_state_size", C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    ("yg_debug_bounds_errors", C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    ("yg_film_save", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    ("yg_film_restore", C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     ("yg_features_read", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("yg_film_relmse", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_double, C.POINTER(C.c_double)]),
     ("yg_last_render_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_uint64),

@@ -1406,7 +1406,7 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
 // 1062-1215): the contribution and the visibility ray of each, summed later in light-vertex
 // order. The light side's MIS context comes prepared with the light vertex.
 #ifndef YG_CONNECT_MIN_BLOCKS
-#define YG_CONNECT_MIN_BLOCKS 1
+#define YG_CONNECT_MIN_BLOCKS 8
 #endif
 __global__ void __launch_bounds__(128, YG_CONNECT_MIN_BLOCKS) wbConnect(const SceneView S, BdptParams B, BdptWave W, uint32_t ci)
 {

@@ -3,6 +3,7 @@
 // (RaytraceCommonResources.cpp, BindlessMaterialManager.cpp, LightManager.cpp,
 // PathTraceStage.cpp) on one CUDA stream.
 #include "yg_internal.h"
+#include "yg_nvtx.h"
 #include "yg_vec.cuh"
 
 #include <algorithm>
@@ -267,6 +268,9 @@ void fillSceneView(const yg_context* ctx, float lminf, float lmaxf, bool needRgb
     S.textures = ctx->dTexTable.as<yg::GpuTexture>();
     S.instPrimStart = ctx->dPrimStart.as<uint32_t>();
     S.triOfPrim = ctx->dTriOfPrim.as<uint32_t>();
+    S.nNodes = (uint32_t)ctx->nNodes;
+    S.nTris = (uint32_t)ctx->nTris;
+    S.boundsErrors = ctx->dBoundsErr.as<unsigned int>();
     S.envTexture = ctx->envTexture;
     S.envCube = ctx->envCube ? 1u : 0u;
     S.indices = ctx->dIdx.as<uint32_t>();
@@ -830,6 +834,7 @@ YG_API int yg_bvh_check(yg_context* ctx, uint64_t* n_nodes, uint64_t* depth, uin
 
 YG_API int yg_build_scene(yg_context* ctx)
 {
+    yg::NvtxRange range("yg_build_scene");
     if (!ctx) return fail(YG_ERR_INVALID_ARGUMENT, "null context");
     std::lock_guard<std::mutex> g(ctx->lock);
     cudaSetDevice(ctx->device);
@@ -948,6 +953,11 @@ YG_API int yg_build_scene(yg_context* ctx)
     // each primitive's position in the triangle array, for visibility tests that intersect
     // their target triangle before traversing
     if ((r = upload(ctx, ctx->dPrimStart, primStart.data(), primStart.size()))) return r;
+    if (!ctx->dBoundsErr.p)
+    {
+        YG_CUDA(ctx->dBoundsErr.ensure(16));
+        YG_CUDA(cudaMemsetAsync(ctx->dBoundsErr.p, 0, 16, ctx->stream));
+    }
     YG_CUDA(ctx->dTriOfPrim.ensure(4 * (size_t)std::max<uint32_t>(primStart[nInst], 1)));
     YG_CUDA((cudaError_t)yg::indexTrianglesByPrim(bout.tris, primStart[nInst], ctx->dPrimStart.as<uint32_t>(),
                                                     ctx->dTriOfPrim.as<uint32_t>(), ctx->stream));
@@ -1046,6 +1056,8 @@ YG_API int yg_film_clear(yg_context* ctx, uint32_t w, uint32_t h)
 YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_record* dump)
 {
     if (!ctx || !p) return fail(YG_ERR_INVALID_ARGUMENT, "render: null argument");
+    static const char* const kRangeNames[3] = {"yg_render uni", "yg_render nee", "yg_render bdpt"};
+    yg::NvtxRange range(kRangeNames[p->integrator <= YG_INTEGRATOR_BDPT ? p->integrator : 0]);
     std::lock_guard<std::mutex> g(ctx->lock);
     if (!ctx->sceneBuilt) return fail(YG_ERR_NOT_READY, "render: call yg_build_scene first");
     if (!ctx->cameraSet) return fail(YG_ERR_NOT_READY, "render: camera not set");
@@ -1297,6 +1309,113 @@ YG_API int yg_film_read(yg_context* ctx, float* xyz, float* counts)
         xyz[3 * i + 2] = s[i].z * inv;
         if (counts) counts[i] = c;
     }
+    return YG_OK;
+}
+
+namespace
+{
+// film checkpoint layout: header, then the planes (float4 per pixel) in this order
+struct FilmStateHeader
+{
+    uint64_t magic;
+    uint32_t version, width, height, atrousState, atrousPlanes, reserved;
+};
+constexpr uint64_t kFilmMagic = 0x4D4C4946475930ull; // "0YGFILM"
+constexpr uint32_t kFilmPlanes = 4;                  // sums, compensation, albedo and normal accumulators
+uint32_t atrousPlanesOf(const yg_context* c)
+{
+    const size_t plane = (size_t)c->filmW * c->filmH * sizeof(float4);
+    // the moments exist once an a-trous render has gathered into this film (states 1 and 3)
+    return ((c->atrousState & 1) != 0 && c->dAtrousMom.bytes >= 4 * plane && c->dAtrousOdd.bytes >= plane) ? 5u : 0u;
+}
+size_t filmStateBytes(const yg_context* c)
+{
+    return sizeof(FilmStateHeader) + (size_t)(kFilmPlanes + atrousPlanesOf(c)) * c->filmW * c->filmH * sizeof(float4);
+}
+} // namespace
+
+YG_API int yg_debug_bounds_errors(yg_context* ctx, uint32_t* count)
+{
+    if (!ctx || !count) return fail(YG_ERR_INVALID_ARGUMENT, "bounds errors: null argument");
+#ifndef YG_DEBUG_BOUNDS
+    return fail(YG_ERR_NOT_READY, "bounds errors: the library was built without YG_DEBUG_BOUNDS");
+#else
+    std::lock_guard<std::mutex> g(ctx->lock);
+    *count = 0;
+    if (!ctx->dBoundsErr.p) return YG_OK;
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    YG_CUDA(cudaMemcpy(count, ctx->dBoundsErr.p, 4, cudaMemcpyDeviceToHost));
+    return YG_OK;
+#endif
+}
+
+YG_API int yg_film_state_size(yg_context* ctx, size_t* bytes)
+{
+    if (!ctx || !bytes) return fail(YG_ERR_INVALID_ARGUMENT, "film state: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    if (ctx->filmW == 0) return fail(YG_ERR_NOT_READY, "film: not allocated");
+    *bytes = filmStateBytes(ctx);
+    return YG_OK;
+}
+
+YG_API int yg_film_save(yg_context* ctx, void* host, size_t bytes)
+{
+    if (!ctx || !host) return fail(YG_ERR_INVALID_ARGUMENT, "film save: null argument");
+    std::lock_guard<std::mutex> g(ctx->lock);
+    if (ctx->filmW == 0) return fail(YG_ERR_NOT_READY, "film: not allocated");
+    if (bytes < filmStateBytes(ctx)) return fail(YG_ERR_INVALID_ARGUMENT, "film save: buffer smaller than yg_film_state_size");
+    YG_CUDA(cudaSetDevice(ctx->device));
+    FilmStateHeader h{kFilmMagic, 1u, ctx->filmW, ctx->filmH, (uint32_t)ctx->atrousState, atrousPlanesOf(ctx), 0u};
+    std::memcpy(host, &h, sizeof(h));
+    char* dst = static_cast<char*>(host) + sizeof(h);
+    const size_t plane = (size_t)ctx->filmW * ctx->filmH * sizeof(float4);
+    const DevBuf* planes[4] = {&ctx->dFilmSum, &ctx->dFilmComp, &ctx->dAccA, &ctx->dAccN};
+    for (const DevBuf* b : planes)
+    {
+        YG_CUDA(cudaMemcpyAsync(dst, b->p, plane, cudaMemcpyDeviceToHost, ctx->stream));
+        dst += plane;
+    }
+    if (h.atrousPlanes)
+    {
+        YG_CUDA(cudaMemcpyAsync(dst, ctx->dAtrousMom.p, 4 * plane, cudaMemcpyDeviceToHost, ctx->stream));
+        YG_CUDA(cudaMemcpyAsync(dst + 4 * plane, ctx->dAtrousOdd.p, plane, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return YG_OK;
+}
+
+YG_API int yg_film_restore(yg_context* ctx, const void* host, size_t bytes)
+{
+    if (!ctx || !host) return fail(YG_ERR_INVALID_ARGUMENT, "film restore: null argument");
+    if (bytes < sizeof(FilmStateHeader)) return fail(YG_ERR_INVALID_ARGUMENT, "film restore: not a film state");
+    FilmStateHeader h;
+    std::memcpy(&h, host, sizeof(h));
+    if (h.magic != kFilmMagic || h.version != 1u || h.width == 0 || h.height == 0 || (h.atrousPlanes != 0 && h.atrousPlanes != 5) ||
+        h.atrousState > 3)
+        return fail(YG_ERR_INVALID_ARGUMENT, "film restore: not a film state");
+    const size_t plane = (size_t)h.width * h.height * sizeof(float4);
+    if (bytes < sizeof(h) + (kFilmPlanes + h.atrousPlanes) * plane)
+        return fail(YG_ERR_INVALID_ARGUMENT, "film restore: buffer shorter than its state");
+    int r = yg_film_clear(ctx, h.width, h.height);
+    if (r) return r;
+    std::lock_guard<std::mutex> g(ctx->lock);
+    YG_CUDA(cudaSetDevice(ctx->device));
+    const char* src = static_cast<const char*>(host) + sizeof(h);
+    DevBuf* planes[4] = {&ctx->dFilmSum, &ctx->dFilmComp, &ctx->dAccA, &ctx->dAccN};
+    for (DevBuf* b : planes)
+    {
+        YG_CUDA(cudaMemcpyAsync(b->p, src, plane, cudaMemcpyHostToDevice, ctx->stream));
+        src += plane;
+    }
+    if (h.atrousPlanes)
+    {
+        YG_CUDA(ctx->dAtrousMom.ensure(4 * plane));
+        YG_CUDA(ctx->dAtrousOdd.ensure(plane));
+        YG_CUDA(cudaMemcpyAsync(ctx->dAtrousMom.p, src, 4 * plane, cudaMemcpyHostToDevice, ctx->stream));
+        YG_CUDA(cudaMemcpyAsync(ctx->dAtrousOdd.p, src + 4 * plane, plane, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    YG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->atrousState = (int)h.atrousState;
     return YG_OK;
 }
 

@@ -8,6 +8,7 @@
 // Samples of a launch are written to a [sample][pixel] buffer and folded into the
 // film in sample order, so the film does not depend on thread scheduling.
 #include "yg_wave.cuh"
+#include "yg_nvtx.h"
 
 #include <algorithm>
 
@@ -305,10 +306,16 @@ __global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const __grid
             }
         }
         uint32_t k = warpAppend(Qout.count, alive);
+#ifdef YG_DEBUG_BOUNDS
+        if (alive && !YG_BOUNDS(k < W.capacity, S.boundsErrors)) alive = false;
+#endif
         if (alive) storeQueued(Qout, k, slot, ps, rs, sp.hero, (uint32_t)(rs.point - S.sobol) / kSobolDims);
         if (NEE || S.nPunctual > 0)
         {
             uint32_t q = warpAppend(SQ.count, sr.valid);
+#ifdef YG_DEBUG_BOUNDS
+            if (sr.valid && !YG_BOUNDS(q < W.capacity, S.boundsErrors)) sr.valid = false;
+#endif
             if (sr.valid)
             {
                 SQ.o[q] = mk4(sr.origin.x, sr.origin.y, sr.origin.z, __uint_as_float(alive ? k : (slot | kShadowToSlot)));
@@ -609,6 +616,7 @@ int launchWavefront(const SceneView& S, const LaunchParams& P, void* arena, uint
         uint32_t n = (uint32_t)((P.nSamples - base) < C ? (P.nSamples - base) : C);
         int gblocks = (int)((n + 255) / 256);
         if (gblocks > smCount * 8) gblocks = smCount * 8;
+        NvtxRange waveRange("wave");
         wfGenerate<<<gblocks, 256, 0, stream>>>(S, P, W, QA, base, n);
         ++launches;
         // QA: the live paths in trace order; QB: the same paths regrouped by shading class.

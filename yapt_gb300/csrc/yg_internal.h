@@ -109,6 +109,7 @@ struct yg_context
     DevBuf dCie, dRgb, dSobol, dSobolMat, dSamples, dDump, dFeatA, dFeatN, dRelmse, dRef, dRayCount;
     DevBuf dFilmSum, dFilmComp, dAccA, dAccN, dArena, dPerm;
     DevBuf dPrimStart, dTriOfPrim; // first primitive of each instance; each primitive's triangle slot
+    DevBuf dBoundsErr;             // debug build: out-of-range accesses the kernels refused
     DevBuf dAtrousMom, dAtrousOdd, dAtrousFeat, dAtrousCol, dAtrousVar; // a-trous denoiser state
     std::vector<DevBuf> texBufs;          // decoded texels of each texture
     std::vector<yg::GpuTexture> texTable; // device pointers and sizes, mirrored in dTexTable
@@ -143,7 +144,7 @@ struct yg_context
     {
         DevBuf* all[] = {&dTris, &dNodes, &dInst, &dMat, &dLights, &dPos, &dNrm, &dTan, &dUV, &dIdx, &dSpec, &dCie, &dRgb,
                          &dSobol, &dSobolMat, &dSamples, &dDump, &dFeatA, &dFeatN, &dRelmse, &dRef, &dRayCount, &dFilmSum,
-                         &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm, &dPrimStart, &dTriOfPrim, &dAtrousMom, &dAtrousOdd,
+                         &dFilmComp, &dAccA, &dAccN, &dArena, &dPerm, &dPrimStart, &dTriOfPrim, &dBoundsErr, &dAtrousMom, &dAtrousOdd,
                          &dAtrousFeat, &dAtrousCol, &dAtrousVar};
         for (DevBuf* b : all) b->release();
         for (DevBuf& b : texBufs) b.release();

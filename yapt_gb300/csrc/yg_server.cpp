@@ -9,6 +9,7 @@
 // (scene, camera, seed, sample index, pixel), so a result is the same film whether the
 // request ran alone (yg_render) or merged with any others.
 #include "yg_internal.h"
+#include "yg_nvtx.h"
 
 #include <chrono>
 #include <condition_variable>
@@ -309,6 +310,7 @@ void sobolPlanes(yg_context* ctx, uint32_t first, uint32_t count, uint32_t* out)
 // launches one merged round for the planned segments on stream A
 int launchMerged(yg_server* s, std::vector<Segment>& segs)
 {
+    yg::NvtxRange range("serve merged round");
     const uint32_t slots = s->opt.max_active;
     TableLayout T = tableLayout(slots);
     char* h = s->tablesHost;
@@ -411,6 +413,7 @@ int launchMerged(yg_server* s, std::vector<Segment>& segs)
 
 int launchBdptSlice(yg_server* s, Req& r, uint32_t planes)
 {
+    yg::NvtxRange range("serve BDPT slice");
     yg_context* ctx = s->scenes[r.scene];
     auto key = std::make_pair(r.cw, r.ch);
     if (!s->perms.count(key))

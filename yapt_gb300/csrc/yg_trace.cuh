@@ -144,10 +144,24 @@ __device__ __forceinline__ float biasedByte(uint32_t lo4, uint32_t hi4, int i)
 
 // One ray's traversal, advanced one node at a time by traceStep so that a persistent
 // kernel can hand a lane a new ray as soon as its ray is done.
+// Debug build (YG_DEBUG_BOUNDS): node and triangle indices are checked against the scene's
+// counts before they are read; an out-of-range index is counted in the scene's error word and
+// the access skipped (the traversal ends), so a faulty tree shows as a count, never as a fault.
+#ifdef YG_DEBUG_BOUNDS
+#define YG_BOUNDS(ok, errors)                                                                                          \
+    (((ok) ? true : ((errors) ? (atomicAdd((errors), 1u), false) : false)))
+#else
+#define YG_BOUNDS(ok, errors) true
+#endif
+
 struct TraceState
 {
     const float4* nodes;
     const float4* tris;
+#ifdef YG_DEBUG_BOUNDS
+    uint32_t nNodes, nTris;
+    unsigned int* errors;
+#endif
     float3 o, d, inv;
     float tmin;
     uint32_t oct;
@@ -192,6 +206,11 @@ __device__ __forceinline__ void traceBegin(TraceState& t, const SceneView& S, fl
 {
     t.nodes = S.nodes;
     t.tris = S.tris;
+#ifdef YG_DEBUG_BOUNDS
+    t.nNodes = S.nNodes;
+    t.nTris = S.nTris;
+    t.errors = S.boundsErrors;
+#endif
     t.o = o;
     t.d = d;
     t.inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
@@ -223,6 +242,14 @@ __device__ __forceinline__ bool traceStep(TraceState& t, Stack& st, TraversalCou
     const uint32_t slot = (uint32_t)(__ffs(t.gHits) - 1) ^ t.oct;
     t.gHits &= t.gHits - 1;
     const uint32_t idx = t.gBase + __popc(t.gImask & ((1u << slot) - 1u));
+#ifdef YG_DEBUG_BOUNDS
+    if (!YG_BOUNDS(idx < t.nNodes, t.errors))
+    {
+        t.gHits = 0;
+        t.sp = 0;
+        return false;
+    }
+#endif
     if (++t.visits > kMaxNodeVisits) return false;
     const float4* __restrict__ np = t.nodes + 5 * (size_t)idx;
     const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
@@ -284,6 +311,9 @@ __device__ __forceinline__ bool traceStep(TraceState& t, Stack& st, TraversalCou
         {
             const uint32_t j = __ffs(triHits) - 1;
             triHits &= triHits - 1;
+#ifdef YG_DEBUG_BOUNDS
+            if (!YG_BOUNDS(triBase + j < t.nTris, t.errors)) continue;
+#endif
             intersectTri<FILTER>(t.tris, (int)(triBase + j), t.o, t.d, t.tmin, t.h, t.found, t.onlyInst);
         }
     }

@@ -136,6 +136,8 @@ struct SceneView
     const uint32_t* sobol; // [spp_count][kSobolDims] points of this launch
     const uint32_t* instPrimStart; // first primitive of each instance in the scene's primitive order
     const uint32_t* triOfPrim;     // position in `tris` of each primitive (0xffffffff: none)
+    uint32_t nNodes, nTris;        // wide nodes and triangles (bounds of the debug build's checks)
+    unsigned int* boundsErrors;    // debug build (YG_DEBUG_BOUNDS): out-of-range accesses refused
     GpuCamera cam;
     const GpuTexture* textures;
     int envTexture;        // environment texture, -1: the analytic sky

@@ -115,6 +115,25 @@ class UNet:
     def parameters(self):
         return self.p.detach().cpu().numpy()
 
+    # -- training checkpoints -------------------------------------------------
+    def save_checkpoint(self, path):
+        """Writes the FP32 weights, both Adam moments and the step count (an .npz file): a run
+        restored from it continues with the same updates as the run that wrote it."""
+        self.torch.cuda.synchronize(self.dev)
+        np.savez(path, params=self.p.cpu().numpy(), adam_m=self.m.cpu().numpy(), adam_v=self.v.cpu().numpy(),
+                 step=np.int64(self.step_count), layout=np.int64(self.n))
+
+    @classmethod
+    def load_checkpoint(cls, path, device=0):
+        z = np.load(path)
+        if int(z["layout"]) != parameter_layout()[1]:
+            raise ValueError("checkpoint %s: parameter layout of another network" % path)
+        net = cls(params=z["params"], device=device)
+        net.m.copy_(net.torch.from_numpy(z["adam_m"]).to(net.dev))
+        net.v.copy_(net.torch.from_numpy(z["adam_v"]).to(net.dev))
+        net.step_count = int(z["step"])
+        return net
+
     # -- buffers ------------------------------------------------------------
     def _buffers(self, n, h, w):
         key = (n, h, w)

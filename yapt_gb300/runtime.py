@@ -94,6 +94,21 @@ class Context:
     def synchronize(self):
         N.check(self.lib.yg_synchronize(self.h))
 
+    def film_save(self):
+        """The film's state (compensated sums, counts, feature and a-trous accumulators) as bytes."""
+        n = C.c_size_t()
+        N.check(self.lib.yg_film_state_size(self.h, C.byref(n)))
+        buf = (C.c_uint8 * n.value)()
+        N.check(self.lib.yg_film_save(self.h, buf, n.value))
+        return bytes(buf)
+
+    def film_restore(self, state):
+        """Makes a state from film_save this context's film; renders continue its accumulation."""
+        buf = (C.c_uint8 * len(state)).from_buffer_copy(state)
+        N.check(self.lib.yg_film_restore(self.h, buf, len(state)))
+        w, h = np.frombuffer(state[12:20], np.uint32)
+        self.width, self.height = int(w), int(h)
+
     def film(self):
         xyz = np.zeros((self.height, self.width, 3), np.float32)
         cnt = np.zeros((self.height, self.width), np.float32)
