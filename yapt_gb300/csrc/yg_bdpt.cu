@@ -1137,7 +1137,7 @@ __global__ void __launch_bounds__(128) wbGenerate(const SceneView S, const Launc
 
 // closest hits of the queued camera rays; a queued subsurface exit (d.w = 1) is not traced, its
 // hit is the exit point stored by the vertex that took the subsurface event
-__global__ void __launch_bounds__(128) wbTrace(const SceneView S, RayQueue Q, HitQueue H, const float4* exitHit)
+__global__ void __launch_bounds__(128, YG_TRACE_MIN_BLOCKS) wbTrace(const SceneView S, RayQueue Q, HitQueue H, const float4* exitHit)
 {
     TraversalCount tc{0, 0};
     uint32_t rays = 0;
@@ -1162,7 +1162,10 @@ __global__ void __launch_bounds__(128) wbTrace(const SceneView S, RayQueue Q, Hi
 }
 
 // one camera vertex per queued path (the body of the bounce loop of traceCameraRays)
-__global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchParams P, BdptParams B, BdptWave W,
+#ifndef YG_WBSHADE_MIN_BLOCKS
+#define YG_WBSHADE_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(128, YG_WBSHADE_MIN_BLOCKS) wbShade(const SceneView S, const LaunchParams P, BdptParams B, BdptWave W,
                                               RayQueue Qin, HitQueue H, RayQueue Qout, uint32_t ci)
 {
     const Luts Lt = bdptLuts(S);
@@ -1406,7 +1409,7 @@ __global__ void __launch_bounds__(128) wbShade(const SceneView S, const LaunchPa
 // 1062-1215): the contribution and the visibility ray of each, summed later in light-vertex
 // order. The light side's MIS context comes prepared with the light vertex.
 #ifndef YG_CONNECT_MIN_BLOCKS
-#define YG_CONNECT_MIN_BLOCKS 8
+#define YG_CONNECT_MIN_BLOCKS 16
 #endif
 __global__ void __launch_bounds__(128, YG_CONNECT_MIN_BLOCKS) wbConnect(const SceneView S, BdptParams B, BdptWave W, uint32_t ci)
 {
@@ -1508,7 +1511,7 @@ __global__ void __launch_bounds__(128, YG_CONNECT_MIN_BLOCKS) wbConnect(const Sc
 
 // visibility of the connection records (checkVisibility: the segment must reach the light
 // vertex's own triangle first; toward the environment nothing may be hit)
-__global__ void __launch_bounds__(128) wbVisibility(const SceneView S, BdptWave W)
+__global__ void __launch_bounds__(128, YG_TRACE_MIN_BLOCKS) wbVisibility(const SceneView S, BdptWave W)
 {
     TraversalCount tc{0, 0};
     uint32_t rays = 0;

@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(256) wfGenerate(const __grid_constant__ SceneV
 // Closest hits of the queued paths, each with its shading-class key for the regroup (the class
 // counts are summed per group of lanes that finish together, one atomic per class and group).
 template <bool COUNT>
-__global__ void __launch_bounds__(128) wfTrace(const __grid_constant__ SceneView S, PathQueue Q, HitQueue H, uint8_t* keys,
+__global__ void __launch_bounds__(128, YG_TRACE_MIN_BLOCKS) wfTrace(const __grid_constant__ SceneView S, PathQueue Q, HitQueue H, uint8_t* keys,
                                                uint32_t* classCounts, unsigned long long* rayCtr, unsigned long long* travCtr)
 {
     const uint32_t n = *Q.count;
@@ -242,9 +242,6 @@ __global__ void __launch_bounds__(256) wfRegroupQ(PathQueue A, HitQueue H, const
 // so that the warps resident on an SM run one kind of surface and share its instructions.
 // Continuing paths are appended to Qout (record by record), ended ones leave their radiance in
 // their slot.
-#ifndef YG_SHADE_MIN_BLOCKS
-#define YG_SHADE_MIN_BLOCKS 4
-#endif
 template <bool NEE>
 __global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const __grid_constant__ SceneView S, const __grid_constant__ LaunchParams P, SlotState W,
                                                                    PathQueue Qin, HitQueue H, PathQueue Qout, ShadowQueue SQ,
@@ -330,7 +327,7 @@ __global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const __grid
 // Shadow rays: a visible light adds its contribution to the path's record in the next queue, or
 // to the slot of a path that ended at this vertex.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) wfShadow(const __grid_constant__ SceneView S, SlotState W, PathQueue Qnext, ShadowQueue SQ,
+__global__ void __launch_bounds__(128, YG_TRACE_MIN_BLOCKS) wfShadow(const __grid_constant__ SceneView S, SlotState W, PathQueue Qnext, ShadowQueue SQ,
                                                 unsigned long long* rayCtr, unsigned long long* travCtr)
 {
     const uint32_t n = *SQ.count;

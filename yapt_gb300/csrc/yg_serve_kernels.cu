@@ -169,7 +169,7 @@ __device__ __forceinline__ void shadeBody(const MultiTables& M, const WaveState&
         }
     }
 }
-__global__ void __launch_bounds__(128, 4) wfmShade(MultiTables M, WaveState W, RayQueue Qin, HitQueue H, RayQueue Qout,
+__global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfmShade(MultiTables M, WaveState W, RayQueue Qin, HitQueue H, RayQueue Qout,
                                                 ShadowQueue SQ)
 {
     shadeBody(M, W, Qin, H, Qout, SQ);

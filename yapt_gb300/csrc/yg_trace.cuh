@@ -186,6 +186,10 @@ struct TraceStack
 // rarely touched and the node and triangle loads keep the L1 to themselves.
 constexpr int kSharedStack = 8;
 constexpr int kTraceBlock = 128; // the block size of every kernel that uses traceGrid
+// resident blocks per SM the traversal kernels ask for (__launch_bounds__ minimum)
+#ifndef YG_TRACE_MIN_BLOCKS
+#define YG_TRACE_MIN_BLOCKS 1
+#endif
 struct SharedTraceStack
 {
     uint2* sh; // this thread's slice (entry k at sh[k * kTraceBlock]), or null: local only

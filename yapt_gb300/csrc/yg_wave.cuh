@@ -75,6 +75,13 @@ YG_DEV uint64_t sampleOfSlot(const LaunchParams& P, uint64_t base, uint32_t n, u
     return g0 + (uint64_t)y * W + x;
 }
 
+// Resident 128-thread blocks per SM the shading kernels ask for (__launch_bounds__ minimum): 8
+// (64 registers, the rest spilled to L1-resident local memory) measured faster than 4, 6, 12 or
+// 16 on the NEE workload; more warps hide the instruction-fetch and memory latency.
+#ifndef YG_SHADE_MIN_BLOCKS
+#define YG_SHADE_MIN_BLOCKS 8
+#endif
+
 YG_DEV Luts lutsOf(const SceneView& S)
 {
     return Luts{S.lutSS, S.lutSSAvg, S.lutSSMS, S.lutSSMSAvg, S.lutTransDenser, S.lutTransLighter,
