@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <functional>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -1393,6 +1394,9 @@ YG_API int yg_film_restore(yg_context* ctx, const void* host, size_t bytes)
     if (h.magic != kFilmMagic || h.version != 1u || h.width == 0 || h.height == 0 || (h.atrousPlanes != 0 && h.atrousPlanes != 5) ||
         h.atrousState > 3)
         return fail(YG_ERR_INVALID_ARGUMENT, "film restore: not a film state");
+    // a corrupt header must not wrap the size arithmetic below (9 planes at most)
+    if ((size_t)h.width * h.height > (SIZE_MAX - sizeof(h)) / (9 * sizeof(float4)))
+        return fail(YG_ERR_INVALID_ARGUMENT, "film restore: film size out of range");
     const size_t plane = (size_t)h.width * h.height * sizeof(float4);
     if (bytes < sizeof(h) + (kFilmPlanes + h.atrousPlanes) * plane)
         return fail(YG_ERR_INVALID_ARGUMENT, "film restore: buffer shorter than its state");
