@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(128, YG_SHADE_MIN_BLOCKS) wfShade(const __grid
 // Shadow rays: a visible light adds its contribution to the path's record in the next queue, or
 // to the slot of a path that ended at this vertex.
 template <bool COUNT>
-__global__ void __launch_bounds__(128, YG_TRACE_MIN_BLOCKS) wfShadow(const __grid_constant__ SceneView S, SlotState W, PathQueue Qnext, ShadowQueue SQ,
+__global__ void __launch_bounds__(128, YG_SHADOW_MIN_BLOCKS) wfShadow(const __grid_constant__ SceneView S, SlotState W, PathQueue Qnext, ShadowQueue SQ,
                                                 unsigned long long* rayCtr, unsigned long long* travCtr)
 {
     const uint32_t n = *SQ.count;
