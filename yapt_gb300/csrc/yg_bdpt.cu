@@ -1511,31 +1511,32 @@ __global__ void __launch_bounds__(128, YG_CONNECT_MIN_BLOCKS) wbConnect(const Sc
 
 // visibility of the connection records (checkVisibility: the segment must reach the light
 // vertex's own triangle first; toward the environment nothing may be hit)
-__global__ void __launch_bounds__(128, YG_TRACE_MIN_BLOCKS) wbVisibility(const SceneView S, BdptWave W)
+__global__ void __launch_bounds__(128, YG_SHADOW_MIN_BLOCKS) wbVisibility(const SceneView S, BdptWave W)
 {
     TraversalCount tc{0, 0};
     uint32_t rays = 0;
-    const uint32_t n = *W.connCount;
-    TraceState t;
-    TraceStack st;
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
-    {
-        const float4 d = W.C.d[e];
-        if (d.w < 0.0f)
-        {
-            W.vis[e] = 0;
-            continue;
-        }
-        const float4 o = W.C.o[e];
-        // the light vertex's own triangle must be the first hit; toward a target without
-        // geometry (kPunctualShadow) nothing may be hit
-        const uint2 tg = W.C.target[e];
-        const bool early = shadowBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, tg.x, tg.y);
-        while (traceStep<false>(t, st, &tc))
-            if (shadowStopped(t, early, tg.x, tg.y)) break;
-        W.vis[e] = shadowVisible(t.found, t.h, tg.x, tg.y);
-        ++rays;
-    }
+    uint2 tg = make_uint2(0u, 0u);
+    bool early = false, none = false;
+    traceGridStop<false>(
+        *W.connCount,
+        [&](TraceState& t, uint32_t e) {
+            const float4 d = W.C.d[e];
+            // a record without a connection (d.w < 0) has no ray: its traversal is empty
+            none = d.w < 0.0f;
+            if (none)
+            {
+                t.gHits = 0;
+                t.sp = 0;
+                return;
+            }
+            const float4 o = W.C.o[e];
+            // the light vertex's own triangle must be the first hit; toward a target without
+            // geometry (kPunctualShadow) nothing may be hit
+            tg = W.C.target[e];
+            early = shadowBegin(t, S, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), kRayMinT, d.w, tg.x, tg.y);
+        },
+        [&](const TraceState& t, uint32_t e) { W.vis[e] = !none && shadowVisible(t.found, t.h, tg.x, tg.y); },
+        [&](const TraceState& t) { return shadowStopped(t, early, tg.x, tg.y); }, tc, rays);
 }
 
 // adds each path's visible connections of this bounce, in light-vertex order
