@@ -382,7 +382,8 @@ def run_ours(args, world, rank, local):
     launches = 0
     rays = 0
     kinds = {}
-    time_flag = 0 if bdpt else N.YG_FLAG_TIME_KERNELS
+    time_flag = N.YG_FLAG_TIME_KERNELS
+    timed_kinds = list(N.KERNEL_KINDS) + (["connect"] if bdpt else [])
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
@@ -397,7 +398,7 @@ def run_ours(args, world, rank, local):
             rays += st["rays"]
             if time_flag:
                 kp = ctx.kernel_profile()
-                for k in N.KERNEL_KINDS:
+                for k in timed_kinds:
                     acc = kinds.setdefault(k, {"ms": 0.0, "launches": 0})
                     acc["ms"] += kp[k]["ms"]
                     acc["launches"] += kp[k]["launches"]
@@ -426,11 +427,27 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = read_peaks()
     traffic = None
     if bdpt:
-        # the bidirectional kernels have no counting variant: whole render, node + film bytes unknown
+        # per-kind device time of the camera-side kernels from the timed steps; the connection
+        # records from one counting render of the same workload. Algorithmic bytes of wbConnect,
+        # per record: its (camera slot, light vertex) pair, the camera vertex's surface, context
+        # and state, the prepared light vertex (read once per record, as the kernel does; L1/L2
+        # serve the repeats), and the record written (origin, direction, target, contribution).
+        ctx.render(params(0, flags=N.YG_FLAG_COUNT_TRAVERSAL | N.YG_FLAG_NO_FILM | N.YG_FLAG_TIME_KERNELS))
+        kp = ctx.kernel_profile()
         tc = {"nodes": 0, "triangles": 0}
-        per_launch_bytes = W * H * spp * 16
-        avg_ms = sum(kernel_ms) / len(kernel_ms)
-        dominant = {"kernel": "whole render (bidirectional)", "avg_launch_ms": avg_ms}
+        names = {"trace": "wbTrace", "regroup": "wfClassify+wfRegroup", "shade": "wbShade", "connect": "wbConnect",
+                 "shadow": "wbVisibility+wbAccumulate"}
+        total_ms = sum(v["ms"] for v in kinds.values())
+        records = kp["shadow_rays"] / max(1, kp["connect"]["launches"])
+        per_launch_bytes = records * kp["connection_record_bytes"]
+        avg_ms = kinds["connect"]["ms"] / max(1, kinds["connect"]["launches"])
+        shares = {names[k]: v["ms"] / total_ms for k, v in kinds.items()}
+        dominant = {"kernel": "wbConnect", "largest_share": max(shares, key=shares.get), "timed_share_by_kind": shares,
+                    "kernels": {"wbConnect": {"records_per_launch": records,
+                                              "bytes_per_record": kp["connection_record_bytes"],
+                                              "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_ms": avg_ms,
+                                              "achieved_gbs": per_launch_bytes / (avg_ms / 1e3) / 1e9,
+                                              "share_of_timed_kernels": kinds["connect"]["ms"] / total_ms}}}
     else:
         # per-kind device time from the timed steps; algorithmic bytes from one counting step
         # of the same workload (same kernels, traversal counters on), per bounce:

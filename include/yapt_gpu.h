@@ -406,17 +406,25 @@ YG_API int yg_last_traversal_counts(yg_context* ctx, uint64_t* nodes_visited, ui
 
 /* Per-kernel device time of the most recent wavefront render made with YG_FLAG_TIME_KERNELS
  * (CUDA events on the context stream around every launch of a kind), and with
- * YG_FLAG_COUNT_TRAVERSAL the traversal work split between closest-hit and shadow rays. */
+ * YG_FLAG_COUNT_TRAVERSAL the traversal work split between closest-hit and shadow rays.
+ * A BDPT render times its camera-side kernels by the same kinds (trace: camera rays; regroup:
+ * class keys and regroup; shade: camera vertices; shadow: visibility rays and accumulation)
+ * plus its connection kernel, and counts its connection records. */
 #define YG_KERNEL_TRACE 0   /* closest-hit traversal of the path queue */
 #define YG_KERNEL_REGROUP 1 /* shading-class keys and the regrouping scatter */
 #define YG_KERNEL_SHADE 2   /* surface interaction, BSDF sampling, light sampling */
 #define YG_KERNEL_SHADOW 3  /* shadow-ray traversal */
+#define YG_KERNEL_CONNECT 4 /* BDPT: camera-vertex x light-vertex connections (connect_ms) */
 typedef struct yg_kernel_profile
 {
     float ms[4];          /* summed device milliseconds per YG_KERNEL_* kind */
     uint32_t launches[4]; /* timed launches per kind */
     uint64_t closest_rays, closest_nodes, closest_triangles;
-    uint64_t shadow_rays, shadow_nodes, shadow_triangles;
+    uint64_t shadow_rays, shadow_nodes, shadow_triangles; /* BDPT: shadow_rays = connection records */
+    float connect_ms;                 /* BDPT: the connection kernel's device time */
+    uint32_t connect_launches;
+    uint32_t connection_record_bytes; /* bytes the connection kernel moves per record */
+    uint32_t reserved;
 } yg_kernel_profile;
 YG_API int yg_last_kernel_profile(yg_context* ctx, yg_kernel_profile* out);
 

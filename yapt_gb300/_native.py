@@ -127,7 +127,9 @@ class KernelProfile(C.Structure):
     """yg_kernel_profile: per-kind device time of the last wavefront render."""
     _fields_ = [("ms", C.c_float * 4), ("launches", C.c_uint32 * 4),
                 ("closest_rays", C.c_uint64), ("closest_nodes", C.c_uint64), ("closest_triangles", C.c_uint64),
-                ("shadow_rays", C.c_uint64), ("shadow_nodes", C.c_uint64), ("shadow_triangles", C.c_uint64)]
+                ("shadow_rays", C.c_uint64), ("shadow_nodes", C.c_uint64), ("shadow_triangles", C.c_uint64),
+                ("connect_ms", C.c_float), ("connect_launches", C.c_uint32), ("connection_record_bytes", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 KERNEL_KINDS = ("trace", "regroup", "shade", "shadow")

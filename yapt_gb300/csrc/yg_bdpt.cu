@@ -1511,7 +1511,8 @@ __global__ void __launch_bounds__(128, YG_CONNECT_MIN_BLOCKS) wbConnect(const Sc
 
 // visibility of the connection records (checkVisibility: the segment must reach the light
 // vertex's own triangle first; toward the environment nothing may be hit)
-__global__ void __launch_bounds__(128, YG_SHADOW_MIN_BLOCKS) wbVisibility(const SceneView S, BdptWave W)
+__global__ void __launch_bounds__(128, YG_SHADOW_MIN_BLOCKS) wbVisibility(const SceneView S, BdptWave W,
+                                                                         unsigned long long* travCtr)
 {
     TraversalCount tc{0, 0};
     uint32_t rays = 0;
@@ -1537,6 +1538,7 @@ __global__ void __launch_bounds__(128, YG_SHADOW_MIN_BLOCKS) wbVisibility(const 
         },
         [&](const TraceState& t, uint32_t e) { W.vis[e] = !none && shadowVisible(t.found, t.h, tg.x, tg.y); },
         [&](const TraceState& t) { return shadowStopped(t, early, tg.x, tg.y); }, tc, rays);
+    countRays(travCtr ? travCtr + 5 : nullptr, rays);
 }
 
 // adds each path's visible connections of this bounce, in light-vertex order
@@ -1760,8 +1762,15 @@ size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVer
     return b;
 }
 
+uint32_t bdptConnectionRecordBytes()
+{
+    return (uint32_t)(sizeof(uint2) + sizeof(Surface) + sizeof(SurfaceCtx) + sizeof(ConnVertex) + sizeof(SharedNode) +
+                      16 + 16 + 8 + 16);
+}
+
 int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uint32_t* perm, uint32_t lightPaths,
-               uint32_t maxLightVerts, float3 worldCenter, float worldRadiusSqr, int smCount, cudaStream_t stream)
+               uint32_t maxLightVerts, float3 worldCenter, float worldRadiusSqr, int smCount, cudaStream_t stream,
+               KernelTimer* T)
 {
     BdptParams B;
     const uint64_t cropPix = (uint64_t)P.cropW * P.cropH;
@@ -1849,17 +1858,27 @@ int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uin
         RayQueue* nxt = &QB;
         for (uint32_t ci = 0; ci < P.maxDepth; ++ci)
         {
+            if (T) T->begin(stream);
             wbTrace<<<traceBlocks, 128, 0, stream>>>(S, *cur, H, W.exitHit);
+            if (T) T->end(kKernelTrace, stream);
             cudaMemsetAsync(nxt->count, 0, 4, stream);
             cudaMemsetAsync(W.connCount, 0, 4, stream);
             // shading coherence: hits grouped by material class before the vertex pass
             cudaMemsetAsync(classCounts, 0, 2 * kShadeClasses * 4, stream);
+            if (T) T->begin(stream);
             wfClassify<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(S, *cur, H, keys, classCounts);
             wfRegroup<kShadeClasses><<<smCount * 4, 256, 0, stream>>>(*cur, H, keys, classCounts, classCounts + kShadeClasses, QS, HS);
+            if (T) T->end(kKernelRegroup, stream);
+            if (T) T->begin(stream);
             wbShade<<<shadeBlocks, 128, 0, stream>>>(S, P, B, W, QS, HS, *nxt, ci);
+            if (T) T->end(kKernelShade, stream);
+            if (T) T->begin(stream);
             wbConnect<<<traceBlocks, 128, 0, stream>>>(S, B, W, ci);
-            wbVisibility<<<traceBlocks, 128, 0, stream>>>(S, W);
+            if (T) T->end(kKernelConnect, stream);
+            if (T) T->begin(stream);
+            wbVisibility<<<traceBlocks, 128, 0, stream>>>(S, W, P.traversalCounter);
             wbAccumulate<<<smCount * 4, 256, 0, stream>>>(W, QS);
+            if (T) T->end(kKernelShadow, stream);
             launches += 7;
             RayQueue* t = cur;
             cur = nxt;

@@ -1144,12 +1144,13 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
     YG_CUDA(ctx->dRayCount.ensure(counterBytes));
     YG_CUDA(cudaMemsetAsync(ctx->dRayCount.p, 0, counterBytes, ctx->stream));
     yg::KernelTimer timer{nullptr, nullptr, 0, 0};
-    const bool timeKernels = (p->flags & YG_FLAG_TIME_KERNELS) != 0 && !bdpt && !mega;
+    const bool timeKernels = (p->flags & YG_FLAG_TIME_KERNELS) != 0 && !mega;
     if (timeKernels)
     {
-        // events for every timed launch of the render: 4 kinds per bounce, per wave
+        // events for every timed launch of the render: 4 kinds per bounce, per wave (BDPT: 5
+        // kinds per bounce of waves sized by the BDPT arena, bounded here by 8192 launches)
         uint64_t waves = (npix * (uint64_t)p->spp_count + waveCap - 1) / waveCap;
-        size_t want = (size_t)std::min<uint64_t>(waves * p->max_depth * 4, 1u << 14);
+        size_t want = bdpt ? (size_t)1 << 13 : (size_t)std::min<uint64_t>(waves * p->max_depth * 4, 1u << 14);
         while (ctx->kernelKinds.size() < want)
         {
             cudaEvent_t a = nullptr, b = nullptr;
@@ -1206,7 +1207,7 @@ YG_API int yg_render(yg_context* ctx, const yg_render_params* p, yg_sample_recor
         if (bdpt)
             launches += yg::launchBdpt(S, L, ctx->dArena.p, ctx->dPerm.as<uint32_t>(), lightPaths, lightVerts,
                                        yg::mk3(ctx->worldCenter[0], ctx->worldCenter[1], ctx->worldCenter[2]),
-                                       ctx->worldRadiusSqr, ctx->smCount, ctx->stream);
+                                       ctx->worldRadiusSqr, ctx->smCount, ctx->stream, timeKernels ? &timer : nullptr);
         else if (mega) launches += yg::launchPathKernel(S, L, ctx->smCount, ctx->stream);
         else launches += yg::launchWavefront(S, L, ctx->dArena.p, waveCap, ctx->smCount, ctx->stream,
                                              timeKernels ? &timer : nullptr);
@@ -1278,9 +1279,16 @@ YG_API int yg_last_kernel_profile(yg_context* ctx, yg_kernel_profile* out)
         float t = 0;
         YG_CUDA(cudaEventElapsedTime(&t, ctx->kernelEvents[2 * k], ctx->kernelEvents[2 * k + 1]));
         uint8_t kind = ctx->kernelKinds[k];
+        if (kind == yg::kKernelConnect)
+        {
+            out->connect_ms += t;
+            out->connect_launches += 1;
+            continue;
+        }
         out->ms[kind] += t;
         out->launches[kind] += 1;
     }
+    out->connection_record_bytes = yg::bdptConnectionRecordBytes();
     unsigned long long c[1 + yg::kTraversalCounters] = {};
     if (ctx->dRayCount.p) YG_CUDA(cudaMemcpy(c, ctx->dRayCount.p, sizeof(c), cudaMemcpyDeviceToHost));
     out->closest_nodes = c[1];

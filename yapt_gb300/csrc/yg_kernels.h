@@ -43,7 +43,7 @@ int buildWideBvh(const WideBvhInput& in, WideBvhOutput& out, cudaStream_t stream
 int indexTrianglesByPrim(const float4* tris, uint32_t nTris, const uint32_t* primStart, uint32_t* out, cudaStream_t stream);
 
 // Kernel kinds of the timer (the C-ABI's YG_KERNEL_* values).
-constexpr uint8_t kKernelTrace = 0, kKernelRegroup = 1, kKernelShade = 2, kKernelShadow = 3;
+constexpr uint8_t kKernelTrace = 0, kKernelRegroup = 1, kKernelShade = 2, kKernelShadow = 3, kKernelConnect = 4;
 // Optional CUDA-event timing of launches by kind: events[2k], events[2k+1] bracket the k-th
 // timed launch, whose kind is kinds[k]. Timing stops when the events run out.
 struct KernelTimer
@@ -151,6 +151,13 @@ int gridBarrierCheck(GridBarrier* barrier, uint32_t* passes, uint32_t missing, u
 // permutation of the crop's pixel indices (camera groups take 64 consecutive entries).
 constexpr uint32_t kBdptMaxLightVertices = 16; // MAX_LIGHT_PATH_VERTICES_HARD_LIMIT
 size_t bdptArenaBytes(uint32_t frames, uint32_t lightPaths, uint32_t maxLightVerts, uint64_t cropPixels);
+// With a timer: wbTrace as trace, the class keys and regroup as regroup, wbShade as shade,
+// wbConnect as connect, wbVisibility and wbAccumulate as shadow. With P.traversalCounter, the
+// connection records are counted as shadow rays.
 int launchBdpt(const SceneView& S, const LaunchParams& P, void* arena, const uint32_t* perm, uint32_t lightPaths,
-               uint32_t maxLightVerts, float3 worldCenter, float worldRadiusSqr, int smCount, cudaStream_t stream);
+               uint32_t maxLightVerts, float3 worldCenter, float worldRadiusSqr, int smCount, cudaStream_t stream,
+               KernelTimer* timer = nullptr);
+// bytes one connection record moves in wbConnect: its (slot, light vertex) pair, the camera
+// vertex's surface, context and state, the prepared light vertex, and the record written
+uint32_t bdptConnectionRecordBytes();
 } // namespace yg

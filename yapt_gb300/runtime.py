@@ -180,7 +180,9 @@ class Context:
         kp = N.KernelProfile()
         N.check(self.lib.yg_last_kernel_profile(self.h, C.byref(kp)))
         out = {k: {"ms": kp.ms[i], "launches": kp.launches[i]} for i, k in enumerate(N.KERNEL_KINDS)}
-        for f in ("closest_rays", "closest_nodes", "closest_triangles", "shadow_rays", "shadow_nodes", "shadow_triangles"):
+        out["connect"] = {"ms": kp.connect_ms, "launches": kp.connect_launches}
+        for f in ("closest_rays", "closest_nodes", "closest_triangles", "shadow_rays", "shadow_nodes", "shadow_triangles",
+                  "connection_record_bytes"):
             out[f] = getattr(kp, f)
         return out
 
