@@ -12,6 +12,7 @@ relMSE against the FP64 oracle fixture (4096 spp, indices 0..4095,
 tests/golden/nee_random_shapes_crop128_fp64_4096spp.npz).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload nee|bdpt|serve|denoise] [--no-cpu] [--size S --spp P]
 
 --impl reference times the CPU restatement of the reference integrator (the
 oracle library alone, its own tables, all host threads) on a strided subsample of
@@ -47,11 +48,12 @@ SERVE_WORKLOAD = dict(workload="serve_poisson_8_box_variants_10k_to_2M_triangles
                       spp=[1, 4, 16, 64], integrators=["uni", "nee", "bdpt"], rates_per_s=[50, 100, 200, 400, 800],
                       loads=[0.5, 0.8, 1.0], requests=200, max_depth=8, light_vertices=8, lambda_nm=[380, 780], seed=0)
 SERVE_METRIC = "serve: Msamples/s at full load with p50/p99 latency (Poisson arrivals, mixed sizes/spp/integrators)"
-# --workload denoise: the learned denoiser. Training pairs are rendered by the tracer from seeded
-# box scenes (256x256, 4 spp + first-hit features -> a high-spp target), the U-Net is trained
-# on the GPU with Adam (lr 1e-3), and a held-out 1920x1080 box scene compares the wall time to
-# reach relMSE 1e-3: plain accumulation vs few-spp renders + the network, with a per-tile
-# fallback to plain accumulation where the two-half error estimate exceeds a threshold.
+# --workload denoise: the learned denoiser. Training pairs are rendered by the tracer from 48 seeded
+# box scenes (384x216, inputs at 2-32 spp with first-hit features -> 8192-spp targets), the U-Net
+# is trained on the GPU with Adam (lr 1e-3 decayed to 1e-5), and a held-out 1920x1080 box scene
+# compares the wall time to reach relMSE 1e-3: plain accumulation vs few-spp renders + the
+# network, with a per-tile fallback to plain accumulation where the two-half error estimate
+# exceeds a threshold; three more held-out scenes (960x544) report the network's relMSE.
 DENOISE_WORKLOAD = dict(workload="denoise_unet_box_scenes_1080p", train_scenes=48, train_width=384, train_height=216,
                         train_input_spp=[2, 4, 8, 16, 32], train_target_spp=8192, train_steps=12000, batch=8, crop=128, lr=1e-3,
                         lr_final=1e-5,
