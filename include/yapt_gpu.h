@@ -409,7 +409,8 @@ YG_API int yg_last_traversal_counts(yg_context* ctx, uint64_t* nodes_visited, ui
  * YG_FLAG_COUNT_TRAVERSAL the traversal work split between closest-hit and shadow rays.
  * A BDPT render times its camera-side kernels by the same kinds (trace: camera rays; regroup:
  * class keys and regroup; shade: camera vertices; shadow: visibility rays and accumulation)
- * plus its connection kernel, and counts its connection records. */
+ * plus its connection kernel, and counts its connection records. A render times at most 16,384
+ * launches (BDPT: 8,192); launches beyond that are not timed. */
 #define YG_KERNEL_TRACE 0   /* closest-hit traversal of the path queue */
 #define YG_KERNEL_REGROUP 1 /* shading-class keys and the regrouping scatter */
 #define YG_KERNEL_SHADE 2   /* surface interaction, BSDF sampling, light sampling */
