@@ -378,8 +378,8 @@ static __device__ __noinline__ bool traceInstanceClosest(const SceneView& S, flo
 // closest-hit rays (the rays in flight spread over the whole image), and handing a lane a new
 // ray as soon as it finished (a shared queue cursor) lost more than the idle lanes cost.
 // The group stack stays in local memory: its top entries live in L1 anyway, and staging them
-// in shared memory (YG_TRACE_SHARED_STACK, 8 KB per block) measured 3 % slower on the NEE
-// workload's traversal, the smaller L1 costing more node hits than the stack saves.
+// in shared memory (YG_TRACE_SHARED_STACK, 8 KB per block, plain loop only) measured 3 % slower
+// on the NEE workload's traversal, the smaller L1 costing more node hits than the stack saves.
 // With `stop`, a ray's traversal also ends as soon as stop(state) holds after a node.
 // YG_TRACE_REFILL (closest hit) and YG_SHADOW_REFILL (any hit) set K; 0 is the plain loop.
 #ifndef YG_TRACE_REFILL
