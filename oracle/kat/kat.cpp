@@ -1,0 +1,221 @@
+// TEST INFRASTRUCTURE ONLY: known-answer and consistency checks of the oracle's BSDF lobes
+// (the functions of oracle.cpp behind the plain orc_* interface of refcheck.h). Each check
+// prints one JSON object per line; tests/test_oracle_kat.py judges them.
+//
+//   kat fresnel           dielectric Fresnel at normal incidence against ((eta - 1)/(eta + 1))^2
+//   kat lobe <id> <eta> <ax> <ay> <cos wo> <samples> <seed>
+//       samples the lobe (sampleCondRefl, sampleDielRefl, sampleDiel, cosHemi; ids as in
+//       orc_sample_lobe) from the outgoing direction at the given cosine, histograms the
+//       directions over (cos theta, phi) cells of the sphere, and integrates the lobe's pdf
+//       (orc_pdf_lobe) over each cell; a sample returned as the zero vector (rejected below
+//       the horizon) falls in an extra cell whose expectation is the pdf's mass outside the
+//       lobe's domain.
+//       Prints counts against expectations as a chi-square statistic and the pdf's integral.
+//   kat albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed>
+//       the lobe's directional albedo by its own importance sampling and by quadrature
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../refcheck/refcheck.h"
+
+using namespace refcheck;
+
+namespace
+{
+struct Rng
+{
+    uint64_t s;
+    uint64_t next()
+    {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    float uni() { return (float)((next() >> 40) * (1.0 / 16777216.0)); }
+};
+
+int fresnel()
+{
+    const float etas[] = {1.1f, 1.33f, 1.5f, 1.8f, 2.4f, 1.0f / 1.5f, 1.0f / 1.33f};
+    for (float eta : etas)
+    {
+        const double want = std::pow((eta - 1.0) / (eta + 1.0), 2.0);
+        const double got = orc_fresnel_dd(eta, 1.0f);
+        std::printf("{\"check\": \"fresnel_normal\", \"eta\": %.6f, \"want\": %.9g, \"got\": %.9g}\n", eta, want, got);
+    }
+    return 0;
+}
+
+constexpr int kCosBins = 24, kPhiBins = 48, kSub = 16, kFine = 256;
+constexpr double kPi = 3.14159265358979323846;
+
+void dirOf(double c, double phi, float out[3])
+{
+    const double s = std::sqrt(std::fmax(0.0, 1.0 - c * c));
+    out[0] = (float)(s * std::cos(phi));
+    out[1] = (float)c;
+    out[2] = (float)(s * std::sin(phi));
+}
+
+int lobe(int id, float eta, float ax, float ay, float cosWo, long samples, uint64_t seed)
+{
+    float wo[3];
+    dirOf(cosWo, 0.3, wo);
+    const int aR = 1, aT = 1;
+    std::vector<double> count(kCosBins * kPhiBins + 1, 0.0), expect(kCosBins * kPhiBins + 1, 0.0);
+    Rng rng{seed};
+    for (long n = 0; n < samples; ++n)
+    {
+        float wi[3];
+        const float s0 = rng.uni(), s1 = rng.uni(), sc = rng.uni();
+        orc_sample_lobe(id, eta, ax, ay, wo, s0, s1, sc, aR, aT, wi);
+        if (wi[0] == 0.0f && wi[1] == 0.0f && wi[2] == 0.0f)
+        {
+            count[kCosBins * kPhiBins] += 1.0;
+            continue;
+        }
+        const double len = std::sqrt((double)wi[0] * wi[0] + (double)wi[1] * wi[1] + (double)wi[2] * wi[2]);
+        const double c = std::fmin(1.0, std::fmax(-1.0, wi[1] / len));
+        double phi = std::atan2((double)wi[2], (double)wi[0]);
+        if (phi < 0.0) phi += 2.0 * kPi;
+        const int ic = std::min(kCosBins - 1, (int)((c + 1.0) * 0.5 * kCosBins));
+        const int ip = std::min(kPhiBins - 1, (int)(phi / (2.0 * kPi) * kPhiBins));
+        count[ic * kPhiBins + ip] += 1.0;
+    }
+    // the pdf (per solid angle) integrated over each cell of the lobe's domain (the upper
+    // hemisphere for the reflection lobes 0, 1, 4, 5, the lower one for transmission 2, the
+    // sphere for the dielectric lobe 3, with the outgoing direction above): midpoint rule on
+    // kSub x kSub sub-cells, d(omega) = d(cos theta) d(phi). Outside its domain a lobe's pdf
+    // is not evaluated by the integrator, and samples there are rejected by the sampler.
+    const bool upper = id != 2, lower = id == 2 || id == 3;
+    double integral = 0.0;
+    const double dc = 2.0 / kCosBins, dp = 2.0 * kPi / kPhiBins;
+    // a cell that the edge of the pdf's support crosses (some sub-cells zero, some not) is
+    // integrated again on a kFine x kFine grid: the midpoint rule converges slowly there
+    auto cellMass = [&](int ic, int ip, int sub, bool& edge) {
+        double m = 0.0;
+        bool zero = false, nonzero = false;
+        for (int a = 0; a < sub; ++a)
+            for (int b = 0; b < sub; ++b)
+            {
+                const double c = -1.0 + (ic + (a + 0.5) / sub) * dc;
+                if ((c > 0.0 && !upper) || (c < 0.0 && !lower)) continue;
+                const double phi = (ip + (b + 0.5) / sub) * dp;
+                float wi[3];
+                dirOf(c, phi, wi);
+                const double p = orc_pdf_lobe(id, eta, ax, ay, wo, wi, aR, aT);
+                m += p;
+                (p > 0.0 ? nonzero : zero) = true;
+            }
+        edge = zero && nonzero;
+        return m * dc * dp / ((double)sub * sub);
+    };
+    for (int ic = 0; ic < kCosBins; ++ic)
+        for (int ip = 0; ip < kPhiBins; ++ip)
+        {
+            bool edge = false;
+            double m = cellMass(ic, ip, kSub, edge);
+            if (edge) m = cellMass(ic, ip, kFine, edge);
+            expect[ic * kPhiBins + ip] = m * samples;
+            integral += m;
+        }
+    // the rejected samples' cell, for the samplers that reject (0, 1, 3): the mass of the pdf
+    // outside its domain; the others must put all their mass inside (pdf_integral = 1, up to
+    // the quadrature's error, which would dominate an empty cell's expectation)
+    const bool rejects = id == 0 || id == 1 || id == 3;
+    expect[kCosBins * kPhiBins] = rejects ? std::fmax(0.0, 1.0 - integral) * samples : 0.0;
+    // chi-square over the cells expecting at least 5 samples; the rest are pooled into one
+    double chi2 = 0.0, poolE = 0.0, poolC = 0.0, worst = 0.0;
+    int dof = -1;
+    for (size_t k = 0; k < count.size(); ++k)
+    {
+        if (k == count.size() - 1 && !rejects) continue; // reported as "rejected" (must be 0)
+        if (expect[k] >= 5.0)
+        {
+            const double d = count[k] - expect[k];
+            chi2 += d * d / expect[k];
+            worst = std::fmax(worst, std::fabs(d) / std::sqrt(expect[k]));
+            ++dof;
+        }
+        else
+        {
+            poolE += expect[k];
+            poolC += count[k];
+        }
+    }
+    if (poolE >= 5.0)
+    {
+        const double d = poolC - poolE;
+        chi2 += d * d / poolE;
+        ++dof;
+    }
+    std::printf("{\"check\": \"lobe\", \"lobe\": %d, \"eta\": %.4f, \"ax\": %.4f, \"ay\": %.4f, \"cos_wo\": %.4f, "
+                "\"samples\": %ld, \"chi2\": %.4f, \"dof\": %d, \"worst_z\": %.3f, \"pdf_integral\": %.6f, "
+                "\"rejected\": %.0f, \"pooled_expect\": %.3f, \"pooled_count\": %.0f}\n",
+                id, eta, ax, ay, cosWo, samples, chi2, dof, worst, integral, count[kCosBins * kPhiBins], poolE, poolC);
+    return 0;
+}
+// Directional albedo of an evaluated lobe (orc_eval_lobe: 1 dielectric reflection, 2
+// transmission, 5 sheen) two ways: the estimator an integrator uses, the mean of
+// f(wo, wi) |cos wi| / pdf(wo, wi) over the lobe's own samples (a rejected sample counts 0),
+// and a quadrature of f |cos wi| over the sphere. Equal within the estimator's standard error
+// only if sampling, pdf and evaluation agree.
+int albedo(int id, float eta, float ax, float ay, float cosWo, long samples, uint64_t seed)
+{
+    float wo[3];
+    dirOf(cosWo, 0.3, wo);
+    Rng rng{seed};
+    double sum = 0.0, sum2 = 0.0;
+    for (long n = 0; n < samples; ++n)
+    {
+        float wi[3];
+        const float s0 = rng.uni(), s1 = rng.uni(), sc = rng.uni();
+        orc_sample_lobe(id, eta, ax, ay, wo, s0, s1, sc, 1, 1, wi);
+        double w = 0.0;
+        if (wi[0] != 0.0f || wi[1] != 0.0f || wi[2] != 0.0f)
+        {
+            const double pdf = orc_pdf_lobe(id, eta, ax, ay, wo, wi, 1, 1);
+            if (pdf > 0.0) w = orc_eval_lobe(id, eta, 0.0f, ax, ay, wo, wi) * std::fabs((double)wi[1]) / pdf;
+        }
+        sum += w;
+        sum2 += w * w;
+    }
+    const double mean = sum / samples, se = std::sqrt(std::fmax(0.0, sum2 / samples - mean * mean) / samples);
+    constexpr int nc = 1024, np = 1024;
+    double quad = 0.0;
+    for (int a = 0; a < nc; ++a)
+    {
+        const double c = -1.0 + (a + 0.5) * 2.0 / nc;
+        for (int b = 0; b < np; ++b)
+        {
+            float wi[3];
+            dirOf(c, (b + 0.5) * 2.0 * kPi / np, wi);
+            quad += orc_eval_lobe(id, eta, 0.0f, ax, ay, wo, wi) * std::fabs(c);
+        }
+    }
+    quad *= (2.0 / nc) * (2.0 * kPi / np);
+    std::printf("{\"check\": \"albedo\", \"lobe\": %d, \"eta\": %.4f, \"ax\": %.4f, \"ay\": %.4f, \"cos_wo\": %.4f, "
+                "\"samples\": %ld, \"estimate\": %.7f, \"stderr\": %.7f, \"quadrature\": %.7f}\n",
+                id, eta, ax, ay, cosWo, samples, mean, se, quad);
+    return 0;
+}
+} // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc >= 2 && std::strcmp(argv[1], "fresnel") == 0) return fresnel();
+    if (argc >= 9 && std::strcmp(argv[1], "lobe") == 0)
+        return lobe(std::atoi(argv[2]), (float)std::atof(argv[3]), (float)std::atof(argv[4]), (float)std::atof(argv[5]),
+                    (float)std::atof(argv[6]), std::atol(argv[7]), (uint64_t)std::strtoull(argv[8], nullptr, 10));
+    if (argc >= 9 && std::strcmp(argv[1], "albedo") == 0)
+        return albedo(std::atoi(argv[2]), (float)std::atof(argv[3]), (float)std::atof(argv[4]), (float)std::atof(argv[5]),
+                      (float)std::atof(argv[6]), std::atol(argv[7]), (uint64_t)std::strtoull(argv[8], nullptr, 10));
+    std::fprintf(stderr, "usage: kat fresnel | kat lobe|albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed>\n");
+    return 2;
+}
