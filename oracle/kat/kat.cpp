@@ -13,6 +13,7 @@
 //       Prints counts against expectations as a chi-square statistic and the pdf's integral.
 //   kat albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed>
 //       the lobe's directional albedo by its own importance sampling and by quadrature
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
