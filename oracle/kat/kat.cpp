@@ -13,6 +13,8 @@
 //       Prints counts against expectations as a chi-square statistic and the pdf's integral.
 //   kat albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed>
 //       the lobe's directional albedo by its own importance sampling and by quadrature
+//   kat reciprocity <id> <pairs> <seed>
+//       f(wo, wi) against f(wi, wo) for a reflection lobe
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -206,6 +208,30 @@ int albedo(int id, float eta, float ax, float ay, float cosWo, long samples, uin
                 id, eta, ax, ay, cosWo, samples, mean, se, quad);
     return 0;
 }
+// Helmholtz reciprocity of the reflection lobes with an evaluation (1 dielectric reflection,
+// 5 sheen): f(wo, wi) = f(wi, wo) for random direction pairs above the surface and random
+// roughness; prints the largest relative asymmetry.
+int reciprocity(int id, long pairs, uint64_t seed)
+{
+    Rng rng{seed};
+    double worst = 0.0;
+    long n = 0;
+    for (long k = 0; k < pairs; ++k)
+    {
+        float wo[3], wi[3];
+        dirOf(rng.uni(), 2.0 * kPi * rng.uni(), wo);
+        dirOf(rng.uni(), 2.0 * kPi * rng.uni(), wi);
+        const float ax = 0.05f + 0.9f * rng.uni(), ay = 0.05f + 0.9f * rng.uni(), eta = 1.1f + rng.uni();
+        const double a = orc_eval_lobe(id, eta, 0.0f, ax, ay, wo, wi), b = orc_eval_lobe(id, eta, 0.0f, ax, ay, wi, wo);
+        if (a > 1e-6 || b > 1e-6)
+        {
+            ++n;
+            worst = std::fmax(worst, std::fabs(a - b) / std::fmax(a, b));
+        }
+    }
+    std::printf("{\"check\": \"reciprocity\", \"lobe\": %d, \"pairs\": %ld, \"worst_rel\": %.4g}\n", id, n, worst);
+    return 0;
+}
 } // namespace
 
 int main(int argc, char** argv)
@@ -217,6 +243,9 @@ int main(int argc, char** argv)
     if (argc >= 9 && std::strcmp(argv[1], "albedo") == 0)
         return albedo(std::atoi(argv[2]), (float)std::atof(argv[3]), (float)std::atof(argv[4]), (float)std::atof(argv[5]),
                       (float)std::atof(argv[6]), std::atol(argv[7]), (uint64_t)std::strtoull(argv[8], nullptr, 10));
-    std::fprintf(stderr, "usage: kat fresnel | kat lobe|albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed>\n");
+    if (argc >= 5 && std::strcmp(argv[1], "reciprocity") == 0)
+        return reciprocity(std::atoi(argv[2]), std::atol(argv[3]), (uint64_t)std::strtoull(argv[4], nullptr, 10));
+    std::fprintf(stderr, "usage: kat fresnel | kat lobe|albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed> | "
+                         "kat reciprocity <id> <pairs> <seed>\n");
     return 2;
 }

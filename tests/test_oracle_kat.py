@@ -7,6 +7,7 @@ parity, the CUDA path) is checked against facts that need no reference output:
     histograms over the sphere against the pdf integrated per cell, plus the rejected mass);
   * the estimator f |cos| / pdf over a lobe's own samples converges to the lobe's directional
     albedo computed by quadrature;
+  * the dielectric-reflection and sheen lobes are reciprocal, f(wo, wi) = f(wi, wo);
   * white furnace (WHITE_FURNACE_TEST, raytraceCommon.hlsl:27-28): a convex white object under a
     constant environment looks like the environment, exactly for a Lambertian surface and
     within the multiple-scattering compensation's accuracy for a white rough conductor
@@ -89,6 +90,12 @@ ALBEDO = [
 def test_importance_sampled_albedo_matches_quadrature(kat, case):
     r = kat("albedo", *case, 200000, 11)[0]
     assert abs(r["estimate"] - r["quadrature"]) < 5.0 * r["stderr"] + 2e-4 * r["quadrature"], r
+
+
+@pytest.mark.parametrize("lobe", [1, 5])
+def test_reflection_lobes_are_reciprocal(kat, lobe):
+    r = kat("reciprocity", lobe, 20000, 5)[0]
+    assert r["pairs"] > 15000 and r["worst_rel"] < 1e-4, r
 
 
 def furnace_ratio(material, integrator, spp=32, size=24):
