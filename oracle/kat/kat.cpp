@@ -13,6 +13,8 @@
 //       Prints counts against expectations as a chi-square statistic and the pdf's integral.
 //   kat albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed>
 //       the lobe's directional albedo by its own importance sampling and by quadrature
+//   kat layered <preset> <cos wo> <samples> <seed> <data dir>
+//       the full layered BSDF's sampling against the mixture pdf of evaluateSurface
 //   kat reciprocity <id> <pairs> <seed>
 //       f(wo, wi) against f(wi, wo) for a reflection lobe
 #include <algorithm>
@@ -21,8 +23,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
+#include "../../yapt_gb300/csrc/yg_tables.h"
 #include "../refcheck/refcheck.h"
 
 using namespace refcheck;
@@ -232,6 +236,166 @@ int reciprocity(int id, long pairs, uint64_t seed)
     std::printf("{\"check\": \"reciprocity\", \"lobe\": %d, \"pairs\": %ld, \"worst_rel\": %.4g}\n", id, n, worst);
     return 0;
 }
+// The full layered BSDF as the integrators sample it (closestHit: a layer chosen with the
+// probabilities of calculateNormalizedMaterialLayerSamplingProbabilities, then that layer's
+// getSampleDirectionOSForLayer) against the mixture pdf evaluateSurface reports (the sum of the
+// layers' pdfs weighted by the same probabilities). Presets: 0 clear coat + sheen + 30 % metal
+// over a diffuse base; 1 rough glass (reflection and transmission); 2 rough plastic (specular
+// layer over a diffuse base); 3 anisotropic metal under a rough coat. Needs the LUTs
+// (multiple scattering, sheen) of the shared table generator.
+int setupTables(const char* dataDir)
+{
+    static yg::MsLuts L;
+    static std::vector<double> cie;
+    static std::vector<float> cie321(321 * 4), rgb;
+    static uint32_t point[256] = {};
+    std::string err;
+    yg::buildMsLuts(L);
+    if (!yg::loadCie(std::string(dataDir) + "/cie1931_2deg_d65_1nm.txt", cie, err))
+    {
+        std::fprintf(stderr, "%s\n", err.c_str());
+        return 2;
+    }
+    for (int i = 0; i < 321; ++i)
+        for (int k = 0; k < 4; ++k) cie321[4 * i + k] = (float)cie[4 * (i + 20) + k];
+    yg::buildRgbToSpd(cie, 380, 700, rgb);
+    Tables T;
+    const std::vector<float>* luts[9] = {&L.ss, &L.ssAvg, &L.ssms, &L.ssmsAvg, &L.transDenser, &L.transLighter,
+                                         &L.transAvgDenser, &L.transAvgLighter, &L.sheen};
+    for (int i = 0; i < 9; ++i) T.lut[i] = luts[i]->data();
+    T.cie321x4 = cie321.data();
+    T.rgb64 = rgb.data();
+    T.sobolPoint = point;
+    orc_setup(T);
+    return 0;
+}
+
+Surface preset(int which)
+{
+    Surface s;
+    std::memset(&s, 0, sizeof(s));
+    for (int k = 0; k < 4; ++k)
+    {
+        s.specular[k] = 0.9f - 0.1f * k;
+        s.albedo[k] = 0.6f + 0.05f * k;
+        s.sheenColor[k] = 0.7f;
+    }
+    for (float* n : {s.geoN, s.baseN, s.coatN}) n[0] = 0.0f, n[1] = 1.0f, n[2] = 0.0f;
+    s.tangent[0] = 1.0f;
+    s.ior = 1.5f;
+    s.cauchyA = 1.5f;
+    s.diffOcc = s.specOcc = 1.0f;
+    s.ccIOR = 1.5f;
+    switch (which)
+    {
+    case 0:
+        s.ccAmount = 0.5f, s.ccRough = 0.3f, s.sheenAmount = 0.4f, s.sheenRough = 0.5f, s.metalness = 0.3f;
+        s.roughness = 0.5f, s.specAmount = 1.0f;
+        break;
+    case 1: s.transparency = 1.0f, s.roughness = 0.4f, s.specAmount = 1.0f; break;
+    case 2: s.roughness = 0.45f, s.specAmount = 1.0f; break;
+    default: s.metalness = 1.0f, s.roughness = 0.5f, s.aniso = 0.6f, s.ccAmount = 0.6f, s.ccRough = 0.25f; break;
+    }
+    return s;
+}
+
+int layered(int which, float cosWo, long samples, uint64_t seed, const char* dataDir)
+{
+    if (int r = setupTables(dataDir)) return r;
+    const Surface S = preset(which);
+    float wo[3];
+    dirOf(cosWo, 0.3, wo);
+    const float cur = 1.0f, prev = 1.0f, hero = 550.0f;
+    const int front = 1;
+    float probs[6];
+    orc_layer_probs(S, cur, prev, wo, front, probs);
+    std::vector<double> count(kCosBins * kPhiBins + 1, 0.0), expect(kCosBins * kPhiBins + 1, 0.0);
+    Rng rng{seed};
+    long deltas = 0;
+    for (long n = 0; n < samples; ++n)
+    {
+        float u = rng.uni();
+        int layer = 0;
+        for (; layer < 5; ++layer)
+        {
+            if (u < probs[layer] && probs[layer] > 0.0f) break;
+            u -= probs[layer];
+        }
+        const float sel = rng.uni(), r0 = rng.uni(), r1 = rng.uni();
+        float wi[3];
+        int diffuse = 0, delta = 0;
+        orc_sample_layer(S, hero, cur, prev, wo, front, layer, sel, r0, r1, wi, &diffuse, &delta);
+        deltas += delta;
+        if (wi[0] == 0.0f && wi[1] == 0.0f && wi[2] == 0.0f)
+        {
+            count[kCosBins * kPhiBins] += 1.0;
+            continue;
+        }
+        const double len = std::sqrt((double)wi[0] * wi[0] + (double)wi[1] * wi[1] + (double)wi[2] * wi[2]);
+        const double c = std::fmin(1.0, std::fmax(-1.0, wi[1] / len));
+        double phi = std::atan2((double)wi[2], (double)wi[0]);
+        if (phi < 0.0) phi += 2.0 * kPi;
+        const int ic = std::min(kCosBins - 1, (int)((c + 1.0) * 0.5 * kCosBins));
+        const int ip = std::min(kPhiBins - 1, (int)(phi / (2.0 * kPi) * kPhiBins));
+        count[ic * kPhiBins + ip] += 1.0;
+    }
+    const double dc = 2.0 / kCosBins, dp = 2.0 * kPi / kPhiBins;
+    auto cellMass = [&](int ic, int ip, int sub, bool& edge) {
+        double m = 0.0;
+        bool zero = false, nonzero = false;
+        for (int a = 0; a < sub; ++a)
+            for (int b = 0; b < sub; ++b)
+            {
+                float wi[3];
+                dirOf(-1.0 + (ic + (a + 0.5) / sub) * dc, (ip + (b + 0.5) / sub) * dp, wi);
+                const double p = orc_eval_surface(S, hero, cur, prev, wo, front, wi, 2u /* pdf only */).pdf;
+                m += p;
+                (p > 0.0 ? nonzero : zero) = true;
+            }
+        edge = zero && nonzero;
+        return m * dc * dp / ((double)sub * sub);
+    };
+    double integral = 0.0;
+    for (int ic = 0; ic < kCosBins; ++ic)
+        for (int ip = 0; ip < kPhiBins; ++ip)
+        {
+            bool edge = false;
+            double m = cellMass(ic, ip, kSub, edge);
+            if (edge) m = cellMass(ic, ip, kFine, edge);
+            expect[ic * kPhiBins + ip] = m * samples;
+            integral += m;
+        }
+    expect[kCosBins * kPhiBins] = std::fmax(0.0, 1.0 - integral) * samples;
+    double chi2 = 0.0, poolE = 0.0, poolC = 0.0, worst = 0.0;
+    int dof = -1;
+    for (size_t k = 0; k < count.size(); ++k)
+    {
+        if (expect[k] >= 5.0)
+        {
+            const double d = count[k] - expect[k];
+            chi2 += d * d / expect[k];
+            worst = std::fmax(worst, std::fabs(d) / std::sqrt(expect[k]));
+            ++dof;
+        }
+        else
+        {
+            poolE += expect[k];
+            poolC += count[k];
+        }
+    }
+    if (poolE >= 5.0)
+    {
+        const double d = poolC - poolE;
+        chi2 += d * d / poolE;
+        ++dof;
+    }
+    std::printf("{\"check\": \"layered\", \"preset\": %d, \"cos_wo\": %.4f, \"samples\": %ld, \"chi2\": %.4f, "
+                "\"dof\": %d, \"worst_z\": %.3f, \"pdf_integral\": %.6f, \"rejected\": %.0f, \"deltas\": %ld, "
+                "\"probs\": [%.4f, %.4f, %.4f, %.4f, %.4f, %.4f]}\n",
+                which, cosWo, samples, chi2, dof, worst, integral, count[kCosBins * kPhiBins], deltas, probs[0], probs[1],
+                probs[2], probs[3], probs[4], probs[5]);
+    return 0;
+}
 } // namespace
 
 int main(int argc, char** argv)
@@ -243,6 +407,9 @@ int main(int argc, char** argv)
     if (argc >= 9 && std::strcmp(argv[1], "albedo") == 0)
         return albedo(std::atoi(argv[2]), (float)std::atof(argv[3]), (float)std::atof(argv[4]), (float)std::atof(argv[5]),
                       (float)std::atof(argv[6]), std::atol(argv[7]), (uint64_t)std::strtoull(argv[8], nullptr, 10));
+    if (argc >= 7 && std::strcmp(argv[1], "layered") == 0)
+        return layered(std::atoi(argv[2]), (float)std::atof(argv[3]), std::atol(argv[4]),
+                       (uint64_t)std::strtoull(argv[5], nullptr, 10), argv[6]);
     if (argc >= 5 && std::strcmp(argv[1], "reciprocity") == 0)
         return reciprocity(std::atoi(argv[2]), std::atol(argv[3]), (uint64_t)std::strtoull(argv[4], nullptr, 10));
     std::fprintf(stderr, "usage: kat fresnel | kat lobe|albedo <id> <eta> <ax> <ay> <cos wo> <samples> <seed> | "

@@ -7,6 +7,9 @@ parity, the CUDA path) is checked against facts that need no reference output:
     histograms over the sphere against the pdf integrated per cell, plus the rejected mass);
   * the estimator f |cos| / pdf over a lobe's own samples converges to the lobe's directional
     albedo computed by quadrature;
+  * the full layered BSDF, sampled as the integrators sample it (a layer chosen by its
+    probability, then that layer's sampler), draws directions with the mixture pdf that
+    evaluateSurface reports;
   * the dielectric-reflection and sheen lobes are reciprocal, f(wo, wi) = f(wi, wo);
   * white furnace (WHITE_FURNACE_TEST, raytraceCommon.hlsl:27-28): a convex white object under a
     constant environment looks like the environment, exactly for a Lambertian surface and
@@ -90,6 +93,18 @@ ALBEDO = [
 def test_importance_sampled_albedo_matches_quadrature(kat, case):
     r = kat("albedo", *case, 200000, 11)[0]
     assert abs(r["estimate"] - r["quadrature"]) < 5.0 * r["stderr"] + 2e-4 * r["quadrature"], r
+
+
+# presets of oracle/kat/kat.cpp: 0 clear coat + sheen + 30 % metal over diffuse, 1 rough glass,
+# 2 rough plastic, 3 anisotropic metal under a rough coat
+@pytest.mark.parametrize("preset", [0, 1, 2, 3])
+@pytest.mark.parametrize("cos_wo", [0.7, 0.3])
+def test_layered_bsdf_sampling_matches_its_mixture_pdf(kat, preset, cos_wo):
+    chi2 = pytest.importorskip("scipy.stats").chi2
+    r = kat("layered", preset, cos_wo, 200000, 3, os.path.join(ROOT, "yapt_gb300", "data"))[0]
+    p = float(chi2.sf(r["chi2"], r["dof"]))
+    assert p > 1e-4 and r["deltas"] == 0, r
+    assert r["pdf_integral"] <= 1.0 + 2e-3, r
 
 
 @pytest.mark.parametrize("lobe", [1, 5])
