@@ -70,3 +70,17 @@ def test_ctypes_structs_match_the_header():
             if table[(cname, field)] != off:
                 mismatches.append("%s.%s: offset C %d, ctypes %d" % (cname, field, table[(cname, field)], off))
     assert not mismatches, mismatches
+
+
+def test_header_compiles_cleanly_as_c_and_cpp():
+    """A host in either language includes the header with every warning on and nothing else."""
+    with tempfile.TemporaryDirectory() as tmp:
+        for lang, compiler, std in (("c", "gcc", "-std=c11"), ("cpp", "g++", "-std=c++17")):
+            cc = shutil.which(compiler)
+            if cc is None:
+                pytest.skip("no %s compiler" % compiler)
+            src = os.path.join(tmp, "inc." + lang)
+            with open(src, "w") as f:
+                f.write('#include "yapt_gpu.h"\nint main(void) { return yg_version() > 0 ? 0 : 1; }\n')
+            subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+                            "-c", src, "-o", os.path.join(tmp, "inc_" + lang + ".o")], check=True)
