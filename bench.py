@@ -193,6 +193,16 @@ def allsum(world, v):
     return float(t.item())
 
 
+E2E_MAX_STEPS = 3  # end-to-end steps after the timed ones (at most)
+
+
+def rank_sample_base(rank, spp, warmup, steps):
+    """First sample index of a rank's block: every render a rank makes (warm-up, timed and
+    end-to-end steps) takes its own spp indices from the block, so the ranks' samples are
+    disjoint and together form one image of (ranks x steps x spp) samples."""
+    return rank * spp * (warmup + steps + E2E_MAX_STEPS)
+
+
 def cpu_model():
     """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU baseline's record."""
     try:
@@ -368,7 +378,7 @@ def run_ours(args, world, rank, local):
     W, H, spp = WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["spp"]
     ctx.film_clear(W, H)
     # each rank renders its own block of sample indices of the same image (weak scaling)
-    base = rank * spp * (args.warmup + args.steps)
+    base = rank_sample_base(rank, spp, args.warmup, args.steps)
 
     def params(step, flags=0):
         return ctx.params(WORKLOAD["integrator"], W, H, spp_start=base + step * spp, spp=spp,
@@ -416,7 +426,7 @@ def run_ours(args, world, rank, local):
     xyz = np.zeros((H, W, 3), np.float32)
     barrier(world)
     t1 = time.time()
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, min(args.steps, E2E_MAX_STEPS))
     for s in range(e2e_steps):
         p = params(args.warmup + args.steps + s)
         ctx.render(p)
